@@ -1,0 +1,367 @@
+"""GB300-native falling-sand world tick.
+
+Python host mirror of the reference engine's world-update interface, over the C ABI
+of libfse.so (include/fse.h): ``World.tick()`` is ``world::tick()``
+(source/engine/world.cpp:1036), ``World.tickCells()`` is ``world::tickCells()``
+(world.cpp:2030), ``getTile``/``setTile`` follow world.cpp:999-1008, and the material
+functions follow InitMaterials/RegisterMaterial/PushMaterials
+(source/engine/game_datastruct.cpp:117-300). All compute runs in the CUDA library;
+there is no CPU fallback: without the library or a GPU the calls raise.
+"""
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi
+from ._abi import BODY_DTYPE, PARTICLE_DTYPE, FseConfig, FseError, check, ptr
+
+__all__ = [
+    "World", "Batch", "Server", "MaterialInstance", "FseError", "PARTICLE_DTYPE", "BODY_DTYPE",
+    "InitMaterials", "RegisterMaterial", "PushMaterials", "load_lua_materials", "material_find",
+    "material_count", "material_get", "set_reaction", "set_interaction", "lib",
+    "AIR", "SOLID", "SAND", "SOUP", "GAS", "PASSABLE", "OBJECT", "GEN_EMPTY", "GEN_MIX", "GEN_ZIPF8",
+    "FLUID_ONE",
+]
+
+AIR, SOLID, SAND, SOUP, GAS, PASSABLE, OBJECT = 0, 1, 2, 3, 4, 5, 5
+GEN_EMPTY, GEN_MIX, GEN_ZIPF8 = 0, 1, 2
+FLUID_ONE = 65536
+INTERACT_TRANSFORM_MATERIAL, INTERACT_SPAWN_MATERIAL = 1, 2
+REACT_TEMPERATURE_BELOW, REACT_TEMPERATURE_ABOVE = 4, 5
+
+
+def lib():
+    return _abi.load()
+
+
+@dataclass
+class MaterialInstance:
+    """One cell (MaterialInstance, source/engine/game_datastruct.hpp:207-225) in the
+    SoA layout: scalar = fluid amount (Q16.16) for SOUP materials, temperature otherwise;
+    flags bit 7 = moved, bits 0-5 = settle count."""
+
+    id: int
+    colour: int = 0
+    scalar: int = 0
+    flags: int = 0
+
+
+# ------------------------------------------------------------------ materials
+def InitMaterials():
+    check(lib().fse_materials_begin(), "materials_begin")
+
+
+def RegisterMaterial(s_id, name, index_name, physicsType, slipperyness, alpha, density, iterations, emit=0,
+                     emitColor=0, color=0xFFFFFFFF):
+    out = C.c_int(-1)
+    check(lib().fse_material_register(s_id, name.encode(), index_name.encode(), physicsType, slipperyness, alpha,
+                                      float(density), iterations, emit, emitColor & 0xFFFFFFFF,
+                                      color & 0xFFFFFFFF, C.byref(out)), "RegisterMaterial")
+    return out.value
+
+
+def PushMaterials():
+    check(lib().fse_materials_push(), "PushMaterials")
+
+
+def load_lua_materials(script):
+    n = C.c_int(0)
+    check(lib().fse_materials_load_lua(script.encode(), C.byref(n)), "materials_load_lua")
+    return n.value
+
+
+def material_find(index_name):
+    return lib().fse_material_find(index_name.encode())
+
+
+def material_count():
+    return lib().fse_material_count()
+
+
+def material_get(mid):
+    out = np.zeros(16, np.int32)
+    check(lib().fse_material_get(mid, ptr(out)), "material_get")
+    return out
+
+
+def set_reaction(mat, kind, temperature, result):
+    check(lib().fse_material_set_reaction(mat, kind, temperature, result), "set_reaction")
+
+
+def set_interaction(mat, other, kind, data1, data2, ofs_x, ofs_y):
+    check(lib().fse_material_set_interaction(mat, other, kind, data1, data2, ofs_x, ofs_y), "set_interaction")
+
+
+def _config(chunk_size=128, cell_iter=3, seed=0, particle_capacity=0, spawn_capacity=0, stream=None):
+    return FseConfig(chunk_size, cell_iter, seed & 0xFFFFFFFF, particle_capacity, spawn_capacity,
+                     C.c_void_p(stream) if stream else None)
+
+
+# ---------------------------------------------------------------------- world
+class World:
+    """One device-resident world (world::init grids, world.cpp:43-145)."""
+
+    PLANES = (("id", np.uint16), ("colour", np.uint32), ("scalar", np.int32), ("flags", np.uint8),
+              ("diff", np.int32))
+
+    def __init__(self, width, height, chunk_size=128, cell_iter=3, seed=0, particle_capacity=0, spawn_capacity=0,
+                 stream=None, _handle=None):
+        self.lib = lib()
+        self.width, self.height = int(width), int(height)
+        self._owned = _handle is None
+        if _handle is None:
+            h = C.c_void_p()
+            cfg = _config(chunk_size, cell_iter, seed, particle_capacity, spawn_capacity, stream)
+            check(self.lib.fse_world_create(self.width, self.height, C.byref(cfg), C.byref(h)), "world_create")
+            self.h = h
+        else:
+            self.h = C.c_void_p(_handle)
+
+    def close(self):
+        if getattr(self, "h", None) and self._owned:
+            self.lib.fse_world_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- state
+    def info(self):
+        out = np.zeros(8, np.int32)
+        check(self.lib.fse_world_info(self.h, ptr(out)), "world_info")
+        return dict(zip(("w", "h", "chunk", "cell_iter", "seed", "tick", "particles", "err"), out.tolist()))
+
+    @property
+    def tick_count(self):
+        return self.info()["tick"]
+
+    @tick_count.setter
+    def tick_count(self, t):
+        check(self.lib.fse_world_set_tick(self.h, int(t) & 0xFFFFFFFF), "set_tick")
+
+    def upload(self, planes):
+        n = self.width * self.height
+        arrs = []
+        for k, dt in self.PLANES:
+            a = planes.get(k)
+            arrs.append(None if a is None else np.ascontiguousarray(a, dt).reshape(n))
+        check(self.lib.fse_world_upload(self.h, *[ptr(a) if a is not None else None for a in arrs]), "upload")
+
+    def state(self):
+        n = self.width * self.height
+        out = {k: np.empty(n, dt) for k, dt in self.PLANES}
+        check(self.lib.fse_world_download(self.h, *[ptr(out[k]) for k, _ in self.PLANES]), "download")
+        return {k: v.reshape(self.height, self.width) for k, v in out.items()}
+
+    def generate(self, kind, seed):
+        check(self.lib.fse_world_generate(self.h, kind, seed & 0xFFFFFFFF), "generate")
+
+    def getTile(self, x, y):
+        i, c, s, f = C.c_uint16(), C.c_uint32(), C.c_int32(), C.c_uint8()
+        check(self.lib.fse_world_get_tile(self.h, x, y, C.byref(i), C.byref(c), C.byref(s), C.byref(f)), "getTile")
+        return MaterialInstance(i.value, c.value, s.value, f.value)
+
+    def setTile(self, x, y, tile):
+        check(self.lib.fse_world_set_tile(self.h, x, y, tile.id, tile.colour & 0xFFFFFFFF, tile.scalar,
+                                          tile.flags & 0xFF), "setTile")
+
+    # -- the hot path
+    def tick(self, n=1):
+        """world::tick(), n times."""
+        check(self.lib.fse_world_tick(self.h, n), "tick")
+
+    def tickCells(self):
+        """world::tickCells()."""
+        check(self.lib.fse_particles_tick(self.h), "tickCells")
+
+    def step(self, n=1, graph=False):
+        """n x (world::tick(); world::tickCells()), optionally replayed from a CUDA graph."""
+        fn = self.lib.fse_world_step_graph if graph else self.lib.fse_world_step
+        check(fn(self.h, n), "step")
+
+    def sync(self):
+        check(self.lib.fse_world_sync(self.h), "sync")
+
+    def set_stream(self, stream_ptr):
+        check(self.lib.fse_world_set_stream(self.h, C.c_void_p(stream_ptr) if stream_ptr else None), "set_stream")
+
+    @property
+    def stream(self):
+        return self.lib.fse_world_stream(self.h)
+
+    # -- particles
+    def addCell(self, parts):
+        """world::addCell for an array of PARTICLE_DTYPE records (world.cpp:2292)."""
+        parts = np.ascontiguousarray(parts, PARTICLE_DTYPE)
+        check(self.lib.fse_particles_add(self.h, ptr(parts), len(parts)), "addCell")
+
+    add_particles = addCell
+
+    def particle_count(self):
+        n = C.c_int(0)
+        check(self.lib.fse_particles_count(self.h, C.byref(n)), "particles_count")
+        return n.value
+
+    def particles(self):
+        n = self.particle_count()
+        out = np.zeros(n, PARTICLE_DTYPE)
+        got = C.c_int(0)
+        check(self.lib.fse_particles_read(self.h, ptr(out), n, C.byref(got)), "particles_read")
+        return out[: min(n, got.value)]
+
+    # -- objects
+    def object_stamp(self, bodies):
+        check(self.lib.fse_object_stamp(self.h, ptr(bodies), len(bodies)), "object_stamp")
+
+    def object_readback(self, bodies):
+        rem = C.c_int64(0)
+        check(self.lib.fse_object_readback(self.h, ptr(bodies), len(bodies), C.byref(rem)), "object_readback")
+        return rem.value
+
+    def object_mask(self, out=None):
+        n = self.width * self.height
+        if out is None:
+            out = np.zeros((n + 7) // 8, np.uint8)
+        check(self.lib.fse_object_mask_export(self.h, ptr(out)), "object_mask")
+        return out
+
+    def object_list(self, cap=None):
+        cap = cap if cap is not None else self.width * self.height
+        out = np.zeros(max(cap, 1), np.uint32)
+        n = C.c_int64(0)
+        check(self.lib.fse_object_list_export(self.h, ptr(out), cap, C.byref(n)), "object_list")
+        return out[: min(cap, n.value)], n.value
+
+    # -- ledger
+    def ledger(self):
+        m = material_count()
+        out = np.zeros(6 * m, np.int64)
+        check(self.lib.fse_world_ledger(self.h, ptr(out)), "ledger")
+        return out.reshape(6, m)
+
+    def reset_ledger(self):
+        check(self.lib.fse_world_ledger_reset(self.h), "ledger_reset")
+
+    def census(self):
+        m = material_count()
+        out = np.zeros(4 * m, np.int64)
+        check(self.lib.fse_world_census(self.h, ptr(out)), "census")
+        return out.reshape(4, m)
+
+
+class Batch:
+    """Many worlds ticked by one launch per colour pass (configs with uneven sizes)."""
+
+    def __init__(self, worlds):
+        self.lib = lib()
+        self.worlds = list(worlds)
+        arr = (C.c_void_p * len(self.worlds))(*[w.h.value for w in self.worlds])
+        h = C.c_void_p()
+        check(self.lib.fse_batch_create(arr, len(self.worlds), C.byref(h)), "batch_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fse_batch_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, n=1, graph_ticks=0):
+        if graph_ticks:
+            check(self.lib.fse_batch_step_graph(self.h, n, graph_ticks), "batch_step_graph")
+        else:
+            check(self.lib.fse_batch_step(self.h, n), "batch_step")
+
+    def autotune(self):
+        out = np.zeros(4, np.int32)
+        check(self.lib.fse_batch_autotune(self.h, ptr(out)), "batch_autotune")
+        return {"threads": int(out[0]), "ctas_per_sm": int(out[1]), "us": int(out[2]), "index": int(out[3])}
+
+    def set_launch(self, threads, ctas_per_sm):
+        check(self.lib.fse_batch_set_launch(self.h, threads, ctas_per_sm), "batch_set_launch")
+
+    def sync(self):
+        check(self.lib.fse_batch_sync(self.h), "batch_sync")
+
+
+class Server:
+    """Device-resident worlds served by continuous batching under an HBM budget."""
+
+    def __init__(self, hbm_budget_bytes, max_active):
+        self.lib = lib()
+        h = C.c_void_p()
+        check(self.lib.fse_server_create(int(hbm_budget_bytes), int(max_active), C.byref(h)), "server_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fse_server_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_world(self, width, height, gen_kind=GEN_MIX, gen_seed=1234, **cfg):
+        slot = C.c_int(-1)
+        c = _config(**cfg)
+        st = self.lib.fse_server_add_world(self.h, width, height, C.byref(c), gen_kind, gen_seed & 0xFFFFFFFF,
+                                           C.byref(slot))
+        check(st, "server_add_world")
+        return slot.value
+
+    def try_add_world(self, width, height, gen_kind=GEN_MIX, gen_seed=1234, **cfg):
+        try:
+            return self.add_world(width, height, gen_kind, gen_seed, **cfg)
+        except FseError as e:
+            if e.status == -3:
+                return None
+            raise
+
+    def remove_world(self, slot):
+        check(self.lib.fse_server_remove_world(self.h, slot), "server_remove_world")
+
+    def world(self, slot):
+        p = self.lib.fse_server_world(self.h, slot)
+        return World(0, 0, _handle=p) if p else None
+
+    def bytes_in_use(self):
+        return self.lib.fse_server_bytes_in_use(self.h)
+
+    def now_us(self):
+        return self.lib.fse_server_now_us(self.h)
+
+    def submit(self, slot, n_ticks, arrival_us=None):
+        rid = C.c_int64(-1)
+        t = self.now_us() if arrival_us is None else arrival_us
+        check(self.lib.fse_server_submit(self.h, slot, n_ticks, float(t), C.byref(rid)), "server_submit")
+        return rid.value
+
+    def step(self):
+        act = C.c_int(0)
+        check(self.lib.fse_server_step(self.h, C.byref(act)), "server_step")
+        return act.value
+
+    def poll(self, cap=4096):
+        ids = np.zeros(cap, np.int64)
+        done = np.zeros(cap, np.float64)
+        n = C.c_int(0)
+        check(self.lib.fse_server_poll(self.h, 0.0, ptr(ids), ptr(done), cap, C.byref(n)), "server_poll")
+        return ids[: n.value], done[: n.value]

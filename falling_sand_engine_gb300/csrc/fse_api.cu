@@ -1,0 +1,1088 @@
+// fse_api.cu -- C ABI: material table, world lifecycle, the world::tick() /
+// world::tickCells() launch sequences, CUDA-graph replay, particles, ledger.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <array>
+#include <cstddef>
+#include <cctype>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "fse_host.cuh"
+
+using namespace fse;
+
+// ================================================================ materials
+namespace {
+
+struct HostMat {
+    std::string name, index_name;
+    int type;
+    float density;
+    int iterations, slip, alpha;
+    uint32_t colour;
+    int emit;
+    uint32_t emit_colour;
+    uint32_t f_base;
+    int f_shift, f_lo, f_mod;
+    int32_t f_scalar;
+    int n_react;
+    int react[4][3];
+    int interact;
+};
+
+std::mutex g_mu;
+std::vector<HostMat> g_mats;
+std::vector<std::array<int, 7>> g_inter;
+bool g_dirty = true;
+MatTable g_host_mt;
+
+int max_stability(int slip) {
+    // world.cpp:1623 `int maxStability = 8 / sqrt(slipperyness) + 1;`
+    if (slip <= 0) return 255;
+    int v = (int)(8.0 / sqrt((double)slip) + 1.0);
+    return v > 255 ? 255 : v;
+}
+
+int add_mat(const char *name, const char *index_name, int type, int slip, int alpha, float density, int iterations,
+            int emit, uint32_t emit_colour, uint32_t colour) {
+    if ((int)g_mats.size() >= MAXMAT) return -1;
+    HostMat m{};
+    m.name = name ? name : "";
+    m.index_name = index_name ? index_name : "";
+    m.type = type;
+    m.density = density;
+    m.iterations = iterations;
+    m.slip = slip;
+    m.alpha = alpha;
+    m.colour = colour;
+    m.emit = emit;
+    m.emit_colour = emit_colour;
+    m.f_base = colour;
+    m.f_scalar = (type == T_SOUP) ? Q_DEFAULT : 0;
+    g_mats.push_back(m);
+    g_dirty = true;
+    return (int)g_mats.size() - 1;
+}
+
+int find_mat(const char *index_name) {
+    for (size_t i = 0; i < g_mats.size(); i++)
+        if (g_mats[i].index_name == index_name) return (int)i;
+    return -1;
+}
+
+void set_factory(int mid, uint32_t base, int shift, int lo, int mod, int32_t scalar) {
+    if (mid < 0) return;
+    HostMat &m = g_mats[mid];
+    m.f_base = base;
+    m.f_shift = shift;
+    m.f_lo = lo;
+    m.f_mod = mod;
+    m.f_scalar = scalar;
+    g_dirty = true;
+}
+
+int add_reaction(int mid, int kind, int temp, int res) {
+    if (mid < 0 || mid >= (int)g_mats.size() || res < 0 || res >= (int)g_mats.size()) return FSE_E_INVAL;
+    if (kind != REACT_BELOW && kind != REACT_ABOVE) return FSE_E_INVAL;
+    HostMat &m = g_mats[mid];
+    if (m.n_react >= 4) return FSE_E_INVAL;
+    m.react[m.n_react][0] = kind;
+    m.react[m.n_react][1] = temp;
+    m.react[m.n_react][2] = res;
+    m.n_react++;
+    g_dirty = true;
+    return FSE_OK;
+}
+
+// InitMaterials, source/engine/game_datastruct.cpp:69-111 and :117-280, without
+// the ten rand()-drawn Mat_i materials (never interactive, :196,206); texture
+// colours are replaced by constants (data/assets is absent from the reference).
+void builtin_materials() {
+    g_mats.clear();
+    g_inter.clear();
+    const uint32_t W = 0xffffffffu;
+    add_mat("_AIR", "GENERIC_AIR", T_AIR, 0, 255, 0, 0, 16, 0, W);
+    add_mat("_SOLID", "GENERIC_SOLID", T_SOLID, 0, 255, 1, 0, 0, 0, W);
+    add_mat("_SAND", "GENERIC_SAND", T_SAND, 20, 255, 10, 2, 0, 0, W);
+    add_mat("_LIQUID", "GENERIC_LIQUID", T_SOUP, 0, 255, 1.5f, 3, 0, 0, W);
+    add_mat("_GAS", "GENERIC_GAS", T_GAS, 0, 255, -1, 1, 0, 0, W);
+    add_mat("_PASSABLE", "GENERIC_PASSABLE", T_OBJECT, 0, 255, 0, 0, 0, 0, W);
+    add_mat("_OBJECT", "GENERIC_OBJECT", T_OBJECT, 0, 255, 1000.0f, 0, 0, 0, W);
+    add_mat("Stone", "STONE", T_SOLID, 0, 255, 1, 0, 0, 0, W);
+    add_mat("Grass", "GRASS", T_SAND, 20, 255, 12, 1, 0, 0, W);
+    add_mat("Dirt", "DIRT", T_SAND, 8, 255, 15, 1, 0, 0, W);
+    add_mat("Stone", "SMOOTH_STONE", T_SOLID, 0, 255, 1, 0, 0, 0, W);
+    add_mat("Cobblestone", "COBBLE_STONE", T_SOLID, 0, 255, 1, 0, 0, 0, W);
+    add_mat("Ground", "SMOOTH_DIRT", T_SOLID, 0, 255, 1, 0, 0, 0, W);
+    add_mat("Hard Ground", "COBBLE_DIRT", T_SOLID, 0, 255, 1, 0, 0, 0, W);
+    add_mat("Dirt", "SOFT_DIRT", T_SOLID, 0, 255, 15, 2, 0, 0, W);
+    add_mat("Water", "WATER", T_SOUP, 0, 0x80, 1.5f, 6, 40, 0x3000AFB5u, W);
+    add_mat("Lava", "LAVA", T_SOUP, 0, 0xC0, 2, 1, 40, 0xFFFF6900u, W);
+    add_mat("Cloud", "CLOUD", T_SOLID, 0, 127, 1, 0, 0, 0, W);
+    add_mat("Gold Ore", "GOLD_ORE", T_SAND, 20, 255, 20, 2, 8, 0x804000u, W);
+    add_mat("Molten Gold", "GOLD_MOLTEN", T_SOUP, 0, 255, 20, 2, 8, 0x6FFF9B40u, W);
+    add_mat("Solid Gold", "GOLD_SOLID", T_SOLID, 0, 255, 20, 2, 8, 0, W);
+    add_mat("Iron Ore", "IRON_ORE", T_SAND, 20, 255, 20, 2, 8, 0x7F442Fu, W);
+    add_mat("Obsidian", "OBSIDIAN", T_SOLID, 0, 255, 1, 0, 0, 0, W);
+    add_mat("Steam", "STEAM", T_GAS, 0, 255, -1, 1, 0, 0, W);
+    add_mat("Soft Dirt Sand", "SOFT_DIRT_SAND", T_SAND, 8, 255, 15, 2, 0, 0, W);
+    add_mat("Fire", "FIRE", T_OBJECT, 0, 255, 20, 1, 0, 0, W);
+    add_mat("Flat Cobblestone", "FLAT_COBBLE_STONE", T_SOLID, 0, 255, 1, 0, 0, 0, W);
+    add_mat("Flat Hard Ground", "FLAT_COBBLE_DIRT", T_SOLID, 0, 255, 1, 0, 0, 0, W);
+    add_mat("Test Sand", "TEST_SAND", T_SAND, 20, 255, 10, 2, 0, 0, W);
+    add_mat("Test Textured Sand", "TEST_TEXTURED_SAND", T_SAND, 20, 255, 10, 2, 0, 0, W);
+    add_mat("Test Liquid", "TEST_LIQUID", T_SOUP, 0, 255, 1.5f, 4, 0, 0, W);
+
+    // tile factories, game_datastruct.cpp:320-574
+    set_factory(find_mat("TEST_SAND"), (220u << 16) | 100u, 8, 155, 30, 0);
+    set_factory(find_mat("TEST_TEXTURED_SAND"), 0xDC9B64u, 0, 0, 0, 0);
+    set_factory(find_mat("TEST_LIQUID"), 0x0000FFu, 0, 0, 0, Q_DEFAULT);
+    set_factory(find_mat("STONE"), 0x808080u, 0, 0, 0, 0);
+    set_factory(find_mat("GRASS"), (40u << 16) | 20u, 8, 120, 20, 0);
+    set_factory(find_mat("DIRT"), (40u << 8) | 20u, 16, 60, 10, 0);
+    set_factory(find_mat("SMOOTH_STONE"), 0x9A9A9Au, 0, 0, 0, 0);
+    set_factory(find_mat("COBBLE_STONE"), 0x707070u, 0, 0, 0, 0);
+    set_factory(find_mat("SMOOTH_DIRT"), 0x6B4A2Fu, 0, 0, 0, 0);
+    set_factory(find_mat("COBBLE_DIRT"), 0x5A3D25u, 0, 0, 0, 0);
+    set_factory(find_mat("SOFT_DIRT"), 0x7A5533u, 0, 0, 0, 0);
+    set_factory(find_mat("WATER"), 0x00B69Fu, 0, 0, 0, Q_DEFAULT);
+    set_factory(find_mat("LAVA"), 0xFF7C00u, 0, 0, 0, Q_DEFAULT);
+    set_factory(find_mat("CLOUD"), 0xE6E6F0u, 0, 0, 0, 0);
+    set_factory(find_mat("GOLD_ORE"), 0xC8A032u, 0, 0, 0, 0);
+    set_factory(find_mat("GOLD_MOLTEN"), 0xFFB43Cu, 0, 0, 0, Q_DEFAULT);
+    set_factory(find_mat("GOLD_SOLID"), 0xE6C34Bu, 0, 0, 0, 0);
+    set_factory(find_mat("IRON_ORE"), 0x8C6E5Au, 0, 0, 0, 0);
+    set_factory(find_mat("OBSIDIAN"), 0x1E1428u, 0, 0, 0, 0);
+    set_factory(find_mat("STEAM"), 0x666666u, 0, 0, 0, 0);
+    set_factory(find_mat("FIRE"), (255u << 16) | 50u, 8, 100, 50, 0);
+    set_factory(find_mat("FLAT_COBBLE_STONE"), 0x787878u, 0, 0, 0, 0);
+    set_factory(find_mat("FLAT_COBBLE_DIRT"), 0x624530u, 0, 0, 0, 0);
+    set_factory(find_mat("GENERIC_AIR"), 0x000000u, 0, 0, 0, 0);
+    set_factory(find_mat("GENERIC_SOLID"), 0xff0000u, 0, 0, 0, 0);
+
+    // reactions, game_datastruct.cpp:246-260
+    add_reaction(find_mat("LAVA"), REACT_BELOW, 512, find_mat("OBSIDIAN"));
+    add_reaction(find_mat("WATER"), REACT_ABOVE, 128, find_mat("STEAM"));
+    add_reaction(find_mat("GOLD_ORE"), REACT_ABOVE, 512, find_mat("GOLD_MOLTEN"));
+    add_reaction(find_mat("GOLD_MOLTEN"), REACT_BELOW, 128, find_mat("GOLD_SOLID"));
+    g_dirty = true;
+}
+
+void build_table(MatTable &t) {
+    memset(&t, 0, sizeof(t));
+    t.n = (int)g_mats.size();
+    auto idx = [](const char *s, int def) {
+        int v = find_mat(s);
+        return v < 0 ? def : v;
+    };
+    t.id_air = idx("GENERIC_AIR", 0);
+    t.id_solid = idx("GENERIC_SOLID", 1);
+    t.id_fire = idx("FIRE", -1);
+    t.id_water = idx("WATER", -1);
+    t.id_lava = idx("LAVA", -1);
+    t.id_steam = idx("STEAM", -1);
+    t.id_obsidian = idx("OBSIDIAN", -1);
+    for (int i = 0; i < t.n; i++) {
+        const HostMat &m = g_mats[i];
+        int iters = std::min(std::max(m.iterations, 0), 255);
+        int slip = std::min(std::max(m.slip, 0), 255);
+        t.a[i] = (uint32_t)m.type | ((uint32_t)iters << 8) | ((uint32_t)slip << 16) |
+                 ((uint32_t)max_stability(m.slip) << 24);
+        t.density[i] = m.density;
+        t.f_base[i] = m.f_base;
+        t.f_pack[i] = (uint32_t)(m.f_shift & 0xFF) | ((uint32_t)(m.f_lo & 0xFFF) << 8) | ((uint32_t)(m.f_mod & 0xFFF) << 20);
+        t.f_scalar[i] = m.f_scalar;
+        t.n_react[i] = m.n_react;
+        for (int r = 0; r < m.n_react; r++)
+            for (int k = 0; k < 3; k++) t.react[i][r][k] = m.react[r][k];
+    }
+    t.n_inter = (int)g_inter.size();
+    for (size_t i = 0; i < g_inter.size(); i++)
+        for (int k = 0; k < 7; k++) t.inter[i][k] = g_inter[i][k];
+    t.has_inter = t.n_inter > 0 ? 1 : 0;
+}
+
+struct MatInit {
+    MatInit() { builtin_materials(); }
+} g_mat_init;
+
+}  // namespace
+
+namespace fse {
+MatTable *g_dev_mt = nullptr;
+
+int ensure_materials_pushed() {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_dirty && g_dev_mt) return FSE_OK;
+    build_table(g_host_mt);
+    if (!g_dev_mt) {
+        if (cudaMalloc(&g_dev_mt, sizeof(MatTable)) != cudaSuccess) {
+            g_dev_mt = nullptr;
+            return FSE_E_NOMEM;
+        }
+    } else {
+        // the table may be read by work in flight
+        cudaDeviceSynchronize();
+    }
+    if (cudaMemcpy(g_dev_mt, &g_host_mt, sizeof(MatTable), cudaMemcpyHostToDevice) != cudaSuccess) return FSE_E_CUDA;
+    g_dirty = false;
+    return FSE_OK;
+}
+const MatTable &host_table() {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (g_dirty) build_table(g_host_mt);
+    return g_host_mt;
+}
+
+int sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+int status_from_err(int err) {
+    if (err & ERR_BOUNDS) return FSE_E_BOUNDS;
+    if (err & ERR_TIMEOUT) return FSE_E_TIMEOUT;
+    if (err & (ERR_SPAWN_CAP | ERR_PART_CAP)) return FSE_E_CAPACITY;
+    return FSE_OK;
+}
+
+int tick_halo() {
+    const MatTable &t = host_table();
+    return t.has_inter ? 5 : 2;
+}
+
+int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], const int n_items[4], int max_iter, int C,
+                 int threads, int grid, bool particles, int move_blocks, int stage_blocks, cudaStream_t s) {
+    int halo = tick_halo();
+    for (int iter = 0; iter < max_iter; iter++)  // world.cpp:1050
+        for (int tk = 0; tk < 4; tk++) {         // world.cpp:1057-1060
+            cudaError_t e = launch_colour_pass(d_worlds, items[tk], n_items[tk], iter, tk, g_dev_mt, halo, C, threads,
+                                               grid, s);
+            if (e != cudaSuccess) return FSE_E_CUDA;
+        }
+    if (launch_spawn_append(d_worlds, n_worlds, stage_blocks, s) != cudaSuccess) return FSE_E_CUDA;
+    if (particles && launch_particle_tick(d_worlds, n_worlds, g_dev_mt, move_blocks, s) != cudaSuccess)
+        return FSE_E_CUDA;
+    return FSE_OK;
+}
+}  // namespace fse
+
+extern "C" {
+
+const char *fse_version(void) { return "fse-gb300 0.1 (sm_103a)"; }
+
+const char *fse_status_string(int s) {
+    switch (s) {
+        case FSE_OK: return "ok";
+        case FSE_E_INVAL: return "invalid argument";
+        case FSE_E_NOMEM: return "out of memory";
+        case FSE_E_BUDGET: return "HBM budget exceeded";
+        case FSE_E_CUDA: return "CUDA error";
+        case FSE_E_TIMEOUT: return "device wait timed out";
+        case FSE_E_CAPACITY: return "particle capacity exceeded";
+        case FSE_E_STATE: return "invalid state";
+        case FSE_E_BOUNDS: return "kernel bounds check fired";
+        default: return "unknown status";
+    }
+}
+
+int fse_materials_begin(void) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    builtin_materials();
+    return FSE_OK;
+}
+
+int fse_material_register(int s_id, const char *name, const char *index_name, int physics_type, int slipperyness,
+                          int alpha, float density, int iterations, int emit, uint32_t emit_colour, uint32_t colour,
+                          int *out_id) {
+    (void)s_id;
+    if (physics_type < 0 || physics_type > 5 || !index_name) return FSE_E_INVAL;
+    if (slipperyness < 0 || slipperyness > 255 || iterations < 0 || iterations > 255) return FSE_E_INVAL;
+    std::lock_guard<std::mutex> lk(g_mu);
+    int id = add_mat(name, index_name, physics_type, slipperyness, alpha, density, iterations, emit, emit_colour, colour);
+    if (id < 0) return FSE_E_INVAL;
+    if (out_id) *out_id = id;
+    return FSE_OK;
+}
+
+int fse_material_set_reaction(int mat, int kind, int temperature, int result_mat) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    return add_reaction(mat, kind, temperature, result_mat);
+}
+
+int fse_material_set_interaction(int mat, int other, int kind, int data1_mat, int data2_radius, int ofs_x, int ofs_y) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    int n = (int)g_mats.size();
+    if (mat < 0 || mat >= n || other < 0 || other >= n || data1_mat < 0 || data1_mat >= n) return FSE_E_INVAL;
+    if (kind != INTER_TRANSFORM && kind != INTER_SPAWN) return FSE_E_INVAL;
+    // the shared-memory halo covers offsets with |ofs| + radius <= 5
+    if (data2_radius < 0 || abs(ofs_x) + data2_radius > 5 || abs(ofs_y) + data2_radius > 5) return FSE_E_INVAL;
+    int cnt = 0;
+    for (auto &e : g_inter)
+        if (e[0] == mat && e[1] == other) cnt++;
+    if (cnt >= 4 || g_inter.size() >= 512) return FSE_E_INVAL;
+    g_inter.push_back({mat, other, kind, data1_mat, data2_radius, ofs_x, ofs_y});
+    g_mats[mat].interact = 1;
+    g_dirty = true;
+    return FSE_OK;
+}
+
+int fse_material_set_factory(int mat, uint32_t base, int shift, int lo, int mod, int32_t scalar) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (mat < 0 || mat >= (int)g_mats.size() || shift < 0 || shift > 24 || lo < 0 || lo > 4095 || mod < 0 || mod > 4095)
+        return FSE_E_INVAL;
+    set_factory(mat, base, shift, lo, mod, scalar);
+    return FSE_OK;
+}
+
+int fse_materials_push(void) { return ensure_materials_pushed(); }
+
+int fse_material_count(void) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    return (int)g_mats.size();
+}
+
+int fse_material_find(const char *index_name) {
+    if (!index_name) return -1;
+    std::lock_guard<std::mutex> lk(g_mu);
+    return find_mat(index_name);
+}
+
+int fse_material_get(int id, int32_t out[16]) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (id < 0 || id >= (int)g_mats.size() || !out) return FSE_E_INVAL;
+    const HostMat &m = g_mats[id];
+    int32_t dbits;
+    memcpy(&dbits, &m.density, 4);
+    out[0] = m.type;
+    out[1] = dbits;
+    out[2] = m.iterations;
+    out[3] = m.slip;
+    out[4] = m.slip <= 0 ? (1 << 20) : (int)(8.0 / sqrt((double)m.slip) + 1.0);
+    out[5] = m.alpha;
+    out[6] = (int32_t)m.colour;
+    out[7] = m.emit;
+    out[8] = (int32_t)m.emit_colour;
+    out[9] = (int32_t)m.f_base;
+    out[10] = m.f_shift;
+    out[11] = m.f_lo;
+    out[12] = m.f_mod;
+    out[13] = m.f_scalar;
+    out[14] = m.n_react;
+    out[15] = m.interact;
+    return FSE_OK;
+}
+
+// ---- Lua subset: materials_init(), materials_register(...), materials_push()
+// (the functions game_basic.cpp:79-81 exposes to data/scripts)
+namespace {
+struct LuaTok {
+    const char *p;
+    void ws() {
+        for (;;) {
+            while (*p && isspace((unsigned char)*p)) p++;
+            if (p[0] == '-' && p[1] == '-') {
+                if (p[2] == '[' && p[3] == '[') {
+                    const char *e = strstr(p + 4, "]]");
+                    p = e ? e + 2 : p + strlen(p);
+                } else {
+                    while (*p && *p != '\n') p++;
+                }
+                continue;
+            }
+            break;
+        }
+    }
+    bool str(std::string &out) {
+        ws();
+        if (*p != '"' && *p != '\'') return false;
+        char q = *p++;
+        out.clear();
+        while (*p && *p != q) {
+            if (*p == '\\' && p[1]) p++;
+            out.push_back(*p++);
+        }
+        if (*p != q) return false;
+        p++;
+        return true;
+    }
+    // number with optional unary minus and + - * / between terms
+    bool num(double &v) {
+        ws();
+        if (!term(v)) return false;
+        for (;;) {
+            ws();
+            char op = *p;
+            if (op != '+' && op != '-' && op != '*' && op != '/') return true;
+            p++;
+            double r;
+            if (!term(r)) return false;
+            if (op == '+') v += r;
+            else if (op == '-') v -= r;
+            else if (op == '*') v *= r;
+            else v /= r;
+        }
+    }
+    bool term(double &v) {
+        ws();
+        bool neg = false;
+        while (*p == '-') {
+            neg = !neg;
+            p++;
+            ws();
+        }
+        char *e = nullptr;
+        if (p[0] == '0' && (p[1] == 'x' || p[1] == 'X'))
+            v = (double)strtoull(p, &e, 16);
+        else
+            v = strtod(p, &e);
+        if (e == p) return false;
+        p = e;
+        if (neg) v = -v;
+        return true;
+    }
+    bool ch(char c) {
+        ws();
+        if (*p != c) return false;
+        p++;
+        return true;
+    }
+};
+}  // namespace
+
+int fse_materials_load_lua(const char *script, int *out_count) {
+    if (!script) return FSE_E_INVAL;
+    int count = 0;
+    const char *p = script;
+    for (;;) {
+        const char *reg = strstr(p, "materials_register");
+        const char *ini = strstr(p, "materials_init");
+        const char *next = reg;
+        if (!next || (ini && ini < next)) next = ini;
+        if (!next) break;
+        if (next == ini) {
+            fse_materials_begin();
+            p = ini + 14;
+            continue;
+        }
+        LuaTok t{reg + 18};
+        if (!t.ch('(')) return FSE_E_INVAL;
+        double sid, ptype, slip, alpha, dens, iters, emit, ecol, col;
+        std::string name, iname;
+        if (!t.num(sid) || !t.ch(',') || !t.str(name) || !t.ch(',') || !t.str(iname) || !t.ch(',') || !t.num(ptype) ||
+            !t.ch(',') || !t.num(slip) || !t.ch(',') || !t.num(alpha) || !t.ch(',') || !t.num(dens) || !t.ch(',') ||
+            !t.num(iters) || !t.ch(',') || !t.num(emit) || !t.ch(',') || !t.num(ecol) || !t.ch(',') || !t.num(col) ||
+            !t.ch(')'))
+            return FSE_E_INVAL;
+        int id;
+        int rc = fse_material_register((int)sid, name.c_str(), iname.c_str(), (int)ptype, (int)slip, (int)alpha,
+                                       (float)dens, (int)iters, (int)emit, (uint32_t)(uint64_t)ecol,
+                                       (uint32_t)(uint64_t)col, &id);
+        if (rc != FSE_OK) return rc;
+        count++;
+        p = t.p;
+    }
+    if (out_count) *out_count = count;
+    return FSE_OK;
+}
+
+}  // extern "C"
+
+// ================================================================== worlds
+static void free_world(fse_world *w) {
+    for (auto &g : w->graphs) cudaGraphExecDestroy(g.second);
+    w->graphs.clear();
+    WorldDev &h = w->h;
+    void *ptrs[] = {h.id, h.col, h.sc, h.fl, h.df, h.stage, h.cp_count, h.cp_base, h.p_state, h.p_lxly,
+                    h.req_list, h.req_list2, h.req_target, h.scan_tmp, h.ledger, w->ctr, w->d, w->claim,
+                    w->mask_bits, w->obj_list, w->obj_n};
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+    PartSoA *ps[2] = {&h.p, &h.q};
+    for (PartSoA *p : ps) {
+        void *a[] = {p->x, p->y, p->vx, p->vy, p->ax, p->ay, p->tx, p->ty, p->tf, p->life, p->fade, p->col, p->sc,
+                     p->id, p->fl, p->bits};
+        for (void *q : a)
+            if (q) cudaFree(q);
+    }
+    for (int k = 0; k < 4; k++)
+        if (w->items[k]) cudaFree(w->items[k]);
+    if (w->own_stream && w->stream) cudaStreamDestroy(w->stream);
+    delete w;
+}
+
+template <typename T>
+static bool dalloc(fse_world *w, T **p, size_t n) {
+    size_t b = n * sizeof(T);
+    if (b == 0) b = sizeof(T);
+    if (cudaMalloc((void **)p, b) != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return false;
+    }
+    w->bytes += b;
+    return true;
+}
+
+extern "C" {
+
+int fse_world_create(int width, int height, const fse_config *cfg, fse_world **out) {
+    if (!out || width <= 0 || height <= 0 || (long long)width * height > (1LL << 31) - 1) return FSE_E_INVAL;
+    fse_config c{};
+    if (cfg) c = *cfg;
+    if (c.chunk_size == 0) c.chunk_size = 128;
+    if (c.cell_iter == 0) c.cell_iter = 3;
+    if (c.chunk_size < 16 || c.chunk_size > 128 || c.cell_iter < 0 || c.cell_iter > 64) return FSE_E_INVAL;
+    long long ncell = (long long)width * height;
+    if (c.particle_capacity <= 0) c.particle_capacity = (int)std::max<long long>(65536, ncell / 4);
+    if (c.spawn_capacity <= 0) c.spawn_capacity = c.particle_capacity;
+    int rc = ensure_materials_pushed();
+    if (rc != FSE_OK) return rc;
+    particle_prepare();
+
+    fse_world *w = new fse_world();
+    memset(&w->h, 0, sizeof(w->h));
+    w->W = width;
+    w->H = height;
+    w->C = c.chunk_size;
+    w->cell_iter = c.cell_iter;
+    w->seed = c.seed;
+    w->part_cap = c.particle_capacity;
+    w->stage_cap = c.spawn_capacity;
+    w->threads = 1024;
+    w->grid = 0;
+    if (c.stream) {
+        w->stream = (cudaStream_t)c.stream;
+        w->own_stream = false;
+    } else {
+        if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete w;
+            return FSE_E_CUDA;
+        }
+        w->own_stream = true;
+    }
+    WorldDev &h = w->h;
+    h.W = width;
+    h.H = height;
+    h.C = c.chunk_size;
+    h.cell_iter = c.cell_iter;
+    h.seed = c.seed;
+    h.nCx = ceil_div(width, h.C);
+    h.nCy = ceil_div(height, h.C);
+    h.max_slots = ceil_div(h.nCx, 2) * ceil_div(h.nCy, 2);
+    h.stage_cap = c.spawn_capacity;
+    h.part_cap = c.particle_capacity;
+    size_t n = (size_t)ncell;
+    int ncp = h.cell_iter * 4 * h.max_slots + 1;
+    bool ok = dalloc(w, &h.id, n) && dalloc(w, &h.col, n) && dalloc(w, &h.sc, n) && dalloc(w, &h.fl, n) &&
+              dalloc(w, &h.df, n) && dalloc(w, &h.stage, (size_t)h.stage_cap) && dalloc(w, &h.cp_count, ncp) &&
+              dalloc(w, &h.cp_base, ncp) && dalloc(w, &w->ctr, 16) && dalloc(w, &h.ledger, LED_ROWS * MAXMAT) &&
+              dalloc(w, &h.p_state, (size_t)h.part_cap) && dalloc(w, &h.p_lxly, (size_t)h.part_cap) &&
+              dalloc(w, &h.req_list, (size_t)h.part_cap) && dalloc(w, &h.req_list2, 2 * (size_t)h.part_cap) &&
+              dalloc(w, &h.req_target, (size_t)h.part_cap) && dalloc(w, &h.scan_tmp, particle_scan_blocks() + 1) &&
+              dalloc(w, &w->d, 1);
+    PartSoA *ps[2] = {&h.p, &h.q};
+    size_t pc = (size_t)h.part_cap;
+    for (int k = 0; k < 2 && ok; k++) {
+        PartSoA *p = ps[k];
+        ok = dalloc(w, &p->x, pc) && dalloc(w, &p->y, pc) && dalloc(w, &p->vx, pc) && dalloc(w, &p->vy, pc) &&
+             dalloc(w, &p->ax, pc) && dalloc(w, &p->ay, pc) && dalloc(w, &p->tx, pc) && dalloc(w, &p->ty, pc) &&
+             dalloc(w, &p->tf, pc) && dalloc(w, &p->life, pc) && dalloc(w, &p->fade, pc) && dalloc(w, &p->col, pc) &&
+             dalloc(w, &p->sc, pc) && dalloc(w, &p->id, pc) && dalloc(w, &p->fl, pc) && dalloc(w, &p->bits, pc);
+    }
+    // chunk slots per colour: (world 0 << 20) | slot
+    for (int tk = 0; tk < 4 && ok; tk++) {
+        int ox = tk % 2, oy = 1 - tk / 2;
+        int na = (h.nCx - ox + 1) / 2, nb = (h.nCy - oy + 1) / 2;
+        int ns = std::max(0, na) * std::max(0, nb);
+        w->n_items[tk] = ns;
+        std::vector<uint32_t> v(ns);
+        for (int s = 0; s < ns; s++) v[s] = (uint32_t)s;
+        ok = dalloc(w, &w->items[tk], (size_t)std::max(ns, 1));
+        if (ok && ns) ok = cudaMemcpy(w->items[tk], v.data(), ns * 4, cudaMemcpyHostToDevice) == cudaSuccess;
+    }
+    if (!ok) {
+        free_world(w);
+        return FSE_E_NOMEM;
+    }
+    h.stage_count = w->ctr + 0;
+    h.part_count = w->ctr + 1;
+    h.req_count = w->ctr + 2;  // [3]
+    h.err = w->ctr + 5;
+    h.tick = (uint32_t *)(w->ctr + 6);
+    cudaMemset(w->ctr, 0, 16 * sizeof(int32_t));
+    cudaMemset(h.ledger, 0, LED_ROWS * MAXMAT * sizeof(long long));
+    cudaMemset(h.cp_count, 0, ncp * sizeof(int32_t));
+    // an empty world: GENERIC_AIR everywhere (world.cpp:133-145)
+    cudaMemset(h.id, 0, n * 2);
+    cudaMemset(h.col, 0, n * 4);
+    cudaMemset(h.sc, 0, n * 4);
+    cudaMemset(h.fl, 0, n);
+    cudaMemset(h.df, 0, n * 4);
+    if (cudaMemcpy(w->d, &h, sizeof(WorldDev), cudaMemcpyHostToDevice) != cudaSuccess) {
+        free_world(w);
+        return FSE_E_CUDA;
+    }
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+        free_world(w);
+        return FSE_E_CUDA;
+    }
+    *out = w;
+    return FSE_OK;
+}
+
+int fse_world_destroy(fse_world *w) {
+    if (!w) return FSE_E_INVAL;
+    cudaStreamSynchronize(w->stream);
+    free_world(w);
+    return FSE_OK;
+}
+
+static int read_ctr(fse_world *w, int32_t *out16) {
+    FSE_CUDA_TRY(cudaMemcpyAsync(out16, w->ctr, 16 * sizeof(int32_t), cudaMemcpyDeviceToHost, w->stream));
+    FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
+    return FSE_OK;
+}
+
+static uint32_t read_tick(fse_world *w) {
+    uint32_t t = 0;
+    cudaMemcpyAsync(&t, w->h.tick, 4, cudaMemcpyDeviceToHost, w->stream);
+    cudaStreamSynchronize(w->stream);
+    return t;
+}
+
+int fse_world_info(const fse_world *wc, int32_t out[8]) {
+    fse_world *w = (fse_world *)wc;
+    if (!w || !out) return FSE_E_INVAL;
+    int32_t c[16];
+    int rc = read_ctr(w, c);
+    if (rc) return rc;
+    out[0] = w->W;
+    out[1] = w->H;
+    out[2] = w->C;
+    out[3] = w->cell_iter;
+    out[4] = (int32_t)w->seed;
+    out[5] = (int32_t)read_tick(w);
+    out[6] = c[1];
+    out[7] = c[5];
+    return FSE_OK;
+}
+
+int fse_world_set_tick(fse_world *w, uint32_t tick) {
+    if (!w) return FSE_E_INVAL;
+    FSE_CUDA_TRY(cudaMemcpyAsync(w->h.tick, &tick, 4, cudaMemcpyHostToDevice, w->stream));
+    FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
+    return FSE_OK;
+}
+
+__global__ void k_mask_flags(uint8_t *fl, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        fl[i] &= (uint8_t)~VISITED;
+}
+
+int fse_world_upload(fse_world *w, const uint16_t *id, const uint32_t *col, const int32_t *sc, const uint8_t *fl,
+                     const int32_t *df) {
+    if (!w) return FSE_E_INVAL;
+    size_t n = (size_t)w->W * w->H;
+    const MatTable &t = host_table();
+    if (id)
+        for (size_t i = 0; i < n; i++)
+            if (id[i] >= t.n) return FSE_E_INVAL;
+    if (id) FSE_CUDA_TRY(cudaMemcpyAsync(w->h.id, id, n * 2, cudaMemcpyHostToDevice, w->stream));
+    if (col) FSE_CUDA_TRY(cudaMemcpyAsync(w->h.col, col, n * 4, cudaMemcpyHostToDevice, w->stream));
+    if (sc) FSE_CUDA_TRY(cudaMemcpyAsync(w->h.sc, sc, n * 4, cudaMemcpyHostToDevice, w->stream));
+    if (fl) {
+        FSE_CUDA_TRY(cudaMemcpyAsync(w->h.fl, fl, n, cudaMemcpyHostToDevice, w->stream));
+        // bit 6 of the flags is reserved for the kernel's visited mark
+        k_mask_flags<<<std::max(1, std::min<int>((int)(n / 1024) + 1, 4096)), 256, 0, w->stream>>>(w->h.fl, n);
+    }
+    if (df) FSE_CUDA_TRY(cudaMemcpyAsync(w->h.df, df, n * 4, cudaMemcpyHostToDevice, w->stream));
+    FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
+    return FSE_OK;
+}
+
+int fse_world_download(fse_world *w, uint16_t *id, uint32_t *col, int32_t *sc, uint8_t *fl, int32_t *df) {
+    if (!w) return FSE_E_INVAL;
+    size_t n = (size_t)w->W * w->H;
+    if (id) FSE_CUDA_TRY(cudaMemcpyAsync(id, w->h.id, n * 2, cudaMemcpyDeviceToHost, w->stream));
+    if (col) FSE_CUDA_TRY(cudaMemcpyAsync(col, w->h.col, n * 4, cudaMemcpyDeviceToHost, w->stream));
+    if (sc) FSE_CUDA_TRY(cudaMemcpyAsync(sc, w->h.sc, n * 4, cudaMemcpyDeviceToHost, w->stream));
+    if (fl) FSE_CUDA_TRY(cudaMemcpyAsync(fl, w->h.fl, n, cudaMemcpyDeviceToHost, w->stream));
+    if (df) FSE_CUDA_TRY(cudaMemcpyAsync(df, w->h.df, n * 4, cudaMemcpyDeviceToHost, w->stream));
+    FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
+    return FSE_OK;
+}
+
+// synthetic worlds; the same draw as the oracle's om_world_generate
+__global__ void k_generate(WorldDev *wd, int kind, uint32_t seed, const MatTable *__restrict__ mt, int m_sand,
+                           int m_water, int m_gas, int m_stone, int z0, int z1, int z2, int z3, int z4, int z5, int z6,
+                           int z7) {
+    const WorldDev &w = *wd;
+    const size_t n = (size_t)w.W * w.H;
+    const uint32_t pk = pass_key(seed, 0, PH_GEN + (uint32_t)(kind == FSE_GEN_ZIPF8 ? 1 : (kind == FSE_GEN_MIX ? 0 : 2)));
+    const int top = (w.H * 3) / 5;
+    const int zm[8] = {z0, z1, z2, z3, z4, z5, z6, z7};
+    const int zw[8] = {840, 420, 280, 210, 168, 140, 120, 105};
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        int y = (int)(i / w.W), x = (int)(i % w.W);
+        uint32_t ck = cell_key(pk, (uint32_t)x, (uint32_t)y);
+        uint32_t r = draw_k(ck, 0);
+        int mid = mt->id_air;
+        if (kind == FSE_GEN_MIX) {
+            if (y >= w.H - 8)
+                mid = m_stone;
+            else if (y < top) {
+                uint32_t u = r % 100u;
+                mid = u < 30 ? m_sand : u < 50 ? m_water : u < 60 ? m_gas : u < 75 ? m_stone : mt->id_air;
+            }
+        } else if (kind == FSE_GEN_ZIPF8) {
+            uint32_t u = r % 2283u, acc = 0;
+            for (int k = 0; k < 8; k++) {
+                acc += (uint32_t)zw[k];
+                if (u < acc) {
+                    mid = zm[k];
+                    break;
+                }
+            }
+        }
+        w.id[i] = (uint16_t)mid;
+        w.fl[i] = 0;
+        w.df[i] = 0;
+        w.sc[i] = mt->f_scalar[mid];
+        uint32_t colour = mt->f_base[mid];
+        uint32_t fp = mt->f_pack[mid];
+        int mod = (int)(fp >> 20);
+        if (mod > 0) colour += (uint32_t)((int)((fp >> 8) & 0xFFF) + (int)(draw_k(ck, 1) % (uint32_t)mod)) << (fp & 0xFF);
+        w.col[i] = colour;
+    }
+}
+
+int fse_world_generate(fse_world *w, int kind, uint32_t seed) {
+    if (!w || kind < 0 || kind > 2) return FSE_E_INVAL;
+    int rc = ensure_materials_pushed();
+    if (rc) return rc;
+    auto f = [](const char *s) {
+        int v = fse_material_find(s);
+        return v < 0 ? 0 : v;
+    };
+    size_t n = (size_t)w->W * w->H;
+    int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)sm_count() * 16);
+    k_generate<<<blocks, 256, 0, w->stream>>>(w->d, kind, seed, g_dev_mt, f("GENERIC_SAND"), f("WATER"), f("GENERIC_GAS"),
+                                              f("STONE"), f("GENERIC_AIR"), f("STONE"), f("GENERIC_SAND"), f("WATER"),
+                                              f("GENERIC_GAS"), f("DIRT"), f("GENERIC_LIQUID"), f("SOFT_DIRT_SAND"));
+    FSE_CUDA_TRY(cudaGetLastError());
+    FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
+    return FSE_OK;
+}
+
+int fse_world_get_tile(fse_world *w, int x, int y, uint16_t *id, uint32_t *col, int32_t *sc, uint8_t *fl) {
+    if (!w) return FSE_E_INVAL;
+    if (x < 0 || y < 0 || x >= w->W || y >= w->H) {
+        // world.cpp:1000: out of range reads Tiles_TEST_SOLID
+        if (id) *id = (uint16_t)host_table().id_solid;
+        if (col) *col = 0xff0000u;
+        if (sc) *sc = 0;
+        if (fl) *fl = 0;
+        return FSE_OK;
+    }
+    size_t i = (size_t)y * w->W + x;
+    if (id) FSE_CUDA_TRY(cudaMemcpyAsync(id, w->h.id + i, 2, cudaMemcpyDeviceToHost, w->stream));
+    if (col) FSE_CUDA_TRY(cudaMemcpyAsync(col, w->h.col + i, 4, cudaMemcpyDeviceToHost, w->stream));
+    if (sc) FSE_CUDA_TRY(cudaMemcpyAsync(sc, w->h.sc + i, 4, cudaMemcpyDeviceToHost, w->stream));
+    if (fl) FSE_CUDA_TRY(cudaMemcpyAsync(fl, w->h.fl + i, 1, cudaMemcpyDeviceToHost, w->stream));
+    FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
+    return FSE_OK;
+}
+
+int fse_world_set_tile(fse_world *w, int x, int y, uint16_t id, uint32_t col, int32_t sc, uint8_t fl) {
+    if (!w) return FSE_E_INVAL;
+    if (x < 0 || y < 0 || x >= w->W || y >= w->H) return FSE_OK;  // world.cpp:1005: dropped
+    if (id >= host_table().n) return FSE_E_INVAL;
+    size_t i = (size_t)y * w->W + x;
+    fl &= (uint8_t)~VISITED;
+    int32_t zero = 0;
+    FSE_CUDA_TRY(cudaMemcpyAsync(w->h.id + i, &id, 2, cudaMemcpyHostToDevice, w->stream));
+    FSE_CUDA_TRY(cudaMemcpyAsync(w->h.col + i, &col, 4, cudaMemcpyHostToDevice, w->stream));
+    FSE_CUDA_TRY(cudaMemcpyAsync(w->h.sc + i, &sc, 4, cudaMemcpyHostToDevice, w->stream));
+    FSE_CUDA_TRY(cudaMemcpyAsync(w->h.fl + i, &fl, 1, cudaMemcpyHostToDevice, w->stream));
+    FSE_CUDA_TRY(cudaMemcpyAsync(w->h.df + i, &zero, 4, cudaMemcpyHostToDevice, w->stream));
+    FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
+    return FSE_OK;
+}
+
+static int world_move_blocks(const fse_world *w) { return std::max(1, std::min(sm_count() * 4, ceil_div(w->part_cap, 256))); }
+static int world_stage_blocks(const fse_world *w) { return std::max(1, std::min(sm_count() * 2, ceil_div(w->stage_cap, 256))); }
+
+static int world_enqueue(fse_world *w, bool particles_after_tick, bool tick, bool particles) {
+    int rc = ensure_materials_pushed();
+    if (rc) return rc;
+    if (tick) {
+        rc = enqueue_step(w->d, 1, w->items, w->n_items, w->cell_iter, w->C, w->threads, w->grid, particles_after_tick,
+                          world_move_blocks(w), world_stage_blocks(w), w->stream);
+        if (rc) return rc;
+    } else if (particles) {
+        if (launch_particle_tick(w->d, 1, g_dev_mt, world_move_blocks(w), w->stream) != cudaSuccess) return FSE_E_CUDA;
+    }
+    return FSE_OK;
+}
+
+int fse_world_sync(fse_world *w) {
+    if (!w) return FSE_E_INVAL;
+    int32_t c[16];
+    int rc = read_ctr(w, c);
+    if (rc) return rc;
+    if (cudaGetLastError() != cudaSuccess) return FSE_E_CUDA;
+    return status_from_err(c[5]);
+}
+
+int fse_world_tick(fse_world *w, int n) {
+    if (!w || n < 0) return FSE_E_INVAL;
+    for (int i = 0; i < n; i++) {
+        int rc = world_enqueue(w, false, true, false);
+        if (rc) return rc;
+    }
+    return fse_world_sync(w);
+}
+
+int fse_particles_tick(fse_world *w) {
+    if (!w) return FSE_E_INVAL;
+    int rc = world_enqueue(w, false, false, true);
+    if (rc) return rc;
+    return fse_world_sync(w);
+}
+
+int fse_world_step(fse_world *w, int n) {
+    if (!w || n < 0) return FSE_E_INVAL;
+    for (int i = 0; i < n; i++) {
+        int rc = world_enqueue(w, true, true, true);
+        if (rc) return rc;
+    }
+    return fse_world_sync(w);
+}
+
+// capture `ticks` steps once, replay to cover n
+int fse_world_step_graph(fse_world *w, int n) {
+    if (!w || n < 0) return FSE_E_INVAL;
+    int rc = ensure_materials_pushed();
+    if (rc) return rc;
+    const int G = 32;
+    int done = 0;
+    while (done < n) {
+        int k = std::min(G, n - done);
+        auto it = w->graphs.find(k);
+        cudaGraphExec_t ex;
+        if (it == w->graphs.end()) {
+            cudaGraph_t g;
+            FSE_CUDA_TRY(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
+            int erc = FSE_OK;
+            for (int i = 0; i < k && erc == FSE_OK; i++)
+                erc = enqueue_step(w->d, 1, w->items, w->n_items, w->cell_iter, w->C, w->threads, w->grid, true,
+                                   world_move_blocks(w), world_stage_blocks(w), w->stream);
+            cudaError_t e = cudaStreamEndCapture(w->stream, &g);
+            if (erc != FSE_OK || e != cudaSuccess) return FSE_E_CUDA;
+            FSE_CUDA_TRY(cudaGraphInstantiate(&ex, g, 0));
+            cudaGraphDestroy(g);
+            w->graphs[k] = ex;
+        } else {
+            ex = it->second;
+        }
+        FSE_CUDA_TRY(cudaGraphLaunch(ex, w->stream));
+        done += k;
+    }
+    return fse_world_sync(w);
+}
+
+int fse_world_set_stream(fse_world *w, void *stream) {
+    if (!w) return FSE_E_INVAL;
+    cudaStreamSynchronize(w->stream);
+    for (auto &g : w->graphs) cudaGraphExecDestroy(g.second);
+    w->graphs.clear();
+    if (w->own_stream) cudaStreamDestroy(w->stream);
+    if (stream) {
+        w->stream = (cudaStream_t)stream;
+        w->own_stream = false;
+    } else {
+        FSE_CUDA_TRY(cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking));
+        w->own_stream = true;
+    }
+    return FSE_OK;
+}
+
+void *fse_world_stream(fse_world *w) { return w ? (void *)w->stream : nullptr; }
+
+// =============================================================== particles
+int fse_particles_count(fse_world *w, int *out_n) {
+    if (!w || !out_n) return FSE_E_INVAL;
+    int32_t c[16];
+    int rc = read_ctr(w, c);
+    if (rc) return rc;
+    *out_n = c[1];
+    return FSE_OK;
+}
+
+int fse_particles_add(fse_world *w, const fse_particle *parts, int n) {
+    if (!w || (n > 0 && !parts) || n < 0) return FSE_E_INVAL;
+    if (n == 0) return FSE_OK;
+    int cur;
+    int rc = fse_particles_count(w, &cur);
+    if (rc) return rc;
+    if ((long long)cur + n > w->part_cap) return FSE_E_CAPACITY;
+    std::vector<float> f[9];
+    std::vector<int32_t> life(n), fade(n), sc(n);
+    std::vector<uint32_t> col(n);
+    std::vector<uint16_t> id(n);
+    std::vector<uint8_t> fl(n), bits(n);
+    for (int k = 0; k < 9; k++) f[k].resize(n);
+    const MatTable &t = host_table();
+    for (int i = 0; i < n; i++) {
+        const fse_particle &p = parts[i];
+        if (p.id >= t.n) return FSE_E_INVAL;
+        const float v[9] = {p.x, p.y, p.vx, p.vy, p.ax, p.ay, p.target_x, p.target_y, p.target_force};
+        for (int k = 0; k < 9; k++) f[k][i] = v[k];
+        life[i] = p.lifetime;
+        fade[i] = p.fade_time;
+        sc[i] = p.scalar;
+        col[i] = p.colour;
+        id[i] = p.id;
+        fl[i] = p.flags & (uint8_t)~VISITED;
+        bits[i] = p.bits;
+    }
+    PartSoA &P = w->h.p;
+    float *dst[9] = {P.x, P.y, P.vx, P.vy, P.ax, P.ay, P.tx, P.ty, P.tf};
+    for (int k = 0; k < 9; k++)
+        FSE_CUDA_TRY(cudaMemcpyAsync(dst[k] + cur, f[k].data(), n * 4, cudaMemcpyHostToDevice, w->stream));
+    FSE_CUDA_TRY(cudaMemcpyAsync(P.life + cur, life.data(), n * 4, cudaMemcpyHostToDevice, w->stream));
+    FSE_CUDA_TRY(cudaMemcpyAsync(P.fade + cur, fade.data(), n * 4, cudaMemcpyHostToDevice, w->stream));
+    FSE_CUDA_TRY(cudaMemcpyAsync(P.sc + cur, sc.data(), n * 4, cudaMemcpyHostToDevice, w->stream));
+    FSE_CUDA_TRY(cudaMemcpyAsync(P.col + cur, col.data(), n * 4, cudaMemcpyHostToDevice, w->stream));
+    FSE_CUDA_TRY(cudaMemcpyAsync(P.id + cur, id.data(), n * 2, cudaMemcpyHostToDevice, w->stream));
+    FSE_CUDA_TRY(cudaMemcpyAsync(P.fl + cur, fl.data(), n, cudaMemcpyHostToDevice, w->stream));
+    FSE_CUDA_TRY(cudaMemcpyAsync(P.bits + cur, bits.data(), n, cudaMemcpyHostToDevice, w->stream));
+    int32_t nn = cur + n;
+    FSE_CUDA_TRY(cudaMemcpyAsync(w->h.part_count, &nn, 4, cudaMemcpyHostToDevice, w->stream));
+    FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
+    return FSE_OK;
+}
+
+int fse_particles_read(fse_world *w, fse_particle *out, int cap, int *out_n) {
+    if (!w || cap < 0 || (cap > 0 && !out)) return FSE_E_INVAL;
+    int n;
+    int rc = fse_particles_count(w, &n);
+    if (rc) return rc;
+    if (out_n) *out_n = n;
+    int m = std::min(n, cap);
+    if (m == 0) return FSE_OK;
+    std::vector<float> f[9];
+    std::vector<int32_t> life(m), fade(m), sc(m);
+    std::vector<uint32_t> col(m);
+    std::vector<uint16_t> id(m);
+    std::vector<uint8_t> fl(m), bits(m);
+    PartSoA &P = w->h.p;
+    float *src[9] = {P.x, P.y, P.vx, P.vy, P.ax, P.ay, P.tx, P.ty, P.tf};
+    for (int k = 0; k < 9; k++) {
+        f[k].resize(m);
+        FSE_CUDA_TRY(cudaMemcpyAsync(f[k].data(), src[k], m * 4, cudaMemcpyDeviceToHost, w->stream));
+    }
+    FSE_CUDA_TRY(cudaMemcpyAsync(life.data(), P.life, m * 4, cudaMemcpyDeviceToHost, w->stream));
+    FSE_CUDA_TRY(cudaMemcpyAsync(fade.data(), P.fade, m * 4, cudaMemcpyDeviceToHost, w->stream));
+    FSE_CUDA_TRY(cudaMemcpyAsync(sc.data(), P.sc, m * 4, cudaMemcpyDeviceToHost, w->stream));
+    FSE_CUDA_TRY(cudaMemcpyAsync(col.data(), P.col, m * 4, cudaMemcpyDeviceToHost, w->stream));
+    FSE_CUDA_TRY(cudaMemcpyAsync(id.data(), P.id, m * 2, cudaMemcpyDeviceToHost, w->stream));
+    FSE_CUDA_TRY(cudaMemcpyAsync(fl.data(), P.fl, m, cudaMemcpyDeviceToHost, w->stream));
+    FSE_CUDA_TRY(cudaMemcpyAsync(bits.data(), P.bits, m, cudaMemcpyDeviceToHost, w->stream));
+    FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
+    for (int i = 0; i < m; i++) {
+        fse_particle &p = out[i];
+        p.x = f[0][i];
+        p.y = f[1][i];
+        p.vx = f[2][i];
+        p.vy = f[3][i];
+        p.ax = f[4][i];
+        p.ay = f[5][i];
+        p.target_x = f[6][i];
+        p.target_y = f[7][i];
+        p.target_force = f[8][i];
+        p.lifetime = life[i];
+        p.fade_time = fade[i];
+        p.colour = col[i];
+        p.scalar = sc[i];
+        p.id = id[i];
+        p.flags = fl[i];
+        p.bits = bits[i];
+    }
+    return FSE_OK;
+}
+
+// ================================================================= ledger
+int fse_world_ledger(fse_world *w, int64_t *out) {
+    if (!w || !out) return FSE_E_INVAL;
+    std::vector<long long> buf(LED_ROWS * MAXMAT);
+    FSE_CUDA_TRY(cudaMemcpyAsync(buf.data(), w->h.ledger, buf.size() * 8, cudaMemcpyDeviceToHost, w->stream));
+    FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
+    int n = fse_material_count();
+    for (int r = 0; r < LED_ROWS; r++)
+        for (int m = 0; m < n; m++) out[r * n + m] = buf[r * MAXMAT + m];
+    return FSE_OK;
+}
+
+int fse_world_ledger_reset(fse_world *w) {
+    if (!w) return FSE_E_INVAL;
+    FSE_CUDA_TRY(cudaMemsetAsync(w->h.ledger, 0, LED_ROWS * MAXMAT * 8, w->stream));
+    FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
+    return FSE_OK;
+}
+
+__global__ void k_census(const WorldDev *__restrict__ wd, const MatTable *__restrict__ mt, long long *out) {
+    __shared__ unsigned long long s[4 * MAXMAT];
+    for (int i = threadIdx.x; i < 4 * MAXMAT; i += blockDim.x) s[i] = 0;
+    __syncthreads();
+    const WorldDev &w = *wd;
+    const size_t n = (size_t)w.W * w.H;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        int id = w.id[i];
+        atomicAdd(&s[id], 1ull);
+        if (mt_type(mt->a[id]) == T_SOUP)
+            atomicAdd(&s[MAXMAT + id], (unsigned long long)((long long)w.sc[i] + w.df[i]));
+    }
+    const int np = *w.part_count;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        int id = w.p.id[i];
+        atomicAdd(&s[2 * MAXMAT + id], 1ull);
+        if (mt_type(mt->a[id]) == T_SOUP) atomicAdd(&s[3 * MAXMAT + id], (unsigned long long)(long long)w.p.sc[i]);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 4 * MAXMAT; i += blockDim.x)
+        if (s[i]) atomicAdd((unsigned long long *)&out[i], s[i]);
+}
+
+int fse_world_census(fse_world *w, int64_t *out) {
+    if (!w || !out) return FSE_E_INVAL;
+    int rc = ensure_materials_pushed();
+    if (rc) return rc;
+    long long *d = nullptr;
+    FSE_CUDA_TRY(cudaMalloc(&d, 4 * MAXMAT * 8));
+    cudaMemsetAsync(d, 0, 4 * MAXMAT * 8, w->stream);
+    k_census<<<sm_count() * 2, 512, 0, w->stream>>>(w->d, g_dev_mt, d);
+    std::vector<long long> buf(4 * MAXMAT);
+    cudaMemcpyAsync(buf.data(), d, buf.size() * 8, cudaMemcpyDeviceToHost, w->stream);
+    cudaError_t e = cudaStreamSynchronize(w->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return FSE_E_CUDA;
+    int n = fse_material_count();
+    for (int r = 0; r < 4; r++)
+        for (int m = 0; m < n; m++) out[r * n + m] = buf[r * MAXMAT + m];
+    return FSE_OK;
+}
+
+}  // extern "C"

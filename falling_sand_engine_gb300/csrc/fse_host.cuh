@@ -1,0 +1,62 @@
+// fse_host.cuh -- host-side structures shared by the C ABI translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "fse_internal.cuh"
+
+struct fse_world {
+    int W, H, C, cell_iter;
+    uint32_t seed;
+    int part_cap, stage_cap;
+    cudaStream_t stream;
+    bool own_stream;
+    fse::WorldDev h;      // host mirror of the device descriptor (pointers, sizes)
+    fse::WorldDev *d;     // device descriptor
+    uint32_t *items[4];   // chunk slots per colour
+    int n_items[4];
+    int32_t *ctr;         // small device counters
+    uint32_t *claim;      // object stamp / readback claims (allocated on first use)
+    uint8_t *mask_bits;   // object mask scratch (allocated on first use)
+    uint32_t *obj_list;   // object list scratch
+    size_t obj_list_cap;
+    int64_t *obj_n;       // object list count
+    std::map<int, cudaGraphExec_t> graphs;  // n_ticks -> step graph
+    size_t bytes;         // device bytes owned
+    int threads, grid;    // colour-pass launch shape
+};
+
+namespace fse {
+
+extern MatTable *g_dev_mt;
+int ensure_materials_pushed();
+const MatTable &host_table();
+
+size_t colour_pass_smem(int C, int halo);
+cudaError_t launch_colour_pass(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
+                               const MatTable *mt, int halo, int C, int threads, int grid, cudaStream_t s);
+cudaError_t launch_spawn_append(WorldDev *d_worlds, int n_worlds, int stage_blocks, cudaStream_t s);
+cudaError_t launch_particle_tick(WorldDev *d_worlds, int n_worlds, const MatTable *mt, int move_blocks,
+                                 cudaStream_t s);
+void particle_prepare();
+int particle_scan_blocks();
+int sm_count();
+int status_from_err(int err);
+int tick_halo();
+
+// one world::tick() + optionally world::tickCells() for a set of worlds that
+// share a device descriptor table
+int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], const int n_items[4], int max_iter,
+                 int C, int threads, int grid, bool particles, int move_blocks, int stage_blocks, cudaStream_t s);
+
+}  // namespace fse
+
+#define FSE_CUDA_TRY(expr)                     \
+    do {                                       \
+        cudaError_t e_ = (expr);               \
+        if (e_ != cudaSuccess) return FSE_E_CUDA; \
+    } while (0)

@@ -1,0 +1,144 @@
+// fse_internal.cuh -- device-side definitions shared by the tick, particle and
+// object kernels and by the host orchestration.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/fse.h"
+
+namespace fse {
+
+// PhysicsType, source/engine/game_datastruct.hpp:87-95
+enum : int { T_AIR = 0, T_SOLID = 1, T_SAND = 2, T_SOUP = 3, T_GAS = 4, T_OBJECT = 5 };
+enum : int { INTER_TRANSFORM = 1, INTER_SPAWN = 2, REACT_BELOW = 4, REACT_ABOVE = 5 };
+
+constexpr int MAXMAT = 256;
+constexpr uint8_t MOVED = 0x80;
+constexpr uint8_t VISITED = 0x40;  // shared-memory copy only; never stored to HBM
+constexpr uint8_t SETTLE_MASK = 0x3F;
+constexpr uint16_t DIRTY = 0x8000;  // shared-memory copy only: cell must be written back
+
+// FLUID_* (source/engine/core/const.h:23-34) in Q16.16
+constexpr int32_t Q_MAXV = 32768;
+constexpr int32_t Q_MINV = 33;
+constexpr int32_t Q_MAXCOMP = 6554;
+constexpr int32_t Q_MAXFLOW = 524288;
+constexpr int32_t Q_FREEFALL = 327;
+constexpr int32_t Q_DEFAULT = 131072;
+
+constexpr uint32_t PH_GEN = 0x47454E00u;
+constexpr uint32_t PH_STAMP = 0x5354414Du;
+
+// ledger rows
+enum : int { LED_CN = 0, LED_DN = 1, LED_XN = 2, LED_CF = 3, LED_DF = 4, LED_XF = 5, LED_ROWS = 6 };
+
+// error bits recorded by kernels (world->err)
+enum : int { ERR_SPAWN_CAP = 1, ERR_PART_CAP = 2, ERR_BOUNDS = 4, ERR_TIMEOUT = 8 };
+
+// ------------------------------------------------------------------ RNG
+// lowbias32 integer finaliser (C. Wellons, public domain); keys follow
+// (seed, tick, phase) -> (x, y) -> draw index.
+__host__ __device__ __forceinline__ uint32_t hash32(uint32_t h) {
+    h ^= h >> 16;
+    h *= 0x7feb352dU;
+    h ^= h >> 15;
+    h *= 0x846ca68bU;
+    h ^= h >> 16;
+    return h;
+}
+__host__ __device__ __forceinline__ uint32_t pass_key(uint32_t seed, uint32_t tick, uint32_t phase) {
+    uint32_t h = hash32(seed ^ 0x5bd1e995U);
+    h = hash32(h ^ tick);
+    return hash32(h ^ (phase * 0x9E3779B9U + 0x7F4A7C15U));
+}
+__host__ __device__ __forceinline__ uint32_t cell_key(uint32_t pk, uint32_t x, uint32_t y) {
+    return hash32(hash32(pk ^ x) ^ (y * 0x85EBCA6BU));
+}
+__host__ __device__ __forceinline__ uint32_t draw_k(uint32_t ck, uint32_t k) {
+    return hash32(ck + k * 0x9E3779B9U + 0x632BE5ABU);
+}
+
+// --------------------------------------------------------- material table
+// Packed per-material word A: type | iterations << 8 | slip << 16 | max_stab << 24,
+// word B: density bits. Factory: base colour, (shift | lo << 8 | mod << 20), scalar.
+struct MatTable {
+    int n;
+    int id_air, id_solid, id_fire, id_water, id_lava, id_steam, id_obsidian;
+    int has_inter;
+    uint32_t a[MAXMAT];
+    float density[MAXMAT];
+    uint32_t f_base[MAXMAT];
+    uint32_t f_pack[MAXMAT];
+    int32_t f_scalar[MAXMAT];
+    // reactions: up to 4 per material, (kind, temperature, result)
+    int32_t n_react[MAXMAT];
+    int32_t react[MAXMAT][4][3];
+    // interactions: flat list of (mat, other, kind, data1, data2, ofsx, ofsy), n_inter entries
+    int32_t n_inter;
+    int32_t inter[512][7];
+};
+
+__host__ __device__ __forceinline__ int mt_type(uint32_t a) { return (int)(a & 0xFF); }
+__host__ __device__ __forceinline__ int mt_iter(uint32_t a) { return (int)((a >> 8) & 0xFF); }
+__host__ __device__ __forceinline__ int mt_slip(uint32_t a) { return (int)((a >> 16) & 0xFF); }
+__host__ __device__ __forceinline__ int mt_stab(uint32_t a) { return (int)((a >> 24) & 0xFF); }
+
+// ------------------------------------------------------------------ world
+struct SpawnRec {  // one spawned particle awaiting its place in the list (48 B)
+    uint32_t cp;    // chunk-pass index within the tick
+    uint32_t rank;  // position within that chunk-pass
+    float x, y, vx, vy, ay;
+    uint32_t colour;
+    int32_t scalar;
+    uint16_t id;
+    uint8_t flags;
+    uint8_t bits;
+    int16_t lifetime;
+    int16_t fade;
+    uint32_t pad;
+};
+
+struct PartSoA {  // particle list, structure of arrays
+    float *x, *y, *vx, *vy, *ax, *ay, *tx, *ty, *tf;
+    int32_t *life, *fade;
+    uint32_t *col;
+    int32_t *sc;
+    uint16_t *id;
+    uint8_t *fl, *bits;
+};
+
+struct WorldDev {
+    uint16_t *id;
+    uint32_t *col;
+    int32_t *sc;
+    uint8_t *fl;
+    int32_t *df;  // pending fluid diff; meaningful only where the cell is SOUP
+    int W, H, C, cell_iter;
+    uint32_t seed;
+    uint32_t *tick;  // device counter, advanced on the device so multi-tick graphs replay correctly
+    int nCx, nCy, max_slots;
+    // spawned-particle staging for the current tick
+    SpawnRec *stage;
+    int32_t *stage_count;
+    int32_t stage_cap;
+    int32_t *cp_count;  // [cell_iter * 4 * max_slots]
+    int32_t *cp_base;
+    // particles
+    PartSoA p, q;           // p = live list, q = compaction scratch
+    int32_t *part_count;    // device-resident live count
+    int32_t part_cap;
+    uint8_t *p_state;       // per particle: 0 alive, 1 dead, 2 open deposit request
+    int32_t *p_lxly;        // packed start cell of the request (ly * W + lx)
+    int32_t *req_list;      // open deposit requests (particle indices)
+    int32_t *req_count;     // [2] ping-pong counts
+    int32_t *req_list2;
+    int32_t *req_target;    // per request: target cell, or -1
+    int32_t *scan_tmp;      // block sums for compaction
+    long long *ledger;      // [LED_ROWS][MAXMAT]
+    int32_t *err;
+};
+
+__host__ __device__ __forceinline__ int ceil_div(int a, int b) { return (a + b - 1) / b; }
+
+}  // namespace fse

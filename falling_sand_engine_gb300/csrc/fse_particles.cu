@@ -1,0 +1,546 @@
+// fse_particles.cu -- free particles: the ordered append of particles spawned by
+// the cell tick (world.cpp:1078,1110-1119,1222,1298,1901-1913) and the particle
+// update world::tickCells() (world.cpp:2030-2195).
+//
+// Every kernel takes the world table and handles world blockIdx.y, so one launch
+// serves a single world or a whole batch. Arithmetic on particle state uses the
+// explicitly rounded intrinsics (__fadd_rn, __fmul_rn, __fdiv_rn, __fsqrt_rn) so
+// that no multiply-add is contracted: the FP32 results equal a strict IEEE CPU
+// evaluation of the same expressions bit for bit.
+#include "fse_internal.cuh"
+
+namespace fse {
+
+constexpr int PART_BLOCKS = 64;  // blocks per world for the particle list kernels
+constexpr int PART_THREADS = 256;
+
+// p_state values
+enum : uint8_t { PS_ALIVE = 0, PS_DEAD = 1, PS_DIRECT = 2, PS_SPIRAL = 3 };
+
+__constant__ int8_t c_spiral[1024][2];
+__constant__ int c_spiral_n;
+
+// -------------------------------------------------------------- spawn append
+// Exclusive scan of the per-chunk-pass spawn counts of one world (one CTA per
+// world); reserves the tail of the particle list for this tick's spawns.
+__global__ void k_spawn_scan(const WorldDev *__restrict__ worlds) {
+    const WorldDev &w = worlds[blockIdx.x];
+    __shared__ int s_sum[32];
+    __shared__ int s_carry;
+    const int n = w.cell_iter * 4 * w.max_slots;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    for (int base = 0; base < n; base += blockDim.x) {
+        int i = base + threadIdx.x;
+        int v = (i < n) ? w.cp_count[i] : 0;
+        int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        int inc = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        if (lane == 31) s_sum[wid] = inc;
+        __syncthreads();
+        if (wid == 0) {
+            int s = lane < nw ? s_sum[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                int t = __shfl_up_sync(0xffffffffu, s, o);
+                if (lane >= o) s += t;
+            }
+            if (lane < nw) s_sum[lane] = s;
+        }
+        __syncthreads();
+        int before = (wid > 0 ? s_sum[wid - 1] : 0) + s_carry;
+        if (i < n) w.cp_base[i] = before + inc - v;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry += s_sum[nw - 1];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        int old = *w.part_count;
+        long long nn = (long long)old + s_carry;
+        if (nn > w.part_cap) {
+            atomicOr(w.err, ERR_PART_CAP);
+            nn = w.part_cap;
+        }
+        w.cp_base[n] = old;  // list position of the first spawned particle
+        *w.part_count = (int)nn;
+    }
+}
+
+__global__ void k_spawn_scatter(const WorldDev *__restrict__ worlds) {
+    const WorldDev &w = worlds[blockIdx.y];
+    const int n = min(*w.stage_count, w.stage_cap);
+    const int first = w.cp_base[w.cell_iter * 4 * w.max_slots];
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const SpawnRec s = w.stage[r];
+        long long pos = (long long)first + w.cp_base[s.cp] + s.rank;
+        if (pos >= w.part_cap) continue;  // ERR_PART_CAP already recorded
+        int i = (int)pos;
+        w.p.x[i] = s.x;
+        w.p.y[i] = s.y;
+        w.p.vx[i] = s.vx;
+        w.p.vy[i] = s.vy;
+        w.p.ax[i] = 0.f;
+        w.p.ay[i] = s.ay;
+        w.p.tx[i] = 0.f;
+        w.p.ty[i] = 0.f;
+        w.p.tf[i] = 0.f;
+        w.p.life[i] = s.lifetime;
+        w.p.fade[i] = s.fade;
+        w.p.col[i] = s.colour;
+        w.p.sc[i] = s.scalar;
+        w.p.id[i] = s.id;
+        w.p.fl[i] = s.flags;
+        w.p.bits[i] = s.bits;
+    }
+}
+
+// reset the per-tick spawn bookkeeping and advance the tick counter
+__global__ void k_tick_end(const WorldDev *worlds) {
+    const WorldDev &w = worlds[blockIdx.x];
+    if (threadIdx.x == 0) {
+        *w.stage_count = 0;
+        *w.tick += 1;  // world.cpp:1925
+    }
+}
+
+// ----------------------------------------------------------------- motion
+__device__ __forceinline__ bool out_of_world(float x, float y, int W, int H) {
+    // `x < 0 || (int)x >= width || y < 0 || (int)y >= height` (world.cpp:2056);
+    // written so that NaN and huge values also count as outside
+    return !(x >= 0.0f && x < (float)W && y >= 0.0f && y < (float)H);
+}
+
+__device__ __forceinline__ void led_part(const WorldDev &w, const MatTable *mt, int row_n, int row_f, int id,
+                                         int32_t sc) {
+    int ty = mt_type(mt->a[id]);
+    if (ty == T_AIR) return;
+    atomicAdd((unsigned long long *)&w.ledger[row_n * MAXMAT + id], 1ull);
+    if (ty == T_SOUP && sc != 0)
+        atomicAdd((unsigned long long *)&w.ledger[row_f * MAXMAT + id], (unsigned long long)(long long)sc);
+}
+
+// world.cpp:2032-2188 for every particle against the grid left by the cell tick;
+// collisions become deposit requests resolved by the kernels below.
+__global__ void k_part_move(const WorldDev *__restrict__ worlds, const MatTable *__restrict__ mt) {
+    const WorldDev &w = worlds[blockIdx.y];
+    const int n = *w.part_count;
+    const int W = w.W, H = w.H;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint8_t bits = w.p.bits[i];
+        int32_t life = w.p.life[i];
+        if ((bits & 2) && life <= 0) {  // :2033-2037
+            w.p_state[i] = PS_DEAD;
+            led_part(w, mt, LED_DN, LED_DF, w.p.id[i], w.p.sc[i]);
+            continue;
+        }
+        float x = w.p.x[i], y = w.p.y[i], vx = w.p.vx[i], vy = w.p.vy[i];
+        float tf = w.p.tf[i];
+        if (tf != 0.f) {  // :2039-2051
+            float tdx = __fsub_rn(w.p.tx[i], x), tdy = __fsub_rn(w.p.ty[i], y);
+            float nf = __fsqrt_rn(__fadd_rn(__fmul_rn(tdx, tdx), __fmul_rn(tdy, tdy)));
+            vx = __fadd_rn(vx, __fmul_rn(__fdiv_rn(tdx, nf), tf));
+            vy = __fadd_rn(vy, __fmul_rn(__fdiv_rn(tdy, nf), tf));
+            if (nf < 100.f) {
+                vx = __fmul_rn(vx, 0.95f);
+                vy = __fmul_rn(vy, 0.95f);
+            }
+        }
+        uint8_t st = PS_ALIVE;
+        if (out_of_world(x, y, W, H)) {  // :2056-2059
+            w.p_state[i] = PS_DEAD;
+            w.p.vx[i] = vx;
+            w.p.vy[i] = vy;
+            led_part(w, mt, LED_XN, LED_XF, w.p.id[i], w.p.sc[i]);
+            continue;
+        }
+        const int lx = (int)x, ly = (int)y;
+        vx = __fadd_rn(vx, w.p.ax[i]);  // :2063-2064
+        vy = __fadd_rn(vy, w.p.ay[i]);
+        const int div = (int)__fadd_rn(__fadd_rn(fabsf(vx), fabsf(vy)), 1.0f);
+        const float dvx = __fdiv_rn(vx, (float)div), dvy = __fdiv_rn(vy, (float)div);
+        bool done = false;
+        for (int s = 0; s < div && !done; s++) {  // :2071-2184
+            x = __fadd_rn(x, dvx);
+            y = __fadd_rn(y, dvy);
+            if (out_of_world(x, y, W, H)) {
+                st = PS_DEAD;
+                led_part(w, mt, LED_XN, LED_XF, w.p.id[i], w.p.sc[i]);
+                done = true;
+                break;
+            }
+            int ct = mt_type(mt->a[w.id[(size_t)(int)y * W + (int)x]]);
+            if (!(bits & 1) && ct != T_AIR) {
+                bool isObject = ct == T_OBJECT;
+                int ps = (bits >> 2) & 3;
+                if (ps == 0)
+                    ps = isObject ? 1 : 2;
+                else if (ps == 1 && !isObject)
+                    ps = 2;
+                bits = (uint8_t)((bits & ~0x0Cu) | ((unsigned)ps << 2));
+                if (!isObject || ps == 2) {
+                    if (bits & 2) {
+                        st = PS_DEAD;
+                        led_part(w, mt, LED_DN, LED_DF, w.p.id[i], w.p.sc[i]);
+                    } else {
+                        st = (mt_type(mt->a[w.id[(size_t)ly * W + lx]]) != T_AIR) ? PS_SPIRAL : PS_DIRECT;
+                    }
+                    done = true;
+                }
+            }
+        }
+        if (!done && life > 0) life--;  // :2186-2188
+        w.p.x[i] = x;
+        w.p.y[i] = y;
+        w.p.vx[i] = vx;
+        w.p.vy[i] = vy;
+        w.p.bits[i] = bits;
+        w.p.life[i] = life;
+        w.p_state[i] = st;
+        if (st == PS_DIRECT || st == PS_SPIRAL) {
+            w.p_lxly[i] = ly * W + lx;
+            int j = atomicAdd(&w.req_count[0], 1);
+            w.req_list[j] = i;
+        }
+    }
+}
+
+// ------------------------------------------------------------- deposits
+// Target of a deposit against the current grid (world.cpp:2093-2147):
+// returns cell index, with bit 31 set for a merge into the same liquid; -1 if none.
+__device__ __forceinline__ int dep_target(const WorldDev &w, const MatTable *mt, int i, uint8_t st) {
+    const int W = w.W, H = w.H;
+    if (st == PS_DIRECT) {
+        int c = w.p_lxly[i];
+        if (mt_type(mt->a[w.id[c]]) == T_AIR) return c;
+    }
+    const float x = w.p.x[i], y = w.p.y[i];
+    const int pid = w.p.id[i];
+    const bool psoup = mt_type(mt->a[pid]) == T_SOUP;
+    const int n = c_spiral_n;
+    for (int j = 0; j < n; j++) {
+        int cx = (int)__fadd_rn(x, (float)c_spiral[j][0]);
+        int cy = (int)__fadd_rn(y, (float)c_spiral[j][1]);
+        if (cx < 0 || cy < 0 || cx >= W || cy >= H) continue;
+        int c = cy * W + cx;
+        int cid = w.id[c];
+        if (mt_type(mt->a[cid]) == T_AIR) return c;
+        if (psoup && cid == pid) return c | (int)0x80000000u;
+    }
+    return -1;
+}
+
+__device__ __forceinline__ void dep_fail(const WorldDev &w, int i) {
+    // :2141-2144
+    w.p.vy[i] = -4.0f;
+    w.p.y[i] = __fsub_rn(w.p.y[i], 16.0f);
+    w.p_state[i] = PS_ALIVE;
+}
+__device__ __forceinline__ void dep_merge(const WorldDev &w, const MatTable *mt, int i, int c) {
+    // :2119-2125
+    atomicAdd(&w.sc[c], w.p.sc[i]);
+    w.p_state[i] = PS_DEAD;
+    atomicAdd((unsigned long long *)&w.ledger[LED_DN * MAXMAT + w.p.id[i]], 1ull);
+}
+__device__ __forceinline__ void dep_fill(const WorldDev &w, int i, int c) {
+    // :2115-2118, :2148-2152; the cell's diff word still holds the claim and is
+    // cleared by k_dep_clear
+    w.id[c] = w.p.id[i];
+    w.col[c] = w.p.col[i];
+    w.sc[c] = w.p.sc[i];
+    w.fl[c] = w.p.fl[i];
+    w.p_state[i] = PS_DEAD;
+}
+
+// round 1 over all requests, phase 1: pick targets; AIR targets get the claim sentinel
+__global__ void k_dep_target(const WorldDev *__restrict__ worlds, const MatTable *__restrict__ mt) {
+    const WorldDev &w = worlds[blockIdx.y];
+    const int n = w.req_count[0];
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        int i = w.req_list[j];
+        int t = dep_target(w, mt, i, w.p_state[i]);
+        w.req_target[j] = t;
+        if (t >= 0) w.df[t] = 0x7fffffff;
+    }
+}
+// phase 2: claims (lowest particle index wins an AIR cell), merges, failures
+__global__ void k_dep_claim(const WorldDev *__restrict__ worlds, const MatTable *__restrict__ mt) {
+    const WorldDev &w = worlds[blockIdx.y];
+    const int n = w.req_count[0];
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        int i = w.req_list[j], t = w.req_target[j];
+        if (t == -1)
+            dep_fail(w, i);
+        else if (t < 0)
+            dep_merge(w, mt, i, t & 0x7fffffff);
+        else
+            atomicMin(&w.df[t], i);
+    }
+}
+// phase 3: winners write their tile; losers search again from where they stopped
+__global__ void k_dep_decide(const WorldDev *__restrict__ worlds) {
+    const WorldDev &w = worlds[blockIdx.y];
+    const int n = w.req_count[0];
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        int i = w.req_list[j], t = w.req_target[j];
+        if (t < 0) continue;
+        if (w.df[t] == i) {
+            dep_fill(w, i, t);
+            int k = atomicAdd(&w.req_count[2], 1);  // filled cells, for k_dep_clear
+            w.req_list2[w.part_cap + k] = t;
+        } else {
+            w.p_state[i] = PS_SPIRAL;
+            int k = atomicAdd(&w.req_count[1], 1);
+            w.req_list2[k] = i;
+        }
+    }
+}
+
+// the remaining rounds in one CTA per world (few requests are left after round 1)
+__global__ void k_dep_finish(const WorldDev *__restrict__ worlds, const MatTable *__restrict__ mt) {
+    const WorldDev &w = worlds[blockIdx.x];
+    __shared__ int s_n, s_next, s_fill;
+    if (threadIdx.x == 0) {
+        s_n = w.req_count[1];
+        s_fill = w.req_count[2];
+    }
+    __syncthreads();
+    int32_t *cur = w.req_list2, *nxt = w.req_list;
+    // every round settles at least the lowest open request, so n rounds suffice
+    for (int round = 0; s_n > 0; round++) {
+        if (round > (1 << 22)) {
+            if (threadIdx.x == 0) atomicOr(w.err, ERR_TIMEOUT);
+            break;
+        }
+        const int n = s_n;
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+            int i = cur[j];
+            int t = dep_target(w, mt, i, w.p_state[i]);
+            w.req_target[j] = t;
+            if (t >= 0) w.df[t] = 0x7fffffff;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_next = 0;
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+            int i = cur[j], t = w.req_target[j];
+            if (t == -1)
+                dep_fail(w, i);
+            else if (t < 0)
+                dep_merge(w, mt, i, t & 0x7fffffff);
+            else
+                atomicMin(&w.df[t], i);
+        }
+        __syncthreads();
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+            int i = cur[j], t = w.req_target[j];
+            if (t < 0) continue;
+            if (w.df[t] == i) {
+                dep_fill(w, i, t);
+                int k = atomicAdd(&s_fill, 1);
+                w.req_list2[w.part_cap + k] = t;
+            } else {
+                int k = atomicAdd(&s_next, 1);
+                nxt[k] = i;
+            }
+        }
+        __syncthreads();
+        // losers keep list order? not needed: claims compare particle indices
+        int32_t *tmp = cur;
+        cur = nxt;
+        nxt = tmp;
+        if (threadIdx.x == 0) s_n = s_next;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) w.req_count[2] = s_fill;
+}
+
+// filled cells no longer hold a claim: their diff word becomes 0
+__global__ void k_dep_clear(const WorldDev *__restrict__ worlds) {
+    const WorldDev &w = worlds[blockIdx.y];
+    const int n = w.req_count[2];
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        w.df[w.req_list2[w.part_cap + j]] = 0;
+}
+
+// ------------------------------------------------------------- compaction
+// stable removal of dead particles (std::erase_if, world.cpp:2190) and of
+// particles below the world (world.cpp:2203)
+__device__ __forceinline__ bool keep(const WorldDev &w, int i) {
+    return w.p_state[i] == PS_ALIVE && !(w.p.y[i] > (float)w.H);
+}
+
+__global__ void k_cmp_count(const WorldDev *__restrict__ worlds) {
+    const WorldDev &w = worlds[blockIdx.y];
+    const int n = *w.part_count;
+    const int seg = (n + gridDim.x - 1) / gridDim.x;
+    const int b0 = blockIdx.x * seg, b1 = min(n, b0 + seg);
+    int cnt = 0;
+    for (int i = b0 + threadIdx.x; i < b1; i += blockDim.x) cnt += keep(w, i) ? 1 : 0;
+    __shared__ int s[32];
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) t += s[k];
+        w.scan_tmp[blockIdx.x] = t;
+    }
+}
+
+__global__ void k_cmp_scan(const WorldDev *__restrict__ worlds, int nblocks) {
+    const WorldDev &w = worlds[blockIdx.x];
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int b = 0; b < nblocks; b++) {
+            int v = w.scan_tmp[b];
+            w.scan_tmp[b] = run;
+            run += v;
+        }
+        w.scan_tmp[nblocks] = run;
+    }
+}
+
+__global__ void k_cmp_scatter(const WorldDev *__restrict__ worlds) {
+    const WorldDev &w = worlds[blockIdx.y];
+    const int n = *w.part_count;
+    const int seg = (n + gridDim.x - 1) / gridDim.x;
+    const int b0 = blockIdx.x * seg, b1 = min(n, b0 + seg);
+    __shared__ int s[32];
+    __shared__ int s_carry;
+    if (threadIdx.x == 0) s_carry = w.scan_tmp[blockIdx.x];
+    __syncthreads();
+    for (int base = b0; base < b1; base += blockDim.x) {
+        int i = base + threadIdx.x;
+        int v = (i < b1 && keep(w, i)) ? 1 : 0;
+        int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        unsigned m = __ballot_sync(0xffffffffu, v);
+        int inwarp = __popc(m & ((1u << lane) - 1u));
+        if (lane == 0) s[wid] = __popc(m);
+        __syncthreads();
+        int before = s_carry;
+        for (int k = 0; k < wid; k++) before += s[k];
+        if (v) {
+            int o = before + inwarp;
+            w.q.x[o] = w.p.x[i];
+            w.q.y[o] = w.p.y[i];
+            w.q.vx[o] = w.p.vx[i];
+            w.q.vy[o] = w.p.vy[i];
+            w.q.ax[o] = w.p.ax[i];
+            w.q.ay[o] = w.p.ay[i];
+            w.q.tx[o] = w.p.tx[i];
+            w.q.ty[o] = w.p.ty[i];
+            w.q.tf[o] = w.p.tf[i];
+            w.q.life[o] = w.p.life[i];
+            w.q.fade[o] = w.p.fade[i];
+            w.q.col[o] = w.p.col[i];
+            w.q.sc[o] = w.p.sc[i];
+            w.q.id[o] = w.p.id[i];
+            w.q.fl[o] = w.p.fl[i];
+            w.q.bits[o] = w.p.bits[i];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int t = 0;
+            for (int k = 0; k < nw; k++) t += s[k];
+            s_carry += t;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_cmp_copy(const WorldDev *__restrict__ worlds, int nblocks) {
+    const WorldDev &w = worlds[blockIdx.y];
+    const int m = w.scan_tmp[nblocks];
+    for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < m; o += gridDim.x * blockDim.x) {
+        w.p.x[o] = w.q.x[o];
+        w.p.y[o] = w.q.y[o];
+        w.p.vx[o] = w.q.vx[o];
+        w.p.vy[o] = w.q.vy[o];
+        w.p.ax[o] = w.q.ax[o];
+        w.p.ay[o] = w.q.ay[o];
+        w.p.tx[o] = w.q.tx[o];
+        w.p.ty[o] = w.q.ty[o];
+        w.p.tf[o] = w.q.tf[o];
+        w.p.life[o] = w.q.life[o];
+        w.p.fade[o] = w.q.fade[o];
+        w.p.col[o] = w.q.col[o];
+        w.p.sc[o] = w.q.sc[o];
+        w.p.id[o] = w.q.id[o];
+        w.p.fl[o] = w.q.fl[o];
+        w.p.bits[o] = w.q.bits[o];
+    }
+}
+
+__global__ void k_part_end(const WorldDev *worlds, int nblocks) {
+    const WorldDev &w = worlds[blockIdx.x];
+    if (threadIdx.x == 0) {
+        *w.part_count = w.scan_tmp[nblocks];
+        w.req_count[0] = 0;
+        w.req_count[1] = 0;
+        w.req_count[2] = 0;
+    }
+}
+
+// ---------------------------------------------------------------- launchers
+static bool g_spiral_ready = false;
+
+static void spiral_upload() {
+    if (g_spiral_ready) return;
+    // the spiral walk of world.cpp:2105-2133 (X = Y = 32, maxI = 1024)
+    int8_t tab[1024][2];
+    int X = 32, Y = 32, x = 0, y = 0, dx = 0, dy = -1;
+    int t = X > Y ? X : Y;
+    int maxI = t * t, n = 0;
+    for (int j = 0; j < maxI; j++) {
+        if ((-X / 2 <= x) && (x <= X / 2) && (-Y / 2 <= y) && (y <= Y / 2)) {
+            tab[n][0] = (int8_t)x;
+            tab[n][1] = (int8_t)y;
+            n++;
+        }
+        if ((x == y) || ((x < 0) && (x == -y)) || ((x > 0) && (x == 1 - y))) {
+            t = dx;
+            dx = -dy;
+            dy = t;
+        }
+        x += dx;
+        y += dy;
+    }
+    cudaMemcpyToSymbol(c_spiral, tab, sizeof(tab));
+    cudaMemcpyToSymbol(c_spiral_n, &n, sizeof(int));
+    g_spiral_ready = true;
+}
+
+void particle_prepare() { spiral_upload(); }
+
+// this tick's spawns -> end of the particle list, then the tick counter
+cudaError_t launch_spawn_append(WorldDev *d_worlds, int n_worlds, int stage_blocks, cudaStream_t s) {
+    k_spawn_scan<<<n_worlds, 1024, 0, s>>>(d_worlds);
+    dim3 g(stage_blocks, n_worlds);
+    k_spawn_scatter<<<g, 256, 0, s>>>(d_worlds);
+    k_tick_end<<<n_worlds, 32, 0, s>>>(d_worlds);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_particle_tick(WorldDev *d_worlds, int n_worlds, const MatTable *mt, int move_blocks,
+                                 cudaStream_t s) {
+    spiral_upload();
+    dim3 gm(move_blocks, n_worlds);
+    k_part_move<<<gm, 256, 0, s>>>(d_worlds, mt);
+    k_dep_target<<<gm, 256, 0, s>>>(d_worlds, mt);
+    k_dep_claim<<<gm, 256, 0, s>>>(d_worlds, mt);
+    k_dep_decide<<<gm, 256, 0, s>>>(d_worlds);
+    k_dep_finish<<<n_worlds, 1024, 0, s>>>(d_worlds, mt);
+    k_dep_clear<<<gm, 256, 0, s>>>(d_worlds);
+    dim3 gc(PART_BLOCKS, n_worlds);
+    k_cmp_count<<<gc, PART_THREADS, 0, s>>>(d_worlds);
+    k_cmp_scan<<<n_worlds, 32, 0, s>>>(d_worlds, PART_BLOCKS);
+    k_cmp_scatter<<<gc, PART_THREADS, 0, s>>>(d_worlds);
+    k_cmp_copy<<<gm, 256, 0, s>>>(d_worlds, PART_BLOCKS);
+    k_part_end<<<n_worlds, 32, 0, s>>>(d_worlds, PART_BLOCKS);
+    return cudaGetLastError();
+}
+
+int particle_scan_blocks() { return PART_BLOCKS; }
+
+}  // namespace fse

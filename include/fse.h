@@ -1,0 +1,218 @@
+/*
+ * fse.h -- C ABI of the GB300 falling-sand world tick.
+ *
+ * Drop-in boundary for the reference engine's world update. Every function is
+ * extern "C", takes plain pointers and sizes, returns an int status (0 = FSE_OK,
+ * negative = error) and never throws. Worlds are opaque handles used by one host
+ * thread at a time; each world is bound to one CUDA stream. Device memory is owned
+ * by the library and released by fse_world_destroy().
+ *
+ * Reference interfaces replaced (paths relative to the reference project root):
+ *   fse_materials_begin       InitMaterials()            source/engine/game_datastruct.cpp:117-280
+ *   fse_material_register     RegisterMaterial(...)      source/engine/game_datastruct.cpp:282-289
+ *   fse_materials_push        PushMaterials()            source/engine/game_datastruct.cpp:291-300
+ *   fse_materials_load_lua    Lua materials_register()   source/engine/game_basic.cpp:79-81
+ *   fse_world_create          world::init (grids)        source/engine/world.cpp:43-145
+ *   fse_world_tick            world::tick()              source/engine/world.cpp:1036-1948
+ *   fse_particles_tick        world::tickCells()         source/engine/world.cpp:2030-2195
+ *   fse_particles_add         world::addCell(CellData*)  source/engine/world.cpp:2292
+ *   fse_world_get_tile/set    world::getTile/setTile     source/engine/world.cpp:999-1008
+ *   fse_object_stamp          rigid-body tile stamping   source/engine/game.cpp:1768-1814
+ *   fse_object_readback       rigid-body tile readback   source/engine/game.cpp:1896-1983
+ */
+#ifndef FSE_H
+#define FSE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ status codes */
+#define FSE_OK 0
+#define FSE_E_INVAL (-1)    /* bad argument or handle */
+#define FSE_E_NOMEM (-2)    /* device or host allocation failed */
+#define FSE_E_BUDGET (-3)   /* admission refused by the HBM budget */
+#define FSE_E_CUDA (-4)     /* CUDA runtime error */
+#define FSE_E_TIMEOUT (-5)  /* a bounded device wait gave up */
+#define FSE_E_CAPACITY (-6) /* particle / spawn capacity exceeded (excess dropped) */
+#define FSE_E_STATE (-7)    /* call not valid in the current state */
+#define FSE_E_BOUNDS (-8)   /* a kernel's own bounds check fired (access skipped) */
+
+/* PhysicsType, source/engine/game_datastruct.hpp:87-95 */
+#define FSE_AIR 0
+#define FSE_SOLID 1
+#define FSE_SAND 2
+#define FSE_SOUP 3
+#define FSE_GAS 4
+#define FSE_PASSABLE 5
+#define FSE_OBJECT 5
+
+/* reaction / interaction kinds, source/engine/game_datastruct.hpp:97-103 */
+#define FSE_INTERACT_TRANSFORM_MATERIAL 1
+#define FSE_INTERACT_SPAWN_MATERIAL 2
+#define FSE_REACT_TEMPERATURE_BELOW 4
+#define FSE_REACT_TEMPERATURE_ABOVE 5
+
+/* fluid amounts are Q16.16 fixed point: 1.0 == FSE_FLUID_ONE */
+#define FSE_FLUID_ONE 65536
+
+/* synthetic world generators */
+#define FSE_GEN_EMPTY 0  /* all GENERIC_AIR */
+#define FSE_GEN_MIX 1    /* bottom 8 rows STONE; top 60%: 30% sand, 20% water, 10% gas, 15% stone, 25% air */
+#define FSE_GEN_ZIPF8 2  /* 8 materials, Zipf(s=1) frequencies, whole world */
+
+/* Per-world configuration. Zero-initialise and set what you need. */
+typedef struct fse_config {
+    int32_t chunk_size;   /* colour-partition chunk edge (CHUNK_W/H, const.h:19-20); 0 -> 128 */
+    int32_t cell_iter;    /* iterations per tick (global_def.cell_iter); 0 -> 3 */
+    uint32_t seed;        /* counter-RNG seed (replaces srand/rand) */
+    int32_t particle_capacity; /* max live particles; 0 -> max(65536, cells / 4) */
+    int32_t spawn_capacity;    /* max particles spawned per tick; 0 -> particle_capacity */
+    void *stream;         /* cudaStream_t to bind; NULL -> a library-owned stream */
+} fse_config;
+
+/* One free particle (CellData, source/engine/game_utils/cells.h:15-36). 56 bytes. */
+typedef struct fse_particle {
+    float x, y, vx, vy, ax, ay;
+    float target_x, target_y, target_force;
+    int32_t lifetime, fade_time;
+    uint32_t colour;
+    int32_t scalar; /* fluid amount (Q16.16) for SOUP tiles, temperature otherwise */
+    uint16_t id;    /* material of the carried tile */
+    uint8_t flags;  /* tile flags: bit7 moved, bits0-5 settle count */
+    uint8_t bits;   /* bit0 phase, bit1 temporary, bits2-3 inObjectState */
+} fse_particle;
+
+/* A rigid body stamped into the grid as OBJECT tiles. 48 bytes. */
+typedef struct fse_body {
+    float x, y, sin_a, cos_a; /* body position and sin/cos of its angle */
+    int32_t w, h;             /* tile box (matWidth x matHeight) */
+    uint16_t id;              /* tile material (e.g. GENERIC_OBJECT) */
+    uint16_t pad;
+    uint32_t colour;
+    int32_t n_sand, n_soup;   /* out: SAND / SOUP cells displaced by the last stamp (damping) */
+    int32_t n_placed, n_recovered; /* out: tiles placed by stamp / taken back by readback */
+} fse_body;
+
+typedef struct fse_world fse_world;
+typedef struct fse_batch fse_batch;
+typedef struct fse_server fse_server;
+
+/* ---------------------------------------------------------------- version */
+const char *fse_version(void);
+const char *fse_status_string(int status);
+
+/* -------------------------------------------------------------- materials */
+/* Reset the table to the built-in materials in InitMaterials order (ids 0-27,
+ * then TEST_SAND, TEST_TEXTURED_SAND, TEST_LIQUID as 28-30). */
+int fse_materials_begin(void);
+/* RegisterMaterial(s_id, name, index_name, physicsType, slipperyness, alpha,
+ * density, iterations, emit, emitColor, color); *out_id = the new material id. */
+int fse_material_register(int s_id, const char *name, const char *index_name, int physics_type, int slipperyness,
+                          int alpha, float density, int iterations, int emit, uint32_t emit_colour, uint32_t colour,
+                          int *out_id);
+int fse_material_set_reaction(int mat, int kind, int temperature, int result_mat);
+int fse_material_set_interaction(int mat, int other, int kind, int data1_mat, int data2_radius, int ofs_x, int ofs_y);
+/* tile factory of a material: colour = base + ((lo + rand % mod) << shift) when mod > 0 */
+int fse_material_set_factory(int mat, uint32_t base, int shift, int lo, int mod, int32_t scalar);
+/* Execute the materials_register(...) calls of a Lua script text (the subset of
+ * Lua used by data/scripts: literal arguments and integer/float expressions).
+ * *out_count = number of materials registered. */
+int fse_materials_load_lua(const char *script, int *out_count);
+/* Freeze the table and upload it to the device (PushMaterials). */
+int fse_materials_push(void);
+int fse_material_count(void);
+int fse_material_find(const char *index_name);
+/* 16 ints: type, density bits, iterations, slip, max_stab, alpha, colour, emit,
+ * emit_colour, f_base, f_shift, f_lo, f_mod, f_scalar, n_react, interact */
+int fse_material_get(int id, int32_t out[16]);
+
+/* ----------------------------------------------------------------- worlds */
+int fse_world_create(int width, int height, const fse_config *cfg, fse_world **out);
+int fse_world_destroy(fse_world *world);
+int fse_world_info(const fse_world *world, int32_t out[8]); /* w, h, chunk, cell_iter, seed, tick, particles, err */
+/* host SoA <-> device SoA (cells row-major, width * height each); NULL planes are skipped */
+int fse_world_upload(fse_world *world, const uint16_t *id, const uint32_t *colour, const int32_t *scalar,
+                     const uint8_t *flags, const int32_t *diff);
+int fse_world_download(fse_world *world, uint16_t *id, uint32_t *colour, int32_t *scalar, uint8_t *flags,
+                       int32_t *diff);
+int fse_world_generate(fse_world *world, int kind, uint32_t seed);
+int fse_world_set_tick(fse_world *world, uint32_t tick);
+int fse_world_get_tile(fse_world *world, int x, int y, uint16_t *id, uint32_t *colour, int32_t *scalar,
+                       uint8_t *flags);
+int fse_world_set_tile(fse_world *world, int x, int y, uint16_t id, uint32_t colour, int32_t scalar, uint8_t flags);
+
+/* world::tick(), n times (no particle step in between) */
+int fse_world_tick(fse_world *world, int n_ticks);
+/* world::tickCells() */
+int fse_particles_tick(fse_world *world);
+/* the game-loop order: n x (world::tick(); world::tickCells()) */
+int fse_world_step(fse_world *world, int n_ticks);
+/* record n_ticks steps into a CUDA graph once and replay it: same results as
+ * fse_world_step, fewer launches */
+int fse_world_step_graph(fse_world *world, int n_ticks);
+/* wait for the world's stream; returns the first error the kernels recorded */
+int fse_world_sync(fse_world *world);
+int fse_world_set_stream(fse_world *world, void *stream);
+void *fse_world_stream(fse_world *world);
+
+/* ------------------------------------------------------------- particles */
+int fse_particles_add(fse_world *world, const fse_particle *parts, int n);
+int fse_particles_count(fse_world *world, int *out_n);
+int fse_particles_read(fse_world *world, fse_particle *out, int cap, int *out_n);
+
+/* ---------------------------------------------------------------- objects */
+int fse_object_stamp(fse_world *world, fse_body *bodies, int n);
+int fse_object_readback(fse_world *world, fse_body *bodies, int n, int64_t *out_removed);
+/* 1 bit per cell (row-major, LSB first): physics type == OBJECT; host buffer of
+ * ceil(w*h/8) bytes */
+int fse_object_mask_export(fse_world *world, uint8_t *host_bits);
+/* compact list of OBJECT cell indices (y*w+x, ascending); *out_n = count (may exceed cap) */
+int fse_object_list_export(fse_world *world, uint32_t *host_idx, int64_t cap, int64_t *out_n);
+
+/* ----------------------------------------------------------------- ledger */
+/* 6 rows x fse_material_count(): created_n, destroyed_n, exited_n, created_f,
+ * destroyed_f, exited_f (f in Q16.16) accumulated since creation or reset */
+int fse_world_ledger(fse_world *world, int64_t *out);
+int fse_world_ledger_reset(fse_world *world);
+/* 4 rows: grid_count, grid_fluid (amount + pending diff), part_count, part_fluid */
+int fse_world_census(fse_world *world, int64_t *out);
+
+/* --------------------------------------------------------------- batches */
+/* Many worlds ticked by one launch per colour pass over the chunks of all worlds. */
+int fse_batch_create(fse_world **worlds, int n, fse_batch **out);
+int fse_batch_destroy(fse_batch *batch);
+int fse_batch_step(fse_batch *batch, int n_ticks);
+/* capture graph_ticks steps into one CUDA graph (default 32) and replay */
+int fse_batch_step_graph(fse_batch *batch, int n_ticks, int graph_ticks);
+/* choose launch shape by timing candidates on scratch copies; results never change */
+int fse_batch_autotune(fse_batch *batch, int32_t out_choice[4]);
+int fse_batch_set_launch(fse_batch *batch, int threads, int ctas_per_sm);
+int fse_batch_sync(fse_batch *batch);
+
+/* ---------------------------------------------------------------- serving */
+int fse_server_create(int64_t hbm_budget_bytes, int max_active, fse_server **out);
+int fse_server_destroy(fse_server *srv);
+/* admit a world (allocates it if the HBM budget allows); *out_slot = world slot */
+int fse_server_add_world(fse_server *srv, int width, int height, const fse_config *cfg, int gen_kind,
+                         uint32_t gen_seed, int *out_slot);
+int fse_server_remove_world(fse_server *srv, int slot);
+int64_t fse_server_bytes_in_use(const fse_server *srv);
+fse_world *fse_server_world(fse_server *srv, int slot);
+/* queue a request of n_ticks steps for a world; arrival_us is the caller's clock */
+int fse_server_submit(fse_server *srv, int slot, int n_ticks, double arrival_us, int64_t *out_request);
+/* run one scheduling step: every active request advances one tick in one batched
+ * launch sequence; requests that finish are reported by fse_server_poll */
+int fse_server_step(fse_server *srv, int *out_active);
+/* microseconds since the server was created: the clock of arrivals and completions */
+double fse_server_now_us(const fse_server *srv);
+/* completed requests: ids and completion times (fse_server_now_us clock) */
+int fse_server_poll(fse_server *srv, double now_us, int64_t *ids, double *done_us, int cap, int *out_n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FSE_H */

@@ -1,0 +1,234 @@
+"""ctypes binding of the C oracle (oracle/fse_oracle.c).
+
+Test infrastructure: the checker the CUDA path is compared against.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libfse_oracle.so")
+
+PARTICLE_DTYPE = np.dtype(
+    [
+        ("x", "<f4"), ("y", "<f4"), ("vx", "<f4"), ("vy", "<f4"), ("ax", "<f4"), ("ay", "<f4"),
+        ("target_x", "<f4"), ("target_y", "<f4"), ("target_force", "<f4"),
+        ("lifetime", "<i4"), ("fade_time", "<i4"), ("colour", "<u4"), ("scalar", "<i4"),
+        ("id", "<u2"), ("flags", "u1"), ("bits", "u1"),
+    ]
+)
+assert PARTICLE_DTYPE.itemsize == 56
+
+BODY_DTYPE = np.dtype(
+    [
+        ("x", "<f4"), ("y", "<f4"), ("sin_a", "<f4"), ("cos_a", "<f4"),
+        ("w", "<i4"), ("h", "<i4"), ("id", "<u2"), ("pad", "<u2"), ("colour", "<u4"),
+        ("n_sand", "<i4"), ("n_soup", "<i4"), ("n_placed", "<i4"), ("n_recovered", "<i4"),
+    ]
+)
+assert BODY_DTYPE.itemsize == 48
+
+ORDER_SEQ = 0
+ORDER_PART = 1
+
+
+def build_oracle(force=False):
+    """Compile the oracle with its Makefile (gcc, no reference sources)."""
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(
+        os.path.getmtime(os.path.join(HERE, f)) for f in ("fse_oracle.c", "fse_oracle.h", "Makefile")
+    ):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Oracle:
+    """Process-wide handle on the oracle library (its material table is global)."""
+
+    _lib = None
+
+    def __init__(self):
+        if Oracle._lib is None:
+            build_oracle()
+            lib = C.CDLL(LIB_PATH)
+            vp, i32, u32 = C.c_void_p, C.c_int, C.c_uint32
+            sig = {
+                "om_materials_reset_builtin": (None, []),
+                "om_material_register": (i32, [i32, C.c_char_p, C.c_char_p, i32, i32, i32, C.c_float, i32, i32, u32, u32]),
+                "om_material_set_factory": (i32, [i32, u32, i32, i32, i32, C.c_int32]),
+                "om_material_set_reaction": (i32, [i32, i32, i32, i32]),
+                "om_material_set_interaction": (i32, [i32, i32, i32, i32, i32, i32, i32]),
+                "om_material_count": (i32, []),
+                "om_material_find": (i32, [C.c_char_p]),
+                "om_material_get": (None, [i32, vp]),
+                "om_world_new": (vp, [i32, i32, i32, i32, u32]),
+                "om_world_free": (None, [vp]),
+                "om_world_set": (None, [vp, vp, vp, vp, vp, vp]),
+                "om_world_get": (None, [vp, vp, vp, vp, vp, vp]),
+                "om_world_generate": (None, [vp, i32, u32]),
+                "om_world_set_tick": (None, [vp, u32]),
+                "om_world_get_tick": (u32, [vp]),
+                "om_world_tick": (C.c_long, [vp, i32, i32]),
+                "om_particles_tick": (i32, [vp]),
+                "om_world_step": (None, [vp, i32, i32]),
+                "om_particles_count": (i32, [vp]),
+                "om_particles_get": (None, [vp, vp]),
+                "om_particles_set": (None, [vp, vp, i32]),
+                "om_ledger_get": (None, [vp, vp]),
+                "om_ledger_reset": (None, [vp]),
+                "om_census": (None, [vp, vp]),
+                "om_particles_kinematics_f64": (None, [vp, vp, i32, vp, vp, vp]),
+                "om_particles_kinematics_f32": (None, [vp, vp, i32, vp, vp, vp]),
+                "om_object_stamp": (None, [vp, vp, i32]),
+                "om_object_readback": (C.c_long, [vp, vp, i32]),
+                "om_object_mask": (None, [vp, vp]),
+                "om_set_threads": (None, [i32]),
+                "om_debug_set_lattice": (None, [i32, i32, i32]),
+            }
+            for name, (res, args) in sig.items():
+                f = getattr(lib, name)
+                f.restype = res
+                f.argtypes = args
+            Oracle._lib = lib
+        self.lib = Oracle._lib
+
+    def reset_materials(self):
+        self.lib.om_materials_reset_builtin()
+
+    def material_count(self):
+        return self.lib.om_material_count()
+
+    def find(self, index_name):
+        return self.lib.om_material_find(index_name.encode())
+
+    def material(self, mid):
+        out = np.zeros(16, np.int32)
+        self.lib.om_material_get(mid, _ptr(out))
+        return out
+
+    def register(self, s_id, name, index_name, physics_type, slipperyness, alpha, density, iterations, emit=0,
+                 emit_colour=0, colour=0xFFFFFFFF):
+        return self.lib.om_material_register(s_id, name.encode(), index_name.encode(), physics_type, slipperyness,
+                                             alpha, density, iterations, emit, emit_colour, colour)
+
+    def set_reaction(self, mat, kind, temperature, result):
+        return self.lib.om_material_set_reaction(mat, kind, temperature, result)
+
+    def set_interaction(self, mat, other, kind, data1, data2, ofs_x, ofs_y):
+        return self.lib.om_material_set_interaction(mat, other, kind, data1, data2, ofs_x, ofs_y)
+
+    def set_factory(self, mat, base, shift, lo, mod, scalar):
+        return self.lib.om_material_set_factory(mat, base, shift, lo, mod, scalar)
+
+    def set_threads(self, n):
+        self.lib.om_set_threads(n)
+
+    def debug_set_lattice(self, sweep, px, py):
+        self.lib.om_debug_set_lattice(sweep, px, py)
+
+
+class OracleWorld:
+    """One oracle world (SoA planes + particle list)."""
+
+    def __init__(self, w, h, chunk=128, cell_iter=3, seed=1234):
+        self.o = Oracle()
+        self.lib = self.o.lib
+        self.w, self.h = w, h
+        self.h_ = self.lib.om_world_new(w, h, chunk, cell_iter, seed)
+        if not self.h_:
+            raise ValueError("bad world parameters")
+
+    def __del__(self):
+        try:
+            if self.h_:
+                self.lib.om_world_free(self.h_)
+                self.h_ = None
+        except Exception:
+            pass
+
+    def generate(self, kind, seed):
+        self.lib.om_world_generate(self.h_, kind, seed)
+
+    def set_state(self, planes):
+        n = self.w * self.h
+        arrs = [np.ascontiguousarray(planes[k], dt).reshape(n) for k, dt in
+                (("id", np.uint16), ("colour", np.uint32), ("scalar", np.int32), ("flags", np.uint8),
+                 ("diff", np.int32))]
+        self.lib.om_world_set(self.h_, *[_ptr(a) for a in arrs])
+
+    def state(self):
+        n = self.w * self.h
+        out = {"id": np.empty(n, np.uint16), "colour": np.empty(n, np.uint32), "scalar": np.empty(n, np.int32),
+               "flags": np.empty(n, np.uint8), "diff": np.empty(n, np.int32)}
+        self.lib.om_world_get(self.h_, *[_ptr(out[k]) for k in ("id", "colour", "scalar", "flags", "diff")])
+        return {k: v.reshape(self.h, self.w) for k, v in out.items()}
+
+    @property
+    def tick_count(self):
+        return self.lib.om_world_get_tick(self.h_)
+
+    @tick_count.setter
+    def tick_count(self, t):
+        self.lib.om_world_set_tick(self.h_, t)
+
+    def tick(self, order=ORDER_PART, check_races=False):
+        return self.lib.om_world_tick(self.h_, order, 1 if check_races else 0)
+
+    def particles_tick(self):
+        return self.lib.om_particles_tick(self.h_)
+
+    def step(self, n=1, order=ORDER_PART):
+        self.lib.om_world_step(self.h_, order, n)
+
+    def particles(self):
+        n = self.lib.om_particles_count(self.h_)
+        out = np.zeros(n, PARTICLE_DTYPE)
+        if n:
+            self.lib.om_particles_get(self.h_, _ptr(out))
+        return out
+
+    def set_particles(self, parts):
+        parts = np.ascontiguousarray(parts, PARTICLE_DTYPE)
+        self.lib.om_particles_set(self.h_, _ptr(parts), len(parts))
+
+    def ledger(self):
+        m = self.o.material_count()
+        out = np.zeros(6 * m, np.int64)
+        self.lib.om_ledger_get(self.h_, _ptr(out))
+        return out.reshape(6, m)
+
+    def reset_ledger(self):
+        self.lib.om_ledger_reset(self.h_)
+
+    def census(self):
+        m = self.o.material_count()
+        out = np.zeros(4 * m, np.int64)
+        self.lib.om_census(self.h_, _ptr(out))
+        return out.reshape(4, m)
+
+    def kinematics(self, parts, f64=True):
+        parts = np.ascontiguousarray(parts, PARTICLE_DTYPE)
+        n = len(parts)
+        out = np.zeros(4 * n, np.float64 if f64 else np.float32)
+        ev = np.zeros(n, np.int32)
+        sub = np.zeros(n, np.int32)
+        fn = self.lib.om_particles_kinematics_f64 if f64 else self.lib.om_particles_kinematics_f32
+        fn(self.h_, _ptr(parts), n, _ptr(out), _ptr(ev), _ptr(sub))
+        return out.reshape(n, 4), ev, sub
+
+    def object_stamp(self, bodies):
+        self.lib.om_object_stamp(self.h_, _ptr(bodies), len(bodies))
+
+    def object_readback(self, bodies):
+        return self.lib.om_object_readback(self.h_, _ptr(bodies), len(bodies))
+
+    def object_mask(self):
+        n = self.w * self.h
+        out = np.zeros((n + 7) // 8, np.uint8)
+        self.lib.om_object_mask(self.h_, _ptr(out))
+        return out

@@ -1,0 +1,1722 @@
+/*
+ * fse_oracle.c -- CPU oracle for the falling-sand world tick (TEST INFRASTRUCTURE).
+ *
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load this
+ * library; the product library never links or calls it.
+ *
+ * Each rule below cites the reference line it restates (paths relative to the
+ * reference project root). Deviations from the reference that the GPU design needs
+ * are stated where they occur; they are the same in both update orders:
+ *   - fluid amounts are Q16.16 fixed point (int32) instead of f32, so that flows,
+ *     commits and the mass ledger are exact and order-independent;
+ *   - rand() is replaced by a counter RNG keyed on (seed, tick, iter, sweep, x, y, k);
+ *   - out-of-world reads return the GENERIC_SOLID instance and out-of-world writes
+ *     are dropped, for every access (the reference does this only in getTile/setTile
+ *     and relies on a one-chunk margin elsewhere);
+ *   - the settle counter is 6 bits, saturating at 63 (u8, wrapping, in the reference);
+ *   - soup free-fall splits the amount exactly (remainder to the first particles).
+ */
+#include "fse_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ------------------------------------------------------------------ constants */
+/* PhysicsType, source/engine/game_datastruct.hpp:87-95 */
+enum { T_AIR = 0, T_SOLID = 1, T_SAND = 2, T_SOUP = 3, T_GAS = 4, T_OBJECT = 5 };
+/* interaction/reaction kinds, game_datastruct.hpp:97-103 */
+enum { INTER_TRANSFORM = 1, INTER_SPAWN = 2, REACT_BELOW = 4, REACT_ABOVE = 5 };
+
+#define MAXMAT 256
+#define MOVED 0x80u
+#define SETTLE_MASK 0x3Fu
+
+/* FLUID_* constants, source/engine/core/const.h:23-34, in Q16.16 */
+#define Q_ONE 65536
+#define Q_MAXV 32768     /* FLUID_MaxValue 0.5 */
+#define Q_MINV 33        /* amount < FLUID_MinValue (0.0005 = 32.77) <=> q < 33 */
+#define Q_MAXCOMP 6554   /* FLUID_MaxCompression 0.1 */
+#define Q_MAXFLOW 524288 /* FLUID_MaxFlow 8.0 */
+#define Q_FREEFALL 327   /* amount > 0.005 (327.68) <=> q > 327, world.cpp:1283 */
+#define Q_DEFAULT 131072 /* MaterialInstance::fluidAmount default 2.0f, game_datastruct.hpp:221 */
+
+/* RNG phases */
+#define PH_GEN 0x47454E00u
+#define PH_STAMP 0x5354414Du
+
+/* ---------------------------------------------------------------------- RNG */
+/* lowbias32 integer finaliser (C. Wellons, public domain) */
+static inline uint32_t hash32(uint32_t h) {
+    h ^= h >> 16;
+    h *= 0x7feb352dU;
+    h ^= h >> 15;
+    h *= 0x846ca68bU;
+    h ^= h >> 16;
+    return h;
+}
+static inline uint32_t pass_key(uint32_t seed, uint32_t tick, uint32_t phase) {
+    uint32_t h = hash32(seed ^ 0x5bd1e995U);
+    h = hash32(h ^ tick);
+    return hash32(h ^ (phase * 0x9E3779B9U + 0x7F4A7C15U));
+}
+static inline uint32_t cell_key(uint32_t pk, uint32_t x, uint32_t y) {
+    return hash32(hash32(pk ^ x) ^ (y * 0x85EBCA6BU));
+}
+static inline uint32_t draw_k(uint32_t ck, uint32_t k) { return hash32(ck + k * 0x9E3779B9U + 0x632BE5ABU); }
+
+/* ---------------------------------------------------------------- materials */
+typedef struct {
+    int kind, data1, data2, ofsx, ofsy;
+} inter_t;
+
+typedef struct {
+    int type;
+    float density;
+    int iterations, slip, max_stab, alpha;
+    uint32_t colour;
+    int emit;
+    uint32_t emit_colour;
+    /* tile factory: colour = base + ((lo + draw % mod) << shift) if mod > 0 */
+    uint32_t f_base;
+    int f_shift, f_lo, f_mod;
+    int32_t f_scalar;
+    int n_react;
+    inter_t react[4];
+    int interact;
+    char index_name[48];
+} mat_t;
+
+static mat_t M[MAXMAT];
+static int NMAT = 0;
+static int HAS_INTER = 0;
+/* interactions: (mat, other) -> up to 4 entries */
+typedef struct {
+    int mat, other, n;
+    inter_t e[4];
+} inter_list_t;
+static inter_list_t INTER[512];
+static int NINTER = 0;
+static int ID_AIR = 0, ID_SOLID = 1, ID_FIRE = -1, ID_WATER = -1, ID_LAVA = -1, ID_STEAM = -1, ID_OBSIDIAN = -1;
+
+static int max_stability(int slip) {
+    /* world.cpp:1623 `int maxStability = 8 / sqrt(slipperyness) + 1;` (double math) */
+    if (slip <= 0) return 1 << 20;
+    return (int)(8.0 / sqrt((double)slip) + 1.0);
+}
+
+static int reg(const char *index_name, int type, int slip, int alpha, float density, int iterations, int emit,
+               uint32_t emit_colour, uint32_t colour) {
+    if (NMAT >= MAXMAT) return -1;
+    mat_t *m = &M[NMAT];
+    memset(m, 0, sizeof(*m));
+    m->type = type;
+    m->density = density;
+    m->iterations = iterations;
+    m->slip = slip;
+    m->max_stab = max_stability(slip);
+    m->alpha = alpha;
+    m->colour = colour;
+    m->emit = emit;
+    m->emit_colour = emit_colour;
+    m->f_base = colour;
+    m->f_scalar = (type == T_SOUP) ? Q_DEFAULT : 0;
+    strncpy(m->index_name, index_name, sizeof(m->index_name) - 1);
+    return NMAT++;
+}
+
+int om_material_find(const char *index_name) {
+    for (int i = 0; i < NMAT; i++)
+        if (strcmp(M[i].index_name, index_name) == 0) return i;
+    return -1;
+}
+
+static void refresh_ids(void) {
+    ID_AIR = om_material_find("GENERIC_AIR");
+    ID_SOLID = om_material_find("GENERIC_SOLID");
+    ID_FIRE = om_material_find("FIRE");
+    ID_WATER = om_material_find("WATER");
+    ID_LAVA = om_material_find("LAVA");
+    ID_STEAM = om_material_find("STEAM");
+    ID_OBSIDIAN = om_material_find("OBSIDIAN");
+    if (ID_AIR < 0) ID_AIR = 0;
+    if (ID_SOLID < 0) ID_SOLID = 1;
+}
+
+int om_material_set_factory(int mat, uint32_t base, int shift, int lo, int mod, int32_t scalar) {
+    if (mat < 0 || mat >= NMAT) return -1;
+    M[mat].f_base = base;
+    M[mat].f_shift = shift;
+    M[mat].f_lo = lo;
+    M[mat].f_mod = mod;
+    M[mat].f_scalar = scalar;
+    return 0;
+}
+
+/* InitMaterials, game_datastruct.cpp:69-111 (the constructor calls) and :117-280
+ * (registration order, conduction, reactions, scriptable test materials). The ten
+ * random `Mat_i` materials (:171-239) are drawn with rand() at start-up and are
+ * never made interactive (:196,206); they are left out so that ids are
+ * reproducible: TEST_SAND/TEST_TEXTURED_SAND/TEST_LIQUID get ids 28-30. Texture
+ * colours (data/assets is absent from the reference tree) are replaced by the
+ * constant colours below. */
+void om_materials_reset_builtin(void) {
+    NMAT = 0;
+    NINTER = 0;
+    HAS_INTER = 0;
+    const uint32_t W = 0xffffffffu; /* Material default colour (game_datastruct.hpp:172-176) */
+    reg("GENERIC_AIR", T_AIR, 0, 255, 0, 0, 16, 0, W);
+    reg("GENERIC_SOLID", T_SOLID, 0, 255, 1, 0, 0, 0, W);
+    reg("GENERIC_SAND", T_SAND, 20, 255, 10, 2, 0, 0, W);
+    reg("GENERIC_LIQUID", T_SOUP, 0, 255, 1.5f, 3, 0, 0, W);
+    reg("GENERIC_GAS", T_GAS, 0, 255, -1, 1, 0, 0, W);
+    reg("GENERIC_PASSABLE", T_OBJECT, 0, 255, 0, 0, 0, 0, W);
+    reg("GENERIC_OBJECT", T_OBJECT, 0, 255, 1000.0f, 0, 0, 0, W);
+    reg("STONE", T_SOLID, 0, 255, 1, 0, 0, 0, W);
+    reg("GRASS", T_SAND, 20, 255, 12, 1, 0, 0, W);
+    reg("DIRT", T_SAND, 8, 255, 15, 1, 0, 0, W);
+    reg("SMOOTH_STONE", T_SOLID, 0, 255, 1, 0, 0, 0, W);
+    reg("COBBLE_STONE", T_SOLID, 0, 255, 1, 0, 0, 0, W);
+    reg("SMOOTH_DIRT", T_SOLID, 0, 255, 1, 0, 0, 0, W);
+    reg("COBBLE_DIRT", T_SOLID, 0, 255, 1, 0, 0, 0, W);
+    reg("SOFT_DIRT", T_SOLID, 0, 255, 15, 2, 0, 0, W);
+    reg("WATER", T_SOUP, 0, 0x80, 1.5f, 6, 40, 0x3000AFB5u, W);
+    reg("LAVA", T_SOUP, 0, 0xC0, 2, 1, 40, 0xFFFF6900u, W);
+    reg("CLOUD", T_SOLID, 0, 127, 1, 0, 0, 0, W);
+    reg("GOLD_ORE", T_SAND, 20, 255, 20, 2, 8, 0x804000u, W);
+    reg("GOLD_MOLTEN", T_SOUP, 0, 255, 20, 2, 8, 0x6FFF9B40u, W);
+    reg("GOLD_SOLID", T_SOLID, 0, 255, 20, 2, 8, 0, W);
+    reg("IRON_ORE", T_SAND, 20, 255, 20, 2, 8, 0x7F442Fu, W);
+    reg("OBSIDIAN", T_SOLID, 0, 255, 1, 0, 0, 0, W);
+    reg("STEAM", T_GAS, 0, 255, -1, 1, 0, 0, W);
+    reg("SOFT_DIRT_SAND", T_SAND, 8, 255, 15, 2, 0, 0, W);
+    reg("FIRE", T_OBJECT, 0, 255, 20, 1, 0, 0, W);
+    reg("FLAT_COBBLE_STONE", T_SOLID, 0, 255, 1, 0, 0, 0, W);
+    reg("FLAT_COBBLE_DIRT", T_SOLID, 0, 255, 1, 0, 0, 0, W);
+    reg("TEST_SAND", T_SAND, 20, 255, 10, 2, 0, 0, W);
+    reg("TEST_TEXTURED_SAND", T_SAND, 20, 255, 10, 2, 0, 0, W);
+    reg("TEST_LIQUID", T_SOUP, 0, 255, 1.5f, 4, 0, 0, W);
+    refresh_ids();
+
+    /* tile factories, game_datastruct.cpp:320-574 */
+    om_material_set_factory(om_material_find("TEST_SAND"), (220u << 16) | 100u, 8, 155, 30, 0); /* :320-325 */
+    om_material_set_factory(om_material_find("TEST_TEXTURED_SAND"), 0xDC9B64u, 0, 0, 0, 0);     /* texture */
+    om_material_set_factory(om_material_find("TEST_LIQUID"), 0x0000FFu, 0, 0, 0, Q_DEFAULT);     /* :337-342 */
+    om_material_set_factory(om_material_find("STONE"), 0x808080u, 0, 0, 0, 0);                  /* texture */
+    om_material_set_factory(om_material_find("GRASS"), (40u << 16) | 20u, 8, 120, 20, 0);        /* :358-363 */
+    om_material_set_factory(om_material_find("DIRT"), (40u << 8) | 20u, 16, 60, 10, 0);          /* :365-370 */
+    om_material_set_factory(om_material_find("SMOOTH_STONE"), 0x9A9A9Au, 0, 0, 0, 0);
+    om_material_set_factory(om_material_find("COBBLE_STONE"), 0x707070u, 0, 0, 0, 0);
+    om_material_set_factory(om_material_find("SMOOTH_DIRT"), 0x6B4A2Fu, 0, 0, 0, 0);
+    om_material_set_factory(om_material_find("COBBLE_DIRT"), 0x5A3D25u, 0, 0, 0, 0);
+    om_material_set_factory(om_material_find("SOFT_DIRT"), 0x7A5533u, 0, 0, 0, 0);
+    om_material_set_factory(om_material_find("WATER"), 0x00B69Fu, 0, 0, 0, Q_DEFAULT); /* :427-431 temp -1023 */
+    om_material_set_factory(om_material_find("LAVA"), 0xFF7C00u, 0, 0, 0, Q_DEFAULT);  /* :433-437 temp 1024 */
+    om_material_set_factory(om_material_find("CLOUD"), 0xE6E6F0u, 0, 0, 0, 0);
+    om_material_set_factory(om_material_find("GOLD_ORE"), 0xC8A032u, 0, 0, 0, 0);
+    om_material_set_factory(om_material_find("GOLD_MOLTEN"), 0xFFB43Cu, 0, 0, 0, Q_DEFAULT);
+    om_material_set_factory(om_material_find("GOLD_SOLID"), 0xE6C34Bu, 0, 0, 0, 0);
+    om_material_set_factory(om_material_find("IRON_ORE"), 0x8C6E5Au, 0, 0, 0, 0);
+    om_material_set_factory(om_material_find("OBSIDIAN"), 0x1E1428u, 0, 0, 0, 0);
+    om_material_set_factory(om_material_find("STEAM"), 0x666666u, 0, 0, 0, 0);                  /* :483 */
+    om_material_set_factory(om_material_find("FIRE"), (255u << 16) | 50u, 8, 100, 50, 0);       /* :485-492 */
+    om_material_set_factory(om_material_find("FLAT_COBBLE_STONE"), 0x787878u, 0, 0, 0, 0);
+    om_material_set_factory(om_material_find("FLAT_COBBLE_DIRT"), 0x624530u, 0, 0, 0, 0);
+    om_material_set_factory(ID_AIR, 0x000000u, 0, 0, 0, 0);   /* Tiles_NOTHING, :311 */
+    om_material_set_factory(ID_SOLID, 0xff0000u, 0, 0, 0, 0); /* Tiles_TEST_SOLID, :312 */
+
+    /* reactions, game_datastruct.cpp:246-260 */
+    om_material_set_reaction(ID_LAVA, REACT_BELOW, 512, ID_OBSIDIAN);
+    om_material_set_reaction(ID_WATER, REACT_ABOVE, 128, ID_STEAM);
+    om_material_set_reaction(om_material_find("GOLD_ORE"), REACT_ABOVE, 512, om_material_find("GOLD_MOLTEN"));
+    om_material_set_reaction(om_material_find("GOLD_MOLTEN"), REACT_BELOW, 128, om_material_find("GOLD_SOLID"));
+}
+
+/* RegisterMaterial, game_datastruct.cpp:282-289 */
+int om_material_register(int s_id, const char *name, const char *index_name, int physics_type, int slipperyness,
+                         int alpha, float density, int iterations, int emit, uint32_t emit_colour, uint32_t colour) {
+    (void)s_id;
+    (void)name;
+    if (physics_type < 0 || physics_type > 5) return -1;
+    int id = reg(index_name, physics_type, slipperyness, alpha, density, iterations, emit, emit_colour, colour);
+    refresh_ids();
+    return id;
+}
+
+int om_material_set_reaction(int mat, int kind, int temperature, int result) {
+    if (mat < 0 || mat >= NMAT || result < 0 || result >= NMAT) return -1;
+    if (kind != REACT_BELOW && kind != REACT_ABOVE) return -1;
+    mat_t *m = &M[mat];
+    if (m->n_react >= 4) return -1;
+    m->react[m->n_react].kind = kind;
+    m->react[m->n_react].data1 = temperature;
+    m->react[m->n_react].data2 = result;
+    m->n_react++;
+    return 0;
+}
+
+int om_material_set_interaction(int mat, int other, int kind, int data1, int data2, int ofs_x, int ofs_y) {
+    if (mat < 0 || mat >= NMAT || other < 0 || other >= NMAT || data1 < 0 || data1 >= NMAT) return -1;
+    if (kind != INTER_TRANSFORM && kind != INTER_SPAWN) return -1;
+    if (data2 < 0 || abs(ofs_x) + data2 > 5 || abs(ofs_y) + data2 > 5) return -1;
+    int li = -1;
+    for (int i = 0; i < NINTER; i++)
+        if (INTER[i].mat == mat && INTER[i].other == other) li = i;
+    if (li < 0) {
+        if (NINTER >= 512) return -1;
+        li = NINTER++;
+        INTER[li].mat = mat;
+        INTER[li].other = other;
+        INTER[li].n = 0;
+    }
+    if (INTER[li].n >= 4) return -1;
+    inter_t *e = &INTER[li].e[INTER[li].n++];
+    e->kind = kind;
+    e->data1 = data1;
+    e->data2 = data2;
+    e->ofsx = ofs_x;
+    e->ofsy = ofs_y;
+    M[mat].interact = 1;
+    HAS_INTER = 1;
+    return 0;
+}
+
+static const inter_list_t *find_inter(int mat, int other) {
+    for (int i = 0; i < NINTER; i++)
+        if (INTER[i].mat == mat && INTER[i].other == other) return &INTER[i];
+    return NULL;
+}
+
+int om_material_count(void) { return NMAT; }
+
+void om_material_get(int id, int32_t out[16]) {
+    const mat_t *m = &M[id];
+    int32_t dbits;
+    memcpy(&dbits, &m->density, 4);
+    out[0] = m->type;
+    out[1] = dbits;
+    out[2] = m->iterations;
+    out[3] = m->slip;
+    out[4] = m->max_stab;
+    out[5] = m->alpha;
+    out[6] = (int32_t)m->colour;
+    out[7] = m->emit;
+    out[8] = (int32_t)m->emit_colour;
+    out[9] = (int32_t)m->f_base;
+    out[10] = m->f_shift;
+    out[11] = m->f_lo;
+    out[12] = m->f_mod;
+    out[13] = m->f_scalar;
+    out[14] = m->n_react;
+    out[15] = m->interact;
+}
+
+/* --------------------------------------------------------------------- world */
+typedef struct {
+    uint16_t id;
+    uint8_t fl;
+    int32_t sc;
+    uint32_t col;
+    int32_t df;
+} cell_t;
+
+typedef struct {
+    om_particle *p;
+    int n, cap;
+} pvec;
+
+static void pv_push(pvec *v, const om_particle *p) {
+    if (v->n == v->cap) {
+        v->cap = v->cap ? v->cap * 2 : 64;
+        v->p = (om_particle *)realloc(v->p, (size_t)v->cap * sizeof(om_particle));
+    }
+    v->p[v->n++] = *p;
+}
+
+#define LED_CN 0
+#define LED_DN 1
+#define LED_XN 2
+#define LED_CF 3
+#define LED_DF 4
+#define LED_XF 5
+
+struct om_world {
+    int W, H, C, cell_iter;
+    uint32_t seed, tick;
+    uint16_t *id;
+    uint32_t *col;
+    int32_t *sc;
+    uint8_t *fl;
+    int32_t *df;
+    uint8_t *vis;
+    pvec parts;
+    int64_t led[6][MAXMAT];
+    /* race checker */
+    int check;
+    long viol;
+    int32_t stamp;
+    int32_t *wst, *wown, *rst, *rown;
+};
+
+static inline int inw(const om_world *w, int x, int y) { return x >= 0 && y >= 0 && x < w->W && y < w->H; }
+
+om_world *om_world_new(int w, int h, int chunk, int cell_iter, uint32_t seed) {
+    if (w <= 0 || h <= 0 || chunk < 16 || cell_iter < 0) return NULL;
+    om_world *wd = (om_world *)calloc(1, sizeof(om_world));
+    size_t n = (size_t)w * h;
+    wd->W = w;
+    wd->H = h;
+    wd->C = chunk;
+    wd->cell_iter = cell_iter;
+    wd->seed = seed;
+    wd->id = (uint16_t *)calloc(n, 2);
+    wd->col = (uint32_t *)calloc(n, 4);
+    wd->sc = (int32_t *)calloc(n, 4);
+    wd->fl = (uint8_t *)calloc(n, 1);
+    wd->df = (int32_t *)calloc(n, 4);
+    wd->vis = (uint8_t *)calloc(n, 1);
+    for (size_t i = 0; i < n; i++) wd->id[i] = (uint16_t)ID_AIR;
+    return wd;
+}
+
+void om_world_free(om_world *wd) {
+    if (!wd) return;
+    free(wd->id);
+    free(wd->col);
+    free(wd->sc);
+    free(wd->fl);
+    free(wd->df);
+    free(wd->vis);
+    free(wd->parts.p);
+    free(wd->wst);
+    free(wd->wown);
+    free(wd->rst);
+    free(wd->rown);
+    free(wd);
+}
+
+void om_world_set(om_world *wd, const uint16_t *id, const uint32_t *col, const int32_t *sc, const uint8_t *fl,
+                  const int32_t *df) {
+    size_t n = (size_t)wd->W * wd->H;
+    memcpy(wd->id, id, n * 2);
+    memcpy(wd->col, col, n * 4);
+    memcpy(wd->sc, sc, n * 4);
+    memcpy(wd->fl, fl, n);
+    memcpy(wd->df, df, n * 4);
+}
+
+void om_world_get(const om_world *wd, uint16_t *id, uint32_t *col, int32_t *sc, uint8_t *fl, int32_t *df) {
+    size_t n = (size_t)wd->W * wd->H;
+    memcpy(id, wd->id, n * 2);
+    memcpy(col, wd->col, n * 4);
+    memcpy(sc, wd->sc, n * 4);
+    memcpy(fl, wd->fl, n);
+    memcpy(df, wd->df, n * 4);
+}
+
+void om_world_set_tick(om_world *wd, uint32_t t) { wd->tick = t; }
+uint32_t om_world_get_tick(const om_world *wd) { return wd->tick; }
+
+/* ----------------------------------------------------------- race checker */
+static void chk_init(om_world *w) {
+    size_t n = (size_t)w->W * w->H;
+    if (!w->wst) {
+        w->wst = (int32_t *)calloc(n, 4);
+        w->wown = (int32_t *)calloc(n, 4);
+        w->rst = (int32_t *)calloc(n, 4);
+        w->rown = (int32_t *)calloc(n, 4);
+    }
+}
+static int32_t g_owner; /* linear index of the active cell (checker runs single-threaded) */
+static inline void chk(om_world *w, int x, int y, int write) {
+    if (!w->check || !inw(w, x, y)) return;
+    size_t i = (size_t)y * w->W + x;
+    int32_t s = w->stamp, o = g_owner;
+    if (w->wst[i] == s && w->wown[i] != o) w->viol++;
+    if (write) {
+        if (w->rst[i] == s && w->rown[i] != o) w->viol++;
+        w->wst[i] = s;
+        w->wown[i] = o;
+    } else {
+        if (w->rst[i] == s) {
+            if (w->rown[i] != o) w->rown[i] = -2;
+        } else {
+            w->rst[i] = s;
+            w->rown[i] = o;
+        }
+    }
+}
+
+/* ------------------------------------------------------- cell accessors */
+/* getTile/setTile bounds policy, world.cpp:999-1008, applied to every access */
+static inline int gid(om_world *w, int x, int y) {
+    chk(w, x, y, 0);
+    return inw(w, x, y) ? w->id[(size_t)y * w->W + x] : ID_SOLID;
+}
+static inline int gtype(om_world *w, int x, int y) { return M[gid(w, x, y)].type; }
+static inline cell_t gcell(om_world *w, int x, int y) {
+    cell_t c;
+    chk(w, x, y, 0);
+    if (!inw(w, x, y)) {
+        c.id = (uint16_t)ID_SOLID;
+        c.fl = 0;
+        c.sc = 0;
+        c.col = 0xff0000u;
+        c.df = 0;
+        return c;
+    }
+    size_t i = (size_t)y * w->W + x;
+    c.id = w->id[i];
+    c.fl = w->fl[i];
+    c.sc = w->sc[i];
+    c.col = w->col[i];
+    c.df = (M[c.id].type == T_SOUP) ? w->df[i] : 0;
+    return c;
+}
+static inline void pcell(om_world *w, int x, int y, cell_t c) {
+    chk(w, x, y, 1);
+    if (!inw(w, x, y)) return;
+    size_t i = (size_t)y * w->W + x;
+    w->id[i] = c.id;
+    w->fl[i] = c.fl;
+    w->sc[i] = c.sc;
+    w->col[i] = c.col;
+    w->df[i] = (M[c.id].type == T_SOUP) ? c.df : 0;
+}
+static inline void set_moved(om_world *w, int x, int y, int on) {
+    chk(w, x, y, 1);
+    if (!inw(w, x, y)) return;
+    size_t i = (size_t)y * w->W + x;
+    if (on)
+        w->fl[i] |= MOVED;
+    else
+        w->fl[i] &= (uint8_t)~MOVED;
+}
+static inline void add_diff(om_world *w, int x, int y, int32_t v) {
+    chk(w, x, y, 1);
+    if (!inw(w, x, y)) return;
+    w->df[(size_t)y * w->W + x] += v;
+}
+static inline int getvis(om_world *w, int x, int y) {
+    chk(w, x, y, 0);
+    return inw(w, x, y) ? w->vis[(size_t)y * w->W + x] : 0;
+}
+static inline void setvis(om_world *w, int x, int y) {
+    chk(w, x, y, 1);
+    if (inw(w, x, y)) w->vis[(size_t)y * w->W + x] = 1;
+}
+
+static inline cell_t nothing(void) {
+    cell_t c = {(uint16_t)ID_AIR, 0, 0, 0u, 0};
+    return c;
+}
+
+/* ------------------------------------------------------------ rule context */
+typedef struct {
+    om_world *w;
+    uint32_t pk; /* pass key for (tick, iter, sweep) */
+    uint32_t ck; /* cell key */
+    uint32_t k;  /* draw counter */
+    int iter;
+    pvec *spawn; /* particles spawned by this chunk-pass, in order */
+    int64_t (*led)[MAXMAT];
+} rctx;
+
+static inline uint32_t D(rctx *c) { return draw_k(c->ck, c->k++); }
+
+static inline void led_add(rctx *c, int row, int mat, int64_t v) {
+    if (mat < 0 || M[mat].type == T_AIR || v == 0) return;
+#pragma omp atomic
+    c->led[row][mat] += v;
+}
+
+/* account a cell replaced by a conversion (not a move) */
+static void led_replace(rctx *c, cell_t old, cell_t nw) {
+    led_add(c, LED_DN, old.id, 1);
+    if (M[old.id].type == T_SOUP) led_add(c, LED_DF, old.id, (int64_t)old.sc + old.df);
+    led_add(c, LED_CN, nw.id, 1);
+    if (M[nw.id].type == T_SOUP) led_add(c, LED_CF, nw.id, (int64_t)nw.sc + nw.df);
+}
+
+/* TilesCreate(id, x, y), game_datastruct.cpp:494-574: colour from the factory
+ * (one draw when the factory jitters a channel), scalar = temperature or, for
+ * SOUP materials, the default amount */
+static cell_t create_tile(rctx *c, int mid) {
+    const mat_t *m = &M[mid];
+    cell_t t;
+    t.id = (uint16_t)mid;
+    t.fl = 0;
+    t.df = 0;
+    t.sc = m->f_scalar;
+    t.col = m->f_base;
+    if (m->f_mod > 0) t.col = m->f_base + ((uint32_t)(m->f_lo + (int)(D(c) % (uint32_t)m->f_mod)) << m->f_shift);
+    return t;
+}
+
+static void spawn(rctx *c, cell_t tile, int x, int y, float vx, float vy, float ax, float ay, int temporary,
+                  int lifetime, int fade) {
+    /* CellData(tile, x, y, vx, vy, ax, ay), source/engine/game_utils/cells.h:15-35 */
+    om_particle p;
+    memset(&p, 0, sizeof(p));
+    p.x = (float)x;
+    p.y = (float)y;
+    p.vx = vx;
+    p.vy = vy;
+    p.ax = ax;
+    p.ay = ay;
+    p.lifetime = lifetime;
+    p.fade_time = fade;
+    p.colour = tile.col;
+    p.scalar = tile.sc;
+    p.id = tile.id;
+    p.flags = tile.fl;
+    p.bits = (uint8_t)(temporary ? 2 : 0);
+    pv_push(c->spawn, &p);
+}
+
+/* CalculateVerticalFlowValue, world.cpp:1021-1034, in Q16.16 */
+static inline int32_t vflow(int32_t rem, int32_t dst) {
+    int64_t sum = (int64_t)rem + dst;
+    if (sum <= Q_MAXV) return Q_MAXV;
+    if (sum < 2 * Q_MAXV + Q_MAXCOMP)
+        return (int32_t)(((int64_t)Q_MAXV * Q_MAXV + sum * Q_MAXCOMP) / (Q_MAXV + Q_MAXCOMP));
+    return (int32_t)((sum + Q_MAXCOMP) / 2);
+}
+static inline int32_t clampflow(int32_t flow, int32_t rem) {
+    /* world.cpp:1320-1321 and the three copies below it */
+    if (flow < 0) flow = 0;
+    int32_t lim = rem < Q_MAXFLOW ? rem : Q_MAXFLOW;
+    if (flow > lim) flow = lim;
+    return flow;
+}
+
+/* ---------------------------------------------------------------- sweep A */
+static void rule_a(rctx *c, int x, int y) {
+    om_world *w = c->w;
+    if (getvis(w, x, y)) return; /* world.cpp:1091 */
+    cell_t t = gcell(w, x, y);
+    const mat_t *m = &M[t.id];
+    if (c->iter >= m->iterations) { /* world.cpp:1093-1096 */
+        setvis(w, x, y);
+        return;
+    }
+    int type = m->type;
+    c->ck = cell_key(c->pk, (uint32_t)x, (uint32_t)y);
+    c->k = 0;
+
+    if ((int)t.id == ID_FIRE) { /* world.cpp:1101-1146 */
+        if (D(c) % 10 == 0) t.col = (255u << 16) | ((uint32_t)(100 + (int)(D(c) % 50)) << 8) | 50u;
+        if (D(c) % 10 == 0) {
+            float vx = (float)((int)(D(c) % 10) - 5) / 20.0f;
+            float vy = -((float)(int)(D(c) % 10) / 10.0f) / 3.0f + -0.5f;
+            spawn(c, t, x, y - 1, vx, vy, 0.0f, 0.01f, 1, 30, 10);
+            led_add(c, LED_CN, t.id, 1);
+        }
+        if (D(c) % 150 == 0) {
+            led_replace(c, t, nothing());
+            pcell(w, x, y, nothing());
+            setvis(w, x, y);
+        } else {
+            int found = 0;
+            for (int xx = -2; xx <= 2; xx++)
+                for (int yy = -2; yy <= 2; yy++) {
+                    if (gtype(w, x + xx, y + yy) == T_SOLID) {
+                        found = 1;
+                        if (D(c) % 500 == 0) {
+                            cell_t f = create_tile(c, ID_FIRE);
+                            if (inw(w, x + xx, y + yy)) led_replace(c, gcell(w, x + xx, y + yy), f);
+                            pcell(w, x + xx, y + yy, f);
+                            setvis(w, x + xx, y + yy);
+                        }
+                    }
+                }
+            if (!found && D(c) % 120 == 0) {
+                led_replace(c, gcell(w, x, y), nothing());
+                pcell(w, x, y, nothing());
+                setvis(w, x, y);
+            }
+        }
+    }
+
+    if (type == T_SAND) {
+        cell_t below = gcell(w, x, y + 1); /* world.cpp:1150 */
+        int bt = M[below.id].type;
+        const inter_list_t *il = m->interact ? find_inter(t.id, below.id) : NULL;
+        if (il && il->n > 0) { /* world.cpp:1153-1179 (signed offsets) */
+            for (int i = 0; i < il->n; i++) {
+                const inter_t *in = &il->e[i];
+                for (int xx = in->ofsx - in->data2; xx <= in->ofsx + in->data2; xx++)
+                    for (int yy = in->ofsy - in->data2; yy <= in->ofsy + in->data2; yy++) {
+                        if (in->kind == INTER_TRANSFORM) {
+                            if (gid(w, x + xx, y + yy) == below.id) {
+                                cell_t nt = create_tile(c, in->data1);
+                                if (inw(w, x + xx, y + yy)) led_replace(c, gcell(w, x + xx, y + yy), nt);
+                                pcell(w, x + xx, y + yy, nt);
+                                setvis(w, x + xx, y + yy);
+                            }
+                        } else {
+                            if ((xx == 0 && yy == 0) || gid(w, x + xx, y + yy) == ID_AIR) {
+                                cell_t nt = create_tile(c, in->data1);
+                                if (inw(w, x + xx, y + yy)) led_replace(c, gcell(w, x + xx, y + yy), nt);
+                                pcell(w, x + xx, y + yy, nt);
+                                setvis(w, x + xx, y + yy);
+                            }
+                        }
+                    }
+            }
+            return;
+        }
+        if (m->n_react > 0) { /* world.cpp:1181-1204 */
+            int react = 0;
+            for (int i = 0; i < m->n_react; i++) {
+                const inter_t *r = &m->react[i];
+                int hit = (r->kind == REACT_BELOW) ? (t.sc < r->data1) : (t.sc > r->data1);
+                if (hit) {
+                    cell_t nt = create_tile(c, r->data2);
+                    if (M[nt.id].type != T_SOUP) nt.sc = t.sc; /* keeps the temperature */
+                    led_replace(c, gcell(w, x, y), nt);
+                    pcell(w, x, y, nt);
+                    setvis(w, x, y);
+                    react = 1;
+                }
+            }
+            if (react) return;
+        }
+        /* world.cpp:1206-1267 */
+        int canB = (bt == T_AIR || (bt != T_SOLID && M[below.id].density < m->density));
+        if (!canB) return;
+        cell_t bl = gcell(w, x - 1, y + 1), br = gcell(w, x + 1, y + 1);
+        int blt = M[bl.id].type, brt = M[br.id].type;
+        int canL = (blt == T_AIR || (blt != T_SOLID && M[bl.id].density < m->density));
+        int canR = (brt == T_AIR || (brt != T_SOLID && M[br.id].density < m->density));
+        if (!((canL || canR) && D(c) % 20 == 0)) {
+            if (bt == T_AIR && gtype(w, x, y + 2) == T_AIR && gtype(w, x, y + 3) == T_AIR &&
+                gtype(w, x, y + 4) == T_AIR) {
+                pcell(w, x, y, below);
+                float vx = (float)((int)(D(c) % 10) - 5) / 20.0f;
+                float vy = (float)(-((int)(D(c) % 2) + 3)) / 10.0f + 1.5f;
+                spawn(c, t, x, y + 1, vx, vy, 0.0f, 0.1f, 0, 0, 60);
+            } else {
+                pcell(w, x, y, below);
+                if (D(c) % 2 == 0) t.fl |= MOVED;
+                pcell(w, x, y + 1, t);
+                setvis(w, x, y + 1);
+            }
+            if (D(c) % 2 == 0) {
+                if (x > 0 && gtype(w, x - 1, y + 1) == T_SAND) {
+                    if (D(c) % 2 == 0) set_moved(w, x - 1, y + 1, 1);
+                }
+                if (x < w->W - 1 && gtype(w, x + 1, y + 1) == T_SAND) {
+                    if (D(c) % 2 == 0) set_moved(w, x + 1, y + 1, 1);
+                }
+            }
+        }
+    } else if (type == T_SOUP) { /* world.cpp:1269-1567 */
+        if (t.sc == 0) return;
+        if (t.sc < Q_MINV) {
+            led_add(c, LED_DF, t.id, t.sc);
+            t.sc = 0;
+            pcell(w, x, y, t);
+            return;
+        }
+        if (t.sc > Q_FREEFALL && gtype(w, x, y + 1) == T_AIR && gtype(w, x, y + 2) == T_AIR &&
+            gtype(w, x, y + 3) == T_AIR && gtype(w, x, y + 4) == T_AIR) { /* world.cpp:1283-1305 */
+            pcell(w, x, y, nothing());
+            int n = t.sc >> 18; /* int(amount / 4) */
+            if (n < 1) n = 1;
+            int32_t base = t.sc / n, extra = t.sc % n;
+            led_add(c, LED_DF, t.id, t.df); /* the pending diff of the cell is dropped */
+            led_add(c, LED_CN, t.id, n - 1);
+            for (int i = 0; i < n; i++) {
+                cell_t nt = t;
+                nt.sc = base + (i < extra ? 1 : 0);
+                nt.df = 0;
+                nt.fl = 0;
+                float vx = (float)((int)(D(c) % 10) - 5) / 30.0f;
+                float vy = (float)(-((int)(D(c) % 2) + 3)) / 10.0f + 1.0f;
+                spawn(c, nt, x, y + 1, vx, vy, 0.0f, 0.1f, 0, 0, 60);
+            }
+            return;
+        }
+        if (t.fl & MOVED) return;
+        int32_t start = t.sc, rem = t.sc;
+        cell_t bottom = gcell(w, x, y + 1);
+        int bT = M[bottom.id].type;
+        int airBelow = bT == T_AIR;
+        if ((airBelow && c->iter <= 2) || bottom.id == t.id) {
+            int32_t dst = (bT == T_SOUP) ? bottom.sc : 0;
+            int32_t flow = clampflow(vflow(start, dst) - dst, start);
+            if (flow != 0) {
+                rem -= flow;
+                t.df -= flow;
+                if (bT == T_AIR) {
+                    cell_t nt = {t.id, 0, 0, t.col, flow};
+                    pcell(w, x, y + 1, nt);
+                    led_add(c, LED_CN, t.id, 1);
+                } else
+                    add_diff(w, x, y + 1, flow);
+            }
+        } else if (c->iter == 0 && bT == T_SOUP && bottom.id != t.id) {
+            if (D(c) % 10 == 0) {
+                pcell(w, x, y, bottom);
+                pcell(w, x, y + 1, t);
+                return;
+            }
+        }
+        if (rem < Q_MINV) {
+            t.df -= rem;
+            led_add(c, LED_DF, t.id, rem);
+            pcell(w, x, y, t);
+            return;
+        }
+        cell_t left = gcell(w, x - 1, y);
+        int lT = M[left.id].type;
+        int canL = (lT == T_AIR || left.id == t.id) && !airBelow;
+        cell_t right = gcell(w, x + 1, y);
+        int rT = M[right.id].type;
+        int canR = (rT == T_AIR || right.id == t.id) && !airBelow;
+        if (canL) {
+            int32_t dst = (lT == T_SOUP) ? left.sc : 0;
+            int32_t flow = clampflow((rem - dst) / (canR ? 3 : 2), rem);
+            if (flow != 0) {
+                rem -= flow;
+                t.df -= flow;
+                if (lT == T_AIR) {
+                    cell_t nt = {t.id, 0, 0, t.col, flow};
+                    pcell(w, x - 1, y, nt);
+                    led_add(c, LED_CN, t.id, 1);
+                } else
+                    add_diff(w, x - 1, y, flow);
+            }
+        }
+        if (rem < Q_MINV) {
+            t.df -= rem;
+            led_add(c, LED_DF, t.id, rem);
+            pcell(w, x, y, t);
+            return;
+        }
+        if (canR) {
+            int32_t dst = (rT == T_SOUP) ? right.sc : 0;
+            int32_t flow = clampflow((rem - dst) / 2, rem);
+            if (flow != 0) {
+                rem -= flow;
+                t.df -= flow;
+                if (rT == T_AIR) {
+                    cell_t nt = {t.id, 0, 0, t.col, flow};
+                    pcell(w, x + 1, y, nt);
+                    led_add(c, LED_CN, t.id, 1);
+                } else
+                    add_diff(w, x + 1, y, flow);
+            }
+        }
+        if (rem < Q_MINV) {
+            t.df -= rem;
+            led_add(c, LED_DF, t.id, rem);
+            pcell(w, x, y, t);
+            return;
+        }
+        cell_t top = gcell(w, x, y - 1);
+        int tT = M[top.id].type;
+        if (tT == T_AIR || top.id == t.id) {
+            int32_t dst = (tT == T_SOUP) ? top.sc : 0;
+            int32_t flow = clampflow(rem - vflow(rem, dst), rem);
+            if (flow != 0) {
+                rem -= flow;
+                t.df -= flow;
+                if (tT == T_AIR) {
+                    cell_t nt = {t.id, 0, 0, t.col, flow};
+                    pcell(w, x, y - 1, nt);
+                    led_add(c, LED_CN, t.id, 1);
+                } else
+                    add_diff(w, x, y - 1, flow);
+            }
+        } else if (c->iter == 0 && tT == T_SOUP && top.id != t.id) {
+            if (D(c) % 10 == 0) {
+                pcell(w, x, y, top);
+                pcell(w, x, y - 1, t);
+                return;
+            }
+        }
+        if (rem < Q_MINV) {
+            t.df -= rem;
+            led_add(c, LED_DF, t.id, rem);
+            pcell(w, x, y, t);
+            return;
+        }
+        if (start == rem) { /* world.cpp:1472-1483 */
+            uint8_t s = t.fl & SETTLE_MASK;
+            if (s < SETTLE_MASK) s++;
+            t.fl = (uint8_t)((t.fl & ~SETTLE_MASK) | s);
+            if (s >= 10) t.fl |= MOVED;
+        } else {
+            if (tT == T_SOUP) set_moved(w, x, y - 1, 0);
+            if (bT == T_SOUP) set_moved(w, x, y + 1, 0);
+            if (lT == T_SOUP) set_moved(w, x - 1, y, 0);
+            if (rT == T_SOUP) set_moved(w, x + 1, y, 0);
+        }
+        pcell(w, x, y, t);
+        /* WATER on LAVA, world.cpp:1519-1537 */
+        if ((int)t.id == ID_WATER && gid(w, x, y + 1) == ID_LAVA) {
+            cell_t st = create_tile(c, ID_STEAM);
+            led_replace(c, t, st);
+            pcell(w, x, y, st);
+            cell_t ob = create_tile(c, ID_OBSIDIAN);
+            led_replace(c, gcell(w, x, y + 1), ob);
+            pcell(w, x, y + 1, ob);
+            setvis(w, x, y + 1);
+            for (int xx = -1; xx <= 1; xx++)
+                for (int yy = 0; yy <= 2; yy++) {
+                    if (gid(w, x + xx, y + yy) == ID_LAVA) {
+                        cell_t o2 = create_tile(c, ID_OBSIDIAN);
+                        led_replace(c, gcell(w, x + xx, y + yy), o2);
+                        pcell(w, x + xx, y + yy, o2);
+                        setvis(w, x + xx, y + yy);
+                    }
+                }
+            return;
+        }
+    } else if (type == T_GAS) { /* world.cpp:1569-1585 */
+        int above = gtype(w, x, y - 1);
+        int aboveL = gtype(w, x - 1, y - 1);
+        int aboveR = gtype(w, x + 1, y - 1);
+        if (above == T_AIR && !((aboveL == T_AIR || aboveR == T_AIR) && D(c) % 2 == 0)) {
+            pcell(w, x, y, gcell(w, x, y - 1));
+            pcell(w, x, y - 1, t);
+            setvis(w, x, y - 1);
+        }
+    }
+}
+
+/* ---------------------------------------------------------------- sweep B */
+static void rule_b(rctx *c, int x, int y) {
+    om_world *w = c->w;
+    if (getvis(w, x, y)) return; /* world.cpp:1597 */
+    cell_t t = gcell(w, x, y);
+    const mat_t *m = &M[t.id];
+    int type = m->type;
+    if (type != T_SAND && type != T_SOUP && type != T_GAS) return;
+    c->ck = cell_key(c->pk, (uint32_t)x, (uint32_t)y);
+    c->k = 0;
+    if (type == T_SAND) { /* world.cpp:1602-1727 */
+        cell_t bl = gcell(w, x - 1, y + 1), br = gcell(w, x + 1, y + 1);
+        int blt = M[bl.id].type, brt = M[br.id].type;
+        int canL = (blt == T_AIR || (blt != T_SOLID && M[bl.id].density < m->density));
+        int canR = (brt == T_AIR || (brt != T_SOLID && M[br.id].density < m->density));
+        int stopped = !(t.fl & MOVED);
+        int slip = m->slip;
+        if (stopped) {
+            int drop = 0;
+            for (int pil = 0; pil < 10; pil++) {
+                int l = gtype(w, x - 1, y + 1 + pil);
+                int r = gtype(w, x + 1, y + 1 + pil);
+                if (l == T_AIR || r == T_AIR) drop++;
+            }
+            int d = drop + 1 - m->max_stab;
+            if (d > 0) {
+                int chance = 1000 / d;
+                if (chance < 1000) {
+                    if (D(c) % (uint32_t)chance == 0) {
+                        stopped = 0;
+                        set_moved(w, x, y, 1);
+                    }
+                }
+            }
+        }
+        if (stopped || !(canL || canR)) {
+            set_moved(w, x, y, 0);
+            return;
+        }
+        int shouldMove = (slip > 0) ? (D(c) % (uint32_t)(2 * slip) != 0) : 1;
+        if (shouldMove && (canL || canR)) {
+            if (D(c) % 2 == 0) {
+                if (gtype(w, x, y + 1) == T_SAND) {
+                    if (D(c) % 2 == 0) set_moved(w, x, y + 1, 1);
+                }
+            }
+        }
+        if (shouldMove && canL && (!canR || D(c) % 2 == 0)) {
+            if (gtype(w, x - 1, y) == T_AIR) {
+                pcell(w, x - 1, y, bl);
+                setvis(w, x - 1, y);
+                pcell(w, x, y, nothing());
+            } else {
+                pcell(w, x, y, bl);
+                setvis(w, x, y);
+            }
+            if (slip > 0 && D(c) % (uint32_t)(20 * slip) == 0) t.fl &= (uint8_t)~MOVED;
+            pcell(w, x - 1, y + 1, t);
+            setvis(w, x - 1, y + 1);
+        } else if (shouldMove && canR) {
+            if (gtype(w, x + 1, y) == T_AIR) {
+                pcell(w, x + 1, y, br);
+                pcell(w, x, y, nothing());
+            } else {
+                pcell(w, x, y, br);
+                setvis(w, x, y);
+            }
+            if (slip > 0 && D(c) % (uint32_t)(20 * slip) == 0) t.fl &= (uint8_t)~MOVED;
+            pcell(w, x + 1, y + 1, t);
+            setvis(w, x + 1, y + 1);
+        } else {
+            set_moved(w, x, y, 0);
+        }
+    } else if (type == T_SOUP) { /* world.cpp:1728-1745 */
+        t.sc += t.df;
+        t.df = 0;
+        if (t.sc < Q_MINV) {
+            led_add(c, LED_DN, t.id, 1);
+            led_add(c, LED_DF, t.id, t.sc);
+            pcell(w, x, y, nothing());
+            setvis(w, x, y);
+        } else {
+            pcell(w, x, y, t);
+            setvis(w, x, y);
+        }
+    } else { /* GAS, world.cpp:1799-1818 */
+        int aboveL = gtype(w, x - 1, y - 1);
+        int aboveR = gtype(w, x + 1, y - 1);
+        if (aboveL == T_AIR && !(aboveR == T_AIR && D(c) % 2 == 0)) {
+            pcell(w, x, y, gcell(w, x - 1, y - 1));
+            pcell(w, x - 1, y - 1, t);
+            setvis(w, x - 1, y - 1);
+        } else if (aboveR == T_AIR) {
+            pcell(w, x, y, gcell(w, x + 1, y - 1));
+            pcell(w, x + 1, y - 1, t);
+            setvis(w, x + 1, y - 1);
+        }
+    }
+}
+
+/* ---------------------------------------------------------------- sweep C */
+static void rule_c(rctx *c, int x, int y) {
+    om_world *w = c->w;
+    if (getvis(w, x, y)) return; /* world.cpp:1831 */
+    cell_t t = gcell(w, x, y);
+    if (M[t.id].type != T_GAS) return;
+    c->ck = cell_key(c->pk, (uint32_t)x, (uint32_t)y);
+    c->k = 0;
+    /* world.cpp:1862-1889 */
+    int l = gtype(w, x - 1, y);
+    int r = gtype(w, x + 1, y);
+    if (l == T_AIR && !(r == T_AIR && D(c) % 2 == 0)) {
+        pcell(w, x, y, gcell(w, x - 1, y));
+        pcell(w, x - 1, y, t);
+        setvis(w, x - 1, y);
+    } else if (r == T_AIR) {
+        pcell(w, x, y, gcell(w, x + 1, y));
+        pcell(w, x + 1, y, t);
+        setvis(w, x + 1, y);
+    } else if ((int)t.id == ID_STEAM) {
+        if (D(c) % 10 == 0) {
+            cell_t wt = create_tile(c, ID_WATER);
+            led_replace(c, t, wt);
+            pcell(w, x, y, wt);
+        }
+    }
+}
+
+/* ------------------------------------------------------------ lattices */
+/* Sub-phase lattice (Px, Py) per sweep and chunk mode: two cells of one sub-phase
+ * differ by a multiple of Px in x or (same column) of Py in y, which keeps every
+ * cell's write set disjoint from every other cell's read and write sets. */
+enum { MODE_NARROW = 0, MODE_FIRE = 1, MODE_INTER = 2 };
+static int DBG_PX[3] = {0, 0, 0}, DBG_PY[3] = {0, 0, 0};
+/* test hook: force a lattice for one sweep (0 restores the derived one), so a test
+ * can plant a too-small spacing and see the race checker fire */
+void om_debug_set_lattice(int sweep, int px, int py) {
+    if (sweep < 0 || sweep > 2) return;
+    DBG_PX[sweep] = px;
+    DBG_PY[sweep] = py;
+}
+static void lattice(int sweep, int mode, int *px, int *py) {
+    if (DBG_PX[sweep] > 0) {
+        *px = DBG_PX[sweep];
+        *py = DBG_PY[sweep];
+        return;
+    }
+    if (sweep == 0) {
+        if (mode == MODE_INTER) {
+            *px = 11;
+            *py = 11;
+        } else if (mode == MODE_FIRE) {
+            *px = 5;
+            *py = 7;
+        } else {
+            *px = 3;
+            *py = 6;
+        }
+    } else if (sweep == 1) {
+        *px = 3;
+        *py = 12;
+    } else {
+        *px = 3;
+        *py = 1;
+    }
+}
+
+static int chunk_mode(const om_world *w, int cx, int cy) {
+    if (HAS_INTER) return MODE_INTER;
+    if (ID_FIRE < 0) return MODE_NARROW;
+    int x1 = cx + w->C < w->W ? cx + w->C : w->W, y1 = cy + w->C < w->H ? cy + w->C : w->H;
+    for (int y = cy; y < y1; y++)
+        for (int x = cx; x < x1; x++)
+            if (w->id[(size_t)y * w->W + x] == (uint16_t)ID_FIRE) return MODE_FIRE;
+    return MODE_NARROW;
+}
+
+typedef void (*rule_fn)(rctx *, int, int);
+
+static void process_chunk(om_world *w, int order, int iter, int cx, int cy, pvec *spawn) {
+    rctx c;
+    memset(&c, 0, sizeof(c));
+    c.w = w;
+    c.iter = iter;
+    c.spawn = spawn;
+    c.led = w->led;
+    int x1 = cx + w->C < w->W ? cx + w->C : w->W, y1 = cy + w->C < w->H ? cy + w->C : w->H;
+    rule_fn rules[3] = {rule_a, rule_b, rule_c};
+    int mode = (order == OM_ORDER_PART) ? chunk_mode(w, cx, cy) : MODE_NARROW;
+    for (int sweep = 0; sweep < 3; sweep++) {
+        c.pk = pass_key(w->seed, w->tick, (uint32_t)(iter * 3 + sweep));
+        if (order == OM_ORDER_SEQ) {
+            /* world.cpp:1084-1087 (and 1589, 1823): bottom-to-top, left-to-right */
+            for (int y = y1 - 1; y >= cy; y--)
+                for (int x = cx; x < x1; x++) rules[sweep](&c, x, y);
+        } else {
+            int px, py;
+            lattice(sweep, mode, &px, &py);
+            for (int ry = py - 1; ry >= 0; ry--)
+                for (int rx = 0; rx < px; rx++) {
+                    w->stamp++;
+                    for (int y = cy + ry; y < y1; y += py)
+                        for (int x = cx + rx; x < x1; x += px) {
+                            g_owner = y * w->W + x;
+                            rules[sweep](&c, x, y);
+                        }
+                }
+        }
+    }
+}
+
+long om_world_tick(om_world *w, int order, int check_races) {
+    w->check = check_races ? 1 : 0;
+    w->viol = 0;
+    if (w->check) chk_init(w);
+    int nCx = (w->W + w->C - 1) / w->C, nCy = (w->H + w->C - 1) / w->C;
+    size_t ncell = (size_t)w->W * w->H;
+    for (int iter = 0; iter < w->cell_iter; iter++) { /* world.cpp:1050 */
+        for (int tk = 0; tk < 4; tk++) {              /* world.cpp:1057-1060 */
+            int ox = tk % 2, oy = 1 - tk / 2;
+            memset(w->vis, 0, ncell); /* world.cpp:1046,1066-1067 */
+            int na = (nCx - ox + 1) / 2, nb = (nCy - oy + 1) / 2;
+            int nslot = na * nb;
+            if (nslot <= 0) continue;
+            pvec *sp = (pvec *)calloc((size_t)nslot, sizeof(pvec));
+            /* chunks of one colour are independent (2-chunk spacing); slot order is
+             * cx-major like the task push order of world.cpp:1073-1077 */
+#pragma omp parallel for schedule(dynamic, 1) if (!w->check)
+            for (int s = 0; s < nslot; s++) {
+                int a = s / nb, b = s % nb;
+                int cx = (ox + 2 * a) * w->C, cy = (oy + 2 * b) * w->C;
+                process_chunk(w, order, iter, cx, cy, &sp[s]);
+            }
+            /* world.cpp:1901-1913: append spawned particles in task order */
+            for (int s = 0; s < nslot; s++) {
+                for (int i = 0; i < sp[s].n; i++) pv_push(&w->parts, &sp[s].p[i]);
+                free(sp[s].p);
+            }
+            free(sp);
+        }
+    }
+    w->tick++; /* world.cpp:1925 */
+    w->check = 0;
+    return w->viol;
+}
+
+/* --------------------------------------------------------------- particles */
+#define P_PHASE 1u
+#define P_TEMP 2u
+#define P_STATE_SHIFT 2
+
+static int SPIRAL_N = 0;
+static int8_t SPIRAL[1024][2];
+static void spiral_init(void) {
+    /* the spiral walk of world.cpp:2105-2133 (X = Y = 32, maxI = 1024) */
+    if (SPIRAL_N) return;
+    int X = 32, Y = 32, x = 0, y = 0, dx = 0, dy = -1;
+    int t = X > Y ? X : Y;
+    int maxI = t * t;
+    int n = 0;
+    for (int j = 0; j < maxI; j++) {
+        if ((-X / 2 <= x) && (x <= X / 2) && (-Y / 2 <= y) && (y <= Y / 2)) {
+            SPIRAL[n][0] = (int8_t)x;
+            SPIRAL[n][1] = (int8_t)y;
+            n++;
+        }
+        if ((x == y) || ((x < 0) && (x == -y)) || ((x > 0) && (x == 1 - y))) {
+            t = dx;
+            dx = -dy;
+            dy = t;
+        }
+        x += dx;
+        y += dy;
+    }
+    SPIRAL_N = n;
+}
+
+enum { REQ_NONE = 0, REQ_DIRECT = 1, REQ_SPIRAL = 2 };
+enum { OUT_ALIVE = 0, OUT_DEAD = 1 };
+
+/* One particle's motion for world::tickCells (world.cpp:2032-2188) against the
+ * grid as it stands before any deposit of this particle tick. Returns the request
+ * kind; *out is OUT_DEAD when the particle is removed without a deposit. */
+static int particle_move(om_world *w, om_particle *p, int *out, int *lx_o, int *ly_o) {
+    *out = OUT_ALIVE;
+    if ((p->bits & P_TEMP) && p->lifetime <= 0) { /* :2033-2037 */
+        *out = OUT_DEAD;
+        return -1; /* destroyed */
+    }
+    if (p->target_force != 0) { /* :2039-2051 */
+        float tdx = p->target_x - p->x;
+        float tdy = p->target_y - p->y;
+        float nf = sqrtf(tdx * tdx + tdy * tdy);
+        p->vx += tdx / nf * p->target_force;
+        p->vy += tdy / nf * p->target_force;
+        if (nf < 100) {
+            p->vx *= 0.95f;
+            p->vy *= 0.95f;
+        }
+    }
+    int lx = (int)p->x, ly = (int)p->y;
+    *lx_o = lx;
+    *ly_o = ly;
+    if (p->x < 0 || (int)p->x >= w->W || p->y < 0 || (int)p->y >= w->H) { /* :2056-2059 */
+        *out = OUT_DEAD;
+        return -2; /* exited */
+    }
+    p->vx += p->ax; /* :2063-2064 */
+    p->vy += p->ay;
+    int div = (int)((fabsf(p->vx) + fabsf(p->vy)) + 1);
+    float dvx = p->vx / div;
+    float dvy = p->vy / div;
+    for (int i = 0; i < div; i++) { /* :2071-2184 */
+        p->x += dvx;
+        p->y += dvy;
+        if (p->x < 0 || (int)p->x >= w->W || p->y < 0 || (int)p->y >= w->H) {
+            *out = OUT_DEAD;
+            return -2;
+        }
+        int ct = M[w->id[(size_t)(int)p->y * w->W + (int)p->x]].type;
+        if (!(p->bits & P_PHASE) && ct != T_AIR) {
+            int isObject = ct == T_OBJECT;
+            int st = (p->bits >> P_STATE_SHIFT) & 3;
+            if (st == 0)
+                st = isObject ? 1 : 2;
+            else if (st == 1 && !isObject)
+                st = 2;
+            p->bits = (uint8_t)((p->bits & ~(3u << P_STATE_SHIFT)) | ((unsigned)st << P_STATE_SHIFT));
+            if (!isObject || st == 2) {
+                if (p->bits & P_TEMP) {
+                    *out = OUT_DEAD;
+                    return -1;
+                }
+                if (M[w->id[(size_t)ly * w->W + lx]].type != T_AIR) return REQ_SPIRAL;
+                return REQ_DIRECT;
+            }
+        }
+    }
+    if (p->lifetime > 0) p->lifetime--; /* :2186-2188 */
+    return REQ_NONE;
+}
+
+/* target of a deposit against the current grid: 1 = fill an AIR cell, 2 = merge
+ * into a cell of the same liquid, 0 = no target (world.cpp:2093-2147) */
+static int find_target(om_world *w, const om_particle *p, int kind, int lx, int ly, int *tx, int *ty) {
+    if (kind == REQ_DIRECT) {
+        if (M[w->id[(size_t)ly * w->W + lx]].type == T_AIR) {
+            *tx = lx;
+            *ty = ly;
+            return 1;
+        }
+    }
+    int psoup = M[p->id].type == T_SOUP;
+    for (int j = 0; j < SPIRAL_N; j++) {
+        int cx = (int)(p->x + (float)SPIRAL[j][0]);
+        int cy = (int)(p->y + (float)SPIRAL[j][1]);
+        if (cx < 0 || cy < 0 || cx >= w->W || cy >= w->H) continue;
+        int cid = w->id[(size_t)cy * w->W + cx];
+        if (M[cid].type == T_AIR) {
+            *tx = cx;
+            *ty = cy;
+            return 1;
+        }
+        if (psoup && cid == p->id) {
+            *tx = cx;
+            *ty = cy;
+            return 2;
+        }
+    }
+    return 0;
+}
+
+int om_particles_tick(om_world *w) {
+    spiral_init();
+    int n = w->parts.n;
+    om_particle *P = w->parts.p;
+    uint8_t *dead = (uint8_t *)calloc((size_t)n + 1, 1);
+    int *req = (int *)malloc(((size_t)n + 1) * sizeof(int));
+    int *rlx = (int *)malloc(((size_t)n + 1) * sizeof(int));
+    int *rly = (int *)malloc(((size_t)n + 1) * sizeof(int));
+    int nreq = 0;
+    int *rq = (int *)malloc(((size_t)n + 1) * sizeof(int));
+    /* phase 1: motion, all particles against the grid left by the cell tick */
+    for (int i = 0; i < n; i++) {
+        int out, lx = 0, ly = 0;
+        int r = particle_move(w, &P[i], &out, &lx, &ly);
+        req[i] = REQ_NONE;
+        if (out == OUT_DEAD) {
+            dead[i] = 1;
+            int64_t f = (M[P[i].id].type == T_SOUP) ? P[i].scalar : 0;
+            if (r == -2) {
+                if (M[P[i].id].type != T_AIR) w->led[LED_XN][P[i].id] += 1;
+                w->led[LED_XF][P[i].id] += f;
+            } else {
+                if (M[P[i].id].type != T_AIR) w->led[LED_DN][P[i].id] += 1;
+                w->led[LED_DF][P[i].id] += f;
+            }
+        } else if (r == REQ_DIRECT || r == REQ_SPIRAL) {
+            req[i] = r;
+            rlx[i] = lx;
+            rly[i] = ly;
+            rq[nreq++] = i;
+        }
+    }
+    /* phase 2: deposits, in rounds; in each round every open request picks its
+     * target against the grid at the start of the round, merges apply at once, and
+     * each AIR cell goes to the lowest-index claimant; losers try again. */
+    int *tx = (int *)malloc(((size_t)nreq + 1) * sizeof(int));
+    int *ty = (int *)malloc(((size_t)nreq + 1) * sizeof(int));
+    int *tk = (int *)malloc(((size_t)nreq + 1) * sizeof(int));
+    int32_t *claim = NULL;
+    size_t ncell = (size_t)w->W * w->H;
+    if (nreq) {
+        claim = (int32_t *)malloc(ncell * sizeof(int32_t));
+        for (size_t i = 0; i < ncell; i++) claim[i] = 0x7fffffff;
+    }
+    while (nreq > 0) {
+        for (int j = 0; j < nreq; j++) {
+            int i = rq[j];
+            tk[j] = find_target(w, &P[i], req[i], rlx[i], rly[i], &tx[j], &ty[j]);
+            if (tk[j] == 1) {
+                size_t ci = (size_t)ty[j] * w->W + tx[j];
+                if (i < claim[ci]) claim[ci] = i;
+            }
+        }
+        int nn = 0;
+        for (int j = 0; j < nreq; j++) {
+            int i = rq[j];
+            om_particle *p = &P[i];
+            if (tk[j] == 0) { /* :2141-2144: no room found */
+                p->vy = -4;
+                p->y -= 16;
+                continue;
+            }
+            size_t ci = (size_t)ty[j] * w->W + tx[j];
+            if (tk[j] == 2) { /* :2119-2125 */
+                w->sc[ci] += p->scalar;
+                dead[i] = 1;
+                w->led[LED_DN][p->id] += 1;
+                continue;
+            }
+            if (claim[ci] == i) { /* :2115-2118 and :2148-2152 */
+                w->id[ci] = p->id;
+                w->col[ci] = p->colour;
+                w->sc[ci] = p->scalar;
+                w->fl[ci] = p->flags;
+                w->df[ci] = 0;
+                dead[i] = 1;
+            } else {
+                req[i] = REQ_SPIRAL; /* the cell was taken: search from here */
+                rq[nn++] = i;
+            }
+        }
+        for (int j = 0; j < nreq; j++)
+            if (tk[j] == 1) claim[(size_t)ty[j] * w->W + tx[j]] = 0x7fffffff;
+        nreq = nn;
+    }
+    /* phase 3: stable erase (std::erase_if, :2190) and the y > height erase (:2203) */
+    int m = 0;
+    for (int i = 0; i < n; i++) {
+        if (dead[i]) continue;
+        if (P[i].y > (float)w->H) continue;
+        P[m++] = P[i];
+    }
+    w->parts.n = m;
+    free(dead);
+    free(req);
+    free(rlx);
+    free(rly);
+    free(rq);
+    free(tx);
+    free(ty);
+    free(tk);
+    free(claim);
+    return m;
+}
+
+void om_world_step(om_world *wd, int order, int n) {
+    for (int i = 0; i < n; i++) {
+        om_world_tick(wd, order, 0);
+        om_particles_tick(wd);
+    }
+}
+
+int om_particles_count(const om_world *wd) { return wd->parts.n; }
+void om_particles_get(const om_world *wd, om_particle *out) {
+    memcpy(out, wd->parts.p, (size_t)wd->parts.n * sizeof(om_particle));
+}
+void om_particles_set(om_world *wd, const om_particle *in, int n) {
+    wd->parts.n = 0;
+    for (int i = 0; i < n; i++) pv_push(&wd->parts, &in[i]);
+}
+
+/* FP64 / FP32 kinematics of one particle step (no deposits), for the precision
+ * check of the FP32 particle kernel. Same control flow as particle_move(). */
+#define KIN_BODY(T, FABS)                                                                                    \
+    for (int i = 0; i < n; i++) {                                                                            \
+        const om_particle *p = &in[i];                                                                       \
+        T x = p->x, y = p->y, vx = p->vx, vy = p->vy;                                                        \
+        ev[i] = 0;                                                                                           \
+        sub[i] = -1;                                                                                         \
+        if ((p->bits & P_TEMP) && p->lifetime <= 0) {                                                        \
+            ev[i] = 2;                                                                                       \
+            goto done_##T;                                                                                   \
+        }                                                                                                    \
+        if (x < 0 || (int)x >= w->W || y < 0 || (int)y >= w->H) {                                            \
+            ev[i] = 1;                                                                                       \
+            goto done_##T;                                                                                   \
+        }                                                                                                    \
+        {                                                                                                    \
+            int lx = (int)x, ly = (int)y;                                                                    \
+            vx += (T)p->ax;                                                                                  \
+            vy += (T)p->ay;                                                                                  \
+            int div = (int)((FABS(vx) + FABS(vy)) + 1);                                                      \
+            T dvx = vx / div, dvy = vy / div;                                                                \
+            for (int s = 0; s < div; s++) {                                                                  \
+                x += dvx;                                                                                    \
+                y += dvy;                                                                                    \
+                if (x < 0 || (int)x >= w->W || y < 0 || (int)y >= w->H) {                                    \
+                    ev[i] = 1;                                                                               \
+                    sub[i] = s;                                                                              \
+                    goto done_##T;                                                                           \
+                }                                                                                            \
+                int ct = M[w->id[(size_t)(int)y * w->W + (int)x]].type;                                      \
+                if (!(p->bits & P_PHASE) && ct != T_AIR && ct != T_OBJECT) {                                 \
+                    sub[i] = s;                                                                              \
+                    if (p->bits & P_TEMP)                                                                    \
+                        ev[i] = 2;                                                                           \
+                    else                                                                                     \
+                        ev[i] = (M[w->id[(size_t)ly * w->W + lx]].type != T_AIR) ? 4 : 3;                    \
+                    goto done_##T;                                                                           \
+                }                                                                                            \
+            }                                                                                                \
+        }                                                                                                    \
+    done_##T:                                                                                                \
+        out4[4 * i + 0] = x;                                                                                 \
+        out4[4 * i + 1] = y;                                                                                 \
+        out4[4 * i + 2] = vx;                                                                                \
+        out4[4 * i + 3] = vy;                                                                                \
+    }
+
+void om_particles_kinematics_f64(const om_world *w, const om_particle *in, int n, double *out4, int32_t *ev,
+                                 int32_t *sub) {
+    KIN_BODY(double, fabs)
+}
+void om_particles_kinematics_f32(const om_world *w, const om_particle *in, int n, float *out4, int32_t *ev,
+                                 int32_t *sub) {
+    KIN_BODY(float, fabsf)
+}
+
+/* ------------------------------------------------------------- generators */
+void om_world_generate(om_world *w, int kind, uint32_t seed) {
+    int mats_mix[5] = {om_material_find("GENERIC_SAND"), om_material_find("WATER"), om_material_find("GENERIC_GAS"),
+                       om_material_find("STONE"), ID_AIR};
+    int mats_z[8] = {ID_AIR,
+                     om_material_find("STONE"),
+                     om_material_find("GENERIC_SAND"),
+                     om_material_find("WATER"),
+                     om_material_find("GENERIC_GAS"),
+                     om_material_find("DIRT"),
+                     om_material_find("GENERIC_LIQUID"),
+                     om_material_find("SOFT_DIRT_SAND")};
+    /* Zipf(s=1) weights 1/k over 8 ranks, scaled by 840 */
+    const int zw[8] = {840, 420, 280, 210, 168, 140, 120, 105};
+    uint32_t pk = pass_key(seed, 0, PH_GEN + (uint32_t)kind);
+    int top = (w->H * 3) / 5;
+    for (int y = 0; y < w->H; y++)
+        for (int x = 0; x < w->W; x++) {
+            uint32_t ck = cell_key(pk, (uint32_t)x, (uint32_t)y);
+            uint32_t r = draw_k(ck, 0);
+            int mid = ID_AIR;
+            if (kind == 0) {
+                if (y >= w->H - 8)
+                    mid = mats_mix[3];
+                else if (y < top) {
+                    uint32_t u = r % 100u;
+                    mid = u < 30 ? mats_mix[0] : u < 50 ? mats_mix[1] : u < 60 ? mats_mix[2] : u < 75 ? mats_mix[3] : ID_AIR;
+                }
+            } else if (kind == 1) {
+                uint32_t u = r % 2283u, acc = 0;
+                for (int k = 0; k < 8; k++) {
+                    acc += (uint32_t)zw[k];
+                    if (u < acc) {
+                        mid = mats_z[k];
+                        break;
+                    }
+                }
+            }
+            const mat_t *m = &M[mid];
+            size_t i = (size_t)y * w->W + x;
+            w->id[i] = (uint16_t)mid;
+            w->fl[i] = 0;
+            w->df[i] = 0;
+            w->sc[i] = m->f_scalar;
+            w->col[i] = m->f_base;
+            if (m->f_mod > 0)
+                w->col[i] = m->f_base + ((uint32_t)(m->f_lo + (int)(draw_k(ck, 1) % (uint32_t)m->f_mod)) << m->f_shift);
+        }
+}
+
+/* ------------------------------------------------------------------ ledger */
+void om_ledger_get(const om_world *w, int64_t *out) {
+    for (int r = 0; r < 6; r++)
+        for (int m = 0; m < NMAT; m++) out[r * NMAT + m] = w->led[r][m];
+}
+void om_ledger_reset(om_world *w) { memset(w->led, 0, sizeof(w->led)); }
+
+void om_census(const om_world *w, int64_t *out) {
+    memset(out, 0, sizeof(int64_t) * 4 * (size_t)NMAT);
+    size_t n = (size_t)w->W * w->H;
+    for (size_t i = 0; i < n; i++) {
+        int id = w->id[i];
+        out[id] += 1;
+        if (M[id].type == T_SOUP) out[NMAT + id] += (int64_t)w->sc[i] + w->df[i];
+    }
+    for (int i = 0; i < w->parts.n; i++) {
+        int id = w->parts.p[i].id;
+        out[2 * NMAT + id] += 1;
+        if (M[id].type == T_SOUP) out[3 * NMAT + id] += w->parts.p[i].scalar;
+    }
+}
+
+/* ------------------------------------------------------------------ objects */
+/* Rigid-body stamping before the tick, source/engine/game.cpp:1768-1814: every
+ * body tile is rotated into the grid, trying offsets (0,0),(1,0),(-1,0),(0,1),
+ * (0,-1); an AIR cell takes the tile; a SAND or SOUP cell is ejected as a particle
+ * and damps the body. Tiles are resolved in rounds: each open tile picks its first
+ * usable offset against the grid at the start of the round and the lowest
+ * (body, tile) index wins a contested cell; the others look again. */
+static const int DIRS[5][2] = {{0, 0}, {1, 0}, {-1, 0}, {0, 1}, {0, -1}};
+
+static void body_tile_pos(const om_body *b, int tx, int ty, int *wx, int *wy) {
+    float fx = (float)tx * b->cos_a - (float)(ty + 1) * b->sin_a + b->x;
+    float fy = (float)tx * b->sin_a + (float)(ty + 1) * b->cos_a + b->y;
+    *wx = (int)fx;
+    *wy = (int)fy;
+}
+
+void om_object_stamp(om_world *w, om_body *bodies, int n) {
+    long total = 0;
+    for (int b = 0; b < n; b++) {
+        bodies[b].n_sand = bodies[b].n_soup = bodies[b].n_placed = 0;
+        total += (long)bodies[b].w * bodies[b].h;
+    }
+    if (total == 0) return;
+    /* open tiles: (body, tile) in body-major, tx-major, ty-minor order */
+    int32_t *ob = (int32_t *)malloc((size_t)total * sizeof(int32_t));
+    int32_t *ot = (int32_t *)malloc((size_t)total * sizeof(int32_t));
+    long *gidx = (long *)malloc((size_t)total * sizeof(long));
+    int *tgt = (int *)malloc((size_t)total * sizeof(int));
+    long no = 0, base = 0;
+    for (int b = 0; b < n; b++) {
+        for (int t = 0; t < bodies[b].w * bodies[b].h; t++) {
+            ob[no] = b;
+            ot[no] = t;
+            gidx[no] = base + t;
+            no++;
+        }
+        base += (long)bodies[b].w * bodies[b].h;
+    }
+    size_t ncell = (size_t)w->W * w->H;
+    long *claim = (long *)malloc(ncell * sizeof(long));
+    for (size_t i = 0; i < ncell; i++) claim[i] = 0x7fffffffffffffffL;
+    uint32_t pk = pass_key(w->seed, w->tick, PH_STAMP);
+    while (no > 0) {
+        for (long j = 0; j < no; j++) {
+            const om_body *bd = &bodies[ob[j]];
+            int txx = ot[j] / bd->h, tyy = ot[j] % bd->h, wx, wy;
+            body_tile_pos(bd, txx, tyy, &wx, &wy);
+            tgt[j] = -1;
+            for (int d = 0; d < 5; d++) {
+                int xd = wx + DIRS[d][0], yd = wy + DIRS[d][1];
+                if (xd < 0 || yd < 0 || xd >= w->W || yd >= w->H) continue;
+                int ty = M[w->id[(size_t)yd * w->W + xd]].type;
+                if (ty == T_AIR || ty == T_SAND || ty == T_SOUP) {
+                    tgt[j] = yd * w->W + xd;
+                    if (gidx[j] < claim[tgt[j]]) claim[tgt[j]] = gidx[j];
+                    break;
+                }
+            }
+        }
+        long nn = 0;
+        for (long j = 0; j < no; j++) {
+            if (tgt[j] < 0) continue; /* no usable cell: the tile is not stamped */
+            size_t ci = (size_t)tgt[j];
+            if (claim[ci] != gidx[j]) {
+                ob[nn] = ob[j];
+                ot[nn] = ot[j];
+                gidx[nn] = gidx[j];
+                nn++;
+                continue;
+            }
+            om_body *bd = &bodies[ob[j]];
+            int ty = M[w->id[ci]].type;
+            if (ty == T_SAND || ty == T_SOUP) {
+                om_particle p;
+                memset(&p, 0, sizeof(p));
+                uint32_t ck = cell_key(pk, (uint32_t)ob[j], (uint32_t)ot[j]);
+                p.x = (float)(int)(ci % (size_t)w->W);
+                p.y = (float)((int)(ci / (size_t)w->W) - 3);
+                p.vx = (float)((int)(draw_k(ck, 0) % 10) - 5) / 10.0f;
+                p.vy = (float)(-((int)(draw_k(ck, 1) % 5) + 5)) / 10.0f;
+                p.ay = 0.1f;
+                p.fade_time = 60;
+                p.id = w->id[ci];
+                p.colour = w->col[ci];
+                p.scalar = w->sc[ci];
+                p.flags = w->fl[ci];
+                pv_push(&w->parts, &p);
+                if (ty == T_SOUP) {
+                    /* the cell's pending diff leaves with it */
+                    w->led[LED_DF][p.id] += w->df[ci];
+                    bd->n_soup++;
+                } else
+                    bd->n_sand++;
+            }
+            w->id[ci] = bd->id;
+            w->col[ci] = bd->colour;
+            w->sc[ci] = 0;
+            w->fl[ci] = 0;
+            w->df[ci] = 0;
+            bd->n_placed++;
+            w->led[LED_CN][bd->id] += 1;
+        }
+        for (long j = 0; j < no; j++)
+            if (tgt[j] >= 0) claim[tgt[j]] = 0x7fffffffffffffffL;
+        no = nn;
+    }
+    free(ob);
+    free(ot);
+    free(gidx);
+    free(tgt);
+    free(claim);
+}
+
+/* Readback after the tick, game.cpp:1896-1983: each body tile takes back the first
+ * cell of its offsets that holds the body's material and erases it (rounds as in
+ * the stamp). */
+long om_object_readback(om_world *w, const om_body *bodies_c, int n) {
+    om_body *bodies = (om_body *)bodies_c;
+    long removed = 0;
+    for (int b = 0; b < n; b++) bodies[b].n_recovered = 0;
+    long total = 0;
+    for (int b = 0; b < n; b++) total += (long)bodies[b].w * bodies[b].h;
+    if (total == 0) return 0;
+    int32_t *ob = (int32_t *)malloc((size_t)total * sizeof(int32_t));
+    int32_t *ot = (int32_t *)malloc((size_t)total * sizeof(int32_t));
+    long *gidx = (long *)malloc((size_t)total * sizeof(long));
+    int *tgt = (int *)malloc((size_t)total * sizeof(int));
+    long no = 0, base = 0;
+    for (int b = 0; b < n; b++) {
+        for (int t = 0; t < bodies[b].w * bodies[b].h; t++) {
+            ob[no] = b;
+            ot[no] = t;
+            gidx[no] = base + t;
+            no++;
+        }
+        base += (long)bodies[b].w * bodies[b].h;
+    }
+    size_t ncell = (size_t)w->W * w->H;
+    long *claim = (long *)malloc(ncell * sizeof(long));
+    for (size_t i = 0; i < ncell; i++) claim[i] = 0x7fffffffffffffffL;
+    while (no > 0) {
+        for (long j = 0; j < no; j++) {
+            const om_body *bd = &bodies[ob[j]];
+            int txx = ot[j] / bd->h, tyy = ot[j] % bd->h, wx, wy;
+            body_tile_pos(bd, txx, tyy, &wx, &wy);
+            tgt[j] = -1;
+            for (int d = 0; d < 5; d++) {
+                int xd = wx + DIRS[d][0], yd = wy + DIRS[d][1];
+                if (xd < 0 || yd < 0 || xd >= w->W || yd >= w->H) continue;
+                if (w->id[(size_t)yd * w->W + xd] == bd->id) {
+                    tgt[j] = yd * w->W + xd;
+                    if (gidx[j] < claim[tgt[j]]) claim[tgt[j]] = gidx[j];
+                    break;
+                }
+            }
+        }
+        long nn = 0;
+        for (long j = 0; j < no; j++) {
+            if (tgt[j] < 0) continue;
+            size_t ci = (size_t)tgt[j];
+            if (claim[ci] != gidx[j]) {
+                ob[nn] = ob[j];
+                ot[nn] = ot[j];
+                gidx[nn] = gidx[j];
+                nn++;
+                continue;
+            }
+            om_body *bd = &bodies[ob[j]];
+            w->led[LED_DN][w->id[ci]] += 1;
+            w->id[ci] = (uint16_t)ID_AIR;
+            w->col[ci] = 0;
+            w->sc[ci] = 0;
+            w->fl[ci] = 0;
+            w->df[ci] = 0;
+            bd->n_recovered++;
+            removed++;
+        }
+        for (long j = 0; j < no; j++)
+            if (tgt[j] >= 0) claim[tgt[j]] = 0x7fffffffffffffffL;
+        no = nn;
+    }
+    free(ob);
+    free(ot);
+    free(gidx);
+    free(tgt);
+    free(claim);
+    return removed;
+}
+
+void om_object_mask(const om_world *w, uint8_t *bits) {
+    size_t n = (size_t)w->W * w->H;
+    memset(bits, 0, (n + 7) / 8);
+    for (size_t i = 0; i < n; i++)
+        if (M[w->id[i]].type == T_OBJECT) bits[i >> 3] |= (uint8_t)(1u << (i & 7));
+}
+
+void om_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+__attribute__((constructor)) static void om_init(void) {
+    om_materials_reset_builtin();
+    spiral_init();
+}
