@@ -1,0 +1,371 @@
+"""Benchmark of the GB300 falling-sand world tick.
+
+Default workload (the metric's single-GPU configuration): one 4096x2048 world with
+the standard material mix plus 1M free particles, plain per-world launch; a step is
+world::tick() + world::tickCells(). Prints one JSON line.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl fse|reference]
+                  [--workload 1|0|2|3|4]
+
+--impl reference times the CPU restatement of the reference tick (reference chunk
+order, all host threads) on the same workload. Workloads 0, 2, 3, 4 are the other
+configurations (512^2 world; 256 uneven worlds batched vs per-world launches;
+16384^2 world with OBJECT boxes; continuous-batching server) for reporting.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_CELL_UPDATE = 22  # 11-byte SoA cell state read once and written once per tick
+METRIC = "Gcell-updates/s"
+L2_FLUSH_BYTES = 512 << 20
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+class Clocks:
+    """nvidia-smi clock/throttle samples taken during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.p = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_%d.csv" % os.getpid())
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ workloads
+def config1_particles(n, w, h, seed):
+    """1M free particles: position uniform over the world, velocity N(0, 2)
+    cells/tick (FP64 draws rounded to f32), gravity 0.1 cells/tick^2, sand tiles."""
+    from falling_sand_engine_gb300 import PARTICLE_DTYPE, material_find
+
+    rng = np.random.default_rng(seed)
+    p = np.zeros(n, PARTICLE_DTYPE)
+    p["x"] = rng.uniform(0, w, n).astype(np.float32)
+    p["y"] = rng.uniform(0, h, n).astype(np.float32)
+    p["vx"] = rng.normal(0.0, 2.0, n).astype(np.float32)
+    p["vy"] = rng.normal(0.0, 2.0, n).astype(np.float32)
+    p["ay"] = np.float32(0.1)
+    p["fade_time"] = 60
+    p["id"] = material_find("GENERIC_SAND")
+    p["colour"] = 0xFFFFFFFF
+    return p
+
+
+def _flush(buf, i):
+    buf.fill_(i & 0x7F)
+
+
+def bench_config1(args, rank, local_rank, world_size):
+    import torch
+
+    import falling_sand_engine_gb300 as fse
+
+    W, H, NP = 4096, 2048, 1_000_000
+    seed = 1234 + rank
+    fse.InitMaterials()
+    fse.PushMaterials()
+    stream = torch.cuda.Stream()
+    world = fse.World(W, H, chunk_size=128, cell_iter=3, seed=seed, particle_capacity=4_000_000,
+                      spawn_capacity=2_000_000, stream=stream.cuda_stream)
+    world.generate(fse.GEN_MIX, seed)
+    world.addCell(config1_particles(NP, W, H, seed))
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
+    for _ in range(args.warmup):
+        world.step(1)
+    cells = W * H
+
+    # timed region: per-step CUDA events on the world's stream, L2 flushed between
+    # steps outside the events
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = Clocks(local_rank)
+    barrier(world_size)
+    torch.cuda.synchronize()
+    world.pass_timing(True)
+    l0 = fse.launch_counter()
+    clocks.start()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            _flush(flush, i)
+            ev[i][0].record(stream)
+            world.enqueue(1, particles=True)
+            ev[i][1].record(stream)
+    world.sync()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    launches = fse.launch_counter() - l0
+    pass_ms, pass_n = world.pass_timing(False)
+    gpu_ms = sum(a.elapsed_time(b) for a, b in ev)
+    gpu_ms = max_over_ranks(gpu_ms, world_size)
+    barrier(world_size)
+
+    value = world_size * cells * args.steps / (gpu_ms / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    avg_pass_s = (pass_ms / max(pass_n, 1)) / 1e3
+    units_per_launch = cells / (3 * 4)  # one launch = one colour x one iteration of the tick
+    achieved = BYTES_PER_CELL_UPDATE * units_per_launch / avg_pass_s / 1e9
+    roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": profile_traffic("colour_pass_config1"),
+            "kernel": "k_colour_pass<2>", "peak_kind": peak_kind,
+            "launch_ms_avg": round(pass_ms / max(pass_n, 1), 4),
+            "tick_frac": round(value * 1e9 * BYTES_PER_CELL_UPDATE / world_size / (peak * 1e9), 4)}
+
+    # end to end through the C ABI with host buffers: every step uploads the grid
+    # from pinned host memory, ticks, and reads the grid back
+    e2e = e2e_config1(world, args, torch, cells, world_size)
+    cpu = None
+    if rank == 0 and world_size == 1 and not args.no_cpu:
+        cpu = cpu_baseline_config1(seed)
+    world.close()
+    return {
+        "metric": METRIC, "value": round(value, 4), "unit": "Gcell/s", "n_gpus": world_size, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(gpu_ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32+f32", "data": "synthetic",
+        "config": {"workload": "config1: one 4096x2048 world (mix: 30% sand, 20% water, 10% gas, 15% rock, 25% air in "
+                               "the top 60%, 8 rock rows) + 1M free particles, plain per-world launch",
+                   "world": [W, H], "particles": NP, "chunk": 128, "cell_iter": 3, "seed": seed,
+                   "l2": "flushed between timed steps (512 MiB write outside the events)",
+                   "parallelism": "one independent world per GPU" if world_size > 1 else "single GPU"},
+        "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
+        "wall_s": round(wall, 3),
+    }
+
+
+def e2e_config1(world, args, torch, cells, world_size):
+    import falling_sand_engine_gb300 as fse
+
+    st = world.state()
+    pinned = {}
+    for k, v in st.items():
+        t = torch.empty(v.size, dtype={np.uint16: torch.int16, np.uint32: torch.int32, np.int32: torch.int32,
+                                       np.uint8: torch.uint8}[v.dtype.type], pin_memory=True)
+        a = t.numpy().view(v.dtype).reshape(v.shape)
+        a[...] = v
+        pinned[k] = (t, a)
+    host = {k: a for k, (t, a) in pinned.items()}
+    bi = sum(a.nbytes for a in host.values())
+    steps = max(1, min(args.steps, 5))
+    world.sync()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        world.upload(host)
+        world.step(1)
+        world.state(out=host)
+    dt = max_over_ranks(time.perf_counter() - t0, world_size)
+    return {"value": round(world_size * cells * steps / dt / 1e9, 4), "unit": "Gcell/s",
+            "h2d_bytes_per_step": int(bi), "d2h_bytes_per_step": int(bi), "steps": steps,
+            "path": "fse_world_upload + fse_world_step + fse_world_download (host-resident grid)"}
+
+
+def cpu_baseline_config1(seed, budget_s=12.0):
+    """The oracle's reference-order tick on the host cores, on a bounded sample of
+    the same workload (full 4096x2048 world + 1M particles, as many steps as fit the
+    time budget, at least one)."""
+    from oracle import Oracle, OracleWorld
+
+    o = Oracle()
+    o.reset_materials()
+    cores = os.cpu_count() or 1
+    o.set_threads(cores)
+    W, H = 4096, 2048
+    ow = OracleWorld(W, H, 128, 3, seed)
+    ow.generate(0, seed)
+    ow.set_particles(config1_particles(1_000_000, W, H, seed))
+    ow.step(1, 0)  # warm-up
+    n, t0 = 0, time.perf_counter()
+    while True:
+        ow.step(1, 0)
+        n += 1
+        if time.perf_counter() - t0 > budget_s or n >= 20:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": round(W * H * n / dt / 1e9, 6), "unit": "Gcell/s", "cores": cores, "kind": "port",
+            "sample": "%d steps (tick + tickCells) of the 4096x2048 world with 1M particles, reference chunk order, "
+                      "after 1 warm-up step" % n}
+
+
+def profile_traffic(name):
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f).get(name)
+    except Exception:
+        return None
+
+
+def barrier(world_size):
+    if world_size > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(v, world_size):
+    if world_size == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(v)], device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------ reference arm
+def reference_arm(args, rank, world_size):
+    if rank != 0:
+        return None
+    from oracle import Oracle, OracleWorld
+
+    o = Oracle()
+    o.reset_materials()
+    cores = os.cpu_count() or 1
+    o.set_threads(cores)
+    W, H = 4096, 2048
+    ow = OracleWorld(W, H, 128, 3, 1234)
+    ow.generate(0, 1234)
+    ow.set_particles(_np_particles(1_000_000, W, H, 1234))
+    for _ in range(args.warmup):
+        ow.step(1, 0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ow.step(1, 0)
+    dt = time.perf_counter() - t0
+    value = W * H * args.steps / dt / 1e9
+    sample = "%d timed steps (tick + tickCells) of the 4096x2048 world with 1M particles after %d warm-up" % (
+        args.steps, args.warmup)
+    return {
+        "impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": "Gcell/s", "n_gpus": world_size,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+f32", "data": "synthetic",
+        "config": {"workload": "config1: one 4096x2048 world + 1M free particles", "world": [W, H],
+                   "particles": 1_000_000, "chunk": 128, "cell_iter": 3,
+                   "impl_note": "CPU restatement of world::tick/tickCells in the reference chunk order "
+                                "(the reference itself does not build here: SDL2/xmake missing)"},
+        "cpu_baseline": {"value": round(value, 6), "unit": "Gcell/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 6), "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def _np_particles(n, w, h, seed):
+    from oracle import PARTICLE_DTYPE
+
+    rng = np.random.default_rng(seed)
+    p = np.zeros(n, PARTICLE_DTYPE)
+    p["x"] = rng.uniform(0, w, n).astype(np.float32)
+    p["y"] = rng.uniform(0, h, n).astype(np.float32)
+    p["vx"] = rng.normal(0.0, 2.0, n).astype(np.float32)
+    p["vy"] = rng.normal(0.0, 2.0, n).astype(np.float32)
+    p["ay"] = np.float32(0.1)
+    p["fade_time"] = 60
+    p["id"] = 2
+    p["colour"] = 0xFFFFFFFF
+    return p
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="fse", choices=["fse", "reference"])
+    ap.add_argument("--workload", type=int, default=1, choices=[0, 1, 2, 3, 4])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, local_rank, world_size = dist_info()
+
+    if args.impl == "reference":
+        out = reference_arm(args, rank, world_size)
+        if out is not None:
+            print(json.dumps(out))
+        return
+
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    if world_size > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    if args.workload == 1:
+        out = bench_config1(args, rank, local_rank, world_size)
+    else:
+        import bench_workloads
+
+        out = bench_workloads.run(args, rank, local_rank, world_size)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+    if world_size > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

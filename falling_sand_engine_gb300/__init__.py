@@ -71,6 +71,11 @@ def load_lua_materials(script):
     return n.value
 
 
+def launch_counter():
+    """Number of CUDA kernels the library has launched in this process."""
+    return lib().fse_launch_counter()
+
+
 def material_find(index_name):
     return lib().fse_material_find(index_name.encode())
 
@@ -117,6 +122,8 @@ class World:
             self.h = h
         else:
             self.h = C.c_void_p(_handle)
+            inf = self.info()
+            self.width, self.height = inf["w"], inf["h"]
 
     def close(self):
         if getattr(self, "h", None) and self._owned:
@@ -157,11 +164,17 @@ class World:
             arrs.append(None if a is None else np.ascontiguousarray(a, dt).reshape(n))
         check(self.lib.fse_world_upload(self.h, *[ptr(a) if a is not None else None for a in arrs]), "upload")
 
-    def state(self):
+    def state(self, out=None):
+        """Download the SoA planes (into `out`, e.g. pinned host arrays, when given)."""
         n = self.width * self.height
-        out = {k: np.empty(n, dt) for k, dt in self.PLANES}
+        if out is None:
+            out = {k: np.empty((self.height, self.width), dt) for k, dt in self.PLANES}
+        for k, dt in self.PLANES:
+            a = out[k]
+            if a.dtype != dt or a.size != n or not a.flags["C_CONTIGUOUS"]:
+                raise ValueError("plane %s must be a C-contiguous %s array of %d cells" % (k, np.dtype(dt), n))
         check(self.lib.fse_world_download(self.h, *[ptr(out[k]) for k, _ in self.PLANES]), "download")
-        return {k: v.reshape(self.height, self.width) for k, v in out.items()}
+        return out
 
     def generate(self, kind, seed):
         check(self.lib.fse_world_generate(self.h, kind, seed & 0xFFFFFFFF), "generate")
@@ -188,6 +201,17 @@ class World:
         """n x (world::tick(); world::tickCells()), optionally replayed from a CUDA graph."""
         fn = self.lib.fse_world_step_graph if graph else self.lib.fse_world_step
         check(fn(self.h, n), "step")
+
+    def enqueue(self, n=1, particles=True):
+        """Queue n steps (or ticks) on the world's stream without waiting."""
+        check(self.lib.fse_world_enqueue(self.h, n, 1 if particles else 0), "enqueue")
+
+    def pass_timing(self, enable):
+        """Start (True) or stop (False) CUDA-event timing of the colour-pass kernel;
+        returns (milliseconds, launches) accumulated since the last start."""
+        ms, n = C.c_double(0.0), C.c_int64(0)
+        check(self.lib.fse_world_pass_timing(self.h, 1 if enable else 0, C.byref(ms), C.byref(n)), "pass_timing")
+        return ms.value, n.value
 
     def sync(self):
         check(self.lib.fse_world_sync(self.h), "sync")

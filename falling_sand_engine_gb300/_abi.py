@@ -60,6 +60,7 @@ SIGNATURES = {
     "fse_particles_tick": (_i, [_vp]),
     "fse_world_step": (_i, [_vp, _i]),
     "fse_world_step_graph": (_i, [_vp, _i]),
+    "fse_world_enqueue": (_i, [_vp, _i, _i]),
     "fse_world_sync": (_i, [_vp]),
     "fse_world_set_stream": (_i, [_vp, _vp]),
     "fse_world_stream": (_vp, [_vp]),
@@ -70,6 +71,8 @@ SIGNATURES = {
     "fse_object_readback": (_i, [_vp, _vp, _i, C.POINTER(_i64)]),
     "fse_object_mask_export": (_i, [_vp, _vp]),
     "fse_object_list_export": (_i, [_vp, _vp, _i64, C.POINTER(_i64)]),
+    "fse_world_pass_timing": (_i, [_vp, _i, C.POINTER(_d), C.POINTER(_i64)]),
+    "fse_launch_counter": (_i64, []),
     "fse_world_ledger": (_i, [_vp, _vp]),
     "fse_world_ledger_reset": (_i, [_vp]),
     "fse_world_census": (_i, [_vp, _vp]),

@@ -8,6 +8,7 @@
 #include <array>
 #include <cstddef>
 #include <cctype>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -262,18 +263,59 @@ int tick_halo() {
     return t.has_inter ? 5 : 2;
 }
 
+static std::atomic<long long> g_launches{0};
+void count_launches(long long n) { g_launches += n; }
+
+cudaEvent_t PassTimer::get() {
+    if (!pool.empty()) {
+        cudaEvent_t e = pool.back();
+        pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+void PassTimer::drain() {
+    for (auto &pr : pending) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, pr.first, pr.second) == cudaSuccess) {
+            ms += t;
+            launches++;
+        }
+        pool.push_back(pr.first);
+        pool.push_back(pr.second);
+    }
+    pending.clear();
+}
+
 int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], const int n_items[4], int max_iter, int C,
-                 int threads, int grid, bool particles, int move_blocks, int stage_blocks, cudaStream_t s) {
+                 int threads, int grid, bool particles, int move_blocks, int stage_blocks, cudaStream_t s,
+                 PassTimer *timer) {
     int halo = tick_halo();
     for (int iter = 0; iter < max_iter; iter++)  // world.cpp:1050
         for (int tk = 0; tk < 4; tk++) {         // world.cpp:1057-1060
+            cudaEvent_t a = nullptr, b = nullptr;
+            if (timer) {
+                a = timer->get();
+                b = timer->get();
+                cudaEventRecord(a, s);
+            }
             cudaError_t e = launch_colour_pass(d_worlds, items[tk], n_items[tk], iter, tk, g_dev_mt, halo, C, threads,
                                                grid, s);
             if (e != cudaSuccess) return FSE_E_CUDA;
+            if (timer) {
+                cudaEventRecord(b, s);
+                timer->record_pair(a, b);
+            }
+            if (n_items[tk] > 0) count_launches(1);
         }
     if (launch_spawn_append(d_worlds, n_worlds, stage_blocks, s) != cudaSuccess) return FSE_E_CUDA;
-    if (particles && launch_particle_tick(d_worlds, n_worlds, g_dev_mt, move_blocks, s) != cudaSuccess)
-        return FSE_E_CUDA;
+    count_launches(3);
+    if (particles) {
+        if (launch_particle_tick(d_worlds, n_worlds, g_dev_mt, move_blocks, s) != cudaSuccess) return FSE_E_CUDA;
+        count_launches(11);
+    }
     return FSE_OK;
 }
 }  // namespace fse
@@ -461,8 +503,37 @@ struct LuaTok {
 };
 }  // namespace
 
-int fse_materials_load_lua(const char *script, int *out_count) {
-    if (!script) return FSE_E_INVAL;
+// the script without Lua comments (-- line, --[[ block ]]), string literals kept
+static std::string strip_lua_comments(const char *s) {
+    std::string out;
+    for (const char *p = s; *p;) {
+        if (*p == '"' || *p == '\'') {
+            char q = *p;
+            out.push_back(*p++);
+            while (*p && *p != q) {
+                if (*p == '\\' && p[1]) out.push_back(*p++);
+                out.push_back(*p++);
+            }
+            if (*p) out.push_back(*p++);
+        } else if (p[0] == '-' && p[1] == '-') {
+            if (p[2] == '[' && p[3] == '[') {
+                const char *e = strstr(p + 4, "]]");
+                p = e ? e + 2 : p + strlen(p);
+            } else {
+                while (*p && *p != '\n') p++;
+            }
+            out.push_back(' ');
+        } else {
+            out.push_back(*p++);
+        }
+    }
+    return out;
+}
+
+int fse_materials_load_lua(const char *script_in, int *out_count) {
+    if (!script_in) return FSE_E_INVAL;
+    const std::string stripped = strip_lua_comments(script_in);
+    const char *script = stripped.c_str();
     int count = 0;
     const char *p = script;
     for (;;) {
@@ -519,6 +590,11 @@ static void free_world(fse_world *w) {
     for (int k = 0; k < 4; k++)
         if (w->items[k]) cudaFree(w->items[k]);
     if (w->own_stream && w->stream) cudaStreamDestroy(w->stream);
+    if (w->timer) {
+        w->timer->drain();
+        for (cudaEvent_t e : w->timer->pool) cudaEventDestroy(e);
+        delete w->timer;
+    }
     delete w;
 }
 
@@ -562,6 +638,7 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
     w->stage_cap = c.spawn_capacity;
     w->threads = 1024;
     w->grid = 0;
+    w->timer = nullptr;
     if (c.stream) {
         w->stream = (cudaStream_t)c.stream;
         w->own_stream = false;
@@ -621,6 +698,7 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
     h.req_count = w->ctr + 2;  // [3]
     h.err = w->ctr + 5;
     h.tick = (uint32_t *)(w->ctr + 6);
+    h.bar = (unsigned *)(w->ctr + 8);  // [8] arrivals, [9] generation
     cudaMemset(w->ctr, 0, 16 * sizeof(int32_t));
     cudaMemset(h.ledger, 0, LED_ROWS * MAXMAT * sizeof(long long));
     cudaMemset(h.cp_count, 0, ncp * sizeof(int32_t));
@@ -691,14 +769,21 @@ __global__ void k_mask_flags(uint8_t *fl, size_t n) {
         fl[i] &= (uint8_t)~VISITED;
 }
 
+// uploaded material ids must index the table: out-of-range ids become GENERIC_AIR
+// and the upload reports FSE_E_INVAL
+__global__ void k_check_ids(uint16_t *id, size_t n, int nmat, int air, int *bad) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        if (id[i] >= nmat) {
+            id[i] = (uint16_t)air;
+            *bad = 1;
+        }
+}
+
 int fse_world_upload(fse_world *w, const uint16_t *id, const uint32_t *col, const int32_t *sc, const uint8_t *fl,
                      const int32_t *df) {
     if (!w) return FSE_E_INVAL;
     size_t n = (size_t)w->W * w->H;
     const MatTable &t = host_table();
-    if (id)
-        for (size_t i = 0; i < n; i++)
-            if (id[i] >= t.n) return FSE_E_INVAL;
     if (id) FSE_CUDA_TRY(cudaMemcpyAsync(w->h.id, id, n * 2, cudaMemcpyHostToDevice, w->stream));
     if (col) FSE_CUDA_TRY(cudaMemcpyAsync(w->h.col, col, n * 4, cudaMemcpyHostToDevice, w->stream));
     if (sc) FSE_CUDA_TRY(cudaMemcpyAsync(w->h.sc, sc, n * 4, cudaMemcpyHostToDevice, w->stream));
@@ -708,8 +793,15 @@ int fse_world_upload(fse_world *w, const uint16_t *id, const uint32_t *col, cons
         k_mask_flags<<<std::max(1, std::min<int>((int)(n / 1024) + 1, 4096)), 256, 0, w->stream>>>(w->h.fl, n);
     }
     if (df) FSE_CUDA_TRY(cudaMemcpyAsync(w->h.df, df, n * 4, cudaMemcpyHostToDevice, w->stream));
+    int bad = 0;
+    if (id) {
+        int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)sm_count() * 8);
+        FSE_CUDA_TRY(cudaMemsetAsync(w->ctr + 7, 0, 4, w->stream));
+        k_check_ids<<<std::max(blocks, 1), 256, 0, w->stream>>>(w->h.id, n, t.n, t.id_air, w->ctr + 7);
+        FSE_CUDA_TRY(cudaMemcpyAsync(&bad, w->ctr + 7, 4, cudaMemcpyDeviceToHost, w->stream));
+    }
     FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
-    return FSE_OK;
+    return bad ? FSE_E_INVAL : FSE_OK;
 }
 
 int fse_world_download(fse_world *w, uint16_t *id, uint32_t *col, int32_t *sc, uint8_t *fl, int32_t *df) {
@@ -829,10 +921,11 @@ static int world_enqueue(fse_world *w, bool particles_after_tick, bool tick, boo
     if (rc) return rc;
     if (tick) {
         rc = enqueue_step(w->d, 1, w->items, w->n_items, w->cell_iter, w->C, w->threads, w->grid, particles_after_tick,
-                          world_move_blocks(w), world_stage_blocks(w), w->stream);
+                          world_move_blocks(w), world_stage_blocks(w), w->stream, w->timer);
         if (rc) return rc;
     } else if (particles) {
         if (launch_particle_tick(w->d, 1, g_dev_mt, world_move_blocks(w), w->stream) != cudaSuccess) return FSE_E_CUDA;
+        count_launches(11);
     }
     return FSE_OK;
 }
@@ -869,6 +962,15 @@ int fse_world_step(fse_world *w, int n) {
         if (rc) return rc;
     }
     return fse_world_sync(w);
+}
+
+int fse_world_enqueue(fse_world *w, int n, int with_particles) {
+    if (!w || n < 0) return FSE_E_INVAL;
+    for (int i = 0; i < n; i++) {
+        int rc = world_enqueue(w, with_particles != 0, true, with_particles != 0);
+        if (rc) return rc;
+    }
+    return cudaGetLastError() == cudaSuccess ? FSE_OK : FSE_E_CUDA;
 }
 
 // capture `ticks` steps once, replay to cover n
@@ -1023,6 +1125,27 @@ int fse_particles_read(fse_world *w, fse_particle *out, int cap, int *out_n) {
     }
     return FSE_OK;
 }
+
+// ============================================================ diagnostics
+int fse_world_pass_timing(fse_world *w, int enable, double *out_ms, int64_t *out_launches) {
+    if (!w) return FSE_E_INVAL;
+    FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
+    if (w->timer) w->timer->drain();
+    if (out_ms) *out_ms = w->timer ? w->timer->ms : 0.0;
+    if (out_launches) *out_launches = w->timer ? w->timer->launches : 0;
+    if (enable) {
+        if (!w->timer) w->timer = new PassTimer();
+        w->timer->ms = 0.0;
+        w->timer->launches = 0;
+    } else if (w->timer) {
+        for (cudaEvent_t e : w->timer->pool) cudaEventDestroy(e);
+        delete w->timer;
+        w->timer = nullptr;
+    }
+    return FSE_OK;
+}
+
+int64_t fse_launch_counter(void) { return (int64_t)g_launches.load(); }
 
 // ================================================================= ledger
 int fse_world_ledger(fse_world *w, int64_t *out) {

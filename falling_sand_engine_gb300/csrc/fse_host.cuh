@@ -9,6 +9,20 @@
 
 #include "fse_internal.cuh"
 
+namespace fse {
+// CUDA events around each colour-pass launch, on the launching stream; read back
+// lazily so timing adds no host synchronisation to the tick
+struct PassTimer {
+    std::vector<cudaEvent_t> pool;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+    double ms = 0.0;
+    long long launches = 0;
+    cudaEvent_t get();
+    void record_pair(cudaEvent_t a, cudaEvent_t b) { pending.push_back({a, b}); }
+    void drain();  // after a synchronize: accumulate and recycle events
+};
+}  // namespace fse
+
 struct fse_world {
     int W, H, C, cell_iter;
     uint32_t seed;
@@ -28,6 +42,7 @@ struct fse_world {
     std::map<int, cudaGraphExec_t> graphs;  // n_ticks -> step graph
     size_t bytes;         // device bytes owned
     int threads, grid;    // colour-pass launch shape
+    fse::PassTimer *timer;  // colour-pass event timer (enabled on request)
 };
 
 namespace fse {
@@ -51,7 +66,9 @@ int tick_halo();
 // one world::tick() + optionally world::tickCells() for a set of worlds that
 // share a device descriptor table
 int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], const int n_items[4], int max_iter,
-                 int C, int threads, int grid, bool particles, int move_blocks, int stage_blocks, cudaStream_t s);
+                 int C, int threads, int grid, bool particles, int move_blocks, int stage_blocks, cudaStream_t s,
+                 PassTimer *timer = nullptr);
+void count_launches(long long n);
 
 }  // namespace fse
 

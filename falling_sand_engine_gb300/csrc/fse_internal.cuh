@@ -137,6 +137,7 @@ struct WorldDev {
     int32_t *scan_tmp;      // block sums for compaction
     long long *ledger;      // [LED_ROWS][MAXMAT]
     int32_t *err;
+    unsigned *bar;          // grid barrier {count, generation} of the cooperative deposit kernel
 };
 
 __host__ __device__ __forceinline__ int ceil_div(int a, int b) { return (a + b - 1) / b; }

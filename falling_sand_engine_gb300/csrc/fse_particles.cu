@@ -7,6 +7,8 @@
 // explicitly rounded intrinsics (__fadd_rn, __fmul_rn, __fdiv_rn, __fsqrt_rn) so
 // that no multiply-add is contracted: the FP32 results equal a strict IEEE CPU
 // evaluation of the same expressions bit for bit.
+#include <algorithm>
+
 #include "fse_internal.cuh"
 
 namespace fse {
@@ -297,62 +299,107 @@ __global__ void k_dep_decide(const WorldDev *__restrict__ worlds) {
     }
 }
 
-// the remaining rounds in one CTA per world (few requests are left after round 1)
-__global__ void k_dep_finish(const WorldDev *__restrict__ worlds, const MatTable *__restrict__ mt) {
-    const WorldDev &w = worlds[blockIdx.x];
-    __shared__ int s_n, s_next, s_fill;
-    if (threadIdx.x == 0) {
-        s_n = w.req_count[1];
-        s_fill = w.req_count[2];
-    }
+// Grid-wide barrier for the cooperative deposit kernel. The spin is bounded: if
+// it ever gives up it records ERR_TIMEOUT and lets the block continue, so a wait
+// can never hang the device.
+struct GridBar {
+    unsigned count;
+    unsigned gen;
+};
+
+__device__ __forceinline__ void grid_sync(GridBar *gb, unsigned nblocks, int32_t *err) {
     __syncthreads();
-    int32_t *cur = w.req_list2, *nxt = w.req_list;
-    // every round settles at least the lowest open request, so n rounds suffice
-    for (int round = 0; s_n > 0; round++) {
-        if (round > (1 << 22)) {
-            if (threadIdx.x == 0) atomicOr(w.err, ERR_TIMEOUT);
-            break;
-        }
-        const int n = s_n;
-        for (int j = threadIdx.x; j < n; j += blockDim.x) {
-            int i = cur[j];
-            int t = dep_target(w, mt, i, w.p_state[i]);
-            w.req_target[j] = t;
-            if (t >= 0) w.df[t] = 0x7fffffff;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) s_next = 0;
-        for (int j = threadIdx.x; j < n; j += blockDim.x) {
-            int i = cur[j], t = w.req_target[j];
-            if (t == -1)
-                dep_fail(w, i);
-            else if (t < 0)
-                dep_merge(w, mt, i, t & 0x7fffffff);
-            else
-                atomicMin(&w.df[t], i);
-        }
-        __syncthreads();
-        for (int j = threadIdx.x; j < n; j += blockDim.x) {
-            int i = cur[j], t = w.req_target[j];
-            if (t < 0) continue;
-            if (w.df[t] == i) {
-                dep_fill(w, i, t);
-                int k = atomicAdd(&s_fill, 1);
-                w.req_list2[w.part_cap + k] = t;
-            } else {
-                int k = atomicAdd(&s_next, 1);
-                nxt[k] = i;
+    if (threadIdx.x == 0) {
+        volatile unsigned *vgen = &gb->gen;
+        const unsigned g = *vgen;
+        __threadfence();
+        if (atomicAdd(&gb->count, 1u) + 1u == nblocks) {
+            gb->count = 0u;
+            __threadfence();
+            atomicAdd(&gb->gen, 1u);
+        } else {
+            long long spins = 0;
+            while (*vgen == g) {
+                if (++spins > (1LL << 25)) {
+                    atomicOr(err, ERR_TIMEOUT);
+                    break;
+                }
+                __nanosleep(100);
             }
         }
-        __syncthreads();
-        // losers keep list order? not needed: claims compare particle indices
-        int32_t *tmp = cur;
-        cur = nxt;
-        nxt = tmp;
-        if (threadIdx.x == 0) s_n = s_next;
-        __syncthreads();
+        __threadfence();
     }
-    if (threadIdx.x == 0) w.req_count[2] = s_fill;
+    __syncthreads();
+}
+
+// Rounds 2.. of the deposit resolution for every world, in one cooperative launch.
+// Open requests of round r live in list (r even: req_list2, odd: req_list) with
+// their count in req_count[1] (r even) / req_count[0] (r odd).
+__global__ void k_dep_rounds(const WorldDev *__restrict__ worlds, int n_worlds, const MatTable *__restrict__ mt) {
+    GridBar *gb = (GridBar *)worlds[0].bar;
+    const unsigned nb = gridDim.x;
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
+    int32_t *err = worlds[0].err;
+    for (int r = 0;; r++) {
+        if (r > (1 << 22)) {
+            if (gtid == 0) atomicOr(err, ERR_TIMEOUT);
+            break;
+        }
+        const int ci = (r & 1) ? 0 : 1, ni = (r & 1) ? 1 : 0;
+        // phase 1: targets against the grid at the start of the round
+        for (int wi = 0; wi < n_worlds; wi++) {
+            const WorldDev &w = worlds[wi];
+            const int n = w.req_count[ci];
+            const int32_t *cur = (r & 1) ? w.req_list : w.req_list2;
+            if (gtid == 0) w.req_count[ni] = 0;
+            for (int j = gtid; j < n; j += gstride) {
+                int i = cur[j];
+                int t = dep_target(w, mt, i, w.p_state[i]);
+                w.req_target[j] = t;
+                if (t >= 0) w.df[t] = 0x7fffffff;
+            }
+        }
+        grid_sync(gb, nb, err);
+        // phase 2: claims, merges, failures
+        for (int wi = 0; wi < n_worlds; wi++) {
+            const WorldDev &w = worlds[wi];
+            const int n = w.req_count[ci];
+            const int32_t *cur = (r & 1) ? w.req_list : w.req_list2;
+            for (int j = gtid; j < n; j += gstride) {
+                int i = cur[j], t = w.req_target[j];
+                if (t == -1)
+                    dep_fail(w, i);
+                else if (t < 0)
+                    dep_merge(w, mt, i, t & 0x7fffffff);
+                else
+                    atomicMin(&w.df[t], i);
+            }
+        }
+        grid_sync(gb, nb, err);
+        // phase 3: winners fill, losers go to the next round's list
+        for (int wi = 0; wi < n_worlds; wi++) {
+            const WorldDev &w = worlds[wi];
+            const int n = w.req_count[ci];
+            const int32_t *cur = (r & 1) ? w.req_list : w.req_list2;
+            int32_t *nxt = (r & 1) ? w.req_list2 : w.req_list;
+            for (int j = gtid; j < n; j += gstride) {
+                int i = cur[j], t = w.req_target[j];
+                if (t < 0) continue;
+                if (w.df[t] == i) {
+                    dep_fill(w, i, t);
+                    int k = atomicAdd(&w.req_count[2], 1);
+                    w.req_list2[w.part_cap + k] = t;
+                } else {
+                    int k = atomicAdd(&w.req_count[ni], 1);
+                    nxt[k] = i;
+                }
+            }
+        }
+        grid_sync(gb, nb, err);
+        int open = 0;
+        for (int wi = 0; wi < n_worlds; wi++) open += worlds[wi].req_count[ni];
+        if (open == 0) break;
+    }
 }
 
 // filled cells no longer hold a claim: their diff word becomes 0
@@ -530,7 +577,29 @@ cudaError_t launch_particle_tick(WorldDev *d_worlds, int n_worlds, const MatTabl
     k_dep_target<<<gm, 256, 0, s>>>(d_worlds, mt);
     k_dep_claim<<<gm, 256, 0, s>>>(d_worlds, mt);
     k_dep_decide<<<gm, 256, 0, s>>>(d_worlds);
-    k_dep_finish<<<n_worlds, 1024, 0, s>>>(d_worlds, mt);
+    {
+        // every block of a cooperative launch is resident, so the grid barrier is safe
+        static int coop_blocks = 0;
+        if (!coop_blocks) {
+            int per_sm = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dep_rounds, 256, 0);
+            int dev = 0, nsm = 1;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+            coop_blocks = std::max(1, std::min(per_sm, 4) * nsm);
+        }
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(coop_blocks);
+        cfg.blockDim = dim3(256);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cudaLaunchKernelEx(&cfg, k_dep_rounds, (const WorldDev *)d_worlds, n_worlds, mt);
+    }
     k_dep_clear<<<gm, 256, 0, s>>>(d_worlds);
     dim3 gc(PART_BLOCKS, n_worlds);
     k_cmp_count<<<gc, PART_THREADS, 0, s>>>(d_worlds);

@@ -9,17 +9,52 @@
 // changed. Inside a sub-phase every cell is processed by its own thread; the
 // lattice spacing makes every write set disjoint from every other cell's read and
 // write sets, so the result does not depend on thread timing.
+//
+// A sub-phase costs about one rule's dependent chain of shared-memory accesses
+// plus one barrier, whatever the mix of materials in a warp (sorting cells by type
+// first was measured and did not pay), so every thread simply runs the rule of its
+// own cells; spawned particles are ranked in the lattice enumeration order.
+//
+// The reference copies neighbour cells into locals and writes those copies back
+// later; no rule modifies such a neighbour between the copy and the write-back, so
+// here the write-back is a move inside shared memory at write time (move()), which
+// keeps only the active cell in registers.
 #include "fse_internal.cuh"
 
+// Optional per-phase cycle counters of the colour pass (build with
+// -DFSE_PHASE_CLOCKS): thread 0 of each CTA accumulates clock64() deltas between
+// barriers; fse_debug_phase_clocks() reads the totals. Off by default: no cost.
+#ifdef FSE_PHASE_CLOCKS
+__device__ unsigned long long g_phase_clk[16];
+#define FSE_PT_DECL                       \
+    __shared__ long long pt_acc[16];      \
+    long long pt_last = clock64();        \
+    if (threadIdx.x < 16) pt_acc[threadIdx.x] = 0;
+#define FSE_PT(k)                           \
+    if (threadIdx.x == 0) {                 \
+        long long t_ = clock64();           \
+        pt_acc[(k)] += t_ - pt_last;        \
+        pt_last = t_;                       \
+    }
+#define FSE_PT_FLUSH     \
+    __syncthreads();     \
+    if (threadIdx.x < 16) atomicAdd(&g_phase_clk[threadIdx.x], (unsigned long long)pt_acc[threadIdx.x]);
+#else
+#define FSE_PT_DECL
+#define FSE_PT(k)
+#define FSE_PT_FLUSH
+#endif
+
 namespace fse {
+
+constexpr int CP_THREADS = 1024;  // >= the largest sweep-A sub-phase (43 x 22 cells for 128-cell chunks)
 
 struct Cell {
     uint16_t id;
     uint8_t fl;
     int32_t sc;
     uint32_t col;
-    int32_t df;   // valid when src < 0
-    int32_t src;  // >= 0: the diff still lives in HBM at this cell index
+    int32_t df;
 };
 
 struct SpawnEv {
@@ -50,6 +85,20 @@ struct Tile {
     int W, H;
     int id_solid, id_air;
     int *err;
+    // sweep-B pillar snapshot: AIR bits of columns ax0.., rows ay0.., 5 words per column
+    const uint32_t *s_air;
+    int ax0, ay0, aw;
+
+    // 10 snapshot bits of column x starting at row y (0 outside the snapshot)
+    __device__ __forceinline__ uint32_t air10(int x, int y) const {
+        int sx = x - ax0, sy = y - ay0;
+        if ((unsigned)sx >= (unsigned)aw || sy < 0) return 0u;
+        const uint32_t *col = s_air + sx * 5;
+        int wi = sy >> 5, b = sy & 31;
+        if (wi >= 5) return 0u;
+        unsigned long long v = col[wi] | ((unsigned long long)(wi + 1 < 5 ? col[wi + 1] : 0u) << 32);
+        return (uint32_t)(v >> b) & 0x3FFu;
+    }
 
     __device__ __forceinline__ bool inw(int x, int y) const {
         return (unsigned)x < (unsigned)W && (unsigned)y < (unsigned)H;
@@ -63,6 +112,7 @@ struct Tile {
     }
     __device__ __forceinline__ void oob() const { atomicOr(err, ERR_BOUNDS); }
 
+    // world.cpp:999-1002: outside the world reads Tiles_TEST_SOLID
     __device__ __forceinline__ int id(int x, int y) const {
         if (!inw(x, y)) return id_solid;
         if (!in_ids(x, y)) {
@@ -72,36 +122,38 @@ struct Tile {
         return s_id[li(x, y)] & 0x7FFF;
     }
     __device__ __forceinline__ int type(int x, int y) const { return mt_type(ma[id(x, y)]); }
-
-    __device__ __forceinline__ Cell get(int x, int y) const {
+    __device__ __forceinline__ int32_t sc(int x, int y) const {
+        if (!inw(x, y) || !in_full(x, y)) return 0;
+        return s_sc[li(x, y)];
+    }
+    __device__ __forceinline__ int32_t df_of(int x, int y) const {
+        if (!inw(x, y) || mt_type(ma[id(x, y)]) != T_SOUP) return 0;
+        return df[y * W + x];
+    }
+    // The active cell. Its df field starts at 0 and collects the change of its
+    // pending diff (put_delta applies it with a reduction); the stored diff is
+    // loaded only where a rule needs the value itself (df_load).
+    __device__ __forceinline__ Cell get_active(int x, int y) const {
         Cell c;
-        c.df = 0;
-        c.src = -1;
-        if (!inw(x, y) || !in_full(x, y)) {
-            if (inw(x, y)) oob();
-            c.id = (uint16_t)id_solid;
-            c.fl = 0;
-            c.sc = 0;
-            c.col = 0xff0000u;  // Tiles_TEST_SOLID, game_datastruct.cpp:312
-            return c;
-        }
         int i = li(x, y);
         c.id = s_id[i] & 0x7FFF;
         c.fl = s_fl[i] & (uint8_t)~VISITED;
         c.sc = s_sc[i];
         c.col = s_col[i];
-        if (mt_type(ma[c.id]) == T_SOUP) c.src = y * W + x;
+        c.df = 0;
         return c;
     }
-    // the active cell: its diff is needed at once
-    __device__ __forceinline__ Cell get_active(int x, int y) const {
-        Cell c = get(x, y);
-        if (c.src >= 0) {
-            c.df = df[c.src];
-            c.src = -1;
-        }
-        return c;
+    __device__ __forceinline__ int32_t df_load(int x, int y) const { return df[y * W + x]; }
+    // write the active cell back at its own position, adding its diff change
+    __device__ __forceinline__ void put_delta(int x, int y, const Cell &c) const {
+        int i = li(x, y);
+        s_id[i] = c.id | DIRTY;
+        s_fl[i] = (uint8_t)((c.fl & (uint8_t)~VISITED) | (s_fl[i] & VISITED));
+        s_sc[i] = c.sc;
+        s_col[i] = c.col;
+        if (c.df != 0) atomicAdd(&df[y * W + x], c.df);  // no return value: a fire-and-forget reduction
     }
+    // world.cpp:1004-1008: outside the world writes are dropped
     __device__ __forceinline__ void put(int x, int y, const Cell &c) const {
         if (!inw(x, y)) return;
         if (!in_full(x, y)) {
@@ -113,11 +165,40 @@ struct Tile {
         s_fl[i] = (uint8_t)((c.fl & (uint8_t)~VISITED) | (s_fl[i] & VISITED));
         s_sc[i] = c.sc;
         s_col[i] = c.col;
-        if (mt_type(ma[c.id]) == T_SOUP) {
-            int g = y * W + x;
-            int32_t v = (c.src >= 0) ? df[c.src] : c.df;
-            df[g] = v;
+        if (mt_type(ma[c.id]) == T_SOUP) df[y * W + x] = c.df;
+    }
+    __device__ __forceinline__ void set_nothing(int x, int y) const {
+        Cell c;
+        c.id = (uint16_t)id_air;
+        c.fl = 0;
+        c.sc = 0;
+        c.col = 0;
+        c.df = 0;
+        put(x, y, c);
+    }
+    // write the cell at (sx, sy) over (dx, dy); the visited mark stays with the position
+    __device__ __forceinline__ void move(int dx, int dy, int sx, int sy) const {
+        if (!inw(dx, dy)) return;
+        if (!in_full(dx, dy)) {
+            oob();
+            return;
         }
+        int d = li(dx, dy);
+        if (!inw(sx, sy) || !in_full(sx, sy)) {
+            if (inw(sx, sy)) oob();
+            s_id[d] = (uint16_t)id_solid | DIRTY;
+            s_fl[d] = (uint8_t)(s_fl[d] & VISITED);
+            s_sc[d] = 0;
+            s_col[d] = 0xff0000u;
+            return;
+        }
+        int s = li(sx, sy);
+        uint16_t v = s_id[s] & 0x7FFF;
+        s_id[d] = v | DIRTY;
+        s_fl[d] = (uint8_t)((s_fl[s] & (uint8_t)~VISITED) | (s_fl[d] & VISITED));
+        s_sc[d] = s_sc[s];
+        s_col[d] = s_col[s];
+        if (mt_type(ma[v]) == T_SOUP) df[dy * W + dx] = df[sy * W + sx];
     }
     __device__ __forceinline__ void set_moved(int x, int y, bool on) const {
         if (!inw(x, y)) return;
@@ -131,12 +212,9 @@ struct Tile {
     }
     __device__ __forceinline__ void add_diff(int x, int y, int32_t v) const {
         if (!inw(x, y)) return;
-        df[y * W + x] += v;
+        atomicAdd(&df[y * W + x], v);  // fire-and-forget reduction: the thread does not wait
     }
-    __device__ __forceinline__ bool vis(int x, int y) const {
-        if (!inw(x, y) || !in_full(x, y)) return false;
-        return (s_fl[li(x, y)] & VISITED) != 0;
-    }
+    __device__ __forceinline__ bool vis(int x, int y) const { return (s_fl[li(x, y)] & VISITED) != 0; }
     __device__ __forceinline__ void setvis(int x, int y) const {
         if (!inw(x, y)) return;
         if (!in_full(x, y)) {
@@ -151,38 +229,44 @@ struct Tile {
 struct Ctx {
     uint32_t pk, ck, k;
     int iter;
+    int id_fire, id_water, id_lava, id_steam, id_obsidian, has_inter;
     const MatTable *mt;
-    long long *led_s;  // shared ledger [LED_ROWS][64]
-    long long *led_g;  // global ledger [LED_ROWS][MAXMAT]
+    long long *led_s;      // shared ledger [LED_ROWS][64]
+    long long *led_g;      // global ledger [LED_ROWS][MAXMAT]
     const uint32_t *ma;
+    const uint8_t *mreact;  // reactions per material (shared)
     SpawnEv ev;
     __device__ __forceinline__ uint32_t D() { return draw_k(ck, k++); }
 };
 
 __device__ __forceinline__ void led_add(Ctx &c, int row, int mat, long long v) {
     if (v == 0 || mt_type(c.ma[mat]) == T_AIR) return;
-    if (mat < 64)
+    if (mat < 64 && v > -(1LL << 24) && v < (1LL << 24)) {
+        // lanes of a warp mostly hit the same counter: sum them first, one atomic per group
+        const unsigned act = __activemask();
+        const unsigned grp = __match_any_sync(act, row * 64 + mat);
+        const int sum = __reduce_add_sync(grp, (int)v);
+        if ((threadIdx.x & 31) == __ffs(grp) - 1)
+            atomicAdd((unsigned long long *)&c.led_s[row * 64 + mat], (unsigned long long)(long long)sum);
+    } else if (mat < 64) {
         atomicAdd((unsigned long long *)&c.led_s[row * 64 + mat], (unsigned long long)v);
-    else
+    } else {
         atomicAdd((unsigned long long *)&c.led_g[row * MAXMAT + mat], (unsigned long long)v);
+    }
 }
-__device__ __forceinline__ void led_replace(Ctx &c, const Cell &old, int32_t old_df, const Cell &nw) {
-    led_add(c, LED_DN, old.id, 1);
-    if (mt_type(c.ma[old.id]) == T_SOUP) led_add(c, LED_DF, old.id, (long long)old.sc + old_df);
-    led_add(c, LED_CN, nw.id, 1);
-    if (mt_type(c.ma[nw.id]) == T_SOUP) led_add(c, LED_CF, nw.id, (long long)nw.sc + nw.df);
+// a conversion (not a move) of the content old -> nw
+__device__ __forceinline__ void led_swap(Ctx &c, int old_id, long long old_fluid, int new_id, long long new_fluid) {
+    led_add(c, LED_DN, old_id, 1);
+    if (mt_type(c.ma[old_id]) == T_SOUP) led_add(c, LED_DF, old_id, old_fluid);
+    led_add(c, LED_CN, new_id, 1);
+    if (mt_type(c.ma[new_id]) == T_SOUP) led_add(c, LED_CF, new_id, new_fluid);
 }
-__device__ __forceinline__ int32_t cell_df(const Tile &t, const Cell &c) { return c.src >= 0 ? t.df[c.src] : c.df; }
-
-__device__ __forceinline__ Cell nothing(int id_air) {
-    Cell c;
-    c.id = (uint16_t)id_air;
-    c.fl = 0;
-    c.sc = 0;
-    c.col = 0;
-    c.df = 0;
-    c.src = -1;
-    return c;
+// conversion of whatever is at (x, y) into nw
+__device__ __forceinline__ void led_replace_at(const Tile &T, Ctx &c, int x, int y, const Cell &nw) {
+    if (!T.inw(x, y)) return;
+    int oid = T.id(x, y);
+    long long of = (mt_type(c.ma[oid]) == T_SOUP) ? (long long)T.sc(x, y) + T.df_of(x, y) : 0;
+    led_swap(c, oid, of, nw.id, (long long)nw.sc + nw.df);
 }
 
 // TilesCreate(id, x, y), game_datastruct.cpp:494-574
@@ -191,7 +275,6 @@ __device__ __forceinline__ Cell create_tile(Ctx &c, int mid) {
     t.id = (uint16_t)mid;
     t.fl = 0;
     t.df = 0;
-    t.src = -1;
     t.sc = __ldg(&c.mt->f_scalar[mid]);
     t.col = __ldg(&c.mt->f_base[mid]);
     uint32_t fp = __ldg(&c.mt->f_pack[mid]);
@@ -235,7 +318,6 @@ __device__ __forceinline__ void soup_flow(const Tile &T, Ctx &c, Cell &t, int32_
         nt.sc = 0;
         nt.col = t.col;
         nt.df = flow;
-        nt.src = -1;
         T.put(nx, ny, nt);
         led_add(c, LED_CN, t.id, 1);
     } else {
@@ -243,42 +325,48 @@ __device__ __forceinline__ void soup_flow(const Tile &T, Ctx &c, Cell &t, int32_
     }
 }
 
+__device__ __forceinline__ void spawn_one(Ctx &c, int kind, int x, int y, const Cell &t, float vx, float vy) {
+    c.ev.n = 1;
+    c.ev.kind = kind;
+    c.ev.x = x;
+    c.ev.y = y;
+    c.ev.id = t.id;
+    c.ev.fl = t.fl;
+    c.ev.col = t.col;
+    c.ev.sc = t.sc;
+    c.ev.vx = vx;
+    c.ev.vy = vy;
+}
+
 // ----------------------------------------------------------------- sweep A
-__device__ void rule_a(const Tile &T, Ctx &c, int x, int y) {
+__device__ __forceinline__ void rule_a(const Tile &T, Ctx &c, int x, int y) {
     if (T.vis(x, y)) return;  // world.cpp:1091
     const uint32_t *ma = T.ma;
     const float *md = T.md;
-    Cell t = T.get_active(x, y);
-    uint32_t a = ma[t.id];
+    const int sid = T.id(x, y);
+    const uint32_t a = ma[sid];
     if (c.iter >= mt_iter(a)) {  // world.cpp:1093-1096
         T.setvis(x, y);
         return;
     }
-    int type = mt_type(a);
+    const int type = mt_type(a);
+    if (type != T_SAND && type != T_SOUP && type != T_GAS && sid != c.id_fire) return;
+    Cell t = T.get_active(x, y);
     c.ck = cell_key(c.pk, (uint32_t)x, (uint32_t)y);
     c.k = 0;
     const MatTable *mt = c.mt;
 
-    if ((int)t.id == mt->id_fire) {  // world.cpp:1101-1146
+    if (sid == c.id_fire) {  // world.cpp:1101-1146
         if (c.D() % 10 == 0) t.col = (255u << 16) | ((uint32_t)(100 + (int)(c.D() % 50)) << 8) | 50u;
         if (c.D() % 10 == 0) {
             float vx = (float)((int)(c.D() % 10) - 5) / 20.0f;
             float vy = -((float)(int)(c.D() % 10) / 10.0f) / 3.0f + -0.5f;
-            c.ev.n = 1;
-            c.ev.kind = 3;
-            c.ev.x = x;
-            c.ev.y = y - 1;
-            c.ev.id = t.id;
-            c.ev.fl = t.fl;
-            c.ev.col = t.col;
-            c.ev.sc = t.sc;
-            c.ev.vx = vx;
-            c.ev.vy = vy;
+            spawn_one(c, 3, x, y - 1, t, vx, vy);
             led_add(c, LED_CN, t.id, 1);
         }
         if (c.D() % 150 == 0) {
-            led_replace(c, t, t.df, nothing(T.id_air));
-            T.put(x, y, nothing(T.id_air));
+            led_swap(c, t.id, (long long)t.sc + t.df, T.id_air, 0);
+            T.set_nothing(x, y);
             T.setvis(x, y);
         } else {
             bool found = false;
@@ -287,48 +375,41 @@ __device__ void rule_a(const Tile &T, Ctx &c, int x, int y) {
                     if (T.type(x + xx, y + yy) == T_SOLID) {
                         found = true;
                         if (c.D() % 500 == 0) {
-                            Cell f = create_tile(c, mt->id_fire);
-                            if (T.inw(x + xx, y + yy)) {
-                                Cell o = T.get(x + xx, y + yy);
-                                led_replace(c, o, cell_df(T, o), f);
-                            }
+                            Cell f = create_tile(c, c.id_fire);
+                            led_replace_at(T, c, x + xx, y + yy, f);
                             T.put(x + xx, y + yy, f);
                             T.setvis(x + xx, y + yy);
                         }
                     }
                 }
             if (!found && c.D() % 120 == 0) {
-                Cell o = T.get(x, y);
-                led_replace(c, o, cell_df(T, o), nothing(T.id_air));
-                T.put(x, y, nothing(T.id_air));
+                led_swap(c, t.id, (long long)t.sc + t.df, T.id_air, 0);
+                T.set_nothing(x, y);
                 T.setvis(x, y);
             }
         }
     }
 
     if (type == T_SAND) {
-        Cell below = T.get(x, y + 1);  // world.cpp:1150
-        int bt = mt_type(ma[below.id]);
-        if (mt->has_inter) {  // world.cpp:1153-1179
+        const int bid = T.id(x, y + 1);  // world.cpp:1150
+        const int bt = mt_type(ma[bid]);
+        if (c.has_inter) {  // world.cpp:1153-1179
             int hit = -1;
             for (int i = 0; i < mt->n_inter; i++)
-                if (mt->inter[i][0] == (int)t.id && mt->inter[i][1] == (int)below.id) hit = i;
+                if (mt->inter[i][0] == (int)t.id && mt->inter[i][1] == bid) hit = i;
             if (hit >= 0) {
                 for (int i = 0; i < mt->n_inter; i++) {
-                    if (mt->inter[i][0] != (int)t.id || mt->inter[i][1] != (int)below.id) continue;
+                    if (mt->inter[i][0] != (int)t.id || mt->inter[i][1] != bid) continue;
                     int kind = mt->inter[i][2], d1 = mt->inter[i][3], d2 = mt->inter[i][4];
                     int ox = mt->inter[i][5], oy = mt->inter[i][6];
                     for (int xx = ox - d2; xx <= ox + d2; xx++)
                         for (int yy = oy - d2; yy <= oy + d2; yy++) {
-                            bool doit = (kind == INTER_TRANSFORM) ? (T.id(x + xx, y + yy) == (int)below.id)
-                                                                  : ((xx == 0 && yy == 0) ||
-                                                                     T.id(x + xx, y + yy) == T.id_air);
+                            bool doit = (kind == INTER_TRANSFORM)
+                                            ? (T.id(x + xx, y + yy) == bid)
+                                            : ((xx == 0 && yy == 0) || T.id(x + xx, y + yy) == T.id_air);
                             if (doit) {
                                 Cell nt = create_tile(c, d1);
-                                if (T.inw(x + xx, y + yy)) {
-                                    Cell o = T.get(x + xx, y + yy);
-                                    led_replace(c, o, cell_df(T, o), nt);
-                                }
+                                led_replace_at(T, c, x + xx, y + yy, nt);
                                 T.put(x + xx, y + yy, nt);
                                 T.setvis(x + xx, y + yy);
                             }
@@ -337,7 +418,7 @@ __device__ void rule_a(const Tile &T, Ctx &c, int x, int y) {
                 return;
             }
         }
-        int nr = mt->n_react[t.id];
+        const int nr = c.mreact[t.id];
         if (nr > 0) {  // world.cpp:1181-1204
             bool react = false;
             for (int i = 0; i < nr; i++) {
@@ -346,8 +427,7 @@ __device__ void rule_a(const Tile &T, Ctx &c, int x, int y) {
                 if (hit) {
                     Cell nt = create_tile(c, res);
                     if (mt_type(ma[nt.id]) != T_SOUP) nt.sc = t.sc;
-                    Cell o = T.get(x, y);
-                    led_replace(c, o, cell_df(T, o), nt);
+                    led_replace_at(T, c, x, y, nt);
                     T.put(x, y, nt);
                     T.setvis(x, y);
                     react = true;
@@ -356,27 +436,17 @@ __device__ void rule_a(const Tile &T, Ctx &c, int x, int y) {
             if (react) return;
         }
         // world.cpp:1206-1267
-        if (!can_sink(ma, md, below.id, t.id)) return;
-        Cell bl = T.get(x - 1, y + 1), br = T.get(x + 1, y + 1);
-        bool canL = can_sink(ma, md, bl.id, t.id);
-        bool canR = can_sink(ma, md, br.id, t.id);
+        if (!can_sink(ma, md, bid, t.id)) return;
+        const bool canL = can_sink(ma, md, T.id(x - 1, y + 1), t.id);
+        const bool canR = can_sink(ma, md, T.id(x + 1, y + 1), t.id);
         if (!((canL || canR) && c.D() % 20 == 0)) {
             if (bt == T_AIR && T.type(x, y + 2) == T_AIR && T.type(x, y + 3) == T_AIR && T.type(x, y + 4) == T_AIR) {
-                T.put(x, y, below);
+                T.move(x, y, x, y + 1);
                 float vx = (float)((int)(c.D() % 10) - 5) / 20.0f;
                 float vy = (float)(-((int)(c.D() % 2) + 3)) / 10.0f + 1.5f;
-                c.ev.n = 1;
-                c.ev.kind = 1;
-                c.ev.x = x;
-                c.ev.y = y + 1;
-                c.ev.id = t.id;
-                c.ev.fl = t.fl;
-                c.ev.col = t.col;
-                c.ev.sc = t.sc;
-                c.ev.vx = vx;
-                c.ev.vy = vy;
+                spawn_one(c, 1, x, y + 1, t, vx, vy);
             } else {
-                T.put(x, y, below);
+                T.move(x, y, x, y + 1);
                 if (c.D() % 2 == 0) t.fl |= MOVED;
                 T.put(x, y + 1, t);
                 T.setvis(x, y + 1);
@@ -395,15 +465,15 @@ __device__ void rule_a(const Tile &T, Ctx &c, int x, int y) {
         if (t.sc < Q_MINV) {
             led_add(c, LED_DF, t.id, t.sc);
             t.sc = 0;
-            T.put(x, y, t);
+            T.put_delta(x, y, t);
             return;
         }
         if (t.sc > Q_FREEFALL && T.type(x, y + 1) == T_AIR && T.type(x, y + 2) == T_AIR &&
             T.type(x, y + 3) == T_AIR && T.type(x, y + 4) == T_AIR) {  // world.cpp:1283-1305
-            T.put(x, y, nothing(T.id_air));
+            led_add(c, LED_DF, t.id, T.df_load(x, y));
+            T.set_nothing(x, y);
             int n = t.sc >> 18;
             if (n < 1) n = 1;
-            led_add(c, LED_DF, t.id, t.df);
             led_add(c, LED_CN, t.id, n - 1);
             c.ev.n = n;
             c.ev.kind = 2;
@@ -419,16 +489,18 @@ __device__ void rule_a(const Tile &T, Ctx &c, int x, int y) {
             return;
         }
         if (t.fl & MOVED) return;
-        int32_t start = t.sc, rem = t.sc;
-        Cell bottom = T.get(x, y + 1);
-        int bT = mt_type(ma[bottom.id]);
-        bool airBelow = bT == T_AIR;
-        if ((airBelow && c.iter <= 2) || bottom.id == t.id) {
-            int32_t dst = (bT == T_SOUP) ? bottom.sc : 0;
+        const int32_t start = t.sc;
+        int32_t rem = t.sc;
+        const int bid = T.id(x, y + 1);
+        const int bT = mt_type(ma[bid]);
+        const bool airBelow = bT == T_AIR;
+        if ((airBelow && c.iter <= 2) || bid == (int)t.id) {
+            int32_t dst = (bT == T_SOUP) ? T.sc(x, y + 1) : 0;
             soup_flow(T, c, t, rem, clampflow(vflow(start, dst) - dst, start), bT, x, y + 1);
-        } else if (c.iter == 0 && bT == T_SOUP && bottom.id != t.id) {
+        } else if (c.iter == 0 && bT == T_SOUP && bid != (int)t.id) {
             if (c.D() % 10 == 0) {
-                T.put(x, y, bottom);
+                t.df += T.df_load(x, y);  // the cell leaves its position: carry the whole diff
+                T.move(x, y, x, y + 1);
                 T.put(x, y + 1, t);
                 return;
             }
@@ -436,43 +508,44 @@ __device__ void rule_a(const Tile &T, Ctx &c, int x, int y) {
         if (rem < Q_MINV) {
             t.df -= rem;
             led_add(c, LED_DF, t.id, rem);
-            T.put(x, y, t);
+            T.put_delta(x, y, t);
             return;
         }
-        Cell left = T.get(x - 1, y);
-        int lT = mt_type(ma[left.id]);
-        bool canL = (lT == T_AIR || left.id == t.id) && !airBelow;
-        Cell right = T.get(x + 1, y);
-        int rT = mt_type(ma[right.id]);
-        bool canR = (rT == T_AIR || right.id == t.id) && !airBelow;
+        const int lid = T.id(x - 1, y);
+        const int lT = mt_type(ma[lid]);
+        const bool canL = (lT == T_AIR || lid == (int)t.id) && !airBelow;
+        const int rid = T.id(x + 1, y);
+        const int rT = mt_type(ma[rid]);
+        const bool canR = (rT == T_AIR || rid == (int)t.id) && !airBelow;
         if (canL) {
-            int32_t dst = (lT == T_SOUP) ? left.sc : 0;
+            int32_t dst = (lT == T_SOUP) ? T.sc(x - 1, y) : 0;
             soup_flow(T, c, t, rem, clampflow((rem - dst) / (canR ? 3 : 2), rem), lT, x - 1, y);
         }
         if (rem < Q_MINV) {
             t.df -= rem;
             led_add(c, LED_DF, t.id, rem);
-            T.put(x, y, t);
+            T.put_delta(x, y, t);
             return;
         }
         if (canR) {
-            int32_t dst = (rT == T_SOUP) ? right.sc : 0;
+            int32_t dst = (rT == T_SOUP) ? T.sc(x + 1, y) : 0;
             soup_flow(T, c, t, rem, clampflow((rem - dst) / 2, rem), rT, x + 1, y);
         }
         if (rem < Q_MINV) {
             t.df -= rem;
             led_add(c, LED_DF, t.id, rem);
-            T.put(x, y, t);
+            T.put_delta(x, y, t);
             return;
         }
-        Cell top = T.get(x, y - 1);
-        int tT = mt_type(ma[top.id]);
-        if (tT == T_AIR || top.id == t.id) {
-            int32_t dst = (tT == T_SOUP) ? top.sc : 0;
+        const int tid = T.id(x, y - 1);
+        const int tT = mt_type(ma[tid]);
+        if (tT == T_AIR || tid == (int)t.id) {
+            int32_t dst = (tT == T_SOUP) ? T.sc(x, y - 1) : 0;
             soup_flow(T, c, t, rem, clampflow(rem - vflow(rem, dst), rem), tT, x, y - 1);
-        } else if (c.iter == 0 && tT == T_SOUP && top.id != t.id) {
+        } else if (c.iter == 0 && tT == T_SOUP && tid != (int)t.id) {
             if (c.D() % 10 == 0) {
-                T.put(x, y, top);
+                t.df += T.df_load(x, y);
+                T.move(x, y, x, y - 1);
                 T.put(x, y - 1, t);
                 return;
             }
@@ -480,7 +553,7 @@ __device__ void rule_a(const Tile &T, Ctx &c, int x, int y) {
         if (rem < Q_MINV) {
             t.df -= rem;
             led_add(c, LED_DF, t.id, rem);
-            T.put(x, y, t);
+            T.put_delta(x, y, t);
             return;
         }
         if (start == rem) {  // world.cpp:1472-1483
@@ -494,23 +567,21 @@ __device__ void rule_a(const Tile &T, Ctx &c, int x, int y) {
             if (lT == T_SOUP) T.set_moved(x - 1, y, false);
             if (rT == T_SOUP) T.set_moved(x + 1, y, false);
         }
-        T.put(x, y, t);
+        T.put_delta(x, y, t);
         // WATER on LAVA, world.cpp:1519-1537
-        if ((int)t.id == mt->id_water && T.id(x, y + 1) == mt->id_lava) {
-            Cell st = create_tile(c, mt->id_steam);
-            led_replace(c, t, t.df, st);
+        if ((int)t.id == c.id_water && T.id(x, y + 1) == c.id_lava) {
+            Cell st = create_tile(c, c.id_steam);
+            led_swap(c, t.id, (long long)t.sc + T.df_load(x, y), st.id, (long long)st.sc);
             T.put(x, y, st);
-            Cell ob = create_tile(c, mt->id_obsidian);
-            Cell o = T.get(x, y + 1);
-            led_replace(c, o, cell_df(T, o), ob);
+            Cell ob = create_tile(c, c.id_obsidian);
+            led_replace_at(T, c, x, y + 1, ob);
             T.put(x, y + 1, ob);
             T.setvis(x, y + 1);
             for (int xx = -1; xx <= 1; xx++)
                 for (int yy = 0; yy <= 2; yy++) {
-                    if (T.id(x + xx, y + yy) == mt->id_lava) {
-                        Cell o2 = create_tile(c, mt->id_obsidian);
-                        Cell oo = T.get(x + xx, y + yy);
-                        led_replace(c, oo, cell_df(T, oo), o2);
+                    if (T.id(x + xx, y + yy) == c.id_lava) {
+                        Cell o2 = create_tile(c, c.id_obsidian);
+                        led_replace_at(T, c, x + xx, y + yy, o2);
                         T.put(x + xx, y + yy, o2);
                         T.setvis(x + xx, y + yy);
                     }
@@ -518,11 +589,11 @@ __device__ void rule_a(const Tile &T, Ctx &c, int x, int y) {
             return;
         }
     } else if (type == T_GAS) {  // world.cpp:1569-1585
-        int above = T.type(x, y - 1);
-        int aboveL = T.type(x - 1, y - 1);
-        int aboveR = T.type(x + 1, y - 1);
+        const int above = T.type(x, y - 1);
+        const int aboveL = T.type(x - 1, y - 1);
+        const int aboveR = T.type(x + 1, y - 1);
         if (above == T_AIR && !((aboveL == T_AIR || aboveR == T_AIR) && c.D() % 2 == 0)) {
-            T.put(x, y, T.get(x, y - 1));
+            T.move(x, y, x, y - 1);
             T.put(x, y - 1, t);
             T.setvis(x, y - 1);
         }
@@ -530,30 +601,25 @@ __device__ void rule_a(const Tile &T, Ctx &c, int x, int y) {
 }
 
 // ----------------------------------------------------------------- sweep B
-__device__ void rule_b(const Tile &T, Ctx &c, int x, int y) {
+__device__ __forceinline__ void rule_b(const Tile &T, Ctx &c, int x, int y) {
     if (T.vis(x, y)) return;  // world.cpp:1597
     const uint32_t *ma = T.ma;
     const float *md = T.md;
-    int sid = T.id(x, y);
-    uint32_t a = ma[sid];
-    int type = mt_type(a);
+    const int sid = T.id(x, y);
+    const uint32_t a = ma[sid];
+    const int type = mt_type(a);
     if (type != T_SAND && type != T_SOUP && type != T_GAS) return;
     Cell t = T.get_active(x, y);
     c.ck = cell_key(c.pk, (uint32_t)x, (uint32_t)y);
     c.k = 0;
     if (type == T_SAND) {  // world.cpp:1602-1727
-        Cell bl = T.get(x - 1, y + 1), br = T.get(x + 1, y + 1);
-        bool canL = can_sink(ma, md, bl.id, t.id);
-        bool canR = can_sink(ma, md, br.id, t.id);
+        const bool canL = can_sink(ma, md, T.id(x - 1, y + 1), sid);
+        const bool canR = can_sink(ma, md, T.id(x + 1, y + 1), sid);
         bool stopped = !(t.fl & MOVED);
-        int slip = mt_slip(a);
+        const int slip = mt_slip(a);
         if (stopped) {
-            int drop = 0;
-            for (int pil = 0; pil < 10; pil++) {
-                int l = T.type(x - 1, y + 1 + pil);
-                int r = T.type(x + 1, y + 1 + pil);
-                if (l == T_AIR || r == T_AIR) drop++;
-            }
+            // world.cpp:1619-1627 over the AIR snapshot taken when sweep B began
+            const int drop = __popc(T.air10(x - 1, y + 1) | T.air10(x + 1, y + 1));
             int d = drop + 1 - mt_stab(a);
             if (d > 0) {
                 int chance = 1000 / d;
@@ -569,7 +635,7 @@ __device__ void rule_b(const Tile &T, Ctx &c, int x, int y) {
             T.set_moved(x, y, false);
             return;
         }
-        bool shouldMove = (slip > 0) ? (c.D() % (uint32_t)(2 * slip) != 0) : true;
+        const bool shouldMove = (slip > 0) ? (c.D() % (uint32_t)(2 * slip) != 0) : true;
         if (shouldMove && (canL || canR)) {
             if (c.D() % 2 == 0) {
                 if (T.type(x, y + 1) == T_SAND) {
@@ -579,11 +645,11 @@ __device__ void rule_b(const Tile &T, Ctx &c, int x, int y) {
         }
         if (shouldMove && canL && (!canR || c.D() % 2 == 0)) {
             if (T.type(x - 1, y) == T_AIR) {
-                T.put(x - 1, y, bl);
+                T.move(x - 1, y, x - 1, y + 1);
                 T.setvis(x - 1, y);
-                T.put(x, y, nothing(T.id_air));
+                T.set_nothing(x, y);
             } else {
-                T.put(x, y, bl);
+                T.move(x, y, x - 1, y + 1);
                 T.setvis(x, y);
             }
             if (slip > 0 && c.D() % (uint32_t)(20 * slip) == 0) t.fl &= (uint8_t)~MOVED;
@@ -591,10 +657,10 @@ __device__ void rule_b(const Tile &T, Ctx &c, int x, int y) {
             T.setvis(x - 1, y + 1);
         } else if (shouldMove && canR) {
             if (T.type(x + 1, y) == T_AIR) {
-                T.put(x + 1, y, br);
-                T.put(x, y, nothing(T.id_air));
+                T.move(x + 1, y, x + 1, y + 1);
+                T.set_nothing(x, y);
             } else {
-                T.put(x, y, br);
+                T.move(x, y, x + 1, y + 1);
                 T.setvis(x, y);
             }
             if (slip > 0 && c.D() % (uint32_t)(20 * slip) == 0) t.fl &= (uint8_t)~MOVED;
@@ -604,26 +670,26 @@ __device__ void rule_b(const Tile &T, Ctx &c, int x, int y) {
             T.set_moved(x, y, false);
         }
     } else if (type == T_SOUP) {  // world.cpp:1728-1745
-        t.sc += t.df;
+        t.sc += T.df_load(x, y);
         t.df = 0;
         if (t.sc < Q_MINV) {
             led_add(c, LED_DN, t.id, 1);
             led_add(c, LED_DF, t.id, t.sc);
-            T.put(x, y, nothing(T.id_air));
+            T.set_nothing(x, y);
             T.setvis(x, y);
         } else {
             T.put(x, y, t);
             T.setvis(x, y);
         }
     } else {  // GAS, world.cpp:1799-1818
-        int aboveL = T.type(x - 1, y - 1);
-        int aboveR = T.type(x + 1, y - 1);
+        const int aboveL = T.type(x - 1, y - 1);
+        const int aboveR = T.type(x + 1, y - 1);
         if (aboveL == T_AIR && !(aboveR == T_AIR && c.D() % 2 == 0)) {
-            T.put(x, y, T.get(x - 1, y - 1));
+            T.move(x, y, x - 1, y - 1);
             T.put(x - 1, y - 1, t);
             T.setvis(x - 1, y - 1);
         } else if (aboveR == T_AIR) {
-            T.put(x, y, T.get(x + 1, y - 1));
+            T.move(x, y, x + 1, y - 1);
             T.put(x + 1, y - 1, t);
             T.setvis(x + 1, y - 1);
         }
@@ -631,28 +697,28 @@ __device__ void rule_b(const Tile &T, Ctx &c, int x, int y) {
 }
 
 // ----------------------------------------------------------------- sweep C
-__device__ void rule_c(const Tile &T, Ctx &c, int x, int y) {
+__device__ __forceinline__ void rule_c(const Tile &T, Ctx &c, int x, int y) {
     if (T.vis(x, y)) return;  // world.cpp:1831
-    int sid = T.id(x, y);
+    const int sid = T.id(x, y);
     if (mt_type(T.ma[sid]) != T_GAS) return;
     Cell t = T.get_active(x, y);
     c.ck = cell_key(c.pk, (uint32_t)x, (uint32_t)y);
     c.k = 0;
     // world.cpp:1862-1889
-    int l = T.type(x - 1, y);
-    int r = T.type(x + 1, y);
+    const int l = T.type(x - 1, y);
+    const int r = T.type(x + 1, y);
     if (l == T_AIR && !(r == T_AIR && c.D() % 2 == 0)) {
-        T.put(x, y, T.get(x - 1, y));
+        T.move(x, y, x - 1, y);
         T.put(x - 1, y, t);
         T.setvis(x - 1, y);
     } else if (r == T_AIR) {
-        T.put(x, y, T.get(x + 1, y));
+        T.move(x, y, x + 1, y);
         T.put(x + 1, y, t);
         T.setvis(x + 1, y);
-    } else if ((int)t.id == c.mt->id_steam) {
+    } else if (sid == c.id_steam) {
         if (c.D() % 10 == 0) {
-            Cell wt = create_tile(c, c.mt->id_water);
-            led_replace(c, t, 0, wt);
+            Cell wt = create_tile(c, c.id_water);
+            led_swap(c, t.id, 0, wt.id, (long long)wt.sc);
             T.put(x, y, wt);
         }
     }
@@ -673,8 +739,9 @@ __device__ __forceinline__ void lattice(int sweep, int mode, int &px, int &py) {
             py = 6;
         }
     } else if (sweep == 1) {
+        // the friction pillar reads the sweep-B snapshot, so only rows y-1..y+1 are live
         px = 3;
-        py = 12;
+        py = 3;
     } else {
         px = 3;
         py = 1;
@@ -710,7 +777,7 @@ __device__ __forceinline__ int block_excl_scan(int v, int *scratch, int *total) 
 }
 
 // write the particles of one spawn event (world.cpp:1110-1119,1222,1298)
-__device__ void emit_spawns(const WorldDev &w, const SpawnEv &ev, uint32_t cp, uint32_t rank0, int base) {
+__device__ __noinline__ void emit_spawns(const WorldDev &w, const SpawnEv &ev, uint32_t cp, uint32_t rank0, int base) {
     int32_t base_amt = 0, extra = 0;
     if (ev.kind == 2) {
         base_amt = ev.sc / ev.n;
@@ -764,47 +831,75 @@ __device__ void emit_spawns(const WorldDev &w, const SpawnEv &ev, uint32_t cp, u
 }
 
 // -------------------------------------------------------------- the kernel
+// shared memory besides the tile planes
+struct SmemHead {
+    uint32_t ma[MAXMAT];
+    float md[MAXMAT];
+    long long led[LED_ROWS * 64];
+    int scan[40];
+    uint8_t mreact[MAXMAT];
+    int cnt[CP_THREADS];  // sweep-A spawns per enumeration index, then their ranks
+    uint32_t air[(128 + 2) * 5];  // sweep-B pillar snapshot (chunk edge <= 128)
+};
+
 // items: (world << 20) | chunk slot within the colour; iter, tk select the pass.
 template <int HALO>
-__global__ void __launch_bounds__(1024, 1)
+__global__ void __launch_bounds__(CP_THREADS, 1)
     k_colour_pass(const WorldDev *__restrict__ worlds, const uint32_t *__restrict__ items, int n_items, int iter, int tk,
                   const MatTable *__restrict__ mt) {
     extern __shared__ __align__(16) unsigned char smem[];
-    uint32_t *s_ma = (uint32_t *)smem;                 // [MAXMAT]
-    float *s_md = (float *)(s_ma + MAXMAT);            // [MAXMAT]
-    long long *s_led = (long long *)(s_md + MAXMAT);   // [LED_ROWS * 64]
-    int *s_scan = (int *)(s_led + LED_ROWS * 64);      // [40]
-    unsigned char *planes = (unsigned char *)(s_scan + 40);
+    __shared__ WorldDev s_w;
+    SmemHead &S = *reinterpret_cast<SmemHead *>(smem);
+    unsigned char *planes = smem + ((sizeof(SmemHead) + 15) & ~(size_t)15);
 
-    const int tid = threadIdx.x, T = blockDim.x;
+    const int tid = threadIdx.x;
+    constexpr int T = CP_THREADS;
     for (int i = tid; i < MAXMAT; i += T) {
-        s_ma[i] = (i < mt->n) ? mt->a[i] : 0u;
-        s_md[i] = (i < mt->n) ? mt->density[i] : 0.f;
+        S.ma[i] = (i < mt->n) ? mt->a[i] : 0u;
+        S.md[i] = (i < mt->n) ? mt->density[i] : 0.f;
+        S.mreact[i] = (uint8_t)((i < mt->n) ? mt->n_react[i] : 0);
     }
-    for (int i = tid; i < LED_ROWS * 64; i += T) s_led[i] = 0;
+    for (int i = tid; i < LED_ROWS * 64; i += T) S.led[i] = 0;
+    Ctx c;
+    c.iter = iter;
+    c.mt = mt;
+    c.led_s = S.led;
+    c.ma = S.ma;
+    c.mreact = S.mreact;
+    c.id_fire = mt->id_fire;
+    c.id_water = mt->id_water;
+    c.id_lava = mt->id_lava;
+    c.id_steam = mt->id_steam;
+    c.id_obsidian = mt->id_obsidian;
+    c.has_inter = mt->has_inter;
+    const int id_solid = mt->id_solid, id_air = mt->id_air;
+    FSE_PT_DECL
     __syncthreads();
 
     const int ox = tk % 2, oy = 1 - tk / 2;
     long long *led_g_last = nullptr;
-    int32_t *err_last = nullptr;
 
     for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
         const uint32_t item = __ldg(&items[it]);
-        const WorldDev &w = worlds[item >> 20];
+        if (tid == 0) s_w = worlds[item >> 20];
+        __syncthreads();
+        FSE_PT(0)
+        const WorldDev &w = s_w;
         const int slot = (int)(item & 0xFFFFF);
         if (led_g_last != w.ledger && led_g_last != nullptr) {
             // flush the shared ledger before switching worlds
-            __syncthreads();
             for (int i = tid; i < LED_ROWS * 64; i += T) {
-                long long v = s_led[i];
+                long long v = S.led[i];
                 if (v) atomicAdd((unsigned long long *)&led_g_last[(i / 64) * MAXMAT + (i % 64)], (unsigned long long)v);
-                s_led[i] = 0;
+                S.led[i] = 0;
             }
             __syncthreads();
         }
         led_g_last = w.ledger;
-        err_last = w.err;
-        if (iter >= w.cell_iter) continue;
+        if (iter >= w.cell_iter) {
+            __syncthreads();
+            continue;
+        }
         const int C = w.C, W = w.W, H = w.H;
         const int nb = (w.nCy - oy + 1) / 2;
         const int cx = (ox + 2 * (slot / nb)) * C, cy = (oy + 2 * (slot % nb)) * C;
@@ -818,12 +913,16 @@ __global__ void __launch_bounds__(1024, 1)
         Tl.y0 = cy - HALO;
         Tl.W = W;
         Tl.H = H;
-        Tl.ma = s_ma;
-        Tl.md = s_md;
+        Tl.ma = S.ma;
+        Tl.md = S.md;
         Tl.df = w.df;
-        Tl.id_solid = mt->id_solid;
-        Tl.id_air = mt->id_air;
+        Tl.id_solid = id_solid;
+        Tl.id_air = id_air;
         Tl.err = w.err;
+        Tl.s_air = S.air;
+        Tl.ax0 = cx - 1;
+        Tl.ay0 = cy + 1;
+        Tl.aw = C + 2;
         const int nid = Tl.RW * Tl.RHI, nfull = Tl.RW * Tl.RHF;
         Tl.s_sc = (int32_t *)planes;
         Tl.s_col = (uint32_t *)(Tl.s_sc + nfull);
@@ -835,18 +934,19 @@ __global__ void __launch_bounds__(1024, 1)
         for (int i = tid; i < nid; i += T) {
             int ly = i / Tl.RW, lx = i - ly * Tl.RW;
             int gx = Tl.x0 + lx, gy = Tl.y0 + ly;
-            uint16_t v = (uint16_t)mt->id_solid;
+            uint16_t v = (uint16_t)id_solid;
             if ((unsigned)gx < (unsigned)W && (unsigned)gy < (unsigned)H) {
                 v = w.id[(size_t)gy * W + gx];
                 if (gx >= cx && gx < cx + C && gy >= cy && gy < cy + C) {
-                    if (mt_iter(s_ma[v]) > iter) active = 1;
-                    if ((int)v == mt->id_fire) fire = 1;
+                    if (mt_iter(S.ma[v]) > iter) active = 1;
+                    if ((int)v == c.id_fire) fire = 1;
                 }
             }
             Tl.s_id[i] = v;
         }
         active = __syncthreads_or(active);
         fire = __syncthreads_or(fire);
+        FSE_PT(1)
         if (!active) {
             // every chunk cell has iterations <= iter: the pass only marks cells visited
             if (tid == 0) w.cp_count[cp] = 0;
@@ -868,51 +968,79 @@ __global__ void __launch_bounds__(1024, 1)
             }
         }
         __syncthreads();
+        FSE_PT(2)
 
-        const int mode = mt->has_inter ? 2 : (fire ? 1 : 0);
+        const int mode = c.has_inter ? 2 : (fire ? 1 : 0);
         const int cw = min(C, W - cx), chh = min(C, H - cy);
-        int running = 0;  // spawns emitted so far by this chunk-pass (thread 0's view is authoritative)
-        Ctx c;
-        c.iter = iter;
-        c.mt = mt;
-        c.led_s = s_led;
+        int running = 0;  // spawns emitted so far by this chunk-pass
         c.led_g = w.ledger;
-        c.ma = s_ma;
         for (int sweep = 0; sweep < 3; sweep++) {
             c.pk = pass_key(w.seed, *w.tick, (uint32_t)(iter * 3 + sweep));
+            if (sweep == 1) {
+                // AIR snapshot for the friction pillar: columns cx-1..cx+C, rows cy+1..cy+C+9
+                for (int task = tid; task < (C + 2) * 5; task += T) {
+                    const int sx = task / 5, wi = task - sx * 5;
+                    uint32_t bits = 0;
+                    for (int b = 0; b < 32; b++) {
+                        const int sy = wi * 32 + b;
+                        if (sy < C + 9) {
+                            const int gx = cx - 1 + sx, gy = cy + 1 + sy;
+                            if (Tl.inw(gx, gy) && Tl.type(gx, gy) == T_AIR) bits |= 1u << b;
+                        }
+                    }
+                    S.air[task] = bits;
+                }
+                __syncthreads();
+            }
             int px, py;
             lattice(sweep, mode, px, py);
             for (int ry = py - 1; ry >= 0; ry--) {
                 for (int rx = 0; rx < px; rx++) {
                     const int nx = (C - rx + px - 1) / px, ny = (C - ry + py - 1) / py;
                     const int total = nx * ny;
-                    for (int base = 0; base < total; base += T) {
-                        const int i = base + tid;
+                    if (sweep == 0) {
+                        // sweep A sub-phases have at most 43 x 22 <= T cells: one per thread,
+                        // so every spawn event stays in its thread until it is ranked
+                        const int e = tid;
                         c.ev.n = 0;
-                        if (i < total) {
-                            const int dy = ry + (i / nx) * py, dx = rx + (i % nx) * px;
+                        S.cnt[tid] = 0;
+                        if (e < total) {
+                            const int dy = ry + (e / nx) * py, dx = rx + (e % nx) * px;
+                            if (dx < cw && dy < chh) rule_a(Tl, c, cx + dx, cy + dy);
+                        }
+                        FSE_PT(3)
+                        // rank spawned particles in enumeration order
+                        if (c.ev.n > 0) S.cnt[e] = c.ev.n;
+                        if (__syncthreads_or(c.ev.n > 0)) {
+                            int tot;
+                            int ex = block_excl_scan(S.cnt[tid], S.scan, &tot);
+                            S.cnt[tid] = ex;
+                            if (tid == 0) S.scan[36] = atomicAdd(w.stage_count, tot);
+                            __syncthreads();
+                            if (c.ev.n > 0) {
+                                int r = S.cnt[e];
+                                emit_spawns(w, c.ev, cp, (uint32_t)(running + r), S.scan[36] + r);
+                            }
+                            running += tot;
+                        }
+                        __syncthreads();
+                        FSE_PT(4)
+                    } else {
+                        // cells of one sub-phase never conflict: each thread takes all of its
+                        // cells in turn, one barrier per sub-phase
+                        for (int e = tid; e < total; e += T) {
+                            const int dy = ry + (e / nx) * py, dx = rx + (e % nx) * px;
                             if (dx < cw && dy < chh) {
-                                if (sweep == 0)
-                                    rule_a(Tl, c, cx + dx, cy + dy);
-                                else if (sweep == 1)
+                                if (sweep == 1)
                                     rule_b(Tl, c, cx + dx, cy + dy);
                                 else
                                     rule_c(Tl, c, cx + dx, cy + dy);
                             }
                         }
-                        if (sweep == 0) {
-                            if (__syncthreads_or(c.ev.n > 0)) {
-                                int tot;
-                                int ex = block_excl_scan(c.ev.n, s_scan, &tot);
-                                if (tid == 0) s_scan[36] = atomicAdd(w.stage_count, tot);
-                                __syncthreads();
-                                int gbase = s_scan[36];
-                                if (c.ev.n > 0) emit_spawns(w, c.ev, cp, (uint32_t)(running + ex), gbase + ex);
-                                running += tot;
-                            }
-                        }
+                        FSE_PT(3 + 2 * sweep)
+                        __syncthreads();
+                        FSE_PT(4 + 2 * sweep)
                     }
-                    __syncthreads();
                 }
             }
         }
@@ -933,45 +1061,58 @@ __global__ void __launch_bounds__(1024, 1)
         }
         if (tid == 0) w.cp_count[cp] = running;
         __syncthreads();
+        FSE_PT(9)
     }
-    (void)err_last;
     if (led_g_last) {
         __syncthreads();
         for (int i = tid; i < LED_ROWS * 64; i += T) {
-            long long v = s_led[i];
+            long long v = S.led[i];
             if (v) atomicAdd((unsigned long long *)&led_g_last[(i / 64) * MAXMAT + (i % 64)], (unsigned long long)v);
         }
     }
+    FSE_PT_FLUSH
 }
 
 size_t colour_pass_smem(int C, int halo) {
     size_t RW = (size_t)C + 2 * halo, RHF = (size_t)C + 2 * halo, RHI = (size_t)C + halo + 10;
     size_t nid = RW * RHI, nfull = RW * RHF;
-    size_t head = MAXMAT * 4 + MAXMAT * 4 + LED_ROWS * 64 * 8 + 40 * 4;
+    size_t head = (sizeof(SmemHead) + 15) & ~(size_t)15;
     return head + nfull * 4 + nfull * 4 + ((nid + 1) & ~(size_t)1) * 2 + nfull;
+}
+
+template <int HALO>
+static cudaError_t launch_t(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
+                            const MatTable *mt, size_t sm, int grid, cudaStream_t s) {
+    // opt in to the full shared-memory carve-out once per instantiation
+    static size_t set = 0;
+    if (set < sm) {
+        cudaFuncSetAttribute(k_colour_pass<HALO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        set = sm;
+    }
+    k_colour_pass<HALO><<<grid, CP_THREADS, sm, s>>>(worlds, items, n_items, iter, tk, mt);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_colour_pass(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
                                const MatTable *mt, int halo, int C, int threads, int grid, cudaStream_t s) {
+    (void)threads;  // the colour pass always runs CP_THREADS threads (see above)
     size_t sm = colour_pass_smem(C, halo);
     if (n_items <= 0) return cudaSuccess;
     if (grid <= 0 || grid > n_items) grid = n_items;
-    // opt in to the full shared-memory carve-out once per process
-    static size_t set5 = 0, set2 = 0;
-    if (halo == 5) {
-        if (set5 < sm) {
-            cudaFuncSetAttribute(k_colour_pass<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-            set5 = sm;
-        }
-        k_colour_pass<5><<<grid, threads, sm, s>>>(worlds, items, n_items, iter, tk, mt);
-    } else {
-        if (set2 < sm) {
-            cudaFuncSetAttribute(k_colour_pass<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-            set2 = sm;
-        }
-        k_colour_pass<2><<<grid, threads, sm, s>>>(worlds, items, n_items, iter, tk, mt);
-    }
-    return cudaGetLastError();
+    if (halo == 5) return launch_t<5>(worlds, items, n_items, iter, tk, mt, sm, grid, s);
+    return launch_t<2>(worlds, items, n_items, iter, tk, mt, sm, grid, s);
 }
 
 }  // namespace fse
+
+#ifdef FSE_PHASE_CLOCKS
+extern "C" int fse_debug_phase_clocks(unsigned long long out[16], int reset) {
+    cudaDeviceSynchronize();
+    cudaMemcpyFromSymbol(out, g_phase_clk, 16 * sizeof(unsigned long long));
+    if (reset) {
+        unsigned long long z[16] = {0};
+        cudaMemcpyToSymbol(g_phase_clk, z, sizeof(z));
+    }
+    return 0;
+}
+#endif

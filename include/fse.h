@@ -151,6 +151,9 @@ int fse_world_tick(fse_world *world, int n_ticks);
 int fse_particles_tick(fse_world *world);
 /* the game-loop order: n x (world::tick(); world::tickCells()) */
 int fse_world_step(fse_world *world, int n_ticks);
+/* enqueue n_ticks steps (with_particles != 0) or ticks on the world's stream and
+ * return without waiting; fse_world_sync() waits and reports kernel errors */
+int fse_world_enqueue(fse_world *world, int n_ticks, int with_particles);
 /* record n_ticks steps into a CUDA graph once and replay it: same results as
  * fse_world_step, fewer launches */
 int fse_world_step_graph(fse_world *world, int n_ticks);
@@ -172,6 +175,14 @@ int fse_object_readback(fse_world *world, fse_body *bodies, int n, int64_t *out_
 int fse_object_mask_export(fse_world *world, uint8_t *host_bits);
 /* compact list of OBJECT cell indices (y*w+x, ascending); *out_n = count (may exceed cap) */
 int fse_object_list_export(fse_world *world, uint32_t *host_idx, int64_t cap, int64_t *out_n);
+
+/* ------------------------------------------------------------ diagnostics */
+/* Time every colour-pass launch of this world with CUDA events on its stream.
+ * enable = 1 starts (and zeroes) the timer, 0 stops it; both first report the
+ * accumulated kernel milliseconds and launch count since the last start. */
+int fse_world_pass_timing(fse_world *world, int enable, double *out_ms, int64_t *out_launches);
+/* kernels this library has launched so far (all worlds, batches and servers) */
+int64_t fse_launch_counter(void);
 
 /* ----------------------------------------------------------------- ledger */
 /* 6 rows x fse_material_count(): created_n, destroyed_n, exited_n, created_f,

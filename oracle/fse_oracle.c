@@ -523,7 +523,19 @@ typedef struct {
     int iter;
     pvec *spawn; /* particles spawned by this chunk-pass, in order */
     int64_t (*led)[MAXMAT];
+    /* partitioned order only: AIR-ness of the cells below the chunk as they stood
+     * when sweep B began, for the friction pillar (NULL: read the live grid) */
+    const uint8_t *snap;
+    int snap_x0, snap_y0, snap_w, snap_h;
 } rctx;
+
+/* the pillar cell (x, y) is AIR: in the snapshot when there is one, else live */
+static inline int pillar_air(rctx *c, int x, int y) {
+    if (!c->snap) return gtype(c->w, x, y) == T_AIR;
+    int sx = x - c->snap_x0, sy = y - c->snap_y0;
+    if (sx < 0 || sy < 0 || sx >= c->snap_w || sy >= c->snap_h) return 0;
+    return c->snap[sy * c->snap_w + sx];
+}
 
 static inline uint32_t D(rctx *c) { return draw_k(c->ck, c->k++); }
 
@@ -910,9 +922,7 @@ static void rule_b(rctx *c, int x, int y) {
         if (stopped) {
             int drop = 0;
             for (int pil = 0; pil < 10; pil++) {
-                int l = gtype(w, x - 1, y + 1 + pil);
-                int r = gtype(w, x + 1, y + 1 + pil);
-                if (l == T_AIR || r == T_AIR) drop++;
+                if (pillar_air(c, x - 1, y + 1 + pil) || pillar_air(c, x + 1, y + 1 + pil)) drop++;
             }
             int d = drop + 1 - m->max_stab;
             if (d > 0) {
@@ -1049,8 +1059,9 @@ static void lattice(int sweep, int mode, int *px, int *py) {
             *py = 6;
         }
     } else if (sweep == 1) {
+        /* the friction pillar reads a snapshot, so only rows y-1..y+1 are live */
         *px = 3;
-        *py = 12;
+        *py = 3;
     } else {
         *px = 3;
         *py = 1;
@@ -1079,8 +1090,28 @@ static void process_chunk(om_world *w, int order, int iter, int cx, int cy, pvec
     int x1 = cx + w->C < w->W ? cx + w->C : w->W, y1 = cy + w->C < w->H ? cy + w->C : w->H;
     rule_fn rules[3] = {rule_a, rule_b, rule_c};
     int mode = (order == OM_ORDER_PART) ? chunk_mode(w, cx, cy) : MODE_NARROW;
+    /* pillar snapshot region: columns cx-1 .. cx+C, rows cy+1 .. cy+C+9 */
+    uint8_t *snap = NULL;
+    c.snap_x0 = cx - 1;
+    c.snap_y0 = cy + 1;
+    c.snap_w = w->C + 2;
+    c.snap_h = w->C + 9;
     for (int sweep = 0; sweep < 3; sweep++) {
         c.pk = pass_key(w->seed, w->tick, (uint32_t)(iter * 3 + sweep));
+        if (sweep == 1 && order == OM_ORDER_PART) {
+            /* partitioned order: the friction pillar of world.cpp:1619-1627 reads the
+             * AIR cells as they stood when sweep B began */
+            snap = (uint8_t *)malloc((size_t)c.snap_w * c.snap_h);
+            for (int sy = 0; sy < c.snap_h; sy++)
+                for (int sx = 0; sx < c.snap_w; sx++) {
+                    int gx = c.snap_x0 + sx, gy = c.snap_y0 + sy;
+                    snap[sy * c.snap_w + sx] =
+                        (uint8_t)(inw(w, gx, gy) && M[w->id[(size_t)gy * w->W + gx]].type == T_AIR);
+                }
+            c.snap = snap;
+        } else {
+            c.snap = NULL;
+        }
         if (order == OM_ORDER_SEQ) {
             /* world.cpp:1084-1087 (and 1589, 1823): bottom-to-top, left-to-right */
             for (int y = y1 - 1; y >= cy; y--)
@@ -1099,6 +1130,7 @@ static void process_chunk(om_world *w, int order, int iter, int cx, int cy, pvec
                 }
         }
     }
+    free(snap);
 }
 
 long om_world_tick(om_world *w, int order, int check_races) {

@@ -1,0 +1,291 @@
+"""GPU parity of the remaining hot-path features against the CPU oracle: fire and
+reactions, material interactions (wide halo), scripted materials, free particles
+(bit-exact FP32 and within 1e-5 of FP64), CUDA-graph replay, batches, the
+autotuner, rigid OBJECT stamping/readback/export and the serving loop."""
+import numpy as np
+import pytest
+
+from helpers import compare_particles, compare_states, material_types
+
+pytestmark = pytest.mark.gpu
+PART = 1
+
+
+def _pair(fse, oracle_mod, w, h, seed, kind=1):
+    world = fse.World(w, h, chunk_size=128, cell_iter=3, seed=seed)
+    world.generate(kind, seed)
+    ow = oracle_mod.OracleWorld(w, h, 128, 3, seed)
+    ow.generate({1: 0, 2: 1}[kind], seed)
+    return world, ow
+
+
+def _sprinkle(fse, state, seed, specs):
+    rng = np.random.default_rng(seed)
+    for name, frac, scalar in specs:
+        m = fse.material_find(name)
+        pick = rng.random(state["id"].shape) < frac
+        state["id"][pick] = m
+        state["scalar"][pick] = scalar
+        state["colour"][pick] = 0x00ABCDEF
+        state["flags"][pick] = 0
+        state["diff"][pick] = 0
+    return state
+
+
+def _run_both(fse, oracle_mod, world, ow, steps, what):
+    types = material_types(fse)
+    for t in range(steps):
+        world.step(1)
+        ow.step(1, PART)
+        compare_states(world.state(), ow.state(), types, "%s step %d" % (what, t))
+        compare_particles(world.particles(), ow.particles(), "%s step %d" % (what, t))
+
+
+def test_fire_lava_steam_reactions(fse, oracle_mod):
+    world, ow = _pair(fse, oracle_mod, 256, 192, 31)
+    s = _sprinkle(fse, world.state(), 3, [("FIRE", 0.02, 0), ("LAVA", 0.03, 2 * 65536), ("STEAM", 0.03, 0),
+                                           ("GOLD_ORE", 0.02, 600), ("COBBLE_STONE", 0.05, 0)])
+    world.upload(s)
+    ow.set_state(s)
+    _run_both(fse, oracle_mod, world, ow, 6, "fire")
+    np.testing.assert_array_equal(world.ledger(), ow.ledger())
+
+
+def test_interactions_use_the_wide_halo(fse, oracle_mod):
+    o = oracle_mod.Oracle()
+    sand, dirt, water, stone = (fse.material_find(n) for n in ("GENERIC_SAND", "DIRT", "WATER", "STONE"))
+    try:
+        fse.set_interaction(sand, water, 1, dirt, 2, 1, 2)
+        fse.set_interaction(sand, stone, 2, water, 1, -2, 0)
+        assert o.set_interaction(sand, water, 1, dirt, 2, 1, 2) == 0
+        assert o.set_interaction(sand, stone, 2, water, 1, -2, 0) == 0
+        fse.PushMaterials()
+        world, ow = _pair(fse, oracle_mod, 256, 256, 8)
+        _run_both(fse, oracle_mod, world, ow, 4, "interactions")
+    finally:
+        fse.InitMaterials()
+        fse.PushMaterials()
+        o.reset_materials()
+
+
+def test_lua_registered_material(fse, oracle_mod):
+    o = oracle_mod.Oracle()
+    script = """
+    -- materials registered from a script, as data/scripts would
+    materials_register(2001, "Heavy Sand", "HEAVY_SAND", 2, 12, 255, 30.5, 2, 0, 0, 0xFFAA3300)
+    materials_register(2002, 'Oil', 'OIL', 3, 0, 0x80, 0.8, 5, 0, 0, 0xFF202020)
+    """
+    try:
+        assert fse.load_lua_materials(script) == 2
+        hs = o.register(2001, "Heavy Sand", "HEAVY_SAND", 2, 12, 255, 30.5, 2, 0, 0, 0xFFAA3300)
+        oil = o.register(2002, "Oil", "OIL", 3, 0, 0x80, 0.8, 5, 0, 0, 0xFF202020)
+        assert (hs, oil) == (fse.material_find("HEAVY_SAND"), fse.material_find("OIL"))
+        for i in range(fse.material_count()):
+            np.testing.assert_array_equal(fse.material_get(i), o.material(i))
+        fse.PushMaterials()
+        world, ow = _pair(fse, oracle_mod, 192, 192, 12)
+        s = _sprinkle(fse, world.state(), 5, [("HEAVY_SAND", 0.1, 0), ("OIL", 0.1, 65536)])
+        world.upload(s)
+        ow.set_state(s)
+        _run_both(fse, oracle_mod, world, ow, 5, "lua")
+    finally:
+        fse.InitMaterials()
+        fse.PushMaterials()
+        o.reset_materials()
+
+
+def _particles(fse, n, w, h, seed, temporary=False):
+    rng = np.random.default_rng(seed)
+    p = np.zeros(n, fse.PARTICLE_DTYPE)
+    p["x"] = rng.uniform(0, w, n).astype(np.float32)
+    p["y"] = rng.uniform(0, h, n).astype(np.float32)
+    p["vx"] = rng.normal(0, 2, n).astype(np.float32)
+    p["vy"] = rng.normal(0, 2, n).astype(np.float32)
+    p["ay"] = np.float32(0.1)
+    p["fade_time"] = 60
+    p["id"] = fse.material_find("GENERIC_SAND")
+    p["colour"] = 0xFFFFFFFF
+    if temporary:
+        p["bits"][::7] = 2
+        p["lifetime"][::7] = rng.integers(0, 5, len(p["lifetime"][::7]))
+    return p
+
+
+def test_free_particles_bit_exact(fse, oracle_mod):
+    world, ow = _pair(fse, oracle_mod, 512, 384, 77)
+    p = _particles(fse, 40000, 512, 384, 1, temporary=True)
+    water = fse.material_find("WATER")
+    p["id"][1::5] = water
+    p["scalar"][1::5] = 65536 * 3
+    world.addCell(p)
+    ow.set_particles(p)
+    _run_both(fse, oracle_mod, world, ow, 6, "particles")
+
+
+def test_particles_within_1e5_of_fp64(fse, oracle_mod):
+    """One tickCells() of free-flying particles vs the FP64 kinematics oracle."""
+    world = fse.World(512, 512, seed=3)  # an empty world: no collisions
+    ow = oracle_mod.OracleWorld(512, 512, 128, 3, 3)
+    p = _particles(fse, 20000, 512, 512, 9)
+    p["x"] = np.clip(p["x"], 64, 448)
+    p["y"] = np.clip(p["y"], 64, 448)
+    world.addCell(p)
+    world.tickCells()
+    g = world.particles()
+    ref, ev, _ = ow.kinematics(p, f64=True)
+    alive = ev == 0
+    assert alive.sum() == len(g)
+    ref = ref[alive]
+    got = np.stack([g["x"], g["y"], g["vx"], g["vy"]], 1).astype(np.float64)
+    rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1.0)
+    assert rel.max() <= 1e-5, rel.max()
+
+
+def test_graph_replay_equals_plain_steps(fse):
+    a = fse.World(384, 256, seed=5)
+    b = fse.World(384, 256, seed=5)
+    a.generate(fse.GEN_MIX, 5)
+    b.generate(fse.GEN_MIX, 5)
+    a.step(40)
+    b.step(40, graph=True)
+    sa, sb = a.state(), b.state()
+    for k in sa:
+        np.testing.assert_array_equal(sa[k], sb[k], err_msg=k)
+    assert a.particles().tobytes() == b.particles().tobytes()
+    assert a.tick_count == b.tick_count == 40
+
+
+def test_batch_equals_individual_worlds(fse):
+    sizes = [(128, 192), (320, 128), (256, 256), (192, 448), (512, 320)]
+    solo = []
+    for i, (w, h) in enumerate(sizes):
+        x = fse.World(w, h, seed=100 + i)
+        x.generate(fse.GEN_MIX, 100 + i)
+        x.step(9)
+        solo.append(x)
+    worlds = []
+    for i, (w, h) in enumerate(sizes):
+        x = fse.World(w, h, seed=100 + i)
+        x.generate(fse.GEN_MIX, 100 + i)
+        worlds.append(x)
+    b = fse.Batch(worlds)
+    b.step(4)
+    b.step(5, graph_ticks=3)
+    for x, y in zip(solo, worlds):
+        sx, sy = x.state(), y.state()
+        for k in sx:
+            np.testing.assert_array_equal(sx[k], sy[k], err_msg=k)
+        assert x.particles().tobytes() == y.particles().tobytes()
+    b.close()
+
+
+def test_autotune_never_changes_results(fse):
+    ref = fse.World(384, 384, seed=44)
+    ref.generate(fse.GEN_MIX, 44)
+    ref.step(6)
+    w = fse.World(384, 384, seed=44)
+    w.generate(fse.GEN_MIX, 44)
+    b = fse.Batch([w])
+    choice = b.autotune()
+    assert choice["threads"] in (256, 512, 1024)
+    assert w.tick_count == 0  # the autotuner restored the world
+    b.step(6)
+    sr, sw = ref.state(), w.state()
+    for k in sr:
+        np.testing.assert_array_equal(sr[k], sw[k], err_msg=k)
+    b.close()
+
+
+def _boxes(fse, n, w, h, seed):
+    rng = np.random.default_rng(seed)
+    b = np.zeros(n, fse.BODY_DTYPE)
+    b["w"] = rng.integers(8, 65, n)
+    b["h"] = rng.integers(8, 65, n)
+    b["x"] = rng.uniform(0, w - 8, n).astype(np.float32)
+    b["y"] = rng.uniform(0, h - 8, n).astype(np.float32)
+    b["cos_a"] = 1.0
+    b["id"] = fse.material_find("GENERIC_OBJECT")
+    b["colour"] = 0xFF00FF00
+    return b
+
+
+def test_object_stamp_readback_and_mask(fse, oracle_mod):
+    types = material_types(fse)
+    world, ow = _pair(fse, oracle_mod, 512, 512, 9, kind=2)
+    bodies = _boxes(fse, 30, 512, 512, 4)
+    # one rotated body as well
+    bodies[0]["sin_a"], bodies[0]["cos_a"] = np.float32(np.sin(0.5)), np.float32(np.cos(0.5))
+    ob = bodies.copy()
+    for t in range(3):
+        world.object_stamp(bodies)
+        ow.object_stamp(ob)
+        for f in ("n_sand", "n_soup", "n_placed"):
+            np.testing.assert_array_equal(bodies[f], ob[f], err_msg=f)
+        compare_states(world.state(), ow.state(), types, "stamp %d" % t)
+        compare_particles(world.particles(), ow.particles(), "stamp %d" % t)
+        world.step(1)
+        ow.step(1, PART)
+        np.testing.assert_array_equal(world.object_mask(), ow.object_mask())
+        lst, n = world.object_list()
+        bits = np.unpackbits(ow.object_mask(), bitorder="little")[: 512 * 512]
+        np.testing.assert_array_equal(lst, np.nonzero(bits)[0].astype(np.uint32))
+        assert n == len(lst)
+        rg = world.object_readback(bodies)
+        ro = ow.object_readback(ob)
+        assert rg == ro
+        np.testing.assert_array_equal(bodies["n_recovered"], ob["n_recovered"])
+        compare_states(world.state(), ow.state(), types, "readback %d" % t)
+
+
+def test_serving_alone_equals_in_the_mix(fse):
+    sizes = [(256, 256), (384, 256), (256, 512)]
+    srv = fse.Server(8 << 30, max_active=8)
+    slots = [srv.add_world(w, h, fse.GEN_MIX, 500 + i, seed=500 + i) for i, (w, h) in enumerate(sizes)]
+    reqs = [(slots[0], 5), (slots[1], 3), (slots[2], 7), (slots[0], 2), (slots[1], 4)]
+    for s, n in reqs:
+        srv.submit(s, n)
+    done = 0
+    for _ in range(200):
+        srv.step()
+        ids, _ = srv.poll()
+        done += len(ids)
+        if done == len(reqs):
+            break
+    assert done == len(reqs)
+    ticks = {slots[0]: 7, slots[1]: 7, slots[2]: 7}
+    for i, (w, h) in enumerate(sizes):
+        alone = fse.World(w, h, seed=500 + i)
+        alone.generate(fse.GEN_MIX, 500 + i)
+        alone.step(ticks[slots[i]])
+        mixed = srv.world(slots[i])
+        sa, sm = alone.state(), mixed.state()
+        for k in sa:
+            np.testing.assert_array_equal(sa[k], sm[k], err_msg="world %d %s" % (i, k))
+        assert alone.particles().tobytes() == mixed.particles().tobytes()
+    srv.close()
+
+
+def test_serving_admission_respects_the_budget(fse):
+    srv = fse.Server(64 << 20, max_active=4)
+    assert srv.try_add_world(256, 256) is not None
+    assert srv.try_add_world(4096, 4096) is None  # refused by the HBM budget
+    assert srv.bytes_in_use() <= 64 << 20
+    srv.close()
+
+
+def test_world_api_roundtrip(fse):
+    w = fse.World(200, 136, seed=1)
+    w.generate(fse.GEN_MIX, 1)
+    s = w.state()
+    t = w.getTile(5, 7)
+    assert (t.id, t.colour) == (int(s["id"][7, 5]), int(s["colour"][7, 5]))
+    assert w.getTile(-1, 0).id == fse.material_find("GENERIC_SOLID")  # world.cpp:1000
+    w.setTile(5, 7, fse.MaterialInstance(fse.material_find("WATER"), 0x1234, 65536, 0))
+    w.setTile(500, 7, fse.MaterialInstance(1))  # dropped, world.cpp:1005
+    assert w.getTile(5, 7).scalar == 65536
+    w.tick_count = 17
+    assert w.tick_count == 17
+    bad = dict(s)
+    bad["id"] = np.full_like(s["id"], 999)
+    with pytest.raises(fse.FseError):
+        w.upload(bad)

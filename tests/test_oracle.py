@@ -77,7 +77,7 @@ def test_race_checker_catches_a_planted_small_lattice(oracle_mod):
         o.debug_set_lattice(0, 2, 6)
         ow = _world(oracle_mod, 256, 256, 3)
         assert ow.tick(PART, check_races=True) > 0
-        o.debug_set_lattice(1, 3, 6)
+        o.debug_set_lattice(1, 3, 2)  # sweep B needs 3 rows between cells of a column
         o.debug_set_lattice(0, 0, 0)
         ow = _world(oracle_mod, 256, 256, 3)
         assert ow.tick(PART, check_races=True) > 0
