@@ -76,6 +76,7 @@ SIGNATURES = {
     "fse_world_ledger": (_i, [_vp, _vp]),
     "fse_world_ledger_reset": (_i, [_vp]),
     "fse_world_census": (_i, [_vp, _vp]),
+    "fse_tick_noalloc": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _u32, _u32, _vp, _i, C.POINTER(_i), _vp]),
     "fse_batch_create": (_i, [_vp, _i, _pp]),
     "fse_batch_destroy": (_i, [_vp]),
     "fse_batch_step": (_i, [_vp, _i]),

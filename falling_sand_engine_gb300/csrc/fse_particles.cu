@@ -560,6 +560,12 @@ static void spiral_upload() {
 
 void particle_prepare() { spiral_upload(); }
 
+// the per-chunk-pass spawn offsets alone (the allocation-free tick writes its own output)
+cudaError_t launch_spawn_scan(WorldDev *d_worlds, int n_worlds, cudaStream_t s) {
+    k_spawn_scan<<<n_worlds, 1024, 0, s>>>(d_worlds);
+    return cudaGetLastError();
+}
+
 // this tick's spawns -> end of the particle list, then the tick counter
 cudaError_t launch_spawn_append(WorldDev *d_worlds, int n_worlds, int stage_blocks, cudaStream_t s) {
     k_spawn_scan<<<n_worlds, 1024, 0, s>>>(d_worlds);

@@ -192,6 +192,33 @@ int fse_world_ledger_reset(fse_world *world);
 /* 4 rows: grid_count, grid_fluid (amount + pending diff), part_count, part_fluid */
 int fse_world_census(fse_world *world, int64_t *out);
 
+/* ------------------------------------------------- allocation-free tick */
+/* One world::tick() (no particle step) on cell planes the caller owns in device
+ * memory, for hosts that cannot let a library allocate device memory: engines
+ * that serve every byte from their own arena under their own budget, and
+ * real-time loops that forbid cudaMalloc/cudaFree after start-up because those
+ * calls can stall the device and can fail under memory pressure mid-frame.
+ * No counterpart in the reference (its tick allocates per-task particle lists).
+ *
+ * id/colour/scalar/flags/diff: device planes of width*height cells, updated in
+ * place. out_spawned: device array of spawn_cap particles that receives the
+ * particles this tick spawns, in the order fse_world_tick would append them;
+ * *out_n_spawned = their number (FSE_E_CAPACITY when more than spawn_cap).
+ * tick: the world's tick count (keys the counter RNG; the caller advances it).
+ * Results equal fse_world_tick's bit for bit.
+ *
+ * Scratch: one fixed device array of about 4 MB inside the library, held by every
+ * GPU that loads it until the process exits. Limits: at most 4096 chunks per
+ * colour (e.g. 8192 x 8192 cells at chunk 128), cell_iter <= 8, at most 65536
+ * particles spawned per tick; larger requests return FSE_E_INVAL. The first call
+ * on a device looks the array up (cudaGetSymbolAddress) and should be made before
+ * any stream capture. Every call shares the array: calls that overlap on the GPU
+ * (other streams, other host threads) race and must not be made. The call calls
+ * no cudaMalloc/cudaFree and returns after its work is done. */
+int fse_tick_noalloc(uint16_t *id, uint32_t *colour, int32_t *scalar, uint8_t *flags, int32_t *diff, int width,
+                     int height, int chunk_size, int cell_iter, uint32_t seed, uint32_t tick, fse_particle *out_spawned,
+                     int spawn_cap, int *out_n_spawned, void *stream);
+
 /* --------------------------------------------------------------- batches */
 /* Many worlds ticked by one launch per colour pass over the chunks of all worlds. */
 int fse_batch_create(fse_world **worlds, int n, fse_batch **out);
