@@ -28,6 +28,10 @@ sys.path.insert(0, ROOT)
 BYTES_PER_CELL_UPDATE = 22  # 11-byte SoA cell state read once and written once per tick
 METRIC = "Gcell-updates/s"
 L2_FLUSH_BYTES = 512 << 20
+REF_BUDGET_S = 90.0  # cap on the timed region of the CPU reference arm
+# ticks per workload: 512^2 world 1000, 4096x2048 world 500, 256 worlds 200,
+# 16384^2 world 100; the server workload is timed by its arrival window instead
+WORKLOAD_TICKS = {0: 1000, 1: 500, 2: 200, 3: 100, 4: 0}
 
 
 def peaks():
@@ -159,6 +163,7 @@ def bench_config1(args, rank, local_rank, world_size):
     clk = clocks.stop()
     launches = fse.launch_counter() - l0
     pass_ms, pass_n = world.pass_timing(False)
+    live_particles = world.particle_count()
     gpu_ms = sum(a.elapsed_time(b) for a, b in ev)
     gpu_ms = max_over_ranks(gpu_ms, world_size)
     barrier(world_size)
@@ -187,7 +192,8 @@ def bench_config1(args, rank, local_rank, world_size):
         "scaling": "weak", "vs_baseline": None, "dtype": "int32+f32", "data": "synthetic",
         "config": {"workload": "config1: one 4096x2048 world (mix: 30% sand, 20% water, 10% gas, 15% rock, 25% air in "
                                "the top 60%, 8 rock rows) + 1M free particles, plain per-world launch",
-                   "world": [W, H], "particles": NP, "chunk": 128, "cell_iter": 3, "seed": seed,
+                   "world": [W, H], "particles": NP, "particles_live_after": live_particles, "chunk": 128,
+                   "cell_iter": 3, "seed": seed,
                    "l2": "flushed between timed steps (512 MiB write outside the events)",
                    "parallelism": "one independent world per GPU" if world_size > 1 else "single GPU"},
         "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
@@ -288,18 +294,24 @@ def reference_arm(args, rank, world_size):
     ow = OracleWorld(W, H, 128, 3, 1234)
     ow.generate(0, 1234)
     ow.set_particles(_np_particles(1_000_000, W, H, 1234))
-    for _ in range(args.warmup):
+    # a step of the CPU tick takes about a second: warm up with at most 3 steps and
+    # time at most REF_BUDGET_S seconds of the K requested steps
+    warm = min(args.warmup, 3)
+    for _ in range(warm):
         ow.step(1, 0)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
+    n, t0 = 0, time.perf_counter()
+    while n < args.steps:
         ow.step(1, 0)
+        n += 1
+        if time.perf_counter() - t0 > REF_BUDGET_S:
+            break
     dt = time.perf_counter() - t0
-    value = W * H * args.steps / dt / 1e9
-    sample = "%d timed steps (tick + tickCells) of the 4096x2048 world with 1M particles after %d warm-up" % (
-        args.steps, args.warmup)
+    value = W * H * n / dt / 1e9
+    sample = ("%d timed steps (tick + tickCells) of the 4096x2048 world with 1M particles after %d warm-up "
+              "(%d requested; the timed region is capped at %.0f s)" % (n, warm, args.steps, REF_BUDGET_S))
     return {
         "impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": "Gcell/s", "n_gpus": world_size,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3),
+        "steps": n, "warmup": warm, "ms_per_step": round(dt * 1e3 / n, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+f32", "data": "synthetic",
         "config": {"workload": "config1: one 4096x2048 world + 1M free particles", "world": [W, H],
                    "particles": 1_000_000, "chunk": 128, "cell_iter": 3,
@@ -330,13 +342,16 @@ def _np_particles(n, w, h, seed):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: the workload's tick count, 500 for the default workload)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="fse", choices=["fse", "reference"])
     ap.add_argument("--workload", type=int, default=1, choices=[0, 1, 2, 3, 4])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.steps is None:
+        args.steps = WORKLOAD_TICKS[args.workload]
     rank, local_rank, world_size = dist_info()
 
     if args.impl == "reference":

@@ -314,7 +314,7 @@ int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], con
     count_launches(3);
     if (particles) {
         if (launch_particle_tick(d_worlds, n_worlds, g_dev_mt, move_blocks, s) != cudaSuccess) return FSE_E_CUDA;
-        count_launches(11);
+        count_launches(PARTICLE_TICK_LAUNCHES);
     }
     return FSE_OK;
 }
@@ -576,7 +576,7 @@ static void free_world(fse_world *w) {
     w->graphs.clear();
     WorldDev &h = w->h;
     void *ptrs[] = {h.id, h.col, h.sc, h.fl, h.df, h.stage, h.cp_count, h.cp_base, h.p_state, h.p_lxly,
-                    h.req_list, h.req_list2, h.req_target, h.scan_tmp, h.ledger, w->ctr, w->d, w->claim,
+                    h.req_list, h.req_list2, h.req_target, h.scan_tmp, h.ledger, h.airmap, w->ctr, w->d, w->claim,
                     w->mask_bits, w->obj_list, w->obj_n};
     for (void *q : ptrs)
         if (q) cudaFree(q);
@@ -660,6 +660,8 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
     h.max_slots = ceil_div(h.nCx, 2) * ceil_div(h.nCy, 2);
     h.stage_cap = c.spawn_capacity;
     h.part_cap = c.particle_capacity;
+    h.amw = ceil_div(width, 8);
+    h.amh = ceil_div(height, 8);
     size_t n = (size_t)ncell;
     int ncp = h.cell_iter * 4 * h.max_slots + 1;
     bool ok = dalloc(w, &h.id, n) && dalloc(w, &h.col, n) && dalloc(w, &h.sc, n) && dalloc(w, &h.fl, n) &&
@@ -668,7 +670,7 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
               dalloc(w, &h.p_state, (size_t)h.part_cap) && dalloc(w, &h.p_lxly, (size_t)h.part_cap) &&
               dalloc(w, &h.req_list, (size_t)h.part_cap) && dalloc(w, &h.req_list2, 2 * (size_t)h.part_cap) &&
               dalloc(w, &h.req_target, (size_t)h.part_cap) && dalloc(w, &h.scan_tmp, particle_scan_blocks() + 1) &&
-              dalloc(w, &w->d, 1);
+              dalloc(w, &h.airmap, (size_t)h.amw * h.amh) && dalloc(w, &w->d, 1);
     PartSoA *ps[2] = {&h.p, &h.q};
     size_t pc = (size_t)h.part_cap;
     for (int k = 0; k < 2 && ok; k++) {
@@ -925,7 +927,7 @@ static int world_enqueue(fse_world *w, bool particles_after_tick, bool tick, boo
         if (rc) return rc;
     } else if (particles) {
         if (launch_particle_tick(w->d, 1, g_dev_mt, world_move_blocks(w), w->stream) != cudaSuccess) return FSE_E_CUDA;
-        count_launches(11);
+        count_launches(PARTICLE_TICK_LAUNCHES);
     }
     return FSE_OK;
 }

@@ -57,6 +57,7 @@ cudaError_t launch_colour_pass(const WorldDev *worlds, const uint32_t *items, in
 cudaError_t launch_spawn_append(WorldDev *d_worlds, int n_worlds, int stage_blocks, cudaStream_t s);
 cudaError_t launch_particle_tick(WorldDev *d_worlds, int n_worlds, const MatTable *mt, int move_blocks,
                                  cudaStream_t s);
+constexpr int PARTICLE_TICK_LAUNCHES = 12;  // kernels launch_particle_tick issues
 void particle_prepare();
 int particle_scan_blocks();
 int sm_count();

@@ -138,6 +138,8 @@ struct WorldDev {
     long long *ledger;      // [LED_ROWS][MAXMAT]
     int32_t *err;
     unsigned *bar;          // grid barrier {count, generation} of the cooperative deposit kernel
+    uint8_t *airmap;        // per 8x8 block of cells: 1 if it held AIR when the particle tick began
+    int amw, amh;           // airmap size in blocks
 };
 
 __host__ __device__ __forceinline__ int ceil_div(int a, int b) { return (a + b - 1) / b; }

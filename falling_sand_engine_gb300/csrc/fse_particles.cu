@@ -13,7 +13,7 @@
 
 namespace fse {
 
-constexpr int PART_BLOCKS = 64;  // blocks per world for the particle list kernels
+constexpr int PART_BLOCKS = 512;  // blocks per world for the particle list kernels (<= k_cmp_scan threads)
 constexpr int PART_THREADS = 256;
 
 // p_state values
@@ -125,7 +125,11 @@ __device__ __forceinline__ void led_part(const WorldDev &w, const MatTable *mt, 
 
 // world.cpp:2032-2188 for every particle against the grid left by the cell tick;
 // collisions become deposit requests resolved by the kernels below.
+__device__ __forceinline__ void load_types(uint8_t *s_type, const MatTable *mt);
+
 __global__ void k_part_move(const WorldDev *__restrict__ worlds, const MatTable *__restrict__ mt) {
+    __shared__ uint8_t s_type[MAXMAT];
+    load_types(s_type, mt);
     const WorldDev &w = worlds[blockIdx.y];
     const int n = *w.part_count;
     const int W = w.W, H = w.H;
@@ -172,7 +176,7 @@ __global__ void k_part_move(const WorldDev *__restrict__ worlds, const MatTable 
                 done = true;
                 break;
             }
-            int ct = mt_type(mt->a[w.id[(size_t)(int)y * W + (int)x]]);
+            int ct = s_type[w.id[(size_t)(int)y * W + (int)x]];
             if (!(bits & 1) && ct != T_AIR) {
                 bool isObject = ct == T_OBJECT;
                 int ps = (bits >> 2) & 3;
@@ -186,7 +190,7 @@ __global__ void k_part_move(const WorldDev *__restrict__ worlds, const MatTable 
                         st = PS_DEAD;
                         led_part(w, mt, LED_DN, LED_DF, w.p.id[i], w.p.sc[i]);
                     } else {
-                        st = (mt_type(mt->a[w.id[(size_t)ly * W + lx]]) != T_AIR) ? PS_SPIRAL : PS_DIRECT;
+                        st = (s_type[w.id[(size_t)ly * W + lx]] != T_AIR) ? PS_SPIRAL : PS_DIRECT;
                     }
                     done = true;
                 }
@@ -209,17 +213,39 @@ __global__ void k_part_move(const WorldDev *__restrict__ worlds, const MatTable 
 }
 
 // ------------------------------------------------------------- deposits
-// Target of a deposit against the current grid (world.cpp:2093-2147):
-// returns cell index, with bit 31 set for a merge into the same liquid; -1 if none.
-__device__ __forceinline__ int dep_target(const WorldDev &w, const MatTable *mt, int i, uint8_t st) {
+// Target of a deposit against the current grid (world.cpp:2093-2147): the cell
+// index, with bit 31 set for a merge into the same liquid; -1 if none.
+// s_type: physics type per material (shared memory).
+//
+// A particle whose search window (the 33x33 cells the spiral walk can reach) holds
+// no AIR can only fail, unless it is a liquid that may merge. The airmap records,
+// per 8x8 block, whether the block held AIR when this particle tick began; deposits
+// only remove AIR, so a window whose blocks are all AIR-free now is AIR-free too and
+// the walk is skipped. The result is the walk's result either way.
+__device__ __forceinline__ int dep_target(const WorldDev &w, const uint8_t *s_type, int i, uint8_t st) {
     const int W = w.W, H = w.H;
     if (st == PS_DIRECT) {
         int c = w.p_lxly[i];
-        if (mt_type(mt->a[w.id[c]]) == T_AIR) return c;
+        if (s_type[w.id[c]] == T_AIR) return c;
     }
     const float x = w.p.x[i], y = w.p.y[i];
     const int pid = w.p.id[i];
-    const bool psoup = mt_type(mt->a[pid]) == T_SOUP;
+    const bool psoup = s_type[pid] == T_SOUP;
+    if (!psoup && x > -32.0f && x < (float)W + 32.0f && y > -32.0f && y < (float)H + 32.0f) {
+        // window [x-17, x+17] x [y-17, y+17] covers every (int)(x + ofs), |ofs| <= 16;
+        // positions far outside the world (or NaN) take the walk unfiltered
+        const int ix = (int)floorf(x), iy = (int)floorf(y);
+        const int bx0 = max(0, (ix - 17) >> 3), bx1 = min(w.amw - 1, (ix + 17) >> 3);
+        const int by0 = max(0, (iy - 17) >> 3), by1 = min(w.amh - 1, (iy + 17) >> 3);
+        bool any = false;
+        for (int by = by0; by <= by1 && !any; by++)
+            for (int bx = bx0; bx <= bx1; bx++)
+                if (w.airmap[by * w.amw + bx]) {
+                    any = true;
+                    break;
+                }
+        if (!any) return -1;
+    }
     const int n = c_spiral_n;
     for (int j = 0; j < n; j++) {
         int cx = (int)__fadd_rn(x, (float)c_spiral[j][0]);
@@ -227,10 +253,35 @@ __device__ __forceinline__ int dep_target(const WorldDev &w, const MatTable *mt,
         if (cx < 0 || cy < 0 || cx >= W || cy >= H) continue;
         int c = cy * W + cx;
         int cid = w.id[c];
-        if (mt_type(mt->a[cid]) == T_AIR) return c;
+        if (s_type[cid] == T_AIR) return c;
         if (psoup && cid == pid) return c | (int)0x80000000u;
     }
     return -1;
+}
+
+// which 8x8 blocks hold AIR, from the grid the cell tick left (one thread per block)
+__global__ void k_air_map(const WorldDev *__restrict__ worlds, const MatTable *__restrict__ mt) {
+    __shared__ uint8_t s_type[MAXMAT];
+    load_types(s_type, mt);
+    const WorldDev &w = worlds[blockIdx.y];
+    const int nb = w.amw * w.amh;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+        const int bx = b % w.amw, by = b / w.amw;
+        const int x0 = bx * 8, y0 = by * 8, x1 = min(x0 + 8, w.W), y1 = min(y0 + 8, w.H);
+        uint8_t any = 0;
+        for (int y = y0; y < y1 && !any; y++)
+            for (int x = x0; x < x1; x++)
+                if (s_type[w.id[(size_t)y * w.W + x]] == T_AIR) {
+                    any = 1;
+                    break;
+                }
+        w.airmap[b] = any;
+    }
+}
+
+__device__ __forceinline__ void load_types(uint8_t *s_type, const MatTable *mt) {
+    for (int k = threadIdx.x; k < MAXMAT; k += blockDim.x) s_type[k] = (uint8_t)(k < mt->n ? mt_type(mt->a[k]) : 0);
+    __syncthreads();
 }
 
 __device__ __forceinline__ void dep_fail(const WorldDev &w, int i) {
@@ -257,11 +308,13 @@ __device__ __forceinline__ void dep_fill(const WorldDev &w, int i, int c) {
 
 // round 1 over all requests, phase 1: pick targets; AIR targets get the claim sentinel
 __global__ void k_dep_target(const WorldDev *__restrict__ worlds, const MatTable *__restrict__ mt) {
+    __shared__ uint8_t s_type[MAXMAT];
+    load_types(s_type, mt);
     const WorldDev &w = worlds[blockIdx.y];
     const int n = w.req_count[0];
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
         int i = w.req_list[j];
-        int t = dep_target(w, mt, i, w.p_state[i]);
+        int t = dep_target(w, s_type, i, w.p_state[i]);
         w.req_target[j] = t;
         if (t >= 0) w.df[t] = 0x7fffffff;
     }
@@ -336,6 +389,8 @@ __device__ __forceinline__ void grid_sync(GridBar *gb, unsigned nblocks, int32_t
 // Open requests of round r live in list (r even: req_list2, odd: req_list) with
 // their count in req_count[1] (r even) / req_count[0] (r odd).
 __global__ void k_dep_rounds(const WorldDev *__restrict__ worlds, int n_worlds, const MatTable *__restrict__ mt) {
+    __shared__ uint8_t s_type[MAXMAT];
+    load_types(s_type, mt);
     GridBar *gb = (GridBar *)worlds[0].bar;
     const unsigned nb = gridDim.x;
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
@@ -354,7 +409,7 @@ __global__ void k_dep_rounds(const WorldDev *__restrict__ worlds, int n_worlds, 
             if (gtid == 0) w.req_count[ni] = 0;
             for (int j = gtid; j < n; j += gstride) {
                 int i = cur[j];
-                int t = dep_target(w, mt, i, w.p_state[i]);
+                int t = dep_target(w, s_type, i, w.p_state[i]);
                 w.req_target[j] = t;
                 if (t >= 0) w.df[t] = 0x7fffffff;
             }
@@ -435,17 +490,31 @@ __global__ void k_cmp_count(const WorldDev *__restrict__ worlds) {
     }
 }
 
+// exclusive scan of the per-block counts (nblocks <= blockDim.x), one block per world
 __global__ void k_cmp_scan(const WorldDev *__restrict__ worlds, int nblocks) {
     const WorldDev &w = worlds[blockIdx.x];
-    if (threadIdx.x == 0) {
-        int run = 0;
-        for (int b = 0; b < nblocks; b++) {
-            int v = w.scan_tmp[b];
-            w.scan_tmp[b] = run;
-            run += v;
-        }
-        w.scan_tmp[nblocks] = run;
+    __shared__ int s[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int v = (int)threadIdx.x < nblocks ? w.scan_tmp[threadIdx.x] : 0;
+    int inc = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
     }
+    if (lane == 31) s[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        int a = lane < nw ? s[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, a, o);
+            if (lane >= o) a += t;
+        }
+        if (lane < nw) s[lane] = a;
+    }
+    __syncthreads();
+    const int excl = (wid > 0 ? s[wid - 1] : 0) + inc - v;
+    if ((int)threadIdx.x < nblocks) w.scan_tmp[threadIdx.x] = excl;
+    if ((int)threadIdx.x == nblocks - 1) w.scan_tmp[nblocks] = excl + v;
 }
 
 __global__ void k_cmp_scatter(const WorldDev *__restrict__ worlds) {
@@ -579,6 +648,7 @@ cudaError_t launch_particle_tick(WorldDev *d_worlds, int n_worlds, const MatTabl
                                  cudaStream_t s) {
     spiral_upload();
     dim3 gm(move_blocks, n_worlds);
+    k_air_map<<<gm, 256, 0, s>>>(d_worlds, mt);
     k_part_move<<<gm, 256, 0, s>>>(d_worlds, mt);
     k_dep_target<<<gm, 256, 0, s>>>(d_worlds, mt);
     k_dep_claim<<<gm, 256, 0, s>>>(d_worlds, mt);
@@ -609,7 +679,7 @@ cudaError_t launch_particle_tick(WorldDev *d_worlds, int n_worlds, const MatTabl
     k_dep_clear<<<gm, 256, 0, s>>>(d_worlds);
     dim3 gc(PART_BLOCKS, n_worlds);
     k_cmp_count<<<gc, PART_THREADS, 0, s>>>(d_worlds);
-    k_cmp_scan<<<n_worlds, 32, 0, s>>>(d_worlds, PART_BLOCKS);
+    k_cmp_scan<<<n_worlds, PART_BLOCKS, 0, s>>>(d_worlds, PART_BLOCKS);
     k_cmp_scatter<<<gc, PART_THREADS, 0, s>>>(d_worlds);
     k_cmp_copy<<<gm, 256, 0, s>>>(d_worlds, PART_BLOCKS);
     k_part_end<<<n_worlds, 32, 0, s>>>(d_worlds, PART_BLOCKS);
