@@ -48,6 +48,22 @@ __device__ unsigned long long g_phase_clk[16];
 namespace fse {
 
 constexpr int CP_THREADS = 1024;  // >= the largest sweep-A sub-phase (43 x 22 cells for 128-cell chunks)
+constexpr int MAXRW = 160;        // tile row width bound (chunk <= 128, halo <= 5), a multiple of 32
+
+// 4-byte global -> shared copy that does not pass through registers (sm_80+ cp.async)
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// q = e / n and r = e % n for 0 <= e < 2^16, 1 <= n <= 256, from a float reciprocal
+// of n: (e + 0.5) / n sits at least 0.5 / n from an integer, far more than the
+// float error, so the truncation is exact.
+__device__ __forceinline__ void divmod_small(int e, int n, float rn, int &q, int &r) {
+    q = (int)(((float)e + 0.5f) * rn);
+    r = e - q * n;
+}
 
 struct Cell {
     uint16_t id;
@@ -929,23 +945,64 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
         Tl.s_id = (uint16_t *)(Tl.s_col + nfull);
         Tl.s_fl = (uint8_t *)(Tl.s_id + ((nid + 1) & ~1));
 
-        // ---- stage material ids; decide skip and lattice mode from the chunk
+        // ---- stage the tile, one warp per row. The 4-byte planes go straight to
+        // shared memory with cp.async; ids and flags are loaded a row at a time, all
+        // loads of a row in flight together. The chunk's ids decide the skip and the
+        // lattice mode.
         int active = 0, fire = 0;
-        for (int i = tid; i < nid; i += T) {
-            int ly = i / Tl.RW, lx = i - ly * Tl.RW;
-            int gx = Tl.x0 + lx, gy = Tl.y0 + ly;
-            uint16_t v = (uint16_t)id_solid;
-            if ((unsigned)gx < (unsigned)W && (unsigned)gy < (unsigned)H) {
-                v = w.id[(size_t)gy * W + gx];
-                if (gx >= cx && gx < cx + C && gy >= cy && gy < cy + C) {
-                    if (mt_iter(S.ma[v]) > iter) active = 1;
-                    if ((int)v == c.id_fire) fire = 1;
+        {
+            const int lane = tid & 31, wid = tid >> 5;
+            constexpr int NW = T / 32;
+            for (int r = wid; r < Tl.RHI; r += NW) {
+                const int gy = Tl.y0 + r;
+                const bool rin = (unsigned)gy < (unsigned)H;
+                const size_t gb = (size_t)gy * W;
+                const bool full = r < Tl.RHF;
+                uint16_t v[MAXRW / 32];
+                uint8_t f[MAXRW / 32];
+#pragma unroll
+                for (int k = 0; k < MAXRW / 32; k++) {
+                    const int lx = lane + 32 * k, gx = Tl.x0 + lx;
+                    v[k] = (uint16_t)id_solid;
+                    f[k] = 0;
+                    if (lx < Tl.RW && rin && (unsigned)gx < (unsigned)W) {
+                        v[k] = w.id[gb + gx];
+                        if (full) f[k] = w.fl[gb + gx];
+                    }
+                }
+                if (full) {
+#pragma unroll
+                    for (int k = 0; k < MAXRW / 32; k++) {
+                        const int lx = lane + 32 * k, gx = Tl.x0 + lx;
+                        if (lx >= Tl.RW) continue;
+                        const int i = r * Tl.RW + lx;
+                        if (rin && (unsigned)gx < (unsigned)W) {
+                            cp_async4(&Tl.s_sc[i], &w.sc[gb + gx]);
+                            cp_async4(&Tl.s_col[i], &w.col[gb + gx]);
+                        } else {
+                            Tl.s_sc[i] = 0;
+                            Tl.s_col[i] = 0xff0000u;
+                        }
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < MAXRW / 32; k++) {
+                    const int lx = lane + 32 * k, gx = Tl.x0 + lx;
+                    if (lx >= Tl.RW) continue;
+                    const int i = r * Tl.RW + lx;
+                    Tl.s_id[i] = v[k];
+                    if (full) Tl.s_fl[i] = f[k];
+                    if (gx >= cx && gx < cx + C && gy >= cy && gy < cy + C && rin && gx < W) {
+                        if (mt_iter(S.ma[v[k]]) > iter) active = 1;
+                        if ((int)v[k] == c.id_fire) fire = 1;
+                    }
                 }
             }
-            Tl.s_id[i] = v;
         }
         active = __syncthreads_or(active);
         fire = __syncthreads_or(fire);
+        cp_async_wait_all();
+        __syncthreads();
         FSE_PT(1)
         if (!active) {
             // every chunk cell has iterations <= iter: the pass only marks cells visited
@@ -953,21 +1010,6 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
             __syncthreads();
             continue;
         }
-        for (int i = tid; i < nfull; i += T) {
-            int ly = i / Tl.RW, lx = i - ly * Tl.RW;
-            int gx = Tl.x0 + lx, gy = Tl.y0 + ly;
-            if ((unsigned)gx < (unsigned)W && (unsigned)gy < (unsigned)H) {
-                size_t g = (size_t)gy * W + gx;
-                Tl.s_fl[i] = w.fl[g];
-                Tl.s_sc[i] = w.sc[g];
-                Tl.s_col[i] = w.col[g];
-            } else {
-                Tl.s_fl[i] = 0;
-                Tl.s_sc[i] = 0;
-                Tl.s_col[i] = 0xff0000u;
-            }
-        }
-        __syncthreads();
         FSE_PT(2)
 
         const int mode = c.has_inter ? 2 : (fire ? 1 : 0);
@@ -995,9 +1037,11 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
             int px, py;
             lattice(sweep, mode, px, py);
             for (int ry = py - 1; ry >= 0; ry--) {
+                const int ny = (C - ry + py - 1) / py;
                 for (int rx = 0; rx < px; rx++) {
-                    const int nx = (C - rx + px - 1) / px, ny = (C - ry + py - 1) / py;
+                    const int nx = (C - rx + px - 1) / px;
                     const int total = nx * ny;
+                    const float rnx = __frcp_rn((float)nx);
                     if (sweep == 0) {
                         // sweep A sub-phases have at most 43 x 22 <= T cells: one per thread,
                         // so every spawn event stays in its thread until it is ranked
@@ -1005,36 +1049,48 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                         c.ev.n = 0;
                         S.cnt[tid] = 0;
                         if (e < total) {
-                            const int dy = ry + (e / nx) * py, dx = rx + (e % nx) * px;
+                            int q, r;
+                            divmod_small(e, nx, rnx, q, r);
+                            const int dy = ry + q * py, dx = rx + r * px;
                             if (dx < cw && dy < chh) rule_a(Tl, c, cx + dx, cy + dy);
                         }
                         FSE_PT(3)
-                        // rank spawned particles in enumeration order
+                        // rank spawned particles in enumeration order. S.cnt[e] and the scan
+                        // scratch are next written after the next sub-phase's barrier, so no
+                        // barrier is needed after this block.
                         if (c.ev.n > 0) S.cnt[e] = c.ev.n;
                         if (__syncthreads_or(c.ev.n > 0)) {
                             int tot;
-                            int ex = block_excl_scan(S.cnt[tid], S.scan, &tot);
-                            S.cnt[tid] = ex;
-                            if (tid == 0) S.scan[36] = atomicAdd(w.stage_count, tot);
-                            __syncthreads();
+                            const int ex = block_excl_scan(S.cnt[tid], S.scan, &tot);
                             if (c.ev.n > 0) {
-                                int r = S.cnt[e];
-                                emit_spawns(w, c.ev, cp, (uint32_t)(running + r), S.scan[36] + r);
+                                // staging slots are taken in any order; the (chunk-pass, rank)
+                                // key orders the particles later
+                                const int base = atomicAdd(w.stage_count, c.ev.n);
+                                emit_spawns(w, c.ev, cp, (uint32_t)(running + ex), base);
                             }
                             running += tot;
                         }
-                        __syncthreads();
                         FSE_PT(4)
                     } else {
                         // cells of one sub-phase never conflict: each thread takes all of its
                         // cells in turn, one barrier per sub-phase
+                        int q, r;
+                        divmod_small(tid, nx, rnx, q, r);
+                        int dq, dr;
+                        divmod_small(T, nx, rnx, dq, dr);
                         for (int e = tid; e < total; e += T) {
-                            const int dy = ry + (e / nx) * py, dx = rx + (e % nx) * px;
+                            const int dy = ry + q * py, dx = rx + r * px;
                             if (dx < cw && dy < chh) {
                                 if (sweep == 1)
                                     rule_b(Tl, c, cx + dx, cy + dy);
                                 else
                                     rule_c(Tl, c, cx + dx, cy + dy);
+                            }
+                            q += dq;
+                            r += dr;
+                            if (r >= nx) {
+                                r -= nx;
+                                q++;
                             }
                         }
                         FSE_PT(3 + 2 * sweep)
@@ -1045,18 +1101,26 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
             }
         }
 
-        // ---- write back the cells this CTA changed (full-state rows inside the world)
-        for (int i = tid; i < nfull; i += T) {
-            uint16_t v = Tl.s_id[i];
-            if (!(v & DIRTY)) continue;
-            int ly = i / Tl.RW, lx = i - ly * Tl.RW;
-            int gx = Tl.x0 + lx, gy = Tl.y0 + ly;
-            if ((unsigned)gx < (unsigned)W && (unsigned)gy < (unsigned)H) {
-                size_t g = (size_t)gy * W + gx;
-                w.id[g] = (uint16_t)(v & 0x7FFF);
-                w.fl[g] = (uint8_t)(Tl.s_fl[i] & (uint8_t)~VISITED);
-                w.sc[g] = Tl.s_sc[i];
-                w.col[g] = Tl.s_col[i];
+        // ---- write back the cells this CTA changed (full-state rows inside the world),
+        // one warp per row
+        {
+            const int lane = tid & 31, wid = tid >> 5;
+            for (int r = wid; r < Tl.RHF; r += T / 32) {
+                const int gy = Tl.y0 + r;
+                if ((unsigned)gy >= (unsigned)H) continue;
+                const size_t gb = (size_t)gy * W;
+#pragma unroll
+                for (int k = 0; k < MAXRW / 32; k++) {
+                    const int lx = lane + 32 * k, gx = Tl.x0 + lx;
+                    if (lx >= Tl.RW || (unsigned)gx >= (unsigned)W) continue;
+                    const int i = r * Tl.RW + lx;
+                    const uint16_t v = Tl.s_id[i];
+                    if (!(v & DIRTY)) continue;
+                    w.id[gb + gx] = (uint16_t)(v & 0x7FFF);
+                    w.fl[gb + gx] = (uint8_t)(Tl.s_fl[i] & (uint8_t)~VISITED);
+                    w.sc[gb + gx] = Tl.s_sc[i];
+                    w.col[gb + gx] = Tl.s_col[i];
+                }
             }
         }
         if (tid == 0) w.cp_count[cp] = running;
