@@ -254,6 +254,354 @@ def cpu_baseline_config1(seed, budget_s=12.0):
                       "after 1 warm-up step" % n}
 
 
+# ------------------------------------------------------- other workloads
+def _common(args, world_size, value, unit, ms_per_step, workload, extra_cfg, launches, clk, e2e=None, cpu=None,
+            higher=True, scaling="weak"):
+    cfg = {"workload": workload}
+    cfg.update(extra_cfg)
+    return {"metric": METRIC, "value": round(value, 4), "unit": unit, "n_gpus": world_size, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": higher,
+            "scaling": scaling, "vs_baseline": None, "dtype": "int32+f32", "data": "synthetic", "config": cfg,
+            "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches)}
+
+
+def _ev(torch):
+    return torch.cuda.Event(enable_timing=True)
+
+
+def bench_config0(args, rank, local_rank, world_size):
+    """512x512 world, reference chunk size, step = tick + tickCells, per-step CUDA
+    events with the L2 flushed between steps; also the 32-tick graph replay."""
+    import torch
+
+    import falling_sand_engine_gb300 as fse
+
+    W = H = 512
+    seed = 1234 + rank
+    fse.InitMaterials()
+    fse.PushMaterials()
+    stream = torch.cuda.Stream()
+    world = fse.World(W, H, chunk_size=128, cell_iter=3, seed=seed, stream=stream.cuda_stream)
+    world.generate(fse.GEN_MIX, seed)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
+    for _ in range(args.warmup):
+        world.step(1)
+    ev = [(_ev(torch), _ev(torch)) for _ in range(args.steps)]
+    clocks = Clocks(local_rank)
+    barrier(world_size)
+    torch.cuda.synchronize()
+    l0 = fse.launch_counter()
+    clocks.start()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            _flush(flush, i)
+            ev[i][0].record(stream)
+            world.enqueue(1, particles=True)
+            ev[i][1].record(stream)
+    world.sync()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = fse.launch_counter() - l0
+    gpu_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in ev), world_size)
+    value = world_size * W * H * args.steps / (gpu_ms / 1e3) / 1e9
+    # the same ticks replayed from 32-tick CUDA graphs (no flush inside a graph)
+    g0, g1 = _ev(torch), _ev(torch)
+    world.step(32, graph=True)
+    torch.cuda.synchronize()
+    n_graph = max(32, (args.steps // 32) * 32)
+    g0.record(stream)
+    world.step(n_graph, graph=True)
+    g1.record(stream)
+    world.sync()
+    torch.cuda.synchronize()
+    graph_ms = g0.elapsed_time(g1)
+    cpu = None
+    if rank == 0 and world_size == 1 and not args.no_cpu:
+        cpu = cpu_baseline_world(W, H, seed, 0, 10.0)
+    world.close()
+    return _common(args, world_size, value, "Gcell/s", gpu_ms / args.steps,
+                   "config0: one 512x512 world (mix in the top 60%, 8 rock rows), reference chunk size 128, "
+                   "1000 ticks, plain per-world launch",
+                   {"world": [W, H], "chunk": 128, "cell_iter": 3, "seed": seed,
+                    "l2": "flushed between timed steps (512 MiB write outside the events)",
+                    "graph32": {"ticks": n_graph, "ms_per_tick": round(graph_ms / n_graph, 4),
+                                "value": round(W * H * n_graph / (graph_ms / 1e3) / 1e9, 4),
+                                "note": "32-tick CUDA graph replay; no L2 flush inside a graph"}},
+                   launches, clk, cpu=cpu)
+
+
+def cpu_baseline_world(W, H, seed, gen_kind, budget_s):
+    """The oracle's reference-order tick on all host cores on a bounded sample of a
+    W x H world of the given generator (as many steps as fit the budget)."""
+    from oracle import Oracle, OracleWorld
+
+    o = Oracle()
+    o.reset_materials()
+    cores = os.cpu_count() or 1
+    o.set_threads(cores)
+    ow = OracleWorld(W, H, 128, 3, seed)
+    ow.generate(gen_kind, seed)
+    ow.step(1, 0)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        ow.step(1, 0)
+        n += 1
+        if time.perf_counter() - t0 > budget_s or n >= 1000:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": round(W * H * n / dt / 1e9, 6), "unit": "Gcell/s", "cores": cores, "kind": "port",
+            "sample": "%d steps (tick + tickCells) of the %dx%d world, reference chunk order, after 1 warm-up step"
+                      % (n, W, H)}
+
+
+def config2_sizes(n, seed):
+    rng = np.random.default_rng(seed)
+    sides = np.arange(128, 2049, 64)
+    return [(int(rng.choice(sides)), int(rng.choice(sides))) for _ in range(n)]
+
+
+def bench_config2(args, rank, local_rank, world_size):
+    """256 worlds of uneven sizes: batched launches replayed from 32-tick CUDA graphs
+    with the autotuned launch shape, against the same worlds stepped one by one
+    through their plain per-world launches (each world on its own stream)."""
+    import torch
+
+    import falling_sand_engine_gb300 as fse
+
+    fse.InitMaterials()
+    fse.PushMaterials()
+    sizes = config2_sizes(256, 1234 + rank)
+    cells = sum(w * h for w, h in sizes)
+
+    def make():
+        ws = []
+        for i, (w, h) in enumerate(sizes):
+            wd = fse.World(w, h, chunk_size=128, cell_iter=3, seed=1234 + i)
+            wd.generate(fse.GEN_MIX, 1234 + i)
+            ws.append(wd)
+        for wd in ws:
+            wd.sync()
+        return ws
+
+    worlds = make()
+    batch = fse.Batch(worlds)
+    choice = batch.autotune()
+    bstream = torch.cuda.ExternalStream(batch.stream)
+    batch.step(args.warmup)
+    batch.sync()
+    clocks = Clocks(local_rank)
+    barrier(world_size)
+    torch.cuda.synchronize()
+    l0 = fse.launch_counter()
+    e0, e1 = _ev(torch), _ev(torch)
+    clocks.start()
+    e0.record(bstream)
+    batch.step(args.steps, graph_ticks=32)
+    e1.record(bstream)
+    batch.sync()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = fse.launch_counter() - l0
+    b_ms = max_over_ranks(e0.elapsed_time(e1), world_size)
+    value = world_size * cells * args.steps / (b_ms / 1e3) / 1e9
+    digest_b = sum(int(w.state()["id"].astype(np.int64).sum()) for w in worlds[:8])
+    batch.close()
+    for w in worlds:
+        w.close()
+    del worlds
+
+    # the same worlds, plain per-world launches: start and end events join all streams
+    worlds = make()
+    streams = [torch.cuda.ExternalStream(w.stream) for w in worlds]
+    for w in worlds:
+        w.step(args.warmup)
+    torch.cuda.synchronize()
+    main = torch.cuda.current_stream()
+    p0, p1 = _ev(torch), _ev(torch)
+    p0.record(main)
+    for s in streams:
+        s.wait_event(p0)
+    for _ in range(args.steps):
+        for w in worlds:
+            w.enqueue(1, particles=True)
+    for s in streams:
+        e = _ev(torch)
+        e.record(s)
+        main.wait_event(e)
+    p1.record(main)
+    torch.cuda.synchronize()
+    for w in worlds:
+        w.sync()
+    p_ms = max_over_ranks(p0.elapsed_time(p1), world_size)
+    per_world = world_size * cells * args.steps / (p_ms / 1e3) / 1e9
+    digest_p = sum(int(w.state()["id"].astype(np.int64).sum()) for w in worlds[:8])
+    for w in worlds:
+        w.close()
+    peak, peak_kind = peaks()
+    return _common(args, world_size, value, "Gcell/s", b_ms / args.steps,
+                   "config2: 256 worlds, sides uniform in {128, 192, ..., 2048}, per-world seeds, mix; batched "
+                   "launches from 32-tick CUDA graphs, autotuned launch shape",
+                   {"worlds": 256, "cells": cells, "chunk": 128, "cell_iter": 3, "autotune": choice,
+                    "l2": "inputs larger than L2 (%.2f GB of grid state)" % (cells * 15 / 1e9),
+                    "per_world_launch": {"value": round(per_world, 4), "ms_per_step": round(p_ms / args.steps, 4)},
+                    "batched_over_per_world": round(value / per_world, 3),
+                    "same_result": digest_b == digest_p,
+                    "hbm_frac_of_tick": round(value * 1e9 * BYTES_PER_CELL_UPDATE / world_size / (peak * 1e9), 5),
+                    "peak_kind": peak_kind},
+                   launches, clk)
+
+
+def bench_config3(args, rank, local_rank, world_size):
+    """16384x16384 world, 8 materials with Zipf frequencies, 200 axis-aligned OBJECT
+    boxes stamped before every tick, taken back after it, and the OBJECT mask
+    (1 bit per cell) exported to the host every tick."""
+    import torch
+
+    import falling_sand_engine_gb300 as fse
+
+    W = H = 16384
+    seed = 1234 + rank
+    fse.InitMaterials()
+    fse.PushMaterials()
+    stream = torch.cuda.Stream()
+    world = fse.World(W, H, chunk_size=128, cell_iter=3, seed=seed, particle_capacity=24 << 20,
+                      spawn_capacity=16 << 20, stream=stream.cuda_stream)
+    world.generate(fse.GEN_ZIPF8, seed)
+    rng = np.random.default_rng(seed)
+    bodies = np.zeros(200, fse.BODY_DTYPE)
+    bodies["w"] = rng.integers(8, 65, 200)
+    bodies["h"] = rng.integers(8, 65, 200)
+    bodies["x"] = rng.uniform(0, W - 64, 200).astype(np.float32)
+    bodies["y"] = rng.uniform(0, H - 64, 200).astype(np.float32)
+    bodies["cos_a"] = 1.0
+    bodies["id"] = fse.material_find("GENERIC_OBJECT")
+    bodies["colour"] = 0xFF808080
+    mask = torch.empty((W * H + 7) // 8, dtype=torch.uint8, pin_memory=True).numpy()
+
+    def one(timed=None):
+        world.object_stamp(bodies)
+        if timed is not None:
+            timed[0].record(stream)
+        world.enqueue(1, particles=True)
+        if timed is not None:
+            timed[1].record(stream)
+        world.object_mask(out=mask)
+        world.object_readback(bodies)
+
+    for _ in range(args.warmup):
+        one()
+    ev = [(_ev(torch), _ev(torch)) for _ in range(args.steps)]
+    clocks = Clocks(local_rank)
+    barrier(world_size)
+    torch.cuda.synchronize()
+    l0 = fse.launch_counter()
+    clocks.start()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            one(ev[i])
+    world.sync()
+    wall = max_over_ranks(time.perf_counter() - t0, world_size)
+    clk = clocks.stop()
+    launches = fse.launch_counter() - l0
+    tick_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in ev), world_size)
+    cells = W * H
+    value = world_size * cells * args.steps / (tick_ms / 1e3) / 1e9
+    n_obj = int(np.unpackbits(mask).sum())
+    world.close()
+    e2e = {"value": round(world_size * cells * args.steps / wall / 1e9, 4), "unit": "Gcell/s",
+           "h2d_bytes_per_step": int(2 * bodies.nbytes), "d2h_bytes_per_step": int(mask.nbytes + 2 * bodies.nbytes),
+           "path": "fse_object_stamp + fse_world_enqueue + fse_object_mask_export + fse_object_readback per tick"}
+    return _common(args, world_size, value, "Gcell/s", tick_ms / args.steps,
+                   "config3: one 16384x16384 world (Zipf-8 materials) with 200 OBJECT boxes stamped, ticked, "
+                   "exported as a 1-bit mask and taken back every tick",
+                   {"world": [W, H], "bodies": 200, "chunk": 128, "cell_iter": 3, "seed": seed,
+                    "l2": "inputs larger than L2 (4 GB of grid state)",
+                    "object_cells_last_mask": n_obj,
+                    "objects_and_export_ms_per_tick": round(wall * 1e3 / args.steps - tick_ms / args.steps, 3)},
+                   launches, clk, e2e=e2e)
+
+
+def bench_config4(args, rank, local_rank, world_size, window_s=1.0):
+    """Serving: 1000 resident worlds (sides uniform in {256, 320, ..., 4096}) under a
+    120 GB admission budget; requests of 1-16 ticks arrive as a Poisson process at
+    2000 req/s for window_s seconds and are served by continuous batching until all
+    are done. Reports throughput and p50/p99 request latency (arrival to done)."""
+    import torch
+
+    import falling_sand_engine_gb300 as fse
+
+    fse.InitMaterials()
+    fse.PushMaterials()
+    rng = np.random.default_rng(1234 + rank)
+    sides = np.arange(256, 4097, 64)
+    srv = fse.Server(120 << 30, 1000)
+    slots, cells = [], {}
+    refused = 0
+    t_add = time.perf_counter()
+    for i in range(1000):
+        w, h = int(rng.choice(sides)), int(rng.choice(sides))
+        s = srv.try_add_world(w, h, fse.GEN_MIX, 1234 + i, seed=1234 + i,
+                              particle_capacity=max(65536, w * h // 32), spawn_capacity=max(65536, w * h // 64))
+        if s is None:
+            refused += 1
+            continue
+        slots.append(s)
+        cells[s] = w * h
+    t_add = time.perf_counter() - t_add
+    # warm-up: one tick of a few worlds
+    for s in slots[:4]:
+        srv.submit(s, 1)
+    while srv.step() > 0:
+        pass
+    srv.poll()
+    n_req = rng.poisson(2000 * window_s)
+    arr = np.sort(rng.uniform(0.0, window_s * 1e6, n_req))
+    req_slot = rng.choice(slots, n_req)
+    req_ticks = rng.integers(1, 17, n_req)
+    clocks = Clocks(local_rank)
+    torch.cuda.synchronize()
+    l0 = fse.launch_counter()
+    clocks.start()
+    base = srv.now_us()
+    nxt, done_n, lat, ids = 0, 0, [], {}
+    steps = 0
+    while done_n < n_req:
+        now = srv.now_us() - base
+        while nxt < n_req and arr[nxt] <= now:
+            rid = srv.submit(int(req_slot[nxt]), int(req_ticks[nxt]), arrival_us=base + arr[nxt])
+            ids[rid] = nxt
+            nxt += 1
+        if srv.step() == 0 and nxt < n_req:
+            time.sleep(max(0.0, (arr[nxt] - (srv.now_us() - base)) / 1e6))
+        steps += 1
+        got, t_done = srv.poll()
+        for rid, td in zip(got, t_done):
+            k = ids.pop(int(rid))
+            lat.append((td - base - arr[k]) / 1e3)
+            done_n += 1
+    total_s = (srv.now_us() - base) / 1e6
+    clk = clocks.stop()
+    launches = fse.launch_counter() - l0
+    work = float(sum(cells[int(s)] * int(t) for s, t in zip(req_slot, req_ticks)))
+    lat = np.array(lat)
+    value = world_size * work / total_s / 1e9
+    bytes_used = srv.bytes_in_use()
+    srv.close()
+    return _common(args, world_size, value, "Gcell/s", total_s * 1e3 / max(steps, 1),
+                   "config4: serving 1000 resident worlds (sides uniform in {256, ..., 4096}), Poisson arrivals at "
+                   "2000 req/s of 1-16 ticks for %.1f s, continuous batching, 120 GB admission budget" % window_s,
+                   {"worlds": len(slots), "worlds_refused_by_budget": refused, "requests": int(n_req),
+                    "hbm_bytes_resident": int(bytes_used), "world_setup_s": round(t_add, 2),
+                    "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 2),
+                                   "p99": round(float(np.percentile(lat, 99)), 2),
+                                   "max": round(float(lat.max()), 2)},
+                    "served_cell_updates": work, "wall_s": round(total_s, 2), "scheduler_steps": steps,
+                    "timing": "host clock from the first arrival to the last completion (the arrival window plus "
+                              "the drain)"},
+                   launches, clk)
+
+
 def profile_traffic(name):
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
@@ -368,12 +716,8 @@ def main():
 
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
-    if args.workload == 1:
-        out = bench_config1(args, rank, local_rank, world_size)
-    else:
-        import bench_workloads
-
-        out = bench_workloads.run(args, rank, local_rank, world_size)
+    run = {0: bench_config0, 1: bench_config1, 2: bench_config2, 3: bench_config3, 4: bench_config4}[args.workload]
+    out = run(args, rank, local_rank, world_size)
     if rank == 0 and out is not None:
         print(json.dumps(out))
     if world_size > 1:

@@ -322,6 +322,10 @@ class Batch:
     def sync(self):
         check(self.lib.fse_batch_sync(self.h), "batch_sync")
 
+    @property
+    def stream(self):
+        return self.lib.fse_batch_stream(self.h)
+
 
 class Server:
     """Device-resident worlds served by continuous batching under an HBM budget."""

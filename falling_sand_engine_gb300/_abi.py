@@ -84,6 +84,7 @@ SIGNATURES = {
     "fse_batch_autotune": (_i, [_vp, _vp]),
     "fse_batch_set_launch": (_i, [_vp, _i, _i]),
     "fse_batch_sync": (_i, [_vp]),
+    "fse_batch_stream": (_vp, [_vp]),
     "fse_server_create": (_i, [_i64, _i, _pp]),
     "fse_server_destroy": (_i, [_vp]),
     "fse_server_add_world": (_i, [_vp, _i, _i, C.POINTER(FseConfig), _i, _u32, C.POINTER(_i)]),

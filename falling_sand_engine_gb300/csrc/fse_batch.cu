@@ -265,6 +265,8 @@ int fse_batch_sync(fse_batch *b) {
     return batch_sync(b);
 }
 
+void *fse_batch_stream(fse_batch *b) { return b ? (void *)b->stream : nullptr; }
+
 }  // extern "C"
 
 // ================================================================ serving

@@ -230,6 +230,8 @@ int fse_batch_step_graph(fse_batch *batch, int n_ticks, int graph_ticks);
 int fse_batch_autotune(fse_batch *batch, int32_t out_choice[4]);
 int fse_batch_set_launch(fse_batch *batch, int threads, int ctas_per_sm);
 int fse_batch_sync(fse_batch *batch);
+/* the CUDA stream (cudaStream_t) the batch enqueues its work on */
+void *fse_batch_stream(fse_batch *batch);
 
 /* ---------------------------------------------------------------- serving */
 int fse_server_create(int64_t hbm_budget_bytes, int max_active, fse_server **out);
