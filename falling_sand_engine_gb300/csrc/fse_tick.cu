@@ -89,7 +89,15 @@ struct SpawnEv {
 // Region: x in [cx - HALO, cx + C + HALO), full state for y in
 // [cy - HALO, cy + C + HALO), material ids only down to y < cy + C + 10 (the
 // deepest read, the friction pillar of world.cpp:1619-1627).
-struct Tile {
+//
+// Every access of the rules stays inside the tile: relative to the active cell
+// they reach x +- 2 (fire), y - 2 .. y + 2 in the full planes, ids down to y + 4
+// (sand and liquid free fall), and the interaction boxes, whose |offset| + radius
+// <= 5 is enforced at registration and which run with HALO = 5; the sweep-B pillar
+// reads ids down to cy + C + 9. So the tile needs no bounds checks. EDGE selects
+// the world bounds policy of world.cpp:999-1008 (outside reads GENERIC_SOLID,
+// outside writes dropped); it is needed only when the tile crosses the world edge.
+struct TileData {
     uint16_t *s_id;
     uint8_t *s_fl;
     int32_t *s_sc;
@@ -100,10 +108,14 @@ struct Tile {
     int x0, y0, RW, RHF, RHI;
     int W, H;
     int id_solid, id_air;
-    int *err;
     // sweep-B pillar snapshot: AIR bits of columns ax0.., rows ay0.., 5 words per column
     const uint32_t *s_air;
     int ax0, ay0, aw;
+};
+
+template <bool EDGE>
+struct Tile : TileData {
+    __device__ __forceinline__ explicit Tile(const TileData &d) : TileData(d) {}
 
     // 10 snapshot bits of column x starting at row y (0 outside the snapshot)
     __device__ __forceinline__ uint32_t air10(int x, int y) const {
@@ -116,30 +128,20 @@ struct Tile {
         return (uint32_t)(v >> b) & 0x3FFu;
     }
 
+    // inside the world (always true away from the world edge)
     __device__ __forceinline__ bool inw(int x, int y) const {
-        return (unsigned)x < (unsigned)W && (unsigned)y < (unsigned)H;
+        return !EDGE || ((unsigned)x < (unsigned)W && (unsigned)y < (unsigned)H);
     }
     __device__ __forceinline__ int li(int x, int y) const { return (y - y0) * RW + (x - x0); }
-    __device__ __forceinline__ bool in_ids(int x, int y) const {
-        return (unsigned)(x - x0) < (unsigned)RW && (unsigned)(y - y0) < (unsigned)RHI;
-    }
-    __device__ __forceinline__ bool in_full(int x, int y) const {
-        return (unsigned)(x - x0) < (unsigned)RW && (unsigned)(y - y0) < (unsigned)RHF;
-    }
-    __device__ __forceinline__ void oob() const { atomicOr(err, ERR_BOUNDS); }
 
     // world.cpp:999-1002: outside the world reads Tiles_TEST_SOLID
     __device__ __forceinline__ int id(int x, int y) const {
         if (!inw(x, y)) return id_solid;
-        if (!in_ids(x, y)) {
-            oob();
-            return id_solid;
-        }
         return s_id[li(x, y)] & 0x7FFF;
     }
     __device__ __forceinline__ int type(int x, int y) const { return mt_type(ma[id(x, y)]); }
     __device__ __forceinline__ int32_t sc(int x, int y) const {
-        if (!inw(x, y) || !in_full(x, y)) return 0;
+        if (!inw(x, y)) return 0;
         return s_sc[li(x, y)];
     }
     __device__ __forceinline__ int32_t df_of(int x, int y) const {
@@ -172,10 +174,6 @@ struct Tile {
     // world.cpp:1004-1008: outside the world writes are dropped
     __device__ __forceinline__ void put(int x, int y, const Cell &c) const {
         if (!inw(x, y)) return;
-        if (!in_full(x, y)) {
-            oob();
-            return;
-        }
         int i = li(x, y);
         s_id[i] = c.id | DIRTY;
         s_fl[i] = (uint8_t)((c.fl & (uint8_t)~VISITED) | (s_fl[i] & VISITED));
@@ -195,13 +193,8 @@ struct Tile {
     // write the cell at (sx, sy) over (dx, dy); the visited mark stays with the position
     __device__ __forceinline__ void move(int dx, int dy, int sx, int sy) const {
         if (!inw(dx, dy)) return;
-        if (!in_full(dx, dy)) {
-            oob();
-            return;
-        }
         int d = li(dx, dy);
-        if (!inw(sx, sy) || !in_full(sx, sy)) {
-            if (inw(sx, sy)) oob();
+        if (!inw(sx, sy)) {
             s_id[d] = (uint16_t)id_solid | DIRTY;
             s_fl[d] = (uint8_t)(s_fl[d] & VISITED);
             s_sc[d] = 0;
@@ -216,15 +209,17 @@ struct Tile {
         s_col[d] = s_col[s];
         if (mt_type(ma[v]) == T_SOUP) df[dy * W + dx] = df[sy * W + sx];
     }
+    // only a change marks the cell for write-back (settled sand clears an already
+    // clear flag every pass)
     __device__ __forceinline__ void set_moved(int x, int y, bool on) const {
         if (!inw(x, y)) return;
-        if (!in_full(x, y)) {
-            oob();
-            return;
-        }
         int i = li(x, y);
-        s_fl[i] = on ? (uint8_t)(s_fl[i] | MOVED) : (uint8_t)(s_fl[i] & (uint8_t)~MOVED);
-        s_id[i] |= DIRTY;
+        const uint8_t f = s_fl[i];
+        const uint8_t nf = on ? (uint8_t)(f | MOVED) : (uint8_t)(f & (uint8_t)~MOVED);
+        if (nf != f) {
+            s_fl[i] = nf;
+            s_id[i] |= DIRTY;
+        }
     }
     __device__ __forceinline__ void add_diff(int x, int y, int32_t v) const {
         if (!inw(x, y)) return;
@@ -233,10 +228,6 @@ struct Tile {
     __device__ __forceinline__ bool vis(int x, int y) const { return (s_fl[li(x, y)] & VISITED) != 0; }
     __device__ __forceinline__ void setvis(int x, int y) const {
         if (!inw(x, y)) return;
-        if (!in_full(x, y)) {
-            oob();
-            return;
-        }
         s_fl[li(x, y)] |= VISITED;
     }
 };
@@ -278,7 +269,8 @@ __device__ __forceinline__ void led_swap(Ctx &c, int old_id, long long old_fluid
     if (mt_type(c.ma[new_id]) == T_SOUP) led_add(c, LED_CF, new_id, new_fluid);
 }
 // conversion of whatever is at (x, y) into nw
-__device__ __forceinline__ void led_replace_at(const Tile &T, Ctx &c, int x, int y, const Cell &nw) {
+template <class TL>
+__device__ __forceinline__ void led_replace_at(const TL &T, Ctx &c, int x, int y, const Cell &nw) {
     if (!T.inw(x, y)) return;
     int oid = T.id(x, y);
     long long of = (mt_type(c.ma[oid]) == T_SOUP) ? (long long)T.sc(x, y) + T.df_of(x, y) : 0;
@@ -322,7 +314,8 @@ __device__ __forceinline__ bool can_sink(const uint32_t *ma, const float *md, in
 }
 
 // one SOUP flow towards (nx, ny), shared by the four directions of world.cpp:1309-1460
-__device__ __forceinline__ void soup_flow(const Tile &T, Ctx &c, Cell &t, int32_t &rem, int32_t flow, int nT, int nx,
+template <class TL>
+__device__ __forceinline__ void soup_flow(const TL &T, Ctx &c, Cell &t, int32_t &rem, int32_t flow, int nT, int nx,
                                           int ny) {
     if (flow == 0) return;
     rem -= flow;
@@ -355,7 +348,8 @@ __device__ __forceinline__ void spawn_one(Ctx &c, int kind, int x, int y, const 
 }
 
 // ----------------------------------------------------------------- sweep A
-__device__ __forceinline__ void rule_a(const Tile &T, Ctx &c, int x, int y) {
+template <class TL>
+__device__ __forceinline__ void rule_a(const TL &T, Ctx &c, int x, int y) {
     if (T.vis(x, y)) return;  // world.cpp:1091
     const uint32_t *ma = T.ma;
     const float *md = T.md;
@@ -617,7 +611,8 @@ __device__ __forceinline__ void rule_a(const Tile &T, Ctx &c, int x, int y) {
 }
 
 // ----------------------------------------------------------------- sweep B
-__device__ __forceinline__ void rule_b(const Tile &T, Ctx &c, int x, int y) {
+template <class TL>
+__device__ __forceinline__ void rule_b(const TL &T, Ctx &c, int x, int y) {
     if (T.vis(x, y)) return;  // world.cpp:1597
     const uint32_t *ma = T.ma;
     const float *md = T.md;
@@ -713,7 +708,8 @@ __device__ __forceinline__ void rule_b(const Tile &T, Ctx &c, int x, int y) {
 }
 
 // ----------------------------------------------------------------- sweep C
-__device__ __forceinline__ void rule_c(const Tile &T, Ctx &c, int x, int y) {
+template <class TL>
+__device__ __forceinline__ void rule_c(const TL &T, Ctx &c, int x, int y) {
     if (T.vis(x, y)) return;  // world.cpp:1831
     const int sid = T.id(x, y);
     if (mt_type(T.ma[sid]) != T_GAS) return;
@@ -921,7 +917,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
         const int cx = (ox + 2 * (slot / nb)) * C, cy = (oy + 2 * (slot % nb)) * C;
         const uint32_t cp = (uint32_t)((iter * 4 + tk) * w.max_slots + slot);
 
-        Tile Tl;
+        TileData Tl;
         Tl.RW = C + 2 * HALO;
         Tl.RHF = C + 2 * HALO;
         Tl.RHI = C + HALO + 10;
@@ -934,7 +930,6 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
         Tl.df = w.df;
         Tl.id_solid = id_solid;
         Tl.id_air = id_air;
-        Tl.err = w.err;
         Tl.s_air = S.air;
         Tl.ax0 = cx - 1;
         Tl.ay0 = cy + 1;
@@ -1016,6 +1011,9 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
         const int cw = min(C, W - cx), chh = min(C, H - cy);
         int running = 0;  // spawns emitted so far by this chunk-pass
         c.led_g = w.ledger;
+        // the world bounds policy matters only where the tile crosses the world edge
+        const bool edge = Tl.x0 < 0 || Tl.y0 < 0 || Tl.x0 + Tl.RW > W || Tl.y0 + Tl.RHI > H;
+        auto sweeps = [&](const auto &Tl) {
         for (int sweep = 0; sweep < 3; sweep++) {
             c.pk = pass_key(w.seed, *w.tick, (uint32_t)(iter * 3 + sweep));
             if (sweep == 1) {
@@ -1100,6 +1098,11 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                 }
             }
         }
+        };
+        if (edge)
+            sweeps(Tile<true>(Tl));
+        else
+            sweeps(Tile<false>(Tl));
 
         // ---- write back the cells this CTA changed (full-state rows inside the world),
         // one warp per row
