@@ -235,6 +235,8 @@ struct Tile : TileData {
 // ------------------------------------------------------------- rule context
 struct Ctx {
     uint32_t pk, ck, k;
+    int kx, ky;   // the active cell, whose key ck is derived on the first draw
+    bool have_ck;
     int iter;
     int id_fire, id_water, id_lava, id_steam, id_obsidian, has_inter;
     const MatTable *mt;
@@ -243,7 +245,22 @@ struct Ctx {
     const uint32_t *ma;
     const uint8_t *mreact;  // reactions per material (shared)
     SpawnEv ev;
-    __device__ __forceinline__ uint32_t D() { return draw_k(ck, k++); }
+    // start the draws of the cell at (x, y); most cells never draw, so the key
+    // (two hash rounds) is computed only when the first draw needs it
+    __device__ __forceinline__ void at(int x, int y) {
+        kx = x;
+        ky = y;
+        have_ck = false;
+        k = 0;
+    }
+    __device__ __forceinline__ uint32_t key() {
+        if (!have_ck) {
+            ck = cell_key(pk, (uint32_t)kx, (uint32_t)ky);
+            have_ck = true;
+        }
+        return ck;
+    }
+    __device__ __forceinline__ uint32_t D() { return draw_k(key(), k++); }
 };
 
 __device__ __forceinline__ void led_add(Ctx &c, int row, int mat, long long v) {
@@ -298,8 +315,8 @@ __device__ __forceinline__ Cell create_tile(Ctx &c, int mid) {
 __device__ __forceinline__ int32_t vflow(int32_t rem, int32_t dst) {
     long long sum = (long long)rem + dst;
     if (sum <= Q_MAXV) return Q_MAXV;
-    if (sum < 2 * Q_MAXV + Q_MAXCOMP)
-        return (int32_t)(((long long)Q_MAXV * Q_MAXV + sum * Q_MAXCOMP) / (Q_MAXV + Q_MAXCOMP));
+    if (sum < 2 * Q_MAXV + Q_MAXCOMP)  // here MAXV^2 + sum * MAXCOMP < 2^31: 32-bit unsigned is exact
+        return (int32_t)(((uint32_t)Q_MAXV * Q_MAXV + (uint32_t)sum * Q_MAXCOMP) / (uint32_t)(Q_MAXV + Q_MAXCOMP));
     return (int32_t)((sum + Q_MAXCOMP) / 2);
 }
 __device__ __forceinline__ int32_t clampflow(int32_t flow, int32_t rem) {
@@ -361,9 +378,15 @@ __device__ __forceinline__ void rule_a(const TL &T, Ctx &c, int x, int y) {
     }
     const int type = mt_type(a);
     if (type != T_SAND && type != T_SOUP && type != T_GAS && sid != c.id_fire) return;
+    if (sid != c.id_fire) {
+        // the common no-op cases, decided before the cell is loaded: sand that
+        // cannot sink (world.cpp:1206, without interactions or reactions) and gas
+        // with no AIR above (world.cpp:1573)
+        if (type == T_SAND && !c.has_inter && c.mreact[sid] == 0 && !can_sink(ma, md, T.id(x, y + 1), sid)) return;
+        if (type == T_GAS && T.type(x, y - 1) != T_AIR) return;
+    }
     Cell t = T.get_active(x, y);
-    c.ck = cell_key(c.pk, (uint32_t)x, (uint32_t)y);
-    c.k = 0;
+    c.at(x, y);
     const MatTable *mt = c.mt;
 
     if (sid == c.id_fire) {  // world.cpp:1101-1146
@@ -493,7 +516,7 @@ __device__ __forceinline__ void rule_a(const TL &T, Ctx &c, int x, int y) {
             c.ev.fl = 0;
             c.ev.col = t.col;
             c.ev.sc = t.sc;
-            c.ev.ck = c.ck;
+            c.ev.ck = c.key();
             c.ev.k0 = c.k;
             c.k += 2 * n;
             return;
@@ -529,7 +552,7 @@ __device__ __forceinline__ void rule_a(const TL &T, Ctx &c, int x, int y) {
         const bool canR = (rT == T_AIR || rid == (int)t.id) && !airBelow;
         if (canL) {
             int32_t dst = (lT == T_SOUP) ? T.sc(x - 1, y) : 0;
-            soup_flow(T, c, t, rem, clampflow((rem - dst) / (canR ? 3 : 2), rem), lT, x - 1, y);
+            soup_flow(T, c, t, rem, clampflow(canR ? (rem - dst) / 3 : (rem - dst) / 2, rem), lT, x - 1, y);
         }
         if (rem < Q_MINV) {
             t.df -= rem;
@@ -611,8 +634,10 @@ __device__ __forceinline__ void rule_a(const TL &T, Ctx &c, int x, int y) {
 }
 
 // ----------------------------------------------------------------- sweep B
+// dfv: the cell's pending fluid diff, read when the sub-phase began (no other cell
+// of the sub-phase writes it)
 template <class TL>
-__device__ __forceinline__ void rule_b(const TL &T, Ctx &c, int x, int y) {
+__device__ __forceinline__ void rule_b(const TL &T, Ctx &c, int x, int y, int32_t dfv) {
     if (T.vis(x, y)) return;  // world.cpp:1597
     const uint32_t *ma = T.ma;
     const float *md = T.md;
@@ -620,13 +645,13 @@ __device__ __forceinline__ void rule_b(const TL &T, Ctx &c, int x, int y) {
     const uint32_t a = ma[sid];
     const int type = mt_type(a);
     if (type != T_SAND && type != T_SOUP && type != T_GAS) return;
-    Cell t = T.get_active(x, y);
-    c.ck = cell_key(c.pk, (uint32_t)x, (uint32_t)y);
-    c.k = 0;
+    c.at(x, y);
     if (type == T_SAND) {  // world.cpp:1602-1727
+        const int i = T.li(x, y);
+        const uint8_t fl0 = T.s_fl[i] & (uint8_t)~VISITED;
         const bool canL = can_sink(ma, md, T.id(x - 1, y + 1), sid);
         const bool canR = can_sink(ma, md, T.id(x + 1, y + 1), sid);
-        bool stopped = !(t.fl & MOVED);
+        bool stopped = !(fl0 & MOVED);
         const int slip = mt_slip(a);
         if (stopped) {
             // world.cpp:1619-1627 over the AIR snapshot taken when sweep B began
@@ -646,6 +671,13 @@ __device__ __forceinline__ void rule_b(const TL &T, Ctx &c, int x, int y) {
             T.set_moved(x, y, false);
             return;
         }
+        // the moving cell as it was when its turn began
+        Cell t;
+        t.id = (uint16_t)sid;
+        t.fl = fl0;
+        t.sc = T.s_sc[i];
+        t.col = T.s_col[i];
+        t.df = 0;
         const bool shouldMove = (slip > 0) ? (c.D() % (uint32_t)(2 * slip) != 0) : true;
         if (shouldMove && (canL || canR)) {
             if (c.D() % 2 == 0) {
@@ -681,7 +713,8 @@ __device__ __forceinline__ void rule_b(const TL &T, Ctx &c, int x, int y) {
             T.set_moved(x, y, false);
         }
     } else if (type == T_SOUP) {  // world.cpp:1728-1745
-        t.sc += T.df_load(x, y);
+        Cell t = T.get_active(x, y);
+        t.sc += dfv;
         t.df = 0;
         if (t.sc < Q_MINV) {
             led_add(c, LED_DN, t.id, 1);
@@ -695,6 +728,8 @@ __device__ __forceinline__ void rule_b(const TL &T, Ctx &c, int x, int y) {
     } else {  // GAS, world.cpp:1799-1818
         const int aboveL = T.type(x - 1, y - 1);
         const int aboveR = T.type(x + 1, y - 1);
+        if (aboveL != T_AIR && aboveR != T_AIR) return;
+        const Cell t = T.get_active(x, y);
         if (aboveL == T_AIR && !(aboveR == T_AIR && c.D() % 2 == 0)) {
             T.move(x, y, x - 1, y - 1);
             T.put(x - 1, y - 1, t);
@@ -713,12 +748,12 @@ __device__ __forceinline__ void rule_c(const TL &T, Ctx &c, int x, int y) {
     if (T.vis(x, y)) return;  // world.cpp:1831
     const int sid = T.id(x, y);
     if (mt_type(T.ma[sid]) != T_GAS) return;
-    Cell t = T.get_active(x, y);
-    c.ck = cell_key(c.pk, (uint32_t)x, (uint32_t)y);
-    c.k = 0;
+    c.at(x, y);
     // world.cpp:1862-1889
     const int l = T.type(x - 1, y);
     const int r = T.type(x + 1, y);
+    if (l != T_AIR && r != T_AIR && sid != c.id_steam) return;
+    const Cell t = T.get_active(x, y);
     if (l == T_AIR && !(r == T_AIR && c.D() % 2 == 0)) {
         T.move(x, y, x - 1, y);
         T.put(x - 1, y, t);
@@ -1076,19 +1111,29 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                         divmod_small(tid, nx, rnx, q, r);
                         int dq, dr;
                         divmod_small(T, nx, rnx, dq, dr);
-                        for (int e = tid; e < total; e += T) {
-                            const int dy = ry + q * py, dx = rx + r * px;
-                            if (dx < cw && dy < chh) {
-                                if (sweep == 1)
-                                    rule_b(Tl, c, cx + dx, cy + dy);
-                                else
-                                    rule_c(Tl, c, cx + dx, cy + dy);
-                            }
-                            q += dq;
-                            r += dr;
-                            if (r >= nx) {
-                                r -= nx;
-                                q++;
+                        if (sweep == 1) {
+                            // at most 43 x 43 < 2 T cells: two per thread, their pending
+                            // diffs requested together before either is processed
+                            const int q1 = q + dq + (r + dr >= nx ? 1 : 0);
+                            const int r1 = r + dr - (r + dr >= nx ? nx : 0);
+                            const int dy0 = ry + q * py, dx0 = rx + r * px;
+                            const int dy1 = ry + q1 * py, dx1 = rx + r1 * px;
+                            const bool v0 = tid < total && dx0 < cw && dy0 < chh;
+                            const bool v1 = tid + T < total && dx1 < cw && dy1 < chh;
+                            const int32_t df0 = v0 ? w.df[(size_t)(cy + dy0) * W + cx + dx0] : 0;
+                            const int32_t df1 = v1 ? w.df[(size_t)(cy + dy1) * W + cx + dx1] : 0;
+                            if (v0) rule_b(Tl, c, cx + dx0, cy + dy0, df0);
+                            if (v1) rule_b(Tl, c, cx + dx1, cy + dy1, df1);
+                        } else {
+                            for (int e = tid; e < total; e += T) {
+                                const int dy = ry + q * py, dx = rx + r * px;
+                                if (dx < cw && dy < chh) rule_c(Tl, c, cx + dx, cy + dy);
+                                q += dq;
+                                r += dr;
+                                if (r >= nx) {
+                                    r -= nx;
+                                    q++;
+                                }
                             }
                         }
                         FSE_PT(3 + 2 * sweep)
