@@ -368,14 +368,21 @@ def bench_config2(args, rank, local_rank, world_size):
 
     import falling_sand_engine_gb300 as fse
 
+    from falling_sand_engine_gb300.sharding import shard_worlds
+
     fse.InitMaterials()
     fse.PushMaterials()
-    sizes = config2_sizes(256, 1234 + rank)
+    # the 256 worlds are split across ranks by cell count (no data exchange); one
+    # rank ticks them all
+    all_sizes = config2_sizes(256, 1234)
+    mine = shard_worlds([w * h for w, h in all_sizes], world_size)[rank]
+    sizes = [all_sizes[i] for i in mine]
     cells = sum(w * h for w, h in sizes)
+    total_cells = sum(w * h for w, h in all_sizes)
 
     def make():
         ws = []
-        for i, (w, h) in enumerate(sizes):
+        for i, (w, h) in zip(mine, sizes):
             wd = fse.World(w, h, chunk_size=128, cell_iter=3, seed=1234 + i)
             wd.generate(fse.GEN_MIX, 1234 + i)
             ws.append(wd)
@@ -403,7 +410,7 @@ def bench_config2(args, rank, local_rank, world_size):
     clk = clocks.stop()
     launches = fse.launch_counter() - l0
     b_ms = max_over_ranks(e0.elapsed_time(e1), world_size)
-    value = world_size * cells * args.steps / (b_ms / 1e3) / 1e9
+    value = total_cells * args.steps / (b_ms / 1e3) / 1e9
     digest_b = sum(int(w.state()["id"].astype(np.int64).sum()) for w in worlds[:8])
     batch.close()
     for w in worlds:
@@ -433,7 +440,7 @@ def bench_config2(args, rank, local_rank, world_size):
     for w in worlds:
         w.sync()
     p_ms = max_over_ranks(p0.elapsed_time(p1), world_size)
-    per_world = world_size * cells * args.steps / (p_ms / 1e3) / 1e9
+    per_world = total_cells * args.steps / (p_ms / 1e3) / 1e9
     digest_p = sum(int(w.state()["id"].astype(np.int64).sum()) for w in worlds[:8])
     for w in worlds:
         w.close()
@@ -441,14 +448,16 @@ def bench_config2(args, rank, local_rank, world_size):
     return _common(args, world_size, value, "Gcell/s", b_ms / args.steps,
                    "config2: 256 worlds, sides uniform in {128, 192, ..., 2048}, per-world seeds, mix; batched "
                    "launches from 32-tick CUDA graphs, autotuned launch shape",
-                   {"worlds": 256, "cells": cells, "chunk": 128, "cell_iter": 3, "autotune": choice,
+                   {"worlds": 256, "cells": total_cells, "worlds_this_rank": len(mine), "chunk": 128,
+                    "cell_iter": 3, "autotune": choice,
                     "l2": "inputs larger than L2 (%.2f GB of grid state)" % (cells * 15 / 1e9),
                     "per_world_launch": {"value": round(per_world, 4), "ms_per_step": round(p_ms / args.steps, 4)},
                     "batched_over_per_world": round(value / per_world, 3),
                     "same_result": digest_b == digest_p,
                     "hbm_frac_of_tick": round(value * 1e9 * BYTES_PER_CELL_UPDATE / world_size / (peak * 1e9), 5),
-                    "peak_kind": peak_kind},
-                   launches, clk)
+                    "peak_kind": peak_kind,
+                    "parallelism": "worlds sharded across %d GPUs by cell count, no collective" % world_size},
+                   launches, clk, scaling="strong")
 
 
 def bench_config3(args, rank, local_rank, world_size):
@@ -531,23 +540,30 @@ def bench_config4(args, rank, local_rank, world_size, window_s=1.0):
 
     import falling_sand_engine_gb300 as fse
 
+    from falling_sand_engine_gb300.sharding import shard_worlds
+
     fse.InitMaterials()
     fse.PushMaterials()
-    rng = np.random.default_rng(1234 + rank)
+    # the same 1000 worlds and request stream on every rank; each rank serves the
+    # worlds of its shard (split by cell count) and the requests addressed to them
+    rng = np.random.default_rng(1234)
     sides = np.arange(256, 4097, 64)
+    dims = [(int(rng.choice(sides)), int(rng.choice(sides))) for _ in range(1000)]
+    mine = shard_worlds([w * h for w, h in dims], world_size)[rank]
     srv = fse.Server(120 << 30, 1000)
-    slots, cells = [], {}
+    slot_of, cells = {}, {}
     refused = 0
     t_add = time.perf_counter()
-    for i in range(1000):
-        w, h = int(rng.choice(sides)), int(rng.choice(sides))
+    for i in mine:
+        w, h = dims[i]
         s = srv.try_add_world(w, h, fse.GEN_MIX, 1234 + i, seed=1234 + i,
                               particle_capacity=max(65536, w * h // 32), spawn_capacity=max(65536, w * h // 64))
         if s is None:
             refused += 1
             continue
-        slots.append(s)
+        slot_of[i] = s
         cells[s] = w * h
+    slots = list(slot_of.values())
     t_add = time.perf_counter() - t_add
     # warm-up: one tick of a few worlds
     for s in slots[:4]:
@@ -555,10 +571,15 @@ def bench_config4(args, rank, local_rank, world_size, window_s=1.0):
     while srv.step() > 0:
         pass
     srv.poll()
-    n_req = rng.poisson(2000 * window_s)
-    arr = np.sort(rng.uniform(0.0, window_s * 1e6, n_req))
-    req_slot = rng.choice(slots, n_req)
-    req_ticks = rng.integers(1, 17, n_req)
+    n_all = rng.poisson(2000 * window_s)
+    arr_all = np.sort(rng.uniform(0.0, window_s * 1e6, n_all))
+    world_all = rng.integers(0, 1000, n_all)
+    ticks_all = rng.integers(1, 17, n_all)
+    keep = np.array([int(i) in slot_of for i in world_all], bool)
+    arr = arr_all[keep]
+    req_slot = np.array([slot_of[int(i)] for i in world_all[keep]], np.int64)
+    req_ticks = ticks_all[keep]
+    n_req = len(arr)
     clocks = Clocks(local_rank)
     torch.cuda.synchronize()
     l0 = fse.launch_counter()
@@ -584,22 +605,37 @@ def bench_config4(args, rank, local_rank, world_size, window_s=1.0):
     clk = clocks.stop()
     launches = fse.launch_counter() - l0
     work = float(sum(cells[int(s)] * int(t) for s, t in zip(req_slot, req_ticks)))
-    lat = np.array(lat)
-    value = world_size * work / total_s / 1e9
+    total_s = max_over_ranks(total_s, world_size)
+    work_all = sum(gather_objects(work, world_size))
+    lat = np.concatenate([np.asarray(x, float) for x in gather_objects(lat, world_size)])
+    value = work_all / total_s / 1e9
     bytes_used = srv.bytes_in_use()
     srv.close()
     return _common(args, world_size, value, "Gcell/s", total_s * 1e3 / max(steps, 1),
                    "config4: serving 1000 resident worlds (sides uniform in {256, ..., 4096}), Poisson arrivals at "
                    "2000 req/s of 1-16 ticks for %.1f s, continuous batching, 120 GB admission budget" % window_s,
-                   {"worlds": len(slots), "worlds_refused_by_budget": refused, "requests": int(n_req),
+                   {"worlds": 1000, "worlds_this_rank": len(slots), "worlds_refused_by_budget": refused,
+                    "requests": int(n_all),
                     "hbm_bytes_resident": int(bytes_used), "world_setup_s": round(t_add, 2),
                     "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 2),
                                    "p99": round(float(np.percentile(lat, 99)), 2),
                                    "max": round(float(lat.max()), 2)},
-                    "served_cell_updates": work, "wall_s": round(total_s, 2), "scheduler_steps": steps,
+                    "served_cell_updates": work_all, "wall_s": round(total_s, 2), "scheduler_steps": steps,
                     "timing": "host clock from the first arrival to the last completion (the arrival window plus "
-                              "the drain)"},
-                   launches, clk)
+                              "the drain), max over ranks",
+                    "parallelism": "worlds sharded across %d GPUs by cell count, no collective" % world_size},
+                   launches, clk, scaling="strong")
+
+
+def gather_objects(obj, world_size):
+    """Every rank's obj, in rank order (a host-side exchange of results, not data)."""
+    if world_size == 1:
+        return [obj]
+    import torch.distributed as dist
+
+    out = [None] * world_size
+    dist.all_gather_object(out, obj)
+    return out
 
 
 def profile_traffic(name):
@@ -623,7 +659,8 @@ def max_over_ranks(v, world_size):
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([float(v)], device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(v)], device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 

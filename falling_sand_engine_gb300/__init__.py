@@ -314,10 +314,11 @@ class Batch:
     def autotune(self):
         out = np.zeros(4, np.int32)
         check(self.lib.fse_batch_autotune(self.h, ptr(out)), "batch_autotune")
-        return {"threads": int(out[0]), "ctas_per_sm": int(out[1]), "us": int(out[2]), "index": int(out[3])}
+        return {"colour_ctas_per_sm": int(out[0]), "particle_blocks": int(out[1]), "us": int(out[2]),
+                "index": int(out[3])}
 
-    def set_launch(self, threads, ctas_per_sm):
-        check(self.lib.fse_batch_set_launch(self.h, threads, ctas_per_sm), "batch_set_launch")
+    def set_launch(self, colour_ctas_per_sm, particle_blocks):
+        check(self.lib.fse_batch_set_launch(self.h, colour_ctas_per_sm, particle_blocks), "batch_set_launch")
 
     def sync(self):
         check(self.lib.fse_batch_sync(self.h), "batch_sync")

@@ -26,7 +26,8 @@ struct fse_batch {
     uint32_t *items[4] = {nullptr, nullptr, nullptr, nullptr};
     int n_items[4] = {0, 0, 0, 0};
     int C = 128, max_iter = 0, move_blocks = 1, stage_blocks = 1;
-    int threads = 1024, grid = 0;  // grid 0 = one CTA per chunk
+    int max_move_blocks = 1;       // particle blocks per world that cover the largest list
+    int threads = 1024, grid = 0;  // grid 0 = one CTA per chunk, else persistent CTAs
     cudaStream_t stream = nullptr;
     std::map<int, cudaGraphExec_t> graphs;
 };
@@ -138,7 +139,8 @@ int fse_batch_create(fse_world **worlds, int n, fse_batch **out) {
         }
         b->worlds.push_back(worlds[i]);
         b->max_iter = std::max(b->max_iter, worlds[i]->cell_iter);
-        b->move_blocks = std::max(b->move_blocks, std::min(sm_count() * 2, ceil_div(worlds[i]->part_cap, 256)));
+        b->max_move_blocks = std::max(b->max_move_blocks, std::min(sm_count() * 2, ceil_div(worlds[i]->part_cap, 256)));
+        b->move_blocks = b->max_move_blocks;
         b->stage_blocks = std::max(b->stage_blocks, std::min(sm_count(), ceil_div(worlds[i]->stage_cap, 256)));
     }
     b->C = worlds[0]->C;
@@ -203,18 +205,23 @@ int fse_batch_step_graph(fse_batch *b, int n, int graph_ticks) {
     return batch_sync(b);
 }
 
-int fse_batch_set_launch(fse_batch *b, int threads, int ctas_per_sm) {
-    if (!b || (threads != 256 && threads != 512 && threads != 1024) || ctas_per_sm < 0) return FSE_E_INVAL;
-    b->threads = threads;
-    b->grid = ctas_per_sm == 0 ? 0 : ctas_per_sm * sm_count();
+int fse_batch_set_launch(fse_batch *b, int colour_ctas_per_sm, int particle_blocks) {
+    if (!b || colour_ctas_per_sm < 0 || colour_ctas_per_sm > 1 || particle_blocks < 0) return FSE_E_INVAL;
+    // one 1024-thread CTA fits an SM, so the persistent grid is one CTA per SM
+    b->grid = colour_ctas_per_sm == 0 ? 0 : sm_count();
+    b->move_blocks = particle_blocks == 0 ? b->max_move_blocks : std::min(particle_blocks, b->max_move_blocks);
     for (auto &g : b->graphs) cudaGraphExecDestroy(g.second);
     b->graphs.clear();
     return FSE_OK;
 }
 
 // Time each launch shape on the batch itself and put every world back as it
-// was; the shape never changes results (each cell is owned by one thread per
-// sub-phase whatever the CTA size).
+// was. The shape never changes results: a chunk's pass does not depend on which
+// CTA runs it or when, and particle kernels stride over their lists whatever the
+// grid. Knobs: the colour-pass grid (one CTA per chunk, scheduled by the hardware,
+// or one persistent CTA per SM walking the chunk list) and the number of blocks
+// each world's particle kernels get (batches of small worlds waste launches on
+// empty blocks).
 int fse_batch_autotune(fse_batch *b, int32_t out_choice[4]) {
     if (!b) return FSE_E_INVAL;
     int rc = batch_sync(b);
@@ -225,7 +232,7 @@ int fse_batch_autotune(fse_batch *b, int32_t out_choice[4]) {
             for (auto &s : snaps) snap_free(s);
             return FSE_E_NOMEM;
         }
-    const int cand[][2] = {{1024, 0}, {512, 0}, {1024, 1}, {512, 1}, {256, 0}};
+    const int cand[][2] = {{0, 0}, {1, 0}, {0, 4}, {0, 16}, {1, 16}};
     float best = 1e30f;
     int bi = 0;
     cudaEvent_t e0, e1;

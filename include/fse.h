@@ -226,9 +226,14 @@ int fse_batch_destroy(fse_batch *batch);
 int fse_batch_step(fse_batch *batch, int n_ticks);
 /* capture graph_ticks steps into one CUDA graph (default 32) and replay */
 int fse_batch_step_graph(fse_batch *batch, int n_ticks, int graph_ticks);
-/* choose launch shape by timing candidates on scratch copies; results never change */
+/* choose the launch shape by timing candidates on the batch itself, then restore
+ * every world; results never change. out_choice: colour_ctas_per_sm,
+ * particle_blocks, microseconds of two timed steps, candidate index */
 int fse_batch_autotune(fse_batch *batch, int32_t out_choice[4]);
-int fse_batch_set_launch(fse_batch *batch, int threads, int ctas_per_sm);
+/* colour_ctas_per_sm: 0 = one CTA per chunk, 1 = one persistent CTA per SM walking
+ * the chunk list; particle_blocks: blocks per world of the particle kernels
+ * (0 = enough for the largest particle list) */
+int fse_batch_set_launch(fse_batch *batch, int colour_ctas_per_sm, int particle_blocks);
 int fse_batch_sync(fse_batch *batch);
 /* the CUDA stream (cudaStream_t) the batch enqueues its work on */
 void *fse_batch_stream(fse_batch *batch);
