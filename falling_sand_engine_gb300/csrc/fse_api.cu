@@ -988,20 +988,26 @@ int fse_world_step_graph(fse_world *w, int n) {
         cudaGraphExec_t ex;
         if (it == w->graphs.end()) {
             cudaGraph_t g;
+            // kernels are counted when a replay launches them, not at capture
+            const long long c0 = fse_launch_counter();
             FSE_CUDA_TRY(cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal));
             int erc = FSE_OK;
             for (int i = 0; i < k && erc == FSE_OK; i++)
                 erc = enqueue_step(w->d, 1, w->items, w->n_items, w->cell_iter, w->C, w->threads, w->grid, true,
                                    world_move_blocks(w), world_stage_blocks(w), w->stream);
             cudaError_t e = cudaStreamEndCapture(w->stream, &g);
+            const long long kn = fse_launch_counter() - c0;
+            count_launches(-kn);
             if (erc != FSE_OK || e != cudaSuccess) return FSE_E_CUDA;
             FSE_CUDA_TRY(cudaGraphInstantiate(&ex, g, 0));
             cudaGraphDestroy(g);
             w->graphs[k] = ex;
+            w->graph_kernels[k] = kn;
         } else {
             ex = it->second;
         }
         FSE_CUDA_TRY(cudaGraphLaunch(ex, w->stream));
+        count_launches(w->graph_kernels[k]);
         done += k;
     }
     return fse_world_sync(w);

@@ -30,6 +30,7 @@ struct fse_batch {
     int threads = 1024, grid = 0;  // grid 0 = one CTA per chunk, else persistent CTAs
     cudaStream_t stream = nullptr;
     std::map<int, cudaGraphExec_t> graphs;
+    std::map<int, long long> graph_kernels;  // kernels one replay launches
 };
 
 namespace {
@@ -189,17 +190,23 @@ int fse_batch_step_graph(fse_batch *b, int n, int graph_ticks) {
         cudaGraphExec_t ex;
         if (it == b->graphs.end()) {
             cudaGraph_t g;
+            // kernels are counted when a replay launches them, not at capture
+            const long long c0 = fse_launch_counter();
             FSE_CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
             int erc = batch_enqueue(b, k);
             cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+            const long long kn = fse_launch_counter() - c0;
+            count_launches(-kn);
             if (erc || e != cudaSuccess) return FSE_E_CUDA;
             FSE_CUDA_TRY(cudaGraphInstantiate(&ex, g, 0));
             cudaGraphDestroy(g);
             b->graphs[k] = ex;
+            b->graph_kernels[k] = kn;
         } else {
             ex = it->second;
         }
         FSE_CUDA_TRY(cudaGraphLaunch(ex, b->stream));
+        count_launches(b->graph_kernels[k]);
         done += k;
     }
     return batch_sync(b);

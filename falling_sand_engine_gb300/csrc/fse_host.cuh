@@ -40,6 +40,7 @@ struct fse_world {
     size_t obj_list_cap;
     int64_t *obj_n;       // object list count
     std::map<int, cudaGraphExec_t> graphs;  // n_ticks -> step graph
+    std::map<int, long long> graph_kernels;  // n_ticks -> kernels one replay launches
     size_t bytes;         // device bytes owned
     int threads, grid;    // colour-pass launch shape
     fse::PassTimer *timer;  // colour-pass event timer (enabled on request)
