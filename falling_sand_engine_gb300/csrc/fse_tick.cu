@@ -26,9 +26,11 @@
 // barriers; fse_debug_phase_clocks() reads the totals. Off by default: no cost.
 #ifdef FSE_PHASE_CLOCKS
 __device__ unsigned long long g_phase_clk[16];
+__device__ unsigned long long g_phase_max[16];  // per phase: the largest CTA total; [15]: largest CTA
 #define FSE_PT_DECL                       \
     __shared__ long long pt_acc[16];      \
     long long pt_last = clock64();        \
+    const long long pt_first = pt_last;   \
     if (threadIdx.x < 16) pt_acc[threadIdx.x] = 0;
 #define FSE_PT(k)                           \
     if (threadIdx.x == 0) {                 \
@@ -36,9 +38,13 @@ __device__ unsigned long long g_phase_clk[16];
         pt_acc[(k)] += t_ - pt_last;        \
         pt_last = t_;                       \
     }
-#define FSE_PT_FLUSH     \
-    __syncthreads();     \
-    if (threadIdx.x < 16) atomicAdd(&g_phase_clk[threadIdx.x], (unsigned long long)pt_acc[threadIdx.x]);
+#define FSE_PT_FLUSH                                                                                   \
+    __syncthreads();                                                                                   \
+    if (threadIdx.x < 15) {                                                                            \
+        atomicAdd(&g_phase_clk[threadIdx.x], (unsigned long long)pt_acc[threadIdx.x]);                 \
+        atomicMax(&g_phase_max[threadIdx.x], (unsigned long long)pt_acc[threadIdx.x]);                 \
+    }                                                                                                  \
+    if (threadIdx.x == 15) atomicMax(&g_phase_max[15], (unsigned long long)(clock64() - pt_first));
 #else
 #define FSE_PT_DECL
 #define FSE_PT(k)
@@ -1224,6 +1230,16 @@ extern "C" int fse_debug_phase_clocks(unsigned long long out[16], int reset) {
     if (reset) {
         unsigned long long z[16] = {0};
         cudaMemcpyToSymbol(g_phase_clk, z, sizeof(z));
+    }
+    return 0;
+}
+// the per-phase maxima over CTAs (out[15]: the longest CTA, start to end)
+extern "C" int fse_debug_phase_max(unsigned long long out[16], int reset) {
+    cudaDeviceSynchronize();
+    cudaMemcpyFromSymbol(out, g_phase_max, 16 * sizeof(unsigned long long));
+    if (reset) {
+        unsigned long long z[16] = {0};
+        cudaMemcpyToSymbol(g_phase_max, z, sizeof(z));
     }
     return 0;
 }
