@@ -388,19 +388,45 @@ __device__ __forceinline__ void grid_sync(GridBar *gb, unsigned nblocks, int32_t
 // Rounds 2.. of the deposit resolution for every world, in one cooperative launch.
 // Open requests of round r live in list (r even: req_list2, odd: req_list) with
 // their count in req_count[1] (r even) / req_count[0] (r odd).
+//
+// The last rounds have few open requests (tens, then one or two on a 4096x2048
+// world), and a grid-wide barrier costs far more than their work. So once a round
+// starts with at most DEP_SOLO_MAX open requests (at most one per thread of a
+// block: each request's walk is a chain of global loads and must not queue behind
+// others), block 0 finishes the rounds alone with block barriers and the other
+// blocks leave. Every block reads the same counts (written before the last grid
+// barrier or before the launch), so they all take the same decision.
+constexpr int DEP_SOLO_MAX = 256;
+
 __global__ void k_dep_rounds(const WorldDev *__restrict__ worlds, int n_worlds, const MatTable *__restrict__ mt) {
     __shared__ uint8_t s_type[MAXMAT];
     load_types(s_type, mt);
     GridBar *gb = (GridBar *)worlds[0].bar;
     const unsigned nb = gridDim.x;
-    const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
     int32_t *err = worlds[0].err;
+    bool solo = false;
     for (int r = 0;; r++) {
         if (r > (1 << 22)) {
-            if (gtid == 0) atomicOr(err, ERR_TIMEOUT);
+            if (threadIdx.x == 0 && blockIdx.x == 0) atomicOr(err, ERR_TIMEOUT);
             break;
         }
         const int ci = (r & 1) ? 0 : 1, ni = (r & 1) ? 1 : 0;
+        if (!solo) {
+            int open = 0;
+            for (int wi = 0; wi < n_worlds; wi++) open += ((volatile int32_t *)worlds[wi].req_count)[ci];
+            if (open <= DEP_SOLO_MAX) {
+                if (blockIdx.x != 0) return;
+                solo = true;
+            }
+        }
+        const int gtid = solo ? (int)threadIdx.x : (int)(blockIdx.x * blockDim.x + threadIdx.x);
+        const int gstride = solo ? (int)blockDim.x : (int)(gridDim.x * blockDim.x);
+        auto sync = [&]() {
+            if (solo)
+                __syncthreads();
+            else
+                grid_sync(gb, nb, err);
+        };
         // phase 1: targets against the grid at the start of the round
         for (int wi = 0; wi < n_worlds; wi++) {
             const WorldDev &w = worlds[wi];
@@ -414,7 +440,7 @@ __global__ void k_dep_rounds(const WorldDev *__restrict__ worlds, int n_worlds, 
                 if (t >= 0) w.df[t] = 0x7fffffff;
             }
         }
-        grid_sync(gb, nb, err);
+        sync();
         // phase 2: claims, merges, failures
         for (int wi = 0; wi < n_worlds; wi++) {
             const WorldDev &w = worlds[wi];
@@ -430,7 +456,7 @@ __global__ void k_dep_rounds(const WorldDev *__restrict__ worlds, int n_worlds, 
                     atomicMin(&w.df[t], i);
             }
         }
-        grid_sync(gb, nb, err);
+        sync();
         // phase 3: winners fill, losers go to the next round's list
         for (int wi = 0; wi < n_worlds; wi++) {
             const WorldDev &w = worlds[wi];
@@ -450,9 +476,9 @@ __global__ void k_dep_rounds(const WorldDev *__restrict__ worlds, int n_worlds, 
                 }
             }
         }
-        grid_sync(gb, nb, err);
+        sync();
         int open = 0;
-        for (int wi = 0; wi < n_worlds; wi++) open += worlds[wi].req_count[ni];
+        for (int wi = 0; wi < n_worlds; wi++) open += ((volatile int32_t *)worlds[wi].req_count)[ni];
         if (open == 0) break;
     }
 }

@@ -89,6 +89,7 @@ class Oracle:
                 "om_object_mask": (None, [vp, vp]),
                 "om_set_threads": (None, [i32]),
                 "om_debug_set_lattice": (None, [i32, i32, i32]),
+                "om_debug_last_rounds": (i32, [vp, i32]),
             }
             for name, (res, args) in sig.items():
                 f = getattr(lib, name)
@@ -130,6 +131,12 @@ class Oracle:
 
     def debug_set_lattice(self, sweep, px, py):
         self.lib.om_debug_set_lattice(sweep, px, py)
+
+    def debug_last_rounds(self):
+        """Open deposit requests per round of the last particle tick."""
+        buf = np.zeros(256, np.int64)
+        n = self.lib.om_debug_last_rounds(buf.ctypes.data_as(C.c_void_p), 256)
+        return buf[: min(n, 256)]
 
 
 class OracleWorld:

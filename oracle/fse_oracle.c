@@ -1041,6 +1041,12 @@ void om_debug_set_lattice(int sweep, int px, int py) {
     DBG_PX[sweep] = px;
     DBG_PY[sweep] = py;
 }
+static int DBG_ROUNDS = 0;
+static int64_t DBG_OPEN[256];
+int om_debug_last_rounds(int64_t *open, int cap) {
+    for (int r = 0; r < DBG_ROUNDS && r < cap && r < 256; r++) open[r] = DBG_OPEN[r];
+    return DBG_ROUNDS;
+}
 static void lattice(int sweep, int mode, int *px, int *py) {
     if (DBG_PX[sweep] > 0) {
         *px = DBG_PX[sweep];
@@ -1338,7 +1344,10 @@ int om_particles_tick(om_world *w) {
         claim = (int32_t *)malloc(ncell * sizeof(int32_t));
         for (size_t i = 0; i < ncell; i++) claim[i] = 0x7fffffff;
     }
+    DBG_ROUNDS = 0;
     while (nreq > 0) {
+        if (DBG_ROUNDS < 256) DBG_OPEN[DBG_ROUNDS] = nreq;
+        DBG_ROUNDS++;
         for (int j = 0; j < nreq; j++) {
             int i = rq[j];
             tk[j] = find_target(w, &P[i], req[i], rlx[i], rly[i], &tx[j], &ty[j]);

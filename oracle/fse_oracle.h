@@ -123,6 +123,9 @@ void om_object_mask(const om_world *wd, uint8_t *bits);
 void om_set_threads(int n);
 /* test hook: override the sub-phase lattice of one sweep (px = 0 restores it) */
 void om_debug_set_lattice(int sweep, int px, int py);
+/* statistics of the last particle tick's deposit rounds: returns the number of
+ * rounds, and the open requests of the first min(rounds, cap) rounds in open[] */
+int om_debug_last_rounds(int64_t *open, int cap);
 
 #ifdef __cplusplus
 }
