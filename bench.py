@@ -182,6 +182,7 @@ def bench_config1(args, rank, local_rank, world_size):
     # end to end through the C ABI with host buffers: every step uploads the grid
     # from pinned host memory, ticks, and reads the grid back
     e2e = e2e_config1(world, args, torch, cells, world_size)
+    render = render_config1(fse, torch, W, H, seed, NP) if rank == 0 else None
     cpu = None
     if rank == 0 and world_size == 1 and not args.no_cpu:
         cpu = cpu_baseline_config1(seed)
@@ -197,8 +198,52 @@ def bench_config1(args, rank, local_rank, world_size):
                    "l2": "flushed between timed steps (512 MiB write outside the events)",
                    "parallelism": "one independent world per GPU" if world_size > 1 else "single GPU"},
         "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
-        "wall_s": round(wall, 3),
+        "wall_s": round(wall, 3), "render": render,
     }
+
+
+def render_config1(fse, torch, W, H, seed, NP, ticks=20):
+    """The render passes on the same workload (a world created with render state):
+    after each tick, the dirty-cell texture pass and the particle layer, timed with
+    CUDA events on the world's stream. Algorithmic bytes of the dirty pass: the
+    1-byte mark of every cell, plus for a dirty cell its id, colour, flow sums and
+    mark (read/cleared) and three texels (27 B), plus 20 B more for a liquid
+    (smoothed flows read and written, flow texel)."""
+    stream = torch.cuda.Stream()
+    world = fse.World(W, H, chunk_size=128, cell_iter=3, seed=seed, particle_capacity=4_000_000,
+                      spawn_capacity=2_000_000, stream=stream.cuda_stream, render=True)
+    world.generate(fse.GEN_MIX, seed)
+    world.addCell(config1_particles(NP, W, H, seed))
+    soup = np.array([fse.material_get(i)[0] == fse.SOUP for i in range(fse.material_count())])
+    world.render_dirty(moving=False)
+    for _ in range(3):
+        world.step(1)
+        world.render_dirty(moving=False)
+    d_ms = c_ms = 0.0
+    nbytes = ndirty = 0
+    e = [_ev(torch) for _ in range(4)]
+    for _ in range(ticks):
+        world.step(1)
+        with torch.cuda.stream(stream):
+            e[0].record(stream)
+            world.render_cells()
+            e[1].record(stream)
+            e[2].record(stream)
+        mv = world.render_dirty(moving=True)
+        with torch.cuda.stream(stream):
+            e[3].record(stream)
+        torch.cuda.synchronize()
+        c_ms += e[0].elapsed_time(e[1])
+        d_ms += e[2].elapsed_time(e[3])
+        nbytes += W * H + 27 * int(mv.sum()) + 20 * int(mv[soup].sum())
+        ndirty += int(mv.sum())
+    peak, peak_kind = peaks()
+    gbs = nbytes / (d_ms / 1e3) / 1e9
+    world.close()
+    return {"dirty_pass_ms": round(d_ms / ticks, 4), "dirty_pass_gcells": round(W * H * ticks / (d_ms / 1e3) / 1e9, 3),
+            "dirty_cells_per_tick": ndirty // ticks, "dirty_pass_gbs": round(gbs, 1),
+            "dirty_pass_frac": round(gbs / peak, 4), "peak": peak, "peak_kind": peak_kind,
+            "particle_layer_ms": round(c_ms / ticks, 4), "ticks": ticks}
 
 
 def e2e_config1(world, args, torch, cells, world_size):

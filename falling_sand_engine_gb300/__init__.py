@@ -21,7 +21,7 @@ __all__ = [
     "InitMaterials", "RegisterMaterial", "PushMaterials", "load_lua_materials", "material_find",
     "material_count", "material_get", "set_reaction", "set_interaction", "lib",
     "AIR", "SOLID", "SAND", "SOUP", "GAS", "PASSABLE", "OBJECT", "GEN_EMPTY", "GEN_MIX", "GEN_ZIPF8",
-    "FLUID_ONE",
+    "FLUID_ONE", "CFG_RENDER", "TEX_PIXELS", "TEX_EMISSION", "TEX_FIRE", "TEX_FLOW", "TEX_CELLS", "write_png",
 ]
 
 AIR, SOLID, SAND, SOUP, GAS, PASSABLE, OBJECT = 0, 1, 2, 3, 4, 5, 5
@@ -98,9 +98,13 @@ def set_interaction(mat, other, kind, data1, data2, ofs_x, ofs_y):
     check(lib().fse_material_set_interaction(mat, other, kind, data1, data2, ofs_x, ofs_y), "set_interaction")
 
 
-def _config(chunk_size=128, cell_iter=3, seed=0, particle_capacity=0, spawn_capacity=0, stream=None):
+CFG_RENDER = 1
+TEX_PIXELS, TEX_EMISSION, TEX_FIRE, TEX_FLOW, TEX_CELLS = 0, 1, 2, 3, 4
+
+
+def _config(chunk_size=128, cell_iter=3, seed=0, particle_capacity=0, spawn_capacity=0, stream=None, render=False):
     return FseConfig(chunk_size, cell_iter, seed & 0xFFFFFFFF, particle_capacity, spawn_capacity,
-                     C.c_void_p(stream) if stream else None)
+                     C.c_void_p(stream) if stream else None, CFG_RENDER if render else 0)
 
 
 # ---------------------------------------------------------------------- world
@@ -111,13 +115,13 @@ class World:
               ("diff", np.int32))
 
     def __init__(self, width, height, chunk_size=128, cell_iter=3, seed=0, particle_capacity=0, spawn_capacity=0,
-                 stream=None, _handle=None):
+                 stream=None, render=False, _handle=None):
         self.lib = lib()
         self.width, self.height = int(width), int(height)
         self._owned = _handle is None
         if _handle is None:
             h = C.c_void_p()
-            cfg = _config(chunk_size, cell_iter, seed, particle_capacity, spawn_capacity, stream)
+            cfg = _config(chunk_size, cell_iter, seed, particle_capacity, spawn_capacity, stream, render)
             check(self.lib.fse_world_create(self.width, self.height, C.byref(cfg), C.byref(h)), "world_create")
             self.h = h
         else:
@@ -282,6 +286,23 @@ class World:
         check(self.lib.fse_world_census(self.h, ptr(out)), "census")
         return out.reshape(4, m)
 
+    # -- headless render textures (worlds created with render=True)
+    def render_dirty(self, moving=True):
+        """The dirty-cell texture pass (game.cpp:1994-2067); returns movingTiles."""
+        out = np.zeros(material_count(), np.int64) if moving else None
+        check(self.lib.fse_world_render_dirty(self.h, ptr(out) if moving else None), "render_dirty")
+        return out
+
+    def render_cells(self):
+        """The particle layer (world::renderCells, world.cpp:2006-2028)."""
+        check(self.lib.fse_world_render_cells(self.h), "render_cells")
+
+    def render_texture(self, which):
+        """A texture as an (H, W, 4) uint8 array of r, g, b, a."""
+        out = np.zeros((self.height, self.width, 4), np.uint8)
+        check(self.lib.fse_world_render_read(self.h, int(which), ptr(out)), "render_read")
+        return out
+
 
 class Batch:
     """Many worlds ticked by one launch per colour pass (configs with uneven sizes)."""
@@ -394,3 +415,21 @@ class Server:
         n = C.c_int(0)
         check(self.lib.fse_server_poll(self.h, 0.0, ptr(ids), ptr(done), cap, C.byref(n)), "server_poll")
         return ids[: n.value], done[: n.value]
+
+
+def write_png(path, rgba):
+    """Write an (H, W, 4) uint8 r, g, b, a array as a PNG file (zlib only)."""
+    import struct
+    import zlib
+
+    a = np.ascontiguousarray(rgba, np.uint8)
+    h, w = a.shape[0], a.shape[1]
+    raw = b"".join(b"\x00" + a[y].tobytes() for y in range(h))
+
+    def chunk(tag, data):
+        return struct.pack(">I", len(data)) + tag + data + struct.pack(">I", zlib.crc32(tag + data) & 0xFFFFFFFF)
+
+    png = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 0))
+    png += chunk(b"IDAT", zlib.compress(raw, 6)) + chunk(b"IEND", b"")
+    with open(path, "wb") as f:
+        f.write(png)

@@ -28,6 +28,7 @@ class FseConfig(C.Structure):
     _fields_ = [
         ("chunk_size", C.c_int32), ("cell_iter", C.c_int32), ("seed", C.c_uint32),
         ("particle_capacity", C.c_int32), ("spawn_capacity", C.c_int32), ("stream", C.c_void_p),
+        ("flags", C.c_int32),
     ]
 
 
@@ -76,6 +77,10 @@ SIGNATURES = {
     "fse_world_ledger": (_i, [_vp, _vp]),
     "fse_world_ledger_reset": (_i, [_vp]),
     "fse_world_census": (_i, [_vp, _vp]),
+    "fse_world_render_dirty": (_i, [_vp, _vp]),
+    "fse_world_render_cells": (_i, [_vp]),
+    "fse_world_render_read": (_i, [_vp, _i, _vp]),
+    "fse_world_render_texture": (_vp, [_vp, _i]),
     "fse_tick_noalloc": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _u32, _u32, _vp, _i, C.POINTER(_i), _vp]),
     "fse_batch_create": (_i, [_vp, _i, _pp]),
     "fse_batch_destroy": (_i, [_vp]),

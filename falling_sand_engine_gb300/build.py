@@ -8,7 +8,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfse.so")
-SOURCES = ["fse_tick.cu", "fse_particles.cu", "fse_objects.cu", "fse_api.cu", "fse_batch.cu", "fse_noalloc.cu"]
+SOURCES = ["fse_tick.cu", "fse_particles.cu", "fse_objects.cu", "fse_api.cu", "fse_batch.cu", "fse_noalloc.cu",
+           "fse_render.cu"]
 HEADERS = ["fse_internal.cuh", "fse_host.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

@@ -201,6 +201,9 @@ void build_table(MatTable &t) {
         t.n_react[i] = m.n_react;
         for (int r = 0; r < m.n_react; r++)
             for (int k = 0; k < 3; k++) t.react[i][r][k] = m.react[r][k];
+        t.alpha[i] = (uint32_t)(uint8_t)m.alpha;
+        t.emit_col[i] = m.emit_colour;
+        t.iterations[i] = m.iterations;
     }
     t.n_inter = (int)g_inter.size();
     for (size_t i = 0; i < g_inter.size(); i++)
@@ -589,6 +592,10 @@ static void free_world(fse_world *w) {
     }
     for (int k = 0; k < 4; k++)
         if (w->items[k]) cudaFree(w->items[k]);
+    void *rs[] = {h.dirty, h.flow, w->pflow, w->owner, w->moving, w->tex[0], w->tex[1], w->tex[2], w->tex[3],
+                  w->tex[4]};
+    for (void *q : rs)
+        if (q) cudaFree(q);
     if (w->own_stream && w->stream) cudaStreamDestroy(w->stream);
     if (w->timer) {
         w->timer->drain();
@@ -679,6 +686,17 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
              dalloc(w, &p->ax, pc) && dalloc(w, &p->ay, pc) && dalloc(w, &p->tx, pc) && dalloc(w, &p->ty, pc) &&
              dalloc(w, &p->tf, pc) && dalloc(w, &p->life, pc) && dalloc(w, &p->fade, pc) && dalloc(w, &p->col, pc) &&
              dalloc(w, &p->sc, pc) && dalloc(w, &p->id, pc) && dalloc(w, &p->fl, pc) && dalloc(w, &p->bits, pc);
+    }
+    if (ok && (c.flags & FSE_CFG_RENDER)) {
+        ok = dalloc(w, &h.dirty, n) && dalloc(w, &h.flow, 2 * n) && dalloc(w, &w->pflow, 2 * n) &&
+             dalloc(w, &w->owner, n) && dalloc(w, &w->moving, (size_t)MAXMAT);
+        for (int k = 0; k < 5 && ok; k++) ok = dalloc(w, &w->tex[k], n);
+        if (ok) {
+            cudaMemset(h.dirty, 1, n);  // the first dirty pass paints every cell
+            cudaMemset(h.flow, 0, 2 * n * sizeof(int32_t));
+            cudaMemset(w->pflow, 0, 2 * n * sizeof(float));
+            for (int k = 0; k < 5; k++) cudaMemset(w->tex[k], 0, n * sizeof(uint32_t));
+        }
     }
     // chunk slots per colour: (world 0 << 20) | slot
     for (int tk = 0; tk < 4 && ok; tk++) {
@@ -802,6 +820,7 @@ int fse_world_upload(fse_world *w, const uint16_t *id, const uint32_t *col, cons
         k_check_ids<<<std::max(blocks, 1), 256, 0, w->stream>>>(w->h.id, n, t.n, t.id_air, w->ctr + 7);
         FSE_CUDA_TRY(cudaMemcpyAsync(&bad, w->ctr + 7, 4, cudaMemcpyDeviceToHost, w->stream));
     }
+    if (w->h.dirty) FSE_CUDA_TRY(cudaMemsetAsync(w->h.dirty, 1, n, w->stream));  // repaint everything
     FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
     return bad ? FSE_E_INVAL : FSE_OK;
 }
@@ -876,6 +895,7 @@ int fse_world_generate(fse_world *w, int kind, uint32_t seed) {
                                               f("STONE"), f("GENERIC_AIR"), f("STONE"), f("GENERIC_SAND"), f("WATER"),
                                               f("GENERIC_GAS"), f("DIRT"), f("GENERIC_LIQUID"), f("SOFT_DIRT_SAND"));
     FSE_CUDA_TRY(cudaGetLastError());
+    if (w->h.dirty) FSE_CUDA_TRY(cudaMemsetAsync(w->h.dirty, 1, (size_t)w->W * w->H, w->stream));
     FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
     return FSE_OK;
 }
@@ -911,6 +931,7 @@ int fse_world_set_tile(fse_world *w, int x, int y, uint16_t id, uint32_t col, in
     FSE_CUDA_TRY(cudaMemcpyAsync(w->h.sc + i, &sc, 4, cudaMemcpyHostToDevice, w->stream));
     FSE_CUDA_TRY(cudaMemcpyAsync(w->h.fl + i, &fl, 1, cudaMemcpyHostToDevice, w->stream));
     FSE_CUDA_TRY(cudaMemcpyAsync(w->h.df + i, &zero, 4, cudaMemcpyHostToDevice, w->stream));
+    if (w->h.dirty) FSE_CUDA_TRY(cudaMemsetAsync(w->h.dirty + i, 1, 1, w->stream));
     FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
     return FSE_OK;
 }

@@ -44,6 +44,12 @@ struct fse_world {
     size_t bytes;         // device bytes owned
     int threads, grid;    // colour-pass launch shape
     fse::PassTimer *timer;  // colour-pass event timer (enabled on request)
+    // render state (FSE_CFG_RENDER): textures, smoothed flows, particle-layer owners,
+    // per-material dirty counts
+    uint32_t *tex[5];
+    float *pflow;
+    int32_t *owner;
+    long long *moving;
 };
 
 namespace fse {

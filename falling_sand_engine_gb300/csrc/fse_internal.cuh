@@ -77,6 +77,10 @@ struct MatTable {
     // interactions: flat list of (mat, other, kind, data1, data2, ofsx, ofsy), n_inter entries
     int32_t n_inter;
     int32_t inter[512][7];
+    // rendering: Material::alpha (u8), emitColor, iterations (unclamped)
+    uint32_t alpha[MAXMAT];
+    uint32_t emit_col[MAXMAT];
+    int32_t iterations[MAXMAT];
 };
 
 __host__ __device__ __forceinline__ int mt_type(uint32_t a) { return (int)(a & 0xFF); }
@@ -140,6 +144,10 @@ struct WorldDev {
     unsigned *bar;          // grid barrier {count, generation} of the cooperative deposit kernel
     uint8_t *airmap;        // per 8x8 block of cells: 1 if it held AIR when the particle tick began
     int amw, amh;           // airmap size in blocks
+    // render state, NULL unless the world renders: cells written since the last
+    // dirty pass, and the tick's flows per cell (Q16.16, x then y, wrapping sums)
+    uint8_t *dirty;
+    int32_t *flow;
 };
 
 __host__ __device__ __forceinline__ int ceil_div(int a, int b) { return (a + b - 1) / b; }

@@ -174,6 +174,7 @@ __global__ void __launch_bounds__(1024) k_obj_rounds(WorldDev *wd, const MatTabl
                 w.sc[tg] = 0;
                 w.fl[tg] = 0;
                 w.df[tg] = 0;
+                if (w.dirty) w.dirty[tg] = 1;
                 atomicAdd(&b.n_placed, 1);
                 atomicAdd((unsigned long long *)&w.ledger[LED_CN * MAXMAT + b.id], 1ull);
             } else if (win) {
@@ -184,6 +185,7 @@ __global__ void __launch_bounds__(1024) k_obj_rounds(WorldDev *wd, const MatTabl
                 w.sc[tg] = 0;
                 w.fl[tg] = 0;
                 w.df[tg] = 0;
+                if (w.dirty) w.dirty[tg] = 1;
                 atomicAdd(&b.n_recovered, 1);
                 rem_local++;
             }

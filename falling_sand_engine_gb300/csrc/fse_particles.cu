@@ -293,6 +293,7 @@ __device__ __forceinline__ void dep_fail(const WorldDev &w, int i) {
 __device__ __forceinline__ void dep_merge(const WorldDev &w, const MatTable *mt, int i, int c) {
     // :2119-2125
     atomicAdd(&w.sc[c], w.p.sc[i]);
+    if (w.dirty) w.dirty[c] = 1;
     w.p_state[i] = PS_DEAD;
     atomicAdd((unsigned long long *)&w.ledger[LED_DN * MAXMAT + w.p.id[i]], 1ull);
 }
@@ -303,6 +304,7 @@ __device__ __forceinline__ void dep_fill(const WorldDev &w, int i, int c) {
     w.col[c] = w.p.col[i];
     w.sc[c] = w.p.sc[i];
     w.fl[c] = w.p.fl[i];
+    if (w.dirty) w.dirty[c] = 1;
     w.p_state[i] = PS_DEAD;
 }
 

@@ -336,11 +336,20 @@ __device__ __forceinline__ bool can_sink(const uint32_t *ma, const float *md, in
     return t == T_AIR || (t != T_SOLID && md[other] < md[self]);
 }
 
-// one SOUP flow towards (nx, ny), shared by the four directions of world.cpp:1309-1460
+// the world of the CTA's current chunk (copied per chunk by thread 0)
+__shared__ WorldDev s_w;
+
+// one SOUP flow from (x, y) towards (x + dx, y + dy), shared by the four directions
+// of world.cpp:1309-1460; a rendering world also adds it to the flow of (x, y)
+// (flowX -= / += flow for left / right, flowY += / -= for down / up,
+// world.cpp:1334,1374,1402,1432), a reduction no other cell of the sub-phase makes
 template <class TL>
-__device__ __forceinline__ void soup_flow(const TL &T, Ctx &c, Cell &t, int32_t &rem, int32_t flow, int nT, int nx,
-                                          int ny) {
+__device__ __forceinline__ void soup_flow(const TL &T, Ctx &c, Cell &t, int32_t &rem, int32_t flow, int nT, int x,
+                                          int y, int dx, int dy) {
     if (flow == 0) return;
+    const int nx = x + dx, ny = y + dy;
+    int32_t *fw = s_w.flow;
+    if (fw) atomicAdd(&fw[2 * ((size_t)y * T.W + x) + (dx != 0 ? 0 : 1)], (dx + dy) * flow);
     rem -= flow;
     t.df -= flow;
     if (nT == T_AIR) {
@@ -535,7 +544,7 @@ __device__ __forceinline__ void rule_a(const TL &T, Ctx &c, int x, int y) {
         const bool airBelow = bT == T_AIR;
         if ((airBelow && c.iter <= 2) || bid == (int)t.id) {
             int32_t dst = (bT == T_SOUP) ? T.sc(x, y + 1) : 0;
-            soup_flow(T, c, t, rem, clampflow(vflow(start, dst) - dst, start), bT, x, y + 1);
+            soup_flow(T, c, t, rem, clampflow(vflow(start, dst) - dst, start), bT, x, y, 0, 1);
         } else if (c.iter == 0 && bT == T_SOUP && bid != (int)t.id) {
             if (c.D() % 10 == 0) {
                 t.df += T.df_load(x, y);  // the cell leaves its position: carry the whole diff
@@ -558,7 +567,7 @@ __device__ __forceinline__ void rule_a(const TL &T, Ctx &c, int x, int y) {
         const bool canR = (rT == T_AIR || rid == (int)t.id) && !airBelow;
         if (canL) {
             int32_t dst = (lT == T_SOUP) ? T.sc(x - 1, y) : 0;
-            soup_flow(T, c, t, rem, clampflow(canR ? (rem - dst) / 3 : (rem - dst) / 2, rem), lT, x - 1, y);
+            soup_flow(T, c, t, rem, clampflow(canR ? (rem - dst) / 3 : (rem - dst) / 2, rem), lT, x, y, -1, 0);
         }
         if (rem < Q_MINV) {
             t.df -= rem;
@@ -568,7 +577,7 @@ __device__ __forceinline__ void rule_a(const TL &T, Ctx &c, int x, int y) {
         }
         if (canR) {
             int32_t dst = (rT == T_SOUP) ? T.sc(x + 1, y) : 0;
-            soup_flow(T, c, t, rem, clampflow((rem - dst) / 2, rem), rT, x + 1, y);
+            soup_flow(T, c, t, rem, clampflow((rem - dst) / 2, rem), rT, x, y, 1, 0);
         }
         if (rem < Q_MINV) {
             t.df -= rem;
@@ -580,7 +589,7 @@ __device__ __forceinline__ void rule_a(const TL &T, Ctx &c, int x, int y) {
         const int tT = mt_type(ma[tid]);
         if (tT == T_AIR || tid == (int)t.id) {
             int32_t dst = (tT == T_SOUP) ? T.sc(x, y - 1) : 0;
-            soup_flow(T, c, t, rem, clampflow(rem - vflow(rem, dst), rem), tT, x, y - 1);
+            soup_flow(T, c, t, rem, clampflow(rem - vflow(rem, dst), rem), tT, x, y, 0, -1);
         } else if (c.iter == 0 && tT == T_SOUP && tid != (int)t.id) {
             if (c.D() % 10 == 0) {
                 t.df += T.df_load(x, y);
@@ -901,7 +910,6 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
     k_colour_pass(const WorldDev *__restrict__ worlds, const uint32_t *__restrict__ items, int n_items, int iter, int tk,
                   const MatTable *__restrict__ mt) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ WorldDev s_w;
     SmemHead &S = *reinterpret_cast<SmemHead *>(smem);
     unsigned char *planes = smem + ((sizeof(SmemHead) + 15) & ~(size_t)15);
 
@@ -1174,6 +1182,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                     w.fl[gb + gx] = (uint8_t)(Tl.s_fl[i] & (uint8_t)~VISITED);
                     w.sc[gb + gx] = Tl.s_sc[i];
                     w.col[gb + gx] = Tl.s_col[i];
+                    if (w.dirty) w.dirty[gb + gx] = 1;
                 }
             }
         }

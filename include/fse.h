@@ -72,7 +72,12 @@ typedef struct fse_config {
     int32_t particle_capacity; /* max live particles; 0 -> max(65536, cells / 4) */
     int32_t spawn_capacity;    /* max particles spawned per tick; 0 -> particle_capacity */
     void *stream;         /* cudaStream_t to bind; NULL -> a library-owned stream */
+    int32_t flags;        /* FSE_CFG_* */
 } fse_config;
+
+/* the world keeps the render state of fse_world_render_*: a per-cell dirty plane
+ * and the tick's per-cell flow sums (13 more bytes per cell, 20 with textures) */
+#define FSE_CFG_RENDER 1
 
 /* One free particle (CellData, source/engine/game_utils/cells.h:15-36). 56 bytes. */
 typedef struct fse_particle {
@@ -191,6 +196,28 @@ int fse_world_ledger(fse_world *world, int64_t *out);
 int fse_world_ledger_reset(fse_world *world);
 /* 4 rows: grid_count, grid_fluid (amount + pending diff), part_count, part_fluid */
 int fse_world_census(fse_world *world, int64_t *out);
+
+/* -------------------------------------------------------------- rendering */
+/* Headless device textures of the game's per-tick texture updates, 4 bytes per
+ * cell (r, g, b, a), row-major. Worlds created with FSE_CFG_RENDER only
+ * (FSE_E_STATE otherwise). Every cell starts dirty; the tick, deposits, bodies
+ * and uploads mark the cells they write. */
+#define FSE_TEX_PIXELS 0   /* pixels_ar: colour and material alpha; AIR transparent */
+#define FSE_TEX_EMISSION 1 /* pixelsEmission_ar: the material's emitColor */
+#define FSE_TEX_FIRE 2     /* pixelsFire_ar: FIRE cells, kept until the cell turns AIR */
+#define FSE_TEX_FLOW 3     /* pixelsFlow_ar: smoothed liquid flow */
+#define FSE_TEX_CELLS 4    /* pixelsCells_ar: the free-particle layer */
+/* the dirty-cell pass (game.cpp:1994-2067): repaints the dirty cells and clears
+ * their marks; moving (fse_material_count() entries, may be NULL) receives the
+ * dirty cells per material (movingTiles) */
+int fse_world_render_dirty(fse_world *world, int64_t *moving);
+/* the particle layer (world::renderCells, world.cpp:2006-2028, after the clear of
+ * game.cpp:1881): later particles in list order cover earlier ones */
+int fse_world_render_cells(fse_world *world);
+/* copy a texture (W * H * 4 bytes) to host memory */
+int fse_world_render_read(fse_world *world, int which, uint8_t *out);
+/* the texture's device pointer (valid until the world is destroyed), NULL on error */
+void *fse_world_render_texture(fse_world *world, int which);
 
 /* ------------------------------------------------- allocation-free tick */
 /* One world::tick() (no particle step) on cell planes the caller owns in device

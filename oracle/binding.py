@@ -90,6 +90,11 @@ class Oracle:
                 "om_set_threads": (None, [i32]),
                 "om_debug_set_lattice": (None, [i32, i32, i32]),
                 "om_debug_last_rounds": (i32, [vp, i32]),
+                "om_render_enable": (None, [vp]),
+                "om_render_dirty": (None, [vp, vp]),
+                "om_render_cells": (None, [vp]),
+                "om_render_get": (None, [vp, i32, vp]),
+                "om_render_dirty_get": (None, [vp, vp]),
             }
             for name, (res, args) in sig.items():
                 f = getattr(lib, name)
@@ -238,4 +243,26 @@ class OracleWorld:
         n = self.w * self.h
         out = np.zeros((n + 7) // 8, np.uint8)
         self.lib.om_object_mask(self.h_, _ptr(out))
+        return out
+
+    # -- render textures
+    def render_enable(self):
+        self.lib.om_render_enable(self.h_)
+
+    def render_dirty(self):
+        moving = np.zeros(256, np.int64)
+        self.lib.om_render_dirty(self.h_, _ptr(moving))
+        return moving[: self.o.material_count()]
+
+    def render_cells(self):
+        self.lib.om_render_cells(self.h_)
+
+    def render_texture(self, which):
+        out = np.zeros((self.h, self.w, 4), np.uint8)
+        self.lib.om_render_get(self.h_, which, _ptr(out))
+        return out
+
+    def render_dirty_plane(self):
+        out = np.zeros((self.h, self.w), np.uint8)
+        self.lib.om_render_dirty_get(self.h_, _ptr(out))
         return out

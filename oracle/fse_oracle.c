@@ -359,7 +359,23 @@ struct om_world {
     long viol;
     int32_t stamp;
     int32_t *wst, *wown, *rst, *rown;
+    /* render state (om_render_enable): cells written since the last dirty pass, the
+     * tick's per-cell flows (Q16.16, x then y, wrapping int32 sums), the textures
+     * (4 bytes r, g, b, a per cell) and the smoothed flows */
+    uint8_t *dirty;
+    int32_t *flow;
+    uint32_t *tex[5];
+    float *pflow;
 };
+
+static inline void mark_dirty(om_world *w, size_t i) {
+    if (w->dirty) w->dirty[i] = 1;
+}
+static inline void add_flow(om_world *w, int x, int y, int axis, int32_t v) {
+    if (!w->flow || x < 0 || y < 0 || x >= w->W || y >= w->H) return;
+    int32_t *f = &w->flow[2 * ((size_t)y * w->W + x) + axis];
+    *f = (int32_t)((uint32_t)*f + (uint32_t)v);
+}
 
 static inline int inw(const om_world *w, int x, int y) { return x >= 0 && y >= 0 && x < w->W && y < w->H; }
 
@@ -395,6 +411,10 @@ void om_world_free(om_world *wd) {
     free(wd->wown);
     free(wd->rst);
     free(wd->rown);
+    free(wd->dirty);
+    free(wd->flow);
+    for (int k = 0; k < 5; k++) free(wd->tex[k]);
+    free(wd->pflow);
     free(wd);
 }
 
@@ -406,6 +426,7 @@ void om_world_set(om_world *wd, const uint16_t *id, const uint32_t *col, const i
     memcpy(wd->sc, sc, n * 4);
     memcpy(wd->fl, fl, n);
     memcpy(wd->df, df, n * 4);
+    if (wd->dirty) memset(wd->dirty, 1, n);
 }
 
 void om_world_get(const om_world *wd, uint16_t *id, uint32_t *col, int32_t *sc, uint8_t *fl, int32_t *df) {
@@ -485,15 +506,17 @@ static inline void pcell(om_world *w, int x, int y, cell_t c) {
     w->sc[i] = c.sc;
     w->col[i] = c.col;
     w->df[i] = (M[c.id].type == T_SOUP) ? c.df : 0;
+    mark_dirty(w, i);
 }
 static inline void set_moved(om_world *w, int x, int y, int on) {
     chk(w, x, y, 1);
     if (!inw(w, x, y)) return;
     size_t i = (size_t)y * w->W + x;
-    if (on)
-        w->fl[i] |= MOVED;
-    else
-        w->fl[i] &= (uint8_t)~MOVED;
+    uint8_t f = on ? (uint8_t)(w->fl[i] | MOVED) : (uint8_t)(w->fl[i] & (uint8_t)~MOVED);
+    if (f != w->fl[i]) {
+        w->fl[i] = f;
+        mark_dirty(w, i); /* a write that changes nothing marks nothing */
+    }
 }
 static inline void add_diff(om_world *w, int x, int y, int32_t v) {
     chk(w, x, y, 1);
@@ -770,6 +793,7 @@ static void rule_a(rctx *c, int x, int y) {
                     led_add(c, LED_CN, t.id, 1);
                 } else
                     add_diff(w, x, y + 1, flow);
+                add_flow(w, x, y, 1, flow); /* :1334 flowY += flow */
             }
         } else if (c->iter == 0 && bT == T_SOUP && bottom.id != t.id) {
             if (D(c) % 10 == 0) {
@@ -802,6 +826,7 @@ static void rule_a(rctx *c, int x, int y) {
                     led_add(c, LED_CN, t.id, 1);
                 } else
                     add_diff(w, x - 1, y, flow);
+                add_flow(w, x, y, 0, -flow); /* :1374 flowX -= flow */
             }
         }
         if (rem < Q_MINV) {
@@ -822,6 +847,7 @@ static void rule_a(rctx *c, int x, int y) {
                     led_add(c, LED_CN, t.id, 1);
                 } else
                     add_diff(w, x + 1, y, flow);
+                add_flow(w, x, y, 0, flow); /* :1402 flowX += flow */
             }
         }
         if (rem < Q_MINV) {
@@ -844,6 +870,7 @@ static void rule_a(rctx *c, int x, int y) {
                     led_add(c, LED_CN, t.id, 1);
                 } else
                     add_diff(w, x, y - 1, flow);
+                add_flow(w, x, y, 1, -flow); /* :1432 flowY -= flow */
             }
         } else if (c->iter == 0 && tT == T_SOUP && top.id != t.id) {
             if (D(c) % 10 == 0) {
@@ -1368,6 +1395,7 @@ int om_particles_tick(om_world *w) {
             size_t ci = (size_t)ty[j] * w->W + tx[j];
             if (tk[j] == 2) { /* :2119-2125 */
                 w->sc[ci] += p->scalar;
+                mark_dirty(w, ci);
                 dead[i] = 1;
                 w->led[LED_DN][p->id] += 1;
                 continue;
@@ -1376,6 +1404,7 @@ int om_particles_tick(om_world *w) {
                 w->id[ci] = p->id;
                 w->col[ci] = p->colour;
                 w->sc[ci] = p->scalar;
+                mark_dirty(w, ci);
                 w->fl[ci] = p->flags;
                 w->df[ci] = 0;
                 dead[i] = 1;
@@ -1529,6 +1558,99 @@ void om_world_generate(om_world *w, int kind, uint32_t seed) {
             if (m->f_mod > 0)
                 w->col[i] = m->f_base + ((uint32_t)(m->f_lo + (int)(draw_k(ck, 1) % (uint32_t)m->f_mod)) << m->f_shift);
         }
+    if (w->dirty) memset(w->dirty, 1, (size_t)w->W * w->H);
+}
+
+/* --------------------------------------------------------------- rendering */
+/* Headless textures of the game's per-tick update, 4 bytes (r, g, b, a) per cell.
+ * om_render_enable allocates them with every cell dirty; from then on the tick,
+ * particle deposits and bodies mark the cells they write, and soup flows add to
+ * the per-cell flow sums (world.cpp:1334,1374,1402,1432). */
+void om_render_enable(om_world *w) {
+    size_t n = (size_t)w->W * w->H;
+    if (w->dirty) return;
+    w->dirty = (uint8_t *)malloc(n);
+    memset(w->dirty, 1, n);
+    w->flow = (int32_t *)calloc(2 * n, 4);
+    for (int k = 0; k < 5; k++) w->tex[k] = (uint32_t *)calloc(n, 4);
+    w->pflow = (float *)calloc(2 * n, 4);
+}
+
+static inline uint32_t rgba(uint32_t r, uint32_t g, uint32_t b, uint32_t a) {
+    return (r & 0xff) | ((g & 0xff) << 8) | ((b & 0xff) << 16) | ((a & 0xff) << 24);
+}
+
+/* flow texture channel, game.cpp:2048-2053 (double arithmetic, truncation to u8) */
+static inline uint32_t flow_byte(float f, int iterations) {
+    double a = (double)f * (3.0 / iterations + 0.5) / 4.0 + 0.5;
+    double c = a < 0.0 ? 0.0 : a;
+    c = c > 1.0 ? 1.0 : c;
+    return (uint32_t)(c * 255);
+}
+
+/* the dirty-cell pass, game.cpp:1994-2067: moving[mat] counts the dirty cells */
+void om_render_dirty(om_world *w, int64_t *moving) {
+    if (!w->dirty) return;
+    size_t n = (size_t)w->W * w->H;
+    if (moving) memset(moving, 0, sizeof(int64_t) * NMAT);
+    for (size_t i = 0; i < n; i++) {
+        if (!w->dirty[i]) continue;
+        w->dirty[i] = 0;
+        const mat_t *m = &M[w->id[i]];
+        if (moving) moving[w->id[i]]++;
+        int32_t *fl = &w->flow[2 * i];
+        if (m->type == T_AIR) {
+            w->tex[0][i] = 0;
+            w->tex[2][i] = 0;
+            w->tex[1][i] = 0;
+            fl[0] = fl[1] = 0;
+            continue;
+        }
+        uint32_t col = w->col[i], emit = m->emit_colour;
+        w->tex[0][i] = rgba(col >> 16, col >> 8, col, (uint32_t)m->alpha);
+        w->tex[1][i] = rgba(emit >> 16, emit >> 8, emit, emit >> 24);
+        if ((int)w->id[i] == ID_FIRE) w->tex[2][i] = rgba(col >> 16, col >> 8, col, (uint32_t)m->alpha);
+        if (m->type == T_SOUP) {
+            float *pf = &w->pflow[2 * i];
+            float fx = (float)fl[0] * (1.0f / 65536.0f), fy = (float)fl[1] * (1.0f / 65536.0f);
+            /* f32 + (f32 - f32) * 0.25 evaluated in double, stored as f32 */
+            float nfx = (float)((double)pf[0] + (double)(fx - pf[0]) * 0.25);
+            float nfy = (float)((double)pf[1] + (double)(fy - pf[1]) * 0.25);
+            if (nfy < 0) nfy = (float)((double)nfy * 0.5);
+            w->tex[3][i] = rgba(flow_byte(nfx, m->iterations), flow_byte(nfy, m->iterations), 0, 0xff);
+            pf[0] = nfx;
+            pf[1] = nfy;
+        }
+        fl[0] = fl[1] = 0;
+    }
+}
+
+/* the particle layer, world::renderCells (world.cpp:2006-2028) after the clear of
+ * game.cpp:1881: particles in list order, a later one over an earlier one */
+void om_render_cells(om_world *w) {
+    if (!w->tex[4]) return;
+    size_t n = (size_t)w->W * w->H;
+    memset(w->tex[4], 0, n * 4);
+    for (int k = 0; k < w->parts.n; k++) {
+        const om_particle *p = &w->parts.p[k];
+        if (!(p->x >= 0 && p->x < (float)w->W && p->y >= 0 && p->y < (float)w->H)) continue;
+        float amod = 1.0f;
+        if ((p->bits & 2) && p->lifetime < p->fade_time) amod = (float)p->lifetime / (float)p->fade_time;
+        float a = (float)(uint8_t)M[p->id].alpha * amod; /* Material::alpha is a u8 */
+        uint32_t ab = a > 0.0f ? (uint32_t)a : 0u; /* negative lifetimes draw transparent */
+        size_t i = (size_t)(int)p->y * w->W + (int)p->x;
+        w->tex[4][i] = rgba(p->colour >> 16, p->colour >> 8, p->colour, ab);
+    }
+}
+
+/* which: 0 pixels, 1 emission, 2 fire, 3 flow, 4 particle layer */
+void om_render_get(const om_world *w, int which, uint32_t *out) {
+    if (which < 0 || which > 4 || !w->tex[which]) return;
+    memcpy(out, w->tex[which], (size_t)w->W * w->H * 4);
+}
+
+void om_render_dirty_get(const om_world *w, uint8_t *out) {
+    if (w->dirty) memcpy(out, w->dirty, (size_t)w->W * w->H);
 }
 
 /* ------------------------------------------------------------------ ledger */
@@ -1652,6 +1774,7 @@ void om_object_stamp(om_world *w, om_body *bodies, int n) {
             w->sc[ci] = 0;
             w->fl[ci] = 0;
             w->df[ci] = 0;
+            mark_dirty(w, ci);
             bd->n_placed++;
             w->led[LED_CN][bd->id] += 1;
         }
@@ -1727,6 +1850,7 @@ long om_object_readback(om_world *w, const om_body *bodies_c, int n) {
             w->sc[ci] = 0;
             w->fl[ci] = 0;
             w->df[ci] = 0;
+            mark_dirty(w, ci);
             bd->n_recovered++;
             removed++;
         }

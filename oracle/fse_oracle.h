@@ -127,6 +127,14 @@ void om_debug_set_lattice(int sweep, int px, int py);
  * rounds, and the open requests of the first min(rounds, cap) rounds in open[] */
 int om_debug_last_rounds(int64_t *open, int cap);
 
+/* headless render textures (game.cpp:1994-2067, world.cpp:2006-2028), 4 bytes
+ * r, g, b, a per cell; which: 0 pixels, 1 emission, 2 fire, 3 flow, 4 particles */
+void om_render_enable(om_world *w);
+void om_render_dirty(om_world *w, int64_t *moving);
+void om_render_cells(om_world *w);
+void om_render_get(const om_world *w, int which, uint32_t *out);
+void om_render_dirty_get(const om_world *w, uint8_t *out);
+
 #ifdef __cplusplus
 }
 #endif
