@@ -203,7 +203,7 @@ void build_table(MatTable &t) {
             for (int k = 0; k < 3; k++) t.react[i][r][k] = m.react[r][k];
         t.alpha[i] = (uint32_t)(uint8_t)m.alpha;
         t.emit_col[i] = m.emit_colour;
-        t.iterations[i] = m.iterations;
+        t.flow_k[i] = 3.0 / m.iterations + 0.5;  // IEEE double, as the reference evaluates it
     }
     t.n_inter = (int)g_inter.size();
     for (size_t i = 0; i < g_inter.size(); i++)

@@ -77,10 +77,11 @@ struct MatTable {
     // interactions: flat list of (mat, other, kind, data1, data2, ofsx, ofsy), n_inter entries
     int32_t n_inter;
     int32_t inter[512][7];
-    // rendering: Material::alpha (u8), emitColor, iterations (unclamped)
+    // rendering: Material::alpha (u8), emitColor, and 3.0 / iterations + 0.5 of the
+    // flow texture (game.cpp:2048), evaluated once in double
     uint32_t alpha[MAXMAT];
     uint32_t emit_col[MAXMAT];
-    int32_t iterations[MAXMAT];
+    double flow_k[MAXMAT];
 };
 
 __host__ __device__ __forceinline__ int mt_type(uint32_t a) { return (int)(a & 0xFF); }

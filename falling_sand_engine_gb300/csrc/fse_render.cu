@@ -4,9 +4,11 @@
 // game.cpp:1881). Textures are device planes of 4 bytes per cell (r, g, b, a).
 //
 // The dirty pass reads one byte per cell (the dirty mark) and touches the rest only
-// for dirty cells, so it is bound by HBM. The flow channel repeats the reference's
-// mixed float/double arithmetic operation by operation with explicitly rounded
-// intrinsics, so it agrees bit for bit with a strict IEEE CPU evaluation.
+// for dirty cells. The flow channel gives the results of the reference's mixed
+// float/double arithmetic bit for bit: the final scaling stays in double, and the
+// smoothing, whose double evaluation provably equals the float one for normal
+// operands, runs in float except for subnormal operands (FP64 is slow here and
+// was the pass's bound when every step ran in double).
 #include <algorithm>
 
 #include "fse_host.cuh"
@@ -25,22 +27,46 @@ __device__ __forceinline__ uint32_t rgba(uint32_t r, uint32_t g, uint32_t b, uin
 }
 
 // game.cpp:2048-2053: a = flow * (3.0 / iterations + 0.5) / 4.0 + 0.5 in double,
-// clamped to [0, 1], times 255, truncated to a byte
-__device__ __forceinline__ uint32_t flow_byte(float f, int iterations) {
-    const double k = __dadd_rn(__ddiv_rn(3.0, (double)iterations), 0.5);
-    const double a = __dadd_rn(__ddiv_rn(__dmul_rn((double)f, k), 4.0), 0.5);
-    double c = a < 0.0 ? 0.0 : a;
-    c = c > 1.0 ? 1.0 : c;
-    return (uint32_t)__dmul_rn(c, 255.0);
+// clamped to [0, 1], times 255, truncated to a byte. k = 3.0 / iterations + 0.5
+// comes from the material table; / 4.0 is the exact * 0.25. (A NaN, from a
+// material with zero iterations, gives 0.)
+__device__ __forceinline__ uint32_t flow_byte(float f, double k) {
+    const double a = __dadd_rn(__dmul_rn(__dmul_rn((double)f, k), 0.25), 0.5);
+    if (!(a > 0.0)) return 0u;
+    return a >= 1.0 ? 255u : (uint32_t)__dmul_rn(a, 255.0);
+}
+
+// prev + (cur - prev) * 0.25 with the product and the sum in double, rounded to
+// float (game.cpp:2041-2042). For normal operands this equals the float
+// evaluation: * 0.25 is exact, and the double sum of two floats is exact unless
+// their exponents differ by more than 28, when the smaller one is below half a
+// float ulp of the larger either way. Subnormal operands (flows decaying towards
+// zero) take the double path.
+__device__ __forceinline__ float smooth(float prev, float cur) {
+    const float d = __fsub_rn(cur, prev);
+    const float m = 0x1p-120f;
+    if ((fabsf(prev) >= m || prev == 0.0f) && (fabsf(d) >= m || d == 0.0f))
+        return __fadd_rn(prev, __fmul_rn(d, 0.25f));
+    return __double2float_rn(__dadd_rn((double)prev, __dmul_rn((double)d, 0.25)));
+}
+
+// v * 0.5 in double, rounded to float (game.cpp:2043): exact halving for normal v
+__device__ __forceinline__ float half_of(float v) {
+    if (fabsf(v) >= 0x1p-120f) return __fmul_rn(v, 0.5f);
+    return __double2float_rn(__dmul_rn((double)v, 0.5));
 }
 
 // one dirty cell of game.cpp:1997-2063
 __device__ __forceinline__ void paint(const WorldDev &w, const RenderTex &rt, size_t i, const uint8_t *s_type,
-                                      const uint32_t *s_alpha, const uint32_t *s_emit, const int *s_iter, int id_fire,
+                                      const uint32_t *s_alpha, const uint32_t *s_emit, const double *s_k, int id_fire,
                                       unsigned *s_mov) {
     w.dirty[i] = 0;
     const int id = w.id[i];
-    atomicAdd(&s_mov[id], 1u);  // movingTiles
+    {
+        // movingTiles: lanes with the same material add once
+        const unsigned grp = __match_any_sync(__activemask(), id);
+        if ((threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&s_mov[id], (unsigned)__popc(grp));
+    }
     int32_t *fl = w.flow + 2 * i;
     const int type = s_type[id];
     if (type == T_AIR) {
@@ -60,11 +86,10 @@ __device__ __forceinline__ void paint(const WorldDev &w, const RenderTex &rt, si
         float *pf = rt.pflow + 2 * i;
         const float fx = __fmul_rn(__int2float_rn(fl[0]), 1.0f / 65536.0f);
         const float fy = __fmul_rn(__int2float_rn(fl[1]), 1.0f / 65536.0f);
-        // f32 + (f32 - f32) * 0.25: the product and the sum in double, stored as f32
-        const float nfx = __double2float_rn(__dadd_rn((double)pf[0], __dmul_rn((double)__fsub_rn(fx, pf[0]), 0.25)));
-        float nfy = __double2float_rn(__dadd_rn((double)pf[1], __dmul_rn((double)__fsub_rn(fy, pf[1]), 0.25)));
-        if (nfy < 0.0f) nfy = __double2float_rn(__dmul_rn((double)nfy, 0.5));
-        rt.tex[3][i] = rgba(flow_byte(nfx, s_iter[id]), flow_byte(nfy, s_iter[id]), 0u, 0xffu);
+        const float nfx = smooth(pf[0], fx);
+        float nfy = smooth(pf[1], fy);
+        if (nfy < 0.0f) nfy = half_of(nfy);
+        rt.tex[3][i] = rgba(flow_byte(nfx, s_k[id]), flow_byte(nfy, s_k[id]), 0u, 0xffu);
         pf[0] = nfx;
         pf[1] = nfy;
     }
@@ -72,34 +97,27 @@ __device__ __forceinline__ void paint(const WorldDev &w, const RenderTex &rt, si
     fl[1] = 0;
 }
 
-// the dirty pass over one world; four cells per thread, their marks read as one word
+// the dirty pass over one world, one cell per thread (consecutive cells on
+// consecutive lanes, so every plane is read and written coalesced)
 __global__ void k_render_dirty(const WorldDev *__restrict__ wd, const MatTable *__restrict__ mt, RenderTex rt) {
     __shared__ uint8_t s_type[MAXMAT];
     __shared__ uint32_t s_alpha[MAXMAT], s_emit[MAXMAT];
-    __shared__ int s_iter[MAXMAT];
+    __shared__ double s_k[MAXMAT];
     __shared__ unsigned s_mov[MAXMAT];
     for (int k = threadIdx.x; k < MAXMAT; k += blockDim.x) {
         const bool ok = k < mt->n;
         s_type[k] = (uint8_t)(ok ? mt_type(mt->a[k]) : 0);
         s_alpha[k] = ok ? mt->alpha[k] : 0u;
         s_emit[k] = ok ? mt->emit_col[k] : 0u;
-        s_iter[k] = ok ? mt->iterations[k] : 1;
+        s_k[k] = ok ? mt->flow_k[k] : 0.0;
         s_mov[k] = 0u;
     }
     __syncthreads();
     const WorldDev &w = *wd;
     const int id_fire = mt->id_fire;
-    const size_t n = (size_t)w.W * w.H, n4 = n / 4;
-    const uint32_t *d4 = reinterpret_cast<const uint32_t *>(w.dirty);  // cudaMalloc alignment
-    for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < n4; g += (size_t)gridDim.x * blockDim.x) {
-        const uint32_t m = d4[g];
-        if (m == 0u) continue;
-#pragma unroll
-        for (int k = 0; k < 4; k++)
-            if ((m >> (8 * k)) & 0xffu) paint(w, rt, 4 * g + k, s_type, s_alpha, s_emit, s_iter, id_fire, s_mov);
-    }
-    for (size_t i = 4 * n4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        if (w.dirty[i]) paint(w, rt, i, s_type, s_alpha, s_emit, s_iter, id_fire, s_mov);
+    const size_t n = (size_t)w.W * w.H;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        if (w.dirty[i]) paint(w, rt, i, s_type, s_alpha, s_emit, s_k, id_fire, s_mov);
     __syncthreads();
     for (int k = threadIdx.x; k < MAXMAT; k += blockDim.x)
         if (s_mov[k]) atomicAdd((unsigned long long *)&rt.moving[k], (unsigned long long)s_mov[k]);
@@ -163,7 +181,7 @@ int fse_world_render_dirty(fse_world *w, int64_t *moving) {
     if (rc) return rc;
     const size_t n = (size_t)w->W * w->H;
     FSE_CUDA_TRY(cudaMemsetAsync(w->moving, 0, MAXMAT * sizeof(long long), w->stream));
-    const int blocks = (int)std::max<size_t>(1, std::min<size_t>((n / 4 + 255) / 256, (size_t)sm_count() * 8));
+    const int blocks = (int)std::max<size_t>(1, std::min<size_t>((n + 255) / 256, (size_t)sm_count() * 16));
     k_render_dirty<<<blocks, 256, 0, w->stream>>>(w->d, g_dev_mt, render_tex(w));
     FSE_CUDA_TRY(cudaGetLastError());
     count_launches(1);

@@ -1583,8 +1583,8 @@ static inline uint32_t rgba(uint32_t r, uint32_t g, uint32_t b, uint32_t a) {
 /* flow texture channel, game.cpp:2048-2053 (double arithmetic, truncation to u8) */
 static inline uint32_t flow_byte(float f, int iterations) {
     double a = (double)f * (3.0 / iterations + 0.5) / 4.0 + 0.5;
-    double c = a < 0.0 ? 0.0 : a;
-    c = c > 1.0 ? 1.0 : c;
+    if (!(a > 0.0)) return 0u; /* also a NaN (zero iterations), which the reference leaves undefined */
+    double c = a > 1.0 ? 1.0 : a;
     return (uint32_t)(c * 255);
 }
 
