@@ -174,6 +174,54 @@ void builtin_materials() {
     g_dirty = true;
 }
 
+// The flow texel byte of game.cpp:2048-2053 for a float flow f and k = 3.0 /
+// iterations + 0.5, in double; volatile temporaries keep each operation separately
+// rounded (no contraction into a fused multiply-add).
+static uint32_t flow_byte_host(float f, double k) {
+    volatile double p = (double)f * k;
+    volatile double q = p * 0.25;
+    volatile double a = q + 0.5;
+    if (!(a > 0.0)) return 0u;
+    if (a >= 1.0) return 255u;
+    volatile double b = a * 255.0;
+    return (uint32_t)b;
+}
+// float <-> unsigned key with the same order (non-NaN values)
+static uint32_t float_key(float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+static float key_float(uint32_t k) {
+    uint32_t u = (k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k;
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+}
+// thr[j] = the smallest float with flow_byte_host >= j, j = 1..255 (thr[0] = -inf);
+// the byte is non-decreasing in f when k > 0
+static bool flow_thresholds(double k, float thr[256]) {
+    if (!(k > 0.0) || !std::isfinite(k)) return false;
+    const uint32_t lo0 = float_key(-INFINITY), hi0 = float_key(INFINITY);
+    thr[0] = -INFINITY;
+    for (int j = 1; j < 256; j++) {
+        uint32_t lo = lo0, hi = hi0;  // invariant: byte(hi) >= j
+        if (flow_byte_host(key_float(hi), k) < (uint32_t)j) {
+            thr[j] = INFINITY;  // not reached by any finite float
+            continue;
+        }
+        while (lo < hi) {
+            const uint32_t mid = lo + (hi - lo) / 2;
+            if (flow_byte_host(key_float(mid), k) >= (uint32_t)j)
+                hi = mid;
+            else
+                lo = mid + 1;
+        }
+        thr[j] = key_float(lo);
+    }
+    return true;
+}
+
 void build_table(MatTable &t) {
     memset(&t, 0, sizeof(t));
     t.n = (int)g_mats.size();
@@ -204,6 +252,7 @@ void build_table(MatTable &t) {
         t.alpha[i] = (uint32_t)(uint8_t)m.alpha;
         t.emit_col[i] = m.emit_colour;
         t.flow_k[i] = 3.0 / m.iterations + 0.5;  // IEEE double, as the reference evaluates it
+        t.flow_thr_ok[i] = (m.type == T_SOUP && flow_thresholds(t.flow_k[i], t.flow_thr[i])) ? 1 : 0;
     }
     t.n_inter = (int)g_inter.size();
     for (size_t i = 0; i < g_inter.size(); i++)

@@ -82,6 +82,13 @@ struct MatTable {
     uint32_t alpha[MAXMAT];
     uint32_t emit_col[MAXMAT];
     double flow_k[MAXMAT];
+    // The flow texel byte is a non-decreasing step function of the float flow for
+    // k > 0: flow_thr[m][j] is the smallest float whose byte is >= j (j = 1..255),
+    // found on the host by bisection with the double arithmetic above, so the
+    // byte of f is the largest j with flow_thr[m][j] <= f. flow_thr_ok[m] = 0:
+    // no table (k <= 0 or not finite), evaluate in double.
+    float flow_thr[MAXMAT][256];
+    uint8_t flow_thr_ok[MAXMAT];
 };
 
 __host__ __device__ __forceinline__ int mt_type(uint32_t a) { return (int)(a & 0xFF); }

@@ -36,6 +36,17 @@ __device__ __forceinline__ uint32_t flow_byte(float f, double k) {
     return a >= 1.0 ? 255u : (uint32_t)__dmul_rn(a, 255.0);
 }
 
+// the same byte from the material's thresholds (the largest j with thr[j] <= f):
+// a float estimate, then exact steps along the table; float compares only
+__device__ __forceinline__ uint32_t flow_byte_thr(float f, const float *__restrict__ thr, float kf) {
+    if (!(f == f)) return 0u;  // NaN: 0, as in the double evaluation
+    const float est = __fmul_rn(__fadd_rn(__fmul_rn(__fmul_rn(f, kf), 0.25f), 0.5f), 255.0f);
+    int j = est >= 255.0f ? 255 : (est > 0.0f ? (int)est : 0);
+    while (j < 255 && f >= thr[j + 1]) j++;
+    while (j > 0 && f < thr[j]) j--;
+    return (uint32_t)j;
+}
+
 // prev + (cur - prev) * 0.25 with the product and the sum in double, rounded to
 // float (game.cpp:2041-2042). For normal operands this equals the float
 // evaluation: * 0.25 is exact, and the double sum of two floats is exact unless
@@ -57,9 +68,9 @@ __device__ __forceinline__ float half_of(float v) {
 }
 
 // one dirty cell of game.cpp:1997-2063
-__device__ __forceinline__ void paint(const WorldDev &w, const RenderTex &rt, size_t i, const uint8_t *s_type,
-                                      const uint32_t *s_alpha, const uint32_t *s_emit, const double *s_k, int id_fire,
-                                      unsigned *s_mov) {
+__device__ __forceinline__ void paint(const WorldDev &w, const MatTable *__restrict__ mt, const RenderTex &rt,
+                                      size_t i, const uint8_t *s_type, const uint32_t *s_alpha, const uint32_t *s_emit,
+                                      const double *s_k, int id_fire, unsigned *s_mov) {
     w.dirty[i] = 0;
     const int id = w.id[i];
     {
@@ -89,7 +100,16 @@ __device__ __forceinline__ void paint(const WorldDev &w, const RenderTex &rt, si
         const float nfx = smooth(pf[0], fx);
         float nfy = smooth(pf[1], fy);
         if (nfy < 0.0f) nfy = half_of(nfy);
-        rt.tex[3][i] = rgba(flow_byte(nfx, s_k[id]), flow_byte(nfy, s_k[id]), 0u, 0xffu);
+        uint32_t bx, by;
+        if (mt->flow_thr_ok[id]) {
+            const float kf = (float)s_k[id];
+            bx = flow_byte_thr(nfx, mt->flow_thr[id], kf);
+            by = flow_byte_thr(nfy, mt->flow_thr[id], kf);
+        } else {
+            bx = flow_byte(nfx, s_k[id]);
+            by = flow_byte(nfy, s_k[id]);
+        }
+        rt.tex[3][i] = rgba(bx, by, 0u, 0xffu);
         pf[0] = nfx;
         pf[1] = nfy;
     }
@@ -117,7 +137,7 @@ __global__ void k_render_dirty(const WorldDev *__restrict__ wd, const MatTable *
     const int id_fire = mt->id_fire;
     const size_t n = (size_t)w.W * w.H;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        if (w.dirty[i]) paint(w, rt, i, s_type, s_alpha, s_emit, s_k, id_fire, s_mov);
+        if (w.dirty[i]) paint(w, mt, rt, i, s_type, s_alpha, s_emit, s_k, id_fire, s_mov);
     __syncthreads();
     for (int k = threadIdx.x; k < MAXMAT; k += blockDim.x)
         if (s_mov[k]) atomicAdd((unsigned long long *)&rt.moving[k], (unsigned long long)s_mov[k]);
