@@ -303,6 +303,29 @@ class World:
         check(self.lib.fse_world_render_read(self.h, int(which), ptr(out)), "render_read")
         return out
 
+    # -- solid islands
+    def physicsCheck(self, x, y, pixels=True):
+        """world::physicsCheck (world.cpp:3330-3445): (cells cut, bbox, colour image or None)."""
+        n = C.c_int(0)
+        bbox = np.zeros(4, np.int32)
+        pix = np.zeros(1000 * 1000, np.uint32) if pixels else None
+        check(self.lib.fse_world_physics_check(self.h, int(x), int(y), C.byref(n), ptr(bbox),
+                                               ptr(pix) if pixels else None, pix.size if pixels else 0),
+              "physics_check")
+        if n.value == 0:
+            return 0, None, None
+        bw, bh = int(bbox[2] - bbox[0] + 1), int(bbox[3] - bbox[1] + 1)
+        img = pix[: bw * bh].reshape(bh, bw).copy() if (pixels and n.value > 10) else None
+        return n.value, bbox, img
+
+    def islands(self, max_cells=1000, remove=False, cap=1 << 16):
+        """Every 4-connected SOLID region of at most max_cells cells: (table, count)."""
+        out = np.zeros(max(cap, 1), _abi.ISLAND_DTYPE)
+        n = C.c_int(0)
+        check(self.lib.fse_world_islands(self.h, int(max_cells), 1 if remove else 0, ptr(out), int(cap),
+                                         C.byref(n)), "islands")
+        return out[: min(cap, n.value)], n.value
+
 
 class Batch:
     """Many worlds ticked by one launch per colour pass (configs with uneven sizes)."""

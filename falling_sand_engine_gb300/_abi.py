@@ -22,6 +22,9 @@ BODY_DTYPE = np.dtype(
         ("n_sand", "<i4"), ("n_soup", "<i4"), ("n_placed", "<i4"), ("n_recovered", "<i4"),
     ]
 )
+# fse_island
+ISLAND_DTYPE = np.dtype([("root", "<i4"), ("cells", "<i4"), ("min_x", "<i4"), ("min_y", "<i4"), ("max_x", "<i4"),
+                         ("max_y", "<i4")])
 
 
 class FseConfig(C.Structure):
@@ -81,6 +84,8 @@ SIGNATURES = {
     "fse_world_render_cells": (_i, [_vp]),
     "fse_world_render_read": (_i, [_vp, _i, _vp]),
     "fse_world_render_texture": (_vp, [_vp, _i]),
+    "fse_world_physics_check": (_i, [_vp, _i, _i, _vp, _vp, _vp, C.c_int64]),
+    "fse_world_islands": (_i, [_vp, _i, _i, _vp, _i, _vp]),
     "fse_tick_noalloc": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _u32, _u32, _vp, _i, C.POINTER(_i), _vp]),
     "fse_batch_create": (_i, [_vp, _i, _pp]),
     "fse_batch_destroy": (_i, [_vp]),

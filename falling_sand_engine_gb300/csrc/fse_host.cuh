@@ -50,6 +50,14 @@ struct fse_world {
     float *pflow;
     int32_t *owner;
     long long *moving;
+    // solid-island scratch (allocated on first use): flood marks and their epoch,
+    // labels and sizes, the flood's cell list, region image, results, island table
+    uint32_t *isl_mark;
+    uint32_t isl_epoch;
+    int32_t *isl_lab, *isl_aux, *isl_list, *isl_out;
+    uint32_t *isl_pix;
+    fse_island *isl_tab;
+    int isl_tab_cap;
 };
 
 namespace fse {

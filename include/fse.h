@@ -219,6 +219,27 @@ int fse_world_render_read(fse_world *world, int which, uint8_t *out);
 /* the texture's device pointer (valid until the world is destroyed), NULL on error */
 void *fse_world_render_texture(fse_world *world, int which);
 
+/* ---------------------------------------------------------- solid islands */
+typedef struct fse_island {
+    int32_t root;  /* the region's smallest cell index (y * W + x) */
+    int32_t cells;
+    int32_t min_x, min_y, max_x, max_y;
+} fse_island;
+/* world::physicsCheck(x, y) (world.cpp:3330-3445): if (x, y) is SOLID and its
+ * 4-connected SOLID region has at most 1000 cells, the region is cut out of the grid
+ * (its cells become GENERIC_AIR, counted as destroyed in the ledger). *out_cells =
+ * cells cut (0: nothing), out_bbox = min x, min y, max x, max y; for more than 10
+ * cells and a non-NULL `pixels` of at least bbox-width * bbox-height entries, the
+ * region's colours as that image, 0 elsewhere (the surface the host makes the rigid
+ * body from). */
+int fse_world_physics_check(fse_world *world, int x, int y, int *out_cells, int32_t out_bbox[4], uint32_t *pixels,
+                            int64_t pixels_cap);
+/* every 4-connected SOLID region at once (connected-component labelling on the
+ * device): the regions of at most max_cells cells, by increasing root; the first
+ * `cap` are written to `out`, *out_n = how many there are; with `remove` they are
+ * all cut out of the grid as physicsCheck does. */
+int fse_world_islands(fse_world *world, int max_cells, int remove, fse_island *out, int cap, int *out_n);
+
 /* ------------------------------------------------- allocation-free tick */
 /* One world::tick() (no particle step) on cell planes the caller owns in device
  * memory, for hosts that cannot let a library allocate device memory: engines

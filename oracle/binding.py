@@ -30,6 +30,9 @@ BODY_DTYPE = np.dtype(
 )
 assert BODY_DTYPE.itemsize == 48
 
+ISLAND_DTYPE = np.dtype([("root", "<i4"), ("cells", "<i4"), ("min_x", "<i4"), ("min_y", "<i4"), ("max_x", "<i4"),
+                         ("max_y", "<i4")])
+
 ORDER_SEQ = 0
 ORDER_PART = 1
 
@@ -95,6 +98,8 @@ class Oracle:
                 "om_render_cells": (None, [vp]),
                 "om_render_get": (None, [vp, i32, vp]),
                 "om_render_dirty_get": (None, [vp, vp]),
+                "om_physics_check": (i32, [vp, i32, i32, vp, vp, i32]),
+                "om_islands": (i32, [vp, i32, i32, vp, i32]),
             }
             for name, (res, args) in sig.items():
                 f = getattr(lib, name)
@@ -266,3 +271,19 @@ class OracleWorld:
         out = np.zeros((self.h, self.w), np.uint8)
         self.lib.om_render_dirty_get(self.h_, _ptr(out))
         return out
+
+    # -- solid islands
+    def physics_check(self, x, y, pixels_cap=1 << 20):
+        bbox = np.zeros(4, np.int32)
+        pix = np.zeros(pixels_cap, np.uint32)
+        n = self.lib.om_physics_check(self.h_, x, y, _ptr(bbox), _ptr(pix), pixels_cap)
+        if n == 0:
+            return 0, None, None
+        bw, bh = bbox[2] - bbox[0] + 1, bbox[3] - bbox[1] + 1
+        img = pix[: bw * bh].reshape(bh, bw).copy() if n > 10 else None
+        return n, bbox, img
+
+    def islands(self, max_cells=1000, remove=False, cap=1 << 16):
+        out = np.zeros(cap, ISLAND_DTYPE)
+        n = self.lib.om_islands(self.h_, max_cells, 1 if remove else 0, _ptr(out), cap)
+        return out[: min(n, cap)], n

@@ -1873,6 +1873,127 @@ void om_object_mask(const om_world *w, uint8_t *bits) {
         if (M[w->id[i]].type == T_OBJECT) bits[i >> 3] |= (uint8_t)(1u << (i & 7));
 }
 
+/* ------------------------------------------------------------ solid islands */
+static inline int is_solid(const om_world *w, size_t i) { return M[w->id[i]].type == T_SOLID; }
+
+/* cut one cell out of the grid (Tiles_NOTHING, dirty), counted as destroyed */
+static void cut_cell(om_world *w, size_t i) {
+    w->led[LED_DN][w->id[i]] += 1;
+    w->id[i] = (uint16_t)ID_AIR;
+    w->col[i] = 0;
+    w->sc[i] = 0;
+    w->fl[i] = 0;
+    w->df[i] = 0;
+    mark_dirty(w, i);
+}
+
+/* world::physicsCheck(x, y), world.cpp:3330-3424, with the recursive 4-way flood
+ * of :3427-3445 as an explicit stack in the same visiting order (+x, +y, -x, -y).
+ * The flood stops counting past 1000 cells, and only a region of at most 1000
+ * cells is cut out, so the result is the whole region or nothing. Returns the
+ * number of cells cut; bbox = min x, min y, max x, max y; for more than 10 cells
+ * `pixels` (if not NULL and big enough) gets the region's colours as a bbox-sized
+ * image, 0 elsewhere (the rigid body's surface, :3357-3365). */
+int om_physics_check(om_world *w, int x, int y, int32_t bbox[4], uint32_t *pixels, int pixels_cap) {
+    if (x < 0 || y < 0 || x >= w->W || y >= w->H) return 0;
+    if (!is_solid(w, (size_t)y * w->W + x)) return 0;
+    size_t n = (size_t)w->W * w->H;
+    uint8_t *vis = (uint8_t *)calloc(n, 1);
+    int32_t *cells = (int32_t *)malloc(1001 * sizeof(int32_t));
+    int32_t *stack = (int32_t *)malloc(4 * 1100 * sizeof(int32_t));
+    int count = 0, sp = 0, minx = w->W, maxx = 0, miny = w->H, maxy = 0;
+    stack[sp++] = y * w->W + x;
+    while (sp > 0) {
+        int c = stack[--sp];
+        if (count > 1000) break; /* :3428 every further call returns */
+        int cx = c % w->W, cy = c / w->W;
+        if (vis[c] || !is_solid(w, (size_t)c)) continue;
+        vis[c] = 1;
+        if (count < 1001) cells[count] = c;
+        count++;
+        if (cx < minx) minx = cx;
+        if (cx > maxx) maxx = cx;
+        if (cy < miny) miny = cy;
+        if (cy > maxy) maxy = cy;
+        /* pushed in reverse so that +x is explored first */
+        if (cy > 0 && sp < 4 * 1100) stack[sp++] = c - w->W;
+        if (cx > 0 && sp < 4 * 1100) stack[sp++] = c - 1;
+        if (cy + 1 < w->H && sp < 4 * 1100) stack[sp++] = c + w->W;
+        if (cx + 1 < w->W && sp < 4 * 1100) stack[sp++] = c + 1;
+    }
+    int cut = 0;
+    if (count > 0 && count <= 1000) {
+        int bw = maxx - minx + 1, bh = maxy - miny + 1;
+        if (count > 10 && pixels && bw * bh <= pixels_cap) {
+            memset(pixels, 0, (size_t)bw * bh * 4);
+            for (int k = 0; k < count; k++) {
+                int c = cells[k];
+                pixels[(c / w->W - miny) * bw + (c % w->W - minx)] = w->col[c];
+            }
+        }
+        for (int k = 0; k < count; k++) cut_cell(w, (size_t)cells[k]);
+        cut = count;
+        bbox[0] = minx;
+        bbox[1] = miny;
+        bbox[2] = maxx;
+        bbox[3] = maxy;
+    }
+    free(vis);
+    free(cells);
+    free(stack);
+    return cut;
+}
+
+/* every 4-connected SOLID region: those of at most max_cells cells are listed in
+ * `out` by increasing root (the region's smallest cell index) and, with `remove`,
+ * cut out of the grid. Returns the number of such regions (entries beyond cap are
+ * not written). */
+int om_islands(om_world *w, int max_cells, int remove, om_island *out, int cap) {
+    size_t n = (size_t)w->W * w->H;
+    uint8_t *vis = (uint8_t *)calloc(n, 1);
+    int32_t *q = (int32_t *)malloc(n * sizeof(int32_t));
+    int found = 0;
+    for (size_t r = 0; r < n; r++) {
+        if (vis[r] || !is_solid(w, r)) continue;
+        size_t head = 0, tail = 0;
+        q[tail++] = (int32_t)r;
+        vis[r] = 1;
+        int minx = w->W, maxx = 0, miny = w->H, maxy = 0;
+        while (head < tail) {
+            int c = q[head++];
+            int cx = c % w->W, cy = c / w->W;
+            if (cx < minx) minx = cx;
+            if (cx > maxx) maxx = cx;
+            if (cy < miny) miny = cy;
+            if (cy > maxy) maxy = cy;
+            int nb[4] = {cx + 1 < w->W ? c + 1 : -1, cx > 0 ? c - 1 : -1, cy + 1 < w->H ? c + w->W : -1,
+                         cy > 0 ? c - w->W : -1};
+            for (int k = 0; k < 4; k++)
+                if (nb[k] >= 0 && !vis[nb[k]] && is_solid(w, (size_t)nb[k])) {
+                    vis[nb[k]] = 1;
+                    q[tail++] = nb[k];
+                }
+        }
+        if ((long)tail <= max_cells) {
+            if (found < cap) {
+                om_island *is = &out[found];
+                is->root = (int32_t)r;
+                is->cells = (int32_t)tail;
+                is->min_x = minx;
+                is->min_y = miny;
+                is->max_x = maxx;
+                is->max_y = maxy;
+            }
+            found++;
+            if (remove)
+                for (size_t k = 0; k < tail; k++) cut_cell(w, (size_t)q[k]);
+        }
+    }
+    free(vis);
+    free(q);
+    return found;
+}
+
 void om_set_threads(int n) {
 #ifdef _OPENMP
     if (n > 0) omp_set_num_threads(n);

@@ -135,6 +135,13 @@ void om_render_cells(om_world *w);
 void om_render_get(const om_world *w, int which, uint32_t *out);
 void om_render_dirty_get(const om_world *w, uint8_t *out);
 
+/* solid islands: world::physicsCheck (world.cpp:3330-3445) and every region at once */
+typedef struct om_island {
+    int32_t root, cells, min_x, min_y, max_x, max_y;
+} om_island;
+int om_physics_check(om_world *w, int x, int y, int32_t bbox[4], uint32_t *pixels, int pixels_cap);
+int om_islands(om_world *w, int max_cells, int remove, om_island *out, int cap);
+
 #ifdef __cplusplus
 }
 #endif
