@@ -239,8 +239,25 @@ def render_config1(fse, torch, W, H, seed, NP, ticks=20):
         ndirty += int(mv.sum())
     peak, peak_kind = peaks()
     gbs = nbytes / (d_ms / 1e3) / 1e9
+    # solid islands on the same world: physicsCheck from random seeds (the drop-in,
+    # one per tick in the reference) and the all-regions labelling pass (each call
+    # is synchronous: host clock around it)
+    rng = np.random.default_rng(seed)
+    t0 = time.perf_counter()
+    cut = 0
+    for _ in range(50):
+        cut += world.physicsCheck(int(rng.integers(0, W)), int(rng.integers(0, H)))[0] > 0
+    pc_ms = (time.perf_counter() - t0) * 1e3 / 50
+    world.islands(1000)
+    t0 = time.perf_counter()
+    for _ in range(5):
+        _, n_isl = world.islands(1000)
+    isl_ms = (time.perf_counter() - t0) * 1e3 / 5
     world.close()
-    return {"dirty_pass_ms": round(d_ms / ticks, 4), "dirty_pass_gcells": round(W * H * ticks / (d_ms / 1e3) / 1e9, 3),
+    islands = {"physics_check_ms": round(pc_ms, 3), "physics_check_cut": int(cut), "label_all_ms": round(isl_ms, 3),
+               "label_all_gcells": round(W * H / (isl_ms / 1e3) / 1e9, 3), "islands_le_1000": int(n_isl)}
+    return {"islands": islands,
+            "dirty_pass_ms": round(d_ms / ticks, 4), "dirty_pass_gcells": round(W * H * ticks / (d_ms / 1e3) / 1e9, 3),
             "dirty_cells_per_tick": ndirty // ticks, "dirty_pass_gbs": round(gbs, 1),
             "dirty_pass_frac": round(gbs / peak, 4), "peak": peak, "peak_kind": peak_kind,
             "particle_layer_ms": round(c_ms / ticks, 4), "ticks": ticks}

@@ -54,7 +54,7 @@ struct fse_world {
     // labels and sizes, the flood's cell list, region image, results, island table
     uint32_t *isl_mark;
     uint32_t isl_epoch;
-    int32_t *isl_lab, *isl_aux, *isl_list, *isl_out;
+    int32_t *isl_lab, *isl_aux, *isl_list, *isl_out, *isl_seg;
     uint32_t *isl_pix;
     fse_island *isl_tab;
     int isl_tab_cap;

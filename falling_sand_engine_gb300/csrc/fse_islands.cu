@@ -197,25 +197,101 @@ __global__ void k_ccl_size(const WorldDev *__restrict__ wd, int32_t *lab, int32_
     }
 }
 
-// the roots of regions of at most max_cells cells; with tab != NULL they get a
-// table entry and aux[r] becomes -(entry + 1)
-__global__ void k_ccl_pick(const WorldDev *__restrict__ wd, const int32_t *lab, int32_t *aux, int max_cells,
-                           int32_t *count, fse_island *tab, int cap) {
+// The regions to report are numbered in root order by a scan over contiguous
+// segments of the cell range (one segment per block), so the table comes out
+// sorted by root. Step 1: per segment, the roots of regions of at most max_cells.
+constexpr int SEG_BLOCKS = 1024;
+constexpr int SEG_THREADS = 256;
+
+__device__ __forceinline__ bool picked(const int32_t *lab, const int32_t *aux, int r, int max_cells) {
+    return lab[r] == r && aux[r] <= max_cells;
+}
+
+__device__ __forceinline__ int block_sum(int v, int *s_warp) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) s_warp[threadIdx.x >> 5] = v;
+    __syncthreads();
+    int t = 0;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) t += s_warp[k];
+    __syncthreads();
+    return t;  // valid in thread 0
+}
+
+__global__ void k_ccl_count(const WorldDev *__restrict__ wd, const int32_t *lab, const int32_t *aux, int max_cells,
+                            int32_t *seg_sum) {
+    __shared__ int s_warp[32];
     const WorldDev &w = *wd;
-    const int n = w.W * w.H;
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
-        if (lab[r] != r || aux[r] > max_cells) continue;
-        const int idx = atomicAdd(count, 1);
-        if (!tab || idx >= cap) continue;
-        fse_island t;
-        t.root = r;
-        t.cells = aux[r];
-        t.min_x = w.W;
-        t.min_y = w.H;
-        t.max_x = -1;
-        t.max_y = -1;
-        tab[idx] = t;
-        aux[r] = -(idx + 1);
+    const int n = w.W * w.H, seg = (n + gridDim.x - 1) / gridDim.x;
+    const int b0 = blockIdx.x * seg, b1 = min(n, b0 + seg);
+    int c = 0;
+    for (int r = b0 + threadIdx.x; r < b1; r += blockDim.x) c += picked(lab, aux, r, max_cells) ? 1 : 0;
+    const int t = block_sum(c, s_warp);
+    if (threadIdx.x == 0) seg_sum[blockIdx.x] = t;
+}
+
+// step 2: exclusive scan of the segment counts (one block of SEG_BLOCKS threads);
+// seg_sum[SEG_BLOCKS] = the total
+__global__ void k_ccl_scan(int32_t *seg_sum) {
+    __shared__ int s[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int v = seg_sum[threadIdx.x];
+    int inc = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += u;
+    }
+    if (lane == 31) s[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        int a = s[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, a, o);
+            if (lane >= o) a += u;
+        }
+        s[lane] = a;
+    }
+    __syncthreads();
+    const int excl = (wid > 0 ? s[wid - 1] : 0) + inc - v;
+    seg_sum[threadIdx.x] = excl;
+    if (threadIdx.x == SEG_BLOCKS - 1) seg_sum[SEG_BLOCKS] = excl + v;
+}
+
+// step 3: each segment numbers its roots in order; aux[r] becomes -(entry + 1)
+__global__ void k_ccl_pick(const WorldDev *__restrict__ wd, const int32_t *lab, int32_t *aux, int max_cells,
+                           const int32_t *seg_base, fse_island *tab) {
+    __shared__ int s_warp[SEG_THREADS / 32];
+    __shared__ int s_carry;
+    const WorldDev &w = *wd;
+    const int n = w.W * w.H, seg = (n + gridDim.x - 1) / gridDim.x;
+    const int b0 = blockIdx.x * seg, b1 = min(n, b0 + seg);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_carry = seg_base[blockIdx.x];
+    __syncthreads();
+    for (int base = b0; base < b1; base += blockDim.x) {
+        const int r = base + threadIdx.x;
+        const bool p = r < b1 && picked(lab, aux, r, max_cells);
+        const unsigned m = __ballot_sync(0xffffffffu, p);
+        if (lane == 0) s_warp[wid] = __popc(m);
+        __syncthreads();
+        int before = s_carry;
+        for (int k = 0; k < wid; k++) before += s_warp[k];
+        if (p) {
+            const int idx = before + __popc(m & ((1u << lane) - 1u));
+            fse_island t;
+            t.root = r;
+            t.cells = aux[r];
+            t.min_x = w.W;
+            t.min_y = w.H;
+            t.max_x = -1;
+            t.max_y = -1;
+            tab[idx] = t;
+            aux[r] = -(idx + 1);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (int k = 0; k < SEG_THREADS / 32; k++) s_carry += s_warp[k];
+        __syncthreads();
     }
 }
 
@@ -299,19 +375,20 @@ int fse_world_islands(fse_world *w, int max_cells, int remove, fse_island *out, 
     int rc = ensure_materials_pushed();
     if (rc) return rc;
     const size_t n = (size_t)w->W * w->H;
-    if (!grow(w, &w->isl_lab, n) || !grow(w, &w->isl_aux, n) || !grow(w, &w->isl_out, 8)) return FSE_E_NOMEM;
+    if (!grow(w, &w->isl_lab, n) || !grow(w, &w->isl_aux, n) || !grow(w, &w->isl_seg, SEG_BLOCKS + 1))
+        return FSE_E_NOMEM;
     const int blocks = (int)std::max<size_t>(1, std::min<size_t>((n + 255) / 256, (size_t)sm_count() * 16));
     cudaStream_t s = w->stream;
     k_ccl_init<<<blocks, 256, 0, s>>>(w->d, g_dev_mt, w->isl_lab);
     k_ccl_unite<<<blocks, 256, 0, s>>>(w->d, w->isl_lab);
     FSE_CUDA_TRY(cudaMemsetAsync(w->isl_aux, 0, n * 4, s));
     k_ccl_size<<<blocks, 256, 0, s>>>(w->d, w->isl_lab, w->isl_aux);
-    FSE_CUDA_TRY(cudaMemsetAsync(w->isl_out, 0, 4, s));
-    k_ccl_pick<<<blocks, 256, 0, s>>>(w->d, w->isl_lab, w->isl_aux, max_cells, w->isl_out, nullptr, 0);
+    k_ccl_count<<<SEG_BLOCKS, SEG_THREADS, 0, s>>>(w->d, w->isl_lab, w->isl_aux, max_cells, w->isl_seg);
+    k_ccl_scan<<<1, SEG_BLOCKS, 0, s>>>(w->isl_seg);
     int32_t found = 0;
-    FSE_CUDA_TRY(cudaMemcpyAsync(&found, w->isl_out, 4, cudaMemcpyDeviceToHost, s));
+    FSE_CUDA_TRY(cudaMemcpyAsync(&found, w->isl_seg + SEG_BLOCKS, 4, cudaMemcpyDeviceToHost, s));
     FSE_CUDA_TRY(cudaStreamSynchronize(s));
-    count_launches(4);
+    count_launches(5);
     if (found > w->isl_tab_cap) {
         if (w->isl_tab) cudaFree(w->isl_tab);
         w->isl_tab = nullptr;
@@ -320,24 +397,16 @@ int fse_world_islands(fse_world *w, int max_cells, int remove, fse_island *out, 
         w->isl_tab_cap = found;
     }
     if (found > 0) {
-        FSE_CUDA_TRY(cudaMemsetAsync(w->isl_out, 0, 4, s));
-        k_ccl_pick<<<blocks, 256, 0, s>>>(w->d, w->isl_lab, w->isl_aux, max_cells, w->isl_out, w->isl_tab, found);
+        k_ccl_pick<<<SEG_BLOCKS, SEG_THREADS, 0, s>>>(w->d, w->isl_lab, w->isl_aux, max_cells, w->isl_seg, w->isl_tab);
         k_ccl_bbox<<<blocks, 256, 0, s>>>(w->d, g_dev_mt, w->isl_lab, w->isl_aux, w->isl_tab, remove);
         FSE_CUDA_TRY(cudaGetLastError());
         count_launches(2);
     }
     if (out_n) *out_n = found;
-    if (cap > 0 && found > 0) {
-        // by increasing root: the table's order is the order the roots were picked in
-        std::vector<fse_island> tab((size_t)found);
-        FSE_CUDA_TRY(cudaMemcpyAsync(tab.data(), w->isl_tab, (size_t)found * sizeof(fse_island),
+    if (cap > 0 && found > 0)  // the table is in root order already
+        FSE_CUDA_TRY(cudaMemcpyAsync(out, w->isl_tab, (size_t)std::min(found, cap) * sizeof(fse_island),
                                      cudaMemcpyDeviceToHost, s));
-        FSE_CUDA_TRY(cudaStreamSynchronize(s));
-        std::sort(tab.begin(), tab.end(), [](const fse_island &a, const fse_island &b) { return a.root < b.root; });
-        std::copy(tab.begin(), tab.begin() + std::min(found, cap), out);
-    } else {
-        FSE_CUDA_TRY(cudaStreamSynchronize(s));
-    }
+    FSE_CUDA_TRY(cudaStreamSynchronize(s));
     int32_t err = 0;
     FSE_CUDA_TRY(cudaMemcpy(&err, w->h.err, 4, cudaMemcpyDeviceToHost));
     return status_from_err(err);
