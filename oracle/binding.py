@@ -10,16 +10,18 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libfse_oracle.so")
+REF_TEMPERATURE_PATH = os.path.join(HERE, "_ref", "libref_temperature.so")
+REFERENCE_WORLD_CPP = "/root/reference/source/engine/world.cpp"
 
 PARTICLE_DTYPE = np.dtype(
     [
         ("x", "<f4"), ("y", "<f4"), ("vx", "<f4"), ("vy", "<f4"), ("ax", "<f4"), ("ay", "<f4"),
         ("target_x", "<f4"), ("target_y", "<f4"), ("target_force", "<f4"),
         ("lifetime", "<i4"), ("fade_time", "<i4"), ("colour", "<u4"), ("scalar", "<i4"),
-        ("id", "<u2"), ("flags", "u1"), ("bits", "u1"),
+        ("id", "<u2"), ("flags", "u1"), ("bits", "u1"), ("temperature", "<i2"), ("reserved", "<u2"),
     ]
 )
-assert PARTICLE_DTYPE.itemsize == 56
+assert PARTICLE_DTYPE.itemsize == 60
 
 BODY_DTYPE = np.dtype(
     [
@@ -100,6 +102,12 @@ class Oracle:
                 "om_render_dirty_get": (None, [vp, vp]),
                 "om_physics_check": (i32, [vp, i32, i32, vp, vp, i32]),
                 "om_islands": (i32, [vp, i32, i32, vp, i32]),
+                "om_material_set_conduction": (i32, [i32, u32, C.c_float, C.c_float]),
+                "om_material_set_factory_temperature": (i32, [i32, C.c_int32]),
+                "om_tick_temperature": (None, [vp]),
+                "om_world_set_temperature": (None, [vp, i32]),
+                "om_temperature_get": (None, [vp, vp]),
+                "om_temperature_set": (None, [vp, vp]),
             }
             for name, (res, args) in sig.items():
                 f = getattr(lib, name)
@@ -135,6 +143,12 @@ class Oracle:
 
     def set_factory(self, mat, base, shift, lo, mod, scalar):
         return self.lib.om_material_set_factory(mat, base, shift, lo, mod, scalar)
+
+    def set_conduction(self, mat, add_temp, cond_self, cond_other):
+        return self.lib.om_material_set_conduction(mat, add_temp, cond_self, cond_other)
+
+    def set_factory_temperature(self, mat, temperature):
+        return self.lib.om_material_set_factory_temperature(mat, temperature)
 
     def set_threads(self, n):
         self.lib.om_set_threads(n)
@@ -250,6 +264,22 @@ class OracleWorld:
         self.lib.om_object_mask(self.h_, _ptr(out))
         return out
 
+    # -- temperature
+    def temperature(self):
+        out = np.zeros(self.w * self.h, np.int16)
+        self.lib.om_temperature_get(self.h_, _ptr(out))
+        return out.reshape(self.h, self.w)
+
+    def set_temperature(self, temps):
+        a = np.ascontiguousarray(temps, np.int16).reshape(self.w * self.h)
+        self.lib.om_temperature_set(self.h_, _ptr(a))
+
+    def tick_temperature(self):
+        self.lib.om_tick_temperature(self.h_)
+
+    def enable_temperature(self, on=True):
+        self.lib.om_world_set_temperature(self.h_, 1 if on else 0)
+
     # -- render textures
     def render_enable(self):
         self.lib.om_render_enable(self.h_)
@@ -287,3 +317,36 @@ class OracleWorld:
         out = np.zeros(cap, ISLAND_DTYPE)
         n = self.lib.om_islands(self.h_, max_cells, 1 if remove else 0, _ptr(out), cap)
         return out[: min(n, cap)], n
+
+
+def build_reference_temperature(force=False):
+    """Compile the reference's own world::tickTemperature (oracle/Makefile `ref`).
+
+    Needs the reference source tree; returns None when it is absent.
+    """
+    if not os.path.exists(REFERENCE_WORLD_CPP):
+        return None
+    if force or not os.path.exists(REF_TEMPERATURE_PATH) or os.path.getmtime(REF_TEMPERATURE_PATH) < max(
+        os.path.getmtime(os.path.join(HERE, f)) for f in ("ref_temperature.cpp", "Makefile")
+    ):
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    return REF_TEMPERATURE_PATH
+
+
+def reference_tick_temperature(lib_path, mat, temp, add_temp, cond_self, cond_other, zone):
+    """One world::tickTemperature of the compiled reference over (mat, temp) arrays."""
+    lib = C.CDLL(lib_path)
+    f = lib.ref_tick_temperature
+    f.restype = C.c_int
+    f.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                  C.c_int, C.c_int, C.c_int, C.c_int]
+    h, w = mat.shape
+    m = np.ascontiguousarray(mat, np.uint16)
+    t = np.ascontiguousarray(temp, np.int16).copy()
+    a = np.ascontiguousarray(add_temp, np.uint32)
+    cs = np.ascontiguousarray(cond_self, np.float32)
+    co = np.ascontiguousarray(cond_other, np.float32)
+    rc = f(w, h, _ptr(m), _ptr(t), len(a), _ptr(a), _ptr(cs), _ptr(co), *zone)
+    if rc != 0:
+        raise ValueError("ref_tick_temperature failed")
+    return t

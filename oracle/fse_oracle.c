@@ -84,6 +84,12 @@ typedef struct {
     uint32_t f_base;
     int f_shift, f_lo, f_mod;
     int32_t f_scalar;
+    /* temperature of a new SOUP tile (the scalar holds its amount); the
+     * MaterialInstance temperature of TilesCreate, game_datastruct.cpp:427-437 */
+    int32_t f_temp;
+    /* Material::addTemp, conductionSelf, conductionOther (game_datastruct.hpp:142-144) */
+    uint32_t add_temp;
+    float cond_self, cond_other;
     int n_react;
     inter_t react[4];
     int interact;
@@ -124,6 +130,8 @@ static int reg(const char *index_name, int type, int slip, int alpha, float dens
     m->emit_colour = emit_colour;
     m->f_base = colour;
     m->f_scalar = (type == T_SOUP) ? Q_DEFAULT : 0;
+    m->cond_self = 1.0f;
+    m->cond_other = 1.0f;
     strncpy(m->index_name, index_name, sizeof(m->index_name) - 1);
     return NMAT++;
 }
@@ -153,6 +161,28 @@ int om_material_set_factory(int mat, uint32_t base, int shift, int lo, int mod, 
     M[mat].f_lo = lo;
     M[mat].f_mod = mod;
     M[mat].f_scalar = scalar;
+    return 0;
+}
+
+int om_material_set_conduction(int mat, uint32_t add_temp, float cond_self, float cond_other) {
+    if (mat < 0 || mat >= NMAT) return -1;
+    M[mat].add_temp = add_temp;
+    M[mat].cond_self = cond_self;
+    M[mat].cond_other = cond_other;
+    return 0;
+}
+
+/* addTemp, conductionSelf and conductionOther (as bits) of a material */
+void om_material_conduction(int mat, uint32_t out[3]) {
+    if (mat < 0 || mat >= NMAT) return;
+    out[0] = M[mat].add_temp;
+    memcpy(&out[1], &M[mat].cond_self, 4);
+    memcpy(&out[2], &M[mat].cond_other, 4);
+}
+
+int om_material_set_factory_temperature(int mat, int32_t temperature) {
+    if (mat < 0 || mat >= NMAT) return -1;
+    M[mat].f_temp = temperature;
     return 0;
 }
 
@@ -227,6 +257,16 @@ void om_materials_reset_builtin(void) {
     om_material_set_factory(om_material_find("FLAT_COBBLE_DIRT"), 0x624530u, 0, 0, 0, 0);
     om_material_set_factory(ID_AIR, 0x000000u, 0, 0, 0, 0);   /* Tiles_NOTHING, :311 */
     om_material_set_factory(ID_SOLID, 0xff0000u, 0, 0, 0, 0); /* Tiles_TEST_SOLID, :312 */
+    om_material_set_factory_temperature(ID_WATER, -1023); /* :427-431 */
+    om_material_set_factory_temperature(ID_LAVA, 1024);   /* :433-437 */
+
+    /* conduction, game_datastruct.cpp:124-141 (double literals rounded to float) */
+    om_material_set_conduction(ID_AIR, 0, (float)0.8, (float)0.8);
+    om_material_set_conduction(ID_LAVA, 2, (float)0.5, (float)0.7);
+    om_material_set_conduction(om_material_find("COBBLE_STONE"), 0, (float)0.01, (float)0.4);
+    om_material_set_conduction(om_material_find("COBBLE_DIRT"), 0, 1.0f, 1.0f);
+    om_material_set_conduction(om_material_find("GOLD_ORE"), 0, 1.0f, 1.0f);
+    om_material_set_conduction(om_material_find("GOLD_MOLTEN"), 0, 1.0f, 1.0f);
 
     /* reactions, game_datastruct.cpp:246-260 */
     om_material_set_reaction(ID_LAVA, REACT_BELOW, 512, ID_OBSIDIAN);
@@ -321,6 +361,7 @@ typedef struct {
     int32_t sc;
     uint32_t col;
     int32_t df;
+    int16_t tp; /* temperature of a SOUP tile (its scalar holds the amount); 0 otherwise */
 } cell_t;
 
 typedef struct {
@@ -346,11 +387,13 @@ static void pv_push(pvec *v, const om_particle *p) {
 struct om_world {
     int W, H, C, cell_iter;
     uint32_t seed, tick;
+    int temp_on; /* om_world_step runs om_tick_temperature every 4th tick */
     uint16_t *id;
     uint32_t *col;
     int32_t *sc;
     uint8_t *fl;
     int32_t *df;
+    int16_t *tp; /* SOUP cells: MaterialInstance::temperature (other cells keep it in sc) */
     uint8_t *vis;
     pvec parts;
     int64_t led[6][MAXMAT];
@@ -393,6 +436,7 @@ om_world *om_world_new(int w, int h, int chunk, int cell_iter, uint32_t seed) {
     wd->sc = (int32_t *)calloc(n, 4);
     wd->fl = (uint8_t *)calloc(n, 1);
     wd->df = (int32_t *)calloc(n, 4);
+    wd->tp = (int16_t *)calloc(n, 2);
     wd->vis = (uint8_t *)calloc(n, 1);
     for (size_t i = 0; i < n; i++) wd->id[i] = (uint16_t)ID_AIR;
     return wd;
@@ -405,6 +449,7 @@ void om_world_free(om_world *wd) {
     free(wd->sc);
     free(wd->fl);
     free(wd->df);
+    free(wd->tp);
     free(wd->vis);
     free(wd->parts.p);
     free(wd->wst);
@@ -487,6 +532,7 @@ static inline cell_t gcell(om_world *w, int x, int y) {
         c.sc = 0;
         c.col = 0xff0000u;
         c.df = 0;
+        c.tp = 0;
         return c;
     }
     size_t i = (size_t)y * w->W + x;
@@ -495,6 +541,7 @@ static inline cell_t gcell(om_world *w, int x, int y) {
     c.sc = w->sc[i];
     c.col = w->col[i];
     c.df = (M[c.id].type == T_SOUP) ? w->df[i] : 0;
+    c.tp = (M[c.id].type == T_SOUP) ? w->tp[i] : 0;
     return c;
 }
 static inline void pcell(om_world *w, int x, int y, cell_t c) {
@@ -506,6 +553,7 @@ static inline void pcell(om_world *w, int x, int y, cell_t c) {
     w->sc[i] = c.sc;
     w->col[i] = c.col;
     w->df[i] = (M[c.id].type == T_SOUP) ? c.df : 0;
+    if (M[c.id].type == T_SOUP) w->tp[i] = c.tp;
     mark_dirty(w, i);
 }
 static inline void set_moved(om_world *w, int x, int y, int on) {
@@ -533,7 +581,7 @@ static inline void setvis(om_world *w, int x, int y) {
 }
 
 static inline cell_t nothing(void) {
-    cell_t c = {(uint16_t)ID_AIR, 0, 0, 0u, 0};
+    cell_t c = {(uint16_t)ID_AIR, 0, 0, 0u, 0, 0};
     return c;
 }
 
@@ -586,6 +634,7 @@ static cell_t create_tile(rctx *c, int mid) {
     t.fl = 0;
     t.df = 0;
     t.sc = m->f_scalar;
+    t.tp = (m->type == T_SOUP) ? (int16_t)m->f_temp : 0;
     t.col = m->f_base;
     if (m->f_mod > 0) t.col = m->f_base + ((uint32_t)(m->f_lo + (int)(D(c) % (uint32_t)m->f_mod)) << m->f_shift);
     return t;
@@ -606,6 +655,7 @@ static void spawn(rctx *c, cell_t tile, int x, int y, float vx, float vy, float 
     p.fade_time = fade;
     p.colour = tile.col;
     p.scalar = tile.sc;
+    p.temperature = (M[tile.id].type == T_SOUP) ? tile.tp : 0;
     p.id = tile.id;
     p.flags = tile.fl;
     p.bits = (uint8_t)(temporary ? 2 : 0);
@@ -711,7 +761,12 @@ static void rule_a(rctx *c, int x, int y) {
                 int hit = (r->kind == REACT_BELOW) ? (t.sc < r->data1) : (t.sc > r->data1);
                 if (hit) {
                     cell_t nt = create_tile(c, r->data2);
-                    if (M[nt.id].type != T_SOUP) nt.sc = t.sc; /* keeps the temperature */
+                    /* keeps the temperature (:1188,1196): in the scalar, or beside the
+                     * amount of a SOUP result */
+                    if (M[nt.id].type != T_SOUP)
+                        nt.sc = t.sc;
+                    else
+                        nt.tp = (int16_t)t.sc;
                     led_replace(c, gcell(w, x, y), nt);
                     pcell(w, x, y, nt);
                     setvis(w, x, y);
@@ -788,7 +843,7 @@ static void rule_a(rctx *c, int x, int y) {
                 rem -= flow;
                 t.df -= flow;
                 if (bT == T_AIR) {
-                    cell_t nt = {t.id, 0, 0, t.col, flow};
+                    cell_t nt = {t.id, 0, 0, t.col, flow, t.tp};
                     pcell(w, x, y + 1, nt);
                     led_add(c, LED_CN, t.id, 1);
                 } else
@@ -821,7 +876,7 @@ static void rule_a(rctx *c, int x, int y) {
                 rem -= flow;
                 t.df -= flow;
                 if (lT == T_AIR) {
-                    cell_t nt = {t.id, 0, 0, t.col, flow};
+                    cell_t nt = {t.id, 0, 0, t.col, flow, t.tp};
                     pcell(w, x - 1, y, nt);
                     led_add(c, LED_CN, t.id, 1);
                 } else
@@ -842,7 +897,7 @@ static void rule_a(rctx *c, int x, int y) {
                 rem -= flow;
                 t.df -= flow;
                 if (rT == T_AIR) {
-                    cell_t nt = {t.id, 0, 0, t.col, flow};
+                    cell_t nt = {t.id, 0, 0, t.col, flow, t.tp};
                     pcell(w, x + 1, y, nt);
                     led_add(c, LED_CN, t.id, 1);
                 } else
@@ -865,7 +920,7 @@ static void rule_a(rctx *c, int x, int y) {
                 rem -= flow;
                 t.df -= flow;
                 if (tT == T_AIR) {
-                    cell_t nt = {t.id, 0, 0, t.col, flow};
+                    cell_t nt = {t.id, 0, 0, t.col, flow, t.tp};
                     pcell(w, x, y - 1, nt);
                     led_add(c, LED_CN, t.id, 1);
                 } else
@@ -1404,6 +1459,7 @@ int om_particles_tick(om_world *w) {
                 w->id[ci] = p->id;
                 w->col[ci] = p->colour;
                 w->sc[ci] = p->scalar;
+                if (M[p->id].type == T_SOUP) w->tp[ci] = p->temperature;
                 mark_dirty(w, ci);
                 w->fl[ci] = p->flags;
                 w->df[ci] = 0;
@@ -1437,12 +1493,19 @@ int om_particles_tick(om_world *w) {
     return m;
 }
 
+void om_tick_temperature(om_world *w);
+/* game::tick's order (game.cpp:1839,1878-1889,2157-2159): world::tick(),
+ * world::tickCells(), then world::tickTemperature() when enabled and the tick
+ * index is 2 modulo GameTick (4, core/const.h:38) */
 void om_world_step(om_world *wd, int order, int n) {
     for (int i = 0; i < n; i++) {
+        uint32_t t = wd->tick;
         om_world_tick(wd, order, 0);
         om_particles_tick(wd);
+        if (wd->temp_on && (t & 3u) == 2u) om_tick_temperature(wd);
     }
 }
+void om_world_set_temperature(om_world *wd, int on) { wd->temp_on = on ? 1 : 0; }
 
 int om_particles_count(const om_world *wd) { return wd->parts.n; }
 void om_particles_get(const om_world *wd, om_particle *out) {
@@ -1554,11 +1617,84 @@ void om_world_generate(om_world *w, int kind, uint32_t seed) {
             w->fl[i] = 0;
             w->df[i] = 0;
             w->sc[i] = m->f_scalar;
+            w->tp[i] = (m->type == T_SOUP) ? (int16_t)m->f_temp : 0;
             w->col[i] = m->f_base;
             if (m->f_mod > 0)
                 w->col[i] = m->f_base + ((uint32_t)(m->f_lo + (int)(draw_k(ck, 1) % (uint32_t)m->f_mod)) << m->f_shift);
         }
     if (w->dirty) memset(w->dirty, 1, (size_t)w->W * w->H);
+}
+
+/* ------------------------------------------------------------- temperature */
+/* The temperature of every cell as the reference keeps it in
+ * MaterialInstance::temperature (i16, game_datastruct.hpp:109,213): SOUP cells
+ * hold it beside their amount, every other cell in its scalar. */
+static inline int16_t temp_at(const om_world *w, size_t i) {
+    return M[w->id[i]].type == T_SOUP ? w->tp[i] : (int16_t)w->sc[i];
+}
+static inline void temp_put(om_world *w, size_t i, int16_t t) {
+    if (M[w->id[i]].type == T_SOUP)
+        w->tp[i] = t;
+    else
+        w->sc[i] = t;
+}
+void om_temperature_get(const om_world *w, int16_t *out) {
+    size_t n = (size_t)w->W * w->H;
+    for (size_t i = 0; i < n; i++) out[i] = temp_at(w, i);
+}
+void om_temperature_set(om_world *w, const int16_t *in) {
+    size_t n = (size_t)w->W * w->H;
+    for (size_t i = 0; i < n; i++) temp_put(w, i, in[i]);
+}
+
+/* float -> int32 the way x86-64's cvttss2si converts it (truncation toward zero;
+ * NaN and values outside the int32 range give INT32_MIN): the conversion of
+ * `newTemps[...] = <f32 expression>` (world.cpp:1989) on the reference's
+ * targets. Written out because a plain C cast of an out-of-range float is
+ * undefined and saturates on other CPUs. */
+static inline int32_t f2i_x86(float r) {
+    if (r >= -2147483648.0f && r < 2147483648.0f) return (int32_t)r;
+    return INT32_MIN;
+}
+
+/* world::tickTemperature, world.cpp:1950-2004: a Jacobi step of the 3x3
+ * conduction stencil over all cells (the reference's tickZone is the world
+ * minus a 128-cell margin, so its stencil never leaves the world; here every
+ * cell is updated and a neighbour outside the world reads Tiles_TEST_SOLID,
+ * whose temperature 0 skips it, world.cpp:1970). Terms are taken in the order
+ * of the FN(...) list, column by column, each operation rounded in float. */
+void om_tick_temperature(om_world *w) {
+    const int W = w->W, H = w->H;
+    size_t n = (size_t)W * H;
+    int16_t *old = (int16_t *)malloc(n * 2);
+    for (size_t i = 0; i < n; i++) old[i] = temp_at(w, i);
+    for (int y = 0; y < H; y++)
+        for (int x = 0; x < W; x++) {
+            float nn = (float)0.01; /* f32 n = 0.01; */
+            float v = 0.0f;
+            for (int xa = -1; xa <= 1; xa++)
+                for (int ya = -1; ya <= 1; ya++) {
+                    int xx = x + xa, yy = y + ya;
+                    if (xx < 0 || yy < 0 || xx >= W || yy >= H) continue;
+                    size_t j = (size_t)yy * W + xx;
+                    int t = old[j];
+                    if (t == 0) continue;
+                    /* abs(temperature) / 64 is integer division, then * conductionOther */
+                    float factor = (float)(abs(t) / 64) * M[w->id[j]].cond_other;
+                    v += (float)t * factor;
+                    nn += factor;
+                }
+            size_t i = (size_t)y * W + x;
+            const mat_t *m = &M[w->id[i]];
+            int t0 = old[i];
+            int32_t r;
+            if (v != 0.0f)
+                r = f2i_x86((float)m->add_temp + v / nn * m->cond_self + (float)t0 * (1.0f - m->cond_self));
+            else
+                r = (int32_t)(m->add_temp + (uint32_t)t0); /* u32 + int, stored into i32 */
+            temp_put(w, i, (int16_t)(uint16_t)(uint32_t)r);
+        }
+    free(old);
 }
 
 /* --------------------------------------------------------------- rendering */
@@ -1760,6 +1896,7 @@ void om_object_stamp(om_world *w, om_body *bodies, int n) {
                 p.id = w->id[ci];
                 p.colour = w->col[ci];
                 p.scalar = w->sc[ci];
+                if (ty == T_SOUP) p.temperature = w->tp[ci];
                 p.flags = w->fl[ci];
                 pv_push(&w->parts, &p);
                 if (ty == T_SOUP) {

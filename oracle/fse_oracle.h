@@ -39,7 +39,7 @@ extern "C" {
 #define OM_ORDER_SEQ 0
 #define OM_ORDER_PART 1
 
-/* Same byte layout as fse_particle in include/fse.h (56 bytes). */
+/* Same byte layout as fse_particle in include/fse.h (60 bytes). */
 typedef struct om_particle {
     float x, y, vx, vy, ax, ay;
     float target_x, target_y, target_force;
@@ -49,6 +49,8 @@ typedef struct om_particle {
     uint16_t id;
     uint8_t flags;
     uint8_t bits; /* bit0 phase, bit1 temporary, bits2-3 inObjectState */
+    int16_t temperature; /* temperature of a SOUP tile (its scalar holds the amount) */
+    uint16_t reserved;
 } om_particle;
 
 typedef struct om_world om_world;
@@ -59,6 +61,12 @@ int om_material_register(int s_id, const char *name, const char *index_name, int
                          int alpha, float density, int iterations, int emit, uint32_t emit_colour, uint32_t colour);
 int om_material_set_factory(int mat, uint32_t base, int shift, int lo, int mod, int32_t scalar);
 int om_material_set_reaction(int mat, int kind, int temperature, int result);
+/* Material::addTemp / conductionSelf / conductionOther */
+int om_material_set_conduction(int mat, uint32_t add_temp, float cond_self, float cond_other);
+/* addTemp, conductionSelf bits, conductionOther bits */
+void om_material_conduction(int mat, uint32_t out[3]);
+/* temperature of a new SOUP tile of this material (TilesCreate) */
+int om_material_set_factory_temperature(int mat, int32_t temperature);
 int om_material_set_interaction(int mat, int other, int kind, int data1, int data2, int ofs_x, int ofs_y);
 int om_material_count(void);
 int om_material_find(const char *index_name);
@@ -83,6 +91,13 @@ long om_world_tick(om_world *wd, int order, int check_races);
 int om_particles_tick(om_world *wd);
 /* world::tick() followed by world::tickCells(), n times */
 void om_world_step(om_world *wd, int order, int n);
+/* world::tickTemperature (world.cpp:1950-2004), one Jacobi step over every cell */
+void om_tick_temperature(om_world *wd);
+/* om_world_step also runs om_tick_temperature after ticks whose index is 2 mod 4 */
+void om_world_set_temperature(om_world *wd, int on);
+/* per-cell temperature (i16): SOUP cells' own plane, the scalar of the others */
+void om_temperature_get(const om_world *wd, int16_t *out);
+void om_temperature_set(om_world *wd, const int16_t *in);
 
 int om_particles_count(const om_world *wd);
 void om_particles_get(const om_world *wd, om_particle *out);
