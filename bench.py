@@ -183,6 +183,7 @@ def bench_config1(args, rank, local_rank, world_size):
     # from pinned host memory, ticks, and reads the grid back
     e2e = e2e_config1(world, args, torch, cells, world_size)
     render = render_config1(fse, torch, W, H, seed, NP) if rank == 0 else None
+    temperature = temperature_config1(fse, torch, W, H, seed, NP) if rank == 0 else None
     cpu = None
     if rank == 0 and world_size == 1 and not args.no_cpu:
         cpu = cpu_baseline_config1(seed)
@@ -198,7 +199,7 @@ def bench_config1(args, rank, local_rank, world_size):
                    "l2": "flushed between timed steps (512 MiB write outside the events)",
                    "parallelism": "one independent world per GPU" if world_size > 1 else "single GPU"},
         "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
-        "wall_s": round(wall, 3), "render": render,
+        "wall_s": round(wall, 3), "render": render, "temperature": temperature,
     }
 
 
@@ -261,6 +262,55 @@ def render_config1(fse, torch, W, H, seed, NP, ticks=20):
             "dirty_cells_per_tick": ndirty // ticks, "dirty_pass_gbs": round(gbs, 1),
             "dirty_pass_frac": round(gbs / peak, 4), "peak": peak, "peak_kind": peak_kind,
             "particle_layer_ms": round(c_ms / ticks, 4), "ticks": ticks}
+
+
+def temperature_config1(fse, torch, W, H, seed, NP, calls=10):
+    """world::tickTemperature on the same workload (a world created with the
+    temperature step, so every fourth step of the warm-up already conducted heat
+    from the -1023 water): standalone conduction steps, each timed with CUDA events
+    on the world's stream with the L2 flushed before it. Algorithmic bytes of one
+    step: id 2 B + scalar 4 B + SOUP temperature 2 B read per cell, plus 4 B
+    (scalar) or 2 B (SOUP temperature) for each cell whose temperature changed,
+    counted from the temperature planes before and after each step."""
+    stream = torch.cuda.Stream()
+    world = fse.World(W, H, chunk_size=128, cell_iter=3, seed=seed, particle_capacity=4_000_000,
+                      spawn_capacity=2_000_000, stream=stream.cuda_stream, temperature_step=True)
+    world.generate(fse.GEN_MIX, seed)
+    world.addCell(config1_particles(NP, W, H, seed))
+    world.step(16)
+    soup = np.array([fse.material_get(i)[0] == fse.SOUP for i in range(fse.material_count())])
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    e = [_ev(torch) for _ in range(2)]
+    ms = 0.0
+    nbytes = nchanged = 0
+    cells = W * H
+    with torch.cuda.stream(stream):
+        world.tickTemperature()  # warm-up (scratch allocation, attribute setup)
+    torch.cuda.synchronize()
+    for i in range(calls):
+        before = world.temperature()
+        ids = world.state()["id"]
+        with torch.cuda.stream(stream):
+            _flush(flush, i)
+            e[0].record(stream)
+            world.tickTemperature()
+            e[1].record(stream)
+        torch.cuda.synchronize()
+        ms += e[0].elapsed_time(e[1])
+        ch = world.temperature() != before
+        sp = soup[ids]
+        nch_soup = int((ch & sp).sum())
+        nch = int(ch.sum())
+        nbytes += 8 * cells + 4 * (nch - nch_soup) + 2 * nch_soup
+        nchanged += nch
+    world.close()
+    peak, peak_kind = peaks()
+    gbs = nbytes / (ms / 1e3) / 1e9
+    return {"step_ms": round(ms / calls, 4), "gcells": round(cells * calls / (ms / 1e3) / 1e9, 3),
+            "changed_cells_per_step": nchanged // calls, "achieved_gbs": round(gbs, 1),
+            "frac": round(gbs / peak, 4), "peak": peak, "peak_kind": peak_kind, "calls": calls,
+            "kernels": "k_temp_tiles + k_temp_commit",
+            "l2": "flushed before each step (512 MiB write outside the events)"}
 
 
 def e2e_config1(world, args, torch, cells, world_size):

@@ -21,7 +21,8 @@ __all__ = [
     "InitMaterials", "RegisterMaterial", "PushMaterials", "load_lua_materials", "material_find",
     "material_count", "material_get", "set_reaction", "set_interaction", "lib",
     "AIR", "SOLID", "SAND", "SOUP", "GAS", "PASSABLE", "OBJECT", "GEN_EMPTY", "GEN_MIX", "GEN_ZIPF8",
-    "FLUID_ONE", "CFG_RENDER", "TEX_PIXELS", "TEX_EMISSION", "TEX_FIRE", "TEX_FLOW", "TEX_CELLS", "write_png",
+    "FLUID_ONE", "CFG_RENDER", "CFG_TEMPERATURE", "CFG_TEMPERATURE_STEP", "set_conduction", "set_factory_temperature", "get_conduction",
+    "TEX_PIXELS", "TEX_EMISSION", "TEX_FIRE", "TEX_FLOW", "TEX_CELLS", "write_png",
 ]
 
 AIR, SOLID, SAND, SOUP, GAS, PASSABLE, OBJECT = 0, 1, 2, 3, 4, 5, 5
@@ -98,13 +99,39 @@ def set_interaction(mat, other, kind, data1, data2, ofs_x, ofs_y):
     check(lib().fse_material_set_interaction(mat, other, kind, data1, data2, ofs_x, ofs_y), "set_interaction")
 
 
+def set_conduction(mat, add_temp, conduction_self, conduction_other):
+    """Material::addTemp / conductionSelf / conductionOther (game_datastruct.hpp:142-144)."""
+    check(lib().fse_material_set_conduction(mat, add_temp & 0xFFFFFFFF, conduction_self, conduction_other),
+          "set_conduction")
+
+
+def set_factory_temperature(mat, temperature):
+    """Temperature of new SOUP tiles of a material (TilesCreate, game_datastruct.cpp:427-437)."""
+    check(lib().fse_material_set_factory_temperature(mat, temperature), "set_factory_temperature")
+
+
+def get_conduction(mat):
+    """(addTemp, conductionSelf, conductionOther, factory temperature) of a material."""
+    out = np.zeros(4, np.uint32)
+    check(lib().fse_material_get_conduction(mat, ptr(out)), "get_conduction")
+    return int(out[0]), float(out[1:2].view(np.float32)[0]), float(out[2:3].view(np.float32)[0]), \
+        int(out[3:4].view(np.int32)[0])
+
+
 CFG_RENDER = 1
+CFG_TEMPERATURE = 2
+CFG_TEMPERATURE_STEP = 4
 TEX_PIXELS, TEX_EMISSION, TEX_FIRE, TEX_FLOW, TEX_CELLS = 0, 1, 2, 3, 4
 
 
-def _config(chunk_size=128, cell_iter=3, seed=0, particle_capacity=0, spawn_capacity=0, stream=None, render=False):
+def _config(chunk_size=128, cell_iter=3, seed=0, particle_capacity=0, spawn_capacity=0, stream=None, render=False,
+            temperature=False, temperature_step=False):
+    """temperature: keep liquid temperatures (FSE_CFG_TEMPERATURE); temperature_step:
+    also run the conduction step every fourth tick inside steps (FSE_CFG_TEMPERATURE_STEP)."""
     return FseConfig(chunk_size, cell_iter, seed & 0xFFFFFFFF, particle_capacity, spawn_capacity,
-                     C.c_void_p(stream) if stream else None, CFG_RENDER if render else 0)
+                     C.c_void_p(stream) if stream else None,
+                     (CFG_RENDER if render else 0) | (CFG_TEMPERATURE if temperature else 0) |
+                     (CFG_TEMPERATURE_STEP if temperature_step else 0))
 
 
 # ---------------------------------------------------------------------- world
@@ -115,13 +142,14 @@ class World:
               ("diff", np.int32))
 
     def __init__(self, width, height, chunk_size=128, cell_iter=3, seed=0, particle_capacity=0, spawn_capacity=0,
-                 stream=None, render=False, _handle=None):
+                 stream=None, render=False, temperature=False, temperature_step=False, _handle=None):
         self.lib = lib()
         self.width, self.height = int(width), int(height)
         self._owned = _handle is None
         if _handle is None:
             h = C.c_void_p()
-            cfg = _config(chunk_size, cell_iter, seed, particle_capacity, spawn_capacity, stream, render)
+            cfg = _config(chunk_size, cell_iter, seed, particle_capacity, spawn_capacity, stream, render, temperature,
+                          temperature_step)
             check(self.lib.fse_world_create(self.width, self.height, C.byref(cfg), C.byref(h)), "world_create")
             self.h = h
         else:
@@ -302,6 +330,23 @@ class World:
         out = np.zeros((self.height, self.width, 4), np.uint8)
         check(self.lib.fse_world_render_read(self.h, int(which), ptr(out)), "render_read")
         return out
+
+    # -- temperature
+    def temperature(self, out=None):
+        """MaterialInstance::temperature of every cell as an (H, W) int16 array."""
+        if out is None:
+            out = np.empty((self.height, self.width), np.int16)
+        check(self.lib.fse_world_temperature_read(self.h, ptr(out)), "temperature_read")
+        return out
+
+    def set_temperature(self, temps):
+        a = np.ascontiguousarray(temps, np.int16)
+        assert a.size == self.width * self.height
+        check(self.lib.fse_world_temperature_write(self.h, ptr(a)), "temperature_write")
+
+    def tickTemperature(self):
+        """world::tickTemperature (world.cpp:1950-2004), enqueued on the world's stream."""
+        check(self.lib.fse_world_tick_temperature(self.h), "tick_temperature")
 
     # -- solid islands
     def physicsCheck(self, x, y, pixels=True):

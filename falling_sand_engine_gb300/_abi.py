@@ -12,9 +12,10 @@ PARTICLE_DTYPE = np.dtype(
         ("x", "<f4"), ("y", "<f4"), ("vx", "<f4"), ("vy", "<f4"), ("ax", "<f4"), ("ay", "<f4"),
         ("target_x", "<f4"), ("target_y", "<f4"), ("target_force", "<f4"),
         ("lifetime", "<i4"), ("fade_time", "<i4"), ("colour", "<u4"), ("scalar", "<i4"),
-        ("id", "<u2"), ("flags", "u1"), ("bits", "u1"),
+        ("id", "<u2"), ("flags", "u1"), ("bits", "u1"), ("temperature", "<i2"), ("reserved", "<u2"),
     ]
 )
+assert PARTICLE_DTYPE.itemsize == 60
 BODY_DTYPE = np.dtype(
     [
         ("x", "<f4"), ("y", "<f4"), ("sin_a", "<f4"), ("cos_a", "<f4"),
@@ -46,6 +47,12 @@ SIGNATURES = {
     "fse_material_set_reaction": (_i, [_i, _i, _i, _i]),
     "fse_material_set_interaction": (_i, [_i, _i, _i, _i, _i, _i, _i]),
     "fse_material_set_factory": (_i, [_i, _u32, _i, _i, _i, C.c_int32]),
+    "fse_material_set_factory_temperature": (_i, [_i, C.c_int32]),
+    "fse_material_set_conduction": (_i, [_i, _u32, _f, _f]),
+    "fse_material_get_conduction": (_i, [_i, _vp]),
+    "fse_world_temperature_read": (_i, [_vp, _vp]),
+    "fse_world_temperature_write": (_i, [_vp, _vp]),
+    "fse_world_tick_temperature": (_i, [_vp]),
     "fse_materials_load_lua": (_i, [C.c_char_p, C.POINTER(_i)]),
     "fse_materials_push": (_i, []),
     "fse_material_count": (_i, []),

@@ -9,7 +9,9 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfse.so")
 SOURCES = ["fse_tick.cu", "fse_particles.cu", "fse_objects.cu", "fse_api.cu", "fse_batch.cu", "fse_noalloc.cu",
-           "fse_render.cu", "fse_islands.cu"]
+           "fse_render.cu", "fse_islands.cu", "fse_temperature.cu", "fse_tick_temp.cu"]
+# sources that include another source
+SOURCE_DEPS = {"fse_tick_temp.cu": ["fse_tick.cu"]}
 HEADERS = ["fse_internal.cuh", "fse_host.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
@@ -36,7 +38,8 @@ def build(verbose=False, force=False, extra=()):
         s = os.path.join(CSRC, src)
         o = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
         objs.append(o)
-        if force or _stale(o, [s] + headers):
+        deps = [os.path.join(CSRC, d) for d in SOURCE_DEPS.get(src, [])]
+        if force or _stale(o, [s] + deps + headers):
             cmd = [nvcc, *ARCH, *FLAGS, *extra, "-c", s, "-o", o]
             if verbose:
                 cmd.insert(1, "-Xptxas=-v")

@@ -31,6 +31,9 @@ struct HostMat {
     uint32_t f_base;
     int f_shift, f_lo, f_mod;
     int32_t f_scalar;
+    int32_t f_temp;  // factory temperature of SOUP tiles
+    uint32_t add_temp;
+    float cond_self, cond_other;
     int n_react;
     int react[4][3];
     int interact;
@@ -65,6 +68,8 @@ int add_mat(const char *name, const char *index_name, int type, int slip, int al
     m.emit_colour = emit_colour;
     m.f_base = colour;
     m.f_scalar = (type == T_SOUP) ? Q_DEFAULT : 0;
+    m.cond_self = 1.0f;  // Material defaults, game_datastruct.hpp:142-144
+    m.cond_other = 1.0f;
     g_mats.push_back(m);
     g_dirty = true;
     return (int)g_mats.size() - 1;
@@ -165,6 +170,22 @@ void builtin_materials() {
     set_factory(find_mat("FLAT_COBBLE_DIRT"), 0x624530u, 0, 0, 0, 0);
     set_factory(find_mat("GENERIC_AIR"), 0x000000u, 0, 0, 0, 0);
     set_factory(find_mat("GENERIC_SOLID"), 0xff0000u, 0, 0, 0, 0);
+    // SOUP factory temperatures, game_datastruct.cpp:427-437
+    g_mats[find_mat("WATER")].f_temp = -1023;
+    g_mats[find_mat("LAVA")].f_temp = 1024;
+    // conduction, game_datastruct.cpp:124-141 (double literals rounded to float)
+    auto cond = [](const char *nm, uint32_t add, double cs, double co) {
+        HostMat &m = g_mats[find_mat(nm)];
+        m.add_temp = add;
+        m.cond_self = (float)cs;
+        m.cond_other = (float)co;
+    };
+    cond("GENERIC_AIR", 0, 0.8, 0.8);
+    cond("LAVA", 2, 0.5, 0.7);
+    cond("COBBLE_STONE", 0, 0.01, 0.4);
+    cond("COBBLE_DIRT", 0, 1.0, 1.0);
+    cond("GOLD_ORE", 0, 1.0, 1.0);
+    cond("GOLD_MOLTEN", 0, 1.0, 1.0);
 
     // reactions, game_datastruct.cpp:246-260
     add_reaction(find_mat("LAVA"), REACT_BELOW, 512, find_mat("OBSIDIAN"));
@@ -246,6 +267,10 @@ void build_table(MatTable &t) {
         t.f_base[i] = m.f_base;
         t.f_pack[i] = (uint32_t)(m.f_shift & 0xFF) | ((uint32_t)(m.f_lo & 0xFFF) << 8) | ((uint32_t)(m.f_mod & 0xFFF) << 20);
         t.f_scalar[i] = m.f_scalar;
+        t.f_temp[i] = m.f_temp;
+        t.add_temp[i] = m.add_temp;
+        t.cond_self[i] = m.cond_self;
+        t.cond_other[i] = m.cond_other;
         t.n_react[i] = m.n_react;
         for (int r = 0; r < m.n_react; r++)
             for (int k = 0; k < 3; k++) t.react[i][r][k] = m.react[r][k];
@@ -343,7 +368,7 @@ void PassTimer::drain() {
 
 int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], const int n_items[4], int max_iter, int C,
                  int threads, int grid, bool particles, int move_blocks, int stage_blocks, cudaStream_t s,
-                 PassTimer *timer) {
+                 PassTimer *timer, int temp_tiles, bool temp_track) {
     int halo = tick_halo();
     for (int iter = 0; iter < max_iter; iter++)  // world.cpp:1050
         for (int tk = 0; tk < 4; tk++) {         // world.cpp:1057-1060
@@ -354,7 +379,7 @@ int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], con
                 cudaEventRecord(a, s);
             }
             cudaError_t e = launch_colour_pass(d_worlds, items[tk], n_items[tk], iter, tk, g_dev_mt, halo, C, threads,
-                                               grid, s);
+                                               grid, s, temp_track);
             if (e != cudaSuccess) return FSE_E_CUDA;
             if (timer) {
                 cudaEventRecord(b, s);
@@ -367,6 +392,10 @@ int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], con
     if (particles) {
         if (launch_particle_tick(d_worlds, n_worlds, g_dev_mt, move_blocks, s) != cudaSuccess) return FSE_E_CUDA;
         count_launches(PARTICLE_TICK_LAUNCHES);
+    }
+    if (temp_tiles > 0) {  // game.cpp:2157-2159, decided per world on the device
+        if (launch_temperature(d_worlds, n_worlds, temp_tiles, g_dev_mt, true, s) != cudaSuccess) return FSE_E_CUDA;
+        count_launches(TEMPERATURE_LAUNCHES);
     }
     return FSE_OK;
 }
@@ -451,6 +480,36 @@ int fse_material_find(const char *index_name) {
     if (!index_name) return -1;
     std::lock_guard<std::mutex> lk(g_mu);
     return find_mat(index_name);
+}
+
+int fse_material_set_factory_temperature(int mat, int32_t temperature) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (mat < 0 || mat >= (int)g_mats.size()) return FSE_E_INVAL;
+    g_mats[mat].f_temp = temperature;
+    g_dirty = true;
+    return FSE_OK;
+}
+
+int fse_material_set_conduction(int mat, uint32_t add_temp, float conduction_self, float conduction_other) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (mat < 0 || mat >= (int)g_mats.size()) return FSE_E_INVAL;
+    HostMat &m = g_mats[mat];
+    m.add_temp = add_temp;
+    m.cond_self = conduction_self;
+    m.cond_other = conduction_other;
+    g_dirty = true;
+    return FSE_OK;
+}
+
+int fse_material_get_conduction(int mat, uint32_t out[4]) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (mat < 0 || mat >= (int)g_mats.size() || !out) return FSE_E_INVAL;
+    const HostMat &m = g_mats[mat];
+    out[0] = m.add_temp;
+    memcpy(&out[1], &m.cond_self, 4);
+    memcpy(&out[2], &m.cond_other, 4);
+    out[3] = (uint32_t)m.f_temp;
+    return FSE_OK;
 }
 
 int fse_material_get(int id, int32_t out[16]) {
@@ -627,7 +686,7 @@ static void free_world(fse_world *w) {
     for (auto &g : w->graphs) cudaGraphExecDestroy(g.second);
     w->graphs.clear();
     WorldDev &h = w->h;
-    void *ptrs[] = {h.id, h.col, h.sc, h.fl, h.df, h.stage, h.cp_count, h.cp_base, h.p_state, h.p_lxly,
+    void *ptrs[] = {h.id, h.col, h.sc, h.fl, h.df, h.tp, h.tnew, h.stage, h.cp_count, h.cp_base, h.p_state, h.p_lxly,
                     h.req_list, h.req_list2, h.req_target, h.scan_tmp, h.ledger, h.airmap, w->ctr, w->d, w->claim,
                     w->mask_bits, w->obj_list, w->obj_n};
     for (void *q : ptrs)
@@ -635,7 +694,7 @@ static void free_world(fse_world *w) {
     PartSoA *ps[2] = {&h.p, &h.q};
     for (PartSoA *p : ps) {
         void *a[] = {p->x, p->y, p->vx, p->vy, p->ax, p->ay, p->tx, p->ty, p->tf, p->life, p->fade, p->col, p->sc,
-                     p->id, p->fl, p->bits};
+                     p->tp, p->id, p->fl, p->bits};
         for (void *q : a)
             if (q) cudaFree(q);
     }
@@ -643,7 +702,7 @@ static void free_world(fse_world *w) {
         if (w->items[k]) cudaFree(w->items[k]);
     void *rs[] = {h.dirty,      h.flow,      w->pflow,    w->owner,    w->moving,   w->tex[0],   w->tex[1],
                   w->tex[2],    w->tex[3],   w->tex[4],   w->isl_mark, w->isl_lab,  w->isl_aux,  w->isl_list,
-                  w->isl_out,   w->isl_pix,  w->isl_tab,  w->isl_seg};
+                  w->isl_out,   w->isl_pix,  w->isl_tab,  w->isl_seg,  w->temp_io};
     for (void *q : rs)
         if (q) cudaFree(q);
     if (w->own_stream && w->stream) cudaStreamDestroy(w->stream);
@@ -736,6 +795,14 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
              dalloc(w, &p->ax, pc) && dalloc(w, &p->ay, pc) && dalloc(w, &p->tx, pc) && dalloc(w, &p->ty, pc) &&
              dalloc(w, &p->tf, pc) && dalloc(w, &p->life, pc) && dalloc(w, &p->fade, pc) && dalloc(w, &p->col, pc) &&
              dalloc(w, &p->sc, pc) && dalloc(w, &p->id, pc) && dalloc(w, &p->fl, pc) && dalloc(w, &p->bits, pc);
+    }
+    if (ok && (c.flags & (FSE_CFG_TEMPERATURE | FSE_CFG_TEMPERATURE_STEP))) {  // liquid temperatures
+        ok = dalloc(w, &h.tp, n) && dalloc(w, &h.p.tp, pc) && dalloc(w, &h.q.tp, pc);
+        if (ok) cudaMemset(h.tp, 0, n * 2);
+    }
+    if (ok && (c.flags & FSE_CFG_TEMPERATURE_STEP)) {  // and the conduction step inside every step
+        h.temp_on = 1;
+        ok = dalloc(w, &h.tnew, temperature_scratch_cells(width, height));
     }
     if (ok && (c.flags & FSE_CFG_RENDER)) {
         ok = dalloc(w, &h.dirty, n) && dalloc(w, &h.flow, 2 * n) && dalloc(w, &w->pflow, 2 * n) &&
@@ -923,6 +990,7 @@ __global__ void k_generate(WorldDev *wd, int kind, uint32_t seed, const MatTable
         w.fl[i] = 0;
         w.df[i] = 0;
         w.sc[i] = mt->f_scalar[mid];
+        if (w.tp) w.tp[i] = mt_type(mt->a[mid]) == T_SOUP ? (int16_t)mt->f_temp[mid] : (int16_t)0;
         uint32_t colour = mt->f_base[mid];
         uint32_t fp = mt->f_pack[mid];
         int mod = (int)(fp >> 20);
@@ -989,12 +1057,16 @@ int fse_world_set_tile(fse_world *w, int x, int y, uint16_t id, uint32_t col, in
 static int world_move_blocks(const fse_world *w) { return std::max(1, std::min(sm_count() * 4, ceil_div(w->part_cap, 256))); }
 static int world_stage_blocks(const fse_world *w) { return std::max(1, std::min(sm_count() * 2, ceil_div(w->stage_cap, 256))); }
 
+// 128 x 32 tiles of the temperature step when the world runs it inside its steps
+static int world_temp_tiles(const fse_world *w) { return w->h.temp_on ? temperature_tiles(w->W, w->H) : 0; }
+
 static int world_enqueue(fse_world *w, bool particles_after_tick, bool tick, bool particles) {
     int rc = ensure_materials_pushed();
     if (rc) return rc;
     if (tick) {
         rc = enqueue_step(w->d, 1, w->items, w->n_items, w->cell_iter, w->C, w->threads, w->grid, particles_after_tick,
-                          world_move_blocks(w), world_stage_blocks(w), w->stream, w->timer);
+                          world_move_blocks(w), world_stage_blocks(w), w->stream, w->timer, world_temp_tiles(w),
+                          w->h.tp != nullptr);
         if (rc) return rc;
     } else if (particles) {
         if (launch_particle_tick(w->d, 1, g_dev_mt, world_move_blocks(w), w->stream) != cudaSuccess) return FSE_E_CUDA;
@@ -1065,7 +1137,8 @@ int fse_world_step_graph(fse_world *w, int n) {
             int erc = FSE_OK;
             for (int i = 0; i < k && erc == FSE_OK; i++)
                 erc = enqueue_step(w->d, 1, w->items, w->n_items, w->cell_iter, w->C, w->threads, w->grid, true,
-                                   world_move_blocks(w), world_stage_blocks(w), w->stream);
+                                   world_move_blocks(w), world_stage_blocks(w), w->stream, nullptr,
+                                   world_temp_tiles(w), w->h.tp != nullptr);
             cudaError_t e = cudaStreamEndCapture(w->stream, &g);
             const long long kn = fse_launch_counter() - c0;
             count_launches(-kn);
@@ -1121,6 +1194,7 @@ int fse_particles_add(fse_world *w, const fse_particle *parts, int n) {
     if ((long long)cur + n > w->part_cap) return FSE_E_CAPACITY;
     std::vector<float> f[9];
     std::vector<int32_t> life(n), fade(n), sc(n);
+    std::vector<int16_t> tp(n);
     std::vector<uint32_t> col(n);
     std::vector<uint16_t> id(n);
     std::vector<uint8_t> fl(n), bits(n);
@@ -1134,6 +1208,7 @@ int fse_particles_add(fse_world *w, const fse_particle *parts, int n) {
         life[i] = p.lifetime;
         fade[i] = p.fade_time;
         sc[i] = p.scalar;
+        tp[i] = p.temperature;
         col[i] = p.colour;
         id[i] = p.id;
         fl[i] = p.flags & (uint8_t)~VISITED;
@@ -1146,6 +1221,7 @@ int fse_particles_add(fse_world *w, const fse_particle *parts, int n) {
     FSE_CUDA_TRY(cudaMemcpyAsync(P.life + cur, life.data(), n * 4, cudaMemcpyHostToDevice, w->stream));
     FSE_CUDA_TRY(cudaMemcpyAsync(P.fade + cur, fade.data(), n * 4, cudaMemcpyHostToDevice, w->stream));
     FSE_CUDA_TRY(cudaMemcpyAsync(P.sc + cur, sc.data(), n * 4, cudaMemcpyHostToDevice, w->stream));
+    if (P.tp) FSE_CUDA_TRY(cudaMemcpyAsync(P.tp + cur, tp.data(), n * 2, cudaMemcpyHostToDevice, w->stream));
     FSE_CUDA_TRY(cudaMemcpyAsync(P.col + cur, col.data(), n * 4, cudaMemcpyHostToDevice, w->stream));
     FSE_CUDA_TRY(cudaMemcpyAsync(P.id + cur, id.data(), n * 2, cudaMemcpyHostToDevice, w->stream));
     FSE_CUDA_TRY(cudaMemcpyAsync(P.fl + cur, fl.data(), n, cudaMemcpyHostToDevice, w->stream));
@@ -1166,6 +1242,7 @@ int fse_particles_read(fse_world *w, fse_particle *out, int cap, int *out_n) {
     if (m == 0) return FSE_OK;
     std::vector<float> f[9];
     std::vector<int32_t> life(m), fade(m), sc(m);
+    std::vector<int16_t> tp(m);
     std::vector<uint32_t> col(m);
     std::vector<uint16_t> id(m);
     std::vector<uint8_t> fl(m), bits(m);
@@ -1178,6 +1255,7 @@ int fse_particles_read(fse_world *w, fse_particle *out, int cap, int *out_n) {
     FSE_CUDA_TRY(cudaMemcpyAsync(life.data(), P.life, m * 4, cudaMemcpyDeviceToHost, w->stream));
     FSE_CUDA_TRY(cudaMemcpyAsync(fade.data(), P.fade, m * 4, cudaMemcpyDeviceToHost, w->stream));
     FSE_CUDA_TRY(cudaMemcpyAsync(sc.data(), P.sc, m * 4, cudaMemcpyDeviceToHost, w->stream));
+    if (P.tp) FSE_CUDA_TRY(cudaMemcpyAsync(tp.data(), P.tp, m * 2, cudaMemcpyDeviceToHost, w->stream));
     FSE_CUDA_TRY(cudaMemcpyAsync(col.data(), P.col, m * 4, cudaMemcpyDeviceToHost, w->stream));
     FSE_CUDA_TRY(cudaMemcpyAsync(id.data(), P.id, m * 2, cudaMemcpyDeviceToHost, w->stream));
     FSE_CUDA_TRY(cudaMemcpyAsync(fl.data(), P.fl, m, cudaMemcpyDeviceToHost, w->stream));
@@ -1201,6 +1279,8 @@ int fse_particles_read(fse_world *w, fse_particle *out, int cap, int *out_n) {
         p.id = id[i];
         p.flags = fl[i];
         p.bits = bits[i];
+        p.temperature = tp[i];
+        p.reserved = 0;
     }
     return FSE_OK;
 }

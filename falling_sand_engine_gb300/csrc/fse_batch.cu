@@ -63,12 +63,28 @@ int build_tables(const std::vector<fse_world *> &ws, WorldDev **d_table, uint32_
     return FSE_OK;
 }
 
+// the most temperature tiles of the worlds that run the temperature step (0: none)
+int temp_tiles_of(const std::vector<fse_world *> &ws) {
+    int t = 0;
+    for (const fse_world *w : ws)
+        if (w->h.temp_on) t = std::max(t, temperature_tiles(w->W, w->H));
+    return t;
+}
+// some world keeps liquid temperatures: the colour pass that copies them runs
+bool temp_track_of(const std::vector<fse_world *> &ws) {
+    for (const fse_world *w : ws)
+        if (w->h.tp) return true;
+    return false;
+}
+
 int batch_enqueue(fse_batch *b, int n) {
     int rc = ensure_materials_pushed();
     if (rc) return rc;
+    const int tt = temp_tiles_of(b->worlds);
+    const bool tr = temp_track_of(b->worlds);
     for (int i = 0; i < n; i++) {
         rc = enqueue_step(b->d_table, (int)b->worlds.size(), b->items, b->n_items, b->max_iter, b->C, b->threads,
-                          b->grid, true, b->move_blocks, b->stage_blocks, b->stream);
+                          b->grid, true, b->move_blocks, b->stage_blocks, b->stream, nullptr, tt, tr);
         if (rc) return rc;
     }
     return FSE_OK;
@@ -94,16 +110,18 @@ bool snap_take(fse_world *w, Snapshot &s, cudaStream_t st) {
     size_t n = (size_t)w->W * w->H;
     const WorldDev &h = w->h;
     std::vector<std::pair<void *, size_t>> list = {
-        {h.id, n * 2}, {h.col, n * 4}, {h.sc, n * 4}, {h.fl, n}, {h.df, n * 4}, {w->ctr, 64},
+        {h.id, n * 2}, {h.col, n * 4}, {h.sc, n * 4}, {h.fl, n}, {h.df, n * 4}, {h.tp, n * 2}, {w->ctr, 64},
         {h.ledger, LED_ROWS * MAXMAT * 8}};
     const PartSoA &p = h.p;
     size_t pc = (size_t)w->part_cap;
     void *pa[] = {p.x, p.y, p.vx, p.vy, p.ax, p.ay, p.tx, p.ty, p.tf, p.life, p.fade, p.col, p.sc};
     for (void *q : pa) list.push_back({q, pc * 4});
     list.push_back({p.id, pc * 2});
+    list.push_back({p.tp, pc * 2});
     list.push_back({p.fl, pc});
     list.push_back({p.bits, pc});
     for (auto &e : list) {
+        if (!e.first) continue;  // planes the world does not keep
         void *d = nullptr;
         if (cudaMalloc(&d, e.second) != cudaSuccess) return false;
         cudaMemcpyAsync(d, e.first, e.second, cudaMemcpyDeviceToDevice, st);
@@ -453,8 +471,10 @@ int fse_server_step(fse_server *s, int *out_active) {
     }
     int rc = ensure_materials_pushed();
     if (rc) return rc;
+    std::vector<fse_world *> act;
+    for (int sl : want) act.push_back(s->slots[sl]);
     rc = enqueue_step(s->d_table, (int)want.size(), s->items, s->n_items, max_iter, s->C, 1024, 0, true, mb, sb,
-                      s->stream);
+                      s->stream, nullptr, temp_tiles_of(act), temp_track_of(act));
     if (rc) return rc;
     if (cudaStreamSynchronize(s->stream) != cudaSuccess) return FSE_E_CUDA;
     double now = std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - s->t0).count();

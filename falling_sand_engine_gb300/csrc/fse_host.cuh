@@ -58,6 +58,8 @@ struct fse_world {
     uint32_t *isl_pix;
     fse_island *isl_tab;
     int isl_tab_cap;
+    // temperature read/write staging (allocated on first use)
+    int16_t *temp_io;
 };
 
 namespace fse {
@@ -67,12 +69,21 @@ int ensure_materials_pushed();
 const MatTable &host_table();
 
 size_t colour_pass_smem(int C, int halo);
+// temp: some world of the table keeps liquid temperatures (tp != NULL)
 cudaError_t launch_colour_pass(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
-                               const MatTable *mt, int halo, int C, int threads, int grid, cudaStream_t s);
+                               const MatTable *mt, int halo, int C, int threads, int grid, cudaStream_t s,
+                               bool temp = false);
 cudaError_t launch_spawn_append(WorldDev *d_worlds, int n_worlds, int stage_blocks, cudaStream_t s);
 cudaError_t launch_particle_tick(WorldDev *d_worlds, int n_worlds, const MatTable *mt, int move_blocks,
                                  cudaStream_t s);
 constexpr int PARTICLE_TICK_LAUNCHES = 12;  // kernels launch_particle_tick issues
+// world::tickTemperature over a set of worlds (max_tiles: the most 128 x 32 tiles of
+// any of them); gated: only worlds with temp_on, after ticks whose index is 2 mod 4
+cudaError_t launch_temperature(const WorldDev *d_worlds, int n_worlds, int max_tiles, const MatTable *mt, bool gated,
+                               cudaStream_t s);
+constexpr int TEMPERATURE_LAUNCHES = 2;
+size_t temperature_scratch_cells(int W, int H);
+int temperature_tiles(int W, int H);
 void particle_prepare();
 int particle_scan_blocks();
 int sm_count();
@@ -83,7 +94,7 @@ int tick_halo();
 // share a device descriptor table
 int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], const int n_items[4], int max_iter,
                  int C, int threads, int grid, bool particles, int move_blocks, int stage_blocks, cudaStream_t s,
-                 PassTimer *timer = nullptr);
+                 PassTimer *timer = nullptr, int temp_tiles = 0, bool temp_track = false);
 void count_launches(long long n);
 
 }  // namespace fse

@@ -89,6 +89,12 @@ struct MatTable {
     // no table (k <= 0 or not finite), evaluate in double.
     float flow_thr[MAXMAT][256];
     uint8_t flow_thr_ok[MAXMAT];
+    // temperature: the factory temperature of SOUP tiles (whose scalar is the
+    // amount), and Material::addTemp / conductionSelf / conductionOther
+    int32_t f_temp[MAXMAT];
+    uint32_t add_temp[MAXMAT];
+    float cond_self[MAXMAT];
+    float cond_other[MAXMAT];
 };
 
 __host__ __device__ __forceinline__ int mt_type(uint32_t a) { return (int)(a & 0xFF); }
@@ -108,7 +114,8 @@ struct SpawnRec {  // one spawned particle awaiting its place in the list (48 B)
     uint8_t bits;
     int16_t lifetime;
     int16_t fade;
-    uint32_t pad;
+    int16_t temp;  // temperature of a SOUP tile
+    uint16_t pad;
 };
 
 struct PartSoA {  // particle list, structure of arrays
@@ -116,6 +123,7 @@ struct PartSoA {  // particle list, structure of arrays
     int32_t *life, *fade;
     uint32_t *col;
     int32_t *sc;
+    int16_t *tp;  // temperature of SOUP tiles
     uint16_t *id;
     uint8_t *fl, *bits;
 };
@@ -126,6 +134,12 @@ struct WorldDev {
     int32_t *sc;
     uint8_t *fl;
     int32_t *df;  // pending fluid diff; meaningful only where the cell is SOUP
+    // temperature of SOUP cells (MaterialInstance::temperature; every other cell
+    // keeps it in sc). Kept only by worlds created with FSE_CFG_TEMPERATURE (NULL
+    // otherwise, and then the particle lists have no temperatures either): liquid
+    // temperatures change no other result of a tick, and copying them with every
+    // liquid move costs the colour pass global-memory round trips.
+    int16_t *tp;
     int W, H, C, cell_iter;
     uint32_t seed;
     uint32_t *tick;  // device counter, advanced on the device so multi-tick graphs replay correctly
@@ -156,6 +170,10 @@ struct WorldDev {
     // dirty pass, and the tick's flows per cell (Q16.16, x then y, wrapping sums)
     uint8_t *dirty;
     int32_t *flow;
+    // temperature step (FSE_CFG_TEMPERATURE): run after ticks whose index is 2 mod 4;
+    // tnew holds the deferred results of tile-edge cells
+    int temp_on;
+    int32_t *tnew;
 };
 
 __host__ __device__ __forceinline__ int ceil_div(int a, int b) { return (a + b - 1) / b; }

@@ -97,6 +97,8 @@ __global__ void k_na_spawn_out(const WorldDev *__restrict__ wd, fse_particle *ou
         p.id = s.id;
         p.flags = s.flags;
         p.bits = s.bits;
+        p.temperature = s.temp;
+        p.reserved = 0;
         out[pos] = p;
     }
 }

@@ -155,6 +155,7 @@ __global__ void __launch_bounds__(1024) k_obj_rounds(WorldDev *wd, const MatTabl
                         w.p.fade[pos] = 60;
                         w.p.col[pos] = w.col[tg];
                         w.p.sc[pos] = w.sc[tg];
+                        if (w.tp) w.p.tp[pos] = ty == T_SOUP ? w.tp[tg] : (int16_t)0;
                         w.p.id[pos] = w.id[tg];
                         w.p.fl[pos] = w.fl[tg];
                         w.p.bits[pos] = 0;

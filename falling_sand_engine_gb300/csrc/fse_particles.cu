@@ -92,6 +92,7 @@ __global__ void k_spawn_scatter(const WorldDev *__restrict__ worlds) {
         w.p.fade[i] = s.fade;
         w.p.col[i] = s.colour;
         w.p.sc[i] = s.scalar;
+        if (w.tp) w.p.tp[i] = s.temp;  // particle temperatures exist with the grid's
         w.p.id[i] = s.id;
         w.p.fl[i] = s.flags;
         w.p.bits[i] = s.bits;
@@ -304,6 +305,9 @@ __device__ __forceinline__ void dep_fill(const WorldDev &w, int i, int c) {
     w.col[c] = w.p.col[i];
     w.sc[c] = w.p.sc[i];
     w.fl[c] = w.p.fl[i];
+    // the target was AIR, whose temperature word means nothing: the particle's
+    // (a SOUP tile's temperature; 0 for the others) is stored without a type test
+    if (w.tp) w.tp[c] = w.p.tp[i];
     if (w.dirty) w.dirty[c] = 1;
     w.p_state[i] = PS_DEAD;
 }
@@ -579,6 +583,7 @@ __global__ void k_cmp_scatter(const WorldDev *__restrict__ worlds) {
             w.q.fade[o] = w.p.fade[i];
             w.q.col[o] = w.p.col[i];
             w.q.sc[o] = w.p.sc[i];
+            if (w.tp) w.q.tp[o] = w.p.tp[i];
             w.q.id[o] = w.p.id[i];
             w.q.fl[o] = w.p.fl[i];
             w.q.bits[o] = w.p.bits[i];
@@ -610,6 +615,7 @@ __global__ void k_cmp_copy(const WorldDev *__restrict__ worlds, int nblocks) {
         w.p.fade[o] = w.q.fade[o];
         w.p.col[o] = w.q.col[o];
         w.p.sc[o] = w.q.sc[o];
+        if (w.tp) w.p.tp[o] = w.q.tp[o];
         w.p.id[o] = w.q.id[o];
         w.p.fl[o] = w.q.fl[o];
         w.p.bits[o] = w.q.bits[o];

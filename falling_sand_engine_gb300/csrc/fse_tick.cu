@@ -19,6 +19,12 @@
 // later; no rule modifies such a neighbour between the copy and the write-back, so
 // here the write-back is a move inside shared memory at write time (move()), which
 // keeps only the active cell in registers.
+//
+// The kernel is built twice (template TEMP): worlds that keep liquid temperatures
+// (FSE_CFG_TEMPERATURE) copy them with every liquid move; the others run code with
+// no trace of that plane. fse_tick_temp.cu compiles the TEMP instantiation as a
+// translation unit of its own (including this file with FSE_TICK_TEMP_TU), so the
+// two build in parallel.
 #include "fse_internal.cuh"
 
 // Optional per-phase cycle counters of the colour pass (build with
@@ -89,6 +95,7 @@ struct SpawnEv {
     int32_t sc;
     float vx, vy;
     uint32_t ck, k0;
+    int16_t tp;  // temperature of a SOUP tile (kind 2; set only where temperatures are kept)
 };
 
 // ------------------------------------------------------- shared-memory tile
@@ -111,6 +118,7 @@ struct TileData {
     const uint32_t *ma;  // material word A in shared memory
     const float *md;     // density in shared memory
     int32_t *df;         // HBM diff plane
+    int16_t *tp;         // HBM temperature plane of SOUP cells (NULL: not kept)
     int x0, y0, RW, RHF, RHI;
     int W, H;
     int id_solid, id_air;
@@ -119,8 +127,9 @@ struct TileData {
     int ax0, ay0, aw;
 };
 
-template <bool EDGE>
+template <bool EDGE, bool TEMP>
 struct Tile : TileData {
+    static constexpr bool kTemp = TEMP;
     __device__ __forceinline__ explicit Tile(const TileData &d) : TileData(d) {}
 
     // 10 snapshot bits of column x starting at row y (0 outside the snapshot)
@@ -213,7 +222,27 @@ struct Tile : TileData {
         s_fl[d] = (uint8_t)((s_fl[s] & (uint8_t)~VISITED) | (s_fl[d] & VISITED));
         s_sc[d] = s_sc[s];
         s_col[d] = s_col[s];
-        if (mt_type(ma[v]) == T_SOUP) df[dy * W + dx] = df[sy * W + sx];
+        if (mt_type(ma[v]) == T_SOUP) {
+            df[dy * W + dx] = df[sy * W + sx];
+            if (TEMP && tp) tp[dy * W + dx] = tp[sy * W + sx];
+        }
+    }
+    // Temperatures of SOUP cells live in HBM beside the diff; the tile's scalar is
+    // their amount. They move only where a SOUP cell moves or is made, so the
+    // rules touch them at those few places and nowhere else.
+    __device__ __forceinline__ int16_t tp_load(int x, int y) const {
+        return (TEMP && tp) ? tp[y * W + x] : (int16_t)0;
+    }
+    __device__ __forceinline__ void tp_store(int x, int y, int16_t v) const {
+        if (TEMP && tp && inw(x, y)) tp[y * W + x] = v;
+    }
+    // put a tile just made by a factory (TilesCreate): a SOUP tile takes the
+    // factory temperature, or `keep` (a reaction keeps the old temperature)
+    __device__ __forceinline__ void put_new(int x, int y, const Cell &c, const MatTable *mt, bool keep = false,
+                                            int32_t keep_t = 0) const {
+        put(x, y, c);
+        if (TEMP && tp && mt_type(ma[c.id]) == T_SOUP)
+            tp_store(x, y, keep ? (int16_t)keep_t : (int16_t)__ldg(&mt->f_temp[c.id]));
     }
     // only a change marks the cell for write-back (settled sand clears an already
     // clear flag every pass)
@@ -360,6 +389,7 @@ __device__ __forceinline__ void soup_flow(const TL &T, Ctx &c, Cell &t, int32_t 
         nt.col = t.col;
         nt.df = flow;
         T.put(nx, ny, nt);
+        T.tp_store(nx, ny, T.tp_load(x, y));  // MaterialInstance(tile.mat, tile.color, tile.temperature)
         led_add(c, LED_CN, t.id, 1);
     } else {
         T.add_diff(nx, ny, flow);
@@ -425,7 +455,7 @@ __device__ __forceinline__ void rule_a(const TL &T, Ctx &c, int x, int y) {
                         if (c.D() % 500 == 0) {
                             Cell f = create_tile(c, c.id_fire);
                             led_replace_at(T, c, x + xx, y + yy, f);
-                            T.put(x + xx, y + yy, f);
+                            T.put_new(x + xx, y + yy, f, mt);
                             T.setvis(x + xx, y + yy);
                         }
                     }
@@ -458,7 +488,7 @@ __device__ __forceinline__ void rule_a(const TL &T, Ctx &c, int x, int y) {
                             if (doit) {
                                 Cell nt = create_tile(c, d1);
                                 led_replace_at(T, c, x + xx, y + yy, nt);
-                                T.put(x + xx, y + yy, nt);
+                                T.put_new(x + xx, y + yy, nt, mt);
                                 T.setvis(x + xx, y + yy);
                             }
                         }
@@ -474,9 +504,11 @@ __device__ __forceinline__ void rule_a(const TL &T, Ctx &c, int x, int y) {
                 bool hit = (kind == REACT_BELOW) ? (t.sc < temp) : (t.sc > temp);
                 if (hit) {
                     Cell nt = create_tile(c, res);
+                    // the temperature is kept (world.cpp:1188,1196): in the scalar,
+                    // or beside the amount of a SOUP result
                     if (mt_type(ma[nt.id]) != T_SOUP) nt.sc = t.sc;
                     led_replace_at(T, c, x, y, nt);
-                    T.put(x, y, nt);
+                    T.put_new(x, y, nt, mt, true, t.sc);
                     T.setvis(x, y);
                     react = true;
                 }
@@ -531,6 +563,7 @@ __device__ __forceinline__ void rule_a(const TL &T, Ctx &c, int x, int y) {
             c.ev.fl = 0;
             c.ev.col = t.col;
             c.ev.sc = t.sc;
+            if (TL::kTemp) c.ev.tp = T.tp_load(x, y);
             c.ev.ck = c.key();
             c.ev.k0 = c.k;
             c.k += 2 * n;
@@ -548,8 +581,10 @@ __device__ __forceinline__ void rule_a(const TL &T, Ctx &c, int x, int y) {
         } else if (c.iter == 0 && bT == T_SOUP && bid != (int)t.id) {
             if (c.D() % 10 == 0) {
                 t.df += T.df_load(x, y);  // the cell leaves its position: carry the whole diff
+                const int16_t tv = T.tp_load(x, y);
                 T.move(x, y, x, y + 1);
                 T.put(x, y + 1, t);
+                T.tp_store(x, y + 1, tv);
                 return;
             }
         }
@@ -593,8 +628,10 @@ __device__ __forceinline__ void rule_a(const TL &T, Ctx &c, int x, int y) {
         } else if (c.iter == 0 && tT == T_SOUP && tid != (int)t.id) {
             if (c.D() % 10 == 0) {
                 t.df += T.df_load(x, y);
+                const int16_t tv = T.tp_load(x, y);
                 T.move(x, y, x, y - 1);
                 T.put(x, y - 1, t);
+                T.tp_store(x, y - 1, tv);
                 return;
             }
         }
@@ -620,17 +657,17 @@ __device__ __forceinline__ void rule_a(const TL &T, Ctx &c, int x, int y) {
         if ((int)t.id == c.id_water && T.id(x, y + 1) == c.id_lava) {
             Cell st = create_tile(c, c.id_steam);
             led_swap(c, t.id, (long long)t.sc + T.df_load(x, y), st.id, (long long)st.sc);
-            T.put(x, y, st);
+            T.put_new(x, y, st, mt);
             Cell ob = create_tile(c, c.id_obsidian);
             led_replace_at(T, c, x, y + 1, ob);
-            T.put(x, y + 1, ob);
+            T.put_new(x, y + 1, ob, mt);
             T.setvis(x, y + 1);
             for (int xx = -1; xx <= 1; xx++)
                 for (int yy = 0; yy <= 2; yy++) {
                     if (T.id(x + xx, y + yy) == c.id_lava) {
                         Cell o2 = create_tile(c, c.id_obsidian);
                         led_replace_at(T, c, x + xx, y + yy, o2);
-                        T.put(x + xx, y + yy, o2);
+                        T.put_new(x + xx, y + yy, o2, mt);
                         T.setvis(x + xx, y + yy);
                     }
                 }
@@ -781,7 +818,7 @@ __device__ __forceinline__ void rule_c(const TL &T, Ctx &c, int x, int y) {
         if (c.D() % 10 == 0) {
             Cell wt = create_tile(c, c.id_water);
             led_swap(c, t.id, 0, wt.id, (long long)wt.sc);
-            T.put(x, y, wt);
+            T.put_new(x, y, wt, c.mt);
         }
     }
 }
@@ -839,7 +876,9 @@ __device__ __forceinline__ int block_excl_scan(int v, int *scratch, int *total) 
 }
 
 // write the particles of one spawn event (world.cpp:1110-1119,1222,1298)
-__device__ __noinline__ void emit_spawns(const WorldDev &w, const SpawnEv &ev, uint32_t cp, uint32_t rank0, int base) {
+template <bool TEMP>
+static __device__ __noinline__ void emit_spawns(const WorldDev &w, const SpawnEv &ev, uint32_t cp, uint32_t rank0,
+                                                int base) {
     int32_t base_amt = 0, extra = 0;
     if (ev.kind == 2) {
         base_amt = ev.sc / ev.n;
@@ -858,6 +897,7 @@ __device__ __noinline__ void emit_spawns(const WorldDev &w, const SpawnEv &ev, u
         r.y = (float)ev.y;
         r.id = ev.id;
         r.colour = ev.col;
+        r.temp = (TEMP && ev.kind == 2) ? ev.tp : (int16_t)0;
         r.pad = 0;
         if (ev.kind == 1) {
             r.vx = ev.vx;
@@ -905,7 +945,7 @@ struct SmemHead {
 };
 
 // items: (world << 20) | chunk slot within the colour; iter, tk select the pass.
-template <int HALO>
+template <int HALO, bool TEMP>
 __global__ void __launch_bounds__(CP_THREADS, 1)
     k_colour_pass(const WorldDev *__restrict__ worlds, const uint32_t *__restrict__ items, int n_items, int iter, int tk,
                   const MatTable *__restrict__ mt) {
@@ -977,6 +1017,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
         Tl.ma = S.ma;
         Tl.md = S.md;
         Tl.df = w.df;
+        Tl.tp = w.tp;
         Tl.id_solid = id_solid;
         Tl.id_air = id_air;
         Tl.s_air = S.air;
@@ -1113,7 +1154,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                                 // staging slots are taken in any order; the (chunk-pass, rank)
                                 // key orders the particles later
                                 const int base = atomicAdd(w.stage_count, c.ev.n);
-                                emit_spawns(w, c.ev, cp, (uint32_t)(running + ex), base);
+                                emit_spawns<TEMP>(w, c.ev, cp, (uint32_t)(running + ex), base);
                             }
                             running += tot;
                         }
@@ -1159,9 +1200,9 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
         }
         };
         if (edge)
-            sweeps(Tile<true>(Tl));
+            sweeps(Tile<true, TEMP>(Tl));
         else
-            sweeps(Tile<false>(Tl));
+            sweeps(Tile<false, TEMP>(Tl));
 
         // ---- write back the cells this CTA changed (full-state rows inside the world),
         // one warp per row
@@ -1200,6 +1241,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
     FSE_PT_FLUSH
 }
 
+#ifndef FSE_TICK_TEMP_TU
 size_t colour_pass_smem(int C, int halo) {
     size_t RW = (size_t)C + 2 * halo, RHF = (size_t)C + 2 * halo, RHI = (size_t)C + halo + 10;
     size_t nid = RW * RHI, nfull = RW * RHF;
@@ -1207,32 +1249,47 @@ size_t colour_pass_smem(int C, int halo) {
     return head + nfull * 4 + nfull * 4 + ((nid + 1) & ~(size_t)1) * 2 + nfull;
 }
 
-template <int HALO>
+#endif
+
+template <int HALO, bool TEMP>
 static cudaError_t launch_t(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
                             const MatTable *mt, size_t sm, int grid, cudaStream_t s) {
     // opt in to the full shared-memory carve-out once per instantiation
     static size_t set = 0;
     if (set < sm) {
-        cudaFuncSetAttribute(k_colour_pass<HALO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(k_colour_pass<HALO, TEMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         set = sm;
     }
-    k_colour_pass<HALO><<<grid, CP_THREADS, sm, s>>>(worlds, items, n_items, iter, tk, mt);
+    k_colour_pass<HALO, TEMP><<<grid, CP_THREADS, sm, s>>>(worlds, items, n_items, iter, tk, mt);
     return cudaGetLastError();
 }
 
+#ifdef FSE_TICK_TEMP_TU
+cudaError_t launch_colour_pass_temp(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
+                                    const MatTable *mt, int halo, size_t sm, int grid, cudaStream_t s) {
+    if (halo == 5) return launch_t<5, true>(worlds, items, n_items, iter, tk, mt, sm, grid, s);
+    return launch_t<2, true>(worlds, items, n_items, iter, tk, mt, sm, grid, s);
+}
+#else
+cudaError_t launch_colour_pass_temp(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
+                                    const MatTable *mt, int halo, size_t sm, int grid, cudaStream_t s);
+
 cudaError_t launch_colour_pass(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
-                               const MatTable *mt, int halo, int C, int threads, int grid, cudaStream_t s) {
+                               const MatTable *mt, int halo, int C, int threads, int grid, cudaStream_t s,
+                               bool temp) {
     (void)threads;  // the colour pass always runs CP_THREADS threads (see above)
     size_t sm = colour_pass_smem(C, halo);
     if (n_items <= 0) return cudaSuccess;
     if (grid <= 0 || grid > n_items) grid = n_items;
-    if (halo == 5) return launch_t<5>(worlds, items, n_items, iter, tk, mt, sm, grid, s);
-    return launch_t<2>(worlds, items, n_items, iter, tk, mt, sm, grid, s);
+    if (temp) return launch_colour_pass_temp(worlds, items, n_items, iter, tk, mt, halo, sm, grid, s);
+    if (halo == 5) return launch_t<5, false>(worlds, items, n_items, iter, tk, mt, sm, grid, s);
+    return launch_t<2, false>(worlds, items, n_items, iter, tk, mt, sm, grid, s);
 }
+#endif
 
 }  // namespace fse
 
-#ifdef FSE_PHASE_CLOCKS
+#if defined(FSE_PHASE_CLOCKS) && !defined(FSE_TICK_TEMP_TU)
 extern "C" int fse_debug_phase_clocks(unsigned long long out[16], int reset) {
     cudaDeviceSynchronize();
     cudaMemcpyFromSymbol(out, g_phase_clk, 16 * sizeof(unsigned long long));

@@ -19,6 +19,7 @@
  *   fse_world_get_tile/set    world::getTile/setTile     source/engine/world.cpp:999-1008
  *   fse_object_stamp          rigid-body tile stamping   source/engine/game.cpp:1768-1814
  *   fse_object_readback       rigid-body tile readback   source/engine/game.cpp:1896-1983
+ *   fse_world_tick_temperature world::tickTemperature()  source/engine/world.cpp:1950-2004
  */
 #ifndef FSE_H
 #define FSE_H
@@ -78,8 +79,21 @@ typedef struct fse_config {
 /* the world keeps the render state of fse_world_render_*: a per-cell dirty plane
  * and the tick's per-cell flow sums (13 more bytes per cell, 20 with textures) */
 #define FSE_CFG_RENDER 1
+/* the world keeps MaterialInstance::temperature for liquids too (2 more bytes per
+ * cell, carried by every liquid move, flow, free fall and deposit, and by
+ * particles): needed by the fse_world_temperature_* calls and by
+ * fse_world_tick_temperature. Without it a world keeps only the temperatures its
+ * scalars hold (every non-liquid cell): liquid temperatures change no other
+ * result of a tick, the temperature calls return FSE_E_STATE and particles read
+ * temperature 0. */
+#define FSE_CFG_TEMPERATURE 2
+/* FSE_CFG_TEMPERATURE, and fse_world_tick/step (and batches and servers) run
+ * world::tickTemperature() after every tick whose index is 2 modulo GameTick (4),
+ * as game::tick does (game.cpp:2157-2159, const.h:38); the test runs on the
+ * device, so step graphs replay it correctly */
+#define FSE_CFG_TEMPERATURE_STEP 4
 
-/* One free particle (CellData, source/engine/game_utils/cells.h:15-36). 56 bytes. */
+/* One free particle (CellData, source/engine/game_utils/cells.h:15-36). 60 bytes. */
 typedef struct fse_particle {
     float x, y, vx, vy, ax, ay;
     float target_x, target_y, target_force;
@@ -89,6 +103,9 @@ typedef struct fse_particle {
     uint16_t id;    /* material of the carried tile */
     uint8_t flags;  /* tile flags: bit7 moved, bits0-5 settle count */
     uint8_t bits;   /* bit0 phase, bit1 temporary, bits2-3 inObjectState */
+    int16_t temperature; /* temperature of a SOUP tile (its scalar holds the amount) in worlds created
+                          with FSE_CFG_TEMPERATURE; 0 otherwise */
+    uint16_t reserved;
 } fse_particle;
 
 /* A rigid body stamped into the grid as OBJECT tiles. 48 bytes. */
@@ -123,6 +140,15 @@ int fse_material_set_reaction(int mat, int kind, int temperature, int result_mat
 int fse_material_set_interaction(int mat, int other, int kind, int data1_mat, int data2_radius, int ofs_x, int ofs_y);
 /* tile factory of a material: colour = base + ((lo + rand % mod) << shift) when mod > 0 */
 int fse_material_set_factory(int mat, uint32_t base, int shift, int lo, int mod, int32_t scalar);
+/* temperature of the tiles the factory makes of a SOUP material (whose scalar is
+ * the amount): WATER -1023, LAVA 1024 (game_datastruct.cpp:427-437); the scalar
+ * is the temperature of every other material */
+int fse_material_set_factory_temperature(int mat, int32_t temperature);
+/* Material::addTemp, conductionSelf, conductionOther (game_datastruct.hpp:142-144,
+ * set in InitMaterials, game_datastruct.cpp:124-141) */
+int fse_material_set_conduction(int mat, uint32_t add_temp, float conduction_self, float conduction_other);
+/* out: addTemp, conductionSelf bits, conductionOther bits, factory temperature */
+int fse_material_get_conduction(int mat, uint32_t out[4]);
 /* Execute the materials_register(...) calls of a Lua script text (the subset of
  * Lua used by data/scripts: literal arguments and integer/float expressions).
  * *out_count = number of materials registered. */
@@ -149,6 +175,18 @@ int fse_world_set_tick(fse_world *world, uint32_t tick);
 int fse_world_get_tile(fse_world *world, int x, int y, uint16_t *id, uint32_t *colour, int32_t *scalar,
                        uint8_t *flags);
 int fse_world_set_tile(fse_world *world, int x, int y, uint16_t id, uint32_t colour, int32_t scalar, uint8_t flags);
+
+/* Temperatures of all cells (int16, MaterialInstance::temperature) of a world
+ * created with FSE_CFG_TEMPERATURE (else FSE_E_STATE): SOUP cells keep theirs
+ * beside the amount, every other cell in its scalar. Upload and set_tile leave
+ * SOUP temperatures as they were; the generators give new SOUP tiles their
+ * factory temperature. */
+int fse_world_temperature_read(fse_world *world, int16_t *out);
+int fse_world_temperature_write(fse_world *world, const int16_t *temps);
+/* world::tickTemperature() (world.cpp:1950-2004): one Jacobi step of the 3x3
+ * conduction stencil over every cell; a neighbour outside the world counts as
+ * temperature 0. Enqueued on the world's stream. */
+int fse_world_tick_temperature(fse_world *world);
 
 /* world::tick(), n times (no particle step in between) */
 int fse_world_tick(fse_world *world, int n_ticks);
@@ -253,7 +291,9 @@ int fse_world_islands(fse_world *world, int max_cells, int remove, fse_island *o
  * particles this tick spawns, in the order fse_world_tick would append them;
  * *out_n_spawned = their number (FSE_E_CAPACITY when more than spawn_cap).
  * tick: the world's tick count (keys the counter RNG; the caller advances it).
- * Results equal fse_world_tick's bit for bit.
+ * Results equal fse_world_tick's bit for bit, except that no temperature plane is
+ * passed: liquid temperatures are not carried, and SOUP particles are spawned
+ * with temperature 0.
  *
  * Scratch: one fixed device array of about 4 MB inside the library, held by every
  * GPU that loads it until the process exits. Limits: at most 4096 chunks per
