@@ -845,6 +845,8 @@ def main():
     ap.add_argument("--impl", default="fse", choices=["fse", "reference"])
     ap.add_argument("--workload", type=int, default=1, choices=[0, 1, 2, 3, 4])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--only", default=None, choices=["render", "temperature"],
+                    help="run only one side measurement of the 4096x2048 workload (for profiling), print its dict")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.steps is None:
@@ -865,6 +867,14 @@ def main():
 
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    if args.only:
+        import falling_sand_engine_gb300 as fse
+
+        fse.InitMaterials()
+        fse.PushMaterials()
+        fn = {"render": render_config1, "temperature": temperature_config1}[args.only]
+        print(json.dumps(fn(fse, torch, 4096, 2048, 1234, 1_000_000)))
+        return
     run = {0: bench_config0, 1: bench_config1, 2: bench_config2, 3: bench_config3, 4: bench_config4}[args.workload]
     out = run(args, rank, local_rank, world_size)
     if rank == 0 and out is not None:

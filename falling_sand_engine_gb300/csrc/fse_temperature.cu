@@ -18,14 +18,17 @@
 // amount), all other cells in the scalar. A neighbour outside the world reads
 // Tiles_TEST_SOLID, temperature 0, so it adds nothing.
 //
-// Kernels. The world is cut into 128 x 32 tiles, one 256-thread CTA each. A CTA
-// stages its tile plus a one-cell ring in shared memory as per-cell (v term,
-// n term) pairs, computes its 4096 results with a 3 x 3 register window that
-// slides down each column, and writes changed temperatures in place, except on
-// the tile's own edge ring: those cells are what the neighbouring tiles read as
-// their halo, so their results go to a side array and k_temp_commit stores them
-// after every tile has read its halo. HBM traffic: id 2 B + scalar 4 B + tp 2 B
-// read per cell, plus 4 B (scalar) or 2 B (tp) per changed cell written.
+// Kernels. The world is cut into 128 x 32 tiles; persistent 256-thread CTAs take
+// them in turn. A CTA stages its tile plus a one-cell ring in shared memory as
+// per-cell (v term, n term) pairs -- each thread loads one column, 17 rows, with
+// 32-bit cell offsets, and keeps its own 16 cells in registers -- then computes
+// its 16 results with a 3 x 3 register window sliding down the column and writes
+// changed temperatures in place, except on the tile's own edge ring: those cells
+// are what the neighbouring tiles read as their halo, so their results go to a
+// side array and k_temp_commit stores them after every tile has read its halo.
+// HBM traffic: id 2 B + scalar 4 B + tp 2 B read per cell, plus 4 B (scalar) or
+// 2 B (tp) per changed cell written. Worlds have fewer than 2^31 cells
+// (fse_world_create), so 32-bit offsets address every cell.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -43,10 +46,9 @@ constexpr int TT_ROWS_PER_THREAD = TT_X * TT_Y / TT_THREADS;  // 16 consecutive 
 constexpr uint32_t TC_CHANGED = 0x10000u, TC_SOUP = 0x20000u;
 
 struct TempSmem {
-    float pv[TT_RY * TT_RX];  // (float)t * factor of each staged cell (0 where t == 0)
-    float pn[TT_RY * TT_RX];  // factor (0 where t == 0)
-    int16_t t[TT_Y * TT_X];   // the tile's own temperatures
-    uint16_t id[TT_Y * TT_X];  // material | 0x8000 where a scalar holds a value outside int16 (always stored)
+    // per staged cell: x = (float)t * factor (the v term), y = factor (the n term);
+    // both 0 where t == 0
+    float2 pvn[TT_RY * TT_RX];
     float cs[MAXMAT], co[MAXMAT];
     uint32_t add[MAXMAT];
     uint8_t soup[MAXMAT];
@@ -77,12 +79,15 @@ __device__ __forceinline__ void ring_pos(int e, int &lx, int &ly) {
         ly = e - (2 * TT_X + TT_Y - 2) + 1;
     }
 }
-__device__ __forceinline__ int ring_index(int lx, int ly) {
-    if (ly == 0) return lx;
-    if (ly == TT_Y - 1) return TT_X + lx;
-    if (lx == 0) return 2 * TT_X + ly - 1;
-    if (lx == TT_X - 1) return 2 * TT_X + (TT_Y - 2) + ly - 1;
-    return -1;
+// (v, n) + (p, f) as one paired instruction: add.rn.f32x2 rounds each lane to
+// nearest like add.rn.f32, so the two sums are exactly the two scalar chains
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "add.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
 }
 
 // x86-64 cvttss2si: truncation toward zero; NaN and values outside the int32
@@ -91,8 +96,24 @@ __device__ __forceinline__ int32_t f2i_x86(float r) {
     return (r >= -2147483648.0f && r < 2147483648.0f) ? __float2int_rz(r) : (int32_t)0x80000000;
 }
 
-__global__ void __launch_bounds__(TT_THREADS) k_temp_tiles(const WorldDev *__restrict__ worlds,
-                                                          const MatTable *__restrict__ mt, int gated) {
+// (v term, n term) of one staged cell: world.cpp:1970-1974 for a neighbour with
+// temperature t (0 where t == 0, which adds nothing)
+__device__ __forceinline__ void temp_terms(int t, float co, float &pv, float &pn) {
+    pv = 0.0f;
+    pn = 0.0f;
+    if (t != 0) {
+        const int at = t < 0 ? -t : t;  // |t| <= 32768: abs(t) / 64 is a shift
+        pn = __fmul_rn((float)(at >> 6), co);
+        pv = __fmul_rn((float)t, pn);
+    }
+}
+
+// Thread (lx = tid % 128, g = tid / 128) stages column lx + 1 of staged rows
+// 17g .. 17g + 16 (the region is 34 rows x 130 columns: the tile and its ring),
+// keeping its own cells (staged rows 1 .. 16 for g = 0, 17 .. 32 for g = 1) in
+// registers, then computes output rows 16g .. 16g + 15 of column lx.
+__global__ void __launch_bounds__(TT_THREADS, 4) k_temp_tiles(const WorldDev *__restrict__ worlds,
+                                                             const MatTable *__restrict__ mt, int gated) {
     extern __shared__ __align__(16) unsigned char tsm_raw[];
     TempSmem &S = *reinterpret_cast<TempSmem *>(tsm_raw);
     const WorldDev &w = worlds[blockIdx.y];
@@ -109,74 +130,86 @@ __global__ void __launch_bounds__(TT_THREADS) k_temp_tiles(const WorldDev *__res
     const uint16_t *__restrict__ gid = w.id;
     const int32_t *__restrict__ gsc = w.sc;
     const int16_t *__restrict__ gtp = w.tp;
+    const int lx = tid % TT_X, g = tid / TT_X;
+    const bool col_ring = lx == 0 || lx == TT_X - 1;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int x0 = (tile % ntx) * TT_X, y0 = (tile / ntx) * TT_Y;
+        const int gx = x0 + lx;
+        const bool xin = gx < W;
         __syncthreads();  // the previous tile's readers are done; material params are in place
-        // stage the region [x0 - 1, x0 + TT_X] x [y0 - 1, y0 + TT_Y]
-#pragma unroll 6
-        for (int r = tid; r < TT_RY * TT_RX; r += TT_THREADS) {
-            const int ry = r / TT_RX, rx = r - ry * TT_RX;
-            const int gx = x0 - 1 + rx, gy = y0 - 1 + ry;
-            int t = 0, id = 0, wide = 0;
-            if ((unsigned)gx < (unsigned)W && (unsigned)gy < (unsigned)H) {
-                const size_t g = (size_t)gy * W + gx;
-                id = gid[g] & (MAXMAT - 1);  // ids are checked on upload; the mask keeps tables in bounds
-                const int32_t sc = gsc[g];
-                const int16_t tp = gtp ? gtp[g] : (int16_t)0;
-                const bool soup = S.soup[id] != 0;
-                t = soup ? (int)tp : (int)(int16_t)sc;
-                wide = !soup && sc != (int32_t)(int16_t)sc;
+        // own cells: t (low 16 bits) | material << 16 | 1 << 31 where the scalar is wider than int16
+        uint32_t own[TT_ROWS_PER_THREAD];
+        // ---- stage column lx + 1, rows 17g .. 17g + 16
+        {
+            const int ry0 = 17 * g;
+            int gy = y0 - 1 + ry0;
+            uint32_t o = (uint32_t)gy * (uint32_t)W + (uint32_t)gx;  // wraps for gy = -1: used only in the world
+#pragma unroll
+            for (int i = 0; i < 17; i++, gy++, o += (uint32_t)W) {
+                int t = 0, id = 0;
+                uint32_t wide = 0;
+                if (xin && (unsigned)gy < (unsigned)H) {
+                    id = gid[o] & (MAXMAT - 1);  // ids are checked on upload; the mask keeps tables in bounds
+                    const int32_t sc = gsc[o];
+                    const int16_t tp = gtp ? gtp[o] : (int16_t)0;
+                    const bool soup = S.soup[id] != 0;
+                    t = soup ? (int)tp : (int)(int16_t)sc;
+                    wide = (!soup && sc != (int32_t)(int16_t)sc) ? 0x80000000u : 0u;
+                }
+                float pv, pn;
+                temp_terms(t, S.co[id], pv, pn);
+                S.pvn[(ry0 + i) * TT_RX + lx + 1] = make_float2(pv, pn);
+                // own rows: staged 1 .. 16 (g = 0: i = 1 .. 16; g = 1: i = 0 .. 15); g is
+                // warp-uniform and both branches index `own` with constants
+                const uint32_t packed = (uint32_t)(uint16_t)t | ((uint32_t)id << 16) | wide;
+                if (g == 0) {
+                    if (i >= 1) own[i - 1] = packed;
+                } else {
+                    if (i < TT_ROWS_PER_THREAD) own[i] = packed;
+                }
             }
-            float pv = 0.0f, pn = 0.0f;
-            if (t != 0) {  // world.cpp:1970-1974
-                const int at = t < 0 ? -t : t;
-                pn = __fmul_rn((float)(at / 64), S.co[id]);
-                pv = __fmul_rn((float)t, pn);
+        }
+        // ---- the ring columns 0 and 129 of the region (34 rows each)
+        if (tid < 2 * TT_RY) {
+            const int side = tid / TT_RY, ry = tid % TT_RY;
+            const int hx = side ? x0 + TT_X : x0 - 1, hy = y0 - 1 + ry;
+            int t = 0, id = 0;
+            if ((unsigned)hx < (unsigned)W && (unsigned)hy < (unsigned)H) {
+                const uint32_t o = (uint32_t)hy * (uint32_t)W + (uint32_t)hx;
+                id = gid[o] & (MAXMAT - 1);
+                t = S.soup[id] ? (int)(gtp ? gtp[o] : (int16_t)0) : (int)(int16_t)gsc[o];
             }
-            S.pv[r] = pv;
-            S.pn[r] = pn;
-            if (ry >= 1 && ry <= TT_Y && rx >= 1 && rx <= TT_X) {
-                const int o = (ry - 1) * TT_X + (rx - 1);
-                S.t[o] = (int16_t)t;
-                S.id[o] = (uint16_t)(id | (wide << 15));
-            }
+            float pv, pn;
+            temp_terms(t, S.co[id], pv, pn);
+            S.pvn[ry * TT_RX + (side ? TT_RX - 1 : 0)] = make_float2(pv, pn);
         }
         __syncthreads();
-        // each thread: column lx, TT_ROWS_PER_THREAD consecutive rows from ly0
-        const int lx = tid % TT_X, ly0 = (tid / TT_X) * TT_ROWS_PER_THREAD;
-        const int gx = x0 + lx;
-        // window columns lx .. lx + 2 of the staged region (xa = -1, 0, 1), rows k .. k + 2
-        float v0[3], v1[3], v2[3], n0[3], n1[3], n2[3];
+        // ---- outputs: column lx, rows ly0 .. ly0 + 15, window = staged columns lx .. lx + 2
+        const int ly0 = g * TT_ROWS_PER_THREAD;
+        float2 q0[3], q1[3], q2[3];
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            v0[c] = S.pv[ly0 * TT_RX + lx + c];
-            n0[c] = S.pn[ly0 * TT_RX + lx + c];
-            v1[c] = S.pv[(ly0 + 1) * TT_RX + lx + c];
-            n1[c] = S.pn[(ly0 + 1) * TT_RX + lx + c];
+            q0[c] = S.pvn[ly0 * TT_RX + lx + c];
+            q1[c] = S.pvn[(ly0 + 1) * TT_RX + lx + c];
         }
-#pragma unroll 4
-        for (int k = 0; k < TT_ROWS_PER_THREAD; k++) {
+        uint32_t o = (uint32_t)(y0 + ly0) * (uint32_t)W + (uint32_t)gx;
+#pragma unroll
+        for (int k = 0; k < TT_ROWS_PER_THREAD; k++, o += (uint32_t)W) {
             const int ly = ly0 + k;
 #pragma unroll
-            for (int c = 0; c < 3; c++) {
-                v2[c] = S.pv[(ly + 2) * TT_RX + lx + c];
-                n2[c] = S.pn[(ly + 2) * TT_RX + lx + c];
-            }
-            const int gy = y0 + ly;
-            if (gx < W && gy < H) {
-                float v = 0.0f, n = 0.01f;  // f32 v = 0; f32 n = 0.01;
+            for (int c = 0; c < 3; c++) q2[c] = S.pvn[(ly + 2) * TT_RX + lx + c];
+            if (xin && y0 + ly < H) {
+                float2 vn = make_float2(0.0f, 0.01f);  // f32 v = 0; f32 n = 0.01;
 #pragma unroll
                 for (int c = 0; c < 3; c++) {  // FN(xa, -1), FN(xa, 0), FN(xa, 1)
-                    v = __fadd_rn(v, v0[c]);
-                    n = __fadd_rn(n, n0[c]);
-                    v = __fadd_rn(v, v1[c]);
-                    n = __fadd_rn(n, n1[c]);
-                    v = __fadd_rn(v, v2[c]);
-                    n = __fadd_rn(n, n2[c]);
+                    vn = add2(vn, q0[c]);
+                    vn = add2(vn, q1[c]);
+                    vn = add2(vn, q2[c]);
                 }
-                const int o = ly * TT_X + lx;
-                const int t0 = S.t[o];
-                const int idw = S.id[o], id = idw & 0x7FFF;
+                const float v = vn.x, n = vn.y;
+                const uint32_t me = own[k];
+                const int t0 = (int)(int16_t)(me & 0xFFFFu);
+                const int id = (int)((me >> 16) & (MAXMAT - 1));
                 const uint32_t add = S.add[id];
                 int32_t r;
                 if (v != 0.0f) {  // world.cpp:1988-1990
@@ -188,26 +221,26 @@ __global__ void __launch_bounds__(TT_THREADS) k_temp_tiles(const WorldDev *__res
                 }
                 const int16_t nt = (int16_t)(uint16_t)(uint32_t)r;
                 const bool soup = S.soup[id] != 0;
-                const bool changed = nt != t0 || (idw >> 15);
-                const int e = ring_index(lx, ly);
-                const size_t g = (size_t)gy * W + gx;
-                if (e >= 0) {
+                const bool changed = nt != t0 || (me >> 31);
+                // tile-edge cells are read by the neighbouring tiles: deferred
+                const bool row_ring = (g == 0 && k == 0) || (g == 1 && k == TT_ROWS_PER_THREAD - 1);
+                if (row_ring || col_ring) {
+                    const int e = row_ring ? (ly == 0 ? lx : TT_X + lx)
+                                           : (lx == 0 ? 2 * TT_X + ly - 1 : 2 * TT_X + (TT_Y - 2) + ly - 1);
                     w.tnew[(size_t)tile * TT_RING + e] =
                         (int32_t)((changed ? TC_CHANGED : 0u) | (soup ? TC_SOUP : 0u) | (uint32_t)(uint16_t)nt);
                 } else if (changed) {
                     if (soup) {
-                        if (w.tp) w.tp[g] = nt;
+                        if (gtp) w.tp[o] = nt;
                     } else {
-                        w.sc[g] = nt;
+                        w.sc[o] = nt;
                     }
                 }
             }
 #pragma unroll
             for (int c = 0; c < 3; c++) {
-                v0[c] = v1[c];
-                n0[c] = n1[c];
-                v1[c] = v2[c];
-                n1[c] = n2[c];
+                q0[c] = q1[c];
+                q1[c] = q2[c];
             }
         }
     }

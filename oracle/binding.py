@@ -11,6 +11,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libfse_oracle.so")
 REF_TEMPERATURE_PATH = os.path.join(HERE, "_ref", "libref_temperature.so")
+REF_LZ4_PATH = os.path.join(HERE, "_ref", "liblz4ref.so")
 REFERENCE_WORLD_CPP = "/root/reference/source/engine/world.cpp"
 
 PARTICLE_DTYPE = np.dtype(
@@ -108,6 +109,11 @@ class Oracle:
                 "om_world_set_temperature": (None, [vp, i32]),
                 "om_temperature_get": (None, [vp, vp]),
                 "om_temperature_set": (None, [vp, vp]),
+                "om_lz4_bound": (i32, [i32]),
+                "om_lz4_encode": (i32, [vp, i32, vp, i32]),
+                "om_lz4_decode": (i32, [vp, i32, vp, i32]),
+                "om_world_pack": (i32, [vp, i32, vp, C.c_int64, vp]),
+                "om_world_unpack": (i32, [vp, vp, vp, i32, vp]),
             }
             for name, (res, args) in sig.items():
                 f = getattr(lib, name)
@@ -264,6 +270,25 @@ class OracleWorld:
         self.lib.om_object_mask(self.h_, _ptr(out))
         return out
 
+    # -- chunk .pack codec
+    def pack(self, phase=0):
+        """All chunks row-major in the reference's .pack layout: (bytes, offsets)."""
+        n = ((self.w + 127) // 128) * ((self.h + 127) // 128)
+        cap = n * (17 + 2 * (393216 + 393216 // 255 + 16)) + 16
+        out = np.zeros(cap, np.uint8)
+        offs = np.zeros(n + 1, np.int64)
+        rc = self.lib.om_world_pack(self.h_, phase, _ptr(out), cap, _ptr(offs))
+        if rc < 0:
+            raise ValueError("pack failed")
+        return out[: offs[-1]].copy(), offs
+
+    def unpack(self, data, offsets):
+        data = np.ascontiguousarray(data, np.uint8)
+        offsets = np.ascontiguousarray(offsets, np.int64)
+        phases = np.zeros(len(offsets) - 1, np.int8)
+        rc = self.lib.om_world_unpack(self.h_, _ptr(data), _ptr(offsets), len(offsets) - 1, _ptr(phases))
+        return rc, phases
+
     # -- temperature
     def temperature(self):
         out = np.zeros(self.w * self.h, np.int16)
@@ -350,3 +375,62 @@ def reference_tick_temperature(lib_path, mat, temp, add_temp, cond_self, cond_ot
     if rc != 0:
         raise ValueError("ref_tick_temperature failed")
     return t
+
+
+def lz4_encode(buf):
+    """The oracle's LZ4 block encoder (16 fixed match distances, greedy)."""
+    o = Oracle()
+    buf = np.ascontiguousarray(buf, np.uint8)
+    cap = o.lib.om_lz4_bound(len(buf))
+    dst = np.zeros(cap, np.uint8)
+    m = o.lib.om_lz4_encode(_ptr(buf), len(buf), _ptr(dst), cap)
+    if m < 0:
+        raise ValueError("encode failed")
+    return dst[:m].copy()
+
+
+def lz4_decode(src, cap):
+    """The oracle's LZ4 block decoder: (decoded bytes, status = size or negative)."""
+    o = Oracle()
+    src = np.ascontiguousarray(src, np.uint8)
+    dst = np.zeros(max(cap, 1), np.uint8)
+    m = o.lib.om_lz4_decode(_ptr(src), len(src), _ptr(dst), cap)
+    return dst[: max(m, 0)].copy(), m
+
+
+def build_reference_lz4(force=False):
+    """Compile the reference's vendored LZ4 (oracle/Makefile `ref`); None without the reference tree."""
+    if not os.path.exists(REFERENCE_WORLD_CPP):
+        return None
+    if force or not os.path.exists(REF_LZ4_PATH):
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    return REF_LZ4_PATH
+
+
+class ReferenceLZ4:
+    """LZ4_compress_fast / LZ4_decompress_safe of the reference's vendored LZ4 1.9.4."""
+
+    def __init__(self, path):
+        lib = C.CDLL(path)
+        lib.LZ4_compress_fast.restype = C.c_int
+        lib.LZ4_compress_fast.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int]
+        lib.LZ4_decompress_safe.restype = C.c_int
+        lib.LZ4_decompress_safe.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
+        lib.LZ4_compressBound.restype = C.c_int
+        lib.LZ4_compressBound.argtypes = [C.c_int]
+        self.lib = lib
+
+    def compress(self, data, acceleration=10):
+        data = np.ascontiguousarray(data, np.uint8)
+        cap = self.lib.LZ4_compressBound(len(data))
+        dst = np.zeros(cap, np.uint8)
+        m = self.lib.LZ4_compress_fast(_ptr(data), _ptr(dst), len(data), cap, acceleration)
+        if m <= 0:
+            raise ValueError("LZ4_compress_fast failed")
+        return dst[:m].copy()
+
+    def decompress(self, src, size):
+        src = np.ascontiguousarray(src, np.uint8)
+        dst = np.zeros(max(size, 1), np.uint8)
+        m = self.lib.LZ4_decompress_safe(_ptr(src), _ptr(dst), len(src), size)
+        return dst[: max(m, 0)].copy(), m

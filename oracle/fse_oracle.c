@@ -1697,6 +1697,264 @@ void om_tick_temperature(om_world *w) {
     free(old);
 }
 
+/* ------------------------------------------------------------ chunk .pack */
+/* Chunk::ChunkWrite / ChunkRead (source/engine/chunk.cpp:219-330, 68-200) with the
+ * record MaterialInstanceData {u32 index; u32 color; i16 temperature} (12 bytes
+ * with 2 of padding, chunk.hpp:26-30): per 128 x 128 chunk, the i8 generation
+ * phase, then src_size (int, 128*128*2*12), the LZ4 block size of the tile and
+ * layer2 records, src_size2 (int, 128*128*4) and the LZ4 block size of the
+ * background, then the two LZ4 blocks. This world has no second layer and no
+ * background: layer2 records and background words are written as zeros
+ * (GENERIC_AIR, colour 0, temperature 0) and skipped on reading.
+ *
+ * LZ4 block format (the vendored LZ4 1.9.4, source/libs/lz4, as its documented
+ * block format): sequences of token (literal length << 4 | match length - 4),
+ * optional 255-run length bytes, literals, a 16-bit little-endian offset,
+ * optional match length bytes; the last sequence holds literals only, and the
+ * last match starts at least 12 bytes before the end of the block.
+ *
+ * The encoder here is this project's own (the GPU kernels compute the same parse
+ * with a warp per chunk): instead of a hash table of earlier positions it tries
+ * 16 fixed distances matched to the 12-byte record and the 128-cell chunk row,
+ * which on generated worlds gives smaller blocks than LZ4_compress_fast with the
+ * acceleration 10 Chunk::ChunkWrite uses. Any LZ4 block decoder reads them. */
+#define PK_EDGE 128
+#define PK_CELLS (PK_EDGE * PK_EDGE)
+#define PK_SRC1 (PK_CELLS * 2 * 12)
+#define PK_SRC2 (PK_CELLS * 4)
+#define PK_HEADER 17
+
+int om_lz4_bound(int n) { return n + n / 255 + 16; }
+
+static int pk_put_len(uint8_t *dst, int op, int cap, int v) { /* v >= 15 already taken out of the nibble */
+    while (v >= 255) {
+        if (op >= cap) return -1;
+        dst[op++] = 255;
+        v -= 255;
+    }
+    if (op >= cap) return -1;
+    dst[op++] = (uint8_t)v;
+    return op;
+}
+
+/* one sequence: literal records [ls, ls + nl) and, when ml > 0, a match of ml
+ * bytes at distance off bytes */
+static int pk_emit(uint8_t *dst, int op, int cap, const uint8_t *rec, int R, int ls, int nl, int off, int ml) {
+    const int lb = nl * R;
+    const int mcode = ml > 0 ? ml - 4 : 0;
+    if (op >= cap) return -1;
+    dst[op++] = (uint8_t)(((lb < 15 ? lb : 15) << 4) | (ml > 0 ? (mcode < 15 ? mcode : 15) : 0));
+    if (lb >= 15 && (op = pk_put_len(dst, op, cap, lb - 15)) < 0) return -1;
+    if (lb > cap - op) return -1;
+    memcpy(dst + op, rec + (size_t)ls * R, (size_t)lb);
+    op += lb;
+    if (ml > 0) {
+        if (cap - op < 2) return -1;
+        dst[op++] = (uint8_t)(off & 255);
+        dst[op++] = (uint8_t)(off >> 8);
+        if (mcode >= 15 && (op = pk_put_len(dst, op, cap, mcode - 15)) < 0) return -1;
+    }
+    return op;
+}
+
+/* The candidate distances of the encoder, ascending (a tie goes to the nearer):
+ * small multiples of 4 and of the 12-byte record, and the cells one chunk row
+ * (128 records = 1536 bytes) and two rows above, with their diagonal neighbours. */
+static const int PK_DIST[16] = {4, 8, 12, 16, 20, 24, 36, 48, 60, 72, 84, 96, 1524, 1536, 1548, 3072};
+
+/* LZ4 block of buf[0, n): greedy from the first byte -- at position p, the
+ * longest run buf[p + i] == buf[p + i - d] over the candidate distances d <= p
+ * (ties to the smaller d) is taken as a match when it is at least 4 bytes long,
+ * else p is a literal. A match starts at most n - 12 and ends at most n - 5 (the
+ * block format's end conditions). Returns the block size, or -1 when cap is too
+ * small. */
+int om_lz4_encode(const uint8_t *buf, int n, uint8_t *dst, int cap) {
+    const int mflimit = n - 12, mend = n - 5;
+    int p = 0, anchor = 0, op = 0;
+    while (p <= mflimit) {
+        int best = 0, bd = 0;
+        for (int k = 0; k < 16 && PK_DIST[k] <= p; k++) {
+            const int d = PK_DIST[k];
+            if (memcmp(buf + p, buf + p - d, 4) != 0) continue;
+            int L = 4;
+            while (p + L < mend && buf[p + L] == buf[p + L - d]) L++;
+            if (L > best) {
+                best = L;
+                bd = d;
+            }
+        }
+        if (best >= 4) {
+            op = pk_emit(dst, op, cap, buf, 1, anchor, p - anchor, bd, best);
+            if (op < 0) return -1;
+            p += best;
+            anchor = p;
+        } else {
+            p++;
+        }
+    }
+    return pk_emit(dst, op, cap, buf, 1, anchor, n - anchor, 0, 0);
+}
+
+/* LZ4 block decoder; returns the decoded size, or a negative value for a block
+ * that reads or writes out of bounds or refers before the start */
+int om_lz4_decode(const uint8_t *src, int n, uint8_t *dst, int cap) {
+    int ip = 0, op = 0;
+    for (;;) {
+        if (ip >= n) return -1;
+        const int token = src[ip++];
+        int ll = token >> 4;
+        if (ll == 15) {
+            int b;
+            do {
+                if (ip >= n) return -2;
+                b = src[ip++];
+                ll += b;
+                if (ll > cap) return -3;
+            } while (b == 255);
+        }
+        if (ll > n - ip || ll > cap - op) return -3;
+        memcpy(dst + op, src + ip, (size_t)ll);
+        ip += ll;
+        op += ll;
+        if (ip == n) return op; /* the last sequence: literals only */
+        if (n - ip < 2) return -4;
+        const int off = src[ip] | (src[ip + 1] << 8);
+        ip += 2;
+        if (off == 0 || off > op) return -5;
+        int ml = token & 15;
+        if (ml == 15) {
+            int b;
+            do {
+                if (ip >= n) return -6;
+                b = src[ip++];
+                ml += b;
+                if (ml > cap) return -7;
+            } while (b == 255);
+        }
+        ml += 4;
+        if (ml > cap - op) return -7;
+        for (int k = 0; k < ml; k++) dst[op + k] = dst[op - off + k]; /* overlapping copies repeat the pattern */
+        op += ml;
+    }
+}
+
+/* the MaterialInstanceData buffer of chunk (cx, cy): tile records, then the
+ * (zero) second layer; cells outside the world are GENERIC_AIR records */
+static void pk_records(const om_world *w, int cx, int cy, uint8_t *rec) {
+    memset(rec, 0, PK_SRC1);
+    for (int j = 0; j < PK_CELLS; j++) {
+        int x = cx * PK_EDGE + (j % PK_EDGE), y = cy * PK_EDGE + (j / PK_EDGE);
+        if (x >= w->W || y >= w->H) continue;
+        size_t i = (size_t)y * w->W + x;
+        uint32_t id = w->id[i], col = w->col[i];
+        int16_t t = temp_at(w, i);
+        uint8_t *r = rec + (size_t)j * 12;
+        memcpy(r, &id, 4);
+        memcpy(r + 4, &col, 4);
+        memcpy(r + 8, &t, 2);
+    }
+}
+
+/* every chunk of the world, row-major, into out (offsets[k] = start of chunk k,
+ * offsets[n] = total); returns the chunk count or -1 when cap is too small */
+int om_world_pack(const om_world *w, int phase, uint8_t *out, int64_t cap, int64_t *offsets) {
+    const int ncx = (w->W + PK_EDGE - 1) / PK_EDGE, ncy = (w->H + PK_EDGE - 1) / PK_EDGE;
+    uint8_t *rec = (uint8_t *)malloc(PK_SRC1);
+    uint8_t *bg = (uint8_t *)calloc(PK_SRC2, 1);
+    uint8_t *c1 = (uint8_t *)malloc((size_t)om_lz4_bound(PK_SRC1));
+    uint8_t *c2 = (uint8_t *)malloc((size_t)om_lz4_bound(PK_SRC2));
+    int64_t op = 0;
+    int rc = ncx * ncy;
+    const int n2 = om_lz4_encode(bg, PK_SRC2, c2, om_lz4_bound(PK_SRC2));
+    for (int k = 0; k < ncx * ncy && rc >= 0; k++) {
+        pk_records(w, k % ncx, k / ncx, rec);
+        const int n1 = om_lz4_encode(rec, PK_SRC1, c1, om_lz4_bound(PK_SRC1));
+        offsets[k] = op;
+        if (n1 < 0 || n2 < 0 || op + PK_HEADER + n1 + n2 > cap) {
+            rc = -1;
+            break;
+        }
+        const int8_t ph = (int8_t)phase;
+        const int32_t hd[4] = {PK_SRC1, n1, PK_SRC2, n2};
+        memcpy(out + op, &ph, 1);
+        memcpy(out + op + 1, hd, 16);
+        memcpy(out + op + PK_HEADER, c1, (size_t)n1);
+        memcpy(out + op + PK_HEADER + n1, c2, (size_t)n2);
+        op += PK_HEADER + n1 + n2;
+    }
+    if (rc >= 0) offsets[ncx * ncy] = op;
+    free(rec);
+    free(bg);
+    free(c1);
+    free(c2);
+    return rc;
+}
+
+/* ChunkRead for every chunk: tiles take the records' material, colour and
+ * temperature (a SOUP tile's amount is the MaterialInstance default 2.0,
+ * game_datastruct.hpp:216); flags and pending diffs are cleared. phases[k] gets
+ * each chunk's generation phase. Returns 0, or -1 - k for the first chunk k that
+ * is malformed (bad header, sizes or block, or a material index out of range),
+ * in which case no chunk from k on has been written. */
+int om_world_unpack(om_world *w, const uint8_t *in, const int64_t *offsets, int n_chunks, int8_t *phases) {
+    const int ncx = (w->W + PK_EDGE - 1) / PK_EDGE, ncy = (w->H + PK_EDGE - 1) / PK_EDGE;
+    if (n_chunks != ncx * ncy) return -1;
+    uint8_t *rec = (uint8_t *)malloc(PK_SRC1);
+    uint8_t *bg = (uint8_t *)malloc(PK_SRC2);
+    int rc = 0;
+    for (int k = 0; k < n_chunks && rc == 0; k++) {
+        const int64_t len = offsets[k + 1] - offsets[k];
+        const uint8_t *p = in + offsets[k];
+        int32_t hd[4];
+        if (len < PK_HEADER) {
+            rc = -1 - k;
+            break;
+        }
+        memcpy(hd, p + 1, 16);
+        if (hd[0] != PK_SRC1 || hd[2] != PK_SRC2 || hd[1] < 0 || hd[3] < 0 ||
+            (int64_t)PK_HEADER + hd[1] + hd[3] > len ||
+            om_lz4_decode(p + PK_HEADER, hd[1], rec, PK_SRC1) != PK_SRC1 ||
+            om_lz4_decode(p + PK_HEADER + hd[1], hd[3], bg, PK_SRC2) != PK_SRC2) {
+            rc = -1 - k;
+            break;
+        }
+        for (int j = 0; j < PK_CELLS; j++) {
+            uint32_t id;
+            memcpy(&id, rec + (size_t)j * 12, 4);
+            if (id >= (uint32_t)NMAT) rc = -1 - k;
+        }
+        if (rc) break;
+        if (phases) phases[k] = (int8_t)p[0];
+        const int cx = k % ncx, cy = k / ncx;
+        for (int j = 0; j < PK_CELLS; j++) {
+            int x = cx * PK_EDGE + (j % PK_EDGE), y = cy * PK_EDGE + (j / PK_EDGE);
+            if (x >= w->W || y >= w->H) continue;
+            size_t i = (size_t)y * w->W + x;
+            const uint8_t *r = rec + (size_t)j * 12;
+            uint32_t id, col;
+            int16_t t;
+            memcpy(&id, r, 4);
+            memcpy(&col, r + 4, 4);
+            memcpy(&t, r + 8, 2);
+            w->id[i] = (uint16_t)id;
+            w->col[i] = col;
+            w->fl[i] = 0;
+            w->df[i] = 0;
+            if (M[id].type == T_SOUP) {
+                w->sc[i] = Q_DEFAULT;
+                w->tp[i] = t;
+            } else {
+                w->sc[i] = t;
+                w->tp[i] = 0;
+            }
+            mark_dirty(w, i);
+        }
+    }
+    free(rec);
+    free(bg);
+    return rc;
+}
+
 /* --------------------------------------------------------------- rendering */
 /* Headless textures of the game's per-tick update, 4 bytes (r, g, b, a) per cell.
  * om_render_enable allocates them with every cell dirty; from then on the tick,

@@ -95,6 +95,13 @@ void om_world_step(om_world *wd, int order, int n);
 void om_tick_temperature(om_world *wd);
 /* om_world_step also runs om_tick_temperature after ticks whose index is 2 mod 4 */
 void om_world_set_temperature(om_world *wd, int on);
+/* chunk .pack codec (chunk.cpp:219-330): LZ4 block format helpers and whole-world
+ * pack/unpack, chunks row-major; see fse_oracle.c for the layout */
+int om_lz4_bound(int n);
+int om_lz4_encode(const uint8_t *buf, int n, uint8_t *dst, int cap);
+int om_lz4_decode(const uint8_t *src, int n, uint8_t *dst, int cap);
+int om_world_pack(const om_world *wd, int phase, uint8_t *out, int64_t cap, int64_t *offsets);
+int om_world_unpack(om_world *wd, const uint8_t *in, const int64_t *offsets, int n_chunks, int8_t *phases);
 /* per-cell temperature (i16): SOUP cells' own plane, the scalar of the others */
 void om_temperature_get(const om_world *wd, int16_t *out);
 void om_temperature_set(om_world *wd, const int16_t *in);
