@@ -331,6 +331,27 @@ class World:
         check(self.lib.fse_world_render_read(self.h, int(which), ptr(out)), "render_read")
         return out
 
+    # -- chunk .pack codec
+    def pack(self, phase=0):
+        """Chunk::ChunkWrite for every chunk (chunk.cpp:219-330): (bytes, offsets)."""
+        nb, nc = C.c_int64(0), C.c_int(0)
+        check(self.lib.fse_world_pack_bound(self.width, self.height, C.byref(nb), C.byref(nc)), "pack_bound")
+        out = np.empty(nb.value, np.uint8)
+        offs = np.zeros(nc.value + 1, np.int64)
+        check(self.lib.fse_world_pack(self.h, int(phase), ptr(out), nb.value, ptr(offs), C.byref(nc)), "pack")
+        return out[: offs[-1]], offs
+
+    def unpack(self, data, offsets):
+        """Chunk::ChunkRead for every chunk: the chunks' generation phases."""
+        data = np.ascontiguousarray(data, np.uint8)
+        offsets = np.ascontiguousarray(offsets, np.int64)
+        phases = np.zeros(len(offsets) - 1, np.int8)
+        bad = C.c_int(-1)
+        st = self.lib.fse_world_unpack(self.h, ptr(data), ptr(offsets), len(offsets) - 1, ptr(phases), C.byref(bad))
+        if st != 0:
+            raise FseError(st, "unpack (chunk %d)" % bad.value)
+        return phases
+
     # -- temperature
     def temperature(self, out=None):
         """MaterialInstance::temperature of every cell as an (H, W) int16 array."""

@@ -53,6 +53,9 @@ SIGNATURES = {
     "fse_world_temperature_read": (_i, [_vp, _vp]),
     "fse_world_temperature_write": (_i, [_vp, _vp]),
     "fse_world_tick_temperature": (_i, [_vp]),
+    "fse_world_pack_bound": (_i, [_i, _i, _vp, _vp]),
+    "fse_world_pack": (_i, [_vp, _i, _vp, _i64, _vp, _vp]),
+    "fse_world_unpack": (_i, [_vp, _vp, _vp, _i, _vp, _vp]),
     "fse_materials_load_lua": (_i, [C.c_char_p, C.POINTER(_i)]),
     "fse_materials_push": (_i, []),
     "fse_material_count": (_i, []),

@@ -1,0 +1,580 @@
+// fse_pack.cu -- the chunk .pack codec: Chunk::ChunkWrite / Chunk::ChunkRead
+// (source/engine/chunk.cpp:219-330 and 68-200) for every 128 x 128 chunk of a
+// device world.
+//
+// A .pack file is the chunk's i8 generation phase, four ints -- src_size
+// (128*128*2 MaterialInstanceData records of 12 bytes: {u32 index, u32 color,
+// i16 temperature, 2 bytes of padding}, chunk.hpp:26-30, tiles then layer2),
+// the size of its LZ4 block, src_size2 (the 128*128 u32 background) and the size
+// of that block -- then the two LZ4 blocks (the block format of the vendored
+// LZ4 1.9.4, source/libs/lz4). This world has no second layer and no background:
+// they are written as zeros and skipped on reading.
+//
+// Writing. k_pack_stage lays the tile records of a group of chunks out in HBM;
+// k_lz4_encode compresses each block with one warp. The encoder is this
+// project's own: at each byte p it takes the longest run buf[p + i] ==
+// buf[p + i - d] over 16 fixed distances d (ties to the nearer) when it is at
+// least 4 bytes, else p is a literal -- the distances are multiples of 4 and of
+// the 12-byte record, and one or two chunk rows (1536 bytes) back with the
+// diagonal neighbours. The warp tests 32 positions at once for a 4-byte match
+// and extends all candidate runs 32 bytes at a time; runs whose remaining bytes
+// lie in the zero second layer on both sides are extended to the end at once.
+// On generated worlds the blocks come out smaller than those of the reference's
+// LZ4_compress_fast(..., 10). k_pack_assemble writes headers and blocks.
+//
+// Reading. k_lz4_decode decodes each block with one warp: tokens, lengths and
+// literals come through a shared-memory window of the input, and matches whose
+// offset fits a shared-memory ring of the latest output are copied from it (others
+// from HBM). Every length and offset is checked against both buffers: a malformed
+// block yields a negative status and no access out of bounds. k_unpack_check
+// rejects material indices outside the table; k_unpack_scatter writes id, colour
+// and temperature into the planes (a SOUP tile's amount is the MaterialInstance
+// default 2.0, game_datastruct.hpp:216).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "fse_host.cuh"
+#include "fse_internal.cuh"
+
+namespace fse {
+namespace {
+
+constexpr int PK_EDGE = 128;
+constexpr int PK_CELLS = PK_EDGE * PK_EDGE;
+constexpr int PK_TILES = PK_CELLS * 12;     // tile records of one chunk
+constexpr int PK_SRC1 = PK_CELLS * 2 * 12;  // tiles + layer2
+constexpr int PK_SRC2 = PK_CELLS * 4;       // background
+constexpr int PK_HEADER = 17;
+constexpr int PK_GROUP = 1024;  // chunks per device pass (bounds the scratch)
+__host__ __device__ constexpr int lz4_bound(int n) { return n + n / 255 + 16; }
+constexpr int PK_SLOT1 = (lz4_bound(PK_SRC1) + 15) & ~15;
+constexpr int PK_SLOT2 = (lz4_bound(PK_SRC2) + 15) & ~15;
+
+__constant__ int c_dist[16] = {4, 8, 12, 16, 20, 24, 36, 48, 60, 72, 84, 96, 1524, 1536, 1548, 3072};
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// ------------------------------------------------------------------ stage
+__global__ void k_pack_stage(const WorldDev *__restrict__ wd, const MatTable *__restrict__ mt, uint32_t *stage,
+                             int chunk0, int n_chunks) {
+    const WorldDev &w = *wd;
+    const int ncx = (w.W + PK_EDGE - 1) / PK_EDGE;
+    const long long total = (long long)n_chunks * PK_CELLS;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(e / PK_CELLS), j = (int)(e - (long long)c * PK_CELLS);
+        const int k = chunk0 + c;
+        const int x = (k % ncx) * PK_EDGE + (j % PK_EDGE), y = (k / ncx) * PK_EDGE + (j / PK_EDGE);
+        uint32_t id = 0, col = 0, tw = 0;
+        if (x < w.W && y < w.H) {
+            const size_t i = (size_t)y * w.W + x;
+            id = w.id[i];
+            col = w.col[i];
+            const int16_t t = mt_type(mt->a[id]) == T_SOUP ? (w.tp ? w.tp[i] : (int16_t)0) : (int16_t)w.sc[i];
+            tw = (uint32_t)(uint16_t)t;  // i16 temperature, then 2 bytes of padding (0)
+        }
+        uint32_t *r = stage + (size_t)c * (PK_TILES / 4) + (size_t)j * 3;
+        r[0] = id;
+        r[1] = col;
+        r[2] = tw;
+    }
+}
+
+// ----------------------------------------------------------------- encode
+// The block's bytes: buf[0, T) from HBM (4-byte aligned), zeros from T to n.
+struct Src {
+    const uint32_t *w;  // T / 4 words
+    int T;
+    __device__ __forceinline__ uint32_t word(int i) const { return (4 * i < T) ? __ldg(w + i) : 0u; }
+    __device__ __forceinline__ uint32_t load4(int p) const {
+        const int i = p >> 2, s = (p & 3) * 8;
+        return __funnelshift_r(word(i), word(i + 1), s);
+    }
+    __device__ __forceinline__ uint32_t byte(int p) const { return (word(p >> 2) >> ((p & 3) * 8)) & 0xFFu; }
+};
+
+// one sequence: literals [ls, ls + nl), then (when ml > 0) a match of ml bytes at
+// distance off; returns the new output position, or -1 when it would not fit
+__device__ int emit_seq(const Src &s, uint8_t *dst, int op, int cap, int ls, int nl, int off, int ml) {
+    const int lane = threadIdx.x & 31;
+    const int mcode = ml > 0 ? ml - 4 : 0;
+    const int lext = nl >= 15 ? (nl - 15) / 255 + 1 : 0;
+    const int mext = (ml > 0 && mcode >= 15) ? (mcode - 15) / 255 + 1 : 0;
+    const int need = 1 + lext + nl + (ml > 0 ? 2 + mext : 0);
+    if (need > cap - op) return -1;
+    if (lane == 0) {
+        dst[op] = (uint8_t)(((nl < 15 ? nl : 15) << 4) | (ml > 0 ? (mcode < 15 ? mcode : 15) : 0));
+        int o = op + 1;
+        if (nl >= 15) {
+            int v = nl - 15;
+            for (; v >= 255; v -= 255) dst[o++] = 255;
+            dst[o++] = (uint8_t)v;
+        }
+        o += nl;
+        if (ml > 0) {
+            dst[o++] = (uint8_t)(off & 255);
+            dst[o++] = (uint8_t)(off >> 8);
+            if (mcode >= 15) {
+                int v = mcode - 15;
+                for (; v >= 255; v -= 255) dst[o++] = 255;
+                dst[o++] = (uint8_t)v;
+            }
+        }
+    }
+    const int lo = op + 1 + lext;
+    for (int i = lane; i < nl; i += 32) dst[lo + i] = (uint8_t)s.byte(ls + i);
+    return op + need;
+}
+
+// one warp per block: block b of the group (stage words at stage + b * T / 4)
+__global__ void __launch_bounds__(128) k_lz4_encode(const uint32_t *__restrict__ stage, int T, int n, int n_blocks,
+                                                    uint8_t *out, int slot, int *sizes) {
+    const int lane = threadIdx.x & 31;
+    const int b = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    if (b >= n_blocks) return;
+    Src s{stage + (size_t)b * (T / 4), T};
+    uint8_t *dst = out + (size_t)b * slot;
+    const int mflimit = n - 12, mend = n - 5;
+    int p = 0, anchor = 0, op = 0;
+    while (p <= mflimit && op >= 0) {
+        // the first position of [p, p + 32) with a 4-byte match at some distance
+        const int q = p + lane;
+        unsigned cm = 0;
+        if (q <= mflimit) {
+            const uint32_t v = s.load4(q);
+#pragma unroll
+            for (int k = 0; k < 16; k++) {
+                const int d = c_dist[k];
+                if (d <= q && s.load4(q - d) == v) cm |= 1u << k;
+            }
+        }
+        const unsigned any = __ballot_sync(FULL, cm != 0);
+        if (!any) {
+            p += 32;
+            continue;
+        }
+        const int f = __ffs(any) - 1;
+        const int q0 = p + f;
+        unsigned alive = __shfl_sync(FULL, cm, f);
+        // extend every candidate run, 32 bytes per step
+        int len[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) len[k] = 0;
+        for (int base = 0; alive; base += 32) {
+            const int x = q0 + base + lane;
+            const uint32_t bx = (x < mend) ? s.byte(x) : 0u;
+#pragma unroll
+            for (int k = 0; k < 16; k++) {
+                if (!(alive & (1u << k))) continue;
+                const int d = c_dist[k];
+                if (q0 + base - d >= s.T) {  // both sides in the zero tail from here on: equal to the end
+                    len[k] = mend - q0;
+                    alive &= ~(1u << k);
+                    continue;
+                }
+                const bool eq = x < mend && s.byte(x - d) == bx;
+                const unsigned miss = __ballot_sync(FULL, !eq);
+                if (miss) {
+                    len[k] = base + __ffs(miss) - 1;
+                    alive &= ~(1u << k);
+                }
+            }
+        }
+        int best = 0, bd = 0;
+#pragma unroll
+        for (int k = 0; k < 16; k++)
+            if (len[k] > best) {
+                best = len[k];
+                bd = c_dist[k];
+            }
+        op = emit_seq(s, dst, op, slot, anchor, q0 - anchor, bd, best);
+        p = q0 + best;
+        anchor = p;
+    }
+    if (op >= 0) op = emit_seq(s, dst, op, slot, anchor, n - anchor, 0, 0);
+    __syncwarp();
+    if (lane == 0) sizes[b] = op;  // -1: did not fit (cannot happen within the bound)
+}
+
+// ---------------------------------------------------------------- assemble
+// chunk c of the group: phase, sizes, block 1 (slot c), block 2 (shared)
+__global__ void k_pack_assemble(const uint8_t *__restrict__ enc1, int slot1, const int *__restrict__ size1,
+                                const uint8_t *__restrict__ enc2, int size2, const long long *__restrict__ offs,
+                                int n_chunks, int8_t phase, uint8_t *out) {
+    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        uint8_t *o = out + offs[c];
+        const int n1 = size1[c];
+        if (threadIdx.x == 0) {
+            const int32_t hd[4] = {PK_SRC1, n1, PK_SRC2, size2};
+            o[0] = (uint8_t)phase;
+            const uint8_t *hb = reinterpret_cast<const uint8_t *>(hd);
+            for (int i = 0; i < 16; i++) o[1 + i] = hb[i];
+        }
+        const uint8_t *e1 = enc1 + (size_t)c * slot1;
+        for (int i = threadIdx.x; i < n1; i += blockDim.x) o[PK_HEADER + i] = e1[i];
+        for (int i = threadIdx.x; i < size2; i += blockDim.x) o[PK_HEADER + n1 + i] = enc2[i];
+    }
+}
+
+// ------------------------------------------------------------------ decode
+constexpr int DEC_WIN = 2048;   // input window per warp
+constexpr int DEC_RING = 8192;  // latest output per warp
+constexpr int DEC_WARPS = 4;
+
+struct DecSmem {
+    uint8_t win[DEC_WARPS][DEC_WIN];
+    uint8_t ring[DEC_WARPS][DEC_RING];
+};
+
+// the input window holds src[wb, wb + DEC_WIN) (clipped to n); reads outside it
+// refill it at the requested position
+struct DecIn {
+    const uint8_t *src;
+    int n, wb;
+    uint8_t *win;
+    __device__ __forceinline__ void fill(int at) {
+        __syncwarp();
+        wb = at;
+        const int lane = threadIdx.x & 31;
+        for (int i = lane; i < DEC_WIN && at + i < n; i += 32) win[i] = src[at + i];
+        __syncwarp();
+    }
+    __device__ __forceinline__ int get(int ip) {  // 0 <= ip < n
+        if (ip < wb || ip >= wb + DEC_WIN) fill(ip);
+        return win[ip - wb];
+    }
+};
+
+__device__ int warp_lz4_decode(const uint8_t *src, int n, uint8_t *dst, int cap, uint8_t *win, uint8_t *ring) {
+    const int lane = threadIdx.x & 31;
+    DecIn in{src, n, 0, win};
+    in.fill(0);
+    int ip = 0, op = 0;
+    for (;;) {
+        if (ip >= n) return -1;
+        const int token = in.get(ip++);
+        int ll = token >> 4;
+        if (ll == 15) {
+            int b;
+            do {
+                if (ip >= n) return -2;
+                b = in.get(ip++);
+                ll += b;
+                if (ll > cap) return -3;
+            } while (b == 255);
+        }
+        if (ll > n - ip || ll > cap - op) return -3;
+        // literals: from the window when they lie in it, else from HBM
+        const bool inwin = ip >= in.wb && ip + ll <= in.wb + DEC_WIN && ip + ll <= n;
+        for (int i = lane; i < ll; i += 32) {
+            const uint8_t v = inwin ? in.win[ip - in.wb + i] : src[ip + i];
+            dst[op + i] = v;
+            ring[(op + i) & (DEC_RING - 1)] = v;
+        }
+        ip += ll;
+        op += ll;
+        if (ip == n) return op;  // the last sequence: literals only
+        if (n - ip < 2) return -4;
+        const int off = in.get(ip) | (in.get(ip + 1) << 8);
+        ip += 2;
+        if (off == 0 || off > op) return -5;
+        int ml = token & 15;
+        if (ml == 15) {
+            int b;
+            do {
+                if (ip >= n) return -6;
+                b = in.get(ip++);
+                ml += b;
+                if (ml > cap) return -7;
+            } while (b == 255);
+        }
+        ml += 4;
+        if (ml > cap - op) return -7;
+        __syncwarp();  // the bytes the match reads are written
+        // byte j of the match repeats byte (j mod off) of the `off` bytes before it, so
+        // no byte of a round depends on another one of the same round. From the ring,
+        // a round copies at most DEC_RING - off bytes, so that it overwrites no ring
+        // slot it reads; the next round reads the `off` bytes before it again.
+        const bool from_ring = off <= DEC_RING - 32;
+        for (int done = 0; done < ml;) {
+            const int m = from_ring ? min(ml - done, DEC_RING - off) : ml - done;
+            const int base = op + done;
+            int sidx = off >= 32 ? lane : lane % off;
+            for (int j = lane; j < m; j += 32) {
+                const int from = base - off + sidx;
+                const uint8_t v = from_ring ? ring[from & (DEC_RING - 1)] : dst[from];
+                dst[base + j] = v;
+                ring[(base + j) & (DEC_RING - 1)] = v;
+                sidx += 32;
+                if (off >= 32) {
+                    if (sidx >= off) sidx -= off;
+                } else {
+                    sidx %= off;
+                }
+            }
+            __syncwarp();
+            done += m;
+        }
+        op += ml;
+    }
+}
+
+// block b: src + offs[b], lens[b] bytes -> out + b * slot; status[b] = decoded
+// size or a negative error
+__global__ void __launch_bounds__(DEC_WARPS * 32) k_lz4_decode(const uint8_t *__restrict__ src,
+                                                               const long long *__restrict__ offs,
+                                                               const int *__restrict__ lens, int n_blocks, int expect,
+                                                               uint8_t *out, int slot, int *status) {
+    __shared__ DecSmem S;
+    const int wi = threadIdx.x / 32, lane = threadIdx.x & 31;
+    const int b = blockIdx.x * DEC_WARPS + wi;
+    if (b >= n_blocks) return;
+    int r = -8;
+    if (lens[b] > 0) r = warp_lz4_decode(src + offs[b], lens[b], out + (size_t)b * slot, expect, S.win[wi], S.ring[wi]);
+    if (lane == 0) status[b] = r;
+}
+
+// chunks whose records name a material outside the table: the lowest such chunk
+__global__ void k_unpack_check(const uint8_t *__restrict__ rec, int slot, int n_chunks, int n_mat, int *first_bad) {
+    const long long total = (long long)n_chunks * PK_CELLS;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(e / PK_CELLS), j = (int)(e - (long long)c * PK_CELLS);
+        const uint8_t *r = rec + (size_t)c * slot + (size_t)j * 12;
+        const uint32_t id = (uint32_t)r[0] | ((uint32_t)r[1] << 8) | ((uint32_t)r[2] << 16) | ((uint32_t)r[3] << 24);
+        if (id >= (uint32_t)n_mat) atomicMin(first_bad, c);
+    }
+}
+
+__global__ void k_unpack_scatter(const WorldDev *__restrict__ wd, const MatTable *__restrict__ mt,
+                                 const uint8_t *__restrict__ rec, int slot, int chunk0, int n_chunks) {
+    const WorldDev &w = *wd;
+    const int ncx = (w.W + PK_EDGE - 1) / PK_EDGE;
+    const long long total = (long long)n_chunks * PK_CELLS;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(e / PK_CELLS), j = (int)(e - (long long)c * PK_CELLS);
+        const int k = chunk0 + c;
+        const int x = (k % ncx) * PK_EDGE + (j % PK_EDGE), y = (k / ncx) * PK_EDGE + (j / PK_EDGE);
+        if (x >= w.W || y >= w.H) continue;
+        const uint8_t *r = rec + (size_t)c * slot + (size_t)j * 12;
+        const uint32_t id = (uint32_t)r[0] | ((uint32_t)r[1] << 8) | ((uint32_t)r[2] << 16) | ((uint32_t)r[3] << 24);
+        const uint32_t col = (uint32_t)r[4] | ((uint32_t)r[5] << 8) | ((uint32_t)r[6] << 16) | ((uint32_t)r[7] << 24);
+        const int16_t t = (int16_t)(uint16_t)((uint32_t)r[8] | ((uint32_t)r[9] << 8));
+        const size_t i = (size_t)y * w.W + x;
+        w.id[i] = (uint16_t)id;
+        w.col[i] = col;
+        w.fl[i] = 0;
+        w.df[i] = 0;
+        if (mt_type(mt->a[id]) == T_SOUP) {
+            w.sc[i] = Q_DEFAULT;  // MaterialInstance::fluidAmount = 2.0
+            if (w.tp) w.tp[i] = t;
+        } else {
+            w.sc[i] = t;
+        }
+        if (w.dirty) w.dirty[i] = 1;
+    }
+}
+
+int grid_for(long long work, int per) {
+    return (int)std::max(1LL, std::min<long long>((work + per - 1) / per, sm_count() * 16LL));
+}
+
+}  // namespace
+}  // namespace fse
+
+using namespace fse;
+
+extern "C" {
+
+int fse_world_pack_bound(int width, int height, int64_t *out_bytes, int *out_chunks) {
+    if (width <= 0 || height <= 0) return FSE_E_INVAL;
+    const long long n = (long long)((width + PK_EDGE - 1) / PK_EDGE) * ((height + PK_EDGE - 1) / PK_EDGE);
+    if (out_bytes) *out_bytes = n * (PK_HEADER + lz4_bound(PK_SRC1) + lz4_bound(PK_SRC2));
+    if (out_chunks) *out_chunks = (int)n;
+    return FSE_OK;
+}
+
+int fse_world_pack(fse_world *w, int generation_phase, uint8_t *out, int64_t cap, int64_t *offsets, int *out_n_chunks) {
+    if (!w || !out || !offsets) return FSE_E_INVAL;
+    int rc = ensure_materials_pushed();
+    if (rc) return rc;
+    int nch = 0;
+    fse_world_pack_bound(w->W, w->H, nullptr, &nch);
+    if (out_n_chunks) *out_n_chunks = nch;
+    const int G = std::min(PK_GROUP, nch);
+    uint32_t *stage = nullptr;
+    uint8_t *enc1 = nullptr, *enc2 = nullptr, *dout = nullptr;
+    int *sizes = nullptr;
+    long long *doffs = nullptr;
+    cudaStream_t s = w->stream;
+    auto cleanup = [&]() {
+        void *ps[] = {stage, enc1, enc2, dout, sizes, doffs};
+        for (void *q : ps)
+            if (q) cudaFree(q);
+    };
+    if (cudaMalloc(&stage, (size_t)G * PK_TILES) != cudaSuccess || cudaMalloc(&enc1, (size_t)G * PK_SLOT1) != cudaSuccess ||
+        cudaMalloc(&enc2, PK_SLOT2) != cudaSuccess || cudaMalloc(&sizes, (size_t)(G + 1) * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&doffs, (size_t)G * sizeof(long long)) != cudaSuccess ||
+        cudaMalloc(&dout, (size_t)G * (PK_HEADER + PK_SLOT1 + PK_SLOT2)) != cudaSuccess) {
+        cleanup();
+        return FSE_E_NOMEM;
+    }
+    // the background block: 64 KB of zeros, the same for every chunk
+    k_lz4_encode<<<1, 128, 0, s>>>(stage, 0, PK_SRC2, 1, enc2, PK_SLOT2, sizes + G);
+    int size2 = 0;
+    std::vector<int> sz(G);
+    std::vector<long long> offs(G);
+    int64_t pos = 0;
+    for (int c0 = 0; c0 < nch && rc == FSE_OK; c0 += G) {
+        const int g = std::min(G, nch - c0);
+        k_pack_stage<<<grid_for((long long)g * PK_CELLS, 256), 256, 0, s>>>(w->d, g_dev_mt, stage, c0, g);
+        k_lz4_encode<<<(g + 3) / 4, 128, 0, s>>>(stage, PK_TILES, PK_SRC1, g, enc1, PK_SLOT1, sizes);
+        if (cudaMemcpyAsync(sz.data(), sizes, g * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            (c0 == 0 && cudaMemcpyAsync(&size2, sizes + G, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
+            cudaStreamSynchronize(s) != cudaSuccess) {
+            rc = FSE_E_CUDA;
+            break;
+        }
+        long long rel = 0;
+        for (int c = 0; c < g; c++) {
+            if (sz[c] < 0 || size2 < 0) rc = FSE_E_CUDA;
+            offs[c] = rel;
+            offsets[c0 + c] = pos + rel;
+            rel += PK_HEADER + sz[c] + size2;
+        }
+        if (rc) break;
+        if (pos + rel > cap) {
+            rc = FSE_E_CAPACITY;
+            break;
+        }
+        if (cudaMemcpyAsync(doffs, offs.data(), g * sizeof(long long), cudaMemcpyHostToDevice, s) != cudaSuccess) {
+            rc = FSE_E_CUDA;
+            break;
+        }
+        k_pack_assemble<<<std::min(g, sm_count() * 8), 256, 0, s>>>(enc1, PK_SLOT1, sizes, enc2, size2, doffs, g,
+                                                                   (int8_t)generation_phase, dout);
+        if (cudaMemcpyAsync(out + pos, dout, (size_t)rel, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) {
+            rc = FSE_E_CUDA;
+            break;
+        }
+        pos += rel;
+    }
+    if (rc == FSE_OK) offsets[nch] = pos;
+    count_launches(1 + 3LL * ((nch + G - 1) / G));
+    cleanup();
+    return rc;
+}
+
+int fse_world_unpack(fse_world *w, const uint8_t *in, const int64_t *offsets, int n_chunks, int8_t *out_phases,
+                     int *out_bad_chunk) {
+    if (!w || !in || !offsets) return FSE_E_INVAL;
+    if (out_bad_chunk) *out_bad_chunk = -1;
+    int nch = 0;
+    fse_world_pack_bound(w->W, w->H, nullptr, &nch);
+    if (n_chunks != nch) return FSE_E_INVAL;
+    int rc = ensure_materials_pushed();
+    if (rc) return rc;
+    const int nmat = host_table().n;
+    // headers on the host: the first malformed chunk ends the load (chunks before it are written)
+    int bad = nch;
+    std::vector<long long> o1(nch), o2(nch);
+    std::vector<int> l1(nch), l2(nch);
+    for (int k = 0; k < nch; k++) {
+        const long long len = offsets[k + 1] - offsets[k];
+        int32_t hd[4] = {0, 0, 0, 0};
+        if (offsets[k] < 0 || len < PK_HEADER) {
+            bad = k;
+            break;
+        }
+        memcpy(hd, in + offsets[k] + 1, 16);
+        if (hd[0] != PK_SRC1 || hd[2] != PK_SRC2 || hd[1] <= 0 || hd[3] <= 0 ||
+            (long long)PK_HEADER + hd[1] + hd[3] > len) {
+            bad = k;
+            break;
+        }
+        if (out_phases) out_phases[k] = (int8_t)in[offsets[k]];
+        o1[k] = offsets[k] + PK_HEADER;
+        l1[k] = hd[1];
+        o2[k] = offsets[k] + PK_HEADER + hd[1];
+        l2[k] = hd[3];
+    }
+    const int G = std::max(1, std::min(PK_GROUP, nch));
+    uint8_t *din = nullptr, *rec = nullptr, *bgo = nullptr;
+    long long *doff = nullptr;
+    int *dlen = nullptr, *dst = nullptr;
+    cudaStream_t s = w->stream;
+    auto cleanup = [&]() {
+        void *ps[] = {din, rec, bgo, doff, dlen, dst};
+        for (void *q : ps)
+            if (q) cudaFree(q);
+    };
+    if (cudaMalloc(&rec, (size_t)G * PK_SRC1) != cudaSuccess || cudaMalloc(&bgo, (size_t)G * PK_SRC2) != cudaSuccess ||
+        cudaMalloc(&doff, (size_t)2 * G * sizeof(long long)) != cudaSuccess ||
+        cudaMalloc(&dlen, (size_t)2 * G * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&dst, (size_t)(2 * G + 1) * sizeof(int)) != cudaSuccess) {
+        cleanup();
+        return FSE_E_NOMEM;
+    }
+    std::vector<int> st(2 * G);
+    for (int c0 = 0; c0 < bad && rc == FSE_OK; c0 += G) {
+        const int g = std::min(G, bad - c0);
+        // the group's input, one copy
+        const long long lo = offsets[c0], hi = offsets[c0 + g];
+        if (din) cudaFree(din);
+        din = nullptr;
+        if (cudaMalloc(&din, (size_t)(hi - lo)) != cudaSuccess) {
+            rc = FSE_E_NOMEM;
+            break;
+        }
+        std::vector<long long> ho(2 * g);
+        std::vector<int> hl(2 * g);
+        for (int c = 0; c < g; c++) {
+            ho[c] = o1[c0 + c] - lo;
+            hl[c] = l1[c0 + c];
+            ho[g + c] = o2[c0 + c] - lo;
+            hl[g + c] = l2[c0 + c];
+        }
+        const int big = 0x7fffffff;
+        if (cudaMemcpyAsync(din, in + lo, (size_t)(hi - lo), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(doff, ho.data(), 2 * g * sizeof(long long), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(dlen, hl.data(), 2 * g * sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(dst + 2 * G, &big, sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess) {
+            rc = FSE_E_CUDA;
+            break;
+        }
+        k_lz4_decode<<<(g + DEC_WARPS - 1) / DEC_WARPS, DEC_WARPS * 32, 0, s>>>(din, doff, dlen, g, PK_SRC1, rec,
+                                                                              PK_SRC1, dst);
+        k_lz4_decode<<<(g + DEC_WARPS - 1) / DEC_WARPS, DEC_WARPS * 32, 0, s>>>(din, doff + g, dlen + g, g, PK_SRC2,
+                                                                              bgo, PK_SRC2, dst + g);
+        k_unpack_check<<<grid_for((long long)g * PK_CELLS, 256), 256, 0, s>>>(rec, PK_SRC1, g, nmat, dst + 2 * G);
+        int first_bad_id = big;
+        if (cudaMemcpyAsync(st.data(), dst, 2 * g * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaMemcpyAsync(&first_bad_id, dst + 2 * G, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) {
+            rc = FSE_E_CUDA;
+            break;
+        }
+        int gbad = std::min(g, first_bad_id);
+        for (int c = 0; c < g; c++)
+            if (st[c] != PK_SRC1 || st[g + c] != PK_SRC2) gbad = std::min(gbad, c);
+        if (gbad > 0)
+            k_unpack_scatter<<<grid_for((long long)gbad * PK_CELLS, 256), 256, 0, s>>>(w->d, g_dev_mt, rec, PK_SRC1,
+                                                                                        c0, gbad);
+        count_launches(3 + (gbad > 0 ? 1 : 0));
+        if (gbad < g) bad = c0 + gbad;
+    }
+    if (rc == FSE_OK && cudaStreamSynchronize(s) != cudaSuccess) rc = FSE_E_CUDA;
+    cleanup();
+    if (rc) return rc;
+    if (bad < nch) {
+        if (out_bad_chunk) *out_bad_chunk = bad;
+        return FSE_E_INVAL;
+    }
+    return FSE_OK;
+}
+
+}  // extern "C"

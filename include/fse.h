@@ -20,6 +20,7 @@
  *   fse_object_stamp          rigid-body tile stamping   source/engine/game.cpp:1768-1814
  *   fse_object_readback       rigid-body tile readback   source/engine/game.cpp:1896-1983
  *   fse_world_tick_temperature world::tickTemperature()  source/engine/world.cpp:1950-2004
+ *   fse_world_pack/unpack     Chunk::ChunkWrite/ChunkRead source/engine/chunk.cpp:68-330
  */
 #ifndef FSE_H
 #define FSE_H
@@ -187,6 +188,30 @@ int fse_world_temperature_write(fse_world *world, const int16_t *temps);
  * conduction stencil over every cell; a neighbour outside the world counts as
  * temperature 0. Enqueued on the world's stream. */
 int fse_world_tick_temperature(fse_world *world);
+
+/* ------------------------------------------------------- chunk .pack codec */
+/* Chunk::ChunkWrite for every 128 x 128 chunk, row-major (chunk k covers cells
+ * x = (k % ceil(w/128)) * 128 + [0, 128), y = (k / ceil(w/128)) * 128 + [0, 128);
+ * cells outside the world are GENERIC_AIR records): each .pack is the i8
+ * generation phase, src_size, the tile block's size, src_size2, the background
+ * block's size (ints) and two LZ4 blocks (chunk.cpp:219-330). The records are
+ * MaterialInstanceData {u32 index, u32 colour, i16 temperature} (chunk.hpp:26-30);
+ * the second layer and the background, which this world does not have, are
+ * zeros. Liquid temperatures are written as 0 unless the world keeps them
+ * (FSE_CFG_TEMPERATURE). out: host buffer of cap bytes; offsets[k] = start of
+ * chunk k's .pack in out, offsets[n] = total; *out_n_chunks = n. */
+int fse_world_pack_bound(int width, int height, int64_t *out_bytes, int *out_chunks);
+int fse_world_pack(fse_world *world, int generation_phase, uint8_t *out, int64_t cap, int64_t *offsets,
+                   int *out_n_chunks);
+/* Chunk::ChunkRead for every chunk: in + offsets as fse_world_pack writes them (any
+ * LZ4 encoder's blocks are read). Tiles take the records' material, colour and
+ * temperature; a SOUP tile's amount is the MaterialInstance default 2.0, flags
+ * and pending diffs are cleared. out_phases[k] (optional) = chunk k's generation
+ * phase. A malformed chunk (header, sizes, LZ4 block or a material index out of
+ * range) ends the load: FSE_E_INVAL with *out_bad_chunk = its index, the chunks
+ * before it written, none after. */
+int fse_world_unpack(fse_world *world, const uint8_t *in, const int64_t *offsets, int n_chunks, int8_t *out_phases,
+                     int *out_bad_chunk);
 
 /* world::tick(), n times (no particle step in between) */
 int fse_world_tick(fse_world *world, int n_ticks);

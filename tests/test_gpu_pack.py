@@ -1,0 +1,114 @@
+"""Chunk .pack codec on the GPU (Chunk::ChunkWrite / ChunkRead, chunk.cpp:68-330).
+
+The device encoder writes exactly the oracle's bytes; the device decoder reads the
+.pack files the reference's own LZ4 made (tests/golden/pack.npz) and the oracle's,
+and refuses malformed chunks at the same chunk as the oracle.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from pack_cases import HEADER, SRC1, sample_world, split_blocks
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "pack.npz")
+
+
+def _device_copy(fse, ow, w, h):
+    """A device world (keeping liquid temperatures) holding the oracle world's state."""
+    world = fse.World(w, h, seed=1, temperature=True)
+    st = ow.state()
+    world.upload(st)
+    world.set_temperature(ow.temperature())
+    return world
+
+
+@pytest.mark.parametrize("w,h,seed", [(256, 192, 77), (200, 136, 5), (384, 256, 9), (128, 128, 3)])
+def test_pack_matches_oracle(fse, oracle_mod, w, h, seed):
+    oracle_mod.Oracle().reset_materials()
+    ow = sample_world(oracle_mod, w, h, seed)
+    world = _device_copy(fse, ow, w, h)
+    for phase in (0, -3):
+        data, offs = world.pack(phase)
+        odata, ooffs = ow.pack(phase)
+        assert np.array_equal(offs, ooffs) and np.array_equal(data, odata), (w, h, phase)
+
+
+def test_unpack_reference_files(fse, oracle_mod):
+    g = np.load(GOLDEN)
+    w, h, seed, phase = [int(v) for v in g["params"]]
+    world = fse.World(w, h, seed=1, temperature=True)
+    phases = world.unpack(g["ref_data"], g["ref_offsets"])
+    assert np.all(phases == phase)
+    st = world.state()
+    assert np.array_equal(st["id"], g["id"]) and np.array_equal(st["colour"], g["colour"])
+    assert np.array_equal(world.temperature(), g["temperature"])
+    types = np.array([fse.material_get(i)[0] for i in range(fse.material_count())])
+    soup = types[st["id"]] == fse.SOUP
+    assert np.all(st["scalar"][soup] == 2 * fse.FLUID_ONE)
+    assert not st["flags"].any()
+    # the oracle reads the same files to the same state
+    ow = oracle_mod.OracleWorld(w, h, 128, 3, 1)
+    rc, _ = ow.unpack(g["ref_data"], g["ref_offsets"])
+    assert rc == 0
+    o = ow.state()
+    for k in ("id", "colour", "scalar", "flags"):
+        assert np.array_equal(st[k], o[k]), k
+
+
+@pytest.mark.parametrize("w,h", [(384, 256), (200, 136)])
+def test_pack_unpack_roundtrip_and_resume(fse, oracle_mod, w, h):
+    """pack -> unpack into a fresh world restores ids, colours and temperatures; both
+    worlds then tick identically (liquid amounts read back as 2.0 on both sides)."""
+    world = fse.World(w, h, seed=11, temperature=True)
+    world.generate(fse.GEN_MIX, 11)
+    world.step(5)
+    data, offs = world.pack(1)
+    a = fse.World(w, h, seed=11, temperature=True)
+    assert np.all(a.unpack(data, offs) == 1)
+    sa, s0 = a.state(), world.state()
+    assert np.array_equal(sa["id"], s0["id"]) and np.array_equal(sa["colour"], s0["colour"])
+    assert np.array_equal(a.temperature(), world.temperature())
+    b = fse.World(w, h, seed=11, temperature=True)
+    b.unpack(data, offs)
+    a.step(4)
+    b.step(4)
+    for k, v in a.state().items():
+        assert np.array_equal(v, b.state()[k]), k
+
+
+def test_unpack_rejects_malformed(fse, oracle_mod):
+    """A chunk with a bad header, size or block ends the load at that chunk, as in the
+    oracle; the chunks before it are written."""
+    oracle_mod.Oracle().reset_materials()
+    ow = sample_world(oracle_mod, 384, 256, 4)
+    data, offs = ow.pack(0)
+    cases = []
+    d = data.copy()
+    d[offs[2] + 1: offs[2] + 5] = np.array([SRC1 + 12], "<i4").view(np.uint8)  # src_size of chunk 2
+    cases.append((d, offs.copy(), 2))
+    d = data.copy()
+    hd, c1, _ = split_blocks(data, offs, 4)
+    d[offs[4] + HEADER: offs[4] + HEADER + 6] = 255  # runaway literal length in chunk 4
+    cases.append((d, offs.copy(), 4))
+    d = data.copy()
+    o = offs.copy()
+    o[3] = o[2] + 10  # chunk 2 shorter than a header
+    cases.append((d, o, 2))
+    d = data.copy()
+    d[offs[1] + HEADER + hd[1] - 3: offs[1] + HEADER + hd[1]] = 0  # chunk 1: block cut short of its size
+    hd1 = split_blocks(data, offs, 1)[0]
+    d[offs[1] + 5: offs[1] + 9] = np.array([hd1[1] - 40], "<i4").view(np.uint8)
+    cases.append((d, offs.copy(), 1))
+    for d, o, k in cases:
+        world = fse.World(384, 256, seed=1, temperature=True)
+        with pytest.raises(fse.FseError):
+            world.unpack(d, o)
+        ob = oracle_mod.OracleWorld(384, 256, 128, 3, 1)
+        rc, _ = ob.unpack(d, o)
+        assert rc == -1 - k, (rc, k)
+        gs, os_ = world.state(), ob.state()
+        for key in ("id", "colour", "scalar"):
+            assert np.array_equal(gs[key], os_[key]), (key, k)
