@@ -184,6 +184,7 @@ def bench_config1(args, rank, local_rank, world_size):
     e2e = e2e_config1(world, args, torch, cells, world_size)
     render = render_config1(fse, torch, W, H, seed, NP) if rank == 0 else None
     temperature = temperature_config1(fse, torch, W, H, seed, NP) if rank == 0 else None
+    pack = pack_config1(fse, torch, W, H, seed, NP) if rank == 0 else None
     cpu = None
     if rank == 0 and world_size == 1 and not args.no_cpu:
         cpu = cpu_baseline_config1(seed)
@@ -199,7 +200,7 @@ def bench_config1(args, rank, local_rank, world_size):
                    "l2": "flushed between timed steps (512 MiB write outside the events)",
                    "parallelism": "one independent world per GPU" if world_size > 1 else "single GPU"},
         "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
-        "wall_s": round(wall, 3), "render": render, "temperature": temperature,
+        "wall_s": round(wall, 3), "render": render, "temperature": temperature, "pack": pack,
     }
 
 
@@ -311,6 +312,62 @@ def temperature_config1(fse, torch, W, H, seed, NP, calls=10):
             "frac": round(gbs / peak, 4), "peak": peak, "peak_kind": peak_kind, "calls": calls,
             "kernels": "k_temp_tiles + k_temp_commit",
             "l2": "flushed before each step (512 MiB write outside the events)"}
+
+
+def pack_config1(fse, torch, W, H, seed, NP, calls=5):
+    """The chunk .pack codec (Chunk::ChunkWrite / ChunkRead) on the same workload
+    after 16 steps: every 128x128 chunk packed into host memory and read back,
+    host clock around each call (the calls are synchronous and include the
+    host<->device copies). Throughput counts the uncompressed .pack payload, 393216
+    + 65536 bytes per chunk. CPU leg: the oracle's C restatement of the same
+    codec, one thread, on 16 chunks of the same world."""
+    import oracle as om
+
+    om.build_oracle()
+    om.Oracle().reset_materials()
+    world = fse.World(W, H, chunk_size=128, cell_iter=3, seed=seed, particle_capacity=4_000_000,
+                      spawn_capacity=2_000_000, temperature=True)
+    world.generate(fse.GEN_MIX, seed)
+    world.addCell(config1_particles(NP, W, H, seed))
+    world.step(16)
+    world.sync()
+    data, offs = world.pack(0)  # warm-up
+    world.unpack(data, offs)
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        data, offs = world.pack(0)
+    pack_s = (time.perf_counter() - t0) / calls
+    back = fse.World(W, H, seed=seed, temperature=True)
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        back.unpack(data, offs)
+    unpack_s = (time.perf_counter() - t0) / calls
+    same = bool(np.array_equal(back.state()["id"], world.state()["id"]))
+    n = len(offs) - 1
+    raw = n * (393216 + 65536)
+    # CPU: the oracle on a 512 x 512 corner (16 chunks) of the same state
+    st = world.state()
+    temps = world.temperature()
+    ow = om.OracleWorld(512, 512, 128, 3, seed)
+    sub = {k: np.ascontiguousarray(v[:512, :512]) for k, v in st.items()}
+    ow.set_state(sub)
+    ow.set_temperature(np.ascontiguousarray(temps[:512, :512]))
+    t0 = time.perf_counter()
+    od, oo = ow.pack(0)
+    cpu_pack_s = time.perf_counter() - t0
+    ob = om.OracleWorld(512, 512, 128, 3, seed)
+    t0 = time.perf_counter()
+    ob.unpack(od, oo)
+    cpu_unpack_s = time.perf_counter() - t0
+    world.close()
+    back.close()
+    return {"chunks": n, "packed_bytes": int(offs[-1]), "ratio": round(offs[-1] / raw, 4),
+            "pack_ms": round(pack_s * 1e3, 3), "unpack_ms": round(unpack_s * 1e3, 3),
+            "pack_gbs": round(raw / pack_s / 1e9, 2), "unpack_gbs": round(raw / unpack_s / 1e9, 2),
+            "roundtrip_ids_equal": same,
+            "cpu_oracle": {"chunks": len(oo) - 1, "threads": 1, "pack_ms_per_chunk": round(cpu_pack_s * 1e3 / (len(oo) - 1), 3),
+                           "unpack_ms_per_chunk": round(cpu_unpack_s * 1e3 / (len(oo) - 1), 3)},
+            "timing": "host clock around the synchronous host-buffer calls (copies included)"}
 
 
 def e2e_config1(world, args, torch, cells, world_size):
@@ -845,7 +902,7 @@ def main():
     ap.add_argument("--impl", default="fse", choices=["fse", "reference"])
     ap.add_argument("--workload", type=int, default=1, choices=[0, 1, 2, 3, 4])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--only", default=None, choices=["render", "temperature"],
+    ap.add_argument("--only", default=None, choices=["render", "temperature", "pack"],
                     help="run only one side measurement of the 4096x2048 workload (for profiling), print its dict")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -872,7 +929,7 @@ def main():
 
         fse.InitMaterials()
         fse.PushMaterials()
-        fn = {"render": render_config1, "temperature": temperature_config1}[args.only]
+        fn = {"render": render_config1, "temperature": temperature_config1, "pack": pack_config1}[args.only]
         print(json.dumps(fn(fse, torch, 4096, 2048, 1234, 1_000_000)))
         return
     run = {0: bench_config0, 1: bench_config1, 2: bench_config2, 3: bench_config3, 4: bench_config4}[args.workload]

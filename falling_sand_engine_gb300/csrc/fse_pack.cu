@@ -11,14 +11,17 @@
 // they are written as zeros and skipped on reading.
 //
 // Writing. k_pack_stage lays the tile records of a group of chunks out in HBM;
-// k_lz4_encode compresses each block with one warp. The encoder is this
+// k_lz4_parse / k_lz4_plan / k_lz4_emit compress each block, one warp per
+// 24 KB segment (see seg_run). The encoder is this
 // project's own: at each byte p it takes the longest run buf[p + i] ==
 // buf[p + i - d] over 16 fixed distances d (ties to the nearer) when it is at
 // least 4 bytes, else p is a literal -- the distances are multiples of 4 and of
 // the 12-byte record, and one or two chunk rows (1536 bytes) back with the
 // diagonal neighbours. The warp tests 32 positions at once for a 4-byte match
-// and extends all candidate runs 32 bytes at a time; runs whose remaining bytes
-// lie in the zero second layer on both sides are extended to the end at once.
+// and extends all candidate runs 128 bytes at a time, reading the block through
+// an 8 KB shared-memory window that slides along (3 KB behind the position, for
+// the farthest distance); runs whose remaining bytes lie in the zero second
+// layer on both sides are extended to the end at once.
 // On generated worlds the blocks come out smaller than those of the reference's
 // LZ4_compress_fast(..., 10). k_pack_assemble writes headers and blocks.
 //
@@ -83,21 +86,42 @@ __global__ void k_pack_stage(const WorldDev *__restrict__ wd, const MatTable *__
 }
 
 // ----------------------------------------------------------------- encode
-// The block's bytes: buf[0, T) from HBM (4-byte aligned), zeros from T to n.
+constexpr int ENC_WIN = 8192;  // bytes of the block a warp keeps in shared memory
+constexpr int ENC_WARPS = 4;
+constexpr int ENC_BACK = 3072 + 32;  // the farthest distance and a word of slack
+
+// The block's bytes: buf[0, T) from HBM (4-byte aligned), zeros from T to n. The
+// warp reads them through a window of shared memory, [wb, wb + ENC_WIN), which
+// need() moves (all lanes agree on wb) so that it covers the bytes a step reads.
 struct Src {
     const uint32_t *w;  // T / 4 words
     int T;
-    __device__ __forceinline__ uint32_t word(int i) const { return (4 * i < T) ? __ldg(w + i) : 0u; }
+    uint32_t *sw;  // the window, ENC_WIN / 4 words
+    int wb;        // a multiple of 4
+    __device__ __forceinline__ uint32_t gword(int i) const { return (4 * i < T) ? __ldg(w + i) : 0u; }
+    __device__ __forceinline__ void fill(int at) {
+        __syncwarp();
+        wb = at;
+        const int i0 = at >> 2;
+        for (int i = threadIdx.x & 31; i < ENC_WIN / 4; i += 32) sw[i] = gword(i0 + i);
+        __syncwarp();
+    }
+    // the window covers [lo, hi) afterwards (hi - lo <= ENC_WIN - 4)
+    __device__ __forceinline__ void need(int lo, int hi) {
+        if (lo < wb || hi > wb + ENC_WIN) fill(max(lo, 0) & ~3);
+    }
+    __device__ __forceinline__ uint32_t word(int i) const { return sw[i - (wb >> 2)]; }
     __device__ __forceinline__ uint32_t load4(int p) const {
         const int i = p >> 2, s = (p & 3) * 8;
         return __funnelshift_r(word(i), word(i + 1), s);
     }
     __device__ __forceinline__ uint32_t byte(int p) const { return (word(p >> 2) >> ((p & 3) * 8)) & 0xFFu; }
+    __device__ __forceinline__ uint32_t gbyte(int p) const { return (gword(p >> 2) >> ((p & 3) * 8)) & 0xFFu; }
 };
 
 // one sequence: literals [ls, ls + nl), then (when ml > 0) a match of ml bytes at
 // distance off; returns the new output position, or -1 when it would not fit
-__device__ int emit_seq(const Src &s, uint8_t *dst, int op, int cap, int ls, int nl, int off, int ml) {
+__device__ int emit_seq(Src &s, uint8_t *dst, int op, int cap, int ls, int nl, int off, int ml) {
     const int lane = threadIdx.x & 31;
     const int mcode = ml > 0 ? ml - 4 : 0;
     const int lext = nl >= 15 ? (nl - 15) / 255 + 1 : 0;
@@ -124,25 +148,50 @@ __device__ int emit_seq(const Src &s, uint8_t *dst, int op, int cap, int ls, int
         }
     }
     const int lo = op + 1 + lext;
-    for (int i = lane; i < nl; i += 32) dst[lo + i] = (uint8_t)s.byte(ls + i);
+    if (nl + 8 <= ENC_WIN - 8) {  // through the window
+        s.need(ls, ls + nl + 8);
+        for (int i = lane; i < nl; i += 32) dst[lo + i] = (uint8_t)s.byte(ls + i);
+    } else {
+        for (int i = lane; i < nl; i += 32) dst[lo + i] = (uint8_t)s.gbyte(ls + i);
+    }
     return op + need;
 }
 
-// one warp per block: block b of the group (stage words at stage + b * T / 4)
-__global__ void __launch_bounds__(128) k_lz4_encode(const uint32_t *__restrict__ stage, int T, int n, int n_blocks,
-                                                    uint8_t *out, int slot, int *sizes) {
+// Segments: the parse is the sequential greedy parse with every match ending at
+// the latest at the end of the ENC_SEG-byte segment it starts in, so each segment
+// can be parsed by its own warp (a match still refers to any earlier byte of the
+// block). A segment's first sequence takes over the literals left at the end of
+// the segments before it, so writing needs each segment's start of literals
+// (its `anchor`): k_lz4_parse records per segment what writing it costs apart
+// from that first literal run, k_lz4_plan carries the anchors and places the
+// segments, and k_lz4_emit parses again and writes.
+constexpr int ENC_SEG = 24576;
+struct SegInfo {
+    int m;       // sequences with a match that start in the segment
+    int first;   // the position of its first match (when m > 0)
+    int last;    // the position after its last match (when m > 0)
+    int fixed;   // bytes of its sequences apart from the first one's token, length bytes and literals
+};
+__host__ __device__ __forceinline__ int len_bytes(int v) { return v >= 15 ? (v - 15) / 255 + 1 : 0; }
+
+// parse (EMIT = false: fill *info) or parse and write (EMIT = true: from dst[op],
+// literals starting at `anchor`) the segment [a, b) of an n-byte block; returns
+// the output position after the segment's sequences (EMIT) or -1 when they would
+// not fit in cap, and leaves in `anchor` the start of the literals after them
+template <bool EMIT>
+__device__ int seg_run(Src &s, int n, int a, int b, int &anchor, uint8_t *dst, int op, int cap, SegInfo *info) {
     const int lane = threadIdx.x & 31;
-    const int b = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-    if (b >= n_blocks) return;
-    Src s{stage + (size_t)b * (T / 4), T};
-    uint8_t *dst = out + (size_t)b * slot;
     const int mflimit = n - 12, mend = n - 5;
-    int p = 0, anchor = 0, op = 0;
-    while (p <= mflimit && op >= 0) {
+    const int lim = min(mend, b);       // a match ends at the latest here
+    const int stop = min(b, mflimit + 1);  // matches start before here
+    int p = a, m = 0, first = -1, fixed = 0;
+    if (!EMIT) anchor = a;
+    while (p < stop && op >= 0) {
         // the first position of [p, p + 32) with a 4-byte match at some distance
+        s.need(p - ENC_BACK, p + 40);
         const int q = p + lane;
         unsigned cm = 0;
-        if (q <= mflimit) {
+        if (q < stop && q + 4 <= lim) {
             const uint32_t v = s.load4(q);
 #pragma unroll
             for (int k = 0; k < 16; k++) {
@@ -158,26 +207,32 @@ __global__ void __launch_bounds__(128) k_lz4_encode(const uint32_t *__restrict__
         const int f = __ffs(any) - 1;
         const int q0 = p + f;
         unsigned alive = __shfl_sync(FULL, cm, f);
-        // extend every candidate run, 32 bytes per step
+        // extend every candidate run, 128 bytes per step (4 per lane): a run ends at
+        // the first byte that differs or at lim
         int len[16];
 #pragma unroll
         for (int k = 0; k < 16; k++) len[k] = 0;
-        for (int base = 0; alive; base += 32) {
-            const int x = q0 + base + lane;
-            const uint32_t bx = (x < mend) ? s.byte(x) : 0u;
+        for (int base = 0; alive; base += 128) {
+            s.need(q0 + base - ENC_BACK, q0 + base + 136);
+            const int x = q0 + base + 4 * lane;
+            const int vb = min(max(lim - x, 0), 4);  // bytes of this lane before lim
+            const uint32_t over = vb == 4 ? 0u : (vb == 0 ? 0xffffffffu : (0xffffffffu << (8 * vb)));
+            const uint32_t av = s.load4(x);
 #pragma unroll
             for (int k = 0; k < 16; k++) {
                 if (!(alive & (1u << k))) continue;
                 const int d = c_dist[k];
-                if (q0 + base - d >= s.T) {  // both sides in the zero tail from here on: equal to the end
-                    len[k] = mend - q0;
+                if (q0 + base - d >= s.T) {  // both sides in the zero tail from here on: equal up to lim
+                    len[k] = lim - q0;
                     alive &= ~(1u << k);
                     continue;
                 }
-                const bool eq = x < mend && s.byte(x - d) == bx;
-                const unsigned miss = __ballot_sync(FULL, !eq);
+                const uint32_t diff = (av ^ s.load4(x - d)) | over;
+                const unsigned miss = __ballot_sync(FULL, diff != 0);
                 if (miss) {
-                    len[k] = base + __ffs(miss) - 1;
+                    const int fl = __ffs(miss) - 1;
+                    const uint32_t df = __shfl_sync(FULL, diff, fl);
+                    len[k] = base + 4 * fl + ((__ffs(df) - 1) >> 3);
                     alive &= ~(1u << k);
                 }
             }
@@ -189,13 +244,85 @@ __global__ void __launch_bounds__(128) k_lz4_encode(const uint32_t *__restrict__
                 best = len[k];
                 bd = c_dist[k];
             }
-        op = emit_seq(s, dst, op, slot, anchor, q0 - anchor, bd, best);
+        if (EMIT) {
+            op = emit_seq(s, dst, op, cap, anchor, q0 - anchor, bd, best);
+        } else {
+            const int mpart = 2 + len_bytes(best - 4);
+            if (m == 0) {
+                first = q0;
+                fixed += mpart;
+            } else {
+                const int nl = q0 - anchor;
+                fixed += 1 + len_bytes(nl) + nl + mpart;
+            }
+        }
+        m++;
         p = q0 + best;
         anchor = p;
     }
-    if (op >= 0) op = emit_seq(s, dst, op, slot, anchor, n - anchor, 0, 0);
-    __syncwarp();
-    if (lane == 0) sizes[b] = op;  // -1: did not fit (cannot happen within the bound)
+    if (!EMIT && lane == 0) *info = SegInfo{m, first, anchor, fixed};
+    return op;
+}
+
+// phase 1: one warp per (block, segment)
+__global__ void __launch_bounds__(ENC_WARPS * 32) k_lz4_parse(const uint32_t *__restrict__ stage, int T, int n,
+                                                             int n_blocks, SegInfo *info) {
+    __shared__ uint32_t s_win[ENC_WARPS][ENC_WIN / 4];
+    const int nseg = (n + ENC_SEG - 1) / ENC_SEG;
+    const int u = blockIdx.x * ENC_WARPS + threadIdx.x / 32;
+    if (u >= n_blocks * nseg) return;
+    const int b = u / nseg, k = u - b * nseg;
+    Src s{stage + (size_t)b * (T / 4), T, s_win[threadIdx.x / 32], 0};
+    s.fill(max(k * ENC_SEG - ENC_BACK, 0) & ~3);
+    int anchor = 0;
+    seg_run<false>(s, n, k * ENC_SEG, min(n, (k + 1) * ENC_SEG), anchor, nullptr, 0, 0, info + u);
+}
+
+// phase 2: one thread per block: each segment's first literal start and output
+// position, and the block size (-1 when it would exceed cap)
+__global__ void k_lz4_plan(const SegInfo *__restrict__ info, int n, int n_blocks, int cap, int *seg_anchor,
+                           int *seg_out, int *sizes) {
+    const int nseg = (n + ENC_SEG - 1) / ENC_SEG;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < n_blocks; b += gridDim.x * blockDim.x) {
+        long long op = 0;
+        int anchor = 0;
+        for (int k = 0; k < nseg; k++) {
+            const SegInfo &g = info[b * nseg + k];
+            seg_anchor[b * nseg + k] = anchor;
+            seg_out[b * nseg + k] = (int)min(op, (long long)cap);
+            if (g.m > 0) {
+                const int nl = g.first - anchor;
+                op += 1 + len_bytes(nl) + nl + g.fixed;
+                anchor = g.last;
+            }
+        }
+        const int nl = n - anchor;  // the last sequence: literals only
+        op += 1 + len_bytes(nl) + nl;
+        sizes[b] = op <= cap ? (int)op : -1;
+    }
+}
+
+// phase 3: one warp per (block, segment); the last segment also writes the final
+// literals
+__global__ void __launch_bounds__(ENC_WARPS * 32) k_lz4_emit(const uint32_t *__restrict__ stage, int T, int n,
+                                                            int n_blocks, const int *__restrict__ seg_anchor,
+                                                            const int *__restrict__ seg_out,
+                                                            const int *__restrict__ sizes, uint8_t *out, int slot) {
+    __shared__ uint32_t s_win[ENC_WARPS][ENC_WIN / 4];
+    const int nseg = (n + ENC_SEG - 1) / ENC_SEG;
+    const int u = blockIdx.x * ENC_WARPS + threadIdx.x / 32;
+    if (u >= n_blocks * nseg) return;
+    const int b = u / nseg, k = u - b * nseg;
+    if (sizes[b] < 0) return;  // does not fit: nothing is written (cannot happen within the bound)
+    Src s{stage + (size_t)b * (T / 4), T, s_win[threadIdx.x / 32], 0};
+    s.fill(max(k * ENC_SEG - ENC_BACK, 0) & ~3);
+    uint8_t *dst = out + (size_t)b * slot;
+    const int a = k * ENC_SEG, e = min(n, (k + 1) * ENC_SEG);
+    // the segment writes [seg_out[u], its end); it ends where the next one starts
+    const int end = (k + 1 < nseg) ? seg_out[u + 1] : sizes[b];
+    int anchor = seg_anchor[u];
+    int op = seg_run<true>(s, n, a, e, anchor, dst, seg_out[u], end, nullptr);
+    if (k + 1 == nseg && op >= 0) op = emit_seq(s, dst, op, end, anchor, n - anchor, 0, 0);  // the last sequence
 }
 
 // ---------------------------------------------------------------- assemble
@@ -378,6 +505,17 @@ __global__ void k_unpack_scatter(const WorldDev *__restrict__ wd, const MatTable
     }
 }
 
+// the three encoder phases for n_blocks blocks of n bytes (T of them staged)
+void encode_blocks(const uint32_t *stage, int T, int n, int n_blocks, uint8_t *out, int slot, int *sizes,
+                   SegInfo *info, int *anc, int *sout, cudaStream_t s) {
+    const int units = n_blocks * ((n + ENC_SEG - 1) / ENC_SEG);
+    const int grid = (units + ENC_WARPS - 1) / ENC_WARPS;
+    k_lz4_parse<<<grid, ENC_WARPS * 32, 0, s>>>(stage, T, n, n_blocks, info);
+    k_lz4_plan<<<(n_blocks + 127) / 128, 128, 0, s>>>(info, n, n_blocks, slot, anc, sout, sizes);
+    k_lz4_emit<<<grid, ENC_WARPS * 32, 0, s>>>(stage, T, n, n_blocks, anc, sout, sizes, out, slot);
+}
+constexpr int ENC_MAXSEG = (PK_SRC1 + ENC_SEG - 1) / ENC_SEG;
+
 int grid_for(long long work, int per) {
     return (int)std::max(1LL, std::min<long long>((work + per - 1) / per, sm_count() * 16LL));
 }
@@ -407,23 +545,27 @@ int fse_world_pack(fse_world *w, int generation_phase, uint8_t *out, int64_t cap
     const int G = std::min(PK_GROUP, nch);
     uint32_t *stage = nullptr;
     uint8_t *enc1 = nullptr, *enc2 = nullptr, *dout = nullptr;
-    int *sizes = nullptr;
+    int *sizes = nullptr, *anc = nullptr, *sout = nullptr;
+    SegInfo *info = nullptr;
     long long *doffs = nullptr;
     cudaStream_t s = w->stream;
     auto cleanup = [&]() {
-        void *ps[] = {stage, enc1, enc2, dout, sizes, doffs};
+        void *ps[] = {stage, enc1, enc2, dout, sizes, doffs, anc, sout, info};
         for (void *q : ps)
             if (q) cudaFree(q);
     };
     if (cudaMalloc(&stage, (size_t)G * PK_TILES) != cudaSuccess || cudaMalloc(&enc1, (size_t)G * PK_SLOT1) != cudaSuccess ||
         cudaMalloc(&enc2, PK_SLOT2) != cudaSuccess || cudaMalloc(&sizes, (size_t)(G + 1) * sizeof(int)) != cudaSuccess ||
         cudaMalloc(&doffs, (size_t)G * sizeof(long long)) != cudaSuccess ||
-        cudaMalloc(&dout, (size_t)G * (PK_HEADER + PK_SLOT1 + PK_SLOT2)) != cudaSuccess) {
+        cudaMalloc(&dout, (size_t)G * (PK_HEADER + PK_SLOT1 + PK_SLOT2)) != cudaSuccess ||
+        cudaMalloc(&info, (size_t)G * ENC_MAXSEG * sizeof(SegInfo)) != cudaSuccess ||
+        cudaMalloc(&anc, (size_t)G * ENC_MAXSEG * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&sout, (size_t)G * ENC_MAXSEG * sizeof(int)) != cudaSuccess) {
         cleanup();
         return FSE_E_NOMEM;
     }
     // the background block: 64 KB of zeros, the same for every chunk
-    k_lz4_encode<<<1, 128, 0, s>>>(stage, 0, PK_SRC2, 1, enc2, PK_SLOT2, sizes + G);
+    encode_blocks(stage, 0, PK_SRC2, 1, enc2, PK_SLOT2, sizes + G, info, anc, sout, s);
     int size2 = 0;
     std::vector<int> sz(G);
     std::vector<long long> offs(G);
@@ -431,7 +573,7 @@ int fse_world_pack(fse_world *w, int generation_phase, uint8_t *out, int64_t cap
     for (int c0 = 0; c0 < nch && rc == FSE_OK; c0 += G) {
         const int g = std::min(G, nch - c0);
         k_pack_stage<<<grid_for((long long)g * PK_CELLS, 256), 256, 0, s>>>(w->d, g_dev_mt, stage, c0, g);
-        k_lz4_encode<<<(g + 3) / 4, 128, 0, s>>>(stage, PK_TILES, PK_SRC1, g, enc1, PK_SLOT1, sizes);
+        encode_blocks(stage, PK_TILES, PK_SRC1, g, enc1, PK_SLOT1, sizes, info, anc, sout, s);
         if (cudaMemcpyAsync(sz.data(), sizes, g * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
             (c0 == 0 && cudaMemcpyAsync(&size2, sizes + G, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
             cudaStreamSynchronize(s) != cudaSuccess) {
@@ -464,7 +606,7 @@ int fse_world_pack(fse_world *w, int generation_phase, uint8_t *out, int64_t cap
         pos += rel;
     }
     if (rc == FSE_OK) offsets[nch] = pos;
-    count_launches(1 + 3LL * ((nch + G - 1) / G));
+    count_launches(3 + 5LL * ((nch + G - 1) / G));
     cleanup();
     return rc;
 }

@@ -1766,18 +1766,30 @@ static const int PK_DIST[16] = {4, 8, 12, 16, 20, 24, 36, 48, 60, 72, 84, 96, 15
  * longest run buf[p + i] == buf[p + i - d] over the candidate distances d <= p
  * (ties to the smaller d) is taken as a match when it is at least 4 bytes long,
  * else p is a literal. A match starts at most n - 12 and ends at most n - 5 (the
- * block format's end conditions). Returns the block size, or -1 when cap is too
- * small. */
+ * block format's end conditions), and ends at the latest at the end of the
+ * 24576-byte segment it starts in (segments are parsed in parallel on the GPU;
+ * a match still refers to any earlier byte). Returns the block size, or -1 when
+ * cap is too small. */
+#define PK_SEG 24576
 int om_lz4_encode(const uint8_t *buf, int n, uint8_t *dst, int cap) {
     const int mflimit = n - 12, mend = n - 5;
     int p = 0, anchor = 0, op = 0;
     while (p <= mflimit) {
         int best = 0, bd = 0;
+        const int seg_end = (p / PK_SEG + 1) * PK_SEG;
+        const int lim = mend < seg_end ? mend : seg_end;
         for (int k = 0; k < 16 && PK_DIST[k] <= p; k++) {
             const int d = PK_DIST[k];
-            if (memcmp(buf + p, buf + p - d, 4) != 0) continue;
+            if (p + 4 > lim || memcmp(buf + p, buf + p - d, 4) != 0) continue;
             int L = 4;
-            while (p + L < mend && buf[p + L] == buf[p + L - d]) L++;
+            while (p + L + 8 <= lim) { /* 8 bytes at a time: the first differing byte */
+                uint64_t x, y;
+                memcpy(&x, buf + p + L, 8);
+                memcpy(&y, buf + p + L - d, 8);
+                if (x != y) break;
+                L += 8;
+            }
+            while (p + L < lim && buf[p + L] == buf[p + L - d]) L++;
             if (L > best) {
                 best = L;
                 bd = d;
