@@ -187,63 +187,92 @@ __device__ int seg_run(Src &s, int n, int a, int b, int &anchor, uint8_t *dst, i
     int p = a, m = 0, first = -1, fixed = 0;
     if (!EMIT) anchor = a;
     while (p < stop && op >= 0) {
-        // the first position of [p, p + 32) with a 4-byte match at some distance
-        s.need(p - ENC_BACK, p + 40);
-        const int q = p + lane;
-        unsigned cm = 0;
-        if (q < stop && q + 4 <= lim) {
-            const uint32_t v = s.load4(q);
+        // candidates at p itself: lane k < 16 tests distance k
+        s.need(p - ENC_BACK, p + 136);
+        int q0 = p;
+        unsigned cm = __ballot_sync(FULL, lane < 16 && c_dist[lane & 15] <= p && p + 4 <= lim &&
+                                              s.load4(p) == s.load4(p - c_dist[lane & 15]));
+        if (!cm) {
+            // none: the first position of [p + 1, p + 33) with a 4-byte match at some distance
+            const int q = p + 1 + lane;
+            unsigned m = 0;
+            if (q < stop && q + 4 <= lim) {
+                const uint32_t v = s.load4(q);
 #pragma unroll
-            for (int k = 0; k < 16; k++) {
-                const int d = c_dist[k];
-                if (d <= q && s.load4(q - d) == v) cm |= 1u << k;
-            }
-        }
-        const unsigned any = __ballot_sync(FULL, cm != 0);
-        if (!any) {
-            p += 32;
-            continue;
-        }
-        const int f = __ffs(any) - 1;
-        const int q0 = p + f;
-        unsigned alive = __shfl_sync(FULL, cm, f);
-        // extend every candidate run, 128 bytes per step (4 per lane): a run ends at
-        // the first byte that differs or at lim
-        int len[16];
-#pragma unroll
-        for (int k = 0; k < 16; k++) len[k] = 0;
-        for (int base = 0; alive; base += 128) {
-            s.need(q0 + base - ENC_BACK, q0 + base + 136);
-            const int x = q0 + base + 4 * lane;
-            const int vb = min(max(lim - x, 0), 4);  // bytes of this lane before lim
-            const uint32_t over = vb == 4 ? 0u : (vb == 0 ? 0xffffffffu : (0xffffffffu << (8 * vb)));
-            const uint32_t av = s.load4(x);
-#pragma unroll
-            for (int k = 0; k < 16; k++) {
-                if (!(alive & (1u << k))) continue;
-                const int d = c_dist[k];
-                if (q0 + base - d >= s.T) {  // both sides in the zero tail from here on: equal up to lim
-                    len[k] = lim - q0;
-                    alive &= ~(1u << k);
-                    continue;
-                }
-                const uint32_t diff = (av ^ s.load4(x - d)) | over;
-                const unsigned miss = __ballot_sync(FULL, diff != 0);
-                if (miss) {
-                    const int fl = __ffs(miss) - 1;
-                    const uint32_t df = __shfl_sync(FULL, diff, fl);
-                    len[k] = base + 4 * fl + ((__ffs(df) - 1) >> 3);
-                    alive &= ~(1u << k);
+                for (int k = 0; k < 16; k++) {
+                    const int d = c_dist[k];
+                    if (d <= q && s.load4(q - d) == v) m |= 1u << k;
                 }
             }
-        }
-        int best = 0, bd = 0;
-#pragma unroll
-        for (int k = 0; k < 16; k++)
-            if (len[k] > best) {
-                best = len[k];
-                bd = c_dist[k];
+            const unsigned any = __ballot_sync(FULL, m != 0);
+            if (!any) {
+                p += 33;
+                continue;
             }
+            const int f = __ffs(any) - 1;
+            q0 = p + 1 + f;
+            cm = __shfl_sync(FULL, m, f);
+            s.need(q0 - ENC_BACK, q0 + 136);
+        }
+        // run lengths: lane k extends candidate k by itself up to 128 bytes, 4 at a time
+        int L = 0;
+        bool open = false;
+        if (lane < 16 && ((cm >> lane) & 1u)) {
+            const int d = c_dist[lane];
+            const int top = min(lim - q0, 128);
+            L = 4;
+            while (L < top) {
+                const int take = min(4, top - L);
+                uint32_t diff = s.load4(q0 + L) ^ s.load4(q0 + L - d);
+                if (take < 4) diff |= 0xffffffffu << (8 * take);
+                if (diff) {
+                    L += (__ffs(diff) - 1) >> 3;
+                    break;
+                }
+                L += 4;
+            }
+            open = L == 128 && q0 + 128 < lim;
+        }
+        unsigned alive = __ballot_sync(FULL, open);
+        if (alive) {
+            // runs of 128 bytes and more: the whole warp extends them, 128 bytes per step
+            int len[16];
+#pragma unroll
+            for (int k = 0; k < 16; k++) len[k] = 0;
+            for (int base = 128; alive; base += 128) {
+                s.need(q0 + base - ENC_BACK, q0 + base + 136);
+                const int x = q0 + base + 4 * lane;
+                const int vb = min(max(lim - x, 0), 4);  // bytes of this lane before lim
+                const uint32_t over = vb == 4 ? 0u : (vb == 0 ? 0xffffffffu : (0xffffffffu << (8 * vb)));
+                const uint32_t av = s.load4(x);
+#pragma unroll
+                for (int k = 0; k < 16; k++) {
+                    if (!(alive & (1u << k))) continue;
+                    const int d = c_dist[k];
+                    if (q0 + base - d >= s.T) {  // both sides in the zero tail from here on: equal up to lim
+                        len[k] = lim - q0;
+                        alive &= ~(1u << k);
+                        continue;
+                    }
+                    const uint32_t diff = (av ^ s.load4(x - d)) | over;
+                    const unsigned miss = __ballot_sync(FULL, diff != 0);
+                    if (miss) {
+                        const int fl = __ffs(miss) - 1;
+                        const uint32_t df = __shfl_sync(FULL, diff, fl);
+                        len[k] = base + 4 * fl + ((__ffs(df) - 1) >> 3);
+                        alive &= ~(1u << k);
+                    }
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 16; k++)
+                if (open && lane == k) L = len[k];
+        }
+        // the longest run, ties to the nearer distance (smaller k)
+        const unsigned key = (lane < 16 && ((cm >> lane) & 1u)) ? ((unsigned)L << 4) | (unsigned)(15 - lane) : 0u;
+        const unsigned top_key = __reduce_max_sync(FULL, key);
+        const int best = (int)(top_key >> 4);
+        const int bd = c_dist[15 - (int)(top_key & 15u)];
         if (EMIT) {
             op = emit_seq(s, dst, op, cap, anchor, q0 - anchor, bd, best);
         } else {
