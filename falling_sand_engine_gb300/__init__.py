@@ -352,6 +352,19 @@ class World:
             raise FseError(st, "unpack (chunk %d)" % bad.value)
         return phases
 
+    # -- exact checkpoints
+    def checkpoint(self):
+        """Every plane, particle, the tick, seed and ledger, LZ4-compressed: bytes."""
+        nb, size = C.c_int64(0), C.c_int64(0)
+        check(self.lib.fse_world_checkpoint_bound(self.h, C.byref(nb)), "checkpoint_bound")
+        out = np.empty(nb.value, np.uint8)
+        check(self.lib.fse_world_checkpoint(self.h, ptr(out), nb.value, C.byref(size)), "checkpoint")
+        return out[: size.value].copy()
+
+    def restore(self, data):
+        data = np.ascontiguousarray(data, np.uint8)
+        check(self.lib.fse_world_restore(self.h, ptr(data), data.size), "restore")
+
     # -- temperature
     def temperature(self, out=None):
         """MaterialInstance::temperature of every cell as an (H, W) int16 array."""

@@ -56,6 +56,9 @@ SIGNATURES = {
     "fse_world_pack_bound": (_i, [_i, _i, _vp, _vp]),
     "fse_world_pack": (_i, [_vp, _i, _vp, _i64, _vp, _vp]),
     "fse_world_unpack": (_i, [_vp, _vp, _vp, _i, _vp, _vp]),
+    "fse_world_checkpoint_bound": (_i, [_vp, _vp]),
+    "fse_world_checkpoint": (_i, [_vp, _vp, _i64, _vp]),
+    "fse_world_restore": (_i, [_vp, _vp, _i64]),
     "fse_materials_load_lua": (_i, [C.c_char_p, C.POINTER(_i)]),
     "fse_materials_push": (_i, []),
     "fse_material_count": (_i, []),

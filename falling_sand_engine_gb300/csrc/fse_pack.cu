@@ -749,3 +749,287 @@ int fse_world_unpack(fse_world *w, const uint8_t *in, const int64_t *offsets, in
 }
 
 }  // extern "C"
+
+// ============================================================ checkpoints
+// An exact checkpoint of a world: header, then sections (every plane, the particle
+// arrays, the ledger), each as LZ4 blocks of at most CK_BLOCK bytes written by the
+// encoder above. Layout (little-endian):
+//   "FSECKPT1", i32 W, H, chunk, cell_iter, u32 seed, tick, i32 flags (bit 0:
+//   liquid temperatures), i32 particles, i32 sections;
+//   per section: u32 tag, i64 bytes, i32 blocks; per block: i32 raw, i32 packed, bytes.
+namespace fse {
+namespace {
+
+constexpr int CK_BLOCK = 4 << 20;
+constexpr int CK_GROUP = 16;  // blocks encoded or decoded per pass
+constexpr int CK_SLOT = (lz4_bound(CK_BLOCK) + 15) & ~15;
+constexpr int CK_SEGS = (CK_BLOCK + ENC_SEG - 1) / ENC_SEG;
+constexpr char CK_MAGIC[8] = {'F', 'S', 'E', 'C', 'K', 'P', 'T', '1'};
+
+struct CkSection {
+    uint32_t tag;
+    void *dev;
+    int64_t bytes;
+};
+
+// the sections of a world holding np particles, in file order
+std::vector<CkSection> ck_sections(fse_world *w, int np) {
+    const WorldDev &h = w->h;
+    const int64_t n = (int64_t)w->W * w->H, p = np;
+    std::vector<CkSection> v = {{1, h.id, 2 * n}, {2, h.col, 4 * n}, {3, h.sc, 4 * n}, {4, h.fl, n}, {5, h.df, 4 * n}};
+    if (h.tp) v.push_back({6, h.tp, 2 * n});
+    const PartSoA &q = h.p;
+    void *f4[] = {q.x, q.y, q.vx, q.vy, q.ax, q.ay, q.tx, q.ty, q.tf, q.life, q.fade, q.col, q.sc};
+    for (int k = 0; k < 13; k++) v.push_back({(uint32_t)(16 + k), f4[k], 4 * p});
+    v.push_back({29, q.id, 2 * p});
+    v.push_back({30, q.fl, p});
+    v.push_back({31, q.bits, p});
+    if (h.tp) v.push_back({32, q.tp, 2 * p});
+    v.push_back({40, h.ledger, (int64_t)LED_ROWS * MAXMAT * 8});
+    return v;
+}
+
+struct CkScratch {
+    uint32_t *stage = nullptr;
+    uint8_t *enc = nullptr;
+    int *sizes = nullptr, *anc = nullptr, *sout = nullptr, *status = nullptr;
+    SegInfo *info = nullptr;
+    uint8_t *din = nullptr;
+    long long *doff = nullptr;
+    int *dlen = nullptr;
+    bool ok() const { return stage && enc && sizes && anc && sout && status && info && din && doff && dlen; }
+    void alloc() {
+        cudaMalloc(&stage, (size_t)CK_GROUP * CK_BLOCK + 16);  // + a zeroed word after the data
+        cudaMalloc(&enc, (size_t)CK_GROUP * CK_SLOT);
+        cudaMalloc(&sizes, (CK_GROUP + 1) * sizeof(int));
+        cudaMalloc(&anc, (size_t)CK_GROUP * CK_SEGS * sizeof(int));
+        cudaMalloc(&sout, (size_t)CK_GROUP * CK_SEGS * sizeof(int));
+        cudaMalloc(&status, (CK_GROUP + 1) * sizeof(int));
+        cudaMalloc(&info, (size_t)CK_GROUP * CK_SEGS * sizeof(SegInfo));
+        cudaMalloc(&din, (size_t)CK_GROUP * CK_SLOT);
+        cudaMalloc(&doff, (CK_GROUP + 1) * sizeof(long long));
+        cudaMalloc(&dlen, (CK_GROUP + 1) * sizeof(int));
+    }
+    void release() {
+        void *ps[] = {stage, enc, sizes, anc, sout, status, info, din, doff, dlen};
+        for (void *q : ps)
+            if (q) cudaFree(q);
+    }
+};
+
+// host writer with a capacity check
+struct Out {
+    uint8_t *p;
+    int64_t cap, n = 0;
+    bool room(int64_t k) const { return n + k <= cap; }
+    template <class T>
+    bool put(const T &v) {
+        if (!room(sizeof(T))) return false;
+        memcpy(p + n, &v, sizeof(T));
+        n += sizeof(T);
+        return true;
+    }
+};
+
+int ck_write_section(const CkSection &sec, Out &o, CkScratch &sc, cudaStream_t s) {
+    const int nblk = (int)((sec.bytes + CK_BLOCK - 1) / CK_BLOCK);
+    if (!o.put(sec.tag) || !o.put((int64_t)sec.bytes) || !o.put((int32_t)nblk)) return FSE_E_CAPACITY;
+    std::vector<int> sz(CK_GROUP);
+    for (int g0 = 0; g0 < nblk; g0 += CK_GROUP) {
+        const int g = std::min(CK_GROUP, nblk - g0);
+        const int64_t lo = (int64_t)g0 * CK_BLOCK, hi = std::min(sec.bytes, (int64_t)(g0 + g) * CK_BLOCK);
+        const int64_t span = hi - lo;
+        if (cudaMemcpyAsync(sc.stage, (const uint8_t *)sec.dev + lo, (size_t)span, cudaMemcpyDeviceToDevice, s) !=
+                cudaSuccess ||
+            cudaMemsetAsync((uint8_t *)sc.stage + span, 0, 4, s) != cudaSuccess)  // word-aligned tail
+            return FSE_E_CUDA;
+        const int full = (int)(span / CK_BLOCK), tail = (int)(span - (int64_t)full * CK_BLOCK);
+        if (full) encode_blocks(sc.stage, CK_BLOCK, CK_BLOCK, full, sc.enc, CK_SLOT, sc.sizes, sc.info, sc.anc, sc.sout, s);
+        if (tail)
+            encode_blocks(sc.stage + (size_t)full * (CK_BLOCK / 4), (tail + 3) & ~3, tail, 1,
+                          sc.enc + (size_t)full * CK_SLOT, CK_SLOT, sc.sizes + full, sc.info, sc.anc, sc.sout, s);
+        count_launches(3LL * ((full ? 1 : 0) + (tail ? 1 : 0)));
+        if (cudaMemcpyAsync(sz.data(), sc.sizes, g * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return FSE_E_CUDA;
+        for (int b = 0; b < g; b++) {
+            const int raw = b < full ? CK_BLOCK : tail;
+            if (sz[b] < 0) return FSE_E_CUDA;
+            if (!o.put((int32_t)raw) || !o.put((int32_t)sz[b]) || !o.room(sz[b])) return FSE_E_CAPACITY;
+            if (cudaMemcpyAsync(o.p + o.n, sc.enc + (size_t)b * CK_SLOT, (size_t)sz[b], cudaMemcpyDeviceToHost, s) !=
+                cudaSuccess)
+                return FSE_E_CUDA;
+            o.n += sz[b];
+        }
+        if (cudaStreamSynchronize(s) != cudaSuccess) return FSE_E_CUDA;
+    }
+    return FSE_OK;
+}
+
+// host reader with bounds checks
+struct In {
+    const uint8_t *p;
+    int64_t size, n = 0;
+    template <class T>
+    bool get(T &v) {
+        if (n + (int64_t)sizeof(T) > size) return false;
+        memcpy(&v, p + n, sizeof(T));
+        n += sizeof(T);
+        return true;
+    }
+};
+
+int ck_read_section(const CkSection &sec, In &in, CkScratch &sc, cudaStream_t s) {
+    uint32_t tag;
+    int64_t bytes;
+    int32_t nblk;
+    if (!in.get(tag) || !in.get(bytes) || !in.get(nblk) || tag != sec.tag || bytes != sec.bytes ||
+        nblk != (int32_t)((bytes + CK_BLOCK - 1) / CK_BLOCK))
+        return FSE_E_INVAL;
+    std::vector<long long> off(CK_GROUP);
+    std::vector<int> len(CK_GROUP), st(CK_GROUP);
+    for (int g0 = 0; g0 < nblk; g0 += CK_GROUP) {
+        const int g = std::min((int)CK_GROUP, nblk - g0);
+        long long pos = 0;
+        int full = 0, tail = 0;
+        for (int b = 0; b < g; b++) {
+            int32_t raw, packed;
+            if (!in.get(raw) || !in.get(packed)) return FSE_E_INVAL;
+            const int64_t want = std::min((int64_t)CK_BLOCK, bytes - (int64_t)(g0 + b) * CK_BLOCK);
+            if (raw != want || packed <= 0 || packed > CK_SLOT || in.n + packed > in.size) return FSE_E_INVAL;
+            if (cudaMemcpyAsync(sc.din + pos, in.p + in.n, (size_t)packed, cudaMemcpyHostToDevice, s) != cudaSuccess)
+                return FSE_E_CUDA;
+            in.n += packed;
+            off[b] = pos;
+            len[b] = packed;
+            pos += packed;
+            if (raw == CK_BLOCK)
+                full++;
+            else
+                tail = raw;
+        }
+        if (cudaMemcpyAsync(sc.doff, off.data(), g * sizeof(long long), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(sc.dlen, len.data(), g * sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess)
+            return FSE_E_CUDA;
+        uint8_t *dst = (uint8_t *)sec.dev + (int64_t)g0 * CK_BLOCK;
+        if (full)
+            k_lz4_decode<<<(full + DEC_WARPS - 1) / DEC_WARPS, DEC_WARPS * 32, 0, s>>>(sc.din, sc.doff, sc.dlen, full,
+                                                                                    CK_BLOCK, dst, CK_BLOCK, sc.status);
+        if (tail)
+            k_lz4_decode<<<1, DEC_WARPS * 32, 0, s>>>(sc.din, sc.doff + full, sc.dlen + full, 1, tail,
+                                                     dst + (size_t)full * CK_BLOCK, CK_BLOCK, sc.status + full);
+        count_launches((full ? 1 : 0) + (tail ? 1 : 0));
+        if (cudaMemcpyAsync(st.data(), sc.status, g * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return FSE_E_CUDA;
+        for (int b = 0; b < g; b++)
+            if (st[b] != (b < full ? CK_BLOCK : tail)) return FSE_E_INVAL;
+    }
+    return FSE_OK;
+}
+
+}  // namespace
+}  // namespace fse
+
+extern "C" {
+
+int fse_world_checkpoint_bound(fse_world *w, int64_t *out_bytes) {
+    if (!w || !out_bytes) return FSE_E_INVAL;
+    int32_t info[8];
+    int rc = fse_world_info(w, info);
+    if (rc) return rc;
+    int64_t total = 64;
+    for (const CkSection &sec : ck_sections(w, info[6])) {  // a block never grows past lz4_bound(raw)
+        const int64_t nblk = (sec.bytes + CK_BLOCK - 1) / CK_BLOCK;
+        total += 16 + nblk * 24 + sec.bytes + sec.bytes / 255;
+    }
+    *out_bytes = total;
+    return FSE_OK;
+}
+
+int fse_world_checkpoint(fse_world *w, uint8_t *out, int64_t cap, int64_t *out_size) {
+    if (!w || !out || !out_size) return FSE_E_INVAL;
+    int32_t info[8];
+    int rc = fse_world_info(w, info);  // also waits for the world's work
+    if (rc) return rc;
+    const std::vector<CkSection> secs = ck_sections(w, info[6]);
+    Out o{out, cap};
+    if (!o.room(8)) return FSE_E_CAPACITY;
+    memcpy(out, CK_MAGIC, 8);
+    o.n = 8;
+    const int32_t flags = w->h.tp ? 1 : 0;
+    if (!o.put((int32_t)w->W) || !o.put((int32_t)w->H) || !o.put((int32_t)w->C) || !o.put((int32_t)w->cell_iter) ||
+        !o.put((uint32_t)w->h.seed) || !o.put((uint32_t)info[5]) || !o.put(flags) || !o.put((int32_t)info[6]) ||
+        !o.put((int32_t)secs.size()))
+        return FSE_E_CAPACITY;
+    CkScratch sc;
+    sc.alloc();
+    if (!sc.ok()) {
+        sc.release();
+        return FSE_E_NOMEM;
+    }
+    for (const CkSection &sec : secs) {
+        rc = ck_write_section(sec, o, sc, w->stream);
+        if (rc) break;
+    }
+    sc.release();
+    if (rc) return rc;
+    *out_size = o.n;
+    return FSE_OK;
+}
+
+int fse_world_restore(fse_world *w, const uint8_t *in, int64_t size) {
+    if (!w || !in || size < 0) return FSE_E_INVAL;
+    FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
+    int rc = FSE_OK;
+    In r{in, size};
+    char magic[8];
+    int32_t W, H, C, it, flags, np, nsec;
+    uint32_t seed, tick;
+    if (size < 8) return FSE_E_INVAL;
+    memcpy(magic, in, 8);
+    r.n = 8;
+    if (memcmp(magic, CK_MAGIC, 8) != 0 || !r.get(W) || !r.get(H) || !r.get(C) || !r.get(it) || !r.get(seed) ||
+        !r.get(tick) || !r.get(flags) || !r.get(np) || !r.get(nsec))
+        return FSE_E_INVAL;
+    if (W != w->W || H != w->H || C != w->C || it != w->cell_iter || np < 0) return FSE_E_INVAL;
+    if ((flags & 1) && !w->h.tp) return FSE_E_STATE;  // liquid temperatures need FSE_CFG_TEMPERATURE
+    if (np > w->part_cap) return FSE_E_CAPACITY;
+    // sections in file order; a world that keeps liquid temperatures restores a file
+    // without them as 0
+    std::vector<CkSection> secs = ck_sections(w, np);
+    if (!(flags & 1)) {
+        std::vector<CkSection> keep;
+        for (const CkSection &sc : secs)
+            if (sc.tag != 6 && sc.tag != 32) keep.push_back(sc);
+        secs.swap(keep);
+        if (w->h.tp && cudaMemsetAsync(w->h.tp, 0, (size_t)w->W * w->H * 2, w->stream) != cudaSuccess)
+            return FSE_E_CUDA;
+    }
+    if (nsec != (int32_t)secs.size()) return FSE_E_INVAL;
+    CkScratch sc;
+    sc.alloc();
+    if (!sc.ok()) {
+        sc.release();
+        return FSE_E_NOMEM;
+    }
+    for (const CkSection &sec : secs) {
+        rc = ck_read_section(sec, r, sc, w->stream);
+        if (rc) break;
+    }
+    sc.release();
+    if (rc) return rc;
+    // counters: live particles and the tick; nothing in flight, no error
+    int32_t ctr[16] = {0};
+    ctr[1] = np;
+    ctr[6] = (int32_t)tick;
+    w->seed = seed;
+    w->h.seed = seed;
+    FSE_CUDA_TRY(cudaMemcpyAsync(w->ctr, ctr, sizeof(ctr), cudaMemcpyHostToDevice, w->stream));
+    FSE_CUDA_TRY(cudaMemcpyAsync(w->d, &w->h, sizeof(WorldDev), cudaMemcpyHostToDevice, w->stream));
+    if (w->h.dirty) FSE_CUDA_TRY(cudaMemsetAsync(w->h.dirty, 1, (size_t)w->W * w->H, w->stream));
+    FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
+    return FSE_OK;
+}
+
+}  // extern "C"

@@ -213,6 +213,18 @@ int fse_world_pack(fse_world *world, int generation_phase, uint8_t *out, int64_t
 int fse_world_unpack(fse_world *world, const uint8_t *in, const int64_t *offsets, int n_chunks, int8_t *out_phases,
                      int *out_bad_chunk);
 
+/* Exact checkpoint of a world (the .pack files keep only material, colour and
+ * temperature): every plane, the particle list, the tick counter, seed and ledger,
+ * as LZ4 blocks written by the .pack encoder. A world restored from it (same
+ * size, chunk size and cell_iter; particle capacity at least the checkpoint's
+ * particles) continues bit for bit as the original would. Liquid temperatures are
+ * saved when the world keeps them; restoring them needs FSE_CFG_TEMPERATURE
+ * (FSE_E_STATE otherwise). Malformed input (sizes, block lengths, LZ4 tokens)
+ * returns FSE_E_INVAL; like the .pack files the format has no checksum. */
+int fse_world_checkpoint_bound(fse_world *world, int64_t *out_bytes);
+int fse_world_checkpoint(fse_world *world, uint8_t *out, int64_t cap, int64_t *out_size);
+int fse_world_restore(fse_world *world, const uint8_t *in, int64_t size);
+
 /* world::tick(), n times (no particle step in between) */
 int fse_world_tick(fse_world *world, int n_ticks);
 /* world::tickCells() */

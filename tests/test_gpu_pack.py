@@ -112,3 +112,81 @@ def test_unpack_rejects_malformed(fse, oracle_mod):
         gs, os_ = world.state(), ob.state()
         for key in ("id", "colour", "scalar"):
             assert np.array_equal(gs[key], os_[key]), (key, k)
+
+
+def _same_world(fse, a, b, temperature):
+    for k, v in a.state().items():
+        assert np.array_equal(v, b.state()[k]), k
+    pa, pb = a.particles(), b.particles()
+    assert pa.tobytes() == pb.tobytes()
+    assert np.array_equal(a.ledger(), b.ledger())
+    assert a.tick_count == b.tick_count
+    if temperature:
+        assert np.array_equal(a.temperature(), b.temperature())
+
+
+@pytest.mark.parametrize("temperature", [False, True])
+def test_checkpoint_restore_is_exact(fse, temperature):
+    """A world restored from a checkpoint (into a world made with another seed)
+    continues bit for bit as the original: planes, particles, ledger, tick."""
+    kw = dict(temperature=True, temperature_step=True) if temperature else {}
+    a = fse.World(320, 256, seed=21, **kw)
+    a.generate(fse.GEN_MIX, 21)
+    rng = np.random.default_rng(0)
+    p = np.zeros(2000, fse.PARTICLE_DTYPE)
+    p["x"] = rng.uniform(0, 320, 2000)
+    p["y"] = rng.uniform(0, 200, 2000)
+    p["vx"] = rng.normal(0, 2, 2000)
+    p["vy"] = rng.normal(0, 2, 2000)
+    p["ay"] = 0.1
+    p["id"] = 2
+    p["colour"] = 0xFFFF00
+    a.addCell(p)
+    a.step(7)
+    data = a.checkpoint()
+    b = fse.World(320, 256, seed=999, **kw)
+    b.restore(data)
+    _same_world(fse, a, b, temperature)
+    a.step(9)
+    b.step(9)
+    _same_world(fse, a, b, temperature)
+    # a checkpoint of a 5 Mcell world spans several 4 MB blocks per plane
+    big = fse.World(2560, 2048, seed=3, **kw)
+    big.generate(fse.GEN_MIX, 3)
+    big.step(2)
+    c = fse.World(2560, 2048, seed=4, **kw)
+    c.restore(big.checkpoint())
+    big.step(2)
+    c.step(2)
+    _same_world(fse, big, c, temperature)
+
+
+def test_restore_rejects_mismatch_and_corruption(fse):
+    a = fse.World(256, 192, seed=1, temperature=True)
+    a.generate(fse.GEN_MIX, 1)
+    a.step(3)
+    data = a.checkpoint()
+    with pytest.raises(fse.FseError):
+        fse.World(256, 256, seed=1, temperature=True).restore(data)  # another size
+    with pytest.raises(fse.FseError):
+        fse.World(256, 192, seed=1).restore(data)  # liquid temperatures need FSE_CFG_TEMPERATURE
+    for cut in (10, 60, len(data) // 2, len(data) - 1):
+        with pytest.raises(fse.FseError):
+            fse.World(256, 192, seed=1, temperature=True).restore(data[:cut])
+    # header 44 bytes; first section: tag @44, bytes @48, blocks @56; first block: raw @60, packed @64, data @68
+    # (the format has no checksum, like .pack files: a changed literal byte inside a block
+    # decodes; lengths, sizes and tokens are checked)
+    for at, val in ((0, 0), (48, 1), (60, 7), (64, 0x7FFFFFF0), (68, 0xFF)):
+        bad = data.copy()
+        bad[at] = val if val <= 0xFF else 0
+        if val > 0xFF:
+            bad[at:at + 4] = np.array([val], "<i4").view(np.uint8)
+        with pytest.raises(fse.FseError):
+            fse.World(256, 192, seed=1, temperature=True).restore(bad)
+    # a checkpoint without liquid temperatures restores into a world that keeps them as 0
+    d = fse.World(256, 192, seed=1)
+    d.generate(fse.GEN_MIX, 1)
+    e = fse.World(256, 192, seed=1, temperature=True)
+    e.restore(d.checkpoint())
+    types = np.array([fse.material_get(i)[0] for i in range(fse.material_count())])
+    assert not e.temperature()[types[e.state()["id"]] == fse.SOUP].any()
