@@ -12,6 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libfse_oracle.so")
 REF_TEMPERATURE_PATH = os.path.join(HERE, "_ref", "libref_temperature.so")
 REF_LZ4_PATH = os.path.join(HERE, "_ref", "liblz4ref.so")
+REF_CELLS_PATH = os.path.join(HERE, "_ref", "libref_cells.so")
 REFERENCE_WORLD_CPP = "/root/reference/source/engine/world.cpp"
 
 PARTICLE_DTYPE = np.dtype(
@@ -434,3 +435,36 @@ class ReferenceLZ4:
         dst = np.zeros(max(size, 1), np.uint8)
         m = self.lib.LZ4_decompress_safe(_ptr(src), _ptr(dst), len(src), size)
         return dst[: max(m, 0)].copy(), m
+
+
+def build_reference_cells(force=False):
+    """Compile the reference's own world::tickCells (oracle/Makefile `ref`); None without the tree."""
+    if not os.path.exists(REFERENCE_WORLD_CPP):
+        return None
+    if force or not os.path.exists(REF_CELLS_PATH) or os.path.getmtime(REF_CELLS_PATH) < os.path.getmtime(
+            os.path.join(HERE, "ref_particles.cpp")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    return REF_CELLS_PATH
+
+
+def reference_tick_cells(lib_path, ids, colours, amounts, mat_types, parts):
+    """One world::tickCells of the compiled reference: (ids, colours, amounts, dirty, survivors)."""
+    lib = C.CDLL(lib_path)
+    f = lib.ref_tick_cells
+    f.restype = C.c_int
+    f.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                  C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    h, w = ids.shape
+    i2 = np.ascontiguousarray(ids, np.uint16).copy()
+    c2 = np.ascontiguousarray(colours, np.uint32).copy()
+    a2 = np.ascontiguousarray(amounts, np.int32).copy()
+    d2 = np.zeros((h, w), np.uint8)
+    mt = np.ascontiguousarray(mat_types, np.int32)
+    pin = np.ascontiguousarray(parts, PARTICLE_DTYPE)
+    pout = np.zeros(max(len(pin), 1), PARTICLE_DTYPE)
+    nout = C.c_int(0)
+    rc = f(w, h, _ptr(i2), _ptr(c2), _ptr(a2), _ptr(d2), _ptr(mt), len(mt), _ptr(pin), len(pin), _ptr(pout),
+           C.byref(nout))
+    if rc != 0:
+        raise ValueError("ref_tick_cells failed")
+    return i2, c2, a2, d2, pout[: nout.value].copy()
