@@ -457,18 +457,17 @@ __device__ int warp_lz4_decode(const uint8_t *src, int n, uint8_t *dst, int cap,
         for (int done = 0; done < ml;) {
             const int m = from_ring ? min(ml - done, DEC_RING - off) : ml - done;
             const int base = op + done;
+            // sidx = j mod off, kept without a division in the loop: j grows by 32,
+            // which is step = 32 mod off
             int sidx = off >= 32 ? lane : lane % off;
+            const int step = off >= 32 ? 32 : 32 % off;
             for (int j = lane; j < m; j += 32) {
                 const int from = base - off + sidx;
                 const uint8_t v = from_ring ? ring[from & (DEC_RING - 1)] : dst[from];
                 dst[base + j] = v;
                 ring[(base + j) & (DEC_RING - 1)] = v;
-                sidx += 32;
-                if (off >= 32) {
-                    if (sidx >= off) sidx -= off;
-                } else {
-                    sidx %= off;
-                }
+                sidx += step;
+                if (sidx >= off) sidx -= off;
             }
             __syncwarp();
             done += m;

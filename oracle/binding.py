@@ -13,6 +13,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libfse_oracle.so")
 REF_TEMPERATURE_PATH = os.path.join(HERE, "_ref", "libref_temperature.so")
 REF_LZ4_PATH = os.path.join(HERE, "_ref", "liblz4ref.so")
 REF_CELLS_PATH = os.path.join(HERE, "_ref", "libref_cells.so")
+REF_RENDER_PATH = os.path.join(HERE, "_ref", "libref_render.so")
 REFERENCE_WORLD_CPP = "/root/reference/source/engine/world.cpp"
 
 PARTICLE_DTYPE = np.dtype(
@@ -102,6 +103,8 @@ class Oracle:
                 "om_render_cells": (None, [vp]),
                 "om_render_get": (None, [vp, i32, vp]),
                 "om_render_dirty_get": (None, [vp, vp]),
+                "om_render_set": (None, [vp, vp, vp, vp]),
+                "om_render_pflow_get": (None, [vp, vp]),
                 "om_physics_check": (i32, [vp, i32, i32, vp, vp, i32]),
                 "om_islands": (i32, [vp, i32, i32, vp, i32]),
                 "om_material_set_conduction": (i32, [i32, u32, C.c_float, C.c_float]),
@@ -323,6 +326,17 @@ class OracleWorld:
         self.lib.om_render_get(self.h_, which, _ptr(out))
         return out
 
+    def render_set(self, dirty, flow, pflow):
+        d = np.ascontiguousarray(dirty, np.uint8)
+        f = np.ascontiguousarray(flow, np.int32)
+        p = np.ascontiguousarray(pflow, np.float32)
+        self.lib.om_render_set(self.h_, _ptr(d), _ptr(f), _ptr(p))
+
+    def render_pflow(self):
+        out = np.zeros((self.h, self.w, 2), np.float32)
+        self.lib.om_render_pflow_get(self.h_, _ptr(out))
+        return out
+
     def render_dirty_plane(self):
         out = np.zeros((self.h, self.w), np.uint8)
         self.lib.om_render_dirty_get(self.h_, _ptr(out))
@@ -468,3 +482,35 @@ def reference_tick_cells(lib_path, ids, colours, amounts, mat_types, parts):
     if rc != 0:
         raise ValueError("ref_tick_cells failed")
     return i2, c2, a2, d2, pout[: nout.value].copy()
+
+
+def build_reference_render(force=False):
+    """Compile the reference's own dirty-pixel loop of game::tick (oracle/Makefile `ref`)."""
+    if not os.path.exists(REFERENCE_WORLD_CPP):
+        return None
+    if force or not os.path.exists(REF_RENDER_PATH) or os.path.getmtime(REF_RENDER_PATH) < os.path.getmtime(
+            os.path.join(HERE, "ref_render.cpp")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    return REF_RENDER_PATH
+
+
+def reference_render_dirty(lib_path, ids, colours, dirty, flow_x, flow_y, prev_x, prev_y, mats, fire_id):
+    """One pass of the reference's dirty-pixel loop: textures (pixels, fire, emission, flow
+    as (H, W, 4) bytes), the updated flows and smoothed flows, the u16 moving counts."""
+    lib = C.CDLL(lib_path)
+    f = lib.ref_render_dirty
+    f.restype = C.c_int
+    f.argtypes = [C.c_int] * 2 + [C.c_void_p] * 7 + [C.c_int] + [C.c_void_p] * 4 + [C.c_int] + [C.c_void_p] * 5
+    h, w = ids.shape
+    arrs = [np.ascontiguousarray(a, dt).copy() for a, dt in
+            ((ids, np.uint16), (colours, np.uint32), (dirty, np.uint8), (flow_x, np.float32), (flow_y, np.float32),
+             (prev_x, np.float32), (prev_y, np.float32))]
+    types, alpha, emit, iters = [np.ascontiguousarray(a, dt) for a, dt in
+                                 zip(mats, (np.int32, np.uint8, np.uint32, np.int32))]
+    tex = [np.zeros((h, w, 4), np.uint8) for _ in range(4)]
+    moving = np.zeros(len(types), np.uint16)
+    rc = f(w, h, *[_ptr(a) for a in arrs], len(types), _ptr(types), _ptr(alpha), _ptr(emit), _ptr(iters), fire_id,
+           *[_ptr(t) for t in tex], _ptr(moving))
+    if rc != 0:
+        raise ValueError("ref_render_dirty failed")
+    return tex, arrs[3], arrs[4], arrs[5], arrs[6], moving

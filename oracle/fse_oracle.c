@@ -2055,6 +2055,17 @@ void om_render_get(const om_world *w, int which, uint32_t *out) {
     memcpy(out, w->tex[which], (size_t)w->W * w->H * 4);
 }
 
+/* set the dirty marks, the tick's flow sums (Q16.16 pairs) and the smoothed flows */
+void om_render_set(om_world *w, const uint8_t *dirty, const int32_t *flow, const float *pflow) {
+    if (!w->dirty) return;
+    size_t n = (size_t)w->W * w->H;
+    if (dirty) memcpy(w->dirty, dirty, n);
+    if (flow) memcpy(w->flow, flow, 2 * n * sizeof(int32_t));
+    if (pflow) memcpy(w->pflow, pflow, 2 * n * sizeof(float));
+}
+void om_render_pflow_get(const om_world *w, float *out) {
+    if (w->pflow) memcpy(out, w->pflow, 2 * (size_t)w->W * w->H * sizeof(float));
+}
 void om_render_dirty_get(const om_world *w, uint8_t *out) {
     if (w->dirty) memcpy(out, w->dirty, (size_t)w->W * w->H);
 }

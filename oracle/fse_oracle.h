@@ -156,6 +156,8 @@ void om_render_dirty(om_world *w, int64_t *moving);
 void om_render_cells(om_world *w);
 void om_render_get(const om_world *w, int which, uint32_t *out);
 void om_render_dirty_get(const om_world *w, uint8_t *out);
+void om_render_set(om_world *wd, const uint8_t *dirty, const int32_t *flow, const float *pflow);
+void om_render_pflow_get(const om_world *wd, float *out);
 
 /* solid islands: world::physicsCheck (world.cpp:3330-3445) and every region at once */
 typedef struct om_island {
