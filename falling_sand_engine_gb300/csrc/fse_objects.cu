@@ -2,11 +2,9 @@
 // (source/engine/game.cpp:1768-1814), readback after it (game.cpp:1896-1983) and
 // the per-tick OBJECT-cell export to the host-side rigid-body solver.
 //
-// Stamp and readback resolve body tiles in rounds inside one CTA per world: each
-// open tile picks its first usable offset against the grid at the start of the
-// round, the lowest (body, tile) index wins a contested cell, the rest look again.
-// Lists stay in (body, tile) order, so displaced particles are appended in a fixed
-// order.
+// Stamp and readback resolve body tiles inside one CTA per world by deferred
+// acceptance (see k_obj_rounds): the result is the reference's tile-by-tile one,
+// and displaced particles are appended in (body, tile) order.
 #include <algorithm>
 #include <vector>
 
@@ -48,163 +46,223 @@ __device__ __forceinline__ int block_scan_excl(int v, int *s, int *total) {
     return before + inc - v;
 }
 
-// mode 0 = stamp, 1 = readback. open/next: 2 lists of total tiles; prefix[b] =
-// first global tile index of body b.
+__device__ __forceinline__ int body_of(const uint32_t *__restrict__ prefix, int nb, uint32_t g) {
+    int lo = 0, hi = nb - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (prefix[mid] <= g) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// mode 0 = stamp, 1 = readback; prefix[b] = first global tile index of body b.
+// ptr (per tile: the next offset to try, 5 = none left) and held (per tile: the
+// cell it holds, -1 = none) are scratch of prefix[nb] entries.
+//
+// The reference walks the tiles one after another (bodies in order, tx-major,
+// ty-minor): each takes the first of its five cells that is usable at that moment
+// (stamp: AIR, SAND or SOUP; readback: the body's material), and a taken cell is
+// not usable by the tiles after it. Here the tiles propose in parallel, each cell
+// keeping its lowest proposer (claim = atomicMin of the tile index) and displacing
+// higher ones, a rejected or displaced tile proposing its next cell: deferred
+// acceptance with the same priority order at every cell, whose outcome is the
+// sequential one. Usability is read from the grid before any write, since only the
+// taking itself makes a cell unusable. Displaced particles are then appended in
+// tile order.
+__device__ __forceinline__ bool tile_usable(const WorldDev &w, const MatTable *__restrict__ mt, int mode, int c,
+                                            int body_id) {
+    const int cid = w.id[c];
+    if (mode == 0) {
+        const int ty = mt_type(mt->a[cid]);
+        return ty == T_AIR || ty == T_SAND || ty == T_SOUP;
+    }
+    return cid == body_id;
+}
+
+// tile g proposes its next usable cell from ptr[g] on (a cell claimed by an
+// earlier tile is skipped for good); returns the proposer displaced from that cell
+// (or 0xffffffff), and records the cell in held[g] (-1 when none is left)
+__device__ __forceinline__ uint32_t tile_propose(const WorldDev &w, const MatTable *__restrict__ mt,
+                                                 const fse_body *__restrict__ bodies,
+                                                 const uint32_t *__restrict__ prefix, int nb, int mode, uint32_t g,
+                                                 uint32_t *ptr, int32_t *held, uint32_t *claim) {
+    const int bi = body_of(prefix, nb, g);
+    const fse_body b = bodies[bi];
+    const int t = (int)(g - prefix[bi]);
+    int wx, wy;
+    body_pos(b, t / b.h, t % b.h, wx, wy);
+    int d = (int)ptr[g];
+    for (; d < 5; d++) {
+        const int xd = wx + c_dirs[d][0], yd = wy + c_dirs[d][1];
+        if (xd < 0 || yd < 0 || xd >= w.W || yd >= w.H) continue;
+        const int c = yd * w.W + xd;
+        if (!tile_usable(w, mt, mode, c, (int)b.id) || claim[c] < g) continue;
+        const uint32_t old = atomicMin(&claim[c], g);
+        ptr[g] = (uint32_t)d;
+        held[g] = c;
+        return old;
+    }
+    ptr[g] = 5;
+    held[g] = -1;
+    return 0xffffffffu;
+}
+
+// mode 0 = stamp, 1 = readback; prefix[b] = first global tile index of body b.
+// Scratch of prefix[nb] entries: ptr (the next offset to try, 5 = none left), held
+// (the cell a tile holds, -1 = none), two work lists and a queued mark.
+//
+// The reference walks the tiles one after another (bodies in order, tx-major,
+// ty-minor): each takes the first of its five cells that is usable at that moment
+// (stamp: AIR, SAND or SOUP; readback: the body's material), and a taken cell is
+// not usable by the tiles after it. Here the tiles propose in parallel, each cell
+// keeping its lowest proposer (claim = atomicMin of the tile index) and displacing
+// higher ones, a rejected or displaced tile proposing its next cell: deferred
+// acceptance with the same priority order at every cell, whose outcome is the
+// sequential one. Usability is read from the grid before any write, since only the
+// taking itself makes a cell unusable. After one round over all tiles, only the
+// tiles that lost a cell and the holders their proposals displace are looked at.
+// Displaced particles are then appended in tile order.
 __global__ void __launch_bounds__(1024) k_obj_rounds(WorldDev *wd, const MatTable *__restrict__ mt, fse_body *bodies,
-                                                     const uint32_t *__restrict__ prefix, int nb, uint32_t *open,
-                                                     uint32_t *next, int32_t *target, uint32_t *claim, int mode,
+                                                     const uint32_t *__restrict__ prefix, int nb, uint32_t *ptr,
+                                                     int32_t *held, uint32_t *list_a, uint32_t *list_b,
+                                                     uint32_t *queued, uint32_t *claim, int mode,
                                                      long long *removed) {
     WorldDev &w = *wd;
-    const int W = w.W, H = w.H;
+    const int W = w.W;
     __shared__ int s_scan[40];
-    __shared__ int s_n, s_next, s_spawn_base;
+    __shared__ int s_na, s_nb, s_spawn_base;
+    const uint32_t total = prefix[nb];
     if (threadIdx.x == 0) {
-        s_n = (int)prefix[nb];
         s_spawn_base = *w.part_count;
+        s_na = 0;
+    }
+    for (uint32_t g = threadIdx.x; g < total; g += blockDim.x) {
+        ptr[g] = 0;
+        queued[g] = 0;
     }
     __syncthreads();
-    for (int j = threadIdx.x; j < s_n; j += blockDim.x) open[j] = (uint32_t)j;
+    // ---- first round: every tile proposes
+    for (uint32_t g = threadIdx.x; g < total; g += blockDim.x)
+        tile_propose(w, mt, bodies, prefix, nb, mode, g, ptr, held, claim);
     __syncthreads();
-    const uint32_t pk = pass_key(w.seed, *w.tick, PH_STAMP);
-    long long rem_local = 0;
-    for (int round = 0; s_n > 0; round++) {
-        if (round > (1 << 22)) {
+    for (uint32_t g = threadIdx.x; g < total; g += blockDim.x) {
+        const int c = held[g];
+        if (c >= 0 && claim[c] != g) {  // lost its cell to an earlier tile
+            held[g] = -1;
+            ptr[g] += 1;
+            if (ptr[g] < 5) list_a[atomicAdd(&s_na, 1)] = g;
+        }
+    }
+    __syncthreads();
+    // ---- later rounds over the open tiles (list_a) and the holders they displace
+    for (long long round = 0; s_na > 0; round++) {
+        if (round > 8LL * total + 8) {  // cannot happen: every round moves a pointer forward
             if (threadIdx.x == 0) atomicOr(w.err, ERR_TIMEOUT);
             break;
         }
-        const int n = s_n;
-        // targets + claims
-        for (int j = threadIdx.x; j < n; j += blockDim.x) {
-            uint32_t g = open[j];
-            int lo = 0, hi = nb - 1;
-            while (lo < hi) {
-                int mid = (lo + hi + 1) >> 1;
-                if (prefix[mid] <= g) lo = mid; else hi = mid - 1;
+        const int na = s_na;
+        if (threadIdx.x == 0) s_nb = 0;
+        __syncthreads();
+        // propose; the proposer and the holder it may displace are checked next
+        for (int j = threadIdx.x; j < na; j += blockDim.x) {
+            const uint32_t g = list_a[j];
+            const uint32_t old = tile_propose(w, mt, bodies, prefix, nb, mode, g, ptr, held, claim);
+            if (held[g] >= 0 && atomicExch(&queued[g], 1u) == 0u) list_b[atomicAdd(&s_nb, 1)] = g;
+            if (old != 0xffffffffu && old > g && atomicExch(&queued[old], 1u) == 0u) list_b[atomicAdd(&s_nb, 1)] = old;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_na = 0;
+        __syncthreads();
+        const int nbv = s_nb;
+        for (int j = threadIdx.x; j < nbv; j += blockDim.x) {
+            const uint32_t g = list_b[j];
+            queued[g] = 0;
+            const int c = held[g];
+            if (c >= 0 && claim[c] != g) {
+                held[g] = -1;
+                ptr[g] += 1;
+                if (ptr[g] < 5) list_a[atomicAdd(&s_na, 1)] = g;
             }
-            const fse_body b = bodies[lo];
-            int t = (int)(g - prefix[lo]);
-            int wx, wy;
-            body_pos(b, t / b.h, t % b.h, wx, wy);
-            int tg = -1;
-            for (int d = 0; d < 5; d++) {
-                int xd = wx + c_dirs[d][0], yd = wy + c_dirs[d][1];
-                if (xd < 0 || yd < 0 || xd >= W || yd >= H) continue;
-                int c = yd * W + xd;
-                int cid = w.id[c];
-                bool ok;
-                if (mode == 0) {
-                    int ty = mt_type(mt->a[cid]);
-                    ok = ty == T_AIR || ty == T_SAND || ty == T_SOUP;
+        }
+        __syncthreads();
+    }
+    // ---- apply, tiles in order; reads of the cells first (the displaced
+    // particles), then the writes
+    const uint32_t pk = pass_key(w.seed, *w.tick, PH_STAMP);
+    if (mode == 0) {
+        for (uint32_t base = 0; base < total; base += blockDim.x) {
+            const uint32_t g = base + threadIdx.x;
+            const int tg = g < total ? held[g] : -1;
+            int ty = -1;
+            if (tg >= 0) ty = mt_type(mt->a[w.id[tg]]);
+            const bool spawn = ty == T_SAND || ty == T_SOUP;
+            int tot_s;
+            const int ex_s = block_scan_excl(spawn ? 1 : 0, s_scan, &tot_s);
+            if (spawn) {
+                const int bi = body_of(prefix, nb, g);
+                fse_body &b = bodies[bi];
+                const int pos = s_spawn_base + ex_s;
+                if (pos < w.part_cap) {
+                    const uint32_t ck = cell_key(pk, (uint32_t)bi, g - prefix[bi]);
+                    // CellData(tile, wxd, wyd - 3, (rand()%10-5)/10.0f, -(rand()%5+5)/10.0f, 0, 0.1)
+                    w.p.x[pos] = (float)(tg % W);
+                    w.p.y[pos] = (float)(tg / W - 3);
+                    w.p.vx[pos] = (float)((int)(draw_k(ck, 0) % 10) - 5) / 10.0f;
+                    w.p.vy[pos] = (float)(-((int)(draw_k(ck, 1) % 5) + 5)) / 10.0f;
+                    w.p.ax[pos] = 0.f;
+                    w.p.ay[pos] = 0.1f;
+                    w.p.tx[pos] = 0.f;
+                    w.p.ty[pos] = 0.f;
+                    w.p.tf[pos] = 0.f;
+                    w.p.life[pos] = 0;
+                    w.p.fade[pos] = 60;
+                    w.p.col[pos] = w.col[tg];
+                    w.p.sc[pos] = w.sc[tg];
+                    if (w.tp) w.p.tp[pos] = ty == T_SOUP ? w.tp[tg] : (int16_t)0;
+                    w.p.id[pos] = w.id[tg];
+                    w.p.fl[pos] = w.fl[tg];
+                    w.p.bits[pos] = 0;
                 } else {
-                    ok = cid == (int)b.id;
+                    atomicOr(w.err, ERR_PART_CAP);
                 }
-                if (ok) {
-                    tg = c;
-                    break;
+                if (ty == T_SOUP) {
+                    atomicAdd((unsigned long long *)&w.ledger[LED_DF * MAXMAT + w.id[tg]],
+                              (unsigned long long)(long long)w.df[tg]);
+                    atomicAdd(&b.n_soup, 1);
+                } else {
+                    atomicAdd(&b.n_sand, 1);
                 }
-            }
-            target[j] = tg;
-            if (tg >= 0) atomicMin(&claim[tg], g);
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) s_next = 0;
-        __syncthreads();
-        // decide, in list order: winners apply, losers stay open (stable)
-        for (int base = 0; base < n; base += blockDim.x) {
-            int j = base + threadIdx.x;
-            uint32_t g = j < n ? open[j] : 0;
-            int tg = j < n ? target[j] : -1;
-            bool win = tg >= 0 && claim[tg] == g;
-            bool lose = tg >= 0 && !win;
-            int bi = 0;
-            bool spawn = false;
-            if (win) {
-                int lo = 0, hi = nb - 1;
-                while (lo < hi) {
-                    int mid = (lo + hi + 1) >> 1;
-                    if (prefix[mid] <= g) lo = mid; else hi = mid - 1;
-                }
-                bi = lo;
-                if (mode == 0) {
-                    int ty = mt_type(mt->a[w.id[tg]]);
-                    spawn = ty == T_SAND || ty == T_SOUP;
-                }
-            }
-            int tot_l, tot_s;
-            int ex_l = block_scan_excl(lose ? 1 : 0, s_scan, &tot_l);
-            int ex_s = block_scan_excl(spawn ? 1 : 0, s_scan, &tot_s);
-            if (lose) next[s_next + ex_l] = g;
-            if (win && mode == 0) {
-                fse_body &b = bodies[bi];
-                if (spawn) {
-                    int ty = mt_type(mt->a[w.id[tg]]);
-                    int pos = s_spawn_base + ex_s;
-                    if (pos < w.part_cap) {
-                        uint32_t ck = cell_key(pk, (uint32_t)bi, (uint32_t)(g - prefix[bi]));
-                        // CellData(tile, wxd, wyd - 3, (rand()%10-5)/10.0f, -(rand()%5+5)/10.0f, 0, 0.1)
-                        w.p.x[pos] = (float)(tg % W);
-                        w.p.y[pos] = (float)(tg / W - 3);
-                        w.p.vx[pos] = (float)((int)(draw_k(ck, 0) % 10) - 5) / 10.0f;
-                        w.p.vy[pos] = (float)(-((int)(draw_k(ck, 1) % 5) + 5)) / 10.0f;
-                        w.p.ax[pos] = 0.f;
-                        w.p.ay[pos] = 0.1f;
-                        w.p.tx[pos] = 0.f;
-                        w.p.ty[pos] = 0.f;
-                        w.p.tf[pos] = 0.f;
-                        w.p.life[pos] = 0;
-                        w.p.fade[pos] = 60;
-                        w.p.col[pos] = w.col[tg];
-                        w.p.sc[pos] = w.sc[tg];
-                        if (w.tp) w.p.tp[pos] = ty == T_SOUP ? w.tp[tg] : (int16_t)0;
-                        w.p.id[pos] = w.id[tg];
-                        w.p.fl[pos] = w.fl[tg];
-                        w.p.bits[pos] = 0;
-                    } else {
-                        atomicOr(w.err, ERR_PART_CAP);
-                    }
-                    if (ty == T_SOUP) {
-                        atomicAdd((unsigned long long *)&w.ledger[LED_DF * MAXMAT + w.id[tg]],
-                                  (unsigned long long)(long long)w.df[tg]);
-                        atomicAdd(&b.n_soup, 1);
-                    } else {
-                        atomicAdd(&b.n_sand, 1);
-                    }
-                }
-                w.id[tg] = b.id;
-                w.col[tg] = b.colour;
-                w.sc[tg] = 0;
-                w.fl[tg] = 0;
-                w.df[tg] = 0;
-                if (w.dirty) w.dirty[tg] = 1;
-                atomicAdd(&b.n_placed, 1);
-                atomicAdd((unsigned long long *)&w.ledger[LED_CN * MAXMAT + b.id], 1ull);
-            } else if (win) {
-                fse_body &b = bodies[bi];
-                atomicAdd((unsigned long long *)&w.ledger[LED_DN * MAXMAT + w.id[tg]], 1ull);
-                w.id[tg] = (uint16_t)mt->id_air;
-                w.col[tg] = 0;
-                w.sc[tg] = 0;
-                w.fl[tg] = 0;
-                w.df[tg] = 0;
-                if (w.dirty) w.dirty[tg] = 1;
-                atomicAdd(&b.n_recovered, 1);
-                rem_local++;
             }
             __syncthreads();
-            if (threadIdx.x == 0) {
-                s_next += tot_l;
-                s_spawn_base += tot_s;
-            }
+            if (threadIdx.x == 0) s_spawn_base += tot_s;
             __syncthreads();
         }
-        for (int j = threadIdx.x; j < n; j += blockDim.x)
-            if (target[j] >= 0) claim[target[j]] = 0xffffffffu;
-        __syncthreads();
-        uint32_t *t = open;
-        open = next;
-        next = t;
-        if (threadIdx.x == 0) s_n = s_next;
-        __syncthreads();
+    }
+    long long rem_local = 0;
+    for (uint32_t g = threadIdx.x; g < total; g += blockDim.x) {
+        const int tg = held[g];
+        if (tg < 0) continue;
+        fse_body &b = bodies[body_of(prefix, nb, g)];
+        if (mode == 0) {
+            w.id[tg] = b.id;
+            w.col[tg] = b.colour;
+            w.sc[tg] = 0;
+            w.fl[tg] = 0;
+            w.df[tg] = 0;
+            atomicAdd(&b.n_placed, 1);
+            atomicAdd((unsigned long long *)&w.ledger[LED_CN * MAXMAT + b.id], 1ull);
+        } else {
+            atomicAdd((unsigned long long *)&w.ledger[LED_DN * MAXMAT + w.id[tg]], 1ull);
+            w.id[tg] = (uint16_t)mt->id_air;
+            w.col[tg] = 0;
+            w.sc[tg] = 0;
+            w.fl[tg] = 0;
+            w.df[tg] = 0;
+            atomicAdd(&b.n_recovered, 1);
+            rem_local++;
+        }
+        if (w.dirty) w.dirty[tg] = 1;
+        claim[tg] = 0xffffffffu;  // every claimed cell has its lowest proposer as holder
     }
     if (rem_local) atomicAdd((unsigned long long *)removed, (unsigned long long)rem_local);
     __syncthreads();
@@ -328,7 +386,8 @@ static int obj_run(fse_world *w, fse_body *bodies, int n, int mode, int64_t *out
     }
     size_t total = prefix[n];
     fse_body *d_b = nullptr;
-    uint32_t *d_pref = nullptr, *d_open = nullptr, *d_next = nullptr;
+    uint32_t *d_pref = nullptr, *d_open = nullptr, *d_next = nullptr, *d_la = nullptr, *d_lb = nullptr,
+             *d_q = nullptr;
     int32_t *d_tgt = nullptr;
     long long *d_rem = nullptr;
     bool ok = cudaMalloc(&d_b, n * sizeof(fse_body)) == cudaSuccess &&
@@ -336,6 +395,9 @@ static int obj_run(fse_world *w, fse_body *bodies, int n, int mode, int64_t *out
               cudaMalloc(&d_open, std::max<size_t>(total, 1) * 4) == cudaSuccess &&
               cudaMalloc(&d_next, std::max<size_t>(total, 1) * 4) == cudaSuccess &&
               cudaMalloc(&d_tgt, std::max<size_t>(total, 1) * 4) == cudaSuccess &&
+              cudaMalloc(&d_la, std::max<size_t>(total, 1) * 4) == cudaSuccess &&
+              cudaMalloc(&d_lb, std::max<size_t>(2 * total, 1) * 4) == cudaSuccess &&
+              cudaMalloc(&d_q, std::max<size_t>(total, 1) * 4) == cudaSuccess &&
               cudaMalloc(&d_rem, 8) == cudaSuccess;
     int result = FSE_OK;
     if (!ok) {
@@ -344,8 +406,8 @@ static int obj_run(fse_world *w, fse_body *bodies, int n, int mode, int64_t *out
         cudaMemcpyAsync(d_b, bodies, n * sizeof(fse_body), cudaMemcpyHostToDevice, w->stream);
         cudaMemcpyAsync(d_pref, prefix.data(), (n + 1) * 4, cudaMemcpyHostToDevice, w->stream);
         cudaMemsetAsync(d_rem, 0, 8, w->stream);
-        k_obj_rounds<<<1, 1024, 0, w->stream>>>(w->d, g_dev_mt, d_b, d_pref, n, d_open, d_next, d_tgt, w->claim, mode,
-                                                d_rem);
+        k_obj_rounds<<<1, 1024, 0, w->stream>>>(w->d, g_dev_mt, d_b, d_pref, n, d_open, d_tgt, d_la, d_lb, d_q,
+                                                w->claim, mode, d_rem);
         long long rem = 0;
         cudaMemcpyAsync(bodies, d_b, n * sizeof(fse_body), cudaMemcpyDeviceToHost, w->stream);
         cudaMemcpyAsync(&rem, d_rem, 8, cudaMemcpyDeviceToHost, w->stream);
@@ -356,6 +418,9 @@ static int obj_run(fse_world *w, fse_body *bodies, int n, int mode, int64_t *out
     cudaFree(d_pref);
     cudaFree(d_open);
     cudaFree(d_next);
+    cudaFree(d_la);
+    cudaFree(d_lb);
+    cudaFree(d_q);
     cudaFree(d_tgt);
     cudaFree(d_rem);
     if (result) return result;

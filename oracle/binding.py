@@ -14,6 +14,7 @@ REF_TEMPERATURE_PATH = os.path.join(HERE, "_ref", "libref_temperature.so")
 REF_LZ4_PATH = os.path.join(HERE, "_ref", "liblz4ref.so")
 REF_CELLS_PATH = os.path.join(HERE, "_ref", "libref_cells.so")
 REF_RENDER_PATH = os.path.join(HERE, "_ref", "libref_render.so")
+REF_OBJECTS_PATH = os.path.join(HERE, "_ref", "libref_objects.so")
 REFERENCE_WORLD_CPP = "/root/reference/source/engine/world.cpp"
 
 PARTICLE_DTYPE = np.dtype(
@@ -514,3 +515,68 @@ def reference_render_dirty(lib_path, ids, colours, dirty, flow_x, flow_y, prev_x
     if rc != 0:
         raise ValueError("ref_render_dirty failed")
     return tex, arrs[3], arrs[4], arrs[5], arrs[6], moving
+
+
+def build_reference_objects(force=False):
+    """Compile the reference's own rigid-body stamp/readback loops (oracle/Makefile `ref`)."""
+    if not os.path.exists(REFERENCE_WORLD_CPP):
+        return None
+    if force or not os.path.exists(REF_OBJECTS_PATH) or os.path.getmtime(REF_OBJECTS_PATH) < os.path.getmtime(
+            os.path.join(HERE, "ref_objects.cpp")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    return REF_OBJECTS_PATH
+
+
+def _ref_bodies(bodies):
+    bf = np.ascontiguousarray(np.stack([bodies["x"], bodies["y"], bodies["sin_a"], bodies["cos_a"]], 1), np.float32)
+    bi = np.ascontiguousarray(np.stack([bodies["w"], bodies["h"], bodies["id"].astype(np.int32),
+                                        bodies["colour"].view(np.int32)], 1), np.int32)
+    return bf, bi
+
+
+def reference_object_stamp(lib_path, ids, colours, types, alpha, air_id, bodies):
+    """The reference's stamp loop over bodies in order: (ids, colours, particles as
+    (id, colour, x, y) rows, per-body [sand, liquid] displacements)."""
+    lib = C.CDLL(lib_path)
+    f = lib.ref_object_stamp
+    f.restype = C.c_int
+    f.argtypes = [C.c_int] * 2 + [C.c_void_p] * 5 + [C.c_int] * 2 + [C.c_void_p] * 2 + [C.c_int] + \
+        [C.c_void_p] * 2 + [C.c_int, C.c_void_p]
+    h, w = ids.shape
+    i2 = np.ascontiguousarray(ids, np.uint16).copy()
+    c2 = np.ascontiguousarray(colours, np.uint32).copy()
+    d2 = np.zeros((h, w), np.uint8)
+    t = np.ascontiguousarray(types, np.int32)
+    a = np.ascontiguousarray(alpha, np.uint8)
+    bf, bi = _ref_bodies(bodies)
+    counts = np.zeros((len(bodies), 2), np.int32)
+    cap = int(bodies["w"].astype(np.int64) @ bodies["h"].astype(np.int64)) + 1
+    parts = np.zeros((cap, 4), np.float32)
+    n = C.c_int(0)
+    rc = f(w, h, _ptr(i2), _ptr(c2), _ptr(d2), _ptr(t), _ptr(a), len(t), air_id, _ptr(bf), _ptr(bi), len(bodies),
+           _ptr(counts), _ptr(parts), cap, C.byref(n))
+    if rc != 0:
+        raise ValueError("ref_object_stamp failed")
+    return i2, c2, parts[: n.value].copy(), counts
+
+
+def reference_object_readback(lib_path, ids, colours, types, alpha, air_id, bodies):
+    """The reference's readback loop: (ids, colours, per-body [recovered, lost])."""
+    lib = C.CDLL(lib_path)
+    f = lib.ref_object_readback
+    f.restype = C.c_int
+    f.argtypes = [C.c_int] * 2 + [C.c_void_p] * 5 + [C.c_int] * 2 + [C.c_void_p] * 2 + [C.c_int] + [C.c_void_p] * 2
+    h, w = ids.shape
+    i2 = np.ascontiguousarray(ids, np.uint16).copy()
+    c2 = np.ascontiguousarray(colours, np.uint32).copy()
+    d2 = np.zeros((h, w), np.uint8)
+    t = np.ascontiguousarray(types, np.int32)
+    a = np.ascontiguousarray(alpha, np.uint8)
+    bf, bi = _ref_bodies(bodies)
+    counts = np.zeros((len(bodies), 2), np.int32)
+    pix = np.zeros((h, w, 4), np.uint8)
+    rc = f(w, h, _ptr(i2), _ptr(c2), _ptr(d2), _ptr(t), _ptr(a), len(t), air_id, _ptr(bf), _ptr(bi), len(bodies),
+           _ptr(counts), _ptr(pix))
+    if rc != 0:
+        raise ValueError("ref_object_readback failed")
+    return i2, c2, counts

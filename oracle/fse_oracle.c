@@ -2108,179 +2108,94 @@ static void body_tile_pos(const om_body *b, int tx, int ty, int *wx, int *wy) {
     *wy = (int)fy;
 }
 
+/* The stamp, game.cpp:1766-1813: bodies in order, tiles tx-major then ty-minor;
+ * each tile takes the first of its five cells that is AIR, SAND or SOUP at that
+ * moment (a cell it takes becomes the body's tile), displacing SAND and SOUP into a
+ * particle (CellData(tile, wxd, wyd - 3, ...), velocities from the counter RNG
+ * instead of rand()) and counting the displacement for the body's damping. */
 void om_object_stamp(om_world *w, om_body *bodies, int n) {
-    long total = 0;
-    for (int b = 0; b < n; b++) {
-        bodies[b].n_sand = bodies[b].n_soup = bodies[b].n_placed = 0;
-        total += (long)bodies[b].w * bodies[b].h;
-    }
-    if (total == 0) return;
-    /* open tiles: (body, tile) in body-major, tx-major, ty-minor order */
-    int32_t *ob = (int32_t *)malloc((size_t)total * sizeof(int32_t));
-    int32_t *ot = (int32_t *)malloc((size_t)total * sizeof(int32_t));
-    long *gidx = (long *)malloc((size_t)total * sizeof(long));
-    int *tgt = (int *)malloc((size_t)total * sizeof(int));
-    long no = 0, base = 0;
-    for (int b = 0; b < n; b++) {
-        for (int t = 0; t < bodies[b].w * bodies[b].h; t++) {
-            ob[no] = b;
-            ot[no] = t;
-            gidx[no] = base + t;
-            no++;
-        }
-        base += (long)bodies[b].w * bodies[b].h;
-    }
-    size_t ncell = (size_t)w->W * w->H;
-    long *claim = (long *)malloc(ncell * sizeof(long));
-    for (size_t i = 0; i < ncell; i++) claim[i] = 0x7fffffffffffffffL;
     uint32_t pk = pass_key(w->seed, w->tick, PH_STAMP);
-    while (no > 0) {
-        for (long j = 0; j < no; j++) {
-            const om_body *bd = &bodies[ob[j]];
-            int txx = ot[j] / bd->h, tyy = ot[j] % bd->h, wx, wy;
-            body_tile_pos(bd, txx, tyy, &wx, &wy);
-            tgt[j] = -1;
+    for (int b = 0; b < n; b++) {
+        om_body *bd = &bodies[b];
+        bd->n_sand = bd->n_soup = bd->n_placed = 0;
+        for (int t = 0; t < bd->w * bd->h; t++) {
+            int wx, wy;
+            body_tile_pos(bd, t / bd->h, t % bd->h, &wx, &wy);
             for (int d = 0; d < 5; d++) {
                 int xd = wx + DIRS[d][0], yd = wy + DIRS[d][1];
                 if (xd < 0 || yd < 0 || xd >= w->W || yd >= w->H) continue;
-                int ty = M[w->id[(size_t)yd * w->W + xd]].type;
-                if (ty == T_AIR || ty == T_SAND || ty == T_SOUP) {
-                    tgt[j] = yd * w->W + xd;
-                    if (gidx[j] < claim[tgt[j]]) claim[tgt[j]] = gidx[j];
-                    break;
+                size_t ci = (size_t)yd * w->W + xd;
+                int ty = M[w->id[ci]].type;
+                if (ty != T_AIR && ty != T_SAND && ty != T_SOUP) continue;
+                if (ty == T_SAND || ty == T_SOUP) {
+                    om_particle p;
+                    memset(&p, 0, sizeof(p));
+                    uint32_t ck = cell_key(pk, (uint32_t)b, (uint32_t)t);
+                    p.x = (float)xd;
+                    p.y = (float)(yd - 3);
+                    p.vx = (float)((int)(draw_k(ck, 0) % 10) - 5) / 10.0f;
+                    p.vy = (float)(-((int)(draw_k(ck, 1) % 5) + 5)) / 10.0f;
+                    p.ay = 0.1f;
+                    p.fade_time = 60;
+                    p.id = w->id[ci];
+                    p.colour = w->col[ci];
+                    p.scalar = w->sc[ci];
+                    if (ty == T_SOUP) p.temperature = w->tp[ci];
+                    p.flags = w->fl[ci];
+                    pv_push(&w->parts, &p);
+                    if (ty == T_SOUP) {
+                        /* the cell's pending diff leaves with it */
+                        w->led[LED_DF][p.id] += w->df[ci];
+                        bd->n_soup++;
+                    } else
+                        bd->n_sand++;
                 }
+                w->id[ci] = bd->id;
+                w->col[ci] = bd->colour;
+                w->sc[ci] = 0;
+                w->fl[ci] = 0;
+                w->df[ci] = 0;
+                mark_dirty(w, ci);
+                bd->n_placed++;
+                w->led[LED_CN][bd->id] += 1;
+                break;
             }
         }
-        long nn = 0;
-        for (long j = 0; j < no; j++) {
-            if (tgt[j] < 0) continue; /* no usable cell: the tile is not stamped */
-            size_t ci = (size_t)tgt[j];
-            if (claim[ci] != gidx[j]) {
-                ob[nn] = ob[j];
-                ot[nn] = ot[j];
-                gidx[nn] = gidx[j];
-                nn++;
-                continue;
-            }
-            om_body *bd = &bodies[ob[j]];
-            int ty = M[w->id[ci]].type;
-            if (ty == T_SAND || ty == T_SOUP) {
-                om_particle p;
-                memset(&p, 0, sizeof(p));
-                uint32_t ck = cell_key(pk, (uint32_t)ob[j], (uint32_t)ot[j]);
-                p.x = (float)(int)(ci % (size_t)w->W);
-                p.y = (float)((int)(ci / (size_t)w->W) - 3);
-                p.vx = (float)((int)(draw_k(ck, 0) % 10) - 5) / 10.0f;
-                p.vy = (float)(-((int)(draw_k(ck, 1) % 5) + 5)) / 10.0f;
-                p.ay = 0.1f;
-                p.fade_time = 60;
-                p.id = w->id[ci];
-                p.colour = w->col[ci];
-                p.scalar = w->sc[ci];
-                if (ty == T_SOUP) p.temperature = w->tp[ci];
-                p.flags = w->fl[ci];
-                pv_push(&w->parts, &p);
-                if (ty == T_SOUP) {
-                    /* the cell's pending diff leaves with it */
-                    w->led[LED_DF][p.id] += w->df[ci];
-                    bd->n_soup++;
-                } else
-                    bd->n_sand++;
-            }
-            w->id[ci] = bd->id;
-            w->col[ci] = bd->colour;
-            w->sc[ci] = 0;
-            w->fl[ci] = 0;
-            w->df[ci] = 0;
-            mark_dirty(w, ci);
-            bd->n_placed++;
-            w->led[LED_CN][bd->id] += 1;
-        }
-        for (long j = 0; j < no; j++)
-            if (tgt[j] >= 0) claim[tgt[j]] = 0x7fffffffffffffffL;
-        no = nn;
     }
-    free(ob);
-    free(ot);
-    free(gidx);
-    free(tgt);
-    free(claim);
 }
 
-/* Readback after the tick, game.cpp:1896-1983: each body tile takes back the first
- * cell of its offsets that holds the body's material and erases it (rounds as in
- * the stamp). */
+/* The readback after the tick, game.cpp:1907-1967: bodies and tiles in the same
+ * order; each tile takes back the first of its five cells that holds the body's
+ * material at that moment and erases it (Tiles_NOTHING). Returns the cells erased.
+ * (The reference also drops a tile from the body when none is found and its own
+ * cell is AIR; the body images stay with the caller here.) */
 long om_object_readback(om_world *w, const om_body *bodies_c, int n) {
     om_body *bodies = (om_body *)bodies_c;
     long removed = 0;
-    for (int b = 0; b < n; b++) bodies[b].n_recovered = 0;
-    long total = 0;
-    for (int b = 0; b < n; b++) total += (long)bodies[b].w * bodies[b].h;
-    if (total == 0) return 0;
-    int32_t *ob = (int32_t *)malloc((size_t)total * sizeof(int32_t));
-    int32_t *ot = (int32_t *)malloc((size_t)total * sizeof(int32_t));
-    long *gidx = (long *)malloc((size_t)total * sizeof(long));
-    int *tgt = (int *)malloc((size_t)total * sizeof(int));
-    long no = 0, base = 0;
     for (int b = 0; b < n; b++) {
-        for (int t = 0; t < bodies[b].w * bodies[b].h; t++) {
-            ob[no] = b;
-            ot[no] = t;
-            gidx[no] = base + t;
-            no++;
-        }
-        base += (long)bodies[b].w * bodies[b].h;
-    }
-    size_t ncell = (size_t)w->W * w->H;
-    long *claim = (long *)malloc(ncell * sizeof(long));
-    for (size_t i = 0; i < ncell; i++) claim[i] = 0x7fffffffffffffffL;
-    while (no > 0) {
-        for (long j = 0; j < no; j++) {
-            const om_body *bd = &bodies[ob[j]];
-            int txx = ot[j] / bd->h, tyy = ot[j] % bd->h, wx, wy;
-            body_tile_pos(bd, txx, tyy, &wx, &wy);
-            tgt[j] = -1;
+        om_body *bd = &bodies[b];
+        bd->n_recovered = 0;
+        for (int t = 0; t < bd->w * bd->h; t++) {
+            int wx, wy;
+            body_tile_pos(bd, t / bd->h, t % bd->h, &wx, &wy);
             for (int d = 0; d < 5; d++) {
                 int xd = wx + DIRS[d][0], yd = wy + DIRS[d][1];
                 if (xd < 0 || yd < 0 || xd >= w->W || yd >= w->H) continue;
-                if (w->id[(size_t)yd * w->W + xd] == bd->id) {
-                    tgt[j] = yd * w->W + xd;
-                    if (gidx[j] < claim[tgt[j]]) claim[tgt[j]] = gidx[j];
-                    break;
-                }
+                size_t ci = (size_t)yd * w->W + xd;
+                if (w->id[ci] != bd->id) continue;
+                w->led[LED_DN][w->id[ci]] += 1;
+                w->id[ci] = (uint16_t)ID_AIR;
+                w->col[ci] = 0;
+                w->sc[ci] = 0;
+                w->fl[ci] = 0;
+                w->df[ci] = 0;
+                mark_dirty(w, ci);
+                bd->n_recovered++;
+                removed++;
+                break;
             }
         }
-        long nn = 0;
-        for (long j = 0; j < no; j++) {
-            if (tgt[j] < 0) continue;
-            size_t ci = (size_t)tgt[j];
-            if (claim[ci] != gidx[j]) {
-                ob[nn] = ob[j];
-                ot[nn] = ot[j];
-                gidx[nn] = gidx[j];
-                nn++;
-                continue;
-            }
-            om_body *bd = &bodies[ob[j]];
-            w->led[LED_DN][w->id[ci]] += 1;
-            w->id[ci] = (uint16_t)ID_AIR;
-            w->col[ci] = 0;
-            w->sc[ci] = 0;
-            w->fl[ci] = 0;
-            w->df[ci] = 0;
-            mark_dirty(w, ci);
-            bd->n_recovered++;
-            removed++;
-        }
-        for (long j = 0; j < no; j++)
-            if (tgt[j] >= 0) claim[tgt[j]] = 0x7fffffffffffffffL;
-        no = nn;
     }
-    free(ob);
-    free(ot);
-    free(gidx);
-    free(tgt);
-    free(claim);
     return removed;
 }
 

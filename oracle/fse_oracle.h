@@ -23,10 +23,14 @@
  * and OM_ORDER_PART is bit-exact with the CUDA kernels.
  *
  * Parity pinning: the reference ships no test, fixture or golden vector for this
- * path (its tests cover only FFI/reflection/promises), and its world.cpp cannot be
- * compiled without SDL2/xmake. Parity is therefore anchored on this restatement,
- * which cites the reference line by line, plus the committed fixtures under
- * tests/golden/ generated from it.
+ * path (its tests cover only FFI/reflection/promises), and its world.cpp as a whole
+ * cannot be compiled without SDL2/xmake. Self-contained pieces of the reference's
+ * own code are compiled in place by oracle/Makefile (target `ref`) and pin this
+ * restatement bit for bit: world::tickCells (the particle update),
+ * world::tickTemperature, the dirty-pixel loop of game::tick and the vendored LZ4.
+ * The cell update itself (libc rand(), float fluid) is anchored on this
+ * restatement, which cites the reference line by line, plus the committed fixtures
+ * under tests/golden/ generated from it.
  */
 #ifndef FSE_ORACLE_H
 #define FSE_ORACLE_H
