@@ -60,3 +60,17 @@ def test_ledger_matches_oracle(fse, oracle_mod):
     ow.step(5, ORDER_PART)
     np.testing.assert_array_equal(world.ledger(), ow.ledger())
     np.testing.assert_array_equal(world.census(), ow.census())
+
+
+@pytest.mark.parametrize("chunk,cell_iter,w,h", [(16, 3, 96, 80), (32, 1, 200, 136), (64, 2, 200, 136),
+                                                  (96, 5, 288, 200), (128, 8, 256, 192), (48, 4, 150, 170)])
+def test_chunk_and_iteration_variants(fse, oracle_mod, chunk, cell_iter, w, h):
+    """Other chunk edges and iteration counts than the reference's 128 / 3, on
+    worlds that are not multiples of the chunk: planes and particles after steps."""
+    types = material_types(fse)
+    world, ow = _pair(fse, oracle_mod, w, h, 4321 + chunk, chunk=chunk, cell_iter=cell_iter)
+    for t in range(4):
+        world.step(1)
+        ow.step(1, ORDER_PART)
+        compare_states(world.state(), ow.state(), types, "chunk %d iter %d step %d" % (chunk, cell_iter, t))
+        compare_particles(world.particles(), ow.particles(), "chunk %d iter %d step %d" % (chunk, cell_iter, t))
