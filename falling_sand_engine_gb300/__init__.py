@@ -14,10 +14,10 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _abi
-from ._abi import BODY_DTYPE, PARTICLE_DTYPE, FseConfig, FseError, check, ptr
+from ._abi import BODY_DTYPE, PARTICLE_DTYPE, TILE_DTYPE, FseConfig, FseError, FseTileLayout, check, ptr
 
 __all__ = [
-    "World", "Batch", "Server", "MaterialInstance", "FseError", "PARTICLE_DTYPE", "BODY_DTYPE",
+    "World", "Batch", "Server", "MaterialInstance", "FseError", "PARTICLE_DTYPE", "BODY_DTYPE", "TILE_DTYPE",
     "InitMaterials", "RegisterMaterial", "PushMaterials", "load_lua_materials", "material_find",
     "material_count", "material_get", "set_reaction", "set_interaction", "lib",
     "AIR", "SOLID", "SAND", "SOUP", "GAS", "PASSABLE", "OBJECT", "GEN_EMPTY", "GEN_MIX", "GEN_ZIPF8",
@@ -206,6 +206,28 @@ class World:
             if a.dtype != dt or a.size != n or not a.flags["C_CONTIGUOUS"]:
                 raise ValueError("plane %s must be a C-contiguous %s array of %d cells" % (k, np.dtype(dt), n))
         check(self.lib.fse_world_download(self.h, *[ptr(out[k]) for k, _ in self.PLANES]), "download")
+        return out
+
+    def upload_tiles(self, tiles):
+        """Load the grid from an (H, W) array of tile structs (TILE_DTYPE, the reference's
+        real_tiles, or any structured dtype with a subset of its field names)."""
+        a = np.ascontiguousarray(tiles)
+        if a.size != self.width * self.height or a.dtype.fields is None:
+            raise ValueError("need a structured array of %d tiles" % (self.width * self.height))
+        lay = FseTileLayout.of(a.dtype)
+        check(self.lib.fse_world_upload_tiles(self.h, ptr(a), C.byref(lay)), "upload_tiles")
+
+    def download_tiles(self, out=None, mat_table=None):
+        """Store the grid into an (H, W) array of tile structs; `mat_table[id]` fills the
+        `mat` pointer field when given."""
+        if out is None:
+            out = np.zeros((self.height, self.width), TILE_DTYPE)
+        if out.size != self.width * self.height or out.dtype.fields is None or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("need a C-contiguous structured array of %d tiles" % (self.width * self.height))
+        lay = FseTileLayout.of(out.dtype)
+        tab = None if mat_table is None else np.ascontiguousarray(mat_table, np.uint64)
+        check(self.lib.fse_world_download_tiles(self.h, ptr(out), C.byref(lay), None if tab is None else ptr(tab),
+                                                0 if tab is None else tab.size), "download_tiles")
         return out
 
     def generate(self, kind, seed):

@@ -28,6 +28,30 @@ ISLAND_DTYPE = np.dtype([("root", "<i4"), ("cells", "<i4"), ("min_x", "<i4"), ("
                          ("max_y", "<i4")])
 
 
+# MaterialInstance (source/engine/game_datastruct.hpp:205-222) on LP64 targets
+TILE_DTYPE = np.dtype(
+    {
+        "names": ["id", "mat", "color", "temperature", "moved", "fluidAmount", "fluidAmountDiff", "settleCount"],
+        "formats": ["<u4", "<u8", "<u4", "<i2", "u1", "<f4", "<f4", "u1"],
+        "offsets": [0, 8, 16, 20, 22, 24, 28, 32],
+        "itemsize": 40,
+    }
+)
+
+
+class FseTileLayout(C.Structure):
+    _fields_ = [(k, C.c_int32) for k in ("stride", "id", "mat", "colour", "temperature", "moved", "fluid_amount",
+                                         "fluid_amount_diff", "settle_count")]
+
+    @classmethod
+    def of(cls, dtype):
+        """The layout of a numpy structured dtype with MaterialInstance's field names."""
+        f = dtype.fields
+        off = lambda k: f[k][1] if k in f else -1
+        return cls(dtype.itemsize, off("id"), off("mat"), off("color"), off("temperature"), off("moved"),
+                   off("fluidAmount"), off("fluidAmountDiff"), off("settleCount"))
+
+
 class FseConfig(C.Structure):
     _fields_ = [
         ("chunk_size", C.c_int32), ("cell_iter", C.c_int32), ("seed", C.c_uint32),
@@ -57,6 +81,8 @@ SIGNATURES = {
     "fse_world_pack": (_i, [_vp, _i, _vp, _i64, _vp, _vp]),
     "fse_world_unpack": (_i, [_vp, _vp, _vp, _i, _vp, _vp]),
     "fse_world_checkpoint_bound": (_i, [_vp, _vp]),
+    "fse_world_upload_tiles": (_i, [_vp, _vp, _vp]),
+    "fse_world_download_tiles": (_i, [_vp, _vp, _vp, _vp, _i]),
     "fse_world_checkpoint": (_i, [_vp, _vp, _i64, _vp]),
     "fse_world_restore": (_i, [_vp, _vp, _i64]),
     "fse_materials_load_lua": (_i, [C.c_char_p, C.POINTER(_i)]),

@@ -702,7 +702,7 @@ static void free_world(fse_world *w) {
         if (w->items[k]) cudaFree(w->items[k]);
     void *rs[] = {h.dirty,      h.flow,      w->pflow,    w->owner,    w->moving,   w->tex[0],   w->tex[1],
                   w->tex[2],    w->tex[3],   w->tex[4],   w->isl_mark, w->isl_lab,  w->isl_aux,  w->isl_list,
-                  w->isl_out,   w->isl_pix,  w->isl_tab,  w->isl_seg,  w->temp_io};
+                  w->isl_out,   w->isl_pix,  w->isl_tab,  w->isl_seg,  w->temp_io, w->tile_stage};
     for (void *q : rs)
         if (q) cudaFree(q);
     if (w->own_stream && w->stream) cudaStreamDestroy(w->stream);

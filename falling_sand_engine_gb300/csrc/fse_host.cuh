@@ -60,6 +60,9 @@ struct fse_world {
     int isl_tab_cap;
     // temperature read/write staging (allocated on first use)
     int16_t *temp_io;
+    // array-of-structs tile staging (allocated on first use)
+    uint8_t *tile_stage;
+    size_t tile_stage_bytes;
 };
 
 namespace fse {

@@ -17,6 +17,7 @@
  *   fse_particles_tick        world::tickCells()         source/engine/world.cpp:2030-2195
  *   fse_particles_add         world::addCell(CellData*)  source/engine/world.cpp:2292
  *   fse_world_get_tile/set    world::getTile/setTile     source/engine/world.cpp:999-1008
+ *   fse_world_upload/download_tiles  real_tiles (MaterialInstance[]) source/engine/game_datastruct.hpp:205-222
  *   fse_object_stamp          rigid-body tile stamping   source/engine/game.cpp:1768-1814
  *   fse_object_readback       rigid-body tile readback   source/engine/game.cpp:1896-1983
  *   fse_world_tick_temperature world::tickTemperature()  source/engine/world.cpp:1950-2004
@@ -176,6 +177,34 @@ int fse_world_set_tick(fse_world *world, uint32_t tick);
 int fse_world_get_tile(fse_world *world, int x, int y, uint16_t *id, uint32_t *colour, int32_t *scalar,
                        uint8_t *flags);
 int fse_world_set_tile(fse_world *world, int x, int y, uint16_t id, uint32_t colour, int32_t scalar, uint8_t flags);
+
+/* Array-of-structs grids such as the reference's real_tiles: where the fields of
+ * the caller's tile struct lie (byte offsets, -1 = absent; 4-byte fields 4-aligned,
+ * the temperature 2-aligned, the pointer slot 8-aligned, stride a multiple of 8). */
+typedef struct fse_tile_layout {
+    int32_t stride;            /* bytes per tile */
+    int32_t id;                /* u32 material index (MaterialInstance::id == mat->id) */
+    int32_t mat;               /* pointer slot written on download from mat_table[id] */
+    int32_t colour;            /* u32 */
+    int32_t temperature;       /* i16 */
+    int32_t moved;             /* bool / u8 */
+    int32_t fluid_amount;      /* f32 */
+    int32_t fluid_amount_diff; /* f32 */
+    int32_t settle_count;      /* u8 */
+} fse_tile_layout;
+/* MaterialInstance (game_datastruct.hpp:205-222) on LP64 targets, 40 bytes */
+#define FSE_TILE_LAYOUT_MATERIAL_INSTANCE {40, 0, 8, 16, 20, 22, 24, 28, 32}
+/* Load the whole grid from / store it into such an array (width * height tiles,
+ * row-major): liquid amounts and diffs are rounded to the nearest 1/65536, the
+ * settle count saturates at 63, a liquid's temperature is kept only by worlds with
+ * FSE_CFG_TEMPERATURE. Download writes id, colour, temperature, moved and settle
+ * count of every tile, the amounts of liquid tiles only, and (with a mat_table of
+ * n_mat pointers, and layout->mat >= 0) the Material pointer; other bytes are kept.
+ * The conversion runs on the device: the array travels once per upload, twice per
+ * download (read, then written back). */
+int fse_world_upload_tiles(fse_world *world, const void *tiles, const fse_tile_layout *layout);
+int fse_world_download_tiles(fse_world *world, void *tiles, const fse_tile_layout *layout, const uint64_t *mat_table,
+                             int n_mat);
 
 /* Temperatures of all cells (int16, MaterialInstance::temperature) of a world
  * created with FSE_CFG_TEMPERATURE (else FSE_E_STATE): SOUP cells keep theirs

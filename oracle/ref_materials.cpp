@@ -4,9 +4,12 @@
 // source/engine/game_datastruct.cpp:70-111 with the Material constructor it calls
 // (game_datastruct.cpp:40-52) and the delegating constructors of
 // game_datastruct.hpp:160-167 -- so that the material table restated here can be
-// checked against it. oracle/Makefile (target `ref`) extracts the three pieces,
+// checked against it; and the tile struct MaterialInstance (game_datastruct.hpp:
+// 206-224, with its size assertion), whose field offsets the library's default
+// array-of-structs tile layout must match. oracle/Makefile (target `ref`) extracts the three pieces,
 // unchanged, into _ref/; this file supplies a stand-in Material with the fields they
 // set, the GAME() registry they fill, and a C entry point.
+#include <cstddef>
 #include <cstdint>
 #include <cstring>
 #include <string>
@@ -15,6 +18,9 @@ typedef uint32_t mat_id;
 typedef uint32_t u32;
 typedef uint8_t u8;
 typedef float f32;
+typedef int16_t i16;
+typedef mat_id mat_instance_id;
+typedef i16 mat_temperature;
 
 enum PhysicsType { AIR = 0, SOLID = 1, SAND = 2, SOUP = 3, GAS = 4, PASSABLE = 5, OBJECT = 5 };
 
@@ -32,6 +38,23 @@ struct Material {
 #include "material_ctors.inc"
 };
 #include "material_ctor_def.inc"
+
+#include "material_instance.inc"
+
+// sizeof and the offsets of id, mat, color, temperature, moved, fluidAmount,
+// fluidAmountDiff, settleCount
+extern "C" void ref_tile_layout(int32_t *out) {
+    const int32_t v[9] = {(int32_t)sizeof(MaterialInstance),
+                          (int32_t)offsetof(MaterialInstance, id),
+                          (int32_t)offsetof(MaterialInstance, mat),
+                          (int32_t)offsetof(MaterialInstance, color),
+                          (int32_t)offsetof(MaterialInstance, temperature),
+                          (int32_t)offsetof(MaterialInstance, moved),
+                          (int32_t)offsetof(MaterialInstance, fluidAmount),
+                          (int32_t)offsetof(MaterialInstance, fluidAmountDiff),
+                          (int32_t)offsetof(MaterialInstance, settleCount)};
+    memcpy(out, v, sizeof(v));
+}
 
 struct MaterialsList {
     Material GENERIC_AIR, GENERIC_SOLID, GENERIC_SAND, GENERIC_LIQUID, GENERIC_GAS, GENERIC_PASSABLE, GENERIC_OBJECT,

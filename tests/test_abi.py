@@ -77,6 +77,9 @@ def test_bad_arguments_are_status_codes(lib):
     assert L.fse_material_register(0, b"x", b"X", 9, 0, 255, 1.0, 1, 0, 0, 0, C.byref(out)) == -1
     assert L.fse_material_set_interaction(2, 15, 1, 9, 4, 2, 0) == -1  # reach 6 > halo
     assert L.fse_world_tick(None, 1) == -1
+    lay = lib._abi.FseTileLayout.of(lib.TILE_DTYPE)
+    assert L.fse_world_upload_tiles(None, None, C.byref(lay)) == -1
+    assert L.fse_world_download_tiles(None, None, C.byref(lay), None, 0) == -1
     assert L.fse_status_string(-3) == b"HBM budget exceeded"
     with pytest.raises(lib.FseError):
         lib.RegisterMaterial(0, "bad", "BAD", 7, 0, 255, 1.0, 1)

@@ -118,3 +118,24 @@ def test_conduction_reactions_factories_match_reference_text(oracle_mod):
         assert fse.lib().fse_material_get_conduction(fse.lib().fse_material_find(name.encode()),
                                                      buf.ctypes.data_as(ctypes.c_void_p)) == 0
         assert int(buf[3:4].view(np.int32)[0]) == t, name
+
+
+def test_tile_layout_matches_reference():
+    """TILE_DTYPE, its fse_tile_layout and FSE_TILE_LAYOUT_MATERIAL_INSTANCE against
+    sizeof / offsetof of the reference's own MaterialInstance class
+    (game_datastruct.hpp:206-224), compiled unchanged."""
+    from oracle.binding import HERE
+
+    _ref_table()  # builds the harness
+    lib = C.CDLL(os.path.join(HERE, "_ref", "libref_materials.so"))
+    ref = np.zeros(9, np.int32)
+    lib.ref_tile_layout.restype = None
+    lib.ref_tile_layout(ref.ctypes.data_as(C.c_void_p))
+    import falling_sand_engine_gb300 as fse
+    from falling_sand_engine_gb300._abi import FseTileLayout
+
+    lay = FseTileLayout.of(fse.TILE_DTYPE)
+    assert [getattr(lay, k) for k, _ in FseTileLayout._fields_] == ref.tolist()
+    hdr = open(os.path.join(os.path.dirname(HERE), "include", "fse.h")).read()
+    m = re.search(r"#define FSE_TILE_LAYOUT_MATERIAL_INSTANCE \{([^}]*)\}", hdr)
+    assert [int(v) for v in m.group(1).split(",")] == ref.tolist()
