@@ -375,6 +375,10 @@ class World:
         return phases
 
     # -- exact checkpoints
+    def trim(self):
+        """Free the device scratch kept by pack / unpack / the tile-struct calls."""
+        check(self.lib.fse_world_trim(self.h), "trim")
+
     def checkpoint(self):
         """Every plane, particle, the tick, seed and ledger, LZ4-compressed: bytes."""
         nb, size = C.c_int64(0), C.c_int64(0)

@@ -82,6 +82,7 @@ SIGNATURES = {
     "fse_world_unpack": (_i, [_vp, _vp, _vp, _i, _vp, _vp]),
     "fse_world_checkpoint_bound": (_i, [_vp, _vp]),
     "fse_world_upload_tiles": (_i, [_vp, _vp, _vp]),
+    "fse_world_trim": (_i, [_vp]),
     "fse_world_download_tiles": (_i, [_vp, _vp, _vp, _vp, _i]),
     "fse_world_checkpoint": (_i, [_vp, _vp, _i64, _vp]),
     "fse_world_restore": (_i, [_vp, _vp, _i64]),

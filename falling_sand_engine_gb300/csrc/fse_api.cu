@@ -705,6 +705,8 @@ static void free_world(fse_world *w) {
                   w->isl_out,   w->isl_pix,  w->isl_tab,  w->isl_seg,  w->temp_io, w->tile_stage};
     for (void *q : rs)
         if (q) cudaFree(q);
+    for (void *q : w->pk_scr)
+        if (q) cudaFree(q);
     if (w->own_stream && w->stream) cudaStreamDestroy(w->stream);
     if (w->timer) {
         w->timer->drain();

@@ -63,6 +63,9 @@ struct fse_world {
     // array-of-structs tile staging (allocated on first use)
     uint8_t *tile_stage;
     size_t tile_stage_bytes;
+    // pack / unpack scratch, grown on first use and kept until fse_world_trim
+    void *pk_scr[16];
+    size_t pk_scr_bytes[16];
 };
 
 namespace fse {

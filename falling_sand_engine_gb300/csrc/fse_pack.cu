@@ -25,11 +25,14 @@
 // On generated worlds the blocks come out smaller than those of the reference's
 // LZ4_compress_fast(..., 10). k_pack_assemble writes headers and blocks.
 //
-// Reading. k_lz4_decode decodes each block with one warp: tokens, lengths and
-// literals come through a shared-memory window of the input, and matches whose
-// offset fits a shared-memory ring of the latest output are copied from it (others
-// from HBM). Every length and offset is checked against both buffers: a malformed
-// block yields a negative status and no access out of bounds. k_unpack_check
+// Reading. k_lz4_decode gives each block a CTA of two warps: the block is loaded
+// whole into shared memory, warp 0 parses its sequences (tokens, lengths, offsets)
+// into one half of a queue while warp 1 copies the sequences of the other half, and
+// matches whose offset fits a shared-memory ring of the latest output are copied
+// from it (others from HBM). Blocks longer than the shared-memory cap are decoded
+// by one warp through a window of the input. Every length and offset is checked
+// against both buffers: a malformed block yields a negative status and no access
+// out of bounds. k_unpack_check
 // rejects material indices outside the table; k_unpack_scatter writes id, colour
 // and temperature into the planes (a SOUP tile's amount is the MaterialInstance
 // default 2.0, game_datastruct.hpp:216).
@@ -377,12 +380,6 @@ __global__ void k_pack_assemble(const uint8_t *__restrict__ enc1, int slot1, con
 // ------------------------------------------------------------------ decode
 constexpr int DEC_WIN = 2048;   // input window per warp
 constexpr int DEC_RING = 8192;  // latest output per warp
-constexpr int DEC_WARPS = 4;
-
-struct DecSmem {
-    uint8_t win[DEC_WARPS][DEC_WIN];
-    uint8_t ring[DEC_WARPS][DEC_RING];
-};
 
 // the input window holds src[wb, wb + DEC_WIN) (clipped to n); reads outside it
 // refill it at the requested position
@@ -476,19 +473,292 @@ __device__ int warp_lz4_decode(const uint8_t *src, int n, uint8_t *dst, int cap,
     }
 }
 
+// ---- the pipelined decoder: a whole block in shared memory, one warp parsing
+// sequences into a double-buffered queue while the other copies them
+constexpr int DEC_BATCH = 128;                // sequences per queue half
+constexpr int DEC_CAP_MAX = 64 * 1024;        // largest block held whole in shared memory
+constexpr int DEC_FIXED = 2 * DEC_BATCH * 16 + DEC_RING + 32;
+
+// an extended length (LZ4's 255-continued bytes) read by the whole warp, 32 bytes
+// per step: adds the bytes to len and moves ip past them; false when the input ends
+// first or len passes cap
+__device__ __forceinline__ bool ext_len(const uint8_t *c, int n, int &ip, int &len, int cap) {
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        const int p = ip + lane;
+        const int b = p < n ? (int)c[p] : -1;
+        const unsigned stop = __ballot_sync(0xffffffffu, b != 255);
+        if (!stop) {
+            len += 255 * 32;
+            ip += 32;
+            if (len > cap) return false;
+            continue;
+        }
+        const int k = __ffs(stop) - 1;
+        const int bk = __shfl_sync(0xffffffffu, b, k);
+        if (bk < 0) return false;
+        len += 255 * k + bk;
+        ip += k + 1;
+        return len <= cap;
+    }
+}
+
+// one sequence at ip (all lanes, same values): {literal start, literal length,
+// offset, match length} in d; 1 = the last sequence (literals only), 0 = more,
+// negative = malformed (the same conditions as warp_lz4_decode)
+__device__ __forceinline__ int parse_seq(const uint8_t *c, const uint32_t *area32, int pad, int n, int cap, int &ip,
+                                         int &op, int4 &d) {
+    if (ip + 8 <= n) {
+        // the common sequence from eight bytes at ip (three aligned words): at most
+        // four literals, the offset and at most one extra match-length byte inside
+        const int pos = pad + ip, w = pos >> 2, sh = (pos & 3) * 8;
+        const uint32_t a = area32[w], b = area32[w + 1], e = area32[w + 2];
+        const uint64_t v = ((uint64_t)__funnelshift_r(b, e, sh) << 32) | __funnelshift_r(a, b, sh);
+        const int token = (int)(v & 255), ll = token >> 4, m4 = token & 15;
+        const int x = m4 == 15 ? (int)((v >> (8 * (3 + ll))) & 255) : 0;
+        if (ll <= 4 && x < 255) {
+            if (ll > cap - op) return -3;
+            d.x = ip + 1;
+            d.y = ll;
+            op += ll;
+            const int off = (int)((v >> (8 * (1 + ll))) & 0xffff);
+            if (off == 0 || off > op) return -5;
+            const int ml = m4 + x + 4;
+            ip += 3 + ll + (m4 == 15);
+            if (ml > cap - op) return -7;
+            d.z = off;
+            d.w = ml;
+            op += ml;
+            return 0;
+        }
+    }
+    if (ip >= n) return -1;
+    const int token = c[ip++];
+    int ll = token >> 4;
+    if (ll == 15) {
+        const int b = ip < n ? (int)c[ip] : -1;
+        if (b >= 0 && b < 255) {
+            ll += b;
+            ip++;
+        } else if (!ext_len(c, n, ip, ll, cap)) {
+            return -3;
+        }
+    }
+    if (ll > n - ip || ll > cap - op) return -3;
+    d.x = ip;
+    d.y = ll;
+    ip += ll;
+    op += ll;
+    if (ip == n) {
+        d.z = d.w = 0;
+        return 1;
+    }
+    if (n - ip < 2) return -4;
+    const int off = c[ip] | (c[ip + 1] << 8);
+    ip += 2;
+    if (off == 0 || off > op) return -5;
+    int ml = token & 15;
+    if (ml == 15) {
+        const int b = ip < n ? (int)c[ip] : -1;
+        if (b >= 0 && b < 255) {
+            ml += b;
+            ip++;
+        } else if (!ext_len(c, n, ip, ml, cap)) {
+            return -7;
+        }
+    }
+    ml += 4;
+    if (ml > cap - op) return -7;
+    d.z = off;
+    d.w = ml;
+    op += ml;
+    return 0;
+}
+
+// out[k0 + j] = src[spos + j] for j < len, by the warp, into the block's output
+// and the ring. Source bytes are src8[pos & smask] (the ring: smask = DEC_RING - 1;
+// linear buffers: -1); none of them is written by the copy. Runs of 128 bytes and
+// more move as aligned 4-byte words of the output, each built from two aligned
+// source words with a funnel shift; the rest bytewise.
+__device__ __forceinline__ void copy_run(uint8_t *dst, uint8_t *ring, const uint8_t *src8, int smask, int k0, int spos,
+                                         int len, int lane) {
+    if (len < 128 || ((uintptr_t)dst & 3)) {
+        for (int i = lane; i < len; i += 32) {
+            const uint8_t v = src8[(spos + i) & smask];
+            dst[k0 + i] = v;
+            ring[(k0 + i) & (DEC_RING - 1)] = v;
+        }
+        return;
+    }
+    const int head = (4 - (k0 & 3)) & 3;
+    const int nw = (len - head) >> 2;
+    const int t0 = head + 4 * nw;  // first tail byte, relative to k0
+    if (lane < head) {
+        const uint8_t v = src8[(spos + lane) & smask];
+        dst[k0 + lane] = v;
+        ring[(k0 + lane) & (DEC_RING - 1)] = v;
+    } else if (lane >= 4 && lane - 4 < len - t0) {
+        const int j = t0 + lane - 4;
+        const uint8_t v = src8[(spos + j) & smask];
+        dst[k0 + j] = v;
+        ring[(k0 + j) & (DEC_RING - 1)] = v;
+    }
+    const uint32_t *src32 = reinterpret_cast<const uint32_t *>(src8);
+    uint32_t *dst32 = reinterpret_cast<uint32_t *>(dst);
+    uint32_t *ring32 = reinterpret_cast<uint32_t *>(ring);
+    const int s0 = spos + head, sh = (s0 & 3) * 8, sw = s0 >> 2, a0 = (k0 + head) >> 2;
+    const int wmask = smask >> 2;  // -1 stays -1
+    for (int i = lane; i < nw; i += 32) {
+        const uint32_t w0 = src32[(sw + i) & wmask];
+        const uint32_t v = sh ? __funnelshift_r(w0, src32[(sw + i + 1) & wmask], sh) : w0;
+        dst32[a0 + i] = v;
+        ring32[(a0 + i) & (DEC_RING / 4 - 1)] = v;
+    }
+}
+
+// a match of ml bytes at op, offset off: out[op + j] = out[op + j - off]. Rounds
+// copy from distance D, a multiple of off (every such distance repeats the
+// pattern once op + j - D >= op - off), so no round reads what it writes: D starts
+// at off and doubles while the source stays readable (from the ring: D <= half of
+// it, so a round of at most D bytes overwrites no slot it reads).
+__device__ __forceinline__ void copy_match(uint8_t *dst, uint8_t *ring, int op, int off, int ml, int lane) {
+    const bool from_ring = off <= DEC_RING / 2;
+    const uint8_t *s8 = from_ring ? ring : dst;
+    const int smask = from_ring ? DEC_RING - 1 : -1;
+    int D = off;
+    for (int done = 0; done < ml;) {
+        const int len = min(ml - done, D);
+        copy_run(dst, ring, s8, smask, op + done, op + done - D, len, lane);
+        __syncwarp();
+        done += len;
+        if (!from_ring || 2 * D <= DEC_RING / 2) D *= 2;
+    }
+}
+
+// the parser warp: up to DEC_BATCH sequences into queue half `buf`; the count, whether
+// more follow, and the result so far (decoded size or error) go to shared memory
+__device__ __forceinline__ void parse_batch(const uint8_t *c, const uint32_t *area32, int pad, int n, int cap, int &ip,
+                                            int &pop, int &state, int4 *desc, int *s_cnt, int *s_more, int *s_res,
+                                            int buf, int lane) {
+    int k = 0;
+    while (k < DEC_BATCH && state == 0) {
+        int4 d;
+        const int r = parse_seq(c, area32, pad, n, cap, ip, pop, d);
+        if (r < 0) {
+            state = r;
+            break;
+        }
+        if (lane == 0) desc[buf * DEC_BATCH + k] = d;
+        k++;
+        if (r == 1) state = 1;
+    }
+    if (lane == 0) {
+        s_cnt[buf] = k;
+        s_more[buf] = state == 0;
+        *s_res = state < 0 ? state : pop;
+    }
+}
+
 // block b: src + offs[b], lens[b] bytes -> out + b * slot; status[b] = decoded
-// size or a negative error
-__global__ void __launch_bounds__(DEC_WARPS * 32) k_lz4_decode(const uint8_t *__restrict__ src,
-                                                               const long long *__restrict__ offs,
-                                                               const int *__restrict__ lens, int n_blocks, int expect,
-                                                               uint8_t *out, int slot, int *status) {
-    __shared__ DecSmem S;
-    const int wi = threadIdx.x / 32, lane = threadIdx.x & 31;
-    const int b = blockIdx.x * DEC_WARPS + wi;
+// size or a negative error. 64 threads per block; blocks longer than cap_in bytes
+// are decoded by warp_lz4_decode through a window.
+__global__ void __launch_bounds__(64, 1) k_lz4_decode(const uint8_t *__restrict__ src, const long long *__restrict__ offs,
+                                                   const int *__restrict__ lens, int n_blocks, int expect,
+                                                   uint8_t *out, int slot, int *status, int cap_in) {
+    extern __shared__ __align__(16) uint8_t dsm[];
+    int4 *desc = reinterpret_cast<int4 *>(dsm);  // [2][DEC_BATCH]
+    uint8_t *ring = dsm + 2 * DEC_BATCH * 16;
+    uint8_t *area = ring + DEC_RING;             // cap_in + 32 bytes
+    __shared__ int s_cnt[2], s_more[2], s_res;
+    const int b = blockIdx.x;
     if (b >= n_blocks) return;
-    int r = -8;
-    if (lens[b] > 0) r = warp_lz4_decode(src + offs[b], lens[b], out + (size_t)b * slot, expect, S.win[wi], S.ring[wi]);
-    if (lane == 0) status[b] = r;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n = lens[b];
+    const uint8_t *in = src + offs[b];
+    uint8_t *dst = out + (size_t)b * slot;
+    if (n <= 0) {
+        if (threadIdx.x == 0) status[b] = -8;
+        return;
+    }
+    if (n > cap_in) {
+        if (warp == 0) {
+            const int r = warp_lz4_decode(in, n, dst, expect, area, ring);
+            if (lane == 0) status[b] = r;
+        }
+        return;
+    }
+    // the block into shared memory: unaligned head and tail bytewise, the rest as
+    // aligned 16-byte words (c[i] == in[i])
+    const int head = min(n, (int)((16 - ((uintptr_t)in & 15)) & 15));
+    const int nvec = (n - head) >> 4;
+    uint8_t *c = area + ((16 - head) & 15);
+    if (threadIdx.x < head) c[threadIdx.x] = in[threadIdx.x];
+    for (int i = head + nvec * 16 + threadIdx.x; i < n; i += 64) c[i] = in[i];
+    {
+        const uint4 *vs = reinterpret_cast<const uint4 *>(in + head);
+        uint4 *vd = reinterpret_cast<uint4 *>(c + head);
+        int i = threadIdx.x;
+        for (; i + 192 < nvec; i += 256) {
+            const uint4 a0 = vs[i], a1 = vs[i + 64], a2 = vs[i + 128], a3 = vs[i + 192];
+            vd[i] = a0;
+            vd[i + 64] = a1;
+            vd[i + 128] = a2;
+            vd[i + 192] = a3;
+        }
+        for (; i < nvec; i += 64) vd[i] = vs[i];
+    }
+    __syncthreads();
+    int ip = 0, pop = 0, state = 0;  // parser: input and output positions, 0 / 1 done / error
+    const uint32_t *area32 = reinterpret_cast<const uint32_t *>(area);
+    const int pad = (int)(c - area);  // c[i] == area[pad + i]
+    if (warp == 0) parse_batch(c, area32, pad, n, expect, ip, pop, state, desc, s_cnt, s_more, &s_res, 0, lane);
+    __syncthreads();
+    int op = 0, buf = 0;  // copier: output position
+    for (;;) {
+        const int cnt = s_cnt[buf];
+        const bool more = s_more[buf] != 0;
+        if (warp == 0) {
+            if (more)
+                parse_batch(c, area32, pad, n, expect, ip, pop, state, desc, s_cnt, s_more, &s_res, buf ^ 1, lane);
+        } else {
+            for (int k = 0; k < cnt; k++) {
+                const int4 d = desc[buf * DEC_BATCH + k];
+                const int ll = d.y, off = d.z, ml = d.w, tot = ll + ml;
+                if (tot <= 32 && off >= ml && off <= DEC_RING - 32) {
+                    // one step: byte j is literal j, or the match's byte from j - off,
+                    // which lies in this literal (>= 0) or before op (in the ring)
+                    if (lane < tot) {
+                        const int sidx = lane < ll ? lane : lane - off;
+                        const uint8_t v = sidx >= 0 ? c[d.x + sidx] : ring[(op + sidx) & (DEC_RING - 1)];
+                        dst[op + lane] = v;
+                        ring[(op + lane) & (DEC_RING - 1)] = v;
+                    }
+                    __syncwarp();
+                } else {
+                    copy_run(dst, ring, area, -1, op, pad + d.x, ll, lane);
+                    __syncwarp();  // the bytes the match reads are written
+                    if (ml) copy_match(dst, ring, op + ll, off, ml, lane);
+                }
+                op += tot;
+            }
+        }
+        if (!more) break;
+        __syncthreads();
+        buf ^= 1;
+    }
+    if (threadIdx.x == 0) status[b] = s_res;
+}
+
+// decode n_blocks blocks whose longest is max_len bytes
+void launch_decode(const uint8_t *src, const long long *offs, const int *lens, int n_blocks, int max_len, int expect,
+                   uint8_t *out, int slot, int *status, cudaStream_t s) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_lz4_decode, cudaFuncAttributeMaxDynamicSharedMemorySize, DEC_FIXED + DEC_CAP_MAX);
+        attr = true;
+    }
+    const int cap_in = std::max(DEC_WIN, std::min(DEC_CAP_MAX, (max_len + 15) & ~15));
+    k_lz4_decode<<<n_blocks, 64, DEC_FIXED + cap_in, s>>>(src, offs, lens, n_blocks, expect, out, slot, status, cap_in);
 }
 
 // chunks whose records name a material outside the table: the lowest such chunk
@@ -563,6 +833,47 @@ int fse_world_pack_bound(int width, int height, int64_t *out_bytes, int *out_chu
     return FSE_OK;
 }
 
+}  // extern "C"
+
+namespace fse {
+namespace {
+// the world's pack scratch buffer k, at least `bytes` long (contents not kept)
+template <typename T>
+bool scratch(fse_world *w, int k, T **p, size_t bytes) {
+    bytes = std::max<size_t>(bytes, 16);
+    if (!w->pk_scr[k] || w->pk_scr_bytes[k] < bytes) {
+        if (w->pk_scr[k]) cudaFree(w->pk_scr[k]);
+        w->pk_scr[k] = nullptr;
+        w->pk_scr_bytes[k] = 0;
+        if (cudaMalloc(&w->pk_scr[k], bytes) != cudaSuccess) {
+            w->pk_scr[k] = nullptr;
+            *p = nullptr;
+            return false;
+        }
+        w->pk_scr_bytes[k] = bytes;
+    }
+    *p = static_cast<T *>(w->pk_scr[k]);
+    return true;
+}
+}  // namespace
+}  // namespace fse
+
+extern "C" {
+
+int fse_world_trim(fse_world *w) {
+    if (!w) return FSE_E_INVAL;
+    FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
+    for (int k = 0; k < 16; k++) {
+        if (w->pk_scr[k]) cudaFree(w->pk_scr[k]);
+        w->pk_scr[k] = nullptr;
+        w->pk_scr_bytes[k] = 0;
+    }
+    if (w->tile_stage) cudaFree(w->tile_stage);
+    w->tile_stage = nullptr;
+    w->tile_stage_bytes = 0;
+    return FSE_OK;
+}
+
 int fse_world_pack(fse_world *w, int generation_phase, uint8_t *out, int64_t cap, int64_t *offsets, int *out_n_chunks) {
     if (!w || !out || !offsets) return FSE_E_INVAL;
     int rc = ensure_materials_pushed();
@@ -577,21 +888,13 @@ int fse_world_pack(fse_world *w, int generation_phase, uint8_t *out, int64_t cap
     SegInfo *info = nullptr;
     long long *doffs = nullptr;
     cudaStream_t s = w->stream;
-    auto cleanup = [&]() {
-        void *ps[] = {stage, enc1, enc2, dout, sizes, doffs, anc, sout, info};
-        for (void *q : ps)
-            if (q) cudaFree(q);
-    };
-    if (cudaMalloc(&stage, (size_t)G * PK_TILES) != cudaSuccess || cudaMalloc(&enc1, (size_t)G * PK_SLOT1) != cudaSuccess ||
-        cudaMalloc(&enc2, PK_SLOT2) != cudaSuccess || cudaMalloc(&sizes, (size_t)(G + 1) * sizeof(int)) != cudaSuccess ||
-        cudaMalloc(&doffs, (size_t)G * sizeof(long long)) != cudaSuccess ||
-        cudaMalloc(&dout, (size_t)G * (PK_HEADER + PK_SLOT1 + PK_SLOT2)) != cudaSuccess ||
-        cudaMalloc(&info, (size_t)G * ENC_MAXSEG * sizeof(SegInfo)) != cudaSuccess ||
-        cudaMalloc(&anc, (size_t)G * ENC_MAXSEG * sizeof(int)) != cudaSuccess ||
-        cudaMalloc(&sout, (size_t)G * ENC_MAXSEG * sizeof(int)) != cudaSuccess) {
-        cleanup();
+    if (!scratch(w, 0, &stage, (size_t)G * PK_TILES) || !scratch(w, 1, &enc1, (size_t)G * PK_SLOT1) ||
+        !scratch(w, 2, &enc2, PK_SLOT2) || !scratch(w, 3, &sizes, (size_t)(G + 1) * sizeof(int)) ||
+        !scratch(w, 4, &doffs, (size_t)G * sizeof(long long)) ||
+        !scratch(w, 5, &info, (size_t)G * ENC_MAXSEG * sizeof(SegInfo)) ||
+        !scratch(w, 6, &anc, (size_t)G * ENC_MAXSEG * sizeof(int)) ||
+        !scratch(w, 7, &sout, (size_t)G * ENC_MAXSEG * sizeof(int)))
         return FSE_E_NOMEM;
-    }
     // the background block: 64 KB of zeros, the same for every chunk
     encode_blocks(stage, 0, PK_SRC2, 1, enc2, PK_SLOT2, sizes + G, info, anc, sout, s);
     int size2 = 0;
@@ -620,6 +923,10 @@ int fse_world_pack(fse_world *w, int generation_phase, uint8_t *out, int64_t cap
             rc = FSE_E_CAPACITY;
             break;
         }
+        if (!scratch(w, 8, &dout, (size_t)rel)) {
+            rc = FSE_E_NOMEM;
+            break;
+        }
         if (cudaMemcpyAsync(doffs, offs.data(), g * sizeof(long long), cudaMemcpyHostToDevice, s) != cudaSuccess) {
             rc = FSE_E_CUDA;
             break;
@@ -635,7 +942,6 @@ int fse_world_pack(fse_world *w, int generation_phase, uint8_t *out, int64_t cap
     }
     if (rc == FSE_OK) offsets[nch] = pos;
     count_launches(3 + 5LL * ((nch + G - 1) / G));
-    cleanup();
     return rc;
 }
 
@@ -677,26 +983,16 @@ int fse_world_unpack(fse_world *w, const uint8_t *in, const int64_t *offsets, in
     long long *doff = nullptr;
     int *dlen = nullptr, *dst = nullptr;
     cudaStream_t s = w->stream;
-    auto cleanup = [&]() {
-        void *ps[] = {din, rec, bgo, doff, dlen, dst};
-        for (void *q : ps)
-            if (q) cudaFree(q);
-    };
-    if (cudaMalloc(&rec, (size_t)G * PK_SRC1) != cudaSuccess || cudaMalloc(&bgo, (size_t)G * PK_SRC2) != cudaSuccess ||
-        cudaMalloc(&doff, (size_t)2 * G * sizeof(long long)) != cudaSuccess ||
-        cudaMalloc(&dlen, (size_t)2 * G * sizeof(int)) != cudaSuccess ||
-        cudaMalloc(&dst, (size_t)(2 * G + 1) * sizeof(int)) != cudaSuccess) {
-        cleanup();
+    if (!scratch(w, 9, &rec, (size_t)G * PK_SRC1) || !scratch(w, 10, &bgo, (size_t)G * PK_SRC2) ||
+        !scratch(w, 11, &doff, (size_t)2 * G * sizeof(long long)) || !scratch(w, 12, &dlen, (size_t)2 * G * sizeof(int)) ||
+        !scratch(w, 13, &dst, (size_t)(2 * G + 1) * sizeof(int)))
         return FSE_E_NOMEM;
-    }
     std::vector<int> st(2 * G);
     for (int c0 = 0; c0 < bad && rc == FSE_OK; c0 += G) {
         const int g = std::min(G, bad - c0);
         // the group's input, one copy
         const long long lo = offsets[c0], hi = offsets[c0 + g];
-        if (din) cudaFree(din);
-        din = nullptr;
-        if (cudaMalloc(&din, (size_t)(hi - lo)) != cudaSuccess) {
+        if (!scratch(w, 14, &din, (size_t)(hi - lo))) {
             rc = FSE_E_NOMEM;
             break;
         }
@@ -716,10 +1012,9 @@ int fse_world_unpack(fse_world *w, const uint8_t *in, const int64_t *offsets, in
             rc = FSE_E_CUDA;
             break;
         }
-        k_lz4_decode<<<(g + DEC_WARPS - 1) / DEC_WARPS, DEC_WARPS * 32, 0, s>>>(din, doff, dlen, g, PK_SRC1, rec,
-                                                                              PK_SRC1, dst);
-        k_lz4_decode<<<(g + DEC_WARPS - 1) / DEC_WARPS, DEC_WARPS * 32, 0, s>>>(din, doff + g, dlen + g, g, PK_SRC2,
-                                                                              bgo, PK_SRC2, dst + g);
+        launch_decode(din, doff, dlen, g, *std::max_element(hl.begin(), hl.begin() + g), PK_SRC1, rec, PK_SRC1, dst, s);
+        launch_decode(din, doff + g, dlen + g, g, *std::max_element(hl.begin() + g, hl.end()), PK_SRC2, bgo, PK_SRC2,
+                      dst + g, s);
         k_unpack_check<<<grid_for((long long)g * PK_CELLS, 256), 256, 0, s>>>(rec, PK_SRC1, g, nmat, dst + 2 * G);
         int first_bad_id = big;
         if (cudaMemcpyAsync(st.data(), dst, 2 * g * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
@@ -738,7 +1033,6 @@ int fse_world_unpack(fse_world *w, const uint8_t *in, const int64_t *offsets, in
         if (gbad < g) bad = c0 + gbad;
     }
     if (rc == FSE_OK && cudaStreamSynchronize(s) != cudaSuccess) rc = FSE_E_CUDA;
-    cleanup();
     if (rc) return rc;
     if (bad < nch) {
         if (out_bad_chunk) *out_bad_chunk = bad;
@@ -912,11 +1206,11 @@ int ck_read_section(const CkSection &sec, In &in, CkScratch &sc, cudaStream_t s)
             return FSE_E_CUDA;
         uint8_t *dst = (uint8_t *)sec.dev + (int64_t)g0 * CK_BLOCK;
         if (full)
-            k_lz4_decode<<<(full + DEC_WARPS - 1) / DEC_WARPS, DEC_WARPS * 32, 0, s>>>(sc.din, sc.doff, sc.dlen, full,
-                                                                                    CK_BLOCK, dst, CK_BLOCK, sc.status);
+            launch_decode(sc.din, sc.doff, sc.dlen, full, *std::max_element(len.begin(), len.begin() + full), CK_BLOCK,
+                          dst, CK_BLOCK, sc.status, s);
         if (tail)
-            k_lz4_decode<<<1, DEC_WARPS * 32, 0, s>>>(sc.din, sc.doff + full, sc.dlen + full, 1, tail,
-                                                     dst + (size_t)full * CK_BLOCK, CK_BLOCK, sc.status + full);
+            launch_decode(sc.din, sc.doff + full, sc.dlen + full, 1, len[full], tail, dst + (size_t)full * CK_BLOCK,
+                          CK_BLOCK, sc.status + full, s);
         count_launches((full ? 1 : 0) + (tail ? 1 : 0));
         if (cudaMemcpyAsync(st.data(), sc.status, g * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
             cudaStreamSynchronize(s) != cudaSuccess)

@@ -241,6 +241,9 @@ int fse_world_pack(fse_world *world, int generation_phase, uint8_t *out, int64_t
  * before it written, none after. */
 int fse_world_unpack(fse_world *world, const uint8_t *in, const int64_t *offsets, int n_chunks, int8_t *out_phases,
                      int *out_bad_chunk);
+/* Pack, unpack and the tile-struct calls keep their device scratch (about 1 MB per
+ * chunk for pack and unpack) between calls; this frees it. */
+int fse_world_trim(fse_world *world);
 
 /* Exact checkpoint of a world (the .pack files keep only material, colour and
  * temperature): every plane, the particle list, the tick counter, seed and ledger,

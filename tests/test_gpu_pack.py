@@ -114,6 +114,44 @@ def test_unpack_rejects_malformed(fse, oracle_mod):
             assert np.array_equal(gs[key], os_[key]), (key, k)
 
 
+def test_large_blocks_odd_offsets_and_trim(fse, oracle_mod):
+    """Chunks whose colours are noise give tile blocks over 64 KB (decoded through the
+    input window) beside ordinary ones (decoded whole from shared memory), in one
+    launch; the files start at every offset mod 16; scratch freed by trim is made
+    again."""
+    oracle_mod.Oracle().reset_materials()
+    w, h = 384, 256
+    ow = sample_world(oracle_mod, w, h, 21)
+    st = ow.state()
+    rng = np.random.default_rng(21)
+    noisy = np.zeros((h, w), bool)
+    noisy[:128, 128:256] = True
+    noisy[128:, :128] = True
+    st["colour"] = np.where(noisy, rng.integers(0, 2 ** 32, (h, w), dtype=np.uint64).astype(np.uint32), st["colour"])
+    ow.set_state(st)
+    world = _device_copy(fse, ow, w, h)
+    data, offs = world.pack(2)
+    odata, ooffs = ow.pack(2)
+    assert np.array_equal(offs, ooffs) and np.array_equal(data, odata)
+    sizes = [split_blocks(data, offs, k)[0][1] for k in range(len(offs) - 1)]
+    assert max(sizes) > 64 * 1024 and min(sizes) < 32 * 1024, sizes
+    for shift in range(16):
+        buf = np.concatenate([np.full(shift, 0xA5, np.uint8), data])
+        b = fse.World(w, h, seed=1, temperature=True)
+        assert np.all(b.unpack(buf, offs + shift) == 2)
+        sb = b.state()
+        assert np.array_equal(sb["id"], st["id"]) and np.array_equal(sb["colour"], st["colour"]), shift
+        assert np.array_equal(b.temperature(), ow.temperature()), shift
+        if shift == 15:
+            b.trim()
+            b.trim()
+            assert np.all(b.unpack(buf, offs + shift) == 2)
+            d2, o2 = b.pack(2)
+            assert np.array_equal(o2, offs) and np.array_equal(d2, data)
+        b.close()
+    world.close()
+
+
 def _same_world(fse, a, b, temperature):
     for k, v in a.state().items():
         assert np.array_equal(v, b.state()[k]), k
