@@ -166,9 +166,11 @@ __device__ int emit_seq(Src &s, uint8_t *dst, int op, int cap, int ls, int nl, i
 // block). A segment's first sequence takes over the literals left at the end of
 // the segments before it, so writing needs each segment's start of literals
 // (its `anchor`): k_lz4_parse records per segment what writing it costs apart
-// from that first literal run, k_lz4_plan carries the anchors and places the
-// segments, and k_lz4_emit parses again and writes.
+// from that first literal run, and its matches (position, distance, length; up to
+// ENC_REC of them), k_lz4_plan carries the anchors and places the segments, and
+// k_lz4_emit writes the recorded matches (a segment with more parses again).
 constexpr int ENC_SEG = 24576;
+constexpr int ENC_REC = 1024;  // matches recorded per segment
 struct SegInfo {
     int m;       // sequences with a match that start in the segment
     int first;   // the position of its first match (when m > 0)
@@ -182,7 +184,8 @@ __host__ __device__ __forceinline__ int len_bytes(int v) { return v >= 15 ? (v -
 // the output position after the segment's sequences (EMIT) or -1 when they would
 // not fit in cap, and leaves in `anchor` the start of the literals after them
 template <bool EMIT>
-__device__ int seg_run(Src &s, int n, int a, int b, int &anchor, uint8_t *dst, int op, int cap, SegInfo *info) {
+__device__ int seg_run(Src &s, int n, int a, int b, int &anchor, uint8_t *dst, int op, int cap, SegInfo *info,
+                       uint2 *rec) {
     const int lane = threadIdx.x & 31;
     const int mflimit = n - 12, mend = n - 5;
     const int lim = min(mend, b);       // a match ends at the latest here
@@ -275,10 +278,12 @@ __device__ int seg_run(Src &s, int n, int a, int b, int &anchor, uint8_t *dst, i
         const unsigned key = (lane < 16 && ((cm >> lane) & 1u)) ? ((unsigned)L << 4) | (unsigned)(15 - lane) : 0u;
         const unsigned top_key = __reduce_max_sync(FULL, key);
         const int best = (int)(top_key >> 4);
-        const int bd = c_dist[15 - (int)(top_key & 15u)];
+        const int bk = 15 - (int)(top_key & 15u);
+        const int bd = c_dist[bk];
         if (EMIT) {
             op = emit_seq(s, dst, op, cap, anchor, q0 - anchor, bd, best);
         } else {
+            if (lane == 0 && m < ENC_REC) rec[m] = make_uint2(((unsigned)q0 << 4) | (unsigned)bk, (unsigned)best);
             const int mpart = 2 + len_bytes(best - 4);
             if (m == 0) {
                 first = q0;
@@ -298,7 +303,7 @@ __device__ int seg_run(Src &s, int n, int a, int b, int &anchor, uint8_t *dst, i
 
 // phase 1: one warp per (block, segment)
 __global__ void __launch_bounds__(ENC_WARPS * 32) k_lz4_parse(const uint32_t *__restrict__ stage, int T, int n,
-                                                             int n_blocks, SegInfo *info) {
+                                                             int n_blocks, SegInfo *info, uint2 *rec) {
     __shared__ uint32_t s_win[ENC_WARPS][ENC_WIN / 4];
     const int nseg = (n + ENC_SEG - 1) / ENC_SEG;
     const int u = blockIdx.x * ENC_WARPS + threadIdx.x / 32;
@@ -307,7 +312,8 @@ __global__ void __launch_bounds__(ENC_WARPS * 32) k_lz4_parse(const uint32_t *__
     Src s{stage + (size_t)b * (T / 4), T, s_win[threadIdx.x / 32], 0};
     s.fill(max(k * ENC_SEG - ENC_BACK, 0) & ~3);
     int anchor = 0;
-    seg_run<false>(s, n, k * ENC_SEG, min(n, (k + 1) * ENC_SEG), anchor, nullptr, 0, 0, info + u);
+    seg_run<false>(s, n, k * ENC_SEG, min(n, (k + 1) * ENC_SEG), anchor, nullptr, 0, 0, info + u,
+                   rec + (size_t)u * ENC_REC);
 }
 
 // phase 2: one thread per block: each segment's first literal start and output
@@ -339,7 +345,9 @@ __global__ void k_lz4_plan(const SegInfo *__restrict__ info, int n, int n_blocks
 __global__ void __launch_bounds__(ENC_WARPS * 32) k_lz4_emit(const uint32_t *__restrict__ stage, int T, int n,
                                                             int n_blocks, const int *__restrict__ seg_anchor,
                                                             const int *__restrict__ seg_out,
-                                                            const int *__restrict__ sizes, uint8_t *out, int slot) {
+                                                            const int *__restrict__ sizes, uint8_t *out, int slot,
+                                                            const SegInfo *__restrict__ info,
+                                                            const uint2 *__restrict__ rec) {
     __shared__ uint32_t s_win[ENC_WARPS][ENC_WIN / 4];
     const int nseg = (n + ENC_SEG - 1) / ENC_SEG;
     const int u = blockIdx.x * ENC_WARPS + threadIdx.x / 32;
@@ -353,7 +361,20 @@ __global__ void __launch_bounds__(ENC_WARPS * 32) k_lz4_emit(const uint32_t *__r
     // the segment writes [seg_out[u], its end); it ends where the next one starts
     const int end = (k + 1 < nseg) ? seg_out[u + 1] : sizes[b];
     int anchor = seg_anchor[u];
-    int op = seg_run<true>(s, n, a, e, anchor, dst, seg_out[u], end, nullptr);
+    int op = seg_out[u];
+    const int m = info[u].m;
+    if (m <= ENC_REC) {
+        // the recorded matches, with their literals
+        const uint2 *r = rec + (size_t)u * ENC_REC;
+        for (int i = 0; i < m && op >= 0; i++) {
+            const uint2 v = r[i];
+            const int q0 = (int)(v.x >> 4), L = (int)v.y;
+            op = emit_seq(s, dst, op, end, anchor, q0 - anchor, c_dist[v.x & 15u], L);
+            anchor = q0 + L;
+        }
+    } else {
+        op = seg_run<true>(s, n, a, e, anchor, dst, op, end, nullptr, nullptr);
+    }
     if (k + 1 == nseg && op >= 0) op = emit_seq(s, dst, op, end, anchor, n - anchor, 0, 0);  // the last sequence
 }
 
@@ -805,12 +826,12 @@ __global__ void k_unpack_scatter(const WorldDev *__restrict__ wd, const MatTable
 
 // the three encoder phases for n_blocks blocks of n bytes (T of them staged)
 void encode_blocks(const uint32_t *stage, int T, int n, int n_blocks, uint8_t *out, int slot, int *sizes,
-                   SegInfo *info, int *anc, int *sout, cudaStream_t s) {
+                   SegInfo *info, int *anc, int *sout, uint2 *rec, cudaStream_t s) {
     const int units = n_blocks * ((n + ENC_SEG - 1) / ENC_SEG);
     const int grid = (units + ENC_WARPS - 1) / ENC_WARPS;
-    k_lz4_parse<<<grid, ENC_WARPS * 32, 0, s>>>(stage, T, n, n_blocks, info);
+    k_lz4_parse<<<grid, ENC_WARPS * 32, 0, s>>>(stage, T, n, n_blocks, info, rec);
     k_lz4_plan<<<(n_blocks + 127) / 128, 128, 0, s>>>(info, n, n_blocks, slot, anc, sout, sizes);
-    k_lz4_emit<<<grid, ENC_WARPS * 32, 0, s>>>(stage, T, n, n_blocks, anc, sout, sizes, out, slot);
+    k_lz4_emit<<<grid, ENC_WARPS * 32, 0, s>>>(stage, T, n, n_blocks, anc, sout, sizes, out, slot, info, rec);
 }
 constexpr int ENC_MAXSEG = (PK_SRC1 + ENC_SEG - 1) / ENC_SEG;
 
@@ -886,6 +907,7 @@ int fse_world_pack(fse_world *w, int generation_phase, uint8_t *out, int64_t cap
     uint8_t *enc1 = nullptr, *enc2 = nullptr, *dout = nullptr;
     int *sizes = nullptr, *anc = nullptr, *sout = nullptr;
     SegInfo *info = nullptr;
+    uint2 *rec = nullptr;
     long long *doffs = nullptr;
     cudaStream_t s = w->stream;
     if (!scratch(w, 0, &stage, (size_t)G * PK_TILES) || !scratch(w, 1, &enc1, (size_t)G * PK_SLOT1) ||
@@ -893,10 +915,11 @@ int fse_world_pack(fse_world *w, int generation_phase, uint8_t *out, int64_t cap
         !scratch(w, 4, &doffs, (size_t)G * sizeof(long long)) ||
         !scratch(w, 5, &info, (size_t)G * ENC_MAXSEG * sizeof(SegInfo)) ||
         !scratch(w, 6, &anc, (size_t)G * ENC_MAXSEG * sizeof(int)) ||
-        !scratch(w, 7, &sout, (size_t)G * ENC_MAXSEG * sizeof(int)))
+        !scratch(w, 7, &sout, (size_t)G * ENC_MAXSEG * sizeof(int)) ||
+        !scratch(w, 15, &rec, (size_t)G * ENC_MAXSEG * ENC_REC * sizeof(uint2)))
         return FSE_E_NOMEM;
     // the background block: 64 KB of zeros, the same for every chunk
-    encode_blocks(stage, 0, PK_SRC2, 1, enc2, PK_SLOT2, sizes + G, info, anc, sout, s);
+    encode_blocks(stage, 0, PK_SRC2, 1, enc2, PK_SLOT2, sizes + G, info, anc, sout, rec, s);
     int size2 = 0;
     std::vector<int> sz(G);
     std::vector<long long> offs(G);
@@ -904,7 +927,7 @@ int fse_world_pack(fse_world *w, int generation_phase, uint8_t *out, int64_t cap
     for (int c0 = 0; c0 < nch && rc == FSE_OK; c0 += G) {
         const int g = std::min(G, nch - c0);
         k_pack_stage<<<grid_for((long long)g * PK_CELLS, 256), 256, 0, s>>>(w->d, g_dev_mt, stage, c0, g);
-        encode_blocks(stage, PK_TILES, PK_SRC1, g, enc1, PK_SLOT1, sizes, info, anc, sout, s);
+        encode_blocks(stage, PK_TILES, PK_SRC1, g, enc1, PK_SLOT1, sizes, info, anc, sout, rec, s);
         if (cudaMemcpyAsync(sz.data(), sizes, g * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
             (c0 == 0 && cudaMemcpyAsync(&size2, sizes + G, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) ||
             cudaStreamSynchronize(s) != cudaSuccess) {
@@ -1087,10 +1110,11 @@ struct CkScratch {
     uint8_t *enc = nullptr;
     int *sizes = nullptr, *anc = nullptr, *sout = nullptr, *status = nullptr;
     SegInfo *info = nullptr;
+    uint2 *rec = nullptr;
     uint8_t *din = nullptr;
     long long *doff = nullptr;
     int *dlen = nullptr;
-    bool ok() const { return stage && enc && sizes && anc && sout && status && info && din && doff && dlen; }
+    bool ok() const { return stage && enc && sizes && anc && sout && status && info && rec && din && doff && dlen; }
     void alloc() {
         cudaMalloc(&stage, (size_t)CK_GROUP * CK_BLOCK + 16);  // + a zeroed word after the data
         cudaMalloc(&enc, (size_t)CK_GROUP * CK_SLOT);
@@ -1099,12 +1123,13 @@ struct CkScratch {
         cudaMalloc(&sout, (size_t)CK_GROUP * CK_SEGS * sizeof(int));
         cudaMalloc(&status, (CK_GROUP + 1) * sizeof(int));
         cudaMalloc(&info, (size_t)CK_GROUP * CK_SEGS * sizeof(SegInfo));
+        cudaMalloc(&rec, (size_t)CK_GROUP * CK_SEGS * ENC_REC * sizeof(uint2));
         cudaMalloc(&din, (size_t)CK_GROUP * CK_SLOT);
         cudaMalloc(&doff, (CK_GROUP + 1) * sizeof(long long));
         cudaMalloc(&dlen, (CK_GROUP + 1) * sizeof(int));
     }
     void release() {
-        void *ps[] = {stage, enc, sizes, anc, sout, status, info, din, doff, dlen};
+        void *ps[] = {stage, enc, sizes, anc, sout, status, info, rec, din, doff, dlen};
         for (void *q : ps)
             if (q) cudaFree(q);
     }
@@ -1137,10 +1162,13 @@ int ck_write_section(const CkSection &sec, Out &o, CkScratch &sc, cudaStream_t s
             cudaMemsetAsync((uint8_t *)sc.stage + span, 0, 4, s) != cudaSuccess)  // word-aligned tail
             return FSE_E_CUDA;
         const int full = (int)(span / CK_BLOCK), tail = (int)(span - (int64_t)full * CK_BLOCK);
-        if (full) encode_blocks(sc.stage, CK_BLOCK, CK_BLOCK, full, sc.enc, CK_SLOT, sc.sizes, sc.info, sc.anc, sc.sout, s);
+        if (full)
+            encode_blocks(sc.stage, CK_BLOCK, CK_BLOCK, full, sc.enc, CK_SLOT, sc.sizes, sc.info, sc.anc, sc.sout, sc.rec,
+                          s);
         if (tail)
             encode_blocks(sc.stage + (size_t)full * (CK_BLOCK / 4), (tail + 3) & ~3, tail, 1,
-                          sc.enc + (size_t)full * CK_SLOT, CK_SLOT, sc.sizes + full, sc.info, sc.anc, sc.sout, s);
+                          sc.enc + (size_t)full * CK_SLOT, CK_SLOT, sc.sizes + full, sc.info, sc.anc, sc.sout,
+                          sc.rec, s);
         count_launches(3LL * ((full ? 1 : 0) + (tail ? 1 : 0)));
         if (cudaMemcpyAsync(sz.data(), sc.sizes, g * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
             cudaStreamSynchronize(s) != cudaSuccess)
