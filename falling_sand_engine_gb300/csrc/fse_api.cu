@@ -98,7 +98,8 @@ int add_reaction(int mid, int kind, int temp, int res) {
     HostMat &m = g_mats[mid];
     if (m.n_react >= 4) return FSE_E_INVAL;
     m.react[m.n_react][0] = kind;
-    m.react[m.n_react][1] = temp;
+    // MaterialInteraction::data1 is a mat_temperature (i16), game_datastruct.hpp:114
+    m.react[m.n_react][1] = (int16_t)temp;
     m.react[m.n_react][2] = res;
     m.n_react++;
     g_dirty = true;

@@ -480,6 +480,9 @@ __device__ __forceinline__ void rule_a(const TL &T, Ctx &c, int x, int y) {
                     if (mt->inter[i][0] != (int)t.id || mt->inter[i][1] != bid) continue;
                     int kind = mt->inter[i][2], d1 = mt->inter[i][3], d2 = mt->inter[i][4];
                     int ox = mt->inter[i][5], oy = mt->inter[i][6];
+                    // the radius is a u32 in the reference, so its loops compare
+                    // unsigned: a box whose low corner is negative is not visited
+                    if (ox - d2 < 0 || oy - d2 < 0) continue;
                     for (int xx = ox - d2; xx <= ox + d2; xx++)
                         for (int yy = oy - d2; yy <= oy + d2; yy++) {
                             bool doit = (kind == INTER_TRANSFORM)

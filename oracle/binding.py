@@ -15,6 +15,7 @@ REF_LZ4_PATH = os.path.join(HERE, "_ref", "liblz4ref.so")
 REF_CELLS_PATH = os.path.join(HERE, "_ref", "libref_cells.so")
 REF_RENDER_PATH = os.path.join(HERE, "_ref", "libref_render.so")
 REF_OBJECTS_PATH = os.path.join(HERE, "_ref", "libref_objects.so")
+REF_TICK_PATH = os.path.join(HERE, "_ref", "libref_tick.so")
 REFERENCE_WORLD_CPP = "/root/reference/source/engine/world.cpp"
 
 PARTICLE_DTYPE = np.dtype(
@@ -73,6 +74,7 @@ class Oracle:
                 "om_material_set_reaction": (i32, [i32, i32, i32, i32]),
                 "om_material_set_interaction": (i32, [i32, i32, i32, i32, i32, i32, i32]),
                 "om_material_count": (i32, []),
+                "om_material_rules": (i32, [vp, vp, i32]),
                 "om_material_find": (i32, [C.c_char_p]),
                 "om_material_get": (None, [i32, vp]),
                 "om_world_new": (vp, [i32, i32, i32, i32, u32]),
@@ -135,6 +137,14 @@ class Oracle:
 
     def find(self, index_name):
         return self.lib.om_material_find(index_name.encode())
+
+    def rules(self):
+        """(reactions (n, 4, 3), interactions (m, 7)) of the material table."""
+        n = self.material_count()
+        react = np.zeros((n, 4, 3), np.int32)
+        inter = np.zeros((4096, 7), np.int32)
+        m = self.lib.om_material_rules(_ptr(react), _ptr(inter), 4096)
+        return react, inter[:m].copy()
 
     def material(self, mid):
         out = np.zeros(16, np.int32)
@@ -483,6 +493,54 @@ def reference_tick_cells(lib_path, ids, colours, amounts, mat_types, parts):
     if rc != 0:
         raise ValueError("ref_tick_cells failed")
     return i2, c2, a2, d2, pout[: nout.value].copy()
+
+
+def build_reference_tick(force=False):
+    """Compile the reference's own world::tick (oracle/Makefile `ref`); None without the tree."""
+    if not os.path.exists(REFERENCE_WORLD_CPP):
+        return None
+    if force or not os.path.exists(REF_TICK_PATH) or os.path.getmtime(REF_TICK_PATH) < os.path.getmtime(
+            os.path.join(HERE, "ref_tick.cpp")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    return REF_TICK_PATH
+
+
+SPECIAL_MATERIALS = ("GENERIC_AIR", "GENERIC_SOLID", "FIRE", "WATER", "LAVA", "STEAM", "OBSIDIAN")
+
+
+def reference_world_tick(lib_path, oracle, ids, colours, temps, moved, cell_iter, seed, tick, n_ticks=1):
+    """n_ticks world::tick() calls of the compiled reference on a grid of non-liquid
+    tiles (ids, colours, temperatures, moved flags), with the oracle's material table
+    and the oracle's draws. Returns (ids, colours, temperatures, moved, particles as
+    (n, 16) int32 rows: id, colour, temperature, x, y, vx, vy, ax, ay, target x, y,
+    force (float bits), phase, temporary, lifetime, fade time; draws made)."""
+    lib = C.CDLL(lib_path)
+    f = lib.ref_world_tick
+    f.restype = C.c_int
+    f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint32, C.c_uint32, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                  C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                  C.c_int, C.c_void_p]
+    n = oracle.material_count()
+    mats = np.zeros((n, 10), np.int32)
+    for i in range(n):
+        m = oracle.material(i)
+        mats[i, :9] = [m[0], m[1], m[2], m[3], m[9], m[10], m[11], m[12], m[13] if m[0] != 3 else 0]
+    special = np.array([oracle.find(s) for s in SPECIAL_MATERIALS], np.int32)
+    react, inter = oracle.rules()
+    h, w = ids.shape
+    i2 = np.ascontiguousarray(ids, np.uint16).copy()
+    c2 = np.ascontiguousarray(colours, np.uint32).copy()
+    t2 = np.ascontiguousarray(temps, np.int32).copy()
+    m2 = np.ascontiguousarray(moved, np.uint8).copy()
+    cap = 1 << 16
+    parts = np.zeros((cap, 16), np.int32)
+    draws = C.c_longlong(0)
+    np_ = f(w, h, cell_iter, seed & 0xFFFFFFFF, tick & 0xFFFFFFFF, n_ticks, n, _ptr(mats), _ptr(special),
+            _ptr(np.ascontiguousarray(react)), len(inter), _ptr(np.ascontiguousarray(inter)), _ptr(i2), _ptr(c2),
+            _ptr(t2), _ptr(m2), _ptr(parts), cap, C.byref(draws))
+    if np_ < 0:
+        raise ValueError("the reference tick wrote outside the grid: the scene needs its solid border")
+    return i2, c2, t2, m2, parts[: min(np_, cap)].copy(), draws.value
 
 
 def build_reference_render(force=False):

@@ -292,7 +292,8 @@ int om_material_set_reaction(int mat, int kind, int temperature, int result) {
     mat_t *m = &M[mat];
     if (m->n_react >= 4) return -1;
     m->react[m->n_react].kind = kind;
-    m->react[m->n_react].data1 = temperature;
+    /* MaterialInteraction::data1 is a mat_temperature (i16), game_datastruct.hpp:114 */
+    m->react[m->n_react].data1 = (int16_t)temperature;
     m->react[m->n_react].data2 = result;
     m->n_react++;
     return 0;
@@ -331,6 +332,34 @@ static const inter_list_t *find_inter(int mat, int other) {
 }
 
 int om_material_count(void) { return NMAT; }
+
+/* every material's reactions (4 rows of kind, temperature, result; kind 0 = none)
+ * and the interactions in registration order (material, other, kind, data1, data2,
+ * ofs_x, ofs_y); returns the number of interaction rows (up to cap written) */
+int om_material_rules(int32_t *react, int32_t *inter, int cap) {
+    memset(react, 0, sizeof(int32_t) * 12 * (size_t)NMAT);
+    for (int m = 0; m < NMAT; m++)
+        for (int q = 0; q < M[m].n_react; q++) {
+            react[12 * m + 3 * q] = M[m].react[q].kind;
+            react[12 * m + 3 * q + 1] = M[m].react[q].data1;
+            react[12 * m + 3 * q + 2] = M[m].react[q].data2;
+        }
+    int n = 0;
+    for (int i = 0; i < NINTER; i++)
+        for (int q = 0; q < INTER[i].n; q++, n++) {
+            if (n >= cap) continue;
+            const inter_t *e = &INTER[i].e[q];
+            int32_t *r = inter + 7 * n;
+            r[0] = INTER[i].mat;
+            r[1] = INTER[i].other;
+            r[2] = e->kind;
+            r[3] = e->data1;
+            r[4] = e->data2;
+            r[5] = e->ofsx;
+            r[6] = e->ofsy;
+        }
+    return n;
+}
 
 void om_material_get(int id, int32_t out[16]) {
     const mat_t *m = &M[id];
@@ -730,9 +759,14 @@ static void rule_a(rctx *c, int x, int y) {
         cell_t below = gcell(w, x, y + 1); /* world.cpp:1150 */
         int bt = M[below.id].type;
         const inter_list_t *il = m->interact ? find_inter(t.id, below.id) : NULL;
-        if (il && il->n > 0) { /* world.cpp:1153-1179 (signed offsets) */
+        if (il && il->n > 0) { /* world.cpp:1153-1179 */
             for (int i = 0; i < il->n; i++) {
                 const inter_t *in = &il->e[i];
+                /* the radius (MaterialInteraction::data2) is a u32, so the loops'
+                 * `xx <= ofsX + data2` compares unsigned: a box whose low corner
+                 * ofs - radius is negative is not visited at all (when ofs + radius
+                 * is negative too the reference never leaves the loop; empty here) */
+                if (in->ofsx - in->data2 < 0 || in->ofsy - in->data2 < 0) continue;
                 for (int xx = in->ofsx - in->data2; xx <= in->ofsx + in->data2; xx++)
                     for (int yy = in->ofsy - in->data2; yy <= in->ofsy + in->data2; yy++) {
                         if (in->kind == INTER_TRANSFORM) {

@@ -53,12 +53,15 @@ def test_fire_lava_steam_reactions(fse, oracle_mod):
 
 def test_interactions_use_the_wide_halo(fse, oracle_mod):
     o = oracle_mod.Oracle()
-    sand, dirt, water, stone = (fse.material_find(n) for n in ("GENERIC_SAND", "DIRT", "WATER", "STONE"))
+    sand, dirt, water, stone, cobble = (fse.material_find(n) for n in ("GENERIC_SAND", "DIRT", "WATER", "STONE",
+                                                                       "COBBLE_STONE"))
+    # boxes reaching 5 cells to the side and below; the last one has a negative low
+    # corner, which the reference's unsigned loop bound never visits
+    rules = [(sand, water, 1, dirt, 2, 3, 2), (sand, stone, 2, water, 1, 1, 4), (sand, cobble, 2, water, 1, -2, 0)]
     try:
-        fse.set_interaction(sand, water, 1, dirt, 2, 1, 2)
-        fse.set_interaction(sand, stone, 2, water, 1, -2, 0)
-        assert o.set_interaction(sand, water, 1, dirt, 2, 1, 2) == 0
-        assert o.set_interaction(sand, stone, 2, water, 1, -2, 0) == 0
+        for r in rules:
+            fse.set_interaction(*r)
+            assert o.set_interaction(*r) == 0
         fse.PushMaterials()
         world, ow = _pair(fse, oracle_mod, 256, 256, 8)
         _run_both(fse, oracle_mod, world, ow, 4, "interactions")

@@ -56,8 +56,8 @@ def test_race_free_with_interactions(oracle_mod):
     o.reset_materials()
     try:
         sand, dirt, water = o.find("GENERIC_SAND"), o.find("DIRT"), o.find("WATER")
-        assert o.set_interaction(sand, water, 1, dirt, 2, 1, 2) == 0
-        assert o.set_interaction(sand, o.find("STONE"), 2, water, 1, -2, 0) == 0
+        assert o.set_interaction(sand, water, 1, dirt, 2, 3, 2) == 0
+        assert o.set_interaction(sand, o.find("STONE"), 2, water, 1, 1, 4) == 0
         ow = _world(oracle_mod, 256, 256, 5)
         for _ in range(3):
             assert ow.tick(PART, check_races=True) == 0

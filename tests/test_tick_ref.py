@@ -1,0 +1,121 @@
+"""The oracle's cell rules against the reference's own world::tick.
+
+oracle/Makefile `ref` compiles world::tick (source/engine/world.cpp:1036-1948)
+unchanged, with the pieces of the reference it calls (oracle/ref_tick.cpp). Its
+rand() returns the oracle's counter draws for the cell being updated, so the
+reference's rules and the oracle's restatement in the reference's chunk order
+(OM_ORDER_SEQ) consume the same numbers. On scenes without liquids (whose amounts
+the reference keeps in f32, this path in Q16.16), every cell (material, colour,
+temperature, moved flag) and every spawned particle must agree bit for bit.
+tests/golden/tick_ref.json keeps digests of the reference's results (made by
+tests/golden/make_tick_ref.py) for machines without the reference tree. The CUDA
+kernels are checked against the same oracle rules in the partitioned order by the
+GPU tests.
+"""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle.binding import ORDER_SEQ
+from tick_cases import CASES, setup_materials, scene
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "tick_ref.json")
+START_TICK = 7
+
+
+def oracle_rows(parts):
+    """Oracle particles as the reference harness's rows (16 int32 each)."""
+    rows = np.zeros((len(parts), 16), np.int32)
+    rows[:, 0] = parts["id"]
+    rows[:, 1] = parts["colour"].view(np.int32)
+    rows[:, 2] = parts["scalar"]
+    for j, k in enumerate(("x", "y", "vx", "vy", "ax", "ay", "target_x", "target_y", "target_force")):
+        rows[:, 3 + j] = np.ascontiguousarray(parts[k]).view(np.int32)
+    rows[:, 12] = parts["bits"] & 1
+    rows[:, 13] = (parts["bits"] >> 1) & 1
+    rows[:, 14] = parts["lifetime"]
+    rows[:, 15] = parts["fade_time"]
+    return rows
+
+
+def digest(ids, colours, temps, moved, rows):
+    h = hashlib.sha256()
+    for a, dt in ((ids, "<u2"), (colours, "<u4"), (temps, "<i4"), (moved, "u1"), (rows, "<i4")):
+        h.update(np.ascontiguousarray(a, dt).tobytes())
+    return h.hexdigest()
+
+
+def run_oracle(oracle_mod, ids, case):
+    w, h, seed, kind, ci, nt = case
+    st = scene(ids, w, h, seed, kind)
+    ow = oracle_mod.OracleWorld(w, h, 128, ci, seed)
+    ow.set_state(st)
+    ow.tick_count = START_TICK
+    for _ in range(nt):
+        ow.tick(order=ORDER_SEQ)
+    o = ow.state()
+    return st, (o["id"], o["colour"], o["scalar"], (o["flags"] >> 7).astype(np.uint8), oracle_rows(ow.particles()))
+
+
+def run_reference(oracle_mod, lib, ids, case):
+    from oracle.binding import reference_world_tick
+
+    w, h, seed, kind, ci, nt = case
+    st = scene(ids, w, h, seed, kind)
+    ri, rc, rt, rm, rp, _ = reference_world_tick(lib, oracle_mod.Oracle(), st["id"], st["colour"], st["scalar"],
+                                                 st["flags"] >> 7, ci, seed, START_TICK, nt)
+    return ri, rc, rt, rm, rp
+
+
+@pytest.fixture()
+def ids(oracle_mod):
+    o = oracle_mod.Oracle()
+    yield setup_materials(o)
+    o.reset_materials()
+
+
+@pytest.mark.parametrize("case", CASES, ids=["%s-%dx%d-i%d-t%d" % (c[3], c[0], c[1], c[4], c[5]) for c in CASES])
+def test_oracle_matches_reference_tick(oracle_mod, ids, case):
+    from oracle.binding import build_reference_tick
+
+    lib = build_reference_tick()
+    if lib is None:
+        pytest.skip("reference tree absent")
+    ref = run_reference(oracle_mod, lib, ids, case)
+    _, got = run_oracle(oracle_mod, ids, case)
+    for name, a, b in zip(("id", "colour", "temperature", "moved", "particles"), ref, got):
+        assert a.shape == b.shape, name
+        bad = np.argwhere(a != b)
+        assert len(bad) == 0, "%s differs at %s: reference %s, oracle %s" % (
+            name, bad[0].tolist(), a[tuple(bad[0])], b[tuple(bad[0])])
+
+
+@pytest.mark.parametrize("case", CASES, ids=["%s-%dx%d-i%d-t%d" % (c[3], c[0], c[1], c[4], c[5]) for c in CASES])
+def test_oracle_matches_reference_digests(oracle_mod, ids, case):
+    golden = json.load(open(GOLDEN))
+    key = "%d_%d_%d_%s_%d_%d" % case
+    _, got = run_oracle(oracle_mod, ids, case)
+    assert digest(*got) == golden[key]["digest"], key
+    assert len(got[4]) == golden[key]["particles"]
+
+
+def test_scenes_exercise_every_rule(oracle_mod, ids):
+    """The scenes move sand and gas, fire every reaction and both interaction kinds,
+    and burn: each rule leaves its mark in the results."""
+    seen = {}
+    for case in CASES:
+        st, (gi, gc, gt, gm, rows) = run_oracle(oracle_mod, ids, case)
+        before = st["id"]
+        seen["spawned gas"] = seen.get("spawned gas", 0) + int(((gi == ids["PIN_GAS"]) & (before != ids["PIN_GAS"])).sum())
+        seen["rock made sand B"] = seen.get("rock made sand B", 0) + int(
+            ((before == ids["PIN_ROCK"]) & (gi == ids["PIN_SAND_B"])).sum())
+        seen["sand C above 536"] = seen.get("sand C above 536", 0) + int(
+            ((before == ids["PIN_SAND_C"]) & (gi == ids["GENERIC_SAND"])).sum())
+        seen["fire particles"] = seen.get("fire particles", 0) + int((rows[:, 0] == ids["FIRE"]).sum())
+        seen["falling sand particles"] = seen.get("falling sand particles", 0) + int(
+            np.isin(rows[:, 0], [ids["PIN_SAND_A"], ids["GENERIC_SAND"]]).sum())
+        seen["moved changed"] = seen.get("moved changed", 0) + int(((st["flags"] >> 7) != gm).sum())
+    assert all(v != 0 for v in seen.values()), seen
