@@ -21,7 +21,7 @@ __all__ = [
     "InitMaterials", "RegisterMaterial", "PushMaterials", "load_lua_materials", "material_find",
     "material_count", "material_get", "set_reaction", "set_interaction", "lib",
     "AIR", "SOLID", "SAND", "SOUP", "GAS", "PASSABLE", "OBJECT", "GEN_EMPTY", "GEN_MIX", "GEN_ZIPF8",
-    "FLUID_ONE", "CFG_RENDER", "CFG_TEMPERATURE", "CFG_TEMPERATURE_STEP", "set_conduction", "set_factory_temperature", "get_conduction",
+    "FLUID_ONE", "CFG_RENDER", "CFG_TEMPERATURE", "CFG_TEMPERATURE_STEP", "CFG_REFERENCE_ORDER", "set_conduction", "set_factory_temperature", "get_conduction",
     "TEX_PIXELS", "TEX_EMISSION", "TEX_FIRE", "TEX_FLOW", "TEX_CELLS", "write_png",
 ]
 
@@ -121,17 +121,21 @@ def get_conduction(mat):
 CFG_RENDER = 1
 CFG_TEMPERATURE = 2
 CFG_TEMPERATURE_STEP = 4
+CFG_REFERENCE_ORDER = 8
 TEX_PIXELS, TEX_EMISSION, TEX_FIRE, TEX_FLOW, TEX_CELLS = 0, 1, 2, 3, 4
 
 
 def _config(chunk_size=128, cell_iter=3, seed=0, particle_capacity=0, spawn_capacity=0, stream=None, render=False,
-            temperature=False, temperature_step=False):
+            temperature=False, temperature_step=False, reference_order=False):
     """temperature: keep liquid temperatures (FSE_CFG_TEMPERATURE); temperature_step:
-    also run the conduction step every fourth tick inside steps (FSE_CFG_TEMPERATURE_STEP)."""
+    also run the conduction step every fourth tick inside steps (FSE_CFG_TEMPERATURE_STEP);
+    reference_order: update each chunk's cells in the reference's own order
+    (FSE_CFG_REFERENCE_ORDER)."""
     return FseConfig(chunk_size, cell_iter, seed & 0xFFFFFFFF, particle_capacity, spawn_capacity,
                      C.c_void_p(stream) if stream else None,
                      (CFG_RENDER if render else 0) | (CFG_TEMPERATURE if temperature else 0) |
-                     (CFG_TEMPERATURE_STEP if temperature_step else 0))
+                     (CFG_TEMPERATURE_STEP if temperature_step else 0) |
+                     (CFG_REFERENCE_ORDER if reference_order else 0))
 
 
 # ---------------------------------------------------------------------- world
@@ -142,14 +146,15 @@ class World:
               ("diff", np.int32))
 
     def __init__(self, width, height, chunk_size=128, cell_iter=3, seed=0, particle_capacity=0, spawn_capacity=0,
-                 stream=None, render=False, temperature=False, temperature_step=False, _handle=None):
+                 stream=None, render=False, temperature=False, temperature_step=False, reference_order=False,
+                 _handle=None):
         self.lib = lib()
         self.width, self.height = int(width), int(height)
         self._owned = _handle is None
         if _handle is None:
             h = C.c_void_p()
             cfg = _config(chunk_size, cell_iter, seed, particle_capacity, spawn_capacity, stream, render, temperature,
-                          temperature_step)
+                          temperature_step, reference_order)
             check(self.lib.fse_world_create(self.width, self.height, C.byref(cfg), C.byref(h)), "world_create")
             self.h = h
         else:

@@ -369,7 +369,7 @@ void PassTimer::drain() {
 
 int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], const int n_items[4], int max_iter, int C,
                  int threads, int grid, bool particles, int move_blocks, int stage_blocks, cudaStream_t s,
-                 PassTimer *timer, int temp_tiles, bool temp_track) {
+                 PassTimer *timer, int temp_tiles, bool temp_track, bool seq) {
     int halo = tick_halo();
     for (int iter = 0; iter < max_iter; iter++)  // world.cpp:1050
         for (int tk = 0; tk < 4; tk++) {         // world.cpp:1057-1060
@@ -380,7 +380,7 @@ int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], con
                 cudaEventRecord(a, s);
             }
             cudaError_t e = launch_colour_pass(d_worlds, items[tk], n_items[tk], iter, tk, g_dev_mt, halo, C, threads,
-                                               grid, s, temp_track);
+                                               grid, s, temp_track, seq);
             if (e != cudaSuccess) return FSE_E_CUDA;
             if (timer) {
                 cudaEventRecord(b, s);
@@ -752,6 +752,7 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
     w->H = height;
     w->C = c.chunk_size;
     w->cell_iter = c.cell_iter;
+    w->seq = (c.flags & FSE_CFG_REFERENCE_ORDER) != 0;
     w->seed = c.seed;
     w->part_cap = c.particle_capacity;
     w->stage_cap = c.spawn_capacity;
@@ -1069,7 +1070,7 @@ static int world_enqueue(fse_world *w, bool particles_after_tick, bool tick, boo
     if (tick) {
         rc = enqueue_step(w->d, 1, w->items, w->n_items, w->cell_iter, w->C, w->threads, w->grid, particles_after_tick,
                           world_move_blocks(w), world_stage_blocks(w), w->stream, w->timer, world_temp_tiles(w),
-                          w->h.tp != nullptr);
+                          w->h.tp != nullptr, w->seq);
         if (rc) return rc;
     } else if (particles) {
         if (launch_particle_tick(w->d, 1, g_dev_mt, world_move_blocks(w), w->stream) != cudaSuccess) return FSE_E_CUDA;
@@ -1141,7 +1142,7 @@ int fse_world_step_graph(fse_world *w, int n) {
             for (int i = 0; i < k && erc == FSE_OK; i++)
                 erc = enqueue_step(w->d, 1, w->items, w->n_items, w->cell_iter, w->C, w->threads, w->grid, true,
                                    world_move_blocks(w), world_stage_blocks(w), w->stream, nullptr,
-                                   world_temp_tiles(w), w->h.tp != nullptr);
+                                   world_temp_tiles(w), w->h.tp != nullptr, w->seq);
             cudaError_t e = cudaStreamEndCapture(w->stream, &g);
             const long long kn = fse_launch_counter() - c0;
             count_launches(-kn);

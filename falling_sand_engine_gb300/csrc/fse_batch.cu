@@ -152,9 +152,9 @@ int fse_batch_create(fse_world **worlds, int n, fse_batch **out) {
             delete b;
             return FSE_E_INVAL;
         }
-        if (i > 0 && worlds[i]->C != worlds[0]->C) {
+        if ((i > 0 && worlds[i]->C != worlds[0]->C) || worlds[i]->seq) {
             delete b;
-            return FSE_E_INVAL;  // one shared-memory tile shape per launch
+            return FSE_E_INVAL;  // one shared-memory tile shape per launch; partitioned order only
         }
         b->worlds.push_back(worlds[i]);
         b->max_iter = std::max(b->max_iter, worlds[i]->cell_iter);
@@ -370,6 +370,7 @@ int fse_server_add_world(fse_server *s, int w, int h, const fse_config *cfg, int
     fse_config c{};
     if (cfg) c = *cfg;
     if (c.chunk_size == 0) c.chunk_size = 128;
+    if (c.flags & FSE_CFG_REFERENCE_ORDER) return FSE_E_INVAL;  // servers batch their worlds
     if (!s->slots.empty()) {
         for (fse_world *x : s->slots)
             if (x && x->C != c.chunk_size) return FSE_E_INVAL;

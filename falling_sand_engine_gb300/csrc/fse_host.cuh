@@ -29,6 +29,7 @@ struct fse_world {
     int part_cap, stage_cap;
     cudaStream_t stream;
     bool own_stream;
+    bool seq;  // FSE_CFG_REFERENCE_ORDER: chunks updated in the reference's order
     fse::WorldDev h;      // host mirror of the device descriptor (pointers, sizes)
     fse::WorldDev *d;     // device descriptor
     uint32_t *items[4];   // chunk slots per colour
@@ -78,7 +79,7 @@ size_t colour_pass_smem(int C, int halo);
 // temp: some world of the table keeps liquid temperatures (tp != NULL)
 cudaError_t launch_colour_pass(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
                                const MatTable *mt, int halo, int C, int threads, int grid, cudaStream_t s,
-                               bool temp = false);
+                               bool temp = false, bool seq = false);
 cudaError_t launch_spawn_append(WorldDev *d_worlds, int n_worlds, int stage_blocks, cudaStream_t s);
 cudaError_t launch_particle_tick(WorldDev *d_worlds, int n_worlds, const MatTable *mt, int move_blocks,
                                  cudaStream_t s);
@@ -100,7 +101,7 @@ int tick_halo();
 // share a device descriptor table
 int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], const int n_items[4], int max_iter,
                  int C, int threads, int grid, bool particles, int move_blocks, int stage_blocks, cudaStream_t s,
-                 PassTimer *timer = nullptr, int temp_tiles = 0, bool temp_track = false);
+                 PassTimer *timer = nullptr, int temp_tiles = 0, bool temp_track = false, bool seq = false);
 void count_launches(long long n);
 
 }  // namespace fse

@@ -127,13 +127,22 @@ struct TileData {
     int ax0, ay0, aw;
 };
 
-template <bool EDGE, bool TEMP>
+// LIVE: the pillar reads the tile as it stands (the reference's own order, where
+// one thread updates the chunk's cells in turn) instead of the sweep-B snapshot
+template <bool EDGE, bool TEMP, bool LIVE = false>
 struct Tile : TileData {
     static constexpr bool kTemp = TEMP;
     __device__ __forceinline__ explicit Tile(const TileData &d) : TileData(d) {}
 
-    // 10 snapshot bits of column x starting at row y (0 outside the snapshot)
+    // 10 AIR bits of column x starting at row y: from the snapshot (0 outside it), or
+    // live
     __device__ __forceinline__ uint32_t air10(int x, int y) const {
+        if constexpr (LIVE) {
+            uint32_t bits = 0;
+            for (int k = 0; k < 10; k++)
+                if (type(x, y + k) == T_AIR) bits |= 1u << k;
+            return bits;
+        }
         int sx = x - ax0, sy = y - ay0;
         if ((unsigned)sx >= (unsigned)aw || sy < 0) return 0u;
         const uint32_t *col = s_air + sx * 5;
@@ -948,7 +957,10 @@ struct SmemHead {
 };
 
 // items: (world << 20) | chunk slot within the colour; iter, tk select the pass.
-template <int HALO, bool TEMP>
+// SEQ: the reference's own order inside each chunk -- thread 0 updates the cells
+// bottom row first, left to right, sweep by sweep (world.cpp:1084-1087, 1589, 1823),
+// with the same rules; the other threads stage and write back
+template <int HALO, bool TEMP, bool SEQ>
 __global__ void __launch_bounds__(CP_THREADS, 1)
     k_colour_pass(const WorldDev *__restrict__ worlds, const uint32_t *__restrict__ items, int n_items, int iter, int tk,
                   const MatTable *__restrict__ mt) {
@@ -1106,6 +1118,31 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
         c.led_g = w.ledger;
         // the world bounds policy matters only where the tile crosses the world edge
         const bool edge = Tl.x0 < 0 || Tl.y0 < 0 || Tl.x0 + Tl.RW > W || Tl.y0 + Tl.RHI > H;
+        auto sweeps_seq = [&](const auto &Tl) {
+            for (int sweep = 0; sweep < 3; sweep++) {
+                c.pk = pass_key(w.seed, *w.tick, (uint32_t)(iter * 3 + sweep));
+                if (tid == 0) {
+                    for (int dy = chh - 1; dy >= 0; dy--)
+                        for (int dx = 0; dx < cw; dx++) {
+                            const int x = cx + dx, y = cy + dy;
+                            if (sweep == 0) {
+                                c.ev.n = 0;
+                                rule_a(Tl, c, x, y);
+                                if (c.ev.n > 0) {
+                                    const int base = atomicAdd(w.stage_count, c.ev.n);
+                                    emit_spawns<TEMP>(w, c.ev, cp, (uint32_t)running, base);
+                                    running += c.ev.n;
+                                }
+                            } else if (sweep == 1) {
+                                rule_b(Tl, c, x, y, w.df[(size_t)y * W + x]);
+                            } else {
+                                rule_c(Tl, c, x, y);
+                            }
+                        }
+                }
+                __syncthreads();
+            }
+        };
         auto sweeps = [&](const auto &Tl) {
         for (int sweep = 0; sweep < 3; sweep++) {
             c.pk = pass_key(w.seed, *w.tick, (uint32_t)(iter * 3 + sweep));
@@ -1202,10 +1239,17 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
             }
         }
         };
-        if (edge)
-            sweeps(Tile<true, TEMP>(Tl));
-        else
-            sweeps(Tile<false, TEMP>(Tl));
+        if constexpr (SEQ) {
+            if (edge)
+                sweeps_seq(Tile<true, TEMP, true>(Tl));
+            else
+                sweeps_seq(Tile<false, TEMP, true>(Tl));
+        } else {
+            if (edge)
+                sweeps(Tile<true, TEMP>(Tl));
+            else
+                sweeps(Tile<false, TEMP>(Tl));
+        }
 
         // ---- write back the cells this CTA changed (full-state rows inside the world),
         // one warp per row
@@ -1244,7 +1288,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
     FSE_PT_FLUSH
 }
 
-#ifndef FSE_TICK_TEMP_TU
+#if !defined(FSE_TICK_TEMP_TU) && !defined(FSE_TICK_SEQ_TU)
 size_t colour_pass_smem(int C, int halo) {
     size_t RW = (size_t)C + 2 * halo, RHF = (size_t)C + 2 * halo, RHI = (size_t)C + halo + 10;
     size_t nid = RW * RHI, nfull = RW * RHF;
@@ -1254,20 +1298,30 @@ size_t colour_pass_smem(int C, int halo) {
 
 #endif
 
-template <int HALO, bool TEMP>
+template <int HALO, bool TEMP, bool SEQ = false>
 static cudaError_t launch_t(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
                             const MatTable *mt, size_t sm, int grid, cudaStream_t s) {
     // opt in to the full shared-memory carve-out once per instantiation
     static size_t set = 0;
     if (set < sm) {
-        cudaFuncSetAttribute(k_colour_pass<HALO, TEMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(k_colour_pass<HALO, TEMP, SEQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         set = sm;
     }
-    k_colour_pass<HALO, TEMP><<<grid, CP_THREADS, sm, s>>>(worlds, items, n_items, iter, tk, mt);
+    k_colour_pass<HALO, TEMP, SEQ><<<grid, CP_THREADS, sm, s>>>(worlds, items, n_items, iter, tk, mt);
     return cudaGetLastError();
 }
 
-#ifdef FSE_TICK_TEMP_TU
+#if defined(FSE_TICK_SEQ_TU)
+cudaError_t launch_colour_pass_seq(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
+                                   const MatTable *mt, int halo, size_t sm, int grid, cudaStream_t s, bool temp) {
+    if (temp) {
+        if (halo == 5) return launch_t<5, true, true>(worlds, items, n_items, iter, tk, mt, sm, grid, s);
+        return launch_t<2, true, true>(worlds, items, n_items, iter, tk, mt, sm, grid, s);
+    }
+    if (halo == 5) return launch_t<5, false, true>(worlds, items, n_items, iter, tk, mt, sm, grid, s);
+    return launch_t<2, false, true>(worlds, items, n_items, iter, tk, mt, sm, grid, s);
+}
+#elif defined(FSE_TICK_TEMP_TU)
 cudaError_t launch_colour_pass_temp(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
                                     const MatTable *mt, int halo, size_t sm, int grid, cudaStream_t s) {
     if (halo == 5) return launch_t<5, true>(worlds, items, n_items, iter, tk, mt, sm, grid, s);
@@ -1276,14 +1330,17 @@ cudaError_t launch_colour_pass_temp(const WorldDev *worlds, const uint32_t *item
 #else
 cudaError_t launch_colour_pass_temp(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
                                     const MatTable *mt, int halo, size_t sm, int grid, cudaStream_t s);
+cudaError_t launch_colour_pass_seq(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
+                                   const MatTable *mt, int halo, size_t sm, int grid, cudaStream_t s, bool temp);
 
 cudaError_t launch_colour_pass(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
                                const MatTable *mt, int halo, int C, int threads, int grid, cudaStream_t s,
-                               bool temp) {
+                               bool temp, bool seq) {
     (void)threads;  // the colour pass always runs CP_THREADS threads (see above)
     size_t sm = colour_pass_smem(C, halo);
     if (n_items <= 0) return cudaSuccess;
     if (grid <= 0 || grid > n_items) grid = n_items;
+    if (seq) return launch_colour_pass_seq(worlds, items, n_items, iter, tk, mt, halo, sm, grid, s, temp);
     if (temp) return launch_colour_pass_temp(worlds, items, n_items, iter, tk, mt, halo, sm, grid, s);
     if (halo == 5) return launch_t<5, false>(worlds, items, n_items, iter, tk, mt, sm, grid, s);
     return launch_t<2, false>(worlds, items, n_items, iter, tk, mt, sm, grid, s);
@@ -1292,7 +1349,7 @@ cudaError_t launch_colour_pass(const WorldDev *worlds, const uint32_t *items, in
 
 }  // namespace fse
 
-#if defined(FSE_PHASE_CLOCKS) && !defined(FSE_TICK_TEMP_TU)
+#if defined(FSE_PHASE_CLOCKS) && !defined(FSE_TICK_TEMP_TU) && !defined(FSE_TICK_SEQ_TU)
 extern "C" int fse_debug_phase_clocks(unsigned long long out[16], int reset) {
     cudaDeviceSynchronize();
     cudaMemcpyFromSymbol(out, g_phase_clk, 16 * sizeof(unsigned long long));
