@@ -185,6 +185,7 @@ def bench_config1(args, rank, local_rank, world_size):
     render = render_config1(fse, torch, W, H, seed, NP) if rank == 0 else None
     temperature = temperature_config1(fse, torch, W, H, seed, NP) if rank == 0 else None
     pack = pack_config1(fse, torch, W, H, seed, NP) if rank == 0 else None
+    reforder = reference_order_config1(fse, torch, W, H, seed, NP) if rank == 0 else None
     cpu = None
     if rank == 0 and world_size == 1 and not args.no_cpu:
         cpu = cpu_baseline_config1(seed)
@@ -201,6 +202,7 @@ def bench_config1(args, rank, local_rank, world_size):
                    "parallelism": "one independent world per GPU" if world_size > 1 else "single GPU"},
         "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
         "wall_s": round(wall, 3), "render": render, "temperature": temperature, "pack": pack,
+        "reference_order": reforder,
     }
 
 
@@ -312,6 +314,35 @@ def temperature_config1(fse, torch, W, H, seed, NP, calls=10):
             "frac": round(gbs / peak, 4), "peak": peak, "peak_kind": peak_kind, "calls": calls,
             "kernels": "k_temp_tiles + k_temp_commit",
             "l2": "flushed before each step (512 MiB write outside the events)"}
+
+
+def reference_order_config1(fse, torch, W, H, seed, NP, steps=3):
+    """The same workload stepped in the reference's own update order inside each chunk
+    (FSE_CFG_REFERENCE_ORDER: one thread per chunk updates its cells in turn, the
+    semantics of the CPU baseline's reference chunk order): steps timed with CUDA
+    events on the world's stream after two warm-up steps, L2 flushed between them."""
+    stream = torch.cuda.Stream()
+    world = fse.World(W, H, chunk_size=128, cell_iter=3, seed=seed, particle_capacity=4_000_000,
+                      spawn_capacity=2_000_000, stream=stream.cuda_stream, reference_order=True)
+    world.generate(fse.GEN_MIX, seed)
+    world.addCell(config1_particles(NP, W, H, seed))
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    e = [_ev(torch) for _ in range(2)]
+    with torch.cuda.stream(stream):
+        world.step(2)
+    torch.cuda.synchronize()
+    ms = 0.0
+    for i in range(steps):
+        with torch.cuda.stream(stream):
+            _flush(flush, i)
+            e[0].record(stream)
+            world.step(1)
+            e[1].record(stream)
+        torch.cuda.synchronize()
+        ms += e[0].elapsed_time(e[1])
+    world.close()
+    return {"ms_per_step": round(ms / steps, 3), "gcells": round(W * H * steps / (ms / 1e3) / 1e9, 4),
+            "steps": steps, "order": "reference: one thread per chunk, cells in world.cpp's loop order"}
 
 
 def pack_config1(fse, torch, W, H, seed, NP, calls=5):
@@ -902,7 +933,7 @@ def main():
     ap.add_argument("--impl", default="fse", choices=["fse", "reference"])
     ap.add_argument("--workload", type=int, default=1, choices=[0, 1, 2, 3, 4])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--only", default=None, choices=["render", "temperature", "pack"],
+    ap.add_argument("--only", default=None, choices=["render", "temperature", "pack", "reference_order"],
                     help="run only one side measurement of the 4096x2048 workload (for profiling), print its dict")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -929,7 +960,8 @@ def main():
 
         fse.InitMaterials()
         fse.PushMaterials()
-        fn = {"render": render_config1, "temperature": temperature_config1, "pack": pack_config1}[args.only]
+        fn = {"render": render_config1, "temperature": temperature_config1, "pack": pack_config1,
+              "reference_order": reference_order_config1}[args.only]
         print(json.dumps(fn(fse, torch, 4096, 2048, 1234, 1_000_000)))
         return
     run = {0: bench_config0, 1: bench_config1, 2: bench_config2, 3: bench_config3, 4: bench_config4}[args.workload]
