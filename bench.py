@@ -164,8 +164,11 @@ def bench_config1(args, rank, local_rank, world_size):
     launches = fse.launch_counter() - l0
     pass_ms, pass_n = world.pass_timing(False)
     live_particles = world.particle_count()
-    gpu_ms = sum(a.elapsed_time(b) for a, b in ev)
+    step_ms = np.array([a.elapsed_time(b) for a, b in ev])
+    gpu_ms = float(step_ms.sum())
     gpu_ms = max_over_ranks(gpu_ms, world_size)
+    tick_latency = {"p50": round(float(np.percentile(step_ms, 50)), 4), "p99": round(float(np.percentile(step_ms, 99)), 4),
+                    "max": round(float(step_ms.max()), 4), "unit": "ms per step (tick + tickCells), CUDA events"}
     barrier(world_size)
 
     value = world_size * cells * args.steps / (gpu_ms / 1e3) / 1e9
@@ -202,7 +205,7 @@ def bench_config1(args, rank, local_rank, world_size):
                    "parallelism": "one independent world per GPU" if world_size > 1 else "single GPU"},
         "roofline": roof, "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
         "wall_s": round(wall, 3), "render": render, "temperature": temperature, "pack": pack,
-        "reference_order": reforder,
+        "reference_order": reforder, "tick_latency": tick_latency,
     }
 
 
@@ -449,9 +452,26 @@ def cpu_baseline_config1(seed, budget_s=12.0):
         if time.perf_counter() - t0 > budget_s or n >= 20:
             break
     dt = time.perf_counter() - t0
+    # beside it: one host thread in the same order, and all threads in the partitioned order
+    o.set_threads(1)
+    t1 = time.perf_counter()
+    ow.step(1, 0)
+    dt1 = time.perf_counter() - t1
+    o.set_threads(cores)
+    ow.step(1, 1)  # warm-up
+    n2, t2 = 0, time.perf_counter()
+    while True:
+        ow.step(1, 1)
+        n2 += 1
+        if time.perf_counter() - t2 > budget_s / 2 or n2 >= 20:
+            break
+    dt2 = time.perf_counter() - t2
     return {"value": round(W * H * n / dt / 1e9, 6), "unit": "Gcell/s", "cores": cores, "kind": "port",
             "sample": "%d steps (tick + tickCells) of the 4096x2048 world with 1M particles, reference chunk order, "
-                      "after 1 warm-up step" % n}
+                      "after 1 warm-up step" % n,
+            "single_thread": {"value": round(W * H / dt1 / 1e9, 6), "sample": "1 step, reference chunk order"},
+            "partitioned_order": {"value": round(W * H * n2 / dt2 / 1e9, 6), "cores": cores,
+                                  "sample": "%d steps, the GPU's partitioned order" % n2}}
 
 
 # ------------------------------------------------------- other workloads
