@@ -321,8 +321,9 @@ def temperature_config1(fse, torch, W, H, seed, NP, calls=10):
 
 def reference_order_config1(fse, torch, W, H, seed, NP, steps=3):
     """The same workload stepped in the reference's own update order inside each chunk
-    (FSE_CFG_REFERENCE_ORDER: one thread per chunk updates its cells in turn, the
-    semantics of the CPU baseline's reference chunk order): steps timed with CUDA
+    (FSE_CFG_REFERENCE_ORDER: the cells of each chunk in world.cpp's loop order, run
+    as a wavefront of one thread per chunk row; the semantics of the CPU baseline's
+    reference chunk order): steps timed with CUDA
     events on the world's stream after two warm-up steps, L2 flushed between them."""
     stream = torch.cuda.Stream()
     world = fse.World(W, H, chunk_size=128, cell_iter=3, seed=seed, particle_capacity=4_000_000,
@@ -345,7 +346,7 @@ def reference_order_config1(fse, torch, W, H, seed, NP, steps=3):
         ms += e[0].elapsed_time(e[1])
     world.close()
     return {"ms_per_step": round(ms / steps, 3), "gcells": round(W * H * steps / (ms / 1e3) / 1e9, 4),
-            "steps": steps, "order": "reference: one thread per chunk, cells in world.cpp's loop order"}
+            "steps": steps, "order": "reference: cells in world.cpp's loop order, one thread per chunk row (wavefront)"}
 
 
 def pack_config1(fse, torch, W, H, seed, NP, calls=5):

@@ -783,7 +783,8 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
     h.amw = ceil_div(width, 8);
     h.amh = ceil_div(height, 8);
     size_t n = (size_t)ncell;
-    int ncp = h.cell_iter * 4 * h.max_slots + 1;
+    h.cp_rows = (c.flags & FSE_CFG_REFERENCE_ORDER) ? h.C : 1;
+    int ncp = h.cell_iter * 4 * h.max_slots * h.cp_rows + 1;
     bool ok = dalloc(w, &h.id, n) && dalloc(w, &h.col, n) && dalloc(w, &h.sc, n) && dalloc(w, &h.fl, n) &&
               dalloc(w, &h.df, n) && dalloc(w, &h.stage, (size_t)h.stage_cap) && dalloc(w, &h.cp_count, ncp) &&
               dalloc(w, &h.cp_base, ncp) && dalloc(w, &w->ctr, 16) && dalloc(w, &h.ledger, LED_ROWS * MAXMAT) &&

@@ -148,7 +148,11 @@ struct WorldDev {
     SpawnRec *stage;
     int32_t *stage_count;
     int32_t stage_cap;
-    int32_t *cp_count;  // [cell_iter * 4 * max_slots]
+    // spawn counts per chunk-pass (cell_iter * 4 * max_slots of them), each split in
+    // cp_rows rows: 1, or the chunk edge in the reference's order, where every chunk
+    // row ranks its own spawns (rows bottom first, the order of world.cpp's loop)
+    int cp_rows;
+    int32_t *cp_count;  // [cell_iter * 4 * max_slots * cp_rows]
     int32_t *cp_base;
     // particles
     PartSoA p, q;           // p = live list, q = compaction scratch

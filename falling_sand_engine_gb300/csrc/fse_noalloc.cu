@@ -141,6 +141,7 @@ extern "C" int fse_tick_noalloc(uint16_t *id, uint32_t *colour, int32_t *scalar,
     h.nCx = nCx;
     h.nCy = nCy;
     h.max_slots = max_slots;
+    h.cp_rows = 1;
     h.stage = (SpawnRec *)(base + OFF_STAGE);
     h.stage_cap = NA_MAX_SPAWNS;
     h.cp_count = (int32_t *)(base + OFF_CPC);

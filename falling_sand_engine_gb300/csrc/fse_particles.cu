@@ -29,7 +29,7 @@ __global__ void k_spawn_scan(const WorldDev *__restrict__ worlds) {
     const WorldDev &w = worlds[blockIdx.x];
     __shared__ int s_sum[32];
     __shared__ int s_carry;
-    const int n = w.cell_iter * 4 * w.max_slots;
+    const int n = w.cell_iter * 4 * w.max_slots * w.cp_rows;
     if (threadIdx.x == 0) s_carry = 0;
     __syncthreads();
     for (int base = 0; base < n; base += blockDim.x) {
@@ -73,7 +73,7 @@ __global__ void k_spawn_scan(const WorldDev *__restrict__ worlds) {
 __global__ void k_spawn_scatter(const WorldDev *__restrict__ worlds) {
     const WorldDev &w = worlds[blockIdx.y];
     const int n = min(*w.stage_count, w.stage_cap);
-    const int first = w.cp_base[w.cell_iter * 4 * w.max_slots];
+    const int first = w.cp_base[w.cell_iter * 4 * w.max_slots * w.cp_rows];
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         const SpawnRec s = w.stage[r];
         long long pos = (long long)first + w.cp_base[s.cp] + s.rank;

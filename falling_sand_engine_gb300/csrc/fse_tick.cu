@@ -957,9 +957,9 @@ struct SmemHead {
 };
 
 // items: (world << 20) | chunk slot within the colour; iter, tk select the pass.
-// SEQ: the reference's own order inside each chunk -- thread 0 updates the cells
-// bottom row first, left to right, sweep by sweep (world.cpp:1084-1087, 1589, 1823),
-// with the same rules; the other threads stage and write back
+// SEQ: the reference's own order inside each chunk (bottom row first, left to right,
+// sweep by sweep; world.cpp:1084-1087, 1589, 1823), with the same rules, run as a
+// wavefront of one thread per chunk row (see sweeps_seq)
 template <int HALO, bool TEMP, bool SEQ>
 __global__ void __launch_bounds__(CP_THREADS, 1)
     k_colour_pass(const WorldDev *__restrict__ worlds, const uint32_t *__restrict__ items, int n_items, int iter, int tk,
@@ -1106,7 +1106,11 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
         FSE_PT(1)
         if (!active) {
             // every chunk cell has iterations <= iter: the pass only marks cells visited
-            if (tid == 0) w.cp_count[cp] = 0;
+            if constexpr (SEQ) {
+                if (tid < w.cp_rows) w.cp_count[cp * w.cp_rows + tid] = 0;
+            } else if (tid == 0) {
+                w.cp_count[cp] = 0;
+            }
             __syncthreads();
             continue;
         }
@@ -1118,30 +1122,45 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
         c.led_g = w.ledger;
         // the world bounds policy matters only where the tile crosses the world edge
         const bool edge = Tl.x0 < 0 || Tl.y0 < 0 || Tl.x0 + Tl.RW > W || Tl.y0 + Tl.RHI > H;
+        // The reference's order as a wavefront: thread k updates chunk row k counted
+        // from the bottom (the row world.cpp's loop takes k-th), cell dx at step
+        // dx + s*k. A cell reads and writes at most RX columns to either side
+        // (RX = 1; 2 with fire; 5 with interactions, whose boxes lie right of the
+        // cell), so two cells whose accesses meet are at least 2*RX+1 = s steps apart
+        // in the reference's order's direction: every cell still sees exactly the
+        // cells the sequential loop would have updated before it, and no two cells
+        // of one step touch the same cell. Each row ranks its own spawns.
         auto sweeps_seq = [&](const auto &Tl) {
+            const int s = mode == 2 ? 11 : (mode == 1 ? 5 : 3);
+            const int k = tid, dy = chh - 1 - tid;
+            const bool row = k < chh;
+            int spawned = 0;
             for (int sweep = 0; sweep < 3; sweep++) {
                 c.pk = pass_key(w.seed, *w.tick, (uint32_t)(iter * 3 + sweep));
-                if (tid == 0) {
-                    for (int dy = chh - 1; dy >= 0; dy--)
-                        for (int dx = 0; dx < cw; dx++) {
-                            const int x = cx + dx, y = cy + dy;
-                            if (sweep == 0) {
-                                c.ev.n = 0;
-                                rule_a(Tl, c, x, y);
-                                if (c.ev.n > 0) {
-                                    const int base = atomicAdd(w.stage_count, c.ev.n);
-                                    emit_spawns<TEMP>(w, c.ev, cp, (uint32_t)running, base);
-                                    running += c.ev.n;
-                                }
-                            } else if (sweep == 1) {
-                                rule_b(Tl, c, x, y, w.df[(size_t)y * W + x]);
-                            } else {
-                                rule_c(Tl, c, x, y);
+                const int steps = cw + s * (chh - 1);
+                for (int t = 0; t < steps; t++) {
+                    const int dx = t - s * k;
+                    if (row && dx >= 0 && dx < cw) {
+                        const int x = cx + dx, y = cy + dy;
+                        if (sweep == 0) {
+                            c.ev.n = 0;
+                            rule_a(Tl, c, x, y);
+                            if (c.ev.n > 0) {
+                                const int base = atomicAdd(w.stage_count, c.ev.n);
+                                emit_spawns<TEMP>(w, c.ev, cp * (uint32_t)w.cp_rows + (uint32_t)k, (uint32_t)spawned,
+                                                  base);
+                                spawned += c.ev.n;
                             }
+                        } else if (sweep == 1) {
+                            rule_b(Tl, c, x, y, w.df[(size_t)y * W + x]);
+                        } else {
+                            rule_c(Tl, c, x, y);
                         }
+                    }
+                    __syncthreads();
                 }
-                __syncthreads();
             }
+            if (tid < w.cp_rows) w.cp_count[cp * w.cp_rows + tid] = spawned;
         };
         auto sweeps = [&](const auto &Tl) {
         for (int sweep = 0; sweep < 3; sweep++) {
@@ -1274,7 +1293,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                 }
             }
         }
-        if (tid == 0) w.cp_count[cp] = running;
+        if (!SEQ && tid == 0) w.cp_count[cp] = running;
         __syncthreads();
         FSE_PT(9)
     }

@@ -94,13 +94,13 @@ typedef struct fse_config {
  * as game::tick does (game.cpp:2157-2159, const.h:38); the test runs on the
  * device, so step graphs replay it correctly */
 #define FSE_CFG_TEMPERATURE_STEP 4
-/* the reference's own update order inside each chunk: one thread updates the
- * chunk's cells in turn, bottom row first and left to right, sweep by sweep
- * (world.cpp:1084-1087, 1589, 1823), with the same rules and draws; the default
- * partitioned order updates a chunk's cells in 30 lattice sub-phases with a
- * thread per cell. Results then equal the reference's world::tick for every rule
- * (liquid amounts in Q16.16 rather than f32); a tick takes tens of times longer.
- * Worlds with it cannot join batches or servers. */
+/* the reference's own update order inside each chunk: the chunk's cells in turn,
+ * bottom row first and left to right, sweep by sweep (world.cpp:1084-1087, 1589,
+ * 1823), with the same rules and draws, run as a wavefront of one thread per chunk
+ * row; the default partitioned order updates a chunk's cells in 30 lattice
+ * sub-phases with a thread per cell. Results then equal the reference's
+ * world::tick for every rule (liquid amounts in Q16.16 rather than f32); a tick
+ * takes about 13 times longer. Worlds with it cannot join batches or servers. */
 #define FSE_CFG_REFERENCE_ORDER 8
 
 /* One free particle (CellData, source/engine/game_utils/cells.h:15-36). 60 bytes. */

@@ -78,13 +78,23 @@ def test_device_matches_reference_digests(fse, scene_ids, case):
     world.close()
 
 
-@pytest.mark.parametrize("w,h,seed,ci", [(384, 256, 21, 3), (300, 200, 22, 2), (512, 384, 23, 3)])
-def test_device_reference_order_matches_oracle(fse, oracle_mod, w, h, seed, ci):
-    """Generated worlds (liquids, gas, sand, solids) with liquid temperatures and the
-    conduction step every fourth tick, stepped in reference order on both sides."""
+@pytest.mark.parametrize("w,h,seed,ci,fire", [(384, 256, 21, 3, False), (300, 200, 22, 2, False),
+                                               (512, 384, 23, 3, False), (384, 320, 24, 3, True)])
+def test_device_reference_order_matches_oracle(fse, oracle_mod, w, h, seed, ci, fire):
+    """Generated worlds (liquids, gas, sand, solids; with fire in one) with liquid
+    temperatures and the conduction step every fourth tick, stepped in reference
+    order on both sides."""
     types = material_types(fse)
     world = fse.World(w, h, cell_iter=ci, seed=seed, temperature=True, temperature_step=True, reference_order=True)
     world.generate(fse.GEN_MIX, seed)
+    if fire:
+        st = world.state()
+        rng = np.random.default_rng(seed)
+        f = rng.random((h, w)) < 0.03
+        st["id"][f] = fse.material_find("FIRE")
+        st["colour"][f] = 0xFF6432
+        st["scalar"][f] = 0
+        world.upload(st)
     ow = oracle_mod.OracleWorld(w, h, 128, ci, seed)
     ow.set_state(world.state())
     ow.enable_temperature(True)
