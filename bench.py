@@ -432,9 +432,24 @@ def e2e_config1(world, args, torch, cells, world_size):
 
 
 def cpu_baseline_config1(seed, budget_s=12.0):
-    """The oracle's reference-order tick on the host cores, on a bounded sample of
-    the same workload (full 4096x2048 world + 1M particles, as many steps as fit the
-    time budget, at least one)."""
+    """The reference's own tick + tickCells on the host cores (when they compile
+    here), and the oracle's reference-order tick beside it, on bounded samples of the
+    same workload (full 4096x2048 world + 1M particles, as many steps as fit the time
+    budget, at least one)."""
+    ref = reference_timing(4096, 2048, seed, 20, 1, budget_s)
+    port = cpu_port_config1(seed, budget_s)
+    if ref is None:
+        return port
+    value, n, cores = ref
+    return {"value": round(value, 6), "unit": "Gcell/s", "cores": cores, "kind": "reference",
+            "sample": "%d steps (tick + tickCells) of the 4096x2048 world with 1M particles after 1 warm-up step; "
+                      % n + REF_NOTE % cores,
+            "port": port}
+
+
+def cpu_port_config1(seed, budget_s=12.0):
+    """The oracle's reference-order tick on the host cores (the port), with one
+    thread and in the partitioned order beside it."""
     from oracle import Oracle, OracleWorld
 
     o = Oracle()
@@ -887,16 +902,61 @@ def max_over_ranks(v, world_size):
 
 
 # ------------------------------------------------------------ reference arm
+REF_NOTE = ("the reference's own world::tick and world::tickCells (source/engine/world.cpp:1036-1948, 2030-2195), "
+            "compiled unchanged from the extracted sources (oracle/ref_tick.cpp) with its chunk tasks on a pool of "
+            "%d worker threads; rand() draws the counter RNG, texture tile factories are constants")
+
+
+def reference_timing(W, H, seed, steps, warm, budget_s):
+    """The reference's own tick + tickCells on the workload, on all host cores:
+    (Gcell/s, steps timed, threads), or None when it cannot be compiled here."""
+    from oracle import Oracle, OracleWorld
+    from oracle.binding import build_reference_tick, reference_world_bench
+
+    try:
+        lib = build_reference_tick()
+    except Exception:  # noqa: BLE001 - no compiler or sources: the port is timed instead
+        lib = None
+    if lib is None:
+        return None
+    o = Oracle()
+    o.reset_materials()
+    cores = os.cpu_count() or 1
+    ow = OracleWorld(W, H, 128, 3, seed)
+    ow.generate(0, seed)
+    st = ow.state()
+    secs, n = reference_world_bench(lib, o, st["id"], st["colour"], ow.temperature(),
+                                    _np_particles(1_000_000, W, H, seed), 3, seed, cores, warm, steps, budget_s)
+    return W * H * n / secs / 1e9, n, cores
+
+
 def reference_arm(args, rank, world_size):
     if rank != 0:
         return None
     from oracle import Oracle, OracleWorld
 
+    W, H = 4096, 2048
+    warm = min(args.warmup, 3)
+    ref = reference_timing(W, H, 1234, args.steps, warm, REF_BUDGET_S)
+    if ref is not None:
+        value, n, cores = ref
+        sample = ("%d timed steps (tick + tickCells) of the 4096x2048 world with 1M particles after %d warm-up "
+                  "(%d requested; the timed region is capped at %.0f s)" % (n, warm, args.steps, REF_BUDGET_S))
+        return {
+            "impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": "Gcell/s", "n_gpus": world_size,
+            "steps": n, "warmup": warm, "ms_per_step": round(W * H / (value * 1e9) * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+f32",
+            "data": "synthetic",
+            "config": {"workload": "config1: one 4096x2048 world + 1M free particles", "world": [W, H],
+                       "particles": 1_000_000, "chunk": 128, "cell_iter": 3, "impl_note": REF_NOTE % cores},
+            "cpu_baseline": {"value": round(value, 6), "unit": "Gcell/s", "cores": cores, "kind": "reference",
+                             "sample": sample},
+            "e2e": {"value": round(value, 6), "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
     o = Oracle()
     o.reset_materials()
     cores = os.cpu_count() or 1
     o.set_threads(cores)
-    W, H = 4096, 2048
     ow = OracleWorld(W, H, 128, 3, 1234)
     ow.generate(0, 1234)
     ow.set_particles(_np_particles(1_000_000, W, H, 1234))
@@ -922,7 +982,7 @@ def reference_arm(args, rank, world_size):
         "config": {"workload": "config1: one 4096x2048 world + 1M free particles", "world": [W, H],
                    "particles": 1_000_000, "chunk": 128, "cell_iter": 3,
                    "impl_note": "CPU restatement of world::tick/tickCells in the reference chunk order "
-                                "(the reference itself does not build here: SDL2/xmake missing)"},
+                                "(the reference's own functions could not be compiled on this machine)"},
         "cpu_baseline": {"value": round(value, 6), "unit": "Gcell/s", "cores": cores, "kind": "port",
                          "sample": sample},
         "e2e": {"value": round(value, 6), "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

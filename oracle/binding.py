@@ -495,14 +495,65 @@ def reference_tick_cells(lib_path, ids, colours, amounts, mat_types, parts):
     return i2, c2, a2, d2, pout[: nout.value].copy()
 
 
+TICK_INC = ("world_tick", "world_gettile", "world_settile", "vertical_flow", "fluid_consts", "interact_defs",
+            "material_interaction", "material_struct", "material_ctor", "material_instance", "material_instance_ctor",
+            "tiles_globals", "cell_data", "cells")
+
+
 def build_reference_tick(force=False):
-    """Compile the reference's own world::tick (oracle/Makefile `ref`); None without the tree."""
-    if not os.path.exists(REFERENCE_WORLD_CPP):
-        return None
-    if force or not os.path.exists(REF_TICK_PATH) or os.path.getmtime(REF_TICK_PATH) < os.path.getmtime(
-            os.path.join(HERE, "ref_tick.cpp")):
+    """Compile the reference's own world::tick and world::tickCells (oracle/Makefile
+    `ref`). Without the reference tree, the pieces oracle/Makefile extracted before
+    (oracle/_ref/*.inc) are compiled where they are present; else None."""
+    fresh = (not force and os.path.exists(REF_TICK_PATH) and
+             os.path.getmtime(REF_TICK_PATH) >= os.path.getmtime(os.path.join(HERE, "ref_tick.cpp")))
+    if fresh:
+        return REF_TICK_PATH
+    if os.path.exists(REFERENCE_WORLD_CPP):
         subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        return REF_TICK_PATH
+    incs = [os.path.join(HERE, "_ref", "tick_%s.inc" % k) for k in TICK_INC]
+    if not all(os.path.exists(p) and os.path.getsize(p) > 0 for p in incs):
+        return None
+    subprocess.run([os.environ.get("CXX", "g++"), "-O2", "-std=c++20", "-fPIC", "-ffp-contract=off", "-Wno-narrowing",
+                    "-pthread", "-shared", "-I" + os.path.join(HERE, "_ref"), "-o", REF_TICK_PATH,
+                    os.path.join(HERE, "ref_tick.cpp")], check=True)
     return REF_TICK_PATH
+
+
+def _reference_tables(oracle):
+    """The oracle's material table in the reference harness's layout."""
+    n = oracle.material_count()
+    mats = np.zeros((n, 10), np.int32)
+    for i in range(n):
+        m = oracle.material(i)
+        mats[i, :9] = [m[0], m[1], m[2], m[3], m[9], m[10], m[11], m[12], m[13] if m[0] != 3 else 0]
+    special = np.array([oracle.find(s) for s in SPECIAL_MATERIALS], np.int32)
+    react, inter = oracle.rules()
+    return n, mats, special, np.ascontiguousarray(react), np.ascontiguousarray(inter)
+
+
+def reference_world_bench(lib_path, oracle, ids, colours, temps, parts, cell_iter, seed, threads, warm, steps,
+                          budget_s):
+    """Times the reference's own world::tick() + world::tickCells() on the grid and
+    particles (PARTICLE_DTYPE) with `threads` pool workers: (seconds, steps timed)."""
+    lib = C.CDLL(lib_path)
+    f = lib.ref_world_bench
+    f.restype = C.c_double
+    f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint32, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                  C.c_int, C.c_double, C.c_void_p]
+    n, mats, special, react, inter = _reference_tables(oracle)
+    h, w = ids.shape
+    pf = np.ascontiguousarray(np.stack([parts[k] for k in ("x", "y", "vx", "vy", "ax", "ay")], 1), np.float32)
+    pi = np.ascontiguousarray(np.stack([parts["id"].astype(np.uint32), parts["colour"]], 1), np.uint32)
+    done = C.c_int(0)
+    secs = f(w, h, cell_iter, seed & 0xFFFFFFFF, n, _ptr(mats), _ptr(special), _ptr(react), len(inter), _ptr(inter),
+             _ptr(np.ascontiguousarray(ids, np.uint16)), _ptr(np.ascontiguousarray(colours, np.uint32)),
+             _ptr(np.ascontiguousarray(temps, np.int32)), len(parts), _ptr(pf), _ptr(pi), threads, warm, steps,
+             float(budget_s), C.byref(done))
+    if secs < 0:
+        raise ValueError("the reference tick wrote outside the grid")
+    return secs, done.value
 
 
 SPECIAL_MATERIALS = ("GENERIC_AIR", "GENERIC_SOLID", "FIRE", "WATER", "LAVA", "STEAM", "OBSIDIAN")
@@ -520,13 +571,7 @@ def reference_world_tick(lib_path, oracle, ids, colours, temps, moved, cell_iter
     f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint32, C.c_uint32, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                   C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                   C.c_int, C.c_void_p]
-    n = oracle.material_count()
-    mats = np.zeros((n, 10), np.int32)
-    for i in range(n):
-        m = oracle.material(i)
-        mats[i, :9] = [m[0], m[1], m[2], m[3], m[9], m[10], m[11], m[12], m[13] if m[0] != 3 else 0]
-    special = np.array([oracle.find(s) for s in SPECIAL_MATERIALS], np.int32)
-    react, inter = oracle.rules()
+    n, mats, special, react, inter = _reference_tables(oracle)
     h, w = ids.shape
     i2 = np.ascontiguousarray(ids, np.uint16).copy()
     c2 = np.ascontiguousarray(colours, np.uint32).copy()

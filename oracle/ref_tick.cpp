@@ -15,9 +15,11 @@
 //  - the tile factories TilesCreate*: their colours come from textures in the
 //    reference; here they follow the oracle's factory parameters (base colour, one
 //    draw when a channel jitters, the factory temperature);
-//  - the thread pools, which run each pushed task at once and hand back a ready
-//    future, so the chunk tasks of a colour run in push order (they touch disjoint
-//    cells; the spawned particles are merged in push order as in the reference);
+//  - the thread pools: by default each pushed task runs at once and hands back a
+//    ready future, so the chunk tasks of a colour run in push order (they touch
+//    disjoint cells; the spawned particles are merged in push order as in the
+//    reference); for timing, a pool of worker threads as the reference's
+//    (world.cpp:59), with the draw state kept per thread;
 //  - rand(): a macro expanded inside the cell loops, where `x`, `y` and `iter` are
 //    the cell being updated; it returns the oracle's counter draw for that cell
 //    update -- keyed on (seed, tick, iter * 3 + sweep, x, y), counted from 0 per
@@ -31,7 +33,12 @@
 //    macro makes each `CellData(...)` construction a brace initialisation, whose
 //    elements are evaluated in order (the int positions narrow to f32 as in the call).
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <thread>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -99,10 +106,10 @@ static inline uint32_t cell_key(uint32_t pk, uint32_t x, uint32_t y) { return h3
 static inline uint32_t draw_k(uint32_t ck, uint32_t k) { return h32(ck + k * 0x9E3779B9U + 0x632BE5ABU); }
 
 static uint32_t g_seed = 0, g_tick = 0;
-static int g_sweep = 2;  // the first `CHUNK_H - 1` makes it 0
-static long long g_cur = -1;  // the cell update the counter belongs to
-static uint32_t g_ck = 0, g_k = 0;
-static long long g_draws = 0;
+static thread_local int g_sweep = 2;       // the first `CHUNK_H - 1` makes it 0
+static thread_local long long g_cur = -1;  // the cell update the counter belongs to
+static thread_local uint32_t g_ck = 0, g_k = 0;
+static thread_local long long g_draws = 0;
 
 struct Draw {
     uint32_t v;
@@ -164,24 +171,66 @@ static GameState g_game_state;
 static Globals global{&g_game_state};
 
 struct Pool {
+    // workers == 0: run each task at once in the caller
+    std::vector<std::thread> workers;
+    std::deque<std::function<void()>> q;
+    std::mutex mu;
+    std::condition_variable cv;
+    bool stop = false;
+    void start(int n) {
+        for (int i = 0; i < n; i++)
+            workers.emplace_back([this] {
+                for (;;) {
+                    std::function<void()> job;
+                    {
+                        std::unique_lock<std::mutex> lk(mu);
+                        cv.wait(lk, [this] { return stop || !q.empty(); });
+                        if (stop && q.empty()) return;
+                        job = std::move(q.front());
+                        q.pop_front();
+                    }
+                    job();
+                }
+            });
+    }
+    void halt() {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            stop = true;
+        }
+        cv.notify_all();
+        for (auto &t : workers) t.join();
+        workers.clear();
+        stop = false;
+    }
     template <class F>
     auto push(F &&f) -> std::future<decltype(f(0))> {
         using R = decltype(f(0));
-        std::promise<R> p;
-        if constexpr (std::is_void_v<R>) {
-            f(0);
-            p.set_value();
-        } else {
-            p.set_value(f(0));
+        if (workers.empty()) {
+            std::promise<R> p;
+            if constexpr (std::is_void_v<R>) {
+                f(0);
+                p.set_value();
+            } else {
+                p.set_value(f(0));
+            }
+            return p.get_future();
         }
-        return p.get_future();
+        auto task = std::make_shared<std::packaged_task<R(int)>>(std::forward<F>(f));
+        std::future<R> fut = task->get_future();
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            q.emplace_back([task] { (*task)(0); });
+        }
+        cv.notify_one();
+        return fut;
     }
 };
 struct WorldSys {
     Pool *tickPool, *tickVisitedPool;
 };
-static Pool g_pool;
-static WorldSys world_sys{&g_pool, &g_pool};
+static Pool g_pool, g_vpool;
+static WorldSys world_sys{&g_pool, &g_vpool};
 
 struct TickZone {
     int x, y, w, h;
@@ -199,10 +248,12 @@ struct world {
     void setTile(int x, int y, MaterialInstance type);
     void physicsCheck(int, int) {}
     void tick();
+    void tickCells();
 };
 
 #include "tick_world_gettile.inc"
 #include "tick_world_settile.inc"
+#include "tick_cells.inc"
 
 // the loops' draws and factories take the cell being updated from their scope;
 // the rand() after the loops (physicsCheck's position) reads these
@@ -235,12 +286,22 @@ static int x = 0, y = 0, iter = 0;
 // phase, temporary, lifetime, fadeTime; floats as bits) up to cap and returns their
 // count (or -1 when a cell outside the grid would be read: the grid needs its
 // border).
-extern "C" int ref_world_tick(int W, int H, int cell_iter, uint32_t seed, uint32_t tick, int n_ticks, int n,
-                              const int32_t *mats, const int32_t *special, const int32_t *reactions, int ni,
-                              const int32_t *inter, uint16_t *ids, uint32_t *cols, int32_t *temps, uint8_t *moved,
-                              int32_t *parts, int cap, long long *draws) {
+struct Registry {
+    std::vector<Material> store;
+    std::vector<int *> n_arrays;
+    std::vector<std::vector<MaterialInteraction> *> i_arrays;
+    ~Registry() {
+        for (int *p : n_arrays) delete[] p;
+        for (auto *p : i_arrays) delete[] p;
+    }
+};
+
+// fills the GAME() registry and the factories from the table (see below)
+static void setup_registry(Registry &reg, int n, const int32_t *mats, const int32_t *special,
+                           const int32_t *reactions, int ni, const int32_t *inter) {
     g_reg = GameReg();
-    std::vector<Material> store((size_t)n);
+    reg.store.assign((size_t)n, Material());
+    std::vector<Material> &store = reg.store;
     g_reg.materials_container.assign((size_t)n, nullptr);
     g_reg.materials_count = n;
     Material *named[7] = {&g_reg.materials_list.GENERIC_AIR, &g_reg.materials_list.GENERIC_SOLID,
@@ -265,8 +326,6 @@ extern "C" int ref_world_tick(int W, int H, int cell_iter, uint32_t seed, uint32
         e.ofsY = r[6];
         ints[r[0]][r[1]].push_back(e);
     }
-    std::vector<int *> n_arrays;
-    std::vector<std::vector<MaterialInteraction> *> i_arrays;
     for (int i = 0; i < n; i++) {
         Material &m = *g_reg.materials_container[i];
         const int32_t *r = mats + 10 * i;
@@ -299,9 +358,18 @@ extern "C" int ref_world_tick(int W, int H, int cell_iter, uint32_t seed, uint32
         m.nInteractions = cnt;
         m.interactions = lists;
         m.interact = any;
-        n_arrays.push_back(cnt);
-        i_arrays.push_back(lists);
+        reg.n_arrays.push_back(cnt);
+        reg.i_arrays.push_back(lists);
     }
+
+}
+
+extern "C" int ref_world_tick(int W, int H, int cell_iter, uint32_t seed, uint32_t tick, int n_ticks, int n,
+                              const int32_t *mats, const int32_t *special, const int32_t *reactions, int ni,
+                              const int32_t *inter, uint16_t *ids, uint32_t *cols, int32_t *temps, uint8_t *moved,
+                              int32_t *parts, int cap, long long *draws) {
+    Registry reg;
+    setup_registry(reg, n, mats, special, reactions, ni, inter);
 
     // the grid with 16 solid rows above and below, so that no read leaves the array
     const size_t N = (size_t)W * H, pad = (size_t)16 * W;
@@ -360,8 +428,75 @@ extern "C" int ref_world_tick(int W, int H, int cell_iter, uint32_t seed, uint32
         np++;
         delete c;
     }
-    for (int *p : n_arrays) delete[] p;
-    for (auto *p : i_arrays) delete[] p;
     if (draws) *draws = g_draws;
     return ok ? np : -1;
+}
+
+// Timing: the reference's own world::tick() + world::tickCells() on a grid (ids,
+// colours, temperatures; liquids at the MaterialInstance default amount) and
+// particles (rows of x, y, vx, vy, ax, ay as floats, then id, colour), `warm`
+// untimed steps then `steps` timed ones, the chunk tasks on a pool of `threads`
+// workers, stopping early once the timed steps pass budget_s seconds (*done = the
+// steps timed). Returns their seconds (negative when the grid's padding was
+// written: the scene needs its border).
+extern "C" double ref_world_bench(int W, int H, int cell_iter, uint32_t seed, int n, const int32_t *mats,
+                                  const int32_t *special, const int32_t *reactions, int ni, const int32_t *inter,
+                                  const uint16_t *ids, const uint32_t *cols, const int32_t *temps, int n_parts,
+                                  const float *pf, const uint32_t *pi, int threads, int warm, int steps,
+                                  double budget_s, int *done) {
+    Registry reg;
+    setup_registry(reg, n, mats, special, reactions, ni, inter);
+    const size_t N = (size_t)W * H, pad = (size_t)16 * W;
+    std::vector<MaterialInstance> tiles(N + 2 * pad, Tiles_TEST_SOLID);
+    std::vector<char> dirty(N), tv1(N), tv2(N);
+    std::vector<f32> fx(N), fy(N);
+    for (size_t i = 0; i < N; i++) tiles[pad + i] = MaterialInstance(g_reg.materials_container[ids[i]], cols[i],
+                                                                      (mat_temperature)temps[i]);
+    world wd;
+    wd.width = W;
+    wd.height = H;
+    wd.real_tiles = tiles.data() + pad;
+    wd.dirty = reinterpret_cast<bool *>(dirty.data());
+    wd.tickVisited1 = reinterpret_cast<bool *>(tv1.data());
+    wd.tickVisited2 = reinterpret_cast<bool *>(tv2.data());
+    wd.flowX = fx.data();
+    wd.flowY = fy.data();
+    wd.tickZone = TickZone{0, 0, W, H};
+    for (int i = 0; i < n_parts; i++) {
+        const float *f = pf + 6 * i;
+        const uint32_t *u = pi + 2 * i;
+        MaterialInstance t(g_reg.materials_container[u[0]], u[1], 0);
+        wd.cells.push_back(new CellData(t, f[0], f[1], f[2], f[3], f[4], f[5]));
+    }
+    global.game->Iso.globaldef.cell_iter = cell_iter;
+    g_seed = seed;
+    if (threads > 1) {
+        g_pool.start(threads);
+        g_vpool.start(1);
+    }
+    double secs = 0;
+    int timed = 0;
+    for (int s = 0; s < warm + steps; s++) {
+        const auto t0 = std::chrono::steady_clock::now();
+        g_tick = (uint32_t)s;
+        wd.tick();
+        wd.tickCells();
+        const auto t1 = std::chrono::steady_clock::now();
+        if (s >= warm) {
+            secs += std::chrono::duration<double>(t1 - t0).count();
+            timed++;
+            if (secs > budget_s) break;
+        }
+    }
+    if (done) *done = timed;
+    if (threads > 1) {
+        g_pool.halt();
+        g_vpool.halt();
+    }
+    int ok = 1;
+    for (size_t i = 0; i < pad; i++)
+        if (tiles[i].mat->id != Tiles_TEST_SOLID.mat->id || tiles[pad + N + i].mat->id != Tiles_TEST_SOLID.mat->id)
+            ok = 0;
+    for (CellData *c : wd.cells) delete c;
+    return ok ? secs : -secs - 1.0;
 }
