@@ -260,6 +260,7 @@ def render_config1(fse, torch, W, H, seed, NP, ticks=20):
     for _ in range(5):
         _, n_isl = world.islands(1000)
     isl_ms = (time.perf_counter() - t0) * 1e3 / 5
+    ref_cpu = render_reference_cpu(fse, world, stream, torch)
     world.close()
     islands = {"physics_check_ms": round(pc_ms, 3), "physics_check_cut": int(cut), "label_all_ms": round(isl_ms, 3),
                "label_all_gcells": round(W * H / (isl_ms / 1e3) / 1e9, 3), "islands_le_1000": int(n_isl)}
@@ -267,7 +268,36 @@ def render_config1(fse, torch, W, H, seed, NP, ticks=20):
             "dirty_pass_ms": round(d_ms / ticks, 4), "dirty_pass_gcells": round(W * H * ticks / (d_ms / 1e3) / 1e9, 3),
             "dirty_cells_per_tick": ndirty // ticks, "dirty_pass_gbs": round(gbs, 1),
             "dirty_pass_frac": round(gbs / peak, 4), "peak": peak, "peak_kind": peak_kind,
-            "particle_layer_ms": round(c_ms / ticks, 4), "ticks": ticks}
+            "particle_layer_ms": round(c_ms / ticks, 4), "ticks": ticks, "cpu_reference": ref_cpu}
+
+
+def render_reference_cpu(fse, world, stream, torch):
+    """The reference's own dirty-pixel loop (game.cpp:1995-2061, compiled unchanged;
+    one host thread, as one task of its pool) on the world after one more step, with
+    the cells that step changed marked dirty: host clock around one pass."""
+    from oracle.binding import build_reference_render, reference_render_dirty
+
+    try:
+        lib = build_reference_render()
+    except Exception:  # noqa: BLE001 - no compiler or sources here
+        lib = None
+    if lib is None:
+        return None
+    before = world.state()
+    with torch.cuda.stream(stream):
+        world.step(1)
+    torch.cuda.synchronize()
+    st = world.state()
+    dirty = ((st["id"] != before["id"]) | (st["colour"] != before["colour"])).astype(np.uint8)
+    mats = np.array([fse.material_get(i) for i in range(fse.material_count())])
+    types, iters, alpha, emit = mats[:, 0], mats[:, 2], mats[:, 5], mats[:, 8].astype(np.uint32)
+    z = np.zeros(st["id"].shape, np.float32)
+    t0 = time.perf_counter()
+    reference_render_dirty(lib, st["id"], st["colour"], dirty, z, z, z, z, (types, alpha, emit, iters),
+                           fse.material_find("FIRE"))
+    ms = (time.perf_counter() - t0) * 1e3
+    return {"dirty_pass_ms": round(ms, 2), "cores": 1, "kind": "reference", "dirty_cells": int(dirty.sum()),
+            "sample": "one pass over the whole world, host clock (includes the harness's copies of the planes)"}
 
 
 def temperature_config1(fse, torch, W, H, seed, NP, calls=10):
@@ -309,10 +339,12 @@ def temperature_config1(fse, torch, W, H, seed, NP, calls=10):
         nch = int(ch.sum())
         nbytes += 8 * cells + 4 * (nch - nch_soup) + 2 * nch_soup
         nchanged += nch
+    cpu = temperature_reference_cpu(fse, world)
     world.close()
     peak, peak_kind = peaks()
     gbs = nbytes / (ms / 1e3) / 1e9
-    return {"step_ms": round(ms / calls, 4), "gcells": round(cells * calls / (ms / 1e3) / 1e9, 3),
+    return {"cpu_reference": cpu, "step_ms": round(ms / calls, 4),
+            "gcells": round(cells * calls / (ms / 1e3) / 1e9, 3),
             "changed_cells_per_step": nchanged // calls, "achieved_gbs": round(gbs, 1),
             "frac": round(gbs / peak, 4), "peak": peak, "peak_kind": peak_kind, "calls": calls,
             "kernels": "k_temp_tiles + k_temp_commit",
@@ -347,6 +379,30 @@ def reference_order_config1(fse, torch, W, H, seed, NP, steps=3):
     world.close()
     return {"ms_per_step": round(ms / steps, 3), "gcells": round(W * H * steps / (ms / 1e3) / 1e9, 4),
             "steps": steps, "order": "reference: cells in world.cpp's loop order, one thread per chunk row (wavefront)"}
+
+
+def temperature_reference_cpu(fse, world):
+    """The reference's own world::tickTemperature (world.cpp:1950-2004, compiled
+    unchanged; single-threaded as in the reference) on the same world, the tick zone
+    one cell inside the world edge: host clock around one step."""
+    from oracle.binding import build_reference_temperature, reference_tick_temperature
+
+    try:
+        lib = build_reference_temperature()
+    except Exception:  # noqa: BLE001 - no compiler or sources here
+        lib = None
+    if lib is None:
+        return None
+    ids = world.state()["id"]
+    temps = world.temperature()
+    cond = np.array([fse.get_conduction(i) for i in range(fse.material_count())], np.float64)
+    h, w = ids.shape
+    t0 = time.perf_counter()
+    reference_tick_temperature(lib, ids, temps, cond[:, 0].astype(np.uint32), cond[:, 1].astype(np.float32),
+                               cond[:, 2].astype(np.float32), (1, 1, w - 2, h - 2))
+    ms = (time.perf_counter() - t0) * 1e3
+    return {"step_ms": round(ms, 2), "gcells": round((w - 2) * (h - 2) / (ms / 1e3) / 1e9, 4), "cores": 1,
+            "kind": "reference", "sample": "one step over the world less its edge cells, host clock"}
 
 
 def pack_config1(fse, torch, W, H, seed, NP, calls=5):

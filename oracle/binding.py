@@ -370,13 +370,24 @@ class OracleWorld:
         return out[: min(n, cap)], n
 
 
-def build_reference_temperature(force=False):
-    """Compile the reference's own world::tickTemperature (oracle/Makefile `ref`).
-
-    Needs the reference source tree; returns None when it is absent.
-    """
-    if not os.path.exists(REFERENCE_WORLD_CPP):
+def _build_from_inc(so_path, cpp, incs, std):
+    """Without the reference tree: compile a harness from the pieces oracle/Makefile
+    extracted before into oracle/_ref (they travel with the repository); None when
+    they are absent."""
+    paths = [os.path.join(HERE, "_ref", i) for i in incs]
+    if not all(os.path.exists(p) and os.path.getsize(p) > 0 for p in paths):
         return None
+    if not os.path.exists(so_path) or os.path.getmtime(so_path) < os.path.getmtime(os.path.join(HERE, cpp)):
+        subprocess.run([os.environ.get("CXX", "g++"), "-O2", "-std=" + std, "-fPIC", "-ffp-contract=off", "-shared",
+                        "-I" + os.path.join(HERE, "_ref"), "-o", so_path, os.path.join(HERE, cpp)], check=True)
+    return so_path
+
+
+def build_reference_temperature(force=False):
+    """Compile the reference's own world::tickTemperature (oracle/Makefile `ref`), or
+    from its extracted pieces without the tree; None when neither is present."""
+    if not os.path.exists(REFERENCE_WORLD_CPP):
+        return _build_from_inc(REF_TEMPERATURE_PATH, "ref_temperature.cpp", ["tick_temperature.inc"], "c++17")
     if force or not os.path.exists(REF_TEMPERATURE_PATH) or os.path.getmtime(REF_TEMPERATURE_PATH) < max(
         os.path.getmtime(os.path.join(HERE, f)) for f in ("ref_temperature.cpp", "Makefile")
     ):
@@ -589,9 +600,10 @@ def reference_world_tick(lib_path, oracle, ids, colours, temps, moved, cell_iter
 
 
 def build_reference_render(force=False):
-    """Compile the reference's own dirty-pixel loop of game::tick (oracle/Makefile `ref`)."""
+    """Compile the reference's own dirty-pixel loop of game::tick (oracle/Makefile `ref`),
+    or from its extracted piece without the tree; None when neither is present."""
     if not os.path.exists(REFERENCE_WORLD_CPP):
-        return None
+        return _build_from_inc(REF_RENDER_PATH, "ref_render.cpp", ["dirty_loop.inc"], "c++20")
     if force or not os.path.exists(REF_RENDER_PATH) or os.path.getmtime(REF_RENDER_PATH) < os.path.getmtime(
             os.path.join(HERE, "ref_render.cpp")):
         subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
