@@ -381,6 +381,41 @@ def reference_order_config1(fse, torch, W, H, seed, NP, steps=3):
             "steps": steps, "order": "reference: cells in world.cpp's loop order, one thread per chunk row (wavefront)"}
 
 
+def pack_reference_cpu(om, data, offs):
+    """The reference's own codec core on the same chunks: its vendored LZ4 1.9.4
+    (LZ4_compress_fast with acceleration 10, as Chunk::ChunkWrite calls it,
+    chunk.cpp:219-330, and LZ4_decompress_safe) on each chunk's two raw blocks, one
+    thread, host clock."""
+    from oracle.binding import ReferenceLZ4, build_reference_lz4, lz4_decode
+
+    try:
+        path = build_reference_lz4()
+    except Exception:  # noqa: BLE001 - no compiler or sources here
+        path = None
+    if path is None:
+        return None
+    ref = ReferenceLZ4(path)
+    blocks = []
+    for k in range(len(offs) - 1):
+        p = data[offs[k]:offs[k + 1]]
+        hd = np.frombuffer(p[1:17].tobytes(), "<i4")
+        b1 = p[17:17 + hd[1]]
+        b2 = p[17 + hd[1]:17 + hd[1] + hd[3]]
+        blocks.append((lz4_decode(b1, int(hd[0]))[0], lz4_decode(b2, int(hd[2]))[0]))
+    t0 = time.perf_counter()
+    packed = [(ref.compress(r1, 10), ref.compress(r2, 10)) for r1, r2 in blocks]
+    pack_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for (c1, c2), (r1, r2) in zip(packed, blocks):
+        ref.decompress(c1, len(r1))
+        ref.decompress(c2, len(r2))
+    unpack_s = time.perf_counter() - t0
+    n = len(blocks)
+    return {"chunks": n, "threads": 1, "kind": "reference", "pack_ms_per_chunk": round(pack_s * 1e3 / n, 3),
+            "unpack_ms_per_chunk": round(unpack_s * 1e3 / n, 3),
+            "packed_bytes_per_chunk": int(sum(len(a) + len(b) for a, b in packed) // n)}
+
+
 def temperature_reference_cpu(fse, world):
     """The reference's own world::tickTemperature (world.cpp:1950-2004, compiled
     unchanged; single-threaded as in the reference) on the same world, the tick zone
@@ -450,9 +485,10 @@ def pack_config1(fse, torch, W, H, seed, NP, calls=5):
     t0 = time.perf_counter()
     ob.unpack(od, oo)
     cpu_unpack_s = time.perf_counter() - t0
+    lz4 = pack_reference_cpu(om, od, oo)
     world.close()
     back.close()
-    return {"chunks": n, "packed_bytes": int(offs[-1]), "ratio": round(offs[-1] / raw, 4),
+    return {"cpu_reference": lz4, "chunks": n, "packed_bytes": int(offs[-1]), "ratio": round(offs[-1] / raw, 4),
             "pack_ms": round(pack_s * 1e3, 3), "unpack_ms": round(unpack_s * 1e3, 3),
             "pack_gbs": round(raw / pack_s / 1e9, 2), "unpack_gbs": round(raw / unpack_s / 1e9, 2),
             "roundtrip_ids_equal": same,

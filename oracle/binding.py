@@ -436,9 +436,16 @@ def lz4_decode(src, cap):
 
 
 def build_reference_lz4(force=False):
-    """Compile the reference's vendored LZ4 (oracle/Makefile `ref`); None without the reference tree."""
+    """Compile the reference's vendored LZ4 (oracle/Makefile `ref`), or its copy in
+    oracle/_ref without the tree; None when neither is present."""
     if not os.path.exists(REFERENCE_WORLD_CPP):
-        return None
+        src = os.path.join(HERE, "_ref", "lz4.c")
+        if not os.path.exists(src):
+            return None
+        if not os.path.exists(REF_LZ4_PATH):
+            subprocess.run([os.environ.get("CC", "gcc"), "-O2", "-fPIC", "-shared", "-I" + os.path.join(HERE, "_ref"),
+                            "-o", REF_LZ4_PATH, src], check=True)
+        return REF_LZ4_PATH
     if force or not os.path.exists(REF_LZ4_PATH):
         subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
     return REF_LZ4_PATH
