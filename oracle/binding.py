@@ -639,6 +639,39 @@ def reference_render_dirty(lib_path, ids, colours, dirty, flow_x, flow_y, prev_x
     return tex, arrs[3], arrs[4], arrs[5], arrs[6], moving
 
 
+REF_PHYSICS_PATH = os.path.join(HERE, "_ref", "libref_physics.so")
+
+
+def build_reference_physics(force=False):
+    """Compile the reference's own world::physicsCheck (oracle/Makefile `ref`), or from
+    its extracted pieces without the tree; None when neither is present."""
+    if not os.path.exists(REFERENCE_WORLD_CPP):
+        return _build_from_inc(REF_PHYSICS_PATH, "ref_physics.cpp",
+                               ["physics_check.inc", "physics_flood.inc", "physics_gettile.inc"], "c++20")
+    if force or not os.path.exists(REF_PHYSICS_PATH) or os.path.getmtime(REF_PHYSICS_PATH) < os.path.getmtime(
+            os.path.join(HERE, "ref_physics.cpp")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    return REF_PHYSICS_PATH
+
+
+def reference_physics_check(lib_path, types, colours, x, y):
+    """One physicsCheck(x, y) of the compiled reference on a grid of physics types and
+    colours: (types after, image or None, (origin x, origin y) or None)."""
+    lib = C.CDLL(lib_path)
+    f = lib.ref_physics_check
+    f.restype = C.c_long
+    f.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_long] + [C.c_void_p] * 4
+    h, w = types.shape
+    t = np.ascontiguousarray(types, np.uint8).copy()
+    c = np.ascontiguousarray(colours, np.uint32)
+    img = np.zeros(1 << 20, np.uint32)
+    o = [C.c_int(0) for _ in range(4)]
+    n = f(w, h, _ptr(t), _ptr(c), x, y, _ptr(img), img.size, *[C.byref(v) for v in o])
+    if n == 0:
+        return t, None, None
+    return t, img[:n].reshape(o[3].value, o[2].value).copy(), (o[0].value, o[1].value)
+
+
 def build_reference_objects(force=False):
     """Compile the reference's own rigid-body stamp/readback loops (oracle/Makefile `ref`)."""
     if not os.path.exists(REFERENCE_WORLD_CPP):
