@@ -73,3 +73,28 @@ def test_islands_match_the_oracle(fse, oracle_mod):
         world.render_dirty()
         ow.render_dirty()
         np.testing.assert_array_equal(world.render_texture(0), ow.render_texture(0))
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_device_physics_check_matches_reference_digests(fse, oracle_mod, seed):
+    """The device physicsCheck, one check after another from the same seed cells,
+    against the digests of the reference's own function (tests/golden/islands_ref.json)."""
+    import json
+
+    from test_islands_ref import GOLDEN, _scene, result_digest, seed_cells
+
+    o = oracle_mod.Oracle()
+    o.reset_materials()
+    types_of = np.array([fse.material_get(i)[0] for i in range(fse.material_count())], np.uint8)
+    ids, colours, starts = _scene(o, seed)
+    h, w = ids.shape
+    z = np.zeros((h, w), np.int32)
+    world = fse.World(w, h, seed=1)
+    world.upload({"id": ids, "colour": colours, "scalar": z, "flags": np.zeros((h, w), np.uint8), "diff": z})
+    got = []
+    for (y, x) in seed_cells(types_of, ids, starts, seed):
+        n, bbox, img = world.physicsCheck(int(x), int(y))
+        org = (int(bbox[0]), int(bbox[1])) if img is not None else None
+        got.append(result_digest(types_of[world.state()["id"]], img, org))
+    world.close()
+    assert got == json.load(open(GOLDEN))[str(seed)]
