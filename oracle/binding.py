@@ -75,6 +75,7 @@ class Oracle:
                 "om_material_set_interaction": (i32, [i32, i32, i32, i32, i32, i32, i32]),
                 "om_material_count": (i32, []),
                 "om_material_rules": (i32, [vp, vp, i32]),
+                "om_material_tile_temperature": (i32, [i32]),
                 "om_material_find": (i32, [C.c_char_p]),
                 "om_material_get": (None, [i32, vp]),
                 "om_world_new": (vp, [i32, i32, i32, i32, u32]),
@@ -544,7 +545,7 @@ def _reference_tables(oracle):
     mats = np.zeros((n, 10), np.int32)
     for i in range(n):
         m = oracle.material(i)
-        mats[i, :9] = [m[0], m[1], m[2], m[3], m[9], m[10], m[11], m[12], m[13] if m[0] != 3 else 0]
+        mats[i, :9] = [m[0], m[1], m[2], m[3], m[9], m[10], m[11], m[12], oracle.lib.om_material_tile_temperature(i)]
     special = np.array([oracle.find(s) for s in SPECIAL_MATERIALS], np.int32)
     react, inter = oracle.rules()
     return n, mats, special, np.ascontiguousarray(react), np.ascontiguousarray(inter)

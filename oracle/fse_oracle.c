@@ -333,6 +333,12 @@ static const inter_list_t *find_inter(int mat, int other) {
 
 int om_material_count(void) { return NMAT; }
 
+/* MaterialInstance::temperature of a new tile of the material (TilesCreate) */
+int om_material_tile_temperature(int mat) {
+    if (mat < 0 || mat >= NMAT) return 0;
+    return M[mat].type == T_SOUP ? M[mat].f_temp : M[mat].f_scalar;
+}
+
 /* every material's reactions (4 rows of kind, temperature, result; kind 0 = none)
  * and the interactions in registration order (material, other, kind, data1, data2,
  * ofs_x, ofs_y); returns the number of interaction rows (up to cap written) */

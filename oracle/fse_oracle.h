@@ -73,6 +73,7 @@ void om_material_conduction(int mat, uint32_t out[3]);
 int om_material_set_factory_temperature(int mat, int32_t temperature);
 int om_material_set_interaction(int mat, int other, int kind, int data1, int data2, int ofs_x, int ofs_y);
 int om_material_count(void);
+int om_material_tile_temperature(int mat);
 int om_material_rules(int32_t *react, int32_t *inter, int cap);
 int om_material_find(const char *index_name);
 /* 16 ints: type, density bits, iterations, slip, max_stab, alpha, colour, emit, emit_colour,

@@ -4,9 +4,13 @@ oracle/Makefile `ref` compiles world::tick (source/engine/world.cpp:1036-1948)
 unchanged, with the pieces of the reference it calls (oracle/ref_tick.cpp). Its
 rand() returns the oracle's counter draws for the cell being updated, so the
 reference's rules and the oracle's restatement in the reference's chunk order
-(OM_ORDER_SEQ) consume the same numbers. On scenes without liquids (whose amounts
-the reference keeps in f32, this path in Q16.16), every cell (material, colour,
-temperature, moved flag) and every spawned particle must agree bit for bit.
+(OM_ORDER_SEQ) consume the same numbers. Every cell (material, colour,
+temperature, moved flag) and every spawned particle must agree bit for bit on the
+scenes without liquids. The reference keeps liquid amounts in f32, this path in
+Q16.16, so with liquids a flow at the FLUID_MinValue threshold can land on either
+side: a scene of 25% water and 5% lava is held to 99.95% of cells identical (in each
+of material, colour, temperature and moved flag) after one tick and 99.9% after
+three (measured: 99.98-99.99% and 99.96-99.99%).
 tests/golden/tick_ref.json keeps digests of the reference's results (made by
 tests/golden/make_tick_ref.py) for machines without the reference tree. The CUDA
 kernels are checked against the same oracle rules in the partitioned order by the
@@ -26,12 +30,13 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "tic
 START_TICK = 7
 
 
-def oracle_rows(parts):
-    """Oracle particles as the reference harness's rows (16 int32 each)."""
+def oracle_rows(parts, soup_ids=()):
+    """Oracle particles as the reference harness's rows (16 int32 each); a liquid
+    particle's temperature is its own field (its scalar is the amount)."""
     rows = np.zeros((len(parts), 16), np.int32)
     rows[:, 0] = parts["id"]
     rows[:, 1] = parts["colour"].view(np.int32)
-    rows[:, 2] = parts["scalar"]
+    rows[:, 2] = np.where(np.isin(parts["id"], list(soup_ids)), parts["temperature"], parts["scalar"])
     for j, k in enumerate(("x", "y", "vx", "vy", "ax", "ay", "target_x", "target_y", "target_force")):
         rows[:, 3 + j] = np.ascontiguousarray(parts[k]).view(np.int32)
     rows[:, 12] = parts["bits"] & 1
@@ -53,11 +58,14 @@ def run_oracle(oracle_mod, ids, case):
     st = scene(ids, w, h, seed, kind)
     ow = oracle_mod.OracleWorld(w, h, 128, ci, seed)
     ow.set_state(st)
+    ow.set_temperature(st["temperature"])
     ow.tick_count = START_TICK
     for _ in range(nt):
         ow.tick(order=ORDER_SEQ)
     o = ow.state()
-    return st, (o["id"], o["colour"], o["scalar"], (o["flags"] >> 7).astype(np.uint8), oracle_rows(ow.particles()))
+    soup = [ids["WATER"], ids["LAVA"]]
+    return st, (o["id"], o["colour"], ow.temperature().astype(np.int32), (o["flags"] >> 7).astype(np.uint8),
+                oracle_rows(ow.particles(), soup))
 
 
 def run_reference(oracle_mod, lib, ids, case):
@@ -65,8 +73,9 @@ def run_reference(oracle_mod, lib, ids, case):
 
     w, h, seed, kind, ci, nt = case
     st = scene(ids, w, h, seed, kind)
-    ri, rc, rt, rm, rp, _ = reference_world_tick(lib, oracle_mod.Oracle(), st["id"], st["colour"], st["scalar"],
-                                                 st["flags"] >> 7, ci, seed, START_TICK, nt)
+    ri, rc, rt, rm, rp, _ = reference_world_tick(lib, oracle_mod.Oracle(), st["id"], st["colour"],
+                                                 st["temperature"].astype(np.int32), st["flags"] >> 7, ci, seed,
+                                                 START_TICK, nt)
     return ri, rc, rt, rm, rp
 
 
@@ -119,3 +128,17 @@ def test_scenes_exercise_every_rule(oracle_mod, ids):
             np.isin(rows[:, 0], [ids["PIN_SAND_A"], ids["GENERIC_SAND"]]).sum())
         seen["moved changed"] = seen.get("moved changed", 0) + int(((st["flags"] >> 7) != gm).sum())
     assert all(v != 0 for v in seen.values()), seen
+
+
+@pytest.mark.parametrize("ticks,share", [(1, 0.9995), (3, 0.999)])
+def test_liquids_track_the_reference(oracle_mod, ids, ticks, share):
+    from oracle.binding import build_reference_tick
+
+    lib = build_reference_tick()
+    if lib is None:
+        pytest.skip("reference tree absent")
+    case = (512, 384, 16, "liquid", 3, ticks)
+    ref = run_reference(oracle_mod, lib, ids, case)
+    _, got = run_oracle(oracle_mod, ids, case)
+    for name, a, b in zip(("id", "colour", "temperature", "moved"), ref, got):
+        assert (a == b).mean() >= share, (name, float((a == b).mean()))

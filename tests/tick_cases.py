@@ -1,9 +1,10 @@
 """Seeded scenes for pinning the oracle's cell rules against the reference's own
 world::tick (source/engine/world.cpp:1036-1948), compiled by oracle/Makefile.
 
-The scenes hold no liquids: the reference keeps fluid amounts in f32 and this path
-in Q16.16 by design, so liquid cells cannot agree bit for bit. Every other rule of
-the tick runs: falling and sliding sand with friction pillars, slipperiness and
+The scenes of CASES hold no liquids: the reference keeps fluid amounts in f32 and
+this path in Q16.16 by design, so a flow at the FLUID_MinValue threshold can land on
+either side and liquid cells cannot agree bit for bit; the "liquid" scene is compared
+with a tolerance instead. Every other rule of the tick runs: falling and sliding sand with friction pillars, slipperiness and
 density, gas rising and spreading, fire (particles, recolouring, spreading to solids,
 burning out), temperature reactions and both kinds of interaction. A solid border
 keeps every read inside the grid (the reference reads raw neighbours there); worlds
@@ -23,6 +24,7 @@ CUSTOM = [
     ("PIN_GAS", 4, 1, 0.5, 3, 0xFF9090FF, 0, 0, 0, 0),
     ("PIN_ROCK", 1, 1, 50.0, 0, 0xFF303030, 0, 0, 0, 0),
 ]
+SOUP, Q_DEFAULT = 3, 131072
 
 
 def setup_materials(o):
@@ -35,7 +37,7 @@ def setup_materials(o):
         assert mid >= 0
         assert o.set_factory(mid, base, sh, lo, mod, temp) == 0
         ids[name] = mid
-    for name in ("GENERIC_AIR", "GENERIC_SOLID", "GENERIC_SAND", "GENERIC_GAS", "FIRE", "STONE"):
+    for name in ("GENERIC_AIR", "GENERIC_SOLID", "GENERIC_SAND", "GENERIC_GAS", "FIRE", "STONE", "WATER", "LAVA"):
         ids[name] = o.find(name)
     a, b, c = ids["PIN_SAND_A"], ids["PIN_SAND_B"], ids["PIN_SAND_C"]
     assert o.set_reaction(a, REACT_ABOVE, 200, b) == 0
@@ -61,6 +63,9 @@ def scene(ids, w, h, seed, kind):
         pal = [ids["PIN_SAND_A"], ids["PIN_SAND_B"], ids["PIN_SAND_C"], ids["GENERIC_SAND"], ids["STONE"],
                ids["PIN_ROCK"]]
         p = np.array([0.16, 0.12, 0.08, 0.16, 0.04, 0.04])
+    elif kind == "liquid":
+        pal = [ids["WATER"], ids["LAVA"], ids["GENERIC_SAND"], ids["GENERIC_GAS"], ids["STONE"]]
+        p = np.array([0.25, 0.05, 0.2, 0.1, 0.1])
     elif kind == "gas":
         pal = [ids["GENERIC_GAS"], ids["PIN_GAS"], ids["GENERIC_SAND"], ids["PIN_ROCK"]]
         p = np.array([0.25, 0.2, 0.1, 0.05])
@@ -82,8 +87,10 @@ def scene(ids, w, h, seed, kind):
     temp = rng.integers(-400, 1400, (h, w)).astype(np.int32)
     temp[mid == air] = 0
     flags = np.where(rng.random((h, w)) < 0.3, 0x80, 0).astype(np.uint8)
-    return {"id": mid.astype(np.uint16), "colour": colour, "scalar": temp, "flags": flags,
-            "diff": np.zeros((h, w), np.int32)}
+    soup = np.isin(mid, [ids["WATER"], ids["LAVA"]])
+    # liquids at the MaterialInstance default amount, their temperature beside it
+    return {"id": mid.astype(np.uint16), "colour": colour, "scalar": np.where(soup, Q_DEFAULT, temp).astype(np.int32),
+            "flags": flags, "diff": np.zeros((h, w), np.int32), "temperature": temp.astype(np.int16)}
 
 
 # (w, h, seed, kind, cell_iter, ticks)
