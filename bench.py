@@ -18,6 +18,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -57,7 +58,9 @@ class Clocks:
     def __init__(self, index):
         self.index = index
         self.p = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_%d.csv" % os.getpid())
+        # the raw samples go to FSE_CLOCKS_DIR (a folder to keep them in) or the temp dir
+        folder = os.environ.get("FSE_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(folder, "clocks_%d.csv" % os.getpid())
 
     def start(self):
         try:
