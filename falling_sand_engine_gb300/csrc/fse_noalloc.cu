@@ -28,7 +28,7 @@ using namespace fse;
 namespace {
 
 // limits of the allocation-free tick
-constexpr int NA_MAX_SLOTS = 4096;      // chunks per colour (e.g. 8192 x 8192 cells at chunk 128)
+constexpr int NA_MAX_SLOTS = 4096;      // chunks per colour (16384 x 16384 cells at chunk 128, 8192 x 8192 at 64)
 constexpr int NA_MAX_ITER = 8;          // cell_iter
 constexpr int NA_MAX_SPAWNS = 65536;    // particles spawned by one tick
 constexpr int NA_CP = NA_MAX_ITER * 4 * NA_MAX_SLOTS + 1;
@@ -43,6 +43,8 @@ constexpr size_t OFF_CPC = (OFF_ITEMS + 4 * NA_MAX_SLOTS * 4 + 255) & ~(size_t)2
 constexpr size_t OFF_CPB = (OFF_CPC + NA_CP * 4 + 255) & ~(size_t)255;                // cp_base
 constexpr size_t OFF_STAGE = (OFF_CPB + NA_CP * 4 + 255) & ~(size_t)255;              // SpawnRec
 constexpr size_t NA_BYTES = OFF_STAGE + (size_t)NA_MAX_SPAWNS * sizeof(SpawnRec);
+static_assert(sizeof(WorldDev) <= OFF_CTR - OFF_DESC, "the world descriptor overlaps the counters");
+static_assert(16 * sizeof(int32_t) <= OFF_MT - OFF_CTR, "the counters overlap the material table");
 
 }  // namespace
 
@@ -168,7 +170,11 @@ extern "C" int fse_tick_noalloc(uint16_t *id, uint32_t *colour, int32_t *scalar,
     }
 
     // everything that must start at zero is cleared on every call: the counters
-    // (spawn count, output count, error bits; the tick is the caller's) and ledger
+    // (spawn count, output count, error bits; the tick is the caller's), the ledger
+    // and the per-chunk-pass spawn counts. The colour pass writes a count only for
+    // the chunk slots a colour has, while the spawn scan sums max_slots of them per
+    // colour, so counts left by an earlier call on a world of another shape would
+    // otherwise shift this call's spawn order.
     int32_t c16[16] = {0};
     c16[6] = (int32_t)tick;
     const MatTable &mt = host_table();
@@ -176,6 +182,8 @@ extern "C" int fse_tick_noalloc(uint16_t *id, uint32_t *colour, int32_t *scalar,
         cudaMemcpyAsync(base + OFF_CTR, c16, sizeof(c16), cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaMemcpyAsync(base + OFF_MT, &mt, sizeof(MatTable), cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaMemsetAsync(base + OFF_LED, 0, LED_ROWS * MAXMAT * 8, s) != cudaSuccess ||
+        cudaMemsetAsync(base + OFF_CPC, 0, ((size_t)cell_iter * 4 * max_slots + 1) * sizeof(int32_t), s) !=
+            cudaSuccess ||
         cudaMemcpyAsync(base + OFF_ITEMS, items, sizeof(items), cudaMemcpyHostToDevice, s) != cudaSuccess)
         return FSE_E_CUDA;
 

@@ -374,7 +374,7 @@ int fse_world_islands(fse_world *world, int max_cells, int remove, fse_island *o
  *
  * Scratch: one fixed device array of about 4 MB inside the library, held by every
  * GPU that loads it until the process exits. Limits: at most 4096 chunks per
- * colour (e.g. 8192 x 8192 cells at chunk 128), cell_iter <= 8, at most 65536
+ * colour (16384 x 16384 cells at chunk 128, 8192 x 8192 at chunk 64), cell_iter <= 8, at most 65536
  * particles spawned per tick; larger requests return FSE_E_INVAL. The first call
  * on a device looks the array up (cudaGetSymbolAddress) and should be made before
  * any stream capture. Every call shares the array: calls that overlap on the GPU

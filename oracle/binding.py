@@ -16,7 +16,12 @@ REF_CELLS_PATH = os.path.join(HERE, "_ref", "libref_cells.so")
 REF_RENDER_PATH = os.path.join(HERE, "_ref", "libref_render.so")
 REF_OBJECTS_PATH = os.path.join(HERE, "_ref", "libref_objects.so")
 REF_TICK_PATH = os.path.join(HERE, "_ref", "libref_tick.so")
-REFERENCE_WORLD_CPP = "/root/reference/source/engine/world.cpp"
+# The reference tree that oracle/Makefile's `ref` recipes extract from: the
+# FSE_REFERENCE_ROOT environment variable, else the tree's mount point in the build
+# container. Where it is absent, the pieces extracted before (oracle/_ref/*.inc)
+# are compiled instead, or the reference-made fixtures under tests/golden are used.
+REFERENCE_ROOT = os.environ.get("FSE_REFERENCE_ROOT") or "/root/reference"
+REFERENCE_WORLD_CPP = os.path.join(REFERENCE_ROOT, "source", "engine", "world.cpp")
 
 PARTICLE_DTYPE = np.dtype(
     [
@@ -43,6 +48,11 @@ ISLAND_DTYPE = np.dtype([("root", "<i4"), ("cells", "<i4"), ("min_x", "<i4"), ("
 ORDER_SEQ = 0
 ORDER_PART = 1
 
+
+
+def make_ref():
+    """Run oracle/Makefile's `ref` target on REFERENCE_ROOT."""
+    subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + REFERENCE_ROOT], check=True)
 
 def build_oracle(force=False):
     """Compile the oracle with its Makefile (gcc, no reference sources)."""
@@ -392,7 +402,7 @@ def build_reference_temperature(force=False):
     if force or not os.path.exists(REF_TEMPERATURE_PATH) or os.path.getmtime(REF_TEMPERATURE_PATH) < max(
         os.path.getmtime(os.path.join(HERE, f)) for f in ("ref_temperature.cpp", "Makefile")
     ):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        make_ref()
     return REF_TEMPERATURE_PATH
 
 
@@ -448,7 +458,7 @@ def build_reference_lz4(force=False):
                             "-o", REF_LZ4_PATH, src], check=True)
         return REF_LZ4_PATH
     if force or not os.path.exists(REF_LZ4_PATH):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        make_ref()
     return REF_LZ4_PATH
 
 
@@ -487,7 +497,7 @@ def build_reference_cells(force=False):
         return None
     if force or not os.path.exists(REF_CELLS_PATH) or os.path.getmtime(REF_CELLS_PATH) < os.path.getmtime(
             os.path.join(HERE, "ref_particles.cpp")):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        make_ref()
     return REF_CELLS_PATH
 
 
@@ -528,7 +538,7 @@ def build_reference_tick(force=False):
     if fresh:
         return REF_TICK_PATH
     if os.path.exists(REFERENCE_WORLD_CPP):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        make_ref()
         return REF_TICK_PATH
     incs = [os.path.join(HERE, "_ref", "tick_%s.inc" % k) for k in TICK_INC]
     if not all(os.path.exists(p) and os.path.getsize(p) > 0 for p in incs):
@@ -614,7 +624,7 @@ def build_reference_render(force=False):
         return _build_from_inc(REF_RENDER_PATH, "ref_render.cpp", ["dirty_loop.inc"], "c++20")
     if force or not os.path.exists(REF_RENDER_PATH) or os.path.getmtime(REF_RENDER_PATH) < os.path.getmtime(
             os.path.join(HERE, "ref_render.cpp")):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        make_ref()
     return REF_RENDER_PATH
 
 
@@ -651,7 +661,7 @@ def build_reference_physics(force=False):
                                ["physics_check.inc", "physics_flood.inc", "physics_gettile.inc"], "c++20")
     if force or not os.path.exists(REF_PHYSICS_PATH) or os.path.getmtime(REF_PHYSICS_PATH) < os.path.getmtime(
             os.path.join(HERE, "ref_physics.cpp")):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        make_ref()
     return REF_PHYSICS_PATH
 
 
@@ -679,7 +689,7 @@ def build_reference_objects(force=False):
         return None
     if force or not os.path.exists(REF_OBJECTS_PATH) or os.path.getmtime(REF_OBJECTS_PATH) < os.path.getmtime(
             os.path.join(HERE, "ref_objects.cpp")):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        make_ref()
     return REF_OBJECTS_PATH
 
 

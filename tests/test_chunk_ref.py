@@ -17,13 +17,12 @@ from pack_cases import sample_world
 
 
 def _lib():
-    from oracle.binding import HERE, REFERENCE_WORLD_CPP
+    from oracle.binding import HERE, REFERENCE_WORLD_CPP, make_ref
 
     if not os.path.exists(REFERENCE_WORLD_CPP):
         pytest.skip("reference tree absent")
-    import subprocess
 
-    subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    make_ref()
     lib = C.CDLL(os.path.join(HERE, "_ref", "libref_chunk.so"))
     lib.ref_chunk_write.argtypes = [C.c_char_p, C.c_int] + [C.c_void_p] * 3
     lib.ref_chunk_read.argtypes = [C.c_char_p] + [C.c_void_p] * 4

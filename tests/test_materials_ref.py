@@ -24,13 +24,12 @@ def _ref_ds():
 
 
 def _ref_table():
-    from oracle.binding import HERE, REFERENCE_WORLD_CPP
+    from oracle.binding import HERE, REFERENCE_WORLD_CPP, make_ref
 
     if not os.path.exists(REFERENCE_WORLD_CPP):
         pytest.skip("reference tree absent")
-    import subprocess
 
-    subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    make_ref()
     lib = C.CDLL(os.path.join(HERE, "_ref", "libref_materials.so"))
     out = np.zeros(64 * 10, np.int32)
     names = C.create_string_buffer(64 * 48)
