@@ -1,16 +1,21 @@
 """Benchmark of the GB300 falling-sand world tick.
 
-Default workload (the metric's single-GPU configuration): one 4096x2048 world with
-the standard material mix plus 1M free particles, plain per-world launch; a step is
-world::tick() + world::tickCells(). Prints one JSON line.
+Default workload (the headline metric: Gcell-updates/s and HBM roofline fraction,
+batched vs per-world launch, tick latency percentiles): 256 worlds of uneven sizes
+(sides uniform in {128, ..., 2048}), the standard material mix, batched launches
+replayed from 32-tick CUDA graphs with the autotuned launch shape, against the same
+worlds stepped through 256 plain per-world launches; a step is world::tick() +
+world::tickCells() of every world. The single 4096x2048 world with 1M free
+particles (plain per-world launch) is reported beside it under "config1". Prints
+one JSON line.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl fse|reference]
-                  [--workload 1|0|2|3|4]
+                  [--workload 2|0|1|3|4]
 
---impl reference times the CPU restatement of the reference tick (reference chunk
-order, all host threads) on the same workload. Workloads 0, 2, 3, 4 are the other
-configurations (512^2 world; 256 uneven worlds batched vs per-world launches;
-16384^2 world with OBJECT boxes; continuous-batching server) for reporting.
+--impl reference times the reference's own world::tick + world::tickCells
+(compiled from its extracted sources, all host threads) on a bounded sample of the
+same workload. Workloads 0, 1, 3, 4 alone: the 512^2 world; the 4096x2048 world
+with particles; the 16384^2 world with OBJECT boxes; the continuous-batching server.
 """
 import argparse
 import json
@@ -691,10 +696,41 @@ def config2_sizes(n, seed):
     return [(int(rng.choice(sides)), int(rng.choice(sides))) for _ in range(n)]
 
 
+CONFIG2_WORLDS = 256
+CONFIG2_SEED = 1234
+CONFIG2_WORKLOAD = ("config2: 256 worlds, sides uniform in {128, 192, ..., 2048}, per-world seeds 1234+i, mix (30% "
+                    "sand, 20% water, 10% gas, 15% rock, 25% air in the top 60%, 8 rock rows); batched launches "
+                    "replayed from 32-tick CUDA graphs with the autotuned launch shape, against 256 plain per-world "
+                    "launches")
+# the worlds of config 2 the CPU legs time (every 32nd: 8 worlds, sizes spread over the range)
+CONFIG2_CPU_SAMPLE = tuple(range(0, CONFIG2_WORLDS, 32))
+
+
+def worlds_digest(worlds, fse):
+    """blake2b over every world's planes (the pending diff only where the cell is a
+    liquid, the only place it means anything) and particle list, in world order."""
+    import hashlib
+
+    soup = np.array([fse.material_get(i)[0] == fse.SOUP for i in range(fse.material_count())])
+    h = hashlib.blake2b(digest_size=16)
+    for w in worlds:
+        st = w.state()
+        for k in ("id", "colour", "scalar", "flags"):
+            h.update(np.ascontiguousarray(st[k]).tobytes())
+        h.update(np.where(soup[st["id"]], st["diff"], 0).astype(np.int32).tobytes())
+        h.update(w.particles().tobytes())
+    return h.hexdigest()
+
+
 def bench_config2(args, rank, local_rank, world_size):
     """256 worlds of uneven sizes: batched launches replayed from 32-tick CUDA graphs
     with the autotuned launch shape, against the same worlds stepped one by one
-    through their plain per-world launches (each world on its own stream)."""
+    through their plain per-world launches (each world on its own stream). Both arms
+    run the same warm-up and timed steps from the same generated worlds and must end
+    in the same state (a digest of every plane and particle of every world). The
+    colour-pass launches and the ticks inside the graphs are timed with CUDA events
+    recorded by the graphs themselves (the roofline's launch time, the tick latency
+    percentiles)."""
     import torch
 
     import falling_sand_engine_gb300 as fse
@@ -705,7 +741,7 @@ def bench_config2(args, rank, local_rank, world_size):
     fse.PushMaterials()
     # the 256 worlds are split across ranks by cell count (no data exchange); one
     # rank ticks them all
-    all_sizes = config2_sizes(256, 1234)
+    all_sizes = config2_sizes(CONFIG2_WORLDS, CONFIG2_SEED)
     mine = shard_worlds([w * h for w, h in all_sizes], world_size)[rank]
     sizes = [all_sizes[i] for i in mine]
     cells = sum(w * h for w, h in sizes)
@@ -714,8 +750,8 @@ def bench_config2(args, rank, local_rank, world_size):
     def make():
         ws = []
         for i, (w, h) in zip(mine, sizes):
-            wd = fse.World(w, h, chunk_size=128, cell_iter=3, seed=1234 + i)
-            wd.generate(fse.GEN_MIX, 1234 + i)
+            wd = fse.World(w, h, chunk_size=128, cell_iter=3, seed=CONFIG2_SEED + i)
+            wd.generate(fse.GEN_MIX, CONFIG2_SEED + i)
             ws.append(wd)
         for wd in ws:
             wd.sync()
@@ -726,6 +762,8 @@ def bench_config2(args, rank, local_rank, world_size):
     choice = batch.autotune()
     bstream = torch.cuda.ExternalStream(batch.stream)
     batch.step(args.warmup)
+    batch.timing(True)
+    batch.prepare_graphs(args.steps, 32)
     batch.sync()
     clocks = Clocks(local_rank)
     barrier(world_size)
@@ -733,16 +771,25 @@ def bench_config2(args, rank, local_rank, world_size):
     l0 = fse.launch_counter()
     e0, e1 = _ev(torch), _ev(torch)
     clocks.start()
+    t0 = time.perf_counter()
     e0.record(bstream)
     batch.step(args.steps, graph_ticks=32)
     e1.record(bstream)
     batch.sync()
     torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
     clk = clocks.stop()
     launches = fse.launch_counter() - l0
+    pass_ms, pass_n, tick_ms = batch.timing(False)
     b_ms = max_over_ranks(e0.elapsed_time(e1), world_size)
     value = total_cells * args.steps / (b_ms / 1e3) / 1e9
-    digest_b = sum(int(w.state()["id"].astype(np.int64).sum()) for w in worlds[:8])
+    digest_b = worlds_digest(worlds, fse)
+
+    # end to end through the C ABI with host buffers: every step uploads each
+    # world's planes from pinned host memory, runs one batched step and reads the
+    # planes back
+    e2e = e2e_worlds(worlds, lambda: batch.step(1), torch, cells, world_size,
+                     "fse_world_upload (every world) + fse_batch_step + fse_world_download (every world)")
     batch.close()
     for w in worlds:
         w.close()
@@ -752,7 +799,9 @@ def bench_config2(args, rank, local_rank, world_size):
     worlds = make()
     streams = [torch.cuda.ExternalStream(w.stream) for w in worlds]
     for w in worlds:
-        w.step(args.warmup)
+        w.enqueue(args.warmup, particles=True)
+    for w in worlds:
+        w.sync()
     torch.cuda.synchronize()
     main = torch.cuda.current_stream()
     p0, p1 = _ev(torch), _ev(torch)
@@ -772,23 +821,136 @@ def bench_config2(args, rank, local_rank, world_size):
         w.sync()
     p_ms = max_over_ranks(p0.elapsed_time(p1), world_size)
     per_world = total_cells * args.steps / (p_ms / 1e3) / 1e9
-    digest_p = sum(int(w.state()["id"].astype(np.int64).sum()) for w in worlds[:8])
+    digest_p = worlds_digest(worlds, fse)
     for w in worlds:
         w.close()
+
     peak, peak_kind = peaks()
-    return _common(args, world_size, value, "Gcell/s", b_ms / args.steps,
-                   "config2: 256 worlds, sides uniform in {128, 192, ..., 2048}, per-world seeds, mix; batched "
-                   "launches from 32-tick CUDA graphs, autotuned launch shape",
-                   {"worlds": 256, "cells": total_cells, "worlds_this_rank": len(mine), "chunk": 128,
-                    "cell_iter": 3, "autotune": choice,
-                    "l2": "inputs larger than L2 (%.2f GB of grid state)" % (cells * 15 / 1e9),
-                    "per_world_launch": {"value": round(per_world, 4), "ms_per_step": round(p_ms / args.steps, 4)},
-                    "batched_over_per_world": round(value / per_world, 3),
-                    "same_result": digest_b == digest_p,
-                    "hbm_frac_of_tick": round(value * 1e9 * BYTES_PER_CELL_UPDATE / world_size / (peak * 1e9), 5),
-                    "peak_kind": peak_kind,
-                    "parallelism": "worlds sharded across %d GPUs by cell count, no collective" % world_size},
-                   launches, clk, scaling="strong")
+    avg_pass_s = (pass_ms / max(pass_n, 1)) / 1e3
+    units_per_launch = cells / (3 * 4)  # one launch = one colour x one iteration over every world
+    achieved = BYTES_PER_CELL_UPDATE * units_per_launch / avg_pass_s / 1e9
+    roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": profile_traffic("colour_pass_config2"),
+            "kernel": "k_colour_pass<2>", "peak_kind": peak_kind,
+            "launch_ms_avg": round(pass_ms / max(pass_n, 1), 4), "launches_timed": int(pass_n),
+            "units": "22 B per cell-update; one launch = one colour of one iteration over all %d worlds "
+                     "(%d cells / 12)" % (len(mine), cells),
+            "tick_frac": round(value * 1e9 * BYTES_PER_CELL_UPDATE / world_size / (peak * 1e9), 5)}
+    lat = {"p50": round(float(np.percentile(tick_ms, 50)), 3), "p99": round(float(np.percentile(tick_ms, 99)), 3),
+           "max": round(float(tick_ms.max()), 3), "ticks": int(len(tick_ms)),
+           "unit": "ms per batched tick (all worlds: tick + tickCells), CUDA events recorded inside the graphs"} \
+        if len(tick_ms) else None
+    cpu = None
+    if rank == 0 and world_size == 1 and not args.no_cpu:
+        cpu = cpu_baseline_config2(all_sizes, budget_s=20.0)
+    sub1 = None
+    if not args.no_config1:
+        sub1 = bench_config1(args, rank, local_rank, world_size)
+    out = _common(args, world_size, value, "Gcell/s", b_ms / args.steps, CONFIG2_WORKLOAD,
+                  {"worlds": CONFIG2_WORLDS, "cells": total_cells, "worlds_this_rank": len(mine), "chunk": 128,
+                   "cell_iter": 3, "autotune": choice, "graph_ticks": 32,
+                   "l2": "inputs larger than L2 (%.2f GB of grid state)" % (cells * 15 / 1e9),
+                   "parallelism": "worlds sharded across %d GPUs by cell count, no collective" % world_size
+                   if world_size > 1 else "single GPU"},
+                  launches, clk, e2e=e2e, cpu=cpu, scaling="strong")
+    out.update({
+        "roofline": roof, "tick_latency": lat, "wall_s": round(wall, 3),
+        "per_world_launch": {"value": round(per_world, 4), "unit": "Gcell/s",
+                             "ms_per_step": round(p_ms / args.steps, 4),
+                             "how": "each world's plain fse_world_enqueue on its own stream, same steps"},
+        "batched_over_per_world": round(value / per_world, 3),
+        "same_result": {"equal": digest_b == digest_p, "digest": digest_b,
+                        "what": "blake2b of every world's planes and particle list after warm-up + timed steps"},
+        "config1": sub1,
+    })
+    return out
+
+
+def e2e_worlds(worlds, step, torch, cells, world_size, path, steps=3):
+    """The metric end to end through the C ABI: every step uploads each world's
+    planes from pinned host memory, runs `step`, and reads every plane back."""
+    pinned = []
+    for w in worlds:
+        st = w.state()
+        host = {}
+        for k, v in st.items():
+            t = torch.empty(v.size, dtype={np.uint16: torch.int16, np.uint32: torch.int32, np.int32: torch.int32,
+                                           np.uint8: torch.uint8}[v.dtype.type], pin_memory=True)
+            a = t.numpy().view(v.dtype).reshape(v.shape)
+            a[...] = v
+            host[k] = (t, a)
+        pinned.append(host)
+    bi = sum(a.nbytes for host in pinned for (t, a) in host.values())
+    for w in worlds:
+        w.sync()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for w, host in zip(worlds, pinned):
+            w.upload({k: a for k, (t, a) in host.items()})
+        step()
+        for w, host in zip(worlds, pinned):
+            w.state(out={k: a for k, (t, a) in host.items()})
+    dt = max_over_ranks(time.perf_counter() - t0, world_size)
+    return {"value": round(world_size * cells * steps / dt / 1e9, 4), "unit": "Gcell/s",
+            "h2d_bytes_per_step": int(bi), "d2h_bytes_per_step": int(bi), "steps": steps, "path": path}
+
+
+def reference_timing_worlds(sizes, sample, steps, warm, budget_s):
+    """The reference's own tick + tickCells, one world after another (each world
+    ticked by its own pool of one worker per host core, as the reference ticks its
+    one world), on the sampled worlds of a batch workload: (Gcell/s, steps per world,
+    threads, cells sampled), or None when it cannot be compiled here."""
+    from oracle import Oracle, OracleWorld
+    from oracle.binding import build_reference_tick, reference_world_bench
+
+    try:
+        lib = build_reference_tick()
+    except Exception:  # noqa: BLE001 - no compiler or sources: the port is timed instead
+        lib = None
+    if lib is None:
+        return None
+    o = Oracle()
+    o.reset_materials()
+    stone = o.find("STONE")
+    cores = os.cpu_count() or 1
+    secs, work, n_min, sampled = 0.0, 0, None, 0
+    for i in sample:
+        W, H = sizes[i]
+        ow = OracleWorld(W, H, 128, 3, CONFIG2_SEED + i)
+        ow.generate(0, CONFIG2_SEED + i)
+        st = ow.state()
+        # The reference's tick walks whole 128 x 128 chunks (world.cpp:1078-1087) and
+        # its worlds are whole chunks; a world whose side is not a multiple of 128 is
+        # given to it padded with rock to the next chunk edge (cells that never move,
+        # as the library's out-of-world cells are solid), and the padded cells count
+        # as cell-updates of the reference.
+        W2, H2 = -(-W // 128) * 128, -(-H // 128) * 128
+        ids = np.full((H2, W2), stone, np.uint16)
+        cols = np.full((H2, W2), 0x808080, np.uint32)
+        temps = np.zeros((H2, W2), np.int32)
+        ids[:H, :W] = st["id"]
+        cols[:H, :W] = st["colour"]
+        temps[:H, :W] = ow.temperature()
+        s, n = reference_world_bench(lib, o, ids, cols, temps, _np_particles(0, W2, H2, CONFIG2_SEED + i), 3,
+                                     CONFIG2_SEED + i, cores, warm, steps, budget_s / len(sample))
+        secs += s
+        work += W2 * H2 * n
+        sampled += W2 * H2
+        n_min = n if n_min is None else min(n_min, n)
+    return work / secs / 1e9, n_min, cores, sampled
+
+
+def cpu_baseline_config2(sizes, budget_s=20.0):
+    """The reference's own tick + tickCells on the host cores, on a bounded sample of
+    the batch: every 32nd world, one step each after one warm-up step."""
+    ref = reference_timing_worlds(sizes, CONFIG2_CPU_SAMPLE, 1, 1, budget_s)
+    if ref is None:
+        return None
+    value, n, cores, sampled = ref
+    return {"value": round(value, 6), "unit": "Gcell/s", "cores": cores, "kind": "reference",
+            "sample": "worlds %s of the 256 (%d cells, padded with rock to whole 128-cell chunks), %d step(s) "
+                      "each after 1 warm-up step, one world after another; " % (list(CONFIG2_CPU_SAMPLE), sampled, n)
+                      + REF_NOTE % cores}
 
 
 def bench_config3(args, rank, local_rank, world_size):
@@ -1028,6 +1190,8 @@ def reference_timing(W, H, seed, steps, warm, budget_s):
 def reference_arm(args, rank, world_size):
     if rank != 0:
         return None
+    if args.workload == 2:
+        return reference_arm_config2(args, world_size)
     from oracle import Oracle, OracleWorld
 
     W, H = 4096, 2048
@@ -1084,6 +1248,43 @@ def reference_arm(args, rank, world_size):
     }
 
 
+# the worlds the reference arm times on the batch workload (every 16th: 16 worlds)
+CONFIG2_REF_SAMPLE = tuple(range(0, CONFIG2_WORLDS, 16))
+
+
+def reference_arm_config2(args, world_size):
+    """The reference's own world::tick + world::tickCells on the batch workload: the
+    same world sizes, seeds and generator (the oracle's generator, equal to the
+    library's cell for cell), every 16th world, each world ticked by its own pool of
+    one worker per host core, one world after another (the reference engine ticks
+    its one world this way). At most 3 warm-up steps and REF_BUDGET_S seconds of
+    timed steps are spread over the sampled worlds."""
+    sizes = config2_sizes(CONFIG2_WORLDS, CONFIG2_SEED)
+    warm = min(args.warmup, 3)
+    ref = reference_timing_worlds(sizes, CONFIG2_REF_SAMPLE, args.steps, warm, REF_BUDGET_S)
+    if ref is None:
+        return {"impl": "reference", "unavailable": "the reference's tick sources are not present to compile"}
+    value, n, cores, sampled = ref
+    sample = ("worlds %s of the 256 (%d cells, padded with rock to whole 128-cell chunks), at least %d timed step(s) each (tick + tickCells) after %d "
+              "warm-up (%d requested; the timed region is capped at %.0f s over all sampled worlds)"
+              % (list(CONFIG2_REF_SAMPLE), sampled, n, warm, args.steps, REF_BUDGET_S))
+    return {
+        "impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": "Gcell/s", "n_gpus": world_size,
+        "steps": n, "warmup": warm, "ms_per_step": round(sampled / (value * 1e9) * 1e3, 3),
+        "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "int32+f32",
+        "data": "synthetic",
+        "config": {"workload": CONFIG2_WORKLOAD, "worlds": CONFIG2_WORLDS, "chunk": 128, "cell_iter": 3,
+                   "same_config": True,
+                   "same_inputs": "world sizes and seeds of config2_sizes(256, 1234); cells from the oracle's "
+                                  "generator, which equals the library's GEN_MIX bit for bit (tests/test_gpu_parity.py "
+                                  "and smoke())",
+                   "impl_note": REF_NOTE % cores},
+        "cpu_baseline": {"value": round(value, 6), "unit": "Gcell/s", "cores": cores, "kind": "reference",
+                         "sample": sample},
+        "e2e": {"value": round(value, 6), "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
 def _np_particles(n, w, h, seed):
     from oracle import PARTICLE_DTYPE
 
@@ -1104,11 +1305,13 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None,
-                    help="timed steps (default: the workload's tick count, 500 for the default workload)")
+                    help="timed steps (default: the workload's tick count, 200 for the default batch workload)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="fse", choices=["fse", "reference"])
-    ap.add_argument("--workload", type=int, default=1, choices=[0, 1, 2, 3, 4])
+    ap.add_argument("--workload", type=int, default=2, choices=[0, 1, 2, 3, 4])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-config1", action="store_true",
+                    help="batch workload: skip the 4096x2048 single-world line reported beside it")
     ap.add_argument("--only", default=None, choices=["render", "temperature", "pack", "reference_order"],
                     help="run only one side measurement of the 4096x2048 workload (for profiling), print its dict")
     args = ap.parse_args()

@@ -465,6 +465,10 @@ class Batch:
         else:
             check(self.lib.fse_batch_step(self.h, n), "batch_step")
 
+    def prepare_graphs(self, n, graph_ticks=32):
+        """Capture the graphs step(n, graph_ticks) will replay, without running them."""
+        check(self.lib.fse_batch_prepare_graphs(self.h, n, graph_ticks), "batch_prepare_graphs")
+
     def autotune(self):
         out = np.zeros(4, np.int32)
         check(self.lib.fse_batch_autotune(self.h, ptr(out)), "batch_autotune")
@@ -476,6 +480,16 @@ class Batch:
 
     def sync(self):
         check(self.lib.fse_batch_sync(self.h), "batch_sync")
+
+    def timing(self, enable, cap=1 << 16):
+        """Start (True) or stop (False) CUDA-event timing of the batch's colour-pass
+        launches and ticks; returns what was accumulated since the last start:
+        (colour-pass ms, colour-pass launches, per-tick ms array)."""
+        ms, n, nt = C.c_double(), C.c_int64(), C.c_int()
+        out = np.zeros(cap, np.float32)
+        check(self.lib.fse_batch_timing(self.h, 1 if enable else 0, C.byref(ms), C.byref(n), ptr(out), cap,
+                                        C.byref(nt)), "batch_timing")
+        return ms.value, n.value, out[: min(cap, nt.value)].copy()
 
     @property
     def stream(self):

@@ -135,6 +135,8 @@ SIGNATURES = {
     "fse_batch_set_launch": (_i, [_vp, _i, _i]),
     "fse_batch_sync": (_i, [_vp]),
     "fse_batch_stream": (_vp, [_vp]),
+    "fse_batch_prepare_graphs": (_i, [_vp, _i, _i]),
+    "fse_batch_timing": (_i, [_vp, _i, C.POINTER(_d), C.POINTER(_i64), _vp, _i, C.POINTER(_i)]),
     "fse_server_create": (_i, [_i64, _i, _pp]),
     "fse_server_destroy": (_i, [_vp]),
     "fse_server_add_world": (_i, [_vp, _i, _i, C.POINTER(FseConfig), _i, _u32, C.POINTER(_i)]),

@@ -365,6 +365,28 @@ void PassTimer::drain() {
         pool.push_back(pr.second);
     }
     pending.clear();
+    for (auto &g : tick_groups) {
+        for (size_t i = 0; i + 1 < g.size(); i++) {
+            float t = 0.f;
+            if (cudaEventElapsedTime(&t, g[i], g[i + 1]) == cudaSuccess) tick_ms.push_back(t);
+        }
+        for (cudaEvent_t e : g) pool.push_back(e);
+    }
+    tick_groups.clear();
+}
+void PassTimer::accumulate(const std::vector<std::pair<cudaEvent_t, cudaEvent_t>> &pairs,
+                           const std::vector<cudaEvent_t> &ticks) {
+    for (auto &pr : pairs) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, pr.first, pr.second) == cudaSuccess) {
+            ms += t;
+            launches++;
+        }
+    }
+    for (size_t i = 0; i + 1 < ticks.size(); i++) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, ticks[i], ticks[i + 1]) == cudaSuccess) tick_ms.push_back(t);
+    }
 }
 
 int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], const int n_items[4], int max_iter, int C,
@@ -377,13 +399,13 @@ int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], con
             if (timer) {
                 a = timer->get();
                 b = timer->get();
-                cudaEventRecord(a, s);
+                if (timer->record(a, s) != cudaSuccess) return FSE_E_CUDA;
             }
             cudaError_t e = launch_colour_pass(d_worlds, items[tk], n_items[tk], iter, tk, g_dev_mt, halo, C, threads,
                                                grid, s, temp_track, seq);
             if (e != cudaSuccess) return FSE_E_CUDA;
             if (timer) {
-                cudaEventRecord(b, s);
+                if (timer->record(b, s) != cudaSuccess) return FSE_E_CUDA;
                 timer->record_pair(a, b);
             }
             if (n_items[tk] > 0) count_launches(1);

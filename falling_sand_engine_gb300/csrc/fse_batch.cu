@@ -31,6 +31,16 @@ struct fse_batch {
     cudaStream_t stream = nullptr;
     std::map<int, cudaGraphExec_t> graphs;
     std::map<int, long long> graph_kernels;  // kernels one replay launches
+    // event timing (fse_batch_timing): colour-pass launches and tick boundaries;
+    // graphs captured while it is on carry the events as nodes and are kept apart
+    PassTimer *timer = nullptr;
+    struct GraphEvents {
+        std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pairs;
+        std::vector<cudaEvent_t> ticks;
+    };
+    std::map<int, cudaGraphExec_t> tgraphs;
+    std::map<int, GraphEvents> tgraph_events;
+    std::map<int, long long> tgraph_kernels;
 };
 
 namespace {
@@ -82,12 +92,37 @@ int batch_enqueue(fse_batch *b, int n) {
     if (rc) return rc;
     const int tt = temp_tiles_of(b->worlds);
     const bool tr = temp_track_of(b->worlds);
+    PassTimer *tm = b->timer;
+    std::vector<cudaEvent_t> ticks;  // tick boundaries: n + 1 events
+    auto boundary = [&]() -> int {
+        if (!tm) return FSE_OK;
+        cudaEvent_t e = tm->get();
+        ticks.push_back(e);
+        return tm->record(e, b->stream) == cudaSuccess ? FSE_OK : FSE_E_CUDA;
+    };
     for (int i = 0; i < n; i++) {
+        if ((rc = boundary())) return rc;
         rc = enqueue_step(b->d_table, (int)b->worlds.size(), b->items, b->n_items, b->max_iter, b->C, b->threads,
-                          b->grid, true, b->move_blocks, b->stage_blocks, b->stream, nullptr, tt, tr);
+                          b->grid, true, b->move_blocks, b->stage_blocks, b->stream, tm, tt, tr);
         if (rc) return rc;
     }
+    if (n > 0 && (rc = boundary())) return rc;
+    if (tm && !ticks.empty()) tm->tick_groups.push_back(ticks);
     return FSE_OK;
+}
+
+void drop_timed_graphs(fse_batch *b) {
+    for (auto &g : b->tgraphs) cudaGraphExecDestroy(g.second);
+    for (auto &g : b->tgraph_events) {
+        for (auto &pr : g.second.pairs) {
+            cudaEventDestroy(pr.first);
+            cudaEventDestroy(pr.second);
+        }
+        for (cudaEvent_t e : g.second.ticks) cudaEventDestroy(e);
+    }
+    b->tgraphs.clear();
+    b->tgraph_events.clear();
+    b->tgraph_kernels.clear();
 }
 
 int batch_sync(fse_batch *b) {
@@ -181,6 +216,12 @@ int fse_batch_destroy(fse_batch *b) {
     if (!b) return FSE_E_INVAL;
     if (b->stream) cudaStreamSynchronize(b->stream);
     for (auto &g : b->graphs) cudaGraphExecDestroy(g.second);
+    drop_timed_graphs(b);
+    if (b->timer) {
+        b->timer->drain();
+        for (cudaEvent_t e : b->timer->pool) cudaEventDestroy(e);
+        delete b->timer;
+    }
     if (b->d_table) cudaFree(b->d_table);
     for (int k = 0; k < 4; k++)
         if (b->items[k]) cudaFree(b->items[k]);
@@ -196,38 +237,112 @@ int fse_batch_step(fse_batch *b, int n) {
     return batch_sync(b);
 }
 
+}  // extern "C"
+
+// The graph of k steps for the batch's current timing mode, captured on first use.
+// With timing on, graphs carry event nodes and are kept apart from the plain ones.
+static int batch_graph(fse_batch *b, int k, cudaGraphExec_t *out) {
+    const bool timed = b->timer != nullptr;
+    auto &graphs = timed ? b->tgraphs : b->graphs;
+    auto &kernels = timed ? b->tgraph_kernels : b->graph_kernels;
+    auto it = graphs.find(k);
+    if (it != graphs.end()) {
+        *out = it->second;
+        return FSE_OK;
+    }
+    cudaGraph_t g;
+    cudaGraphExec_t ex;
+    // kernels are counted when a replay launches them, not at capture
+    const long long c0 = fse_launch_counter();
+    FSE_CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    if (timed) b->timer->capture = true;
+    int erc = batch_enqueue(b, k);
+    cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    const long long kn = fse_launch_counter() - c0;
+    count_launches(-kn);
+    if (timed) {
+        // the events recorded during capture belong to this graph from now on
+        fse_batch::GraphEvents ge;
+        ge.pairs.swap(b->timer->pending);
+        if (!b->timer->tick_groups.empty()) {
+            ge.ticks.swap(b->timer->tick_groups.back());
+            b->timer->tick_groups.pop_back();
+        }
+        b->timer->capture = false;
+        b->tgraph_events[k] = std::move(ge);
+    }
+    if (erc || e != cudaSuccess) return FSE_E_CUDA;
+    FSE_CUDA_TRY(cudaGraphInstantiate(&ex, g, 0));
+    cudaGraphDestroy(g);
+    graphs[k] = ex;
+    kernels[k] = kn;
+    *out = ex;
+    return FSE_OK;
+}
+
+extern "C" {
+
 int fse_batch_step_graph(fse_batch *b, int n, int graph_ticks) {
     if (!b || n < 0) return FSE_E_INVAL;
     if (graph_ticks <= 0) graph_ticks = 32;
     int rc = ensure_materials_pushed();
     if (rc) return rc;
+    const bool timed = b->timer != nullptr;
     int done = 0;
     while (done < n) {
-        int k = std::min(graph_ticks, n - done);
-        auto it = b->graphs.find(k);
+        const int k = std::min(graph_ticks, n - done);
         cudaGraphExec_t ex;
-        if (it == b->graphs.end()) {
-            cudaGraph_t g;
-            // kernels are counted when a replay launches them, not at capture
-            const long long c0 = fse_launch_counter();
-            FSE_CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-            int erc = batch_enqueue(b, k);
-            cudaError_t e = cudaStreamEndCapture(b->stream, &g);
-            const long long kn = fse_launch_counter() - c0;
-            count_launches(-kn);
-            if (erc || e != cudaSuccess) return FSE_E_CUDA;
-            FSE_CUDA_TRY(cudaGraphInstantiate(&ex, g, 0));
-            cudaGraphDestroy(g);
-            b->graphs[k] = ex;
-            b->graph_kernels[k] = kn;
-        } else {
-            ex = it->second;
-        }
+        if ((rc = batch_graph(b, k, &ex))) return rc;
         FSE_CUDA_TRY(cudaGraphLaunch(ex, b->stream));
-        count_launches(b->graph_kernels[k]);
+        count_launches(timed ? b->tgraph_kernels[k] : b->graph_kernels[k]);
+        if (timed) {
+            // each replay is read back before the next one reuses its events
+            const fse_batch::GraphEvents &ge = b->tgraph_events[k];
+            if (!ge.ticks.empty()) FSE_CUDA_TRY(cudaEventSynchronize(ge.ticks.back()));
+            b->timer->accumulate(ge.pairs, ge.ticks);
+        }
         done += k;
     }
     return batch_sync(b);
+}
+
+int fse_batch_prepare_graphs(fse_batch *b, int n, int graph_ticks) {
+    if (!b || n < 0) return FSE_E_INVAL;
+    if (graph_ticks <= 0) graph_ticks = 32;
+    int rc = ensure_materials_pushed();
+    if (rc) return rc;
+    for (int done = 0; done < n;) {
+        const int k = std::min(graph_ticks, n - done);
+        cudaGraphExec_t ex;
+        if ((rc = batch_graph(b, k, &ex))) return rc;
+        done += k;
+    }
+    return FSE_OK;
+}
+
+int fse_batch_timing(fse_batch *b, int enable, double *out_pass_ms, int64_t *out_pass_launches, float *tick_ms,
+                     int cap, int *out_ticks) {
+    if (!b || cap < 0 || (cap > 0 && !tick_ms)) return FSE_E_INVAL;
+    FSE_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    PassTimer *tm = b->timer;
+    if (tm) tm->drain();
+    if (out_pass_ms) *out_pass_ms = tm ? tm->ms : 0.0;
+    if (out_pass_launches) *out_pass_launches = tm ? tm->launches : 0;
+    const int nt = tm ? (int)tm->tick_ms.size() : 0;
+    if (out_ticks) *out_ticks = nt;
+    for (int i = 0; i < std::min(cap, nt); i++) tick_ms[i] = tm->tick_ms[i];
+    if (enable) {
+        if (!b->timer) b->timer = new PassTimer();
+        b->timer->ms = 0.0;
+        b->timer->launches = 0;
+        b->timer->tick_ms.clear();
+    } else if (tm) {
+        drop_timed_graphs(b);
+        for (cudaEvent_t e : tm->pool) cudaEventDestroy(e);
+        delete tm;
+        b->timer = nullptr;
+    }
+    return FSE_OK;
 }
 
 int fse_batch_set_launch(fse_batch *b, int colour_ctas_per_sm, int particle_blocks) {
@@ -237,6 +352,7 @@ int fse_batch_set_launch(fse_batch *b, int colour_ctas_per_sm, int particle_bloc
     b->move_blocks = particle_blocks == 0 ? b->max_move_blocks : std::min(particle_blocks, b->max_move_blocks);
     for (auto &g : b->graphs) cudaGraphExecDestroy(g.second);
     b->graphs.clear();
+    drop_timed_graphs(b);
     return FSE_OK;
 }
 
@@ -257,6 +373,9 @@ int fse_batch_autotune(fse_batch *b, int32_t out_choice[4]) {
             for (auto &s : snaps) snap_free(s);
             return FSE_E_NOMEM;
         }
+    // the candidates' steps are not part of any timing the caller asked for
+    PassTimer *keep_timer = b->timer;
+    b->timer = nullptr;
     const int cand[][2] = {{0, 0}, {1, 0}, {0, 4}, {0, 16}, {1, 16}};
     float best = 1e30f;
     int bi = 0;
@@ -282,6 +401,7 @@ int fse_batch_autotune(fse_batch *b, int32_t out_choice[4]) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     for (auto &s : snaps) snap_free(s);
+    b->timer = keep_timer;
     fse_batch_set_launch(b, cand[bi][0], cand[bi][1]);
     if (out_choice) {
         out_choice[0] = cand[bi][0];

@@ -17,9 +17,21 @@ struct PassTimer {
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
     double ms = 0.0;
     long long launches = 0;
+    // recording into a stream capture: the records become event nodes of the graph
+    bool capture = false;
+    // tick boundaries (batches): one group per enqueue call, n + 1 events for n ticks
+    std::vector<std::vector<cudaEvent_t>> tick_groups;
+    std::vector<float> tick_ms;  // duration of each tick read back so far
     cudaEvent_t get();
+    cudaError_t record(cudaEvent_t e, cudaStream_t s) {
+        return capture ? cudaEventRecordWithFlags(e, s, cudaEventRecordExternal) : cudaEventRecord(e, s);
+    }
     void record_pair(cudaEvent_t a, cudaEvent_t b) { pending.push_back({a, b}); }
     void drain();  // after a synchronize: accumulate and recycle events
+    // accumulate pairs and tick groups recorded by a graph replay (the events stay
+    // with the graph)
+    void accumulate(const std::vector<std::pair<cudaEvent_t, cudaEvent_t>> &pairs,
+                    const std::vector<cudaEvent_t> &ticks);
 };
 }  // namespace fse
 

@@ -391,6 +391,9 @@ int fse_batch_destroy(fse_batch *batch);
 int fse_batch_step(fse_batch *batch, int n_ticks);
 /* capture graph_ticks steps into one CUDA graph (default 32) and replay */
 int fse_batch_step_graph(fse_batch *batch, int n_ticks, int graph_ticks);
+/* capture (without running) the graphs a later fse_batch_step_graph(n_ticks,
+ * graph_ticks) replays, so that the capture cost stays out of a timed region */
+int fse_batch_prepare_graphs(fse_batch *batch, int n_ticks, int graph_ticks);
 /* choose the launch shape by timing candidates on the batch itself, then restore
  * every world; results never change. out_choice: colour_ctas_per_sm,
  * particle_blocks, microseconds of two timed steps, candidate index */
@@ -400,6 +403,15 @@ int fse_batch_autotune(fse_batch *batch, int32_t out_choice[4]);
  * (0 = enough for the largest particle list) */
 int fse_batch_set_launch(fse_batch *batch, int colour_ctas_per_sm, int particle_blocks);
 int fse_batch_sync(fse_batch *batch);
+/* Time the batch's steps with CUDA events on its stream: every colour-pass launch
+ * and every tick, for plain and graph steps (graphs captured while timing is on
+ * carry the events as nodes, and each replay is read back before the next one is
+ * launched). enable = 1 starts (and zeroes) the timers, 0 stops them; both first
+ * report what was accumulated since the last start: colour-pass milliseconds and
+ * launches, and each tick's duration in ms into tick_ms[0 .. min(cap, n) - 1] with
+ * *out_ticks = n. */
+int fse_batch_timing(fse_batch *batch, int enable, double *out_pass_ms, int64_t *out_pass_launches, float *tick_ms,
+                     int cap, int *out_ticks);
 /* the CUDA stream (cudaStream_t) the batch enqueues its work on */
 void *fse_batch_stream(fse_batch *batch);
 
