@@ -122,20 +122,22 @@ CFG_RENDER = 1
 CFG_TEMPERATURE = 2
 CFG_TEMPERATURE_STEP = 4
 CFG_REFERENCE_ORDER = 8
+CFG_F32_FLUID = 16
 TEX_PIXELS, TEX_EMISSION, TEX_FIRE, TEX_FLOW, TEX_CELLS = 0, 1, 2, 3, 4
 
 
 def _config(chunk_size=128, cell_iter=3, seed=0, particle_capacity=0, spawn_capacity=0, stream=None, render=False,
-            temperature=False, temperature_step=False, reference_order=False):
+            temperature=False, temperature_step=False, reference_order=False, f32_fluid=False):
     """temperature: keep liquid temperatures (FSE_CFG_TEMPERATURE); temperature_step:
     also run the conduction step every fourth tick inside steps (FSE_CFG_TEMPERATURE_STEP);
     reference_order: update each chunk's cells in the reference's own order
-    (FSE_CFG_REFERENCE_ORDER)."""
+    (FSE_CFG_REFERENCE_ORDER); f32_fluid: liquid amounts and diffs in the reference's
+    own f32 arithmetic (FSE_CFG_F32_FLUID)."""
     return FseConfig(chunk_size, cell_iter, seed & 0xFFFFFFFF, particle_capacity, spawn_capacity,
                      C.c_void_p(stream) if stream else None,
                      (CFG_RENDER if render else 0) | (CFG_TEMPERATURE if temperature else 0) |
                      (CFG_TEMPERATURE_STEP if temperature_step else 0) |
-                     (CFG_REFERENCE_ORDER if reference_order else 0))
+                     (CFG_REFERENCE_ORDER if reference_order else 0) | (CFG_F32_FLUID if f32_fluid else 0))
 
 
 # ---------------------------------------------------------------------- world
@@ -147,14 +149,14 @@ class World:
 
     def __init__(self, width, height, chunk_size=128, cell_iter=3, seed=0, particle_capacity=0, spawn_capacity=0,
                  stream=None, render=False, temperature=False, temperature_step=False, reference_order=False,
-                 _handle=None):
+                 f32_fluid=False, _handle=None):
         self.lib = lib()
         self.width, self.height = int(width), int(height)
         self._owned = _handle is None
         if _handle is None:
             h = C.c_void_p()
             cfg = _config(chunk_size, cell_iter, seed, particle_capacity, spawn_capacity, stream, render, temperature,
-                          temperature_step, reference_order)
+                          temperature_step, reference_order, f32_fluid)
             check(self.lib.fse_world_create(self.width, self.height, C.byref(cfg), C.byref(h)), "world_create")
             self.h = h
         else:

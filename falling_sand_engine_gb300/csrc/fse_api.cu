@@ -391,7 +391,7 @@ void PassTimer::accumulate(const std::vector<std::pair<cudaEvent_t, cudaEvent_t>
 
 int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], const int n_items[4], int max_iter, int C,
                  int threads, int grid, bool particles, int move_blocks, int stage_blocks, cudaStream_t s,
-                 PassTimer *timer, int temp_tiles, bool temp_track, bool seq) {
+                 PassTimer *timer, int temp_tiles, bool temp_track, bool seq, bool f32) {
     int halo = tick_halo();
     for (int iter = 0; iter < max_iter; iter++)  // world.cpp:1050
         for (int tk = 0; tk < 4; tk++) {         // world.cpp:1057-1060
@@ -402,7 +402,7 @@ int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], con
                 if (timer->record(a, s) != cudaSuccess) return FSE_E_CUDA;
             }
             cudaError_t e = launch_colour_pass(d_worlds, items[tk], n_items[tk], iter, tk, g_dev_mt, halo, C, threads,
-                                               grid, s, temp_track, seq);
+                                               grid, s, temp_track, seq, f32);
             if (e != cudaSuccess) return FSE_E_CUDA;
             if (timer) {
                 if (timer->record(b, s) != cudaSuccess) return FSE_E_CUDA;
@@ -711,7 +711,7 @@ static void free_world(fse_world *w) {
     WorldDev &h = w->h;
     void *ptrs[] = {h.id, h.col, h.sc, h.fl, h.df, h.tp, h.tnew, h.stage, h.cp_count, h.cp_base, h.p_state, h.p_lxly,
                     h.req_list, h.req_list2, h.req_target, h.scan_tmp, h.ledger, h.airmap, w->ctr, w->d, w->claim,
-                    w->mask_bits, w->obj_list, w->obj_n};
+                    w->mask_bits, w->obj_list, w->obj_n, h.merge_list, h.merge_count, h.merge_claim};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     PartSoA *ps[2] = {&h.p, &h.q};
@@ -830,6 +830,14 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
     if (ok && (c.flags & FSE_CFG_TEMPERATURE_STEP)) {  // and the conduction step inside every step
         h.temp_on = 1;
         ok = dalloc(w, &h.tnew, temperature_scratch_cells(width, height));
+    }
+    if (ok && (c.flags & FSE_CFG_F32_FLUID)) {  // f32 amounts, deposits into liquid merged in index order
+        h.f32 = 1;
+        ok = dalloc(w, &h.merge_list, 2 * pc) && dalloc(w, &h.merge_count, 1) && dalloc(w, &h.merge_claim, n);
+        if (ok) {
+            cudaMemset(h.merge_count, 0, sizeof(int32_t));
+            cudaMemset(h.merge_claim, 0xFF, n * sizeof(uint32_t));
+        }
     }
     if (ok && (c.flags & FSE_CFG_RENDER)) {
         ok = dalloc(w, &h.dirty, n) && dalloc(w, &h.flow, 2 * n) && dalloc(w, &w->pflow, 2 * n) &&
@@ -1016,7 +1024,7 @@ __global__ void k_generate(WorldDev *wd, int kind, uint32_t seed, const MatTable
         w.id[i] = (uint16_t)mid;
         w.fl[i] = 0;
         w.df[i] = 0;
-        w.sc[i] = mt->f_scalar[mid];
+        w.sc[i] = soup_scalar(mt, mid, w.f32);
         if (w.tp) w.tp[i] = mt_type(mt->a[mid]) == T_SOUP ? (int16_t)mt->f_temp[mid] : (int16_t)0;
         uint32_t colour = mt->f_base[mid];
         uint32_t fp = mt->f_pack[mid];
@@ -1093,7 +1101,7 @@ static int world_enqueue(fse_world *w, bool particles_after_tick, bool tick, boo
     if (tick) {
         rc = enqueue_step(w->d, 1, w->items, w->n_items, w->cell_iter, w->C, w->threads, w->grid, particles_after_tick,
                           world_move_blocks(w), world_stage_blocks(w), w->stream, w->timer, world_temp_tiles(w),
-                          w->h.tp != nullptr, w->seq);
+                          w->h.tp != nullptr, w->seq, w->h.f32 != 0);
         if (rc) return rc;
     } else if (particles) {
         if (launch_particle_tick(w->d, 1, g_dev_mt, world_move_blocks(w), w->stream) != cudaSuccess) return FSE_E_CUDA;
@@ -1165,7 +1173,7 @@ int fse_world_step_graph(fse_world *w, int n) {
             for (int i = 0; i < k && erc == FSE_OK; i++)
                 erc = enqueue_step(w->d, 1, w->items, w->n_items, w->cell_iter, w->C, w->threads, w->grid, true,
                                    world_move_blocks(w), world_stage_blocks(w), w->stream, nullptr,
-                                   world_temp_tiles(w), w->h.tp != nullptr, w->seq);
+                                   world_temp_tiles(w), w->h.tp != nullptr, w->seq, w->h.f32 != 0);
             cudaError_t e = cudaStreamEndCapture(w->stream, &g);
             const long long kn = fse_launch_counter() - c0;
             count_launches(-kn);
@@ -1361,14 +1369,15 @@ __global__ void k_census(const WorldDev *__restrict__ wd, const MatTable *__rest
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         int id = w.id[i];
         atomicAdd(&s[id], 1ull);
-        if (mt_type(mt->a[id]) == T_SOUP)
+        if (!w.f32 && mt_type(mt->a[id]) == T_SOUP)  // no fluid rows for f32 amounts
             atomicAdd(&s[MAXMAT + id], (unsigned long long)((long long)w.sc[i] + w.df[i]));
     }
     const int np = *w.part_count;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
         int id = w.p.id[i];
         atomicAdd(&s[2 * MAXMAT + id], 1ull);
-        if (mt_type(mt->a[id]) == T_SOUP) atomicAdd(&s[3 * MAXMAT + id], (unsigned long long)(long long)w.p.sc[i]);
+        if (!w.f32 && mt_type(mt->a[id]) == T_SOUP)
+            atomicAdd(&s[3 * MAXMAT + id], (unsigned long long)(long long)w.p.sc[i]);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < 4 * MAXMAT; i += blockDim.x)

@@ -103,7 +103,8 @@ int batch_enqueue(fse_batch *b, int n) {
     for (int i = 0; i < n; i++) {
         if ((rc = boundary())) return rc;
         rc = enqueue_step(b->d_table, (int)b->worlds.size(), b->items, b->n_items, b->max_iter, b->C, b->threads,
-                          b->grid, true, b->move_blocks, b->stage_blocks, b->stream, tm, tt, tr);
+                          b->grid, true, b->move_blocks, b->stage_blocks, b->stream, tm, tt, tr, false,
+                          b->worlds[0]->h.f32 != 0);
         if (rc) return rc;
     }
     if (n > 0 && (rc = boundary())) return rc;
@@ -187,9 +188,11 @@ int fse_batch_create(fse_world **worlds, int n, fse_batch **out) {
             delete b;
             return FSE_E_INVAL;
         }
-        if ((i > 0 && worlds[i]->C != worlds[0]->C) || worlds[i]->seq) {
+        if ((i > 0 && (worlds[i]->C != worlds[0]->C || worlds[i]->h.f32 != worlds[0]->h.f32)) || worlds[i]->seq) {
             delete b;
-            return FSE_E_INVAL;  // one shared-memory tile shape per launch; partitioned order only
+            // one shared-memory tile shape and one kind of liquid amounts per launch;
+            // partitioned order only
+            return FSE_E_INVAL;
         }
         b->worlds.push_back(worlds[i]);
         b->max_iter = std::max(b->max_iter, worlds[i]->cell_iter);
@@ -490,7 +493,8 @@ int fse_server_add_world(fse_server *s, int w, int h, const fse_config *cfg, int
     fse_config c{};
     if (cfg) c = *cfg;
     if (c.chunk_size == 0) c.chunk_size = 128;
-    if (c.flags & FSE_CFG_REFERENCE_ORDER) return FSE_E_INVAL;  // servers batch their worlds
+    // servers batch their worlds in the partitioned order with Q16.16 amounts
+    if (c.flags & (FSE_CFG_REFERENCE_ORDER | FSE_CFG_F32_FLUID)) return FSE_E_INVAL;
     if (!s->slots.empty()) {
         for (fse_world *x : s->slots)
             if (x && x->C != c.chunk_size) return FSE_E_INVAL;

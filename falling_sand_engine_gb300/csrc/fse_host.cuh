@@ -91,11 +91,11 @@ size_t colour_pass_smem(int C, int halo);
 // temp: some world of the table keeps liquid temperatures (tp != NULL)
 cudaError_t launch_colour_pass(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
                                const MatTable *mt, int halo, int C, int threads, int grid, cudaStream_t s,
-                               bool temp = false, bool seq = false);
+                               bool temp = false, bool seq = false, bool f32 = false);
 cudaError_t launch_spawn_append(WorldDev *d_worlds, int n_worlds, int stage_blocks, cudaStream_t s);
 cudaError_t launch_particle_tick(WorldDev *d_worlds, int n_worlds, const MatTable *mt, int move_blocks,
                                  cudaStream_t s);
-constexpr int PARTICLE_TICK_LAUNCHES = 12;  // kernels launch_particle_tick issues
+constexpr int PARTICLE_TICK_LAUNCHES = 13;  // kernels launch_particle_tick issues
 // world::tickTemperature over a set of worlds (max_tiles: the most 128 x 32 tiles of
 // any of them); gated: only worlds with temp_on, after ticks whose index is 2 mod 4
 cudaError_t launch_temperature(const WorldDev *d_worlds, int n_worlds, int max_tiles, const MatTable *mt, bool gated,
@@ -113,7 +113,8 @@ int tick_halo();
 // share a device descriptor table
 int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], const int n_items[4], int max_iter,
                  int C, int threads, int grid, bool particles, int move_blocks, int stage_blocks, cudaStream_t s,
-                 PassTimer *timer = nullptr, int temp_tiles = 0, bool temp_track = false, bool seq = false);
+                 PassTimer *timer = nullptr, int temp_tiles = 0, bool temp_track = false, bool seq = false,
+                 bool f32 = false);
 void count_launches(long long n);
 
 }  // namespace fse

@@ -26,6 +26,13 @@ constexpr int32_t Q_MAXCOMP = 6554;
 constexpr int32_t Q_MAXFLOW = 524288;
 constexpr int32_t Q_FREEFALL = 327;
 constexpr int32_t Q_DEFAULT = 131072;
+// the same constants as the reference's own floats, for worlds created with
+// FSE_CFG_F32_FLUID (amounts and diffs are then f32 bit patterns in the 32-bit planes)
+constexpr float F_MAXV = 0.5f;
+constexpr float F_MINV = 0.0005f;
+constexpr float F_MAXCOMP = 0.1f;
+constexpr float F_MAXFLOW = 8.0f;
+constexpr int32_t F_DEFAULT_BITS = 0x40000000;  // 2.0f, MaterialInstance::fluidAmount's default
 
 constexpr uint32_t PH_GEN = 0x47454E00u;
 constexpr uint32_t PH_STAMP = 0x5354414Du;
@@ -178,7 +185,32 @@ struct WorldDev {
     // tnew holds the deferred results of tile-edge cells
     int temp_on;
     int32_t *tnew;
+    // FSE_CFG_F32_FLUID: liquid amounts and pending diffs are f32 (the reference's
+    // own arithmetic) rather than Q16.16; the ledger then keeps no fluid rows
+    int f32;
+    // f32 worlds: deposits of liquid particles into liquid cells, applied after the
+    // deposit rounds cell by cell in particle-index order (particle indices; the
+    // target cell is in p_lxly), and per-cell claims of that pass (all ones between
+    // ticks)
+    int32_t *merge_list;
+    int32_t *merge_count;
+    uint32_t *merge_claim;
 };
+
+// the amount of a new SOUP tile of material mid (TilesCreate, and the
+// MaterialInstance default 2.0): the factory's Q16.16 scalar, or its f32 value in
+// worlds with f32 amounts; other materials' scalar (a temperature) as it is
+__host__ __device__ __forceinline__ int32_t soup_scalar(const MatTable *mt, int mid, int f32) {
+    const int32_t q = mt->f_scalar[mid];
+    if (!f32 || mt_type(mt->a[mid]) != T_SOUP) return q;
+    const float f = (float)q * (1.0f / 65536.0f);  // exact: q is a multiple of 2^-16 well below 2^24
+    union {
+        float f;
+        int32_t i;
+    } u;
+    u.f = f;
+    return u.i;
+}
 
 __host__ __device__ __forceinline__ int ceil_div(int a, int b) { return (a + b - 1) / b; }
 

@@ -226,8 +226,9 @@ __global__ void __launch_bounds__(1024) k_obj_rounds(WorldDev *wd, const MatTabl
                     atomicOr(w.err, ERR_PART_CAP);
                 }
                 if (ty == T_SOUP) {
-                    atomicAdd((unsigned long long *)&w.ledger[LED_DF * MAXMAT + w.id[tg]],
-                              (unsigned long long)(long long)w.df[tg]);
+                    if (!w.f32)  // f32 amounts: no fluid rows
+                        atomicAdd((unsigned long long *)&w.ledger[LED_DF * MAXMAT + w.id[tg]],
+                                  (unsigned long long)(long long)w.df[tg]);
                     atomicAdd(&b.n_soup, 1);
                 } else {
                     atomicAdd(&b.n_sand, 1);

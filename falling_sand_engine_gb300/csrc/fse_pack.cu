@@ -815,7 +815,7 @@ __global__ void k_unpack_scatter(const WorldDev *__restrict__ wd, const MatTable
         w.fl[i] = 0;
         w.df[i] = 0;
         if (mt_type(mt->a[id]) == T_SOUP) {
-            w.sc[i] = Q_DEFAULT;  // MaterialInstance::fluidAmount = 2.0
+            w.sc[i] = w.f32 ? F_DEFAULT_BITS : Q_DEFAULT;  // MaterialInstance::fluidAmount = 2.0
             if (w.tp) w.tp[i] = t;
         } else {
             w.sc[i] = t;
@@ -1278,7 +1278,8 @@ int fse_world_checkpoint(fse_world *w, uint8_t *out, int64_t cap, int64_t *out_s
     if (!o.room(8)) return FSE_E_CAPACITY;
     memcpy(out, CK_MAGIC, 8);
     o.n = 8;
-    const int32_t flags = w->h.tp ? 1 : 0;
+    // bit 0: liquid temperatures follow; bit 1: liquid amounts are f32
+    const int32_t flags = (w->h.tp ? 1 : 0) | (w->h.f32 ? 2 : 0);
     if (!o.put((int32_t)w->W) || !o.put((int32_t)w->H) || !o.put((int32_t)w->C) || !o.put((int32_t)w->cell_iter) ||
         !o.put((uint32_t)w->h.seed) || !o.put((uint32_t)info[5]) || !o.put(flags) || !o.put((int32_t)info[6]) ||
         !o.put((int32_t)secs.size()))
@@ -1315,6 +1316,7 @@ int fse_world_restore(fse_world *w, const uint8_t *in, int64_t size) {
         return FSE_E_INVAL;
     if (W != w->W || H != w->H || C != w->C || it != w->cell_iter || np < 0) return FSE_E_INVAL;
     if ((flags & 1) && !w->h.tp) return FSE_E_STATE;  // liquid temperatures need FSE_CFG_TEMPERATURE
+    if (((flags & 2) != 0) != (w->h.f32 != 0)) return FSE_E_STATE;  // f32 and Q16.16 amounts do not mix
     if (np > w->part_cap) return FSE_E_CAPACITY;
     // sections in file order; a world that keeps liquid temperatures restores a file
     // without them as 0

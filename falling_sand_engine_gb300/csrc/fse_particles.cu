@@ -120,7 +120,7 @@ __device__ __forceinline__ void led_part(const WorldDev &w, const MatTable *mt, 
     int ty = mt_type(mt->a[id]);
     if (ty == T_AIR) return;
     atomicAdd((unsigned long long *)&w.ledger[row_n * MAXMAT + id], 1ull);
-    if (ty == T_SOUP && sc != 0)
+    if (ty == T_SOUP && sc != 0 && !w.f32)  // f32 amounts: no fluid rows
         atomicAdd((unsigned long long *)&w.ledger[row_f * MAXMAT + id], (unsigned long long)(long long)sc);
 }
 
@@ -293,7 +293,14 @@ __device__ __forceinline__ void dep_fail(const WorldDev &w, int i) {
 }
 __device__ __forceinline__ void dep_merge(const WorldDev &w, const MatTable *mt, int i, int c) {
     // :2119-2125
-    atomicAdd(&w.sc[c], w.p.sc[i]);
+    if (w.f32) {
+        // f32 amounts: added after the rounds, cell by cell in particle-index order
+        // (k_merge_f32), as the reference's list order adds them
+        w.p_lxly[i] = c;
+        w.merge_list[atomicAdd(w.merge_count, 1)] = i;
+    } else {
+        atomicAdd(&w.sc[c], w.p.sc[i]);
+    }
     if (w.dirty) w.dirty[c] = 1;
     w.p_state[i] = PS_DEAD;
     atomicAdd((unsigned long long *)&w.ledger[LED_DN * MAXMAT + w.p.id[i]], 1ull);
@@ -495,6 +502,50 @@ __global__ void k_dep_clear(const WorldDev *__restrict__ worlds) {
     const int n = w.req_count[2];
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
         w.df[w.req_list2[w.part_cap + j]] = 0;
+}
+
+// f32 worlds: the deposits into liquid of this particle tick, applied to each cell in
+// particle-index order (tile.fluidAmount += particle amount, world.cpp:2123, in the
+// reference's float add). One block per world: each round every cell takes its
+// lowest-index pending deposit, so a cell with k deposits is done after k rounds.
+__global__ void k_merge_f32(const WorldDev *__restrict__ worlds) {
+    const WorldDev &w = worlds[blockIdx.x];
+    if (!w.f32) return;
+    __shared__ int s_open, s_next;
+    const int n0 = *w.merge_count;
+    if (n0 == 0) return;
+    // two lists of part_cap entries: the open deposits of this round, the next's
+    int32_t *cur = w.merge_list, *nxt = w.merge_list + w.part_cap;
+    if (threadIdx.x == 0) s_open = n0;
+    __syncthreads();
+    for (int round = 0; round < (1 << 24); round++) {
+        const int n = s_open;
+        if (n == 0) break;
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+            const int i = cur[j];
+            atomicMin(&w.merge_claim[w.p_lxly[i]], (uint32_t)i);
+        }
+        if (threadIdx.x == 0) s_next = 0;
+        __syncthreads();
+        // the winners add (one thread per cell); the others go to the next round
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+            const int i = cur[j];
+            const int c = w.p_lxly[i];
+            if (w.merge_claim[c] == (uint32_t)i)
+                w.sc[c] = __float_as_int(__fadd_rn(__int_as_float(w.sc[c]), __int_as_float(w.p.sc[i])));
+            else
+                nxt[atomicAdd(&s_next, 1)] = i;
+        }
+        __syncthreads();
+        for (int j = threadIdx.x; j < n; j += blockDim.x) w.merge_claim[w.p_lxly[cur[j]]] = 0xFFFFFFFFu;
+        __syncthreads();
+        if (threadIdx.x == 0) s_open = s_next;
+        int32_t *t = cur;
+        cur = nxt;
+        nxt = t;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *w.merge_count = 0;
 }
 
 // ------------------------------------------------------------- compaction
@@ -711,6 +762,7 @@ cudaError_t launch_particle_tick(WorldDev *d_worlds, int n_worlds, const MatTabl
         cudaLaunchKernelEx(&cfg, k_dep_rounds, (const WorldDev *)d_worlds, n_worlds, mt);
     }
     k_dep_clear<<<gm, 256, 0, s>>>(d_worlds);
+    k_merge_f32<<<n_worlds, 1024, 0, s>>>(d_worlds);
     dim3 gc(PART_BLOCKS, n_worlds);
     k_cmp_count<<<gc, PART_THREADS, 0, s>>>(d_worlds);
     k_cmp_scan<<<n_worlds, PART_BLOCKS, 0, s>>>(d_worlds, PART_BLOCKS);

@@ -95,8 +95,9 @@ __device__ __forceinline__ void paint(const WorldDev &w, const MatTable *__restr
     if (id == id_fire) rt.tex[2][i] = px;  // other cells keep their fire texel
     if (type == T_SOUP) {
         float *pf = rt.pflow + 2 * i;
-        const float fx = __fmul_rn(__int2float_rn(fl[0]), 1.0f / 65536.0f);
-        const float fy = __fmul_rn(__int2float_rn(fl[1]), 1.0f / 65536.0f);
+        // the tick's flow sums: f32 in worlds with f32 amounts, else Q16.16
+        const float fx = w.f32 ? __int_as_float(fl[0]) : __fmul_rn(__int2float_rn(fl[0]), 1.0f / 65536.0f);
+        const float fy = w.f32 ? __int_as_float(fl[1]) : __fmul_rn(__int2float_rn(fl[1]), 1.0f / 65536.0f);
         const float nfx = smooth(pf[0], fx);
         float nfy = smooth(pf[1], fy);
         if (nfy < 0.0f) nfy = half_of(nfy);

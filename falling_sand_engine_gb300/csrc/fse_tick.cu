@@ -128,10 +128,12 @@ struct TileData {
 };
 
 // LIVE: the pillar reads the tile as it stands (the reference's own order, where
-// one thread updates the chunk's cells in turn) instead of the sweep-B snapshot
-template <bool EDGE, bool TEMP, bool LIVE = false>
+// one thread updates the chunk's cells in turn) instead of the sweep-B snapshot.
+// F32: liquid amounts and diffs are f32 bit patterns (FSE_CFG_F32_FLUID).
+template <bool EDGE, bool TEMP, bool LIVE = false, bool F32 = false>
 struct Tile : TileData {
     static constexpr bool kTemp = TEMP;
+    static constexpr bool kF32 = F32;
     __device__ __forceinline__ explicit Tile(const TileData &d) : TileData(d) {}
 
     // 10 AIR bits of column x starting at row y: from the snapshot (0 outside it), or
@@ -269,6 +271,24 @@ struct Tile : TileData {
         if (!inw(x, y)) return;
         atomicAdd(&df[y * W + x], v);  // fire-and-forget reduction: the thread does not wait
     }
+    // f32 worlds: fluidAmountDiff += v as the reference's float add. No other cell of
+    // the sub-phase (or wavefront step) touches this diff, and the ones that touched
+    // it before did so in the reference's order, so a plain read-modify-write adds in
+    // that order.
+    __device__ __forceinline__ void add_diff_f(int x, int y, float v) const {
+        if (!inw(x, y)) return;
+        int32_t *p = &df[y * W + x];
+        *p = __float_as_int(__fadd_rn(__int_as_float(*p), v));
+    }
+    // write the active cell back at its own position with its diff (f32 worlds)
+    __device__ __forceinline__ void put_df(int x, int y, const Cell &c, float dfv) const {
+        int i = li(x, y);
+        s_id[i] = c.id | DIRTY;
+        s_fl[i] = (uint8_t)((c.fl & (uint8_t)~VISITED) | (s_fl[i] & VISITED));
+        s_sc[i] = c.sc;
+        s_col[i] = c.col;
+        df[y * W + x] = __float_as_int(dfv);
+    }
     __device__ __forceinline__ bool vis(int x, int y) const { return (s_fl[li(x, y)] & VISITED) != 0; }
     __device__ __forceinline__ void setvis(int x, int y) const {
         if (!inw(x, y)) return;
@@ -283,6 +303,7 @@ struct Ctx {
     bool have_ck;
     int iter;
     int id_fire, id_water, id_lava, id_steam, id_obsidian, has_inter;
+    bool f32;  // f32 liquid amounts: the ledger keeps no fluid rows (a compile-time constant)
     const MatTable *mt;
     long long *led_s;      // shared ledger [LED_ROWS][64]
     long long *led_g;      // global ledger [LED_ROWS][MAXMAT]
@@ -325,16 +346,16 @@ __device__ __forceinline__ void led_add(Ctx &c, int row, int mat, long long v) {
 // a conversion (not a move) of the content old -> nw
 __device__ __forceinline__ void led_swap(Ctx &c, int old_id, long long old_fluid, int new_id, long long new_fluid) {
     led_add(c, LED_DN, old_id, 1);
-    if (mt_type(c.ma[old_id]) == T_SOUP) led_add(c, LED_DF, old_id, old_fluid);
+    if (!c.f32 && mt_type(c.ma[old_id]) == T_SOUP) led_add(c, LED_DF, old_id, old_fluid);
     led_add(c, LED_CN, new_id, 1);
-    if (mt_type(c.ma[new_id]) == T_SOUP) led_add(c, LED_CF, new_id, new_fluid);
+    if (!c.f32 && mt_type(c.ma[new_id]) == T_SOUP) led_add(c, LED_CF, new_id, new_fluid);
 }
 // conversion of whatever is at (x, y) into nw
 template <class TL>
 __device__ __forceinline__ void led_replace_at(const TL &T, Ctx &c, int x, int y, const Cell &nw) {
     if (!T.inw(x, y)) return;
     int oid = T.id(x, y);
-    long long of = (mt_type(c.ma[oid]) == T_SOUP) ? (long long)T.sc(x, y) + T.df_of(x, y) : 0;
+    long long of = (!c.f32 && mt_type(c.ma[oid]) == T_SOUP) ? (long long)T.sc(x, y) + T.df_of(x, y) : 0;
     led_swap(c, oid, of, nw.id, (long long)nw.sc + nw.df);
 }
 
@@ -344,7 +365,7 @@ __device__ __forceinline__ Cell create_tile(Ctx &c, int mid) {
     t.id = (uint16_t)mid;
     t.fl = 0;
     t.df = 0;
-    t.sc = __ldg(&c.mt->f_scalar[mid]);
+    t.sc = soup_scalar(c.mt, mid, c.f32);  // a temperature, or a SOUP tile's amount
     t.col = __ldg(&c.mt->f_base[mid]);
     uint32_t fp = __ldg(&c.mt->f_pack[mid]);
     int mod = (int)(fp >> 20);
@@ -367,6 +388,24 @@ __device__ __forceinline__ int32_t clampflow(int32_t flow, int32_t rem) {
     if (flow < 0) flow = 0;
     int32_t lim = rem < Q_MAXFLOW ? rem : Q_MAXFLOW;
     return flow > lim ? lim : flow;
+}
+
+// CalculateVerticalFlowValue, world.cpp:1021-1034, in the reference's f32: every
+// operation separately rounded as the reference's x86-64 build does (no contraction)
+__device__ __forceinline__ float vflow_f(float rem, float dst) {
+    const float sum = __fadd_rn(rem, dst);
+    if (sum <= F_MAXV) return F_MAXV;
+    if (sum < __fadd_rn(2.0f * F_MAXV, F_MAXCOMP))
+        return __fdiv_rn(__fadd_rn(F_MAXV * F_MAXV, __fmul_rn(sum, F_MAXCOMP)), __fadd_rn(F_MAXV, F_MAXCOMP));
+    return __fdiv_rn(__fadd_rn(sum, F_MAXCOMP), 2.0f);
+}
+// flow = std::max(flow, 0.0f); if (flow > std::min(FLUID_MaxFlow, rem)) flow = ...
+// (world.cpp:1320-1321 and its three copies), with std::max/min's own comparisons;
+// the FLUID_FlowSpeed factor of 1.0f before it changes no float and is left out
+__device__ __forceinline__ float clampflow_f(float flow, float rem) {
+    if (flow < 0.0f) flow = 0.0f;
+    const float lim = (rem < F_MAXFLOW) ? rem : F_MAXFLOW;
+    return (flow > lim) ? lim : flow;
 }
 
 __device__ __forceinline__ bool can_sink(const uint32_t *ma, const float *md, int other, int self) {
@@ -405,6 +444,38 @@ __device__ __forceinline__ void soup_flow(const TL &T, Ctx &c, Cell &t, int32_t 
     }
 }
 
+// f32 worlds: one flow of world.cpp:1309-1460 from (x, y) towards (x + dx, y + dy);
+// dfv is the active cell's fluidAmountDiff, updated in the reference's order
+template <class TL>
+__device__ __forceinline__ void soup_flow_f(const TL &T, Ctx &c, const Cell &t, float &rem, float &dfv, float flow,
+                                            int nT, int x, int y, int dx, int dy) {
+    if (flow == 0.0f) return;
+    const int nx = x + dx, ny = y + dy;
+    float *fw = reinterpret_cast<float *>(s_w.flow);
+    if (fw) {
+        // flowX / flowY of (x, y) (world.cpp:1334,1374,1402,1432): only this cell adds to them
+        float *q = &fw[2 * ((size_t)y * T.W + x) + (dx != 0 ? 0 : 1)];
+        *q = (dx + dy) > 0 ? __fadd_rn(*q, flow) : __fsub_rn(*q, flow);
+    }
+    rem = __fsub_rn(rem, flow);
+    dfv = __fsub_rn(dfv, flow);
+    if (nT == T_AIR) {
+        // MaterialInstance(tile.mat, tile.color, tile.temperature), fluidAmount 0,
+        // then fluidAmountDiff (0) += flow
+        Cell nt;
+        nt.id = t.id;
+        nt.fl = 0;
+        nt.sc = __float_as_int(0.0f);
+        nt.col = t.col;
+        nt.df = __float_as_int(__fadd_rn(0.0f, flow));
+        T.put(nx, ny, nt);
+        T.tp_store(nx, ny, T.tp_load(x, y));
+        led_add(c, LED_CN, t.id, 1);
+    } else {
+        T.add_diff_f(nx, ny, flow);
+    }
+}
+
 __device__ __forceinline__ void spawn_one(Ctx &c, int kind, int x, int y, const Cell &t, float vx, float vy) {
     c.ev.n = 1;
     c.ev.kind = kind;
@@ -416,6 +487,143 @@ __device__ __forceinline__ void spawn_one(Ctx &c, int kind, int x, int y, const 
     c.ev.sc = t.sc;
     c.ev.vx = vx;
     c.ev.vy = vy;
+}
+
+// ------------------------------------------------- sweep A, f32 liquids
+// world.cpp:1269-1567 with the reference's own float amounts (FSE_CFG_F32_FLUID):
+// the same branches as the Q16.16 rule, in f32 with every operation rounded on its
+// own; the cell's fluidAmountDiff is read when its turn begins (it already holds the
+// flows of the cells updated before it) and written back with its own flows
+// subtracted in order, as the reference's copy of the tile does.
+template <class TL>
+__device__ __forceinline__ void rule_a_soup_f32(const TL &T, Ctx &c, Cell &t, int x, int y) {
+    const uint32_t *ma = T.ma;
+    const float amount = __int_as_float(t.sc);
+    if (amount == 0.0f) return;
+    if (amount < F_MINV) {
+        t.sc = __float_as_int(0.0f);
+        T.put_delta(x, y, t);  // t.df is 0: the diff stays as it is
+        return;
+    }
+    // tile.fluidAmount > 0.005 compares in double (0.005 is a double literal)
+    if ((double)amount > 0.005 && T.type(x, y + 1) == T_AIR && T.type(x, y + 2) == T_AIR &&
+        T.type(x, y + 3) == T_AIR && T.type(x, y + 4) == T_AIR) {  // world.cpp:1283-1305
+        T.set_nothing(x, y);
+        int n = (int)__fdiv_rn(amount, 4.0f);  // int n = tile.fluidAmount / 4
+        if (n < 1) n = 1;
+        led_add(c, LED_CN, t.id, n - 1);
+        c.ev.n = n;
+        c.ev.kind = 2;
+        c.ev.x = x;
+        c.ev.y = y + 1;
+        c.ev.id = t.id;
+        c.ev.fl = 0;
+        c.ev.col = t.col;
+        c.ev.sc = t.sc;
+        if (TL::kTemp) c.ev.tp = T.tp_load(x, y);
+        c.ev.ck = c.key();
+        c.ev.k0 = c.k;
+        c.k += 2 * n;
+        return;
+    }
+    if (t.fl & MOVED) return;
+    const float start = amount;
+    float rem = amount;
+    float dfv = __int_as_float(T.df_load(x, y));
+    const int bid = T.id(x, y + 1);
+    const int bT = mt_type(ma[bid]);
+    const bool airBelow = bT == T_AIR;
+    if ((airBelow && c.iter <= 2) || bid == (int)t.id) {
+        const float dst = (bT == T_SOUP) ? __int_as_float(T.sc(x, y + 1)) : 0.0f;
+        soup_flow_f(T, c, t, rem, dfv, clampflow_f(__fsub_rn(vflow_f(start, dst), dst), start), bT, x, y, 0, 1);
+    } else if (c.iter == 0 && bT == T_SOUP && bid != (int)t.id) {
+        if (c.D() % 10 == 0) {
+            t.df = __float_as_int(dfv);  // the cell leaves its position with its diff
+            const int16_t tv = T.tp_load(x, y);
+            T.move(x, y, x, y + 1);
+            T.put(x, y + 1, t);
+            T.tp_store(x, y + 1, tv);
+            return;
+        }
+    }
+    if (rem < F_MINV) {
+        T.put_df(x, y, t, __fsub_rn(dfv, rem));
+        return;
+    }
+    const int lid = T.id(x - 1, y);
+    const int lT = mt_type(ma[lid]);
+    const bool canL = (lT == T_AIR || lid == (int)t.id) && !airBelow;
+    const int rid = T.id(x + 1, y);
+    const int rT = mt_type(ma[rid]);
+    const bool canR = (rT == T_AIR || rid == (int)t.id) && !airBelow;
+    if (canL) {
+        const float dst = (lT == T_SOUP) ? __int_as_float(T.sc(x - 1, y)) : 0.0f;
+        soup_flow_f(T, c, t, rem, dfv, clampflow_f(__fdiv_rn(__fsub_rn(rem, dst), canR ? 3.0f : 2.0f), rem), lT, x,
+                    y, -1, 0);
+    }
+    if (rem < F_MINV) {
+        T.put_df(x, y, t, __fsub_rn(dfv, rem));
+        return;
+    }
+    if (canR) {
+        const float dst = (rT == T_SOUP) ? __int_as_float(T.sc(x + 1, y)) : 0.0f;
+        soup_flow_f(T, c, t, rem, dfv, clampflow_f(__fdiv_rn(__fsub_rn(rem, dst), 2.0f), rem), rT, x, y, 1, 0);
+    }
+    if (rem < F_MINV) {
+        T.put_df(x, y, t, __fsub_rn(dfv, rem));
+        return;
+    }
+    const int tid = T.id(x, y - 1);
+    const int tT = mt_type(ma[tid]);
+    if (tT == T_AIR || tid == (int)t.id) {
+        const float dst = (tT == T_SOUP) ? __int_as_float(T.sc(x, y - 1)) : 0.0f;
+        soup_flow_f(T, c, t, rem, dfv, clampflow_f(__fsub_rn(rem, vflow_f(rem, dst)), rem), tT, x, y, 0, -1);
+    } else if (c.iter == 0 && tT == T_SOUP && tid != (int)t.id) {
+        if (c.D() % 10 == 0) {
+            t.df = __float_as_int(dfv);
+            const int16_t tv = T.tp_load(x, y);
+            T.move(x, y, x, y - 1);
+            T.put(x, y - 1, t);
+            T.tp_store(x, y - 1, tv);
+            return;
+        }
+    }
+    if (rem < F_MINV) {
+        T.put_df(x, y, t, __fsub_rn(dfv, rem));
+        return;
+    }
+    if (start == rem) {  // world.cpp:1472-1483
+        uint8_t s = t.fl & SETTLE_MASK;
+        if (s < SETTLE_MASK) s++;
+        t.fl = (uint8_t)((t.fl & ~SETTLE_MASK) | s);
+        if (s >= 10) t.fl |= MOVED;
+    } else {
+        if (tT == T_SOUP) T.set_moved(x, y - 1, false);
+        if (bT == T_SOUP) T.set_moved(x, y + 1, false);
+        if (lT == T_SOUP) T.set_moved(x - 1, y, false);
+        if (rT == T_SOUP) T.set_moved(x + 1, y, false);
+    }
+    T.put_df(x, y, t, dfv);
+    // WATER on LAVA, world.cpp:1519-1537
+    if ((int)t.id == c.id_water && T.id(x, y + 1) == c.id_lava) {
+        const MatTable *mt = c.mt;
+        Cell st = create_tile(c, c.id_steam);
+        led_swap(c, t.id, 0, st.id, 0);
+        T.put_new(x, y, st, mt);
+        Cell ob = create_tile(c, c.id_obsidian);
+        led_replace_at(T, c, x, y + 1, ob);
+        T.put_new(x, y + 1, ob, mt);
+        T.setvis(x, y + 1);
+        for (int xx = -1; xx <= 1; xx++)
+            for (int yy = 0; yy <= 2; yy++) {
+                if (T.id(x + xx, y + yy) == c.id_lava) {
+                    Cell o2 = create_tile(c, c.id_obsidian);
+                    led_replace_at(T, c, x + xx, y + yy, o2);
+                    T.put_new(x + xx, y + yy, o2, mt);
+                    T.setvis(x + xx, y + yy);
+                }
+            }
+    }
 }
 
 // ----------------------------------------------------------------- sweep A
@@ -552,6 +760,8 @@ __device__ __forceinline__ void rule_a(const TL &T, Ctx &c, int x, int y) {
                 }
             }
         }
+    } else if (TL::kF32 && type == T_SOUP) {
+        rule_a_soup_f32(T, c, t, x, y);
     } else if (type == T_SOUP) {  // world.cpp:1269-1567
         if (t.sc == 0) return;
         if (t.sc < Q_MINV) {
@@ -776,6 +986,19 @@ __device__ __forceinline__ void rule_b(const TL &T, Ctx &c, int x, int y, int32_
         } else {
             T.set_moved(x, y, false);
         }
+    } else if (TL::kF32 && type == T_SOUP) {  // world.cpp:1728-1745 in f32
+        Cell t = T.get_active(x, y);
+        const float a = __fadd_rn(__int_as_float(t.sc), __int_as_float(dfv));
+        t.sc = __float_as_int(a);
+        t.df = __float_as_int(0.0f);
+        if (a < F_MINV) {
+            led_add(c, LED_DN, t.id, 1);
+            T.set_nothing(x, y);
+            T.setvis(x, y);
+        } else {
+            T.put(x, y, t);
+            T.setvis(x, y);
+        }
     } else if (type == T_SOUP) {  // world.cpp:1728-1745
         Cell t = T.get_active(x, y);
         t.sc += dfv;
@@ -888,13 +1111,18 @@ __device__ __forceinline__ int block_excl_scan(int v, int *scratch, int *total) 
 }
 
 // write the particles of one spawn event (world.cpp:1110-1119,1222,1298)
-template <bool TEMP>
+template <bool TEMP, bool F32>
 static __device__ __noinline__ void emit_spawns(const WorldDev &w, const SpawnEv &ev, uint32_t cp, uint32_t rank0,
                                                 int base) {
     int32_t base_amt = 0, extra = 0;
     if (ev.kind == 2) {
-        base_amt = ev.sc / ev.n;
-        extra = ev.sc % ev.n;
+        if (F32) {
+            // f32 amt = tile.fluidAmount / n for every particle (world.cpp:1292)
+            base_amt = __float_as_int(__fdiv_rn(__int_as_float(ev.sc), (float)ev.n));
+        } else {
+            base_amt = ev.sc / ev.n;
+            extra = ev.sc % ev.n;
+        }
     }
     for (int i = 0; i < ev.n; i++) {
         int slot = base + i;
@@ -960,7 +1188,7 @@ struct SmemHead {
 // SEQ: the reference's own order inside each chunk (bottom row first, left to right,
 // sweep by sweep; world.cpp:1084-1087, 1589, 1823), with the same rules, run as a
 // wavefront of one thread per chunk row (see sweeps_seq)
-template <int HALO, bool TEMP, bool SEQ>
+template <int HALO, bool TEMP, bool SEQ, bool F32>
 __global__ void __launch_bounds__(CP_THREADS, 1)
     k_colour_pass(const WorldDev *__restrict__ worlds, const uint32_t *__restrict__ items, int n_items, int iter, int tk,
                   const MatTable *__restrict__ mt) {
@@ -988,6 +1216,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
     c.id_steam = mt->id_steam;
     c.id_obsidian = mt->id_obsidian;
     c.has_inter = mt->has_inter;
+    c.f32 = F32;
     const int id_solid = mt->id_solid, id_air = mt->id_air;
     FSE_PT_DECL
     __syncthreads();
@@ -1147,7 +1376,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                             rule_a(Tl, c, x, y);
                             if (c.ev.n > 0) {
                                 const int base = atomicAdd(w.stage_count, c.ev.n);
-                                emit_spawns<TEMP>(w, c.ev, cp * (uint32_t)w.cp_rows + (uint32_t)k, (uint32_t)spawned,
+                                emit_spawns<TEMP, F32>(w, c.ev, cp * (uint32_t)w.cp_rows + (uint32_t)k, (uint32_t)spawned,
                                                   base);
                                 spawned += c.ev.n;
                             }
@@ -1213,7 +1442,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                                 // staging slots are taken in any order; the (chunk-pass, rank)
                                 // key orders the particles later
                                 const int base = atomicAdd(w.stage_count, c.ev.n);
-                                emit_spawns<TEMP>(w, c.ev, cp, (uint32_t)(running + ex), base);
+                                emit_spawns<TEMP, F32>(w, c.ev, cp, (uint32_t)(running + ex), base);
                             }
                             running += tot;
                         }
@@ -1260,14 +1489,14 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
         };
         if constexpr (SEQ) {
             if (edge)
-                sweeps_seq(Tile<true, TEMP, true>(Tl));
+                sweeps_seq(Tile<true, TEMP, true, F32>(Tl));
             else
-                sweeps_seq(Tile<false, TEMP, true>(Tl));
+                sweeps_seq(Tile<false, TEMP, true, F32>(Tl));
         } else {
             if (edge)
-                sweeps(Tile<true, TEMP>(Tl));
+                sweeps(Tile<true, TEMP, false, F32>(Tl));
             else
-                sweeps(Tile<false, TEMP>(Tl));
+                sweeps(Tile<false, TEMP, false, F32>(Tl));
         }
 
         // ---- write back the cells this CTA changed (full-state rows inside the world),
@@ -1307,7 +1536,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
     FSE_PT_FLUSH
 }
 
-#if !defined(FSE_TICK_TEMP_TU) && !defined(FSE_TICK_SEQ_TU)
+#if !defined(FSE_TICK_TEMP_TU) && !defined(FSE_TICK_SEQ_TU) && !defined(FSE_TICK_F32_TU)
 size_t colour_pass_smem(int C, int halo) {
     size_t RW = (size_t)C + 2 * halo, RHF = (size_t)C + 2 * halo, RHI = (size_t)C + halo + 10;
     size_t nid = RW * RHI, nfull = RW * RHF;
@@ -1317,20 +1546,41 @@ size_t colour_pass_smem(int C, int halo) {
 
 #endif
 
-template <int HALO, bool TEMP, bool SEQ = false>
+template <int HALO, bool TEMP, bool SEQ = false, bool F32 = false>
 static cudaError_t launch_t(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
                             const MatTable *mt, size_t sm, int grid, cudaStream_t s) {
     // opt in to the full shared-memory carve-out once per instantiation
     static size_t set = 0;
     if (set < sm) {
-        cudaFuncSetAttribute(k_colour_pass<HALO, TEMP, SEQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(k_colour_pass<HALO, TEMP, SEQ, F32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sm);
         set = sm;
     }
-    k_colour_pass<HALO, TEMP, SEQ><<<grid, CP_THREADS, sm, s>>>(worlds, items, n_items, iter, tk, mt);
+    k_colour_pass<HALO, TEMP, SEQ, F32><<<grid, CP_THREADS, sm, s>>>(worlds, items, n_items, iter, tk, mt);
     return cudaGetLastError();
 }
 
-#if defined(FSE_TICK_SEQ_TU)
+// Each translation unit that includes this file with one of the defines below
+// compiles one family of instantiations, so that they build in parallel.
+#if defined(FSE_TICK_F32_TU)
+// f32 liquid amounts (FSE_CFG_F32_FLUID), in the partitioned order (FSE_TICK_F32_TU
+// = 1) or in the reference's order (2)
+#define FSE_F32_SEQ (FSE_TICK_F32_TU == 2)
+#if FSE_TICK_F32_TU == 2
+cudaError_t launch_colour_pass_f32_seq(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
+                                       const MatTable *mt, int halo, size_t sm, int grid, cudaStream_t s, bool temp) {
+#else
+cudaError_t launch_colour_pass_f32(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
+                                   const MatTable *mt, int halo, size_t sm, int grid, cudaStream_t s, bool temp) {
+#endif
+    if (temp) {
+        if (halo == 5) return launch_t<5, true, FSE_F32_SEQ, true>(worlds, items, n_items, iter, tk, mt, sm, grid, s);
+        return launch_t<2, true, FSE_F32_SEQ, true>(worlds, items, n_items, iter, tk, mt, sm, grid, s);
+    }
+    if (halo == 5) return launch_t<5, false, FSE_F32_SEQ, true>(worlds, items, n_items, iter, tk, mt, sm, grid, s);
+    return launch_t<2, false, FSE_F32_SEQ, true>(worlds, items, n_items, iter, tk, mt, sm, grid, s);
+}
+#elif defined(FSE_TICK_SEQ_TU)
 cudaError_t launch_colour_pass_seq(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
                                    const MatTable *mt, int halo, size_t sm, int grid, cudaStream_t s, bool temp) {
     if (temp) {
@@ -1351,14 +1601,20 @@ cudaError_t launch_colour_pass_temp(const WorldDev *worlds, const uint32_t *item
                                     const MatTable *mt, int halo, size_t sm, int grid, cudaStream_t s);
 cudaError_t launch_colour_pass_seq(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
                                    const MatTable *mt, int halo, size_t sm, int grid, cudaStream_t s, bool temp);
+cudaError_t launch_colour_pass_f32(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
+                                   const MatTable *mt, int halo, size_t sm, int grid, cudaStream_t s, bool temp);
+cudaError_t launch_colour_pass_f32_seq(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
+                                       const MatTable *mt, int halo, size_t sm, int grid, cudaStream_t s, bool temp);
 
 cudaError_t launch_colour_pass(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
                                const MatTable *mt, int halo, int C, int threads, int grid, cudaStream_t s,
-                               bool temp, bool seq) {
+                               bool temp, bool seq, bool f32) {
     (void)threads;  // the colour pass always runs CP_THREADS threads (see above)
     size_t sm = colour_pass_smem(C, halo);
     if (n_items <= 0) return cudaSuccess;
     if (grid <= 0 || grid > n_items) grid = n_items;
+    if (f32 && seq) return launch_colour_pass_f32_seq(worlds, items, n_items, iter, tk, mt, halo, sm, grid, s, temp);
+    if (f32) return launch_colour_pass_f32(worlds, items, n_items, iter, tk, mt, halo, sm, grid, s, temp);
     if (seq) return launch_colour_pass_seq(worlds, items, n_items, iter, tk, mt, halo, sm, grid, s, temp);
     if (temp) return launch_colour_pass_temp(worlds, items, n_items, iter, tk, mt, halo, sm, grid, s);
     if (halo == 5) return launch_t<5, false>(worlds, items, n_items, iter, tk, mt, sm, grid, s);
@@ -1368,7 +1624,7 @@ cudaError_t launch_colour_pass(const WorldDev *worlds, const uint32_t *items, in
 
 }  // namespace fse
 
-#if defined(FSE_PHASE_CLOCKS) && !defined(FSE_TICK_TEMP_TU) && !defined(FSE_TICK_SEQ_TU)
+#if defined(FSE_PHASE_CLOCKS) && !defined(FSE_TICK_TEMP_TU) && !defined(FSE_TICK_SEQ_TU) && !defined(FSE_TICK_F32_TU)
 extern "C" int fse_debug_phase_clocks(unsigned long long out[16], int reset) {
     cudaDeviceSynchronize();
     cudaMemcpyFromSymbol(out, g_phase_clk, 16 * sizeof(unsigned long long));

@@ -43,8 +43,13 @@ __global__ void k_tiles_in(const WorldDev *__restrict__ wd, const MatTable *__re
         w.col[i] = col;
         w.fl[i] = (uint8_t)((moved ? MOVED : 0) | settle);
         if (mt_type(mt->a[id]) == T_SOUP) {
-            w.sc[i] = L.fluid >= 0 ? to_q16(*reinterpret_cast<const float *>(t + L.fluid)) : Q_DEFAULT;
-            w.df[i] = L.fluid_diff >= 0 ? to_q16(*reinterpret_cast<const float *>(t + L.fluid_diff)) : 0;
+            if (w.f32) {  // f32 amounts: the caller's floats as they are
+                w.sc[i] = L.fluid >= 0 ? *reinterpret_cast<const int32_t *>(t + L.fluid) : F_DEFAULT_BITS;
+                w.df[i] = L.fluid_diff >= 0 ? *reinterpret_cast<const int32_t *>(t + L.fluid_diff) : 0;
+            } else {
+                w.sc[i] = L.fluid >= 0 ? to_q16(*reinterpret_cast<const float *>(t + L.fluid)) : Q_DEFAULT;
+                w.df[i] = L.fluid_diff >= 0 ? to_q16(*reinterpret_cast<const float *>(t + L.fluid_diff)) : 0;
+            }
             if (w.tp) w.tp[i] = temp;
         } else {
             w.sc[i] = temp;
@@ -71,7 +76,10 @@ __global__ void k_tiles_out(const WorldDev *__restrict__ wd, const MatTable *__r
         const uint8_t f = w.fl[i];
         if (L.moved >= 0) t[L.moved] = (f & MOVED) ? 1 : 0;
         if (L.settle >= 0) t[L.settle] = (uint8_t)(f & SETTLE_MASK);
-        if (soup) {
+        if (soup && w.f32) {
+            if (L.fluid >= 0) *reinterpret_cast<int32_t *>(t + L.fluid) = w.sc[i];
+            if (L.fluid_diff >= 0) *reinterpret_cast<int32_t *>(t + L.fluid_diff) = w.df[i];
+        } else if (soup) {
             if (L.fluid >= 0) *reinterpret_cast<float *>(t + L.fluid) = (float)w.sc[i] * (1.0f / 65536.0f);
             if (L.fluid_diff >= 0) *reinterpret_cast<float *>(t + L.fluid_diff) = (float)w.df[i] * (1.0f / 65536.0f);
         }

@@ -102,6 +102,17 @@ typedef struct fse_config {
  * world::tick for every rule (liquid amounts in Q16.16 rather than f32); a tick
  * takes about 13 times longer. Worlds with it cannot join batches or servers. */
 #define FSE_CFG_REFERENCE_ORDER 8
+/* liquid amounts (MaterialInstance::fluidAmount) and pending diffs (fluidAmountDiff)
+ * are kept as the reference's own f32, computed with its float arithmetic (every
+ * operation separately rounded, no contraction), instead of Q16.16 fixed point: the
+ * scalar plane of a SOUP cell, the diff plane, particle scalars of SOUP tiles and the
+ * tile structs then hold f32 bit patterns. Deposits of liquid particles into liquid
+ * add their amounts cell by cell in particle-index order. With
+ * FSE_CFG_REFERENCE_ORDER the tick then equals the reference's world::tick bit for
+ * bit, liquids included. The ledger and census keep no fluid rows (f32 sums are not
+ * conserved); cell counts are kept as ever. Worlds with it cannot join servers, and
+ * a batch takes worlds of one kind only. */
+#define FSE_CFG_F32_FLUID 16
 
 /* One free particle (CellData, source/engine/game_utils/cells.h:15-36). 60 bytes. */
 typedef struct fse_particle {
@@ -109,7 +120,8 @@ typedef struct fse_particle {
     float target_x, target_y, target_force;
     int32_t lifetime, fade_time;
     uint32_t colour;
-    int32_t scalar; /* fluid amount (Q16.16) for SOUP tiles, temperature otherwise */
+    int32_t scalar; /* fluid amount (Q16.16, or f32 bits in FSE_CFG_F32_FLUID worlds) for SOUP tiles,
+                       temperature otherwise */
     uint16_t id;    /* material of the carried tile */
     uint8_t flags;  /* tile flags: bit7 moved, bits0-5 settle count */
     uint8_t bits;   /* bit0 phase, bit1 temporary, bits2-3 inObjectState */
@@ -203,7 +215,8 @@ typedef struct fse_tile_layout {
 /* MaterialInstance (game_datastruct.hpp:205-222) on LP64 targets, 40 bytes */
 #define FSE_TILE_LAYOUT_MATERIAL_INSTANCE {40, 0, 8, 16, 20, 22, 24, 28, 32}
 /* Load the whole grid from / store it into such an array (width * height tiles,
- * row-major): liquid amounts and diffs are rounded to the nearest 1/65536, the
+ * row-major): liquid amounts and diffs are rounded to the nearest 1/65536 (copied
+ * bit for bit in worlds created with FSE_CFG_F32_FLUID), the
  * settle count saturates at 63, a liquid's temperature is kept only by worlds with
  * FSE_CFG_TEMPERATURE. Download writes id, colour, temperature, moved and settle
  * count of every tile, the amounts of liquid tiles only, and (with a mat_table of

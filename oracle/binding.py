@@ -49,10 +49,10 @@ ORDER_SEQ = 0
 ORDER_PART = 1
 
 
-
 def make_ref():
     """Run oracle/Makefile's `ref` target on REFERENCE_ROOT."""
     subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + REFERENCE_ROOT], check=True)
+
 
 def build_oracle(force=False):
     """Compile the oracle with its Makefile (gcc, no reference sources)."""
@@ -125,6 +125,7 @@ class Oracle:
                 "om_material_set_factory_temperature": (i32, [i32, C.c_int32]),
                 "om_tick_temperature": (None, [vp]),
                 "om_world_set_temperature": (None, [vp, i32]),
+                "om_world_set_f32": (None, [vp, i32]),
                 "om_temperature_get": (None, [vp, vp]),
                 "om_temperature_set": (None, [vp, vp]),
                 "om_lz4_bound": (i32, [i32]),
@@ -330,6 +331,10 @@ class OracleWorld:
 
     def enable_temperature(self, on=True):
         self.lib.om_world_set_temperature(self.h_, 1 if on else 0)
+
+    def set_f32(self, on=True):
+        """f32 liquid amounts (the library's FSE_CFG_F32_FLUID); before generate / set_state."""
+        self.lib.om_world_set_f32(self.h_, 1 if on else 0)
 
     # -- render textures
     def render_enable(self):
@@ -615,6 +620,37 @@ def reference_world_tick(lib_path, oracle, ids, colours, temps, moved, cell_iter
     if np_ < 0:
         raise ValueError("the reference tick wrote outside the grid: the scene needs its solid border")
     return i2, c2, t2, m2, parts[: min(np_, cap)].copy(), draws.value
+
+
+def reference_world_tick_fluid(lib_path, oracle, ids, colours, temps, moved, amounts, diffs, settle, cell_iter, seed,
+                               tick, n_ticks=1):
+    """reference_world_tick with every cell's fluidAmount, fluidAmountDiff (f32) and
+    settleCount given and returned; particle rows have 17 ints, the last the carried
+    tile's fluidAmount bits."""
+    lib = C.CDLL(lib_path)
+    f = lib.ref_world_tick_fluid
+    f.restype = C.c_int
+    f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint32, C.c_uint32, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                  C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+    n, mats, special, react, inter = _reference_tables(oracle)
+    h, w = ids.shape
+    i2 = np.ascontiguousarray(ids, np.uint16).copy()
+    c2 = np.ascontiguousarray(colours, np.uint32).copy()
+    t2 = np.ascontiguousarray(temps, np.int32).copy()
+    m2 = np.ascontiguousarray(moved, np.uint8).copy()
+    a2 = np.ascontiguousarray(amounts, np.float32).copy()
+    d2 = np.ascontiguousarray(diffs, np.float32).copy()
+    s2 = np.ascontiguousarray(settle, np.uint8).copy()
+    cap = 1 << 16
+    parts = np.zeros((cap, 17), np.int32)
+    draws = C.c_longlong(0)
+    np_ = f(w, h, cell_iter, seed & 0xFFFFFFFF, tick & 0xFFFFFFFF, n_ticks, n, _ptr(mats), _ptr(special),
+            _ptr(np.ascontiguousarray(react)), len(inter), _ptr(np.ascontiguousarray(inter)), _ptr(i2), _ptr(c2),
+            _ptr(t2), _ptr(m2), _ptr(a2), _ptr(d2), _ptr(s2), _ptr(parts), cap, C.byref(draws))
+    if np_ < 0:
+        raise ValueError("the reference tick wrote outside the grid: the scene needs its solid border")
+    return i2, c2, t2, m2, a2, d2, s2, parts[: min(np_, cap)].copy(), draws.value
 
 
 def build_reference_render(force=False):

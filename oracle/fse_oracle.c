@@ -444,6 +444,9 @@ struct om_world {
     int32_t *flow;
     uint32_t *tex[5];
     float *pflow;
+    /* f32 liquid amounts and diffs (om_world_set_f32): the reference's own float
+     * arithmetic; the ledger and census keep no fluid rows */
+    int f32;
 };
 
 static inline void mark_dirty(om_world *w, size_t i) {
@@ -456,6 +459,32 @@ static inline void add_flow(om_world *w, int x, int y, int axis, int32_t v) {
 }
 
 static inline int inw(const om_world *w, int x, int y) { return x >= 0 && y >= 0 && x < w->W && y < w->H; }
+
+/* f32 bit patterns of the 32-bit planes (f32 worlds) */
+static inline float i2f(int32_t v) {
+    float f;
+    memcpy(&f, &v, 4);
+    return f;
+}
+static inline int32_t f2i(float f) {
+    int32_t v;
+    memcpy(&v, &f, 4);
+    return v;
+}
+/* the amount of a new SOUP tile: the factory's Q16.16 scalar, or its f32 value in f32
+ * worlds (a temperature for other materials) */
+static inline int32_t soup_scalar(const om_world *w, int mid) {
+    if (!w->f32 || M[mid].type != T_SOUP) return M[mid].f_scalar;
+    return f2i((float)M[mid].f_scalar * (1.0f / 65536.0f));
+}
+/* f32 worlds: flowX / flowY of a cell as float bits, added in the reference's order */
+static inline void add_flow_f(om_world *w, int x, int y, int axis, float v, int sub) {
+    if (!w->flow || x < 0 || y < 0 || x >= w->W || y >= w->H) return;
+    int32_t *f = &w->flow[2 * ((size_t)y * w->W + x) + axis];
+    *f = f2i(sub ? i2f(*f) - v : i2f(*f) + v);
+}
+
+void om_world_set_f32(om_world *w, int on) { w->f32 = on ? 1 : 0; }
 
 om_world *om_world_new(int w, int h, int chunk, int cell_iter, uint32_t seed) {
     if (w <= 0 || h <= 0 || chunk < 16 || cell_iter < 0) return NULL;
@@ -647,6 +676,7 @@ static inline uint32_t D(rctx *c) { return draw_k(c->ck, c->k++); }
 
 static inline void led_add(rctx *c, int row, int mat, int64_t v) {
     if (mat < 0 || M[mat].type == T_AIR || v == 0) return;
+    if (c->w->f32 && row >= LED_CF) return; /* f32 amounts: no fluid rows */
 #pragma omp atomic
     c->led[row][mat] += v;
 }
@@ -668,7 +698,7 @@ static cell_t create_tile(rctx *c, int mid) {
     t.id = (uint16_t)mid;
     t.fl = 0;
     t.df = 0;
-    t.sc = m->f_scalar;
+    t.sc = soup_scalar(c->w, mid);
     t.tp = (m->type == T_SOUP) ? (int16_t)m->f_temp : 0;
     t.col = m->f_base;
     if (m->f_mod > 0) t.col = m->f_base + ((uint32_t)(m->f_lo + (int)(D(c) % (uint32_t)m->f_mod)) << m->f_shift);
@@ -711,6 +741,164 @@ static inline int32_t clampflow(int32_t flow, int32_t rem) {
     int32_t lim = rem < Q_MAXFLOW ? rem : Q_MAXFLOW;
     if (flow > lim) flow = lim;
     return flow;
+}
+
+/* CalculateVerticalFlowValue, world.cpp:1021-1034, in the reference's f32 (every
+ * operation rounded on its own: the oracle is built with -ffp-contract=off) */
+static inline float vflow_f(float rem, float dst) {
+    float sum = rem + dst;
+    if (sum <= 0.5f) return 0.5f;
+    if (sum < 2 * 0.5f + 0.1f) return (0.5f * 0.5f + sum * 0.1f) / (0.5f + 0.1f);
+    return (sum + 0.1f) / 2.0f;
+}
+/* std::max(flow, 0.0f) and the std::min(FLUID_MaxFlow, rem) cap, world.cpp:1320-1321;
+ * the FLUID_FlowSpeed factor (1.0f) changes no float */
+static inline float clampflow_f(float flow, float rem) {
+    if (flow < 0.0f) flow = 0.0f;
+    float lim = rem < 8.0f ? rem : 8.0f;
+    return flow > lim ? lim : flow;
+}
+/* one f32 flow from (x, y) towards (x + dx, y + dy), world.cpp:1309-1460 */
+static void soup_flow_f(rctx *c, const cell_t *t, float *rem, float *dfv, float flow, int nT, int x, int y, int dx,
+                        int dy) {
+    om_world *w = c->w;
+    if (flow == 0.0f) return;
+    *rem -= flow;
+    *dfv -= flow;
+    if (nT == T_AIR) {
+        cell_t nt = {t->id, 0, f2i(0.0f), t->col, f2i(0.0f + flow), t->tp};
+        pcell(w, x + dx, y + dy, nt);
+        led_add(c, LED_CN, t->id, 1);
+    } else if (inw(w, x + dx, y + dy)) {
+        chk(w, x + dx, y + dy, 1);
+        int32_t *d = &w->df[(size_t)(y + dy) * w->W + x + dx];
+        *d = f2i(i2f(*d) + flow);
+    }
+    add_flow_f(w, x, y, dx != 0 ? 0 : 1, flow, (dx + dy) < 0);
+}
+/* world.cpp:1269-1567 with f32 amounts; the cell's diff (t->df) already holds the
+ * flows of the cells updated before it, and its own flows are subtracted in order */
+static void rule_a_soup_f32(rctx *c, cell_t t, int x, int y) {
+    om_world *w = c->w;
+    float amount = i2f(t.sc);
+    if (amount == 0.0f) return;
+    if (amount < 0.0005f) {
+        t.sc = f2i(0.0f);
+        pcell(w, x, y, t);
+        return;
+    }
+    if ((double)amount > 0.005 && gtype(w, x, y + 1) == T_AIR && gtype(w, x, y + 2) == T_AIR &&
+        gtype(w, x, y + 3) == T_AIR && gtype(w, x, y + 4) == T_AIR) { /* world.cpp:1283-1305 */
+        pcell(w, x, y, nothing());
+        int n = (int)(amount / 4);
+        if (n < 1) n = 1;
+        led_add(c, LED_CN, t.id, n - 1);
+        for (int i = 0; i < n; i++) {
+            cell_t nt = t;
+            nt.sc = f2i(amount / (float)n);
+            nt.df = 0;
+            nt.fl = 0;
+            float vx = (float)((int)(D(c) % 10) - 5) / 30.0f;
+            float vy = (float)(-((int)(D(c) % 2) + 3)) / 10.0f + 1.0f;
+            spawn(c, nt, x, y + 1, vx, vy, 0.0f, 0.1f, 0, 0, 60);
+        }
+        return;
+    }
+    if (t.fl & MOVED) return;
+    float start = amount, rem = amount, dfv = i2f(t.df);
+    cell_t bottom = gcell(w, x, y + 1);
+    int bT = M[bottom.id].type;
+    int airBelow = bT == T_AIR;
+    if ((airBelow && c->iter <= 2) || bottom.id == t.id) {
+        float dst = (bT == T_SOUP) ? i2f(bottom.sc) : 0.0f;
+        soup_flow_f(c, &t, &rem, &dfv, clampflow_f(vflow_f(start, dst) - dst, start), bT, x, y, 0, 1);
+    } else if (c->iter == 0 && bT == T_SOUP && bottom.id != t.id) {
+        if (D(c) % 10 == 0) {
+            t.df = f2i(dfv);
+            pcell(w, x, y, bottom);
+            pcell(w, x, y + 1, t);
+            return;
+        }
+    }
+    if (rem < 0.0005f) {
+        t.df = f2i(dfv - rem);
+        pcell(w, x, y, t);
+        return;
+    }
+    cell_t left = gcell(w, x - 1, y);
+    int lT = M[left.id].type;
+    int canL = (lT == T_AIR || left.id == t.id) && !airBelow;
+    cell_t right = gcell(w, x + 1, y);
+    int rT = M[right.id].type;
+    int canR = (rT == T_AIR || right.id == t.id) && !airBelow;
+    if (canL) {
+        float dst = (lT == T_SOUP) ? i2f(left.sc) : 0.0f;
+        soup_flow_f(c, &t, &rem, &dfv, clampflow_f((rem - dst) / (canR ? 3.0f : 2.0f), rem), lT, x, y, -1, 0);
+    }
+    if (rem < 0.0005f) {
+        t.df = f2i(dfv - rem);
+        pcell(w, x, y, t);
+        return;
+    }
+    if (canR) {
+        float dst = (rT == T_SOUP) ? i2f(right.sc) : 0.0f;
+        soup_flow_f(c, &t, &rem, &dfv, clampflow_f((rem - dst) / 2.0f, rem), rT, x, y, 1, 0);
+    }
+    if (rem < 0.0005f) {
+        t.df = f2i(dfv - rem);
+        pcell(w, x, y, t);
+        return;
+    }
+    cell_t top = gcell(w, x, y - 1);
+    int tT = M[top.id].type;
+    if (tT == T_AIR || top.id == t.id) {
+        float dst = (tT == T_SOUP) ? i2f(top.sc) : 0.0f;
+        soup_flow_f(c, &t, &rem, &dfv, clampflow_f(rem - vflow_f(rem, dst), rem), tT, x, y, 0, -1);
+    } else if (c->iter == 0 && tT == T_SOUP && top.id != t.id) {
+        if (D(c) % 10 == 0) {
+            t.df = f2i(dfv);
+            pcell(w, x, y, top);
+            pcell(w, x, y - 1, t);
+            return;
+        }
+    }
+    if (rem < 0.0005f) {
+        t.df = f2i(dfv - rem);
+        pcell(w, x, y, t);
+        return;
+    }
+    if (start == rem) { /* world.cpp:1472-1483 */
+        uint8_t s = t.fl & SETTLE_MASK;
+        if (s < SETTLE_MASK) s++;
+        t.fl = (uint8_t)((t.fl & ~SETTLE_MASK) | s);
+        if (s >= 10) t.fl |= MOVED;
+    } else {
+        if (tT == T_SOUP) set_moved(w, x, y - 1, 0);
+        if (bT == T_SOUP) set_moved(w, x, y + 1, 0);
+        if (lT == T_SOUP) set_moved(w, x - 1, y, 0);
+        if (rT == T_SOUP) set_moved(w, x + 1, y, 0);
+    }
+    t.df = f2i(dfv);
+    pcell(w, x, y, t);
+    /* WATER on LAVA, world.cpp:1519-1537 */
+    if ((int)t.id == ID_WATER && gid(w, x, y + 1) == ID_LAVA) {
+        cell_t st = create_tile(c, ID_STEAM);
+        led_replace(c, t, st);
+        pcell(w, x, y, st);
+        cell_t ob = create_tile(c, ID_OBSIDIAN);
+        led_replace(c, gcell(w, x, y + 1), ob);
+        pcell(w, x, y + 1, ob);
+        setvis(w, x, y + 1);
+        for (int xx = -1; xx <= 1; xx++)
+            for (int yy = 0; yy <= 2; yy++) {
+                if (gid(w, x + xx, y + yy) == ID_LAVA) {
+                    cell_t o2 = create_tile(c, ID_OBSIDIAN);
+                    led_replace(c, gcell(w, x + xx, y + yy), o2);
+                    pcell(w, x + xx, y + yy, o2);
+                    setvis(w, x + xx, y + yy);
+                }
+            }
+    }
 }
 
 /* ---------------------------------------------------------------- sweep A */
@@ -844,6 +1032,8 @@ static void rule_a(rctx *c, int x, int y) {
                 }
             }
         }
+    } else if (type == T_SOUP && w->f32) {
+        rule_a_soup_f32(c, t, x, y);
     } else if (type == T_SOUP) { /* world.cpp:1269-1567 */
         if (t.sc == 0) return;
         if (t.sc < Q_MINV) {
@@ -1094,6 +1284,18 @@ static void rule_b(rctx *c, int x, int y) {
             setvis(w, x + 1, y + 1);
         } else {
             set_moved(w, x, y, 0);
+        }
+    } else if (type == T_SOUP && w->f32) { /* world.cpp:1728-1745 in f32 */
+        float a = i2f(t.sc) + i2f(t.df);
+        t.sc = f2i(a);
+        t.df = f2i(0.0f);
+        if (a < 0.0005f) {
+            led_add(c, LED_DN, t.id, 1);
+            pcell(w, x, y, nothing());
+            setvis(w, x, y);
+        } else {
+            pcell(w, x, y, t);
+            setvis(w, x, y);
         }
     } else if (type == T_SOUP) { /* world.cpp:1728-1745 */
         t.sc += t.df;
@@ -1422,6 +1624,16 @@ static int find_target(om_world *w, const om_particle *p, int kind, int lx, int 
     return 0;
 }
 
+typedef struct {
+    int64_t cell;
+    int part;
+} merge_t;
+static int merge_cmp(const void *a, const void *b) {
+    const merge_t *x = (const merge_t *)a, *y = (const merge_t *)b;
+    if (x->cell != y->cell) return x->cell < y->cell ? -1 : 1;
+    return x->part < y->part ? -1 : (x->part > y->part);
+}
+
 int om_particles_tick(om_world *w) {
     spiral_init();
     int n = w->parts.n;
@@ -1439,7 +1651,7 @@ int om_particles_tick(om_world *w) {
         req[i] = REQ_NONE;
         if (out == OUT_DEAD) {
             dead[i] = 1;
-            int64_t f = (M[P[i].id].type == T_SOUP) ? P[i].scalar : 0;
+            int64_t f = (M[P[i].id].type == T_SOUP && !w->f32) ? P[i].scalar : 0; /* f32: no fluid rows */
             if (r == -2) {
                 if (M[P[i].id].type != T_AIR) w->led[LED_XN][P[i].id] += 1;
                 w->led[LED_XF][P[i].id] += f;
@@ -1466,6 +1678,10 @@ int om_particles_tick(om_world *w) {
         claim = (int32_t *)malloc(ncell * sizeof(int32_t));
         for (size_t i = 0; i < ncell; i++) claim[i] = 0x7fffffff;
     }
+    /* f32 worlds: the deposits into liquid, applied after the rounds cell by cell in
+     * particle-index order (the reference's list order of its float adds) */
+    merge_t *mg = (merge_t *)malloc(((size_t)nreq + 1) * sizeof(merge_t));
+    int nmg = 0;
     DBG_ROUNDS = 0;
     while (nreq > 0) {
         if (DBG_ROUNDS < 256) DBG_OPEN[DBG_ROUNDS] = nreq;
@@ -1489,7 +1705,13 @@ int om_particles_tick(om_world *w) {
             }
             size_t ci = (size_t)ty[j] * w->W + tx[j];
             if (tk[j] == 2) { /* :2119-2125 */
-                w->sc[ci] += p->scalar;
+                if (w->f32) { /* added after the rounds, per cell in particle order */
+                    mg[nmg].cell = (int64_t)ci;
+                    mg[nmg].part = i;
+                    nmg++;
+                } else {
+                    w->sc[ci] += p->scalar;
+                }
                 mark_dirty(w, ci);
                 dead[i] = 1;
                 w->led[LED_DN][p->id] += 1;
@@ -1513,6 +1735,14 @@ int om_particles_tick(om_world *w) {
             if (tk[j] == 1) claim[(size_t)ty[j] * w->W + tx[j]] = 0x7fffffff;
         nreq = nn;
     }
+    if (nmg > 0) {
+        qsort(mg, (size_t)nmg, sizeof(merge_t), merge_cmp);
+        for (int k = 0; k < nmg; k++) {
+            int32_t *a = &w->sc[mg[k].cell];
+            *a = f2i(i2f(*a) + i2f(P[mg[k].part].scalar));
+        }
+    }
+    free(mg);
     /* phase 3: stable erase (std::erase_if, :2190) and the y > height erase (:2203) */
     int m = 0;
     for (int i = 0; i < n; i++) {
@@ -1656,7 +1886,7 @@ void om_world_generate(om_world *w, int kind, uint32_t seed) {
             w->id[i] = (uint16_t)mid;
             w->fl[i] = 0;
             w->df[i] = 0;
-            w->sc[i] = m->f_scalar;
+            w->sc[i] = soup_scalar(w, w->id[i]);
             w->tp[i] = (m->type == T_SOUP) ? (int16_t)m->f_temp : 0;
             w->col[i] = m->f_base;
             if (m->f_mod > 0)
@@ -1993,7 +2223,7 @@ int om_world_unpack(om_world *w, const uint8_t *in, const int64_t *offsets, int 
             w->fl[i] = 0;
             w->df[i] = 0;
             if (M[id].type == T_SOUP) {
-                w->sc[i] = Q_DEFAULT;
+                w->sc[i] = w->f32 ? f2i(2.0f) : Q_DEFAULT;
                 w->tp[i] = t;
             } else {
                 w->sc[i] = t;
@@ -2058,7 +2288,9 @@ void om_render_dirty(om_world *w, int64_t *moving) {
         if ((int)w->id[i] == ID_FIRE) w->tex[2][i] = rgba(col >> 16, col >> 8, col, (uint32_t)m->alpha);
         if (m->type == T_SOUP) {
             float *pf = &w->pflow[2 * i];
-            float fx = (float)fl[0] * (1.0f / 65536.0f), fy = (float)fl[1] * (1.0f / 65536.0f);
+            /* the tick's flow sums: f32 in f32 worlds, else Q16.16 */
+            float fx = w->f32 ? i2f(fl[0]) : (float)fl[0] * (1.0f / 65536.0f);
+            float fy = w->f32 ? i2f(fl[1]) : (float)fl[1] * (1.0f / 65536.0f);
             /* f32 + (f32 - f32) * 0.25 evaluated in double, stored as f32 */
             float nfx = (float)((double)pf[0] + (double)(fx - pf[0]) * 0.25);
             float nfy = (float)((double)pf[1] + (double)(fy - pf[1]) * 0.25);
@@ -2123,12 +2355,12 @@ void om_census(const om_world *w, int64_t *out) {
     for (size_t i = 0; i < n; i++) {
         int id = w->id[i];
         out[id] += 1;
-        if (M[id].type == T_SOUP) out[NMAT + id] += (int64_t)w->sc[i] + w->df[i];
+        if (M[id].type == T_SOUP && !w->f32) out[NMAT + id] += (int64_t)w->sc[i] + w->df[i];
     }
     for (int i = 0; i < w->parts.n; i++) {
         int id = w->parts.p[i].id;
         out[2 * NMAT + id] += 1;
-        if (M[id].type == T_SOUP) out[3 * NMAT + id] += w->parts.p[i].scalar;
+        if (M[id].type == T_SOUP && !w->f32) out[3 * NMAT + id] += w->parts.p[i].scalar;
     }
 }
 
@@ -2185,7 +2417,7 @@ void om_object_stamp(om_world *w, om_body *bodies, int n) {
                     pv_push(&w->parts, &p);
                     if (ty == T_SOUP) {
                         /* the cell's pending diff leaves with it */
-                        w->led[LED_DF][p.id] += w->df[ci];
+                        if (!w->f32) w->led[LED_DF][p.id] += w->df[ci];
                         bd->n_soup++;
                     } else
                         bd->n_sand++;

@@ -101,6 +101,9 @@ void om_world_step(om_world *wd, int order, int n);
 void om_tick_temperature(om_world *wd);
 /* om_world_step also runs om_tick_temperature after ticks whose index is 2 mod 4 */
 void om_world_set_temperature(om_world *wd, int on);
+/* f32 liquid amounts and diffs: the reference's own float arithmetic (the GPU's
+ * FSE_CFG_F32_FLUID); set before the world is generated or loaded */
+void om_world_set_f32(om_world *wd, int on);
 /* chunk .pack codec (chunk.cpp:219-330): LZ4 block format helpers and whole-world
  * pack/unpack, chunks row-major; see fse_oracle.c for the layout */
 int om_lz4_bound(int n);

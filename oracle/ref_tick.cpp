@@ -364,10 +364,15 @@ static void setup_registry(Registry &reg, int n, const int32_t *mats, const int3
 
 }
 
-extern "C" int ref_world_tick(int W, int H, int cell_iter, uint32_t seed, uint32_t tick, int n_ticks, int n,
-                              const int32_t *mats, const int32_t *special, const int32_t *reactions, int ni,
-                              const int32_t *inter, uint16_t *ids, uint32_t *cols, int32_t *temps, uint8_t *moved,
-                              int32_t *parts, int cap, long long *draws) {
+// n_ticks world::tick() calls on a grid given as planes. amounts / diffs / settle
+// (NULL: the MaterialInstance defaults 2.0, 0, 0) are each cell's fluidAmount,
+// fluidAmountDiff and settleCount, read and written back as they are; particle rows
+// hold `row` ints (16, or 17 with the carried tile's fluidAmount bits last).
+static int tick_planes(int W, int H, int cell_iter, uint32_t seed, uint32_t tick, int n_ticks, int n,
+                       const int32_t *mats, const int32_t *special, const int32_t *reactions, int ni,
+                       const int32_t *inter, uint16_t *ids, uint32_t *cols, int32_t *temps, uint8_t *moved,
+                       float *amounts, float *diffs, uint8_t *settle, int32_t *parts, int row, int cap,
+                       long long *draws) {
     Registry reg;
     setup_registry(reg, n, mats, special, reactions, ni, inter);
 
@@ -379,6 +384,9 @@ extern "C" int ref_world_tick(int W, int H, int cell_iter, uint32_t seed, uint32
     for (size_t i = 0; i < N; i++) {
         MaterialInstance t(g_reg.materials_container[ids[i]], cols[i], (mat_temperature)temps[i]);
         t.moved = moved[i] != 0;
+        if (amounts) t.fluidAmount = amounts[i];
+        if (diffs) t.fluidAmountDiff = diffs[i];
+        if (settle) t.settleCount = settle[i];
         tiles[pad + i] = t;
     }
     world wd;
@@ -410,11 +418,14 @@ extern "C" int ref_world_tick(int W, int H, int cell_iter, uint32_t seed, uint32
         cols[i] = t.color;
         temps[i] = t.temperature;
         moved[i] = t.moved ? 1 : 0;
+        if (amounts) amounts[i] = t.fluidAmount;
+        if (diffs) diffs[i] = t.fluidAmountDiff;
+        if (settle) settle[i] = t.settleCount;
     }
     int np = 0;
     for (CellData *c : wd.cells) {
         if (np < cap) {
-            int32_t *o = parts + 16 * np;
+            int32_t *o = parts + (size_t)row * np;
             const f32 fv[9] = {c->x, c->y, c->vx, c->vy, c->ax, c->ay, c->targetX, c->targetY, c->targetForce};
             o[0] = (int32_t)c->tile.mat->id;
             o[1] = (int32_t)c->tile.color;
@@ -424,12 +435,32 @@ extern "C" int ref_world_tick(int W, int H, int cell_iter, uint32_t seed, uint32
             o[13] = c->temporary;
             o[14] = c->lifetime;
             o[15] = c->fadeTime;
+            if (row > 16) memcpy(o + 16, &c->tile.fluidAmount, 4);
         }
         np++;
         delete c;
     }
     if (draws) *draws = g_draws;
     return ok ? np : -1;
+}
+
+extern "C" int ref_world_tick(int W, int H, int cell_iter, uint32_t seed, uint32_t tick, int n_ticks, int n,
+                              const int32_t *mats, const int32_t *special, const int32_t *reactions, int ni,
+                              const int32_t *inter, uint16_t *ids, uint32_t *cols, int32_t *temps, uint8_t *moved,
+                              int32_t *parts, int cap, long long *draws) {
+    return tick_planes(W, H, cell_iter, seed, tick, n_ticks, n, mats, special, reactions, ni, inter, ids, cols, temps,
+                       moved, nullptr, nullptr, nullptr, parts, 16, cap, draws);
+}
+
+// the same with every cell's fluidAmount, fluidAmountDiff and settleCount in and out,
+// and particle rows of 17 ints (the carried tile's fluidAmount bits last)
+extern "C" int ref_world_tick_fluid(int W, int H, int cell_iter, uint32_t seed, uint32_t tick, int n_ticks, int n,
+                                    const int32_t *mats, const int32_t *special, const int32_t *reactions, int ni,
+                                    const int32_t *inter, uint16_t *ids, uint32_t *cols, int32_t *temps,
+                                    uint8_t *moved, float *amounts, float *diffs, uint8_t *settle, int32_t *parts,
+                                    int cap, long long *draws) {
+    return tick_planes(W, H, cell_iter, seed, tick, n_ticks, n, mats, special, reactions, ni, inter, ids, cols, temps,
+                       moved, amounts, diffs, settle, parts, 17, cap, draws);
 }
 
 // Timing: the reference's own world::tick() + world::tickCells() on a grid (ids,

@@ -101,3 +101,39 @@ CASES = [
     (256, 384, 14, "fire", 3, 2),
     (256, 256, 15, "sand", 1, 4),
 ]
+
+
+def scene_f32(ids, w, h, seed):
+    """The liquid scene with the reference's own f32 liquid state: amounts spread over
+    (0, 4) with exact zeros, values below FLUID_MinValue and near the free-fall and
+    vertical-flow thresholds; small pending diffs on some cells; settle counts 0-15.
+    Returns the planes of scene() (scalar and diff of liquid cells as f32 bit
+    patterns) plus the float planes "amount" and "fluid_diff" and "settle"."""
+    st = scene(ids, w, h, seed, "liquid")
+    rng = np.random.default_rng(seed + 1000)
+    amount = rng.uniform(0.0, 4.0, (h, w)).astype(np.float32)
+    pick = rng.random((h, w))
+    amount[pick < 0.03] = 0.0
+    amount[(pick >= 0.03) & (pick < 0.06)] = rng.uniform(0.0, 0.001, (h, w)).astype(np.float32)[
+        (pick >= 0.03) & (pick < 0.06)]
+    amount[(pick >= 0.06) & (pick < 0.09)] = np.float32(0.5)
+    amount[(pick >= 0.09) & (pick < 0.12)] = np.float32(2.0)
+    diff = np.where(rng.random((h, w)) < 0.2, rng.uniform(-0.3, 0.3, (h, w)), 0.0).astype(np.float32)
+    settle = rng.integers(0, 16, (h, w)).astype(np.uint8)
+    soup = np.isin(st["id"], [ids["WATER"], ids["LAVA"]])
+    amount = np.where(soup, amount, np.float32(2.0)).astype(np.float32)
+    diff = np.where(soup, diff, np.float32(0.0)).astype(np.float32)
+    settle = np.where(soup, settle, 0).astype(np.uint8)
+    st["scalar"] = np.where(soup, amount.view(np.int32), st["scalar"]).astype(np.int32)
+    st["diff"] = np.where(soup, diff.view(np.int32), 0).astype(np.int32)
+    st["flags"] = (st["flags"] & 0x80) | np.where(soup, settle, 0).astype(np.uint8)
+    st["amount"], st["fluid_diff"], st["settle"] = amount, diff, settle
+    return st
+
+
+# f32 liquid scenes: (w, h, seed, cell_iter, ticks)
+F32_CASES = [
+    (256, 256, 21, 3, 1),
+    (384, 256, 22, 3, 3),
+    (256, 384, 23, 2, 6),
+]
