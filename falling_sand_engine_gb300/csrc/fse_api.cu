@@ -709,8 +709,8 @@ static void free_world(fse_world *w) {
     for (auto &g : w->graphs) cudaGraphExecDestroy(g.second);
     w->graphs.clear();
     WorldDev &h = w->h;
-    void *ptrs[] = {h.id, h.col, h.sc, h.fl, h.df, h.tp, h.tnew, h.stage, h.cp_count, h.cp_base, h.p_state, h.p_lxly,
-                    h.req_list, h.req_list2, h.req_target, h.scan_tmp, h.ledger, h.airmap, w->ctr, w->d, w->claim,
+    void *ptrs[] = {h.id, h.col, h.sc, h.fl, h.df, h.tp, h.tnew, h.stage, h.cp_count, h.cp_base, h.p_state, h.p_box0,
+                    h.p_box1, h.p_cell, h.p_prev, h.chg, h.scan_tmp, h.ledger, h.airmap, w->ctr, w->d, w->claim,
                     w->mask_bits, w->obj_list, w->obj_n, h.merge_list, h.merge_count, h.merge_claim};
     for (void *q : ptrs)
         if (q) cudaFree(q);
@@ -810,10 +810,12 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
     bool ok = dalloc(w, &h.id, n) && dalloc(w, &h.col, n) && dalloc(w, &h.sc, n) && dalloc(w, &h.fl, n) &&
               dalloc(w, &h.df, n) && dalloc(w, &h.stage, (size_t)h.stage_cap) && dalloc(w, &h.cp_count, ncp) &&
               dalloc(w, &h.cp_base, ncp) && dalloc(w, &w->ctr, 16) && dalloc(w, &h.ledger, LED_ROWS * MAXMAT) &&
-              dalloc(w, &h.p_state, (size_t)h.part_cap) && dalloc(w, &h.p_lxly, (size_t)h.part_cap) &&
-              dalloc(w, &h.req_list, (size_t)h.part_cap) && dalloc(w, &h.req_list2, 2 * (size_t)h.part_cap) &&
-              dalloc(w, &h.req_target, (size_t)h.part_cap) && dalloc(w, &h.scan_tmp, particle_scan_blocks() + 1) &&
-              dalloc(w, &h.airmap, (size_t)h.amw * h.amh) && dalloc(w, &w->d, 1);
+              dalloc(w, &h.p_state, (size_t)h.part_cap) && dalloc(w, &h.p_box0, (size_t)h.part_cap) &&
+              dalloc(w, &h.p_box1, (size_t)h.part_cap) && dalloc(w, &h.p_cell, (size_t)h.part_cap) &&
+              dalloc(w, &h.p_prev, (size_t)h.part_cap) && dalloc(w, &h.scan_tmp, particle_scan_blocks() + 1) &&
+              dalloc(w, &h.airmap, (size_t)h.amw * h.amh) && dalloc(w, &h.chg, 2 * (size_t)h.amw * h.amh) &&
+              dalloc(w, &h.merge_list, 2 * (size_t)h.part_cap) && dalloc(w, &h.merge_count, 1) &&
+              dalloc(w, &w->d, 1);
     PartSoA *ps[2] = {&h.p, &h.q};
     size_t pc = (size_t)h.part_cap;
     for (int k = 0; k < 2 && ok; k++) {
@@ -833,11 +835,8 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
     }
     if (ok && (c.flags & FSE_CFG_F32_FLUID)) {  // f32 amounts, deposits into liquid merged in index order
         h.f32 = 1;
-        ok = dalloc(w, &h.merge_list, 2 * pc) && dalloc(w, &h.merge_count, 1) && dalloc(w, &h.merge_claim, n);
-        if (ok) {
-            cudaMemset(h.merge_count, 0, sizeof(int32_t));
-            cudaMemset(h.merge_claim, 0xFF, n * sizeof(uint32_t));
-        }
+        ok = dalloc(w, &h.merge_claim, n);
+        if (ok) cudaMemset(h.merge_claim, 0xFF, n * sizeof(uint32_t));
     }
     if (ok && (c.flags & FSE_CFG_RENDER)) {
         ok = dalloc(w, &h.dirty, n) && dalloc(w, &h.flow, 2 * n) && dalloc(w, &w->pflow, 2 * n) &&
@@ -874,6 +873,7 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
     cudaMemset(w->ctr, 0, 16 * sizeof(int32_t));
     cudaMemset(h.ledger, 0, LED_ROWS * MAXMAT * sizeof(long long));
     cudaMemset(h.cp_count, 0, ncp * sizeof(int32_t));
+    cudaMemset(h.merge_count, 0, sizeof(int32_t));
     // an empty world: GENERIC_AIR everywhere (world.cpp:133-145)
     cudaMemset(h.id, 0, n * 2);
     cudaMemset(h.col, 0, n * 4);

@@ -453,7 +453,8 @@ static int64_t world_footprint(int w, int h, const fse_config *cfg) {
     long long cells = (long long)w * h;
     long long pc = (cfg && cfg->particle_capacity > 0) ? cfg->particle_capacity : std::max<long long>(65536, cells / 4);
     long long sc = (cfg && cfg->spawn_capacity > 0) ? cfg->spawn_capacity : pc;
-    return cells * 15 + pc * (2 * 56 + 1 + 4 * 5) + sc * (long long)sizeof(SpawnRec) + (1 << 20);
+    // planes; two particle SoAs, the outcome byte, four outcome words and two merge-list words
+    return cells * 15 + pc * (2 * 56 + 1 + 4 * 6) + sc * (long long)sizeof(SpawnRec) + (1 << 20);
 }
 
 extern "C" {

@@ -95,7 +95,7 @@ cudaError_t launch_colour_pass(const WorldDev *worlds, const uint32_t *items, in
 cudaError_t launch_spawn_append(WorldDev *d_worlds, int n_worlds, int stage_blocks, cudaStream_t s);
 cudaError_t launch_particle_tick(WorldDev *d_worlds, int n_worlds, const MatTable *mt, int move_blocks,
                                  cudaStream_t s);
-constexpr int PARTICLE_TICK_LAUNCHES = 13;  // kernels launch_particle_tick issues
+constexpr int PARTICLE_TICK_LAUNCHES = 8;  // kernels launch_particle_tick issues
 // world::tickTemperature over a set of worlds (max_tiles: the most 128 x 32 tiles of
 // any of them); gated: only worlds with temp_on, after ticks whose index is 2 mod 4
 cudaError_t launch_temperature(const WorldDev *d_worlds, int n_worlds, int max_tiles, const MatTable *mt, bool gated,

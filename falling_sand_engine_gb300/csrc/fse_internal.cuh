@@ -165,12 +165,13 @@ struct WorldDev {
     PartSoA p, q;           // p = live list, q = compaction scratch
     int32_t *part_count;    // device-resident live count
     int32_t part_cap;
-    uint8_t *p_state;       // per particle: 0 alive, 1 dead, 2 open deposit request
-    int32_t *p_lxly;        // packed start cell of the request (ly * W + lx)
-    int32_t *req_list;      // open deposit requests (particle indices)
-    int32_t *req_count;     // [2] ping-pong counts
-    int32_t *req_list2;
-    int32_t *req_target;    // per request: target cell, or -1
+    uint8_t *p_state;       // per particle: 0 alive, 1 dead; during the update its outcome
+    // per particle during the update: the cells it read as a box (x0 | y0 << 16 and
+    // x1 | y1 << 16; box0 -1: none), the cell it fills or merges into (-1: none), the
+    // fill cell an iteration moved it away from; box0 holds the merge cell afterwards
+    int32_t *p_box0, *p_box1, *p_cell, *p_prev;
+    int32_t *req_count;     // [3] counters of the update (fill changes of even / odd iterations)
+    uint8_t *chg;           // 2 x airmap blocks: blocks whose fills changed (read / written by an iteration)
     int32_t *scan_tmp;      // block sums for compaction
     long long *ledger;      // [LED_ROWS][MAXMAT]
     int32_t *err;
@@ -188,10 +189,10 @@ struct WorldDev {
     // FSE_CFG_F32_FLUID: liquid amounts and pending diffs are f32 (the reference's
     // own arithmetic) rather than Q16.16; the ledger then keeps no fluid rows
     int f32;
-    // f32 worlds: deposits of liquid particles into liquid cells, applied after the
-    // deposit rounds cell by cell in particle-index order (particle indices; the
-    // target cell is in p_lxly), and per-cell claims of that pass (all ones between
-    // ticks)
+    // deposits of liquid particles into liquid cells, applied after the update
+    // (particle indices, 2 x part_cap for the ordered rounds; the target cell is in
+    // p_box0), and in f32 worlds the per-cell claims of those rounds (all ones
+    // between ticks)
     int32_t *merge_list;
     int32_t *merge_count;
     uint32_t *merge_claim;

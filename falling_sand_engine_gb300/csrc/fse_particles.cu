@@ -17,7 +17,7 @@ constexpr int PART_BLOCKS = 512;  // blocks per world for the particle list kern
 constexpr int PART_THREADS = 256;
 
 // p_state values
-enum : uint8_t { PS_ALIVE = 0, PS_DEAD = 1, PS_DIRECT = 2, PS_SPIRAL = 3 };
+enum : uint8_t { PS_ALIVE = 0, PS_DEAD = 1 };
 
 __constant__ int8_t c_spiral[1024][2];
 __constant__ int c_spiral_n;
@@ -124,143 +124,56 @@ __device__ __forceinline__ void led_part(const WorldDev &w, const MatTable *mt, 
         atomicAdd((unsigned long long *)&w.ledger[row_f * MAXMAT + id], (unsigned long long)(long long)sc);
 }
 
-// world.cpp:2032-2188 for every particle against the grid left by the cell tick;
-// collisions become deposit requests resolved by the kernels below.
-__device__ __forceinline__ void load_types(uint8_t *s_type, const MatTable *mt);
-
-__global__ void k_part_move(const WorldDev *__restrict__ worlds, const MatTable *__restrict__ mt) {
-    __shared__ uint8_t s_type[MAXMAT];
-    load_types(s_type, mt);
-    const WorldDev &w = worlds[blockIdx.y];
-    const int n = *w.part_count;
-    const int W = w.W, H = w.H;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint8_t bits = w.p.bits[i];
-        int32_t life = w.p.life[i];
-        if ((bits & 2) && life <= 0) {  // :2033-2037
-            w.p_state[i] = PS_DEAD;
-            led_part(w, mt, LED_DN, LED_DF, w.p.id[i], w.p.sc[i]);
-            continue;
-        }
-        float x = w.p.x[i], y = w.p.y[i], vx = w.p.vx[i], vy = w.p.vy[i];
-        float tf = w.p.tf[i];
-        if (tf != 0.f) {  // :2039-2051
-            float tdx = __fsub_rn(w.p.tx[i], x), tdy = __fsub_rn(w.p.ty[i], y);
-            float nf = __fsqrt_rn(__fadd_rn(__fmul_rn(tdx, tdx), __fmul_rn(tdy, tdy)));
-            vx = __fadd_rn(vx, __fmul_rn(__fdiv_rn(tdx, nf), tf));
-            vy = __fadd_rn(vy, __fmul_rn(__fdiv_rn(tdy, nf), tf));
-            if (nf < 100.f) {
-                vx = __fmul_rn(vx, 0.95f);
-                vy = __fmul_rn(vy, 0.95f);
-            }
-        }
-        uint8_t st = PS_ALIVE;
-        if (out_of_world(x, y, W, H)) {  // :2056-2059
-            w.p_state[i] = PS_DEAD;
-            w.p.vx[i] = vx;
-            w.p.vy[i] = vy;
-            led_part(w, mt, LED_XN, LED_XF, w.p.id[i], w.p.sc[i]);
-            continue;
-        }
-        const int lx = (int)x, ly = (int)y;
-        vx = __fadd_rn(vx, w.p.ax[i]);  // :2063-2064
-        vy = __fadd_rn(vy, w.p.ay[i]);
-        const int div = (int)__fadd_rn(__fadd_rn(fabsf(vx), fabsf(vy)), 1.0f);
-        const float dvx = __fdiv_rn(vx, (float)div), dvy = __fdiv_rn(vy, (float)div);
-        bool done = false;
-        for (int s = 0; s < div && !done; s++) {  // :2071-2184
-            x = __fadd_rn(x, dvx);
-            y = __fadd_rn(y, dvy);
-            if (out_of_world(x, y, W, H)) {
-                st = PS_DEAD;
-                led_part(w, mt, LED_XN, LED_XF, w.p.id[i], w.p.sc[i]);
-                done = true;
-                break;
-            }
-            int ct = s_type[w.id[(size_t)(int)y * W + (int)x]];
-            if (!(bits & 1) && ct != T_AIR) {
-                bool isObject = ct == T_OBJECT;
-                int ps = (bits >> 2) & 3;
-                if (ps == 0)
-                    ps = isObject ? 1 : 2;
-                else if (ps == 1 && !isObject)
-                    ps = 2;
-                bits = (uint8_t)((bits & ~0x0Cu) | ((unsigned)ps << 2));
-                if (!isObject || ps == 2) {
-                    if (bits & 2) {
-                        st = PS_DEAD;
-                        led_part(w, mt, LED_DN, LED_DF, w.p.id[i], w.p.sc[i]);
-                    } else {
-                        st = (s_type[w.id[(size_t)ly * W + lx]] != T_AIR) ? PS_SPIRAL : PS_DIRECT;
-                    }
-                    done = true;
-                }
-            }
-        }
-        if (!done && life > 0) life--;  // :2186-2188
-        w.p.x[i] = x;
-        w.p.y[i] = y;
-        w.p.vx[i] = vx;
-        w.p.vy[i] = vy;
-        w.p.bits[i] = bits;
-        w.p.life[i] = life;
-        w.p_state[i] = st;
-        if (st == PS_DIRECT || st == PS_SPIRAL) {
-            w.p_lxly[i] = ly * W + lx;
-            int j = atomicAdd(&w.req_count[0], 1);
-            w.req_list[j] = i;
-        }
-    }
-}
-
-// ------------------------------------------------------------- deposits
-// Target of a deposit against the current grid (world.cpp:2093-2147): the cell
-// index, with bit 31 set for a merge into the same liquid; -1 if none.
-// s_type: physics type per material (shared memory).
+// ------------------------------------------------------ the particle update
+// world::tickCells (world.cpp:2030-2195) runs the particles one after another in
+// list order, and each one moves, collides and deposits against the grid as the
+// particles before it left it: a deposit can stop a later particle's flight, turn
+// its previous cell from AIR into a tile (so it searches the spiral instead) and
+// take a cell its spiral would have taken. Here every particle is computed at once
+// and the sequential result is reached by iterating to a fixed point:
 //
-// A particle whose search window (the 33x33 cells the spiral walk can reach) holds
-// no AIR can only fail, unless it is a liquid that may merge. The airmap records,
-// per 8x8 block, whether the block held AIR when this particle tick began; deposits
-// only remove AIR, so a window whose blocks are all AIR-free now is AIR-free too and
-// the walk is skipped. The result is the walk's result either way.
-__device__ __forceinline__ int dep_target(const WorldDev &w, const uint8_t *s_type, int i, uint8_t st) {
-    const int W = w.W, H = w.H;
-    if (st == PS_DIRECT) {
-        int c = w.p_lxly[i];
-        if (s_type[w.id[c]] == T_AIR) return c;
-    }
-    const float x = w.p.x[i], y = w.p.y[i];
-    const int pid = w.p.id[i];
-    const bool psoup = s_type[pid] == T_SOUP;
-    if (!psoup && x > -32.0f && x < (float)W + 32.0f && y > -32.0f && y < (float)H + 32.0f) {
-        // window [x-17, x+17] x [y-17, y+17] covers every (int)(x + ofs), |ofs| <= 16;
-        // positions far outside the world (or NaN) take the walk unfiltered
-        const int ix = (int)floorf(x), iy = (int)floorf(y);
-        const int bx0 = max(0, (ix - 17) >> 3), bx1 = min(w.amw - 1, (ix + 17) >> 3);
-        const int by0 = max(0, (iy - 17) >> 3), by1 = min(w.amh - 1, (iy + 17) >> 3);
-        bool any = false;
-        for (int by = by0; by <= by1 && !any; by++)
-            for (int bx = bx0; bx <= bx1; bx++)
-                if (w.airmap[by * w.amw + bx]) {
-                    any = true;
-                    break;
-                }
-        if (!any) return -1;
-    }
-    const int n = c_spiral_n;
-    for (int j = 0; j < n; j++) {
-        int cx = (int)__fadd_rn(x, (float)c_spiral[j][0]);
-        int cy = (int)__fadd_rn(y, (float)c_spiral[j][1]);
-        if (cx < 0 || cy < 0 || cx >= W || cy >= H) continue;
-        int c = cy * W + cx;
-        int cid = w.id[c];
-        if (s_type[cid] == T_AIR) return c;
-        if (psoup && cid == pid) return c | (int)0x80000000u;
-    }
-    return -1;
+//   iteration k computes every particle's outcome (state, and the cell it fills or
+//   merges into) against the grid of this tick's start plus the fills that
+//   particles of lower index made in iteration k - 1;
+//
+// particle 0's outcome is final after iteration 0, particle 1's after iteration 1 at
+// the latest, and so on, so the iteration ends (usually after a few rounds, as long
+// as the chains of particles landing on each other's deposits) when the set of
+// filled cells no longer changes, and its outcome is then exactly the sequential
+// one. Fills are recorded in the diff word of the AIR cell they fill (the diff means
+// nothing in an AIR cell; k_air_map zeroes it): 0x7fffffff - index, the largest
+// value (lowest index) kept by atomicMax. A particle is computed again only if a
+// fill changed near what it read (its bounding box of path and spiral cells against
+// per-8x8-block change marks). The grid itself is written once, after convergence.
+
+// outcome of a particle during the update (p_state); after the commit only
+// PS_ALIVE and PS_DEAD remain
+enum : uint8_t { PS_EXIT = 2, PS_DESTROY = 3, PS_FILL = 4, PS_MERGE = 5, PS_FAIL = 6 };
+
+__device__ __forceinline__ void load_types(uint8_t *s_type, const MatTable *mt) {
+    for (int k = threadIdx.x; k < MAXMAT; k += blockDim.x) s_type[k] = (uint8_t)(k < mt->n ? mt_type(mt->a[k]) : 0);
+    __syncthreads();
 }
 
-// which 8x8 blocks hold AIR, from the grid the cell tick left (one thread per block)
+__device__ __forceinline__ int32_t fill_code(int i) { return 0x7fffffff - i; }
+
+// the material particle i sees at cell c: the grid's, or the tile a particle of
+// lower index deposits there (fills are rewritten between iterations by other
+// blocks, so they are read past L1)
+__device__ __forceinline__ int view_id(const WorldDev &w, const uint8_t *s_type, int c, int i) {
+    int id = w.id[c];
+    if (s_type[id] == T_AIR) {
+        const int32_t v = __ldcg(&w.df[c]);
+        if (v != 0) {
+            const int j = 0x7fffffff - v;
+            if (j < i) id = w.p.id[j];
+        }
+    }
+    return id;
+}
+
+// which 8x8 blocks hold AIR, from the grid the cell tick left (one thread per block);
+// the diff word of every AIR cell is cleared for the fill records
 __global__ void k_air_map(const WorldDev *__restrict__ worlds, const MatTable *__restrict__ mt) {
     __shared__ uint8_t s_type[MAXMAT];
     load_types(s_type, mt);
@@ -270,104 +183,175 @@ __global__ void k_air_map(const WorldDev *__restrict__ worlds, const MatTable *_
         const int bx = b % w.amw, by = b / w.amw;
         const int x0 = bx * 8, y0 = by * 8, x1 = min(x0 + 8, w.W), y1 = min(y0 + 8, w.H);
         uint8_t any = 0;
-        for (int y = y0; y < y1 && !any; y++)
-            for (int x = x0; x < x1; x++)
-                if (s_type[w.id[(size_t)y * w.W + x]] == T_AIR) {
+        for (int y = y0; y < y1; y++)
+            for (int x = x0; x < x1; x++) {
+                const size_t c = (size_t)y * w.W + x;
+                if (s_type[w.id[c]] == T_AIR) {
                     any = 1;
+                    w.df[c] = 0;
+                }
+            }
+        w.airmap[b] = any;
+        w.chg[b] = 0;
+        w.chg[nb + b] = 0;
+    }
+}
+
+// bounding box of the cells a particle read, packed as (x0 | y0 << 16, x1 | y1 << 16)
+struct Box {
+    int x0, y0, x1, y1;
+    __device__ __forceinline__ void add(int x, int y) {
+        x0 = min(x0, x);
+        y0 = min(y0, y);
+        x1 = max(x1, x);
+        y1 = max(y1, y);
+    }
+};
+
+// One particle of world.cpp:2032-2188 against the view of particle i; writes its
+// outcome (state into w.q, kind into p_state, target cell into p_cell, the box of
+// the cells read into p_box0 / p_box1).
+__device__ void part_outcome(const WorldDev &w, const uint8_t *s_type, int i) {
+    uint8_t bits = w.p.bits[i];
+    int32_t life = w.p.life[i];
+    float x = w.p.x[i], y = w.p.y[i], vx = w.p.vx[i], vy = w.p.vy[i];
+    const int W = w.W, H = w.H;
+    uint8_t kind = PS_ALIVE;
+    int cell = -1;
+    Box bx = {W, H, -1, -1};
+    if ((bits & 2) && life <= 0) {  // :2033-2037
+        kind = PS_DESTROY;
+    } else {
+        const float tf = w.p.tf[i];
+        if (tf != 0.f) {  // :2039-2051
+            const float tdx = __fsub_rn(w.p.tx[i], x), tdy = __fsub_rn(w.p.ty[i], y);
+            const float nf = __fsqrt_rn(__fadd_rn(__fmul_rn(tdx, tdx), __fmul_rn(tdy, tdy)));
+            vx = __fadd_rn(vx, __fmul_rn(__fdiv_rn(tdx, nf), tf));
+            vy = __fadd_rn(vy, __fmul_rn(__fdiv_rn(tdy, nf), tf));
+            if (nf < 100.f) {
+                vx = __fmul_rn(vx, 0.95f);
+                vy = __fmul_rn(vy, 0.95f);
+            }
+        }
+        if (out_of_world(x, y, W, H)) {  // :2056-2059
+            kind = PS_EXIT;
+        } else {
+            const int lx = (int)x, ly = (int)y;
+            bx.add(lx, ly);
+            vx = __fadd_rn(vx, w.p.ax[i]);  // :2063-2064
+            vy = __fadd_rn(vy, w.p.ay[i]);
+            const int div = (int)__fadd_rn(__fadd_rn(fabsf(vx), fabsf(vy)), 1.0f);
+            const float dvx = __fdiv_rn(vx, (float)div), dvy = __fdiv_rn(vy, (float)div);
+            int hit = 0;  // 1: deposit at the previous cell, 2: spiral search
+            for (int s = 0; s < div; s++) {  // :2071-2184
+                x = __fadd_rn(x, dvx);
+                y = __fadd_rn(y, dvy);
+                if (out_of_world(x, y, W, H)) {
+                    kind = PS_EXIT;
                     break;
                 }
-        w.airmap[b] = any;
-    }
-}
-
-__device__ __forceinline__ void load_types(uint8_t *s_type, const MatTable *mt) {
-    for (int k = threadIdx.x; k < MAXMAT; k += blockDim.x) s_type[k] = (uint8_t)(k < mt->n ? mt_type(mt->a[k]) : 0);
-    __syncthreads();
-}
-
-__device__ __forceinline__ void dep_fail(const WorldDev &w, int i) {
-    // :2141-2144
-    w.p.vy[i] = -4.0f;
-    w.p.y[i] = __fsub_rn(w.p.y[i], 16.0f);
-    w.p_state[i] = PS_ALIVE;
-}
-__device__ __forceinline__ void dep_merge(const WorldDev &w, const MatTable *mt, int i, int c) {
-    // :2119-2125
-    if (w.f32) {
-        // f32 amounts: added after the rounds, cell by cell in particle-index order
-        // (k_merge_f32), as the reference's list order adds them
-        w.p_lxly[i] = c;
-        w.merge_list[atomicAdd(w.merge_count, 1)] = i;
-    } else {
-        atomicAdd(&w.sc[c], w.p.sc[i]);
-    }
-    if (w.dirty) w.dirty[c] = 1;
-    w.p_state[i] = PS_DEAD;
-    atomicAdd((unsigned long long *)&w.ledger[LED_DN * MAXMAT + w.p.id[i]], 1ull);
-}
-__device__ __forceinline__ void dep_fill(const WorldDev &w, int i, int c) {
-    // :2115-2118, :2148-2152; the cell's diff word still holds the claim and is
-    // cleared by k_dep_clear
-    w.id[c] = w.p.id[i];
-    w.col[c] = w.p.col[i];
-    w.sc[c] = w.p.sc[i];
-    w.fl[c] = w.p.fl[i];
-    // the target was AIR, whose temperature word means nothing: the particle's
-    // (a SOUP tile's temperature; 0 for the others) is stored without a type test
-    if (w.tp) w.tp[c] = w.p.tp[i];
-    if (w.dirty) w.dirty[c] = 1;
-    w.p_state[i] = PS_DEAD;
-}
-
-// round 1 over all requests, phase 1: pick targets; AIR targets get the claim sentinel
-__global__ void k_dep_target(const WorldDev *__restrict__ worlds, const MatTable *__restrict__ mt) {
-    __shared__ uint8_t s_type[MAXMAT];
-    load_types(s_type, mt);
-    const WorldDev &w = worlds[blockIdx.y];
-    const int n = w.req_count[0];
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        int i = w.req_list[j];
-        int t = dep_target(w, s_type, i, w.p_state[i]);
-        w.req_target[j] = t;
-        if (t >= 0) w.df[t] = 0x7fffffff;
-    }
-}
-// phase 2: claims (lowest particle index wins an AIR cell), merges, failures
-__global__ void k_dep_claim(const WorldDev *__restrict__ worlds, const MatTable *__restrict__ mt) {
-    const WorldDev &w = worlds[blockIdx.y];
-    const int n = w.req_count[0];
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        int i = w.req_list[j], t = w.req_target[j];
-        if (t == -1)
-            dep_fail(w, i);
-        else if (t < 0)
-            dep_merge(w, mt, i, t & 0x7fffffff);
-        else
-            atomicMin(&w.df[t], i);
-    }
-}
-// phase 3: winners write their tile; losers search again from where they stopped
-__global__ void k_dep_decide(const WorldDev *__restrict__ worlds) {
-    const WorldDev &w = worlds[blockIdx.y];
-    const int n = w.req_count[0];
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        int i = w.req_list[j], t = w.req_target[j];
-        if (t < 0) continue;
-        if (w.df[t] == i) {
-            dep_fill(w, i, t);
-            int k = atomicAdd(&w.req_count[2], 1);  // filled cells, for k_dep_clear
-            w.req_list2[w.part_cap + k] = t;
-        } else {
-            w.p_state[i] = PS_SPIRAL;
-            int k = atomicAdd(&w.req_count[1], 1);
-            w.req_list2[k] = i;
+                bx.add((int)x, (int)y);
+                const int ct = s_type[view_id(w, s_type, (int)y * W + (int)x, i)];
+                if (!(bits & 1) && ct != T_AIR) {
+                    const bool isObject = ct == T_OBJECT;
+                    int ps = (bits >> 2) & 3;
+                    if (ps == 0)
+                        ps = isObject ? 1 : 2;
+                    else if (ps == 1 && !isObject)
+                        ps = 2;
+                    bits = (uint8_t)((bits & ~0x0Cu) | ((unsigned)ps << 2));
+                    if (!isObject || ps == 2) {
+                        if (bits & 2)
+                            kind = PS_DESTROY;
+                        else
+                            hit = (s_type[view_id(w, s_type, ly * W + lx, i)] != T_AIR) ? 2 : 1;
+                        break;
+                    }
+                }
+            }
+            if (kind == PS_ALIVE && hit == 0 && life > 0) life--;  // :2186-2188
+            if (hit == 1) {  // :2148-2152
+                kind = PS_FILL;
+                cell = ly * W + lx;
+            } else if (hit == 2) {
+                // :2093-2147, the 32x32 spiral from the collision point: the first cell
+                // that is AIR or holds the same liquid. A window (the 33x33 cells the walk
+                // reaches) whose 8x8 blocks held no AIR when the update began holds none
+                // now (deposits only take AIR), so unless the particle is a liquid that
+                // may merge the walk can only fail and is skipped.
+                const int pid = w.p.id[i];
+                const bool psoup = s_type[pid] == T_SOUP;
+                bool walk = true;
+                if (!psoup && x > -32.0f && x < (float)W + 32.0f && y > -32.0f && y < (float)H + 32.0f) {
+                    const int ix = (int)floorf(x), iy = (int)floorf(y);
+                    const int bx0 = max(0, (ix - 17) >> 3), bx1 = min(w.amw - 1, (ix + 17) >> 3);
+                    const int by0 = max(0, (iy - 17) >> 3), by1 = min(w.amh - 1, (iy + 17) >> 3);
+                    bool any = false;
+                    for (int by = by0; by <= by1 && !any; by++)
+                        for (int bxx = bx0; bxx <= bx1; bxx++)
+                            if (w.airmap[by * w.amw + bxx]) {
+                                any = true;
+                                break;
+                            }
+                    walk = any;
+                }
+                int found = -1, j = 0;
+                if (walk) {
+                    for (; j < c_spiral_n; j++) {
+                        const int cx = (int)__fadd_rn(x, (float)c_spiral[j][0]);
+                        const int cy = (int)__fadd_rn(y, (float)c_spiral[j][1]);
+                        if (cx < 0 || cy < 0 || cx >= W || cy >= H) continue;
+                        const int c = cy * W + cx;
+                        const int cid = view_id(w, s_type, c, i);
+                        if (s_type[cid] == T_AIR) {
+                            found = c;
+                            kind = PS_FILL;
+                            break;
+                        }
+                        if (psoup && cid == pid) {
+                            found = c;
+                            kind = PS_MERGE;
+                            break;
+                        }
+                    }
+                    // the cells looked at lie in the square of the last one's ring
+                    const int jr = j < c_spiral_n ? j : c_spiral_n - 1;
+                    const int r = max(abs((int)c_spiral[jr][0]), abs((int)c_spiral[jr][1])) + 1;
+                    bx.add((int)floorf(x) - r, (int)floorf(y) - r);
+                    bx.add((int)floorf(x) + r, (int)floorf(y) + r);
+                }
+                if (found >= 0) {
+                    cell = found;
+                } else {  // :2141-2144
+                    kind = PS_FAIL;
+                    vy = -4.0f;
+                    y = __fsub_rn(y, 16.0f);
+                }
+            }
         }
     }
+    w.q.x[i] = x;
+    w.q.y[i] = y;
+    w.q.vx[i] = vx;
+    w.q.vy[i] = vy;
+    w.q.bits[i] = bits;
+    w.q.life[i] = life;
+    w.p_state[i] = kind;
+    w.p_cell[i] = cell;
+    const int x0 = min(max(bx.x0, 0), W - 1), y0 = min(max(bx.y0, 0), H - 1);
+    const int x1 = min(max(bx.x1, 0), W - 1), y1 = min(max(bx.y1, 0), H - 1);
+    w.p_box0[i] = bx.x1 < 0 ? -1 : (int32_t)((uint32_t)x0 | ((uint32_t)y0 << 16));
+    w.p_box1[i] = (int32_t)((uint32_t)x1 | ((uint32_t)y1 << 16));
 }
 
-// Grid-wide barrier for the cooperative deposit kernel. The spin is bounded: if
-// it ever gives up it records ERR_TIMEOUT and lets the block continue, so a wait
-// can never hang the device.
+// the fill a particle's outcome makes (-1: none)
+__device__ __forceinline__ int fill_of(const WorldDev &w, int i) {
+    return w.p_state[i] == PS_FILL ? w.p_cell[i] : -1;
+}
+
+// Grid-wide barrier of the cooperative update. The spin is bounded: if it ever
+// gives up it records ERR_TIMEOUT and lets the block continue, so a wait can never
+// hang the device.
 struct GridBar {
     unsigned count;
     unsigned gen;
@@ -398,122 +382,155 @@ __device__ __forceinline__ void grid_sync(GridBar *gb, unsigned nblocks, int32_t
     __syncthreads();
 }
 
-// Rounds 2.. of the deposit resolution for every world, in one cooperative launch.
-// Open requests of round r live in list (r even: req_list2, odd: req_list) with
-// their count in req_count[1] (r even) / req_count[0] (r odd).
-//
-// The last rounds have few open requests (tens, then one or two on a 4096x2048
-// world), and a grid-wide barrier costs far more than their work. So once a round
-// starts with at most DEP_SOLO_MAX open requests (at most one per thread of a
-// block: each request's walk is a chain of global loads and must not queue behind
-// others), block 0 finishes the rounds alone with block barriers and the other
-// blocks leave. Every block reads the same counts (written before the last grid
-// barrier or before the launch), so they all take the same decision.
-constexpr int DEP_SOLO_MAX = 256;
+constexpr int SERIAL_MAX_ITER = 1 << 16;
 
-__global__ void k_dep_rounds(const WorldDev *__restrict__ worlds, int n_worlds, const MatTable *__restrict__ mt) {
+// The fixed-point iteration and the commit for every world of the table, in one
+// cooperative launch (every block resident, so the grid barrier is safe).
+// req_count[0..1] of world 0 count the fill changes of even and odd iterations.
+__global__ void k_part_serial(const WorldDev *__restrict__ worlds, int n_worlds, const MatTable *__restrict__ mt) {
     __shared__ uint8_t s_type[MAXMAT];
     load_types(s_type, mt);
     GridBar *gb = (GridBar *)worlds[0].bar;
     const unsigned nb = gridDim.x;
     int32_t *err = worlds[0].err;
-    bool solo = false;
-    for (int r = 0;; r++) {
-        if (r > (1 << 22)) {
-            if (threadIdx.x == 0 && blockIdx.x == 0) atomicOr(err, ERR_TIMEOUT);
+    int32_t *cnt = worlds[0].req_count;
+    const int gtid = (int)(blockIdx.x * blockDim.x + threadIdx.x), gstride = (int)(gridDim.x * blockDim.x);
+    for (int it = 0;; it++) {
+        if (it >= SERIAL_MAX_ITER) {
+            if (gtid == 0) atomicOr(err, ERR_TIMEOUT);
             break;
         }
-        const int ci = (r & 1) ? 0 : 1, ni = (r & 1) ? 1 : 0;
-        if (!solo) {
-            int open = 0;
-            for (int wi = 0; wi < n_worlds; wi++) open += ((volatile int32_t *)worlds[wi].req_count)[ci];
-            if (open <= DEP_SOLO_MAX) {
-                if (blockIdx.x != 0) return;
-                solo = true;
-            }
-        }
-        const int gtid = solo ? (int)threadIdx.x : (int)(blockIdx.x * blockDim.x + threadIdx.x);
-        const int gstride = solo ? (int)blockDim.x : (int)(gridDim.x * blockDim.x);
-        auto sync = [&]() {
-            if (solo)
-                __syncthreads();
-            else
-                grid_sync(gb, nb, err);
-        };
-        // phase 1: targets against the grid at the start of the round
+        const int par = it & 1;
+        // A: outcomes of the particles whose box saw a changed fill (all at first);
+        // changed fills are counted and their blocks marked for the next iteration
         for (int wi = 0; wi < n_worlds; wi++) {
             const WorldDev &w = worlds[wi];
-            const int n = w.req_count[ci];
-            const int32_t *cur = (r & 1) ? w.req_list : w.req_list2;
-            if (gtid == 0) w.req_count[ni] = 0;
-            for (int j = gtid; j < n; j += gstride) {
-                int i = cur[j];
-                int t = dep_target(w, s_type, i, w.p_state[i]);
-                w.req_target[j] = t;
-                if (t >= 0) w.df[t] = 0x7fffffff;
-            }
-        }
-        sync();
-        // phase 2: claims, merges, failures
-        for (int wi = 0; wi < n_worlds; wi++) {
-            const WorldDev &w = worlds[wi];
-            const int n = w.req_count[ci];
-            const int32_t *cur = (r & 1) ? w.req_list : w.req_list2;
-            for (int j = gtid; j < n; j += gstride) {
-                int i = cur[j], t = w.req_target[j];
-                if (t == -1)
-                    dep_fail(w, i);
-                else if (t < 0)
-                    dep_merge(w, mt, i, t & 0x7fffffff);
-                else
-                    atomicMin(&w.df[t], i);
-            }
-        }
-        sync();
-        // phase 3: winners fill, losers go to the next round's list
-        for (int wi = 0; wi < n_worlds; wi++) {
-            const WorldDev &w = worlds[wi];
-            const int n = w.req_count[ci];
-            const int32_t *cur = (r & 1) ? w.req_list : w.req_list2;
-            int32_t *nxt = (r & 1) ? w.req_list2 : w.req_list;
-            for (int j = gtid; j < n; j += gstride) {
-                int i = cur[j], t = w.req_target[j];
-                if (t < 0) continue;
-                if (w.df[t] == i) {
-                    dep_fill(w, i, t);
-                    int k = atomicAdd(&w.req_count[2], 1);
-                    w.req_list2[w.part_cap + k] = t;
+            const int n = *w.part_count;
+            const int nblk = w.amw * w.amh;
+            const uint8_t *seen = w.chg + (size_t)par * nblk;
+            uint8_t *mark = w.chg + (size_t)(1 - par) * nblk;
+            for (int i = gtid; i < n; i += gstride) {
+                int before = -1;
+                if (it > 0) {
+                    const int32_t b0 = w.p_box0[i];
+                    if (b0 < 0) continue;  // read no cell: nothing can change it
+                    const int32_t b1 = w.p_box1[i];
+                    const int x0 = (b0 & 0xFFFF) >> 3, y0 = ((uint32_t)b0 >> 16) >> 3;
+                    const int x1 = (b1 & 0xFFFF) >> 3, y1 = ((uint32_t)b1 >> 16) >> 3;
+                    bool touched = false;
+                    for (int by = y0; by <= y1 && !touched; by++)
+                        for (int bxx = x0; bxx <= x1; bxx++)
+                            if (__ldcg(&seen[by * w.amw + bxx])) {
+                                touched = true;
+                                break;
+                            }
+                    if (!touched) continue;
+                    before = fill_of(w, i);
+                }
+                part_outcome(w, s_type, i);
+                const int after = fill_of(w, i);
+                if (after != before) {
+                    atomicAdd(&cnt[par], 1);
+                    if (before >= 0) mark[(before / w.W >> 3) * w.amw + ((before % w.W) >> 3)] = 1;
+                    if (after >= 0) mark[(after / w.W >> 3) * w.amw + ((after % w.W) >> 3)] = 1;
+                    w.p_prev[i] = before;  // the cell whose record B1 clears
                 } else {
-                    int k = atomicAdd(&w.req_count[ni], 1);
-                    nxt[k] = i;
+                    w.p_prev[i] = -1;
                 }
             }
         }
-        sync();
-        int open = 0;
-        for (int wi = 0; wi < n_worlds; wi++) open += ((volatile int32_t *)worlds[wi].req_count)[ni];
-        if (open == 0) break;
+        grid_sync(gb, nb, err);
+        const int changed = __ldcg(&cnt[par]);
+        if (changed == 0) break;
+        // B1: clear the records of fills that moved away; the marks read in A are done
+        for (int wi = 0; wi < n_worlds; wi++) {
+            const WorldDev &w = worlds[wi];
+            const int n = *w.part_count;
+            const int nblk = w.amw * w.amh;
+            for (int i = gtid; i < n; i += gstride) {
+                const int c = w.p_prev[i];
+                if (c >= 0) w.df[c] = 0;
+                w.p_prev[i] = -1;
+            }
+            uint8_t *seen = w.chg + (size_t)par * nblk;
+            for (int b = gtid; b < nblk; b += gstride) seen[b] = 0;
+        }
+        if (gtid == 0) cnt[1 - par] = 0;
+        grid_sync(gb, nb, err);
+        // B2: every current fill records itself; the lowest index stays
+        for (int wi = 0; wi < n_worlds; wi++) {
+            const WorldDev &w = worlds[wi];
+            const int n = *w.part_count;
+            for (int i = gtid; i < n; i += gstride) {
+                const int c = fill_of(w, i);
+                if (c >= 0) atomicMax(&w.df[c], fill_code(i));
+            }
+        }
+        grid_sync(gb, nb, err);
+    }
+    // the sequential outcome: commit it
+    for (int wi = 0; wi < n_worlds; wi++) {
+        const WorldDev &w = worlds[wi];
+        const int n = *w.part_count;
+        for (int i = gtid; i < n; i += gstride) {
+            const uint8_t k = w.p_state[i];
+            const int c = w.p_cell[i];
+            if (k == PS_EXIT || k == PS_DESTROY) {
+                led_part(w, mt, k == PS_EXIT ? LED_XN : LED_DN, k == PS_EXIT ? LED_XF : LED_DF, w.p.id[i], w.p.sc[i]);
+                w.p_state[i] = PS_DEAD;
+            } else if (k == PS_FILL) {  // :2115-2118, :2148-2152
+                w.id[c] = w.p.id[i];
+                w.col[c] = w.p.col[i];
+                w.sc[c] = w.p.sc[i];
+                w.fl[c] = w.p.fl[i];
+                w.df[c] = 0;
+                // the target was AIR, whose temperature word means nothing: the particle's
+                // (a SOUP tile's temperature; 0 for the others) is stored without a type test
+                if (w.tp) w.tp[c] = w.p.tp[i];
+                if (w.dirty) w.dirty[c] = 1;
+                w.p_state[i] = PS_DEAD;
+            } else if (k == PS_MERGE) {  // :2119-2125, added by k_merge in particle order
+                w.p_box0[i] = c;
+                w.merge_list[atomicAdd(w.merge_count, 1)] = i;
+                if (w.dirty) w.dirty[c] = 1;
+                atomicAdd((unsigned long long *)&w.ledger[LED_DN * MAXMAT + w.p.id[i]], 1ull);
+                w.p_state[i] = PS_DEAD;
+            } else {  // PS_ALIVE, PS_FAIL: the particle lives on
+                w.p.x[i] = w.q.x[i];
+                w.p.y[i] = w.q.y[i];
+                w.p.vx[i] = w.q.vx[i];
+                w.p.vy[i] = w.q.vy[i];
+                w.p.bits[i] = w.q.bits[i];
+                w.p.life[i] = w.q.life[i];
+                w.p_state[i] = PS_ALIVE;
+            }
+        }
+    }
+    if (gtid == 0) {
+        cnt[0] = 0;
+        cnt[1] = 0;
     }
 }
 
-// filled cells no longer hold a claim: their diff word becomes 0
-__global__ void k_dep_clear(const WorldDev *__restrict__ worlds) {
-    const WorldDev &w = worlds[blockIdx.y];
-    const int n = w.req_count[2];
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
-        w.df[w.req_list2[w.part_cap + j]] = 0;
-}
-
-// f32 worlds: the deposits into liquid of this particle tick, applied to each cell in
-// particle-index order (tile.fluidAmount += particle amount, world.cpp:2123, in the
-// reference's float add). One block per world: each round every cell takes its
-// lowest-index pending deposit, so a cell with k deposits is done after k rounds.
-__global__ void k_merge_f32(const WorldDev *__restrict__ worlds) {
+// The deposits into liquid of this particle update: Q16.16 amounts are added at once;
+// f32 amounts (tile.fluidAmount += particle amount, world.cpp:2123, the reference's
+// float add) cell by cell in particle-index order, after any fill of the cell (a
+// fill comes from a lower index). One block per world: each round every cell takes
+// its lowest-index pending deposit, so a cell with k deposits is done after k rounds.
+__global__ void k_merge(const WorldDev *__restrict__ worlds) {
     const WorldDev &w = worlds[blockIdx.x];
-    if (!w.f32) return;
     __shared__ int s_open, s_next;
     const int n0 = *w.merge_count;
     if (n0 == 0) return;
+    if (!w.f32) {
+        for (int j = threadIdx.x; j < n0; j += blockDim.x) {
+            const int i = w.merge_list[j];
+            atomicAdd(&w.sc[w.p_box0[i]], w.p.sc[i]);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) *w.merge_count = 0;
+        return;
+    }
     // two lists of part_cap entries: the open deposits of this round, the next's
     int32_t *cur = w.merge_list, *nxt = w.merge_list + w.part_cap;
     if (threadIdx.x == 0) s_open = n0;
@@ -523,21 +540,21 @@ __global__ void k_merge_f32(const WorldDev *__restrict__ worlds) {
         if (n == 0) break;
         for (int j = threadIdx.x; j < n; j += blockDim.x) {
             const int i = cur[j];
-            atomicMin(&w.merge_claim[w.p_lxly[i]], (uint32_t)i);
+            atomicMin(&w.merge_claim[w.p_box0[i]], (uint32_t)i);
         }
         if (threadIdx.x == 0) s_next = 0;
         __syncthreads();
         // the winners add (one thread per cell); the others go to the next round
         for (int j = threadIdx.x; j < n; j += blockDim.x) {
             const int i = cur[j];
-            const int c = w.p_lxly[i];
+            const int c = w.p_box0[i];
             if (w.merge_claim[c] == (uint32_t)i)
                 w.sc[c] = __float_as_int(__fadd_rn(__int_as_float(w.sc[c]), __int_as_float(w.p.sc[i])));
             else
                 nxt[atomicAdd(&s_next, 1)] = i;
         }
         __syncthreads();
-        for (int j = threadIdx.x; j < n; j += blockDim.x) w.merge_claim[w.p_lxly[cur[j]]] = 0xFFFFFFFFu;
+        for (int j = threadIdx.x; j < n; j += blockDim.x) w.merge_claim[w.p_box0[cur[j]]] = 0xFFFFFFFFu;
         __syncthreads();
         if (threadIdx.x == 0) s_open = s_next;
         int32_t *t = cur;
@@ -734,16 +751,12 @@ cudaError_t launch_particle_tick(WorldDev *d_worlds, int n_worlds, const MatTabl
     spiral_upload();
     dim3 gm(move_blocks, n_worlds);
     k_air_map<<<gm, 256, 0, s>>>(d_worlds, mt);
-    k_part_move<<<gm, 256, 0, s>>>(d_worlds, mt);
-    k_dep_target<<<gm, 256, 0, s>>>(d_worlds, mt);
-    k_dep_claim<<<gm, 256, 0, s>>>(d_worlds, mt);
-    k_dep_decide<<<gm, 256, 0, s>>>(d_worlds);
     {
         // every block of a cooperative launch is resident, so the grid barrier is safe
         static int coop_blocks = 0;
         if (!coop_blocks) {
             int per_sm = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dep_rounds, 256, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_part_serial, 256, 0);
             int dev = 0, nsm = 1;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -759,10 +772,9 @@ cudaError_t launch_particle_tick(WorldDev *d_worlds, int n_worlds, const MatTabl
         attr[0].val.cooperative = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        cudaLaunchKernelEx(&cfg, k_dep_rounds, (const WorldDev *)d_worlds, n_worlds, mt);
+        cudaLaunchKernelEx(&cfg, k_part_serial, (const WorldDev *)d_worlds, n_worlds, mt);
     }
-    k_dep_clear<<<gm, 256, 0, s>>>(d_worlds);
-    k_merge_f32<<<n_worlds, 1024, 0, s>>>(d_worlds);
+    k_merge<<<n_worlds, 1024, 0, s>>>(d_worlds);
     dim3 gc(PART_BLOCKS, n_worlds);
     k_cmp_count<<<gc, PART_THREADS, 0, s>>>(d_worlds);
     k_cmp_scan<<<n_worlds, PART_BLOCKS, 0, s>>>(d_worlds, PART_BLOCKS);

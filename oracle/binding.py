@@ -111,7 +111,6 @@ class Oracle:
                 "om_object_mask": (None, [vp, vp]),
                 "om_set_threads": (None, [i32]),
                 "om_debug_set_lattice": (None, [i32, i32, i32]),
-                "om_debug_last_rounds": (i32, [vp, i32]),
                 "om_render_enable": (None, [vp]),
                 "om_render_dirty": (None, [vp, vp]),
                 "om_render_cells": (None, [vp]),
@@ -188,12 +187,6 @@ class Oracle:
 
     def debug_set_lattice(self, sweep, px, py):
         self.lib.om_debug_set_lattice(sweep, px, py)
-
-    def debug_last_rounds(self):
-        """Open deposit requests per round of the last particle tick."""
-        buf = np.zeros(256, np.int64)
-        n = self.lib.om_debug_last_rounds(buf.ctypes.data_as(C.c_void_p), 256)
-        return buf[: min(n, 256)]
 
 
 class OracleWorld:

@@ -1365,12 +1365,6 @@ void om_debug_set_lattice(int sweep, int px, int py) {
     DBG_PX[sweep] = px;
     DBG_PY[sweep] = py;
 }
-static int DBG_ROUNDS = 0;
-static int64_t DBG_OPEN[256];
-int om_debug_last_rounds(int64_t *open, int cap) {
-    for (int r = 0; r < DBG_ROUNDS && r < cap && r < 256; r++) open[r] = DBG_OPEN[r];
-    return DBG_ROUNDS;
-}
 static void lattice(int sweep, int mode, int *px, int *py) {
     if (DBG_PX[sweep] > 0) {
         *px = DBG_PX[sweep];
@@ -1624,126 +1618,62 @@ static int find_target(om_world *w, const om_particle *p, int kind, int lx, int 
     return 0;
 }
 
-typedef struct {
-    int64_t cell;
-    int part;
-} merge_t;
-static int merge_cmp(const void *a, const void *b) {
-    const merge_t *x = (const merge_t *)a, *y = (const merge_t *)b;
-    if (x->cell != y->cell) return x->cell < y->cell ? -1 : 1;
-    return x->part < y->part ? -1 : (x->part > y->part);
-}
-
+/* world::tickCells (world.cpp:2030-2195) as the reference runs it: particles one
+ * after another in list order, each moving, colliding and depositing against the
+ * grid as the particles before it left it (a deposit is visible to every later
+ * particle's flight, its previous-cell test and its spiral search), then the stable
+ * erase of the removed ones. */
 int om_particles_tick(om_world *w) {
     spiral_init();
     int n = w->parts.n;
     om_particle *P = w->parts.p;
     uint8_t *dead = (uint8_t *)calloc((size_t)n + 1, 1);
-    int *req = (int *)malloc(((size_t)n + 1) * sizeof(int));
-    int *rlx = (int *)malloc(((size_t)n + 1) * sizeof(int));
-    int *rly = (int *)malloc(((size_t)n + 1) * sizeof(int));
-    int nreq = 0;
-    int *rq = (int *)malloc(((size_t)n + 1) * sizeof(int));
-    /* phase 1: motion, all particles against the grid left by the cell tick */
     for (int i = 0; i < n; i++) {
-        int out, lx = 0, ly = 0;
-        int r = particle_move(w, &P[i], &out, &lx, &ly);
-        req[i] = REQ_NONE;
+        om_particle *p = &P[i];
+        int lx = 0, ly = 0, out;
+        int r = particle_move(w, p, &out, &lx, &ly);
         if (out == OUT_DEAD) {
             dead[i] = 1;
-            int64_t f = (M[P[i].id].type == T_SOUP && !w->f32) ? P[i].scalar : 0; /* f32: no fluid rows */
+            int64_t f = (M[p->id].type == T_SOUP && !w->f32) ? p->scalar : 0; /* f32: no fluid rows */
             if (r == -2) {
-                if (M[P[i].id].type != T_AIR) w->led[LED_XN][P[i].id] += 1;
-                w->led[LED_XF][P[i].id] += f;
+                if (M[p->id].type != T_AIR) w->led[LED_XN][p->id] += 1;
+                w->led[LED_XF][p->id] += f;
             } else {
-                if (M[P[i].id].type != T_AIR) w->led[LED_DN][P[i].id] += 1;
-                w->led[LED_DF][P[i].id] += f;
+                if (M[p->id].type != T_AIR) w->led[LED_DN][p->id] += 1;
+                w->led[LED_DF][p->id] += f;
             }
-        } else if (r == REQ_DIRECT || r == REQ_SPIRAL) {
-            req[i] = r;
-            rlx[i] = lx;
-            rly[i] = ly;
-            rq[nreq++] = i;
+            continue;
         }
-    }
-    /* phase 2: deposits, in rounds; in each round every open request picks its
-     * target against the grid at the start of the round, merges apply at once, and
-     * each AIR cell goes to the lowest-index claimant; losers try again. */
-    int *tx = (int *)malloc(((size_t)nreq + 1) * sizeof(int));
-    int *ty = (int *)malloc(((size_t)nreq + 1) * sizeof(int));
-    int *tk = (int *)malloc(((size_t)nreq + 1) * sizeof(int));
-    int32_t *claim = NULL;
-    size_t ncell = (size_t)w->W * w->H;
-    if (nreq) {
-        claim = (int32_t *)malloc(ncell * sizeof(int32_t));
-        for (size_t i = 0; i < ncell; i++) claim[i] = 0x7fffffff;
-    }
-    /* f32 worlds: the deposits into liquid, applied after the rounds cell by cell in
-     * particle-index order (the reference's list order of its float adds) */
-    merge_t *mg = (merge_t *)malloc(((size_t)nreq + 1) * sizeof(merge_t));
-    int nmg = 0;
-    DBG_ROUNDS = 0;
-    while (nreq > 0) {
-        if (DBG_ROUNDS < 256) DBG_OPEN[DBG_ROUNDS] = nreq;
-        DBG_ROUNDS++;
-        for (int j = 0; j < nreq; j++) {
-            int i = rq[j];
-            tk[j] = find_target(w, &P[i], req[i], rlx[i], rly[i], &tx[j], &ty[j]);
-            if (tk[j] == 1) {
-                size_t ci = (size_t)ty[j] * w->W + tx[j];
-                if (i < claim[ci]) claim[ci] = i;
-            }
+        if (r != REQ_DIRECT && r != REQ_SPIRAL) continue;
+        int tx = 0, ty = 0;
+        int k = find_target(w, p, r, lx, ly, &tx, &ty);
+        if (k == 0) { /* :2141-2144: no room found */
+            p->vy = -4;
+            p->y -= 16;
+            continue;
         }
-        int nn = 0;
-        for (int j = 0; j < nreq; j++) {
-            int i = rq[j];
-            om_particle *p = &P[i];
-            if (tk[j] == 0) { /* :2141-2144: no room found */
-                p->vy = -4;
-                p->y -= 16;
-                continue;
-            }
-            size_t ci = (size_t)ty[j] * w->W + tx[j];
-            if (tk[j] == 2) { /* :2119-2125 */
-                if (w->f32) { /* added after the rounds, per cell in particle order */
-                    mg[nmg].cell = (int64_t)ci;
-                    mg[nmg].part = i;
-                    nmg++;
-                } else {
-                    w->sc[ci] += p->scalar;
-                }
-                mark_dirty(w, ci);
-                dead[i] = 1;
-                w->led[LED_DN][p->id] += 1;
-                continue;
-            }
-            if (claim[ci] == i) { /* :2115-2118 and :2148-2152 */
-                w->id[ci] = p->id;
-                w->col[ci] = p->colour;
-                w->sc[ci] = p->scalar;
-                if (M[p->id].type == T_SOUP) w->tp[ci] = p->temperature;
-                mark_dirty(w, ci);
-                w->fl[ci] = p->flags;
-                w->df[ci] = 0;
-                dead[i] = 1;
-            } else {
-                req[i] = REQ_SPIRAL; /* the cell was taken: search from here */
-                rq[nn++] = i;
-            }
+        size_t ci = (size_t)ty * w->W + tx;
+        if (k == 2) { /* :2119-2125 */
+            if (w->f32)
+                w->sc[ci] = f2i(i2f(w->sc[ci]) + i2f(p->scalar));
+            else
+                w->sc[ci] += p->scalar;
+            mark_dirty(w, ci);
+            dead[i] = 1;
+            w->led[LED_DN][p->id] += 1;
+            continue;
         }
-        for (int j = 0; j < nreq; j++)
-            if (tk[j] == 1) claim[(size_t)ty[j] * w->W + tx[j]] = 0x7fffffff;
-        nreq = nn;
+        /* :2115-2118 and :2148-2152 */
+        w->id[ci] = p->id;
+        w->col[ci] = p->colour;
+        w->sc[ci] = p->scalar;
+        if (M[p->id].type == T_SOUP) w->tp[ci] = p->temperature;
+        mark_dirty(w, ci);
+        w->fl[ci] = p->flags;
+        w->df[ci] = 0;
+        dead[i] = 1;
     }
-    if (nmg > 0) {
-        qsort(mg, (size_t)nmg, sizeof(merge_t), merge_cmp);
-        for (int k = 0; k < nmg; k++) {
-            int32_t *a = &w->sc[mg[k].cell];
-            *a = f2i(i2f(*a) + i2f(P[mg[k].part].scalar));
-        }
-    }
-    free(mg);
-    /* phase 3: stable erase (std::erase_if, :2190) and the y > height erase (:2203) */
+    /* the stable erase (std::erase_if, :2179) and the y > height erase (:2190) */
     int m = 0;
     for (int i = 0; i < n; i++) {
         if (dead[i]) continue;
@@ -1752,14 +1682,6 @@ int om_particles_tick(om_world *w) {
     }
     w->parts.n = m;
     free(dead);
-    free(req);
-    free(rlx);
-    free(rly);
-    free(rq);
-    free(tx);
-    free(ty);
-    free(tk);
-    free(claim);
     return m;
 }
 

@@ -154,9 +154,6 @@ void om_object_mask(const om_world *wd, uint8_t *bits);
 void om_set_threads(int n);
 /* test hook: override the sub-phase lattice of one sweep (px = 0 restores it) */
 void om_debug_set_lattice(int sweep, int px, int py);
-/* statistics of the last particle tick's deposit rounds: returns the number of
- * rounds, and the open requests of the first min(rounds, cap) rounds in open[] */
-int om_debug_last_rounds(int64_t *open, int cap);
 
 /* headless render textures (game.cpp:1994-2067, world.cpp:2006-2028), 4 bytes
  * r, g, b, a per cell; which: 0 pixels, 1 emission, 2 fire, 3 flow, 4 particles */

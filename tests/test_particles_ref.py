@@ -76,3 +76,47 @@ def test_oracle_matches_reference_function(oracle_mod):
             removed += len(p) - len(p2)
             ids, col, amt, p = ids2, col2, amt2, p2
     assert moved > 20 and removed > 20  # deposits and removals were exercised
+
+
+def _contested(oracle_mod, g, s, types):
+    from particle_cases import CH, CW
+
+    ids, col, amt = g["%d_ids" % s], g["%d_col" % s], g["%d_amt" % s]
+    ow = oracle_mod.OracleWorld(CW, CH, 128, 3, 1)
+    z = np.zeros((CH, CW), np.int32)
+    ow.set_state({"id": ids, "colour": col, "scalar": np.where(types[ids] == 3, amt, 0).astype(np.int32),
+                  "flags": np.zeros((CH, CW), np.uint8), "diff": z})
+    ow.set_particles(g["%d_parts" % s])
+    return ow, ids, col, amt
+
+
+def test_oracle_matches_reference_on_contested_scenes(oracle_mod):
+    """Particles as dense as on the bench world: flights stop at cells deposited
+    earlier in the same tick, previous cells fill up and spiral searches compete.
+    The oracle runs the particles in list order, as the reference does, and matches
+    its results (tests/golden/particles_contested.npz, made by the reference's own
+    tickCells) bit for bit."""
+    from particle_cases import CH, CW
+
+    g = np.load(os.path.join(os.path.dirname(GOLDEN), "particles_contested.npz"))
+    o = oracle_mod.Oracle()
+    o.reset_materials()
+    types = np.array([o.material(i)[0] for i in range(o.material_count())], np.int32)
+    assert np.array_equal(types, g["types"])
+    deposits = 0
+    for s in g["seeds"]:
+        ow, ids, col, amt = _contested(oracle_mod, g, s, types)
+        for t in range(int(g["ticks"])):
+            ow.particles_tick()
+            st = ow.state()
+            cells = g["%d_t%d_cells" % (s, t)]
+            ids, col, amt = ids.copy().ravel(), col.copy().ravel(), amt.copy().ravel()
+            ids[cells], col[cells], amt[cells] = g["%d_t%d_ids" % (s, t)], g["%d_t%d_col" % (s, t)], \
+                g["%d_t%d_amt" % (s, t)]
+            ids, col, amt = ids.reshape(CH, CW), col.reshape(CH, CW), amt.reshape(CH, CW)
+            assert np.array_equal(st["id"], ids) and np.array_equal(st["colour"], col), (s, t)
+            soup = types[ids] == 3
+            assert np.array_equal(st["scalar"][soup], amt[soup]), (s, t)
+            assert ow.particles().tobytes() == g["%d_t%d_parts" % (s, t)].tobytes(), (s, t)
+            deposits += len(cells)
+    assert deposits > 1000
