@@ -237,6 +237,10 @@ class World:
                                                 0 if tab is None else tab.size), "download_tiles")
         return out
 
+    def set_tick_zone(self, x, y, w, h):
+        """world::tickZone: the rectangle the tick works on (the whole world by default)."""
+        check(self.lib.fse_world_set_tick_zone(self.h, x, y, w, h), "world_set_tick_zone")
+
     def generate(self, kind, seed):
         check(self.lib.fse_world_generate(self.h, kind, seed & 0xFFFFFFFF), "generate")
 

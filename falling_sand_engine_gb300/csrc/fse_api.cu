@@ -739,7 +739,23 @@ static void free_world(fse_world *w) {
     delete w;
 }
 
-template <typename T>
+// the chunk slots of each colour for the current tick zone
+static int world_items(fse_world *w) {
+    const WorldDev &h = w->h;
+    for (int tk = 0; tk < 4; tk++) {
+        int ox = tk % 2, oy = 1 - tk / 2;
+        int na = (h.nCx - ox + 1) / 2, nb = (h.nCy - oy + 1) / 2;
+        int ns = std::max(0, na) * std::max(0, nb);
+        w->n_items[tk] = ns;
+        std::vector<uint32_t> v(ns);
+        for (int s = 0; s < ns; s++) v[s] = (uint32_t)s;
+        if (ns && cudaMemcpy(w->items[tk], v.data(), ns * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+            return FSE_E_CUDA;
+    }
+    return FSE_OK;
+}
+
+template <class T>
 static bool dalloc(fse_world *w, T **p, size_t n) {
     size_t b = n * sizeof(T);
     if (b == 0) b = sizeof(T);
@@ -800,6 +816,10 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
     h.nCx = ceil_div(width, h.C);
     h.nCy = ceil_div(height, h.C);
     h.max_slots = ceil_div(h.nCx, 2) * ceil_div(h.nCy, 2);
+    h.zx = 0;  // the tick zone: the whole world until fse_world_set_tick_zone
+    h.zy = 0;
+    h.zw = width;
+    h.zh = height;
     h.stage_cap = c.spawn_capacity;
     h.part_cap = c.particle_capacity;
     h.amw = ceil_div(width, 8);
@@ -849,17 +869,9 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
             for (int k = 0; k < 5; k++) cudaMemset(w->tex[k], 0, n * sizeof(uint32_t));
         }
     }
-    // chunk slots per colour: (world 0 << 20) | slot
-    for (int tk = 0; tk < 4 && ok; tk++) {
-        int ox = tk % 2, oy = 1 - tk / 2;
-        int na = (h.nCx - ox + 1) / 2, nb = (h.nCy - oy + 1) / 2;
-        int ns = std::max(0, na) * std::max(0, nb);
-        w->n_items[tk] = ns;
-        std::vector<uint32_t> v(ns);
-        for (int s = 0; s < ns; s++) v[s] = (uint32_t)s;
-        ok = dalloc(w, &w->items[tk], (size_t)std::max(ns, 1));
-        if (ok && ns) ok = cudaMemcpy(w->items[tk], v.data(), ns * 4, cudaMemcpyHostToDevice) == cudaSuccess;
-    }
+    // chunk slots per colour: (world 0 << 20) | slot; room for the whole world's
+    for (int tk = 0; tk < 4 && ok; tk++) ok = dalloc(w, &w->items[tk], (size_t)std::max(h.max_slots, 1));
+    if (ok) ok = world_items(w) == FSE_OK;
     if (!ok) {
         free_world(w);
         return FSE_E_NOMEM;
@@ -933,6 +945,28 @@ int fse_world_set_tick(fse_world *w, uint32_t tick) {
     if (!w) return FSE_E_INVAL;
     FSE_CUDA_TRY(cudaMemcpyAsync(w->h.tick, &tick, 4, cudaMemcpyHostToDevice, w->stream));
     FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
+    return FSE_OK;
+}
+
+int fse_world_set_tick_zone(fse_world *w, int x, int y, int width, int height) {
+    if (!w || x < 0 || y < 0 || width < 0 || height < 0 || (long long)x + width > w->W ||
+        (long long)y + height > w->H)
+        return FSE_E_INVAL;
+    FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
+    WorldDev &h = w->h;
+    h.zx = x;
+    h.zy = y;
+    h.zw = width;
+    h.zh = height;
+    h.nCx = ceil_div(width, h.C);
+    h.nCy = ceil_div(height, h.C);
+    int rc = world_items(w);
+    if (rc) return rc;
+    FSE_CUDA_TRY(cudaMemcpy(w->d, &h, sizeof(WorldDev), cudaMemcpyHostToDevice));
+    // captured step graphs hold the old chunk counts
+    for (auto &g : w->graphs) cudaGraphExecDestroy(g.second);
+    w->graphs.clear();
+    w->graph_kernels.clear();
     return FSE_OK;
 }
 

@@ -150,6 +150,11 @@ struct WorldDev {
     int W, H, C, cell_iter;
     uint32_t seed;
     uint32_t *tick;  // device counter, advanced on the device so multi-tick graphs replay correctly
+    // world::tickZone (world.hpp:138), inside the world: chunks start at its corner
+    // (nCx x nCy of them, C cells each way whatever the zone's end), particles outside
+    // it stay as they are, the temperature step changes its cells only; max_slots is
+    // the most chunks of one colour any zone of the world has (the whole world's)
+    int zx, zy, zw, zh;
     int nCx, nCy, max_slots;
     // spawned-particle staging for the current tick
     SpawnRec *stage;

@@ -142,6 +142,8 @@ extern "C" int fse_tick_noalloc(uint16_t *id, uint32_t *colour, int32_t *scalar,
     h.seed = seed;
     h.nCx = nCx;
     h.nCy = nCy;
+    h.zw = width;  // the tick zone is the whole world
+    h.zh = height;
     h.max_slots = max_slots;
     h.cp_rows = 1;
     h.stage = (SpawnRec *)(base + OFF_STAGE);

@@ -233,10 +233,13 @@ __device__ void part_outcome(const WorldDev &w, const uint8_t *s_type, int i) {
                 vy = __fmul_rn(vy, 0.95f);
             }
         }
+        const int lx = (int)x, ly = (int)y;
         if (out_of_world(x, y, W, H)) {  // :2056-2059
             kind = PS_EXIT;
+        } else if (lx < w.zx || ly < w.zy || lx >= w.zx + w.zw || ly >= w.zy + w.zh) {
+            // :2061, outside the tick zone: kept as it is (steered velocity included),
+            // having read no cell
         } else {
-            const int lx = (int)x, ly = (int)y;
             bx.add(lx, ly);
             vx = __fadd_rn(vx, w.p.ax[i]);  // :2063-2064
             vy = __fadd_rn(vy, w.p.ay[i]);

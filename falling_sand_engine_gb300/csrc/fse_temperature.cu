@@ -221,7 +221,10 @@ __global__ void __launch_bounds__(TT_THREADS, 4) k_temp_tiles(const WorldDev *__
                 }
                 const int16_t nt = (int16_t)(uint16_t)(uint32_t)r;
                 const bool soup = S.soup[id] != 0;
-                const bool changed = nt != t0 || (me >> 31);
+                // world.cpp:1952-1953, 1996-2001: only the tick zone's cells change
+                const int gy = y0 + ly;
+                const bool inzone = gx >= w.zx && gy >= w.zy && gx < w.zx + w.zw && gy < w.zy + w.zh;
+                const bool changed = inzone && (nt != t0 || (me >> 31));
                 // tile-edge cells are read by the neighbouring tiles: deferred
                 const bool row_ring = (g == 0 && k == 0) || (g == 1 && k == TT_ROWS_PER_THREAD - 1);
                 if (row_ring || col_ring) {

@@ -1247,7 +1247,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
         }
         const int C = w.C, W = w.W, H = w.H;
         const int nb = (w.nCy - oy + 1) / 2;
-        const int cx = (ox + 2 * (slot / nb)) * C, cy = (oy + 2 * (slot % nb)) * C;
+        const int cx = w.zx + (ox + 2 * (slot / nb)) * C, cy = w.zy + (oy + 2 * (slot % nb)) * C;
         const uint32_t cp = (uint32_t)((iter * 4 + tk) * w.max_slots + slot);
 
         TileData Tl;

@@ -194,6 +194,15 @@ int fse_world_download(fse_world *world, uint16_t *id, uint32_t *colour, int32_t
                        int32_t *diff);
 int fse_world_generate(fse_world *world, int kind, uint32_t seed);
 int fse_world_set_tick(fse_world *world, uint32_t tick);
+/* world::tickZone (world.hpp:138; the game sets it every frame to the world less a
+ * chunk on each side, game.cpp:1629-1636): the rectangle x, y, width, height inside
+ * the world that the tick works on. Chunks start at its corner every chunk_size
+ * cells while the start lies in it, and reach chunk_size cells whatever the zone's
+ * end (world.cpp:1078-1087); particles whose cell is outside it neither move nor
+ * age (their velocity is still steered, world.cpp:2039-2061); the temperature step
+ * changes only its cells (world.cpp:1952-2001). The whole world by default. Batches
+ * and servers use the zone their worlds had when they were made. */
+int fse_world_set_tick_zone(fse_world *world, int x, int y, int width, int height);
 int fse_world_get_tile(fse_world *world, int x, int y, uint16_t *id, uint32_t *colour, int32_t *scalar,
                        uint8_t *flags);
 int fse_world_set_tile(fse_world *world, int x, int y, uint16_t id, uint32_t colour, int32_t scalar, uint8_t flags);

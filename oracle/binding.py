@@ -125,6 +125,7 @@ class Oracle:
                 "om_tick_temperature": (None, [vp]),
                 "om_world_set_temperature": (None, [vp, i32]),
                 "om_world_set_f32": (None, [vp, i32]),
+                "om_world_set_tick_zone": (i32, [vp, i32, i32, i32, i32]),
                 "om_temperature_get": (None, [vp, vp]),
                 "om_temperature_set": (None, [vp, vp]),
                 "om_lz4_bound": (i32, [i32]),
@@ -325,6 +326,10 @@ class OracleWorld:
     def enable_temperature(self, on=True):
         self.lib.om_world_set_temperature(self.h_, 1 if on else 0)
 
+    def set_tick_zone(self, x, y, w, h):
+        """world::tickZone (the whole world by default)."""
+        assert self.lib.om_world_set_tick_zone(self.h_, x, y, w, h) == 0
+
     def set_f32(self, on=True):
         """f32 liquid amounts (the library's FSE_CFG_F32_FLUID); before generate / set_state."""
         self.lib.om_world_set_f32(self.h_, 1 if on else 0)
@@ -499,13 +504,15 @@ def build_reference_cells(force=False):
     return REF_CELLS_PATH
 
 
-def reference_tick_cells(lib_path, ids, colours, amounts, mat_types, parts):
-    """One world::tickCells of the compiled reference: (ids, colours, amounts, dirty, survivors)."""
+def reference_tick_cells(lib_path, ids, colours, amounts, mat_types, parts, zone=None):
+    """One world::tickCells of the compiled reference: (ids, colours, amounts, dirty,
+    survivors); zone: world::tickZone (x, y, w, h), None for the whole world."""
     lib = C.CDLL(lib_path)
-    f = lib.ref_tick_cells
+    f = lib.ref_tick_cells_zone
     f.restype = C.c_int
     f.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
-                  C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+                  C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    z = None if zone is None else np.ascontiguousarray(zone, np.int32)
     h, w = ids.shape
     i2 = np.ascontiguousarray(ids, np.uint16).copy()
     c2 = np.ascontiguousarray(colours, np.uint32).copy()
@@ -516,7 +523,7 @@ def reference_tick_cells(lib_path, ids, colours, amounts, mat_types, parts):
     pout = np.zeros(max(len(pin), 1), PARTICLE_DTYPE)
     nout = C.c_int(0)
     rc = f(w, h, _ptr(i2), _ptr(c2), _ptr(a2), _ptr(d2), _ptr(mt), len(mt), _ptr(pin), len(pin), _ptr(pout),
-           C.byref(nout))
+           C.byref(nout), None if z is None else _ptr(z))
     if rc != 0:
         raise ValueError("ref_tick_cells failed")
     return i2, c2, a2, d2, pout[: nout.value].copy()
@@ -616,18 +623,20 @@ def reference_world_tick(lib_path, oracle, ids, colours, temps, moved, cell_iter
 
 
 def reference_world_tick_fluid(lib_path, oracle, ids, colours, temps, moved, amounts, diffs, settle, cell_iter, seed,
-                               tick, n_ticks=1):
+                               tick, n_ticks=1, zone=None):
     """reference_world_tick with every cell's fluidAmount, fluidAmountDiff (f32) and
     settleCount given and returned; particle rows have 17 ints, the last the carried
-    tile's fluidAmount bits."""
+    tile's fluidAmount bits; zone: world::tickZone (x, y, w, h), None for the whole
+    world."""
     lib = C.CDLL(lib_path)
     f = lib.ref_world_tick_fluid
     f.restype = C.c_int
     f.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint32, C.c_uint32, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                   C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
-                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
     n, mats, special, react, inter = _reference_tables(oracle)
     h, w = ids.shape
+    z = None if zone is None else np.ascontiguousarray(zone, np.int32)
     i2 = np.ascontiguousarray(ids, np.uint16).copy()
     c2 = np.ascontiguousarray(colours, np.uint32).copy()
     t2 = np.ascontiguousarray(temps, np.int32).copy()
@@ -640,7 +649,8 @@ def reference_world_tick_fluid(lib_path, oracle, ids, colours, temps, moved, amo
     draws = C.c_longlong(0)
     np_ = f(w, h, cell_iter, seed & 0xFFFFFFFF, tick & 0xFFFFFFFF, n_ticks, n, _ptr(mats), _ptr(special),
             _ptr(np.ascontiguousarray(react)), len(inter), _ptr(np.ascontiguousarray(inter)), _ptr(i2), _ptr(c2),
-            _ptr(t2), _ptr(m2), _ptr(a2), _ptr(d2), _ptr(s2), _ptr(parts), cap, C.byref(draws))
+            _ptr(t2), _ptr(m2), _ptr(a2), _ptr(d2), _ptr(s2), _ptr(parts), cap, C.byref(draws),
+            None if z is None else _ptr(z))
     if np_ < 0:
         raise ValueError("the reference tick wrote outside the grid: the scene needs its solid border")
     return i2, c2, t2, m2, a2, d2, s2, parts[: min(np_, cap)].copy(), draws.value

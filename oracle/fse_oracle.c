@@ -447,6 +447,9 @@ struct om_world {
     /* f32 liquid amounts and diffs (om_world_set_f32): the reference's own float
      * arithmetic; the ledger and census keep no fluid rows */
     int f32;
+    /* world::tickZone (world.hpp:138): chunk origins of the tick, the particles that
+     * move and the cells the temperature step updates; the whole world by default */
+    int zx, zy, zw, zh;
 };
 
 static inline void mark_dirty(om_world *w, size_t i) {
@@ -503,7 +506,23 @@ om_world *om_world_new(int w, int h, int chunk, int cell_iter, uint32_t seed) {
     wd->tp = (int16_t *)calloc(n, 2);
     wd->vis = (uint8_t *)calloc(n, 1);
     for (size_t i = 0; i < n; i++) wd->id[i] = (uint16_t)ID_AIR;
+    wd->zx = 0;
+    wd->zy = 0;
+    wd->zw = w;
+    wd->zh = h;
     return wd;
+}
+
+int om_world_set_tick_zone(om_world *wd, int x, int y, int w, int h) {
+    if (x < 0 || y < 0 || w < 0 || h < 0 || x + w > wd->W || y + h > wd->H) return -1;
+    wd->zx = x;
+    wd->zy = y;
+    wd->zw = w;
+    wd->zh = h;
+    return 0;
+}
+static inline int in_zone(const om_world *w, int x, int y) {
+    return x >= w->zx && y >= w->zy && x < w->zx + w->zw && y < w->zy + w->zh;
 }
 
 void om_world_free(om_world *wd) {
@@ -1461,7 +1480,9 @@ long om_world_tick(om_world *w, int order, int check_races) {
     w->check = check_races ? 1 : 0;
     w->viol = 0;
     if (w->check) chk_init(w);
-    int nCx = (w->W + w->C - 1) / w->C, nCy = (w->H + w->C - 1) / w->C;
+    /* chunks start at the tick zone's corner, every C cells while the start is in the
+     * zone (world.cpp:1078-1079); a chunk reaches C cells whatever the zone's end */
+    int nCx = (w->zw + w->C - 1) / w->C, nCy = (w->zh + w->C - 1) / w->C;
     size_t ncell = (size_t)w->W * w->H;
     for (int iter = 0; iter < w->cell_iter; iter++) { /* world.cpp:1050 */
         for (int tk = 0; tk < 4; tk++) {              /* world.cpp:1057-1060 */
@@ -1476,7 +1497,7 @@ long om_world_tick(om_world *w, int order, int check_races) {
 #pragma omp parallel for schedule(dynamic, 1) if (!w->check)
             for (int s = 0; s < nslot; s++) {
                 int a = s / nb, b = s % nb;
-                int cx = (ox + 2 * a) * w->C, cy = (oy + 2 * b) * w->C;
+                int cx = w->zx + (ox + 2 * a) * w->C, cy = w->zy + (oy + 2 * b) * w->C;
                 process_chunk(w, order, iter, cx, cy, &sp[s]);
             }
             /* world.cpp:1901-1913: append spawned particles in task order */
@@ -1553,6 +1574,7 @@ static int particle_move(om_world *w, om_particle *p, int *out, int *lx_o, int *
         *out = OUT_DEAD;
         return -2; /* exited */
     }
+    if (!in_zone(w, lx, ly)) return REQ_NONE; /* :2061, outside the tick zone: kept as it is */
     p->vx += p->ax; /* :2063-2064 */
     p->vy += p->ay;
     int div = (int)((fabsf(p->vx) + fabsf(p->vy)) + 1);
@@ -1884,7 +1906,8 @@ void om_tick_temperature(om_world *w) {
                 r = f2i_x86((float)m->add_temp + v / nn * m->cond_self + (float)t0 * (1.0f - m->cond_self));
             else
                 r = (int32_t)(m->add_temp + (uint32_t)t0); /* u32 + int, stored into i32 */
-            temp_put(w, i, (int16_t)(uint16_t)(uint32_t)r);
+            /* world.cpp:1952-1953, 1996-2001: only the tick zone's cells change */
+            if (in_zone(w, x, y)) temp_put(w, i, (int16_t)(uint16_t)(uint32_t)r);
         }
     free(old);
 }

@@ -104,6 +104,10 @@ void om_world_set_temperature(om_world *wd, int on);
 /* f32 liquid amounts and diffs: the reference's own float arithmetic (the GPU's
  * FSE_CFG_F32_FLUID); set before the world is generated or loaded */
 void om_world_set_f32(om_world *wd, int on);
+/* world::tickZone: the rectangle inside the world whose chunks tick (from its
+ * corner), whose particles move and whose temperatures conduct; -1 if it is not
+ * inside the world */
+int om_world_set_tick_zone(om_world *wd, int x, int y, int w, int h);
 /* chunk .pack codec (chunk.cpp:219-330): LZ4 block format helpers and whole-world
  * pack/unpack, chunks row-major; see fse_oracle.c for the layout */
 int om_lz4_bound(int n);

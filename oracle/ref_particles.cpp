@@ -81,10 +81,12 @@ static_assert(sizeof(Part) == 60, "particle record");
 
 // One world::tickCells on a w x h grid. Cells: material index, colour, fluid amount
 // (Q16.16, exact in float for the amounts used) and the material types; particles
-// in list order. The tick zone is the whole world. Outputs the grid (same arrays,
-// updated), the dirty marks, and the surviving particles in order (*n_out).
-extern "C" int ref_tick_cells(int w, int h, uint16_t *id, uint32_t *colour, int32_t *amount, uint8_t *dirty,
-                              const int32_t *mat_type, int n_mat, const Part *in, int n_in, Part *out, int *n_out) {
+// in list order; the tick zone (x, y, w, h; NULL: the whole world). Outputs the grid
+// (same arrays, updated), the dirty marks, and the surviving particles in order
+// (*n_out).
+static int tick_cells(int w, int h, uint16_t *id, uint32_t *colour, int32_t *amount, uint8_t *dirty,
+                      const int32_t *mat_type, int n_mat, const Part *in, int n_in, Part *out, int *n_out,
+                      const int32_t *zone) {
     std::vector<Material> mats((size_t)n_mat);
     for (int k = 0; k < n_mat; k++) {
         mats[k].id = k;
@@ -103,7 +105,7 @@ extern "C" int ref_tick_cells(int w, int h, uint16_t *id, uint32_t *colour, int3
     world wd;
     wd.width = w;
     wd.height = h;
-    wd.tickZone = TickZone{0, 0, w, h};
+    wd.tickZone = zone ? TickZone{zone[0], zone[1], zone[2], zone[3]} : TickZone{0, 0, w, h};
     wd.real_tiles = tiles.data();
     static_assert(sizeof(bool) == 1, "bool");
     wd.dirty = reinterpret_cast<bool *>(dflag.data());
@@ -158,4 +160,15 @@ extern "C" int ref_tick_cells(int w, int h, uint16_t *id, uint32_t *colour, int3
     }
     for (CellData *c : wd.cells) delete c;
     return 0;
+}
+
+extern "C" int ref_tick_cells(int w, int h, uint16_t *id, uint32_t *colour, int32_t *amount, uint8_t *dirty,
+                              const int32_t *mat_type, int n_mat, const Part *in, int n_in, Part *out, int *n_out) {
+    return tick_cells(w, h, id, colour, amount, dirty, mat_type, n_mat, in, n_in, out, n_out, nullptr);
+}
+
+extern "C" int ref_tick_cells_zone(int w, int h, uint16_t *id, uint32_t *colour, int32_t *amount, uint8_t *dirty,
+                                   const int32_t *mat_type, int n_mat, const Part *in, int n_in, Part *out,
+                                   int *n_out, const int32_t *zone) {
+    return tick_cells(w, h, id, colour, amount, dirty, mat_type, n_mat, in, n_in, out, n_out, zone);
 }

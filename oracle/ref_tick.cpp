@@ -372,7 +372,7 @@ static int tick_planes(int W, int H, int cell_iter, uint32_t seed, uint32_t tick
                        const int32_t *mats, const int32_t *special, const int32_t *reactions, int ni,
                        const int32_t *inter, uint16_t *ids, uint32_t *cols, int32_t *temps, uint8_t *moved,
                        float *amounts, float *diffs, uint8_t *settle, int32_t *parts, int row, int cap,
-                       long long *draws) {
+                       long long *draws, const int32_t *zone) {
     Registry reg;
     setup_registry(reg, n, mats, special, reactions, ni, inter);
 
@@ -398,7 +398,7 @@ static int tick_planes(int W, int H, int cell_iter, uint32_t seed, uint32_t tick
     wd.tickVisited2 = reinterpret_cast<bool *>(tv2.data());
     wd.flowX = fx.data();
     wd.flowY = fy.data();
-    wd.tickZone = TickZone{0, 0, W, H};
+    wd.tickZone = zone ? TickZone{zone[0], zone[1], zone[2], zone[3]} : TickZone{0, 0, W, H};
     global.game->Iso.globaldef.cell_iter = cell_iter;
     g_seed = seed;
     g_draws = 0;
@@ -449,18 +449,19 @@ extern "C" int ref_world_tick(int W, int H, int cell_iter, uint32_t seed, uint32
                               const int32_t *inter, uint16_t *ids, uint32_t *cols, int32_t *temps, uint8_t *moved,
                               int32_t *parts, int cap, long long *draws) {
     return tick_planes(W, H, cell_iter, seed, tick, n_ticks, n, mats, special, reactions, ni, inter, ids, cols, temps,
-                       moved, nullptr, nullptr, nullptr, parts, 16, cap, draws);
+                       moved, nullptr, nullptr, nullptr, parts, 16, cap, draws, nullptr);
 }
 
 // the same with every cell's fluidAmount, fluidAmountDiff and settleCount in and out,
-// and particle rows of 17 ints (the carried tile's fluidAmount bits last)
+// particle rows of 17 ints (the carried tile's fluidAmount bits last) and the tick
+// zone (x, y, w, h; NULL: the whole world)
 extern "C" int ref_world_tick_fluid(int W, int H, int cell_iter, uint32_t seed, uint32_t tick, int n_ticks, int n,
                                     const int32_t *mats, const int32_t *special, const int32_t *reactions, int ni,
                                     const int32_t *inter, uint16_t *ids, uint32_t *cols, int32_t *temps,
                                     uint8_t *moved, float *amounts, float *diffs, uint8_t *settle, int32_t *parts,
-                                    int cap, long long *draws) {
+                                    int cap, long long *draws, const int32_t *zone) {
     return tick_planes(W, H, cell_iter, seed, tick, n_ticks, n, mats, special, reactions, ni, inter, ids, cols, temps,
-                       moved, amounts, diffs, settle, parts, 17, cap, draws);
+                       moved, amounts, diffs, settle, parts, 17, cap, draws, zone);
 }
 
 // Timing: the reference's own world::tick() + world::tickCells() on a grid (ids,
