@@ -962,6 +962,10 @@ int fse_world_set_tick_zone(fse_world *w, int x, int y, int width, int height) {
     h.nCy = ceil_div(height, h.C);
     int rc = world_items(w);
     if (rc) return rc;
+    // the colour passes write the spawn counts of the zone's chunk slots only, and the
+    // spawn scan sums every slot: counts left by a larger zone must go
+    const size_t ncp = (size_t)h.cell_iter * 4 * h.max_slots * h.cp_rows + 1;
+    FSE_CUDA_TRY(cudaMemset(h.cp_count, 0, ncp * sizeof(int32_t)));
     FSE_CUDA_TRY(cudaMemcpy(w->d, &h, sizeof(WorldDev), cudaMemcpyHostToDevice));
     // captured step graphs hold the old chunk counts
     for (auto &g : w->graphs) cudaGraphExecDestroy(g.second);

@@ -66,6 +66,8 @@ def test_device_zone_steps_match_oracle(fse, oracle_mod, zone):
 
 
 def test_zone_change_invalidates_step_graphs(fse, oracle_mod):
+    """A zone set after ticks: the step graphs are captured again and the spawn
+    counts of chunk slots the smaller zone no longer has are cleared."""
     types = material_types(fse)
     w, h, seed = 384, 256, 52
     world = fse.World(w, h, seed=seed)
@@ -74,11 +76,14 @@ def test_zone_change_invalidates_step_graphs(fse, oracle_mod):
     ow.generate(0, seed)
     world.step(4, graph=True)
     ow.step(4, ORDER_PART)
+    compare_states(world.state(), ow.state(), types, "before the zone change")
+    compare_particles(world.particles(), ow.particles(), "before the zone change")
     world.set_tick_zone(128, 0, 256, 256)
     ow.set_tick_zone(128, 0, 256, 256)
     world.step(4, graph=True)
     ow.step(4, ORDER_PART)
     compare_states(world.state(), ow.state(), types, "after the zone change")
+    compare_particles(world.particles(), ow.particles(), "after the zone change")
     with pytest.raises(fse.FseError):
         world.set_tick_zone(200, 0, 256, 256)  # reaches past the world
     world.close()
