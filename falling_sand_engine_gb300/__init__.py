@@ -237,6 +237,17 @@ class World:
                                                 0 if tab is None else tab.size), "download_tiles")
         return out
 
+    def particle_iterations(self):
+        """Iterations the last particle update needed (diagnostics)."""
+        n = C.c_int()
+        check(self.lib.fse_world_particle_iterations(self.h, C.byref(n)), "world_particle_iterations")
+        return n.value
+
+    def set_launch(self, colour_shape):
+        """Launch shape of the colour pass: 0 CTA per chunk, 1 persistent CTAs, 2 CTA pair
+        per chunk, 3 persistent pairs (results never depend on it)."""
+        check(self.lib.fse_world_set_launch(self.h, colour_shape), "world_set_launch")
+
     def set_tick_zone(self, x, y, w, h):
         """world::tickZone: the rectangle the tick works on (the whole world by default)."""
         check(self.lib.fse_world_set_tick_zone(self.h, x, y, w, h), "world_set_tick_zone")

@@ -99,6 +99,8 @@ SIGNATURES = {
     "fse_world_generate": (_i, [_vp, _i, _u32]),
     "fse_world_set_tick": (_i, [_vp, _u32]),
     "fse_world_set_tick_zone": (_i, [_vp, _i, _i, _i, _i]),
+    "fse_world_set_launch": (_i, [_vp, _i]),
+    "fse_world_particle_iterations": (_i, [_vp, C.POINTER(_i)]),
     "fse_world_get_tile": (_i, [_vp, _i, _i, _vp, _vp, _vp, _vp]),
     "fse_world_set_tile": (_i, [_vp, _i, _i, C.c_uint16, _u32, C.c_int32, C.c_uint8]),
     "fse_world_tick": (_i, [_vp, _i]),

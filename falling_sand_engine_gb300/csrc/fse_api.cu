@@ -882,6 +882,7 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
     h.err = w->ctr + 5;
     h.tick = (uint32_t *)(w->ctr + 6);
     h.bar = (unsigned *)(w->ctr + 8);  // [8] arrivals, [9] generation
+    h.stats = w->ctr + 10;             // [10] iterations of the last particle update
     cudaMemset(w->ctr, 0, 16 * sizeof(int32_t));
     cudaMemset(h.ledger, 0, LED_ROWS * MAXMAT * sizeof(long long));
     cudaMemset(h.cp_count, 0, ncp * sizeof(int32_t));
@@ -924,6 +925,15 @@ static uint32_t read_tick(fse_world *w) {
     return t;
 }
 
+int fse_world_particle_iterations(fse_world *w, int *out) {
+    if (!w || !out) return FSE_E_INVAL;
+    int32_t c[16];
+    int rc = read_ctr(w, c);
+    if (rc) return rc;
+    *out = c[10];
+    return FSE_OK;
+}
+
 int fse_world_info(const fse_world *wc, int32_t out[8]) {
     fse_world *w = (fse_world *)wc;
     if (!w || !out) return FSE_E_INVAL;
@@ -945,6 +955,16 @@ int fse_world_set_tick(fse_world *w, uint32_t tick) {
     if (!w) return FSE_E_INVAL;
     FSE_CUDA_TRY(cudaMemcpyAsync(w->h.tick, &tick, 4, cudaMemcpyHostToDevice, w->stream));
     FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
+    return FSE_OK;
+}
+
+int fse_world_set_launch(fse_world *w, int colour_shape_id) {
+    if (!w || colour_shape_id < 0 || colour_shape_id > 3) return FSE_E_INVAL;
+    FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
+    colour_shape(colour_shape_id, &w->threads, &w->grid);
+    for (auto &g : w->graphs) cudaGraphExecDestroy(g.second);
+    w->graphs.clear();
+    w->graph_kernels.clear();
     return FSE_OK;
 }
 

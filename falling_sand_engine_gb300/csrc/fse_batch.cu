@@ -349,9 +349,8 @@ int fse_batch_timing(fse_batch *b, int enable, double *out_pass_ms, int64_t *out
 }
 
 int fse_batch_set_launch(fse_batch *b, int colour_ctas_per_sm, int particle_blocks) {
-    if (!b || colour_ctas_per_sm < 0 || colour_ctas_per_sm > 1 || particle_blocks < 0) return FSE_E_INVAL;
-    // one 1024-thread CTA fits an SM, so the persistent grid is one CTA per SM
-    b->grid = colour_ctas_per_sm == 0 ? 0 : sm_count();
+    if (!b || colour_ctas_per_sm < 0 || colour_ctas_per_sm > 3 || particle_blocks < 0) return FSE_E_INVAL;
+    colour_shape(colour_ctas_per_sm, &b->threads, &b->grid);
     b->move_blocks = particle_blocks == 0 ? b->max_move_blocks : std::min(particle_blocks, b->max_move_blocks);
     for (auto &g : b->graphs) cudaGraphExecDestroy(g.second);
     b->graphs.clear();
@@ -379,13 +378,14 @@ int fse_batch_autotune(fse_batch *b, int32_t out_choice[4]) {
     // the candidates' steps are not part of any timing the caller asked for
     PassTimer *keep_timer = b->timer;
     b->timer = nullptr;
-    const int cand[][2] = {{0, 0}, {1, 0}, {0, 4}, {0, 16}, {1, 16}};
+    const int cand[][2] = {{0, 0}, {1, 0}, {0, 4}, {0, 16}, {1, 16}, {2, 4}, {3, 4}, {2, 16}};
+    const int n_cand = (int)(sizeof(cand) / sizeof(cand[0]));
     float best = 1e30f;
     int bi = 0;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    for (int c = 0; c < 5; c++) {
+    for (int c = 0; c < n_cand; c++) {
         fse_batch_set_launch(b, cand[c][0], cand[c][1]);
         batch_enqueue(b, 1);  // warm-up
         cudaEventRecord(e0, b->stream);

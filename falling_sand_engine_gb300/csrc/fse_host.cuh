@@ -117,6 +117,15 @@ int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], con
                  bool f32 = false);
 void count_launches(long long n);
 
+// Launch shapes of the colour pass (threads per CTA, chunk workers; 0 = one per chunk):
+// 0 one 1024-thread CTA per chunk; 1 one persistent CTA per SM walking the chunks;
+// 2 each chunk split over a CTA pair (a cluster of two 512-thread CTAs); 3 persistent
+// pairs, two CTAs per SM
+inline void colour_shape(int shape, int *threads, int *grid) {
+    *threads = shape >= 2 ? 512 : 1024;
+    *grid = (shape == 1 || shape == 3) ? sm_count() : 0;
+}
+
 }  // namespace fse
 
 #define FSE_CUDA_TRY(expr)                     \

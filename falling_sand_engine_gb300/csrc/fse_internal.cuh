@@ -176,7 +176,8 @@ struct WorldDev {
     // fill cell an iteration moved it away from; box0 holds the merge cell afterwards
     int32_t *p_box0, *p_box1, *p_cell, *p_prev;
     int32_t *req_count;     // [3] counters of the update (fill changes of even / odd iterations)
-    uint8_t *chg;           // 2 x airmap blocks: blocks whose fills changed (read / written by an iteration)
+    uint32_t *chg;          // 2 x airmap blocks: lowest index whose fill changed there (read / written by an iteration)
+    int32_t *stats;         // [0]: iterations of the last particle update (of the launch's first world)
     int32_t *scan_tmp;      // block sums for compaction
     long long *ledger;      // [LED_ROWS][MAXMAT]
     int32_t *err;

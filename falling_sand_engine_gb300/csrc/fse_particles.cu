@@ -192,8 +192,8 @@ __global__ void k_air_map(const WorldDev *__restrict__ worlds, const MatTable *_
                 }
             }
         w.airmap[b] = any;
-        w.chg[b] = 0;
-        w.chg[nb + b] = 0;
+        w.chg[b] = 0xFFFFFFFFu;
+        w.chg[nb + b] = 0xFFFFFFFFu;
     }
 }
 
@@ -386,132 +386,177 @@ __device__ __forceinline__ void grid_sync(GridBar *gb, unsigned nblocks, int32_t
 }
 
 constexpr int SERIAL_MAX_ITER = 1 << 16;
+constexpr int SERIAL_MAX_WORLDS = 4096;  // worlds of one launch (a batch holds at most 4095)
+
+// particle g of the launch's worlds taken together: its world (s_pref: prefix sums of
+// the worlds' particle counts, in shared memory) and index in that world
+__device__ __forceinline__ int world_of(const int *s_pref, int n_worlds, int g) {
+    int lo = 0, hi = n_worlds - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_pref[mid] <= g)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
 
 // The fixed-point iteration and the commit for every world of the table, in one
-// cooperative launch (every block resident, so the grid barrier is safe).
-// req_count[0..1] of world 0 count the fill changes of even and odd iterations.
-__global__ void k_part_serial(const WorldDev *__restrict__ worlds, int n_worlds, const MatTable *__restrict__ mt) {
+// cooperative launch (every block resident, so the grid barrier is safe). The
+// particles of all worlds are taken as one index space. Change marks are per 8x8
+// block the lowest index whose fill moved into or out of the block: a particle is
+// computed again only if a lower index changed a fill near what it read.
+// req_count[0..1] of world 0 count the fill changes of even and odd iterations;
+// stats[0] of world 0 receives the number of iterations.
+__global__ void __launch_bounds__(256) k_part_serial(const WorldDev *__restrict__ worlds, int n_worlds,
+                                                      const MatTable *__restrict__ mt) {
     __shared__ uint8_t s_type[MAXMAT];
+    __shared__ int s_pref[SERIAL_MAX_WORLDS + 1];
     load_types(s_type, mt);
+    for (int k = threadIdx.x; k < n_worlds; k += blockDim.x) s_pref[k + 1] = *worlds[k].part_count;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        s_pref[0] = 0;
+        for (int k = 0; k < n_worlds; k++) s_pref[k + 1] += s_pref[k];
+    }
+    __syncthreads();
+    const int total = s_pref[n_worlds];
     GridBar *gb = (GridBar *)worlds[0].bar;
     const unsigned nb = gridDim.x;
     int32_t *err = worlds[0].err;
     int32_t *cnt = worlds[0].req_count;
     const int gtid = (int)(blockIdx.x * blockDim.x + threadIdx.x), gstride = (int)(gridDim.x * blockDim.x);
-    for (int it = 0;; it++) {
+    int it = 0;
+    for (;; it++) {
         if (it >= SERIAL_MAX_ITER) {
             if (gtid == 0) atomicOr(err, ERR_TIMEOUT);
             break;
         }
         const int par = it & 1;
-        // A: outcomes of the particles whose box saw a changed fill (all at first);
-        // changed fills are counted and their blocks marked for the next iteration
-        for (int wi = 0; wi < n_worlds; wi++) {
+        // A: outcomes of the particles whose box saw a fill change by a lower index (all
+        // at first); changed fills are counted and their blocks marked for the next
+        // iteration with the changing index
+        for (int g = gtid; g < total; g += gstride) {
+            const int wi = world_of(s_pref, n_worlds, g);
             const WorldDev &w = worlds[wi];
-            const int n = *w.part_count;
+            const int i = g - s_pref[wi];
             const int nblk = w.amw * w.amh;
-            const uint8_t *seen = w.chg + (size_t)par * nblk;
-            uint8_t *mark = w.chg + (size_t)(1 - par) * nblk;
-            for (int i = gtid; i < n; i += gstride) {
-                int before = -1;
-                if (it > 0) {
-                    const int32_t b0 = w.p_box0[i];
-                    if (b0 < 0) continue;  // read no cell: nothing can change it
-                    const int32_t b1 = w.p_box1[i];
-                    const int x0 = (b0 & 0xFFFF) >> 3, y0 = ((uint32_t)b0 >> 16) >> 3;
-                    const int x1 = (b1 & 0xFFFF) >> 3, y1 = ((uint32_t)b1 >> 16) >> 3;
-                    bool touched = false;
-                    for (int by = y0; by <= y1 && !touched; by++)
-                        for (int bxx = x0; bxx <= x1; bxx++)
-                            if (__ldcg(&seen[by * w.amw + bxx])) {
-                                touched = true;
-                                break;
-                            }
-                    if (!touched) continue;
-                    before = fill_of(w, i);
-                }
-                part_outcome(w, s_type, i);
-                const int after = fill_of(w, i);
-                if (after != before) {
-                    atomicAdd(&cnt[par], 1);
-                    if (before >= 0) mark[(before / w.W >> 3) * w.amw + ((before % w.W) >> 3)] = 1;
-                    if (after >= 0) mark[(after / w.W >> 3) * w.amw + ((after % w.W) >> 3)] = 1;
-                    w.p_prev[i] = before;  // the cell whose record B1 clears
-                } else {
-                    w.p_prev[i] = -1;
-                }
+            const uint32_t *seen = w.chg + (size_t)par * nblk;
+            uint32_t *mark = w.chg + (size_t)(1 - par) * nblk;
+            int before = -1;
+            if (it > 0) {
+                const int32_t b0 = w.p_box0[i];
+                if (b0 < 0) continue;  // read no cell: nothing can change it
+                const int32_t b1 = w.p_box1[i];
+                const int x0 = (b0 & 0xFFFF) >> 3, y0 = ((uint32_t)b0 >> 16) >> 3;
+                const int x1 = (b1 & 0xFFFF) >> 3, y1 = ((uint32_t)b1 >> 16) >> 3;
+                bool touched = false;
+                for (int by = y0; by <= y1 && !touched; by++)
+                    for (int bxx = x0; bxx <= x1; bxx++)
+                        if (__ldcg(&seen[by * w.amw + bxx]) < (uint32_t)i) {
+                            touched = true;
+                            break;
+                        }
+                if (!touched) continue;
+                before = fill_of(w, i);
+            }
+            part_outcome(w, s_type, i);
+            const int after = fill_of(w, i);
+            if (after != before) {
+                atomicAdd(&cnt[par], 1);
+                if (before >= 0) atomicMin(&mark[(before / w.W >> 3) * w.amw + ((before % w.W) >> 3)], (uint32_t)i);
+                if (after >= 0) atomicMin(&mark[(after / w.W >> 3) * w.amw + ((after % w.W) >> 3)], (uint32_t)i);
+                w.p_prev[i] = before;  // the cell whose record B1 clears
+            } else {
+                w.p_prev[i] = -1;
             }
         }
         grid_sync(gb, nb, err);
         const int changed = __ldcg(&cnt[par]);
         if (changed == 0) break;
-        // B1: clear the records of fills that moved away; the marks read in A are done
-        for (int wi = 0; wi < n_worlds; wi++) {
+        // B1: clear the records of fills that moved away and the marks read in A
+        for (int g = gtid; g < total; g += gstride) {
+            const int wi = world_of(s_pref, n_worlds, g);
             const WorldDev &w = worlds[wi];
-            const int n = *w.part_count;
-            const int nblk = w.amw * w.amh;
-            for (int i = gtid; i < n; i += gstride) {
-                const int c = w.p_prev[i];
-                if (c >= 0) w.df[c] = 0;
+            const int i = g - s_pref[wi];
+            const int c = w.p_prev[i];
+            if (c >= 0) {
+                w.df[c] = 0;
                 w.p_prev[i] = -1;
             }
-            uint8_t *seen = w.chg + (size_t)par * nblk;
-            for (int b = gtid; b < nblk; b += gstride) seen[b] = 0;
+        }
+        for (int wi = 0; wi < n_worlds; wi++) {
+            const WorldDev &w = worlds[wi];
+            if (s_pref[wi + 1] == s_pref[wi]) continue;
+            const int nblk = w.amw * w.amh;
+            uint32_t *seen = w.chg + (size_t)par * nblk;
+            for (int b = gtid; b < nblk; b += gstride) seen[b] = 0xFFFFFFFFu;
         }
         if (gtid == 0) cnt[1 - par] = 0;
         grid_sync(gb, nb, err);
         // B2: every current fill records itself; the lowest index stays
-        for (int wi = 0; wi < n_worlds; wi++) {
+        for (int g = gtid; g < total; g += gstride) {
+            const int wi = world_of(s_pref, n_worlds, g);
             const WorldDev &w = worlds[wi];
-            const int n = *w.part_count;
-            for (int i = gtid; i < n; i += gstride) {
-                const int c = fill_of(w, i);
-                if (c >= 0) atomicMax(&w.df[c], fill_code(i));
-            }
+            const int i = g - s_pref[wi];
+            const int c = fill_of(w, i);
+            if (c >= 0) atomicMax(&w.df[c], fill_code(i));
         }
         grid_sync(gb, nb, err);
     }
     // the sequential outcome: commit it
-    for (int wi = 0; wi < n_worlds; wi++) {
+    for (int g = gtid; g < total; g += gstride) {
+        const int wi = world_of(s_pref, n_worlds, g);
         const WorldDev &w = worlds[wi];
-        const int n = *w.part_count;
-        for (int i = gtid; i < n; i += gstride) {
-            const uint8_t k = w.p_state[i];
-            const int c = w.p_cell[i];
-            if (k == PS_EXIT || k == PS_DESTROY) {
-                led_part(w, mt, k == PS_EXIT ? LED_XN : LED_DN, k == PS_EXIT ? LED_XF : LED_DF, w.p.id[i], w.p.sc[i]);
-                w.p_state[i] = PS_DEAD;
-            } else if (k == PS_FILL) {  // :2115-2118, :2148-2152
-                w.id[c] = w.p.id[i];
-                w.col[c] = w.p.col[i];
-                w.sc[c] = w.p.sc[i];
-                w.fl[c] = w.p.fl[i];
-                w.df[c] = 0;
-                // the target was AIR, whose temperature word means nothing: the particle's
-                // (a SOUP tile's temperature; 0 for the others) is stored without a type test
-                if (w.tp) w.tp[c] = w.p.tp[i];
-                if (w.dirty) w.dirty[c] = 1;
-                w.p_state[i] = PS_DEAD;
-            } else if (k == PS_MERGE) {  // :2119-2125, added by k_merge in particle order
-                w.p_box0[i] = c;
-                w.merge_list[atomicAdd(w.merge_count, 1)] = i;
-                if (w.dirty) w.dirty[c] = 1;
-                atomicAdd((unsigned long long *)&w.ledger[LED_DN * MAXMAT + w.p.id[i]], 1ull);
-                w.p_state[i] = PS_DEAD;
-            } else {  // PS_ALIVE, PS_FAIL: the particle lives on
-                w.p.x[i] = w.q.x[i];
-                w.p.y[i] = w.q.y[i];
-                w.p.vx[i] = w.q.vx[i];
-                w.p.vy[i] = w.q.vy[i];
-                w.p.bits[i] = w.q.bits[i];
-                w.p.life[i] = w.q.life[i];
-                w.p_state[i] = PS_ALIVE;
-            }
+        const int i = g - s_pref[wi];
+        const uint8_t k = w.p_state[i];
+        const int c = w.p_cell[i];
+        if (k == PS_EXIT || k == PS_DESTROY) {
+            led_part(w, mt, k == PS_EXIT ? LED_XN : LED_DN, k == PS_EXIT ? LED_XF : LED_DF, w.p.id[i], w.p.sc[i]);
+            w.p_state[i] = PS_DEAD;
+        } else if (k == PS_FILL) {  // :2115-2118, :2148-2152
+            w.id[c] = w.p.id[i];
+            w.col[c] = w.p.col[i];
+            w.sc[c] = w.p.sc[i];
+            w.fl[c] = w.p.fl[i];
+            w.df[c] = 0;
+            // the target was AIR, whose temperature word means nothing: the particle's
+            // (a SOUP tile's temperature; 0 for the others) is stored without a type test
+            if (w.tp) w.tp[c] = w.p.tp[i];
+            if (w.dirty) w.dirty[c] = 1;
+            w.p_state[i] = PS_DEAD;
+        } else if (k == PS_MERGE) {  // :2119-2125, added by k_merge in particle order
+            w.p_box0[i] = c;
+            w.merge_list[atomicAdd(w.merge_count, 1)] = i;
+            if (w.dirty) w.dirty[c] = 1;
+            atomicAdd((unsigned long long *)&w.ledger[LED_DN * MAXMAT + w.p.id[i]], 1ull);
+            w.p_state[i] = PS_DEAD;
+        } else {  // PS_ALIVE, PS_FAIL: the particle lives on
+            w.p.x[i] = w.q.x[i];
+            w.p.y[i] = w.q.y[i];
+            w.p.vx[i] = w.q.vx[i];
+            w.p.vy[i] = w.q.vy[i];
+            w.p.bits[i] = w.q.bits[i];
+            w.p.life[i] = w.q.life[i];
+            w.p_state[i] = PS_ALIVE;
+        }
+    }
+    // the marks of the last iteration are cleared for the next update
+    {
+        const int par = it & 1;
+        for (int wi = 0; wi < n_worlds; wi++) {
+            const WorldDev &w = worlds[wi];
+            if (s_pref[wi + 1] == s_pref[wi]) continue;
+            const int nblk = w.amw * w.amh;
+            uint32_t *mark = w.chg + (size_t)(1 - par) * nblk;
+            for (int b = gtid; b < nblk; b += gstride) mark[b] = 0xFFFFFFFFu;
         }
     }
     if (gtid == 0) {
         cnt[0] = 0;
         cnt[1] = 0;
+        worlds[0].stats[0] = it + 1;
     }
 }
 

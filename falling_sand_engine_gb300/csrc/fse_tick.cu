@@ -125,16 +125,84 @@ struct TileData {
     // sweep-B pillar snapshot: AIR bits of columns ax0.., rows ay0.., 5 words per column
     const uint32_t *s_air;
     int ax0, ay0, aw;
+    // a chunk split over a CTA pair: the partner's copy of the planes (shared::cluster
+    // addresses) and the world row of its first tile row; both copies have RW, RHF
+    // and RHI of this one
+    uint32_t p_id, p_fl, p_sc, p_col;
+    int py0;
 };
+
+// --------------------------------------------------- CTA-pair (cluster) helpers
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+// the address of this CTA's shared location `a` in the shared memory of cluster rank r
+__device__ __forceinline__ uint32_t mapa_rank(uint32_t a, uint32_t r) {
+    uint32_t o;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(o) : "r"(a), "r"(r));
+    return o;
+}
+__device__ __forceinline__ void st_cluster_u8(uint32_t a, uint8_t v) {
+    asm volatile("st.shared::cluster.u8 [%0], %1;" ::"r"(a), "h"((unsigned short)v) : "memory");
+}
+__device__ __forceinline__ void st_cluster_u16(uint32_t a, uint16_t v) {
+    asm volatile("st.shared::cluster.u16 [%0], %1;" ::"r"(a), "h"(v) : "memory");
+}
+__device__ __forceinline__ void st_cluster_u32(uint32_t a, uint32_t v) {
+    asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+// every thread of both CTAs of the pair; the partner's shared-memory stores made
+// before it are visible after it
+__device__ __forceinline__ void cluster_sync() {
+    asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
 
 // LIVE: the pillar reads the tile as it stands (the reference's own order, where
 // one thread updates the chunk's cells in turn) instead of the sweep-B snapshot.
 // F32: liquid amounts and diffs are f32 bit patterns (FSE_CFG_F32_FLUID).
-template <bool EDGE, bool TEMP, bool LIVE = false, bool F32 = false>
+// PAIR: the chunk is split over a CTA pair; every write to a row the partner's tile
+// holds is made in both copies (reads are always local), so both copies of the
+// shared rows stay equal; at the end of a sub-phase the cluster barrier makes them
+// visible.
+template <bool EDGE, bool TEMP, bool LIVE = false, bool F32 = false, bool PAIR = false>
 struct Tile : TileData {
     static constexpr bool kTemp = TEMP;
     static constexpr bool kF32 = F32;
     __device__ __forceinline__ explicit Tile(const TileData &d) : TileData(d) {}
+
+    // the partner's index of cell (x, y): -1 outside its tile; *full: a full-state row
+    __device__ __forceinline__ int pli(int x, int y, bool *full) const {
+        const int r = y - py0;
+        if (r < 0 || r >= RHI) return -1;
+        *full = r < RHF;
+        return r * RW + (x - x0);
+    }
+    // the same bytes as the local copy of cell i, in the partner's copy of (x, y)
+    __device__ __forceinline__ void mirror(int x, int y, int i) const {
+        if constexpr (PAIR) {
+            bool full;
+            const int j = pli(x, y, &full);
+            if (j < 0) return;
+            st_cluster_u16(p_id + 2u * (uint32_t)j, s_id[i]);
+            if (full) {
+                st_cluster_u8(p_fl + (uint32_t)j, s_fl[i]);
+                st_cluster_u32(p_sc + 4u * (uint32_t)j, (uint32_t)s_sc[i]);
+                st_cluster_u32(p_col + 4u * (uint32_t)j, s_col[i]);
+            }
+        }
+    }
+    __device__ __forceinline__ void mirror_idfl(int x, int y, int i) const {
+        if constexpr (PAIR) {
+            bool full;
+            const int j = pli(x, y, &full);
+            if (j < 0) return;
+            st_cluster_u16(p_id + 2u * (uint32_t)j, s_id[i]);
+            if (full) st_cluster_u8(p_fl + (uint32_t)j, s_fl[i]);
+        }
+    }
 
     // 10 AIR bits of column x starting at row y: from the snapshot (0 outside it), or
     // live
@@ -195,6 +263,7 @@ struct Tile : TileData {
         s_fl[i] = (uint8_t)((c.fl & (uint8_t)~VISITED) | (s_fl[i] & VISITED));
         s_sc[i] = c.sc;
         s_col[i] = c.col;
+        mirror(x, y, i);
         if (c.df != 0) atomicAdd(&df[y * W + x], c.df);  // no return value: a fire-and-forget reduction
     }
     // world.cpp:1004-1008: outside the world writes are dropped
@@ -205,6 +274,7 @@ struct Tile : TileData {
         s_fl[i] = (uint8_t)((c.fl & (uint8_t)~VISITED) | (s_fl[i] & VISITED));
         s_sc[i] = c.sc;
         s_col[i] = c.col;
+        mirror(x, y, i);
         if (mt_type(ma[c.id]) == T_SOUP) df[y * W + x] = c.df;
     }
     __device__ __forceinline__ void set_nothing(int x, int y) const {
@@ -225,6 +295,7 @@ struct Tile : TileData {
             s_fl[d] = (uint8_t)(s_fl[d] & VISITED);
             s_sc[d] = 0;
             s_col[d] = 0xff0000u;
+            mirror(dx, dy, d);
             return;
         }
         int s = li(sx, sy);
@@ -233,6 +304,7 @@ struct Tile : TileData {
         s_fl[d] = (uint8_t)((s_fl[s] & (uint8_t)~VISITED) | (s_fl[d] & VISITED));
         s_sc[d] = s_sc[s];
         s_col[d] = s_col[s];
+        mirror(dx, dy, d);
         if (mt_type(ma[v]) == T_SOUP) {
             df[dy * W + dx] = df[sy * W + sx];
             if (TEMP && tp) tp[dy * W + dx] = tp[sy * W + sx];
@@ -265,6 +337,7 @@ struct Tile : TileData {
         if (nf != f) {
             s_fl[i] = nf;
             s_id[i] |= DIRTY;
+            mirror_idfl(x, y, i);
         }
     }
     __device__ __forceinline__ void add_diff(int x, int y, int32_t v) const {
@@ -287,12 +360,15 @@ struct Tile : TileData {
         s_fl[i] = (uint8_t)((c.fl & (uint8_t)~VISITED) | (s_fl[i] & VISITED));
         s_sc[i] = c.sc;
         s_col[i] = c.col;
+        mirror(x, y, i);
         df[y * W + x] = __float_as_int(dfv);
     }
     __device__ __forceinline__ bool vis(int x, int y) const { return (s_fl[li(x, y)] & VISITED) != 0; }
     __device__ __forceinline__ void setvis(int x, int y) const {
         if (!inw(x, y)) return;
-        s_fl[li(x, y)] |= VISITED;
+        const int i = li(x, y);
+        s_fl[i] |= VISITED;
+        mirror_idfl(x, y, i);
     }
 };
 
@@ -1174,30 +1250,45 @@ static __device__ __noinline__ void emit_spawns(const WorldDev &w, const SpawnEv
 
 // -------------------------------------------------------------- the kernel
 // shared memory besides the tile planes
-struct SmemHead {
+template <int NT>
+struct SmemHeadT {
     uint32_t ma[MAXMAT];
     float md[MAXMAT];
     long long led[LED_ROWS * 64];
     int scan[40];
     uint8_t mreact[MAXMAT];
-    int cnt[CP_THREADS];  // sweep-A spawns per enumeration index, then their ranks
+    int cnt[NT];  // sweep-A spawns per enumeration index, then their ranks
     uint32_t air[(128 + 2) * 5];  // sweep-B pillar snapshot (chunk edge <= 128)
+    // CTA pair: what the partner wrote here: [0..1] its chunk flags, [2..3] its spawn
+    // count of a sweep-A sub-phase (alternate slots)
+    uint32_t xch[4];
 };
+using SmemHead = SmemHeadT<CP_THREADS>;
 
 // items: (world << 20) | chunk slot within the colour; iter, tk select the pass.
 // SEQ: the reference's own order inside each chunk (bottom row first, left to right,
 // sweep by sweep; world.cpp:1084-1087, 1589, 1823), with the same rules, run as a
 // wavefront of one thread per chunk row (see sweeps_seq)
-template <int HALO, bool TEMP, bool SEQ, bool F32>
-__global__ void __launch_bounds__(CP_THREADS, 1)
+// PAIR: each chunk is split over the two CTAs of a cluster, 512 threads each: rank 0
+// updates the top half of its rows, rank 1 the bottom half, each staging its half
+// plus the rows its rules reach (the shared rows are kept equal by mirrored writes)
+// and writing back its own rows; sub-phases end with a cluster barrier. A chunk's
+// sub-phases then run on two SMs, and an SM holds halves of two chunks whose
+// barriers interleave.
+template <int HALO, bool TEMP, bool SEQ, bool F32, bool PAIR = false>
+__global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 : 1)
     k_colour_pass(const WorldDev *__restrict__ worlds, const uint32_t *__restrict__ items, int n_items, int iter, int tk,
                   const MatTable *__restrict__ mt) {
+    static_assert(!(PAIR && SEQ), "the reference order runs a chunk in one CTA");
+    constexpr int T = PAIR ? CP_THREADS / 2 : CP_THREADS;
+    using Head = SmemHeadT<T>;
     extern __shared__ __align__(16) unsigned char smem[];
-    SmemHead &S = *reinterpret_cast<SmemHead *>(smem);
-    unsigned char *planes = smem + ((sizeof(SmemHead) + 15) & ~(size_t)15);
+    Head &S = *reinterpret_cast<Head *>(smem);
+    unsigned char *planes = smem + ((sizeof(Head) + 15) & ~(size_t)15);
 
     const int tid = threadIdx.x;
-    constexpr int T = CP_THREADS;
+    const int rank = PAIR ? (int)cluster_rank() : 0;
+    int npass = 0;  // chunks taken so far (the same count in both CTAs of a pair)
     for (int i = tid; i < MAXMAT; i += T) {
         S.ma[i] = (i < mt->n) ? mt->a[i] : 0u;
         S.md[i] = (i < mt->n) ? mt->density[i] : 0.f;
@@ -1224,7 +1315,9 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
     const int ox = tk % 2, oy = 1 - tk / 2;
     long long *led_g_last = nullptr;
 
-    for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const int wstart = PAIR ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
+    const int wstride = PAIR ? (int)(gridDim.x >> 1) : (int)gridDim.x;
+    for (int it = wstart; it < n_items; it += wstride) {
         const uint32_t item = __ldg(&items[it]);
         if (tid == 0) s_w = worlds[item >> 20];
         __syncthreads();
@@ -1250,12 +1343,16 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
         const int cx = w.zx + (ox + 2 * (slot / nb)) * C, cy = w.zy + (oy + 2 * (slot % nb)) * C;
         const uint32_t cp = (uint32_t)((iter * 4 + tk) * w.max_slots + slot);
 
+        // the chunk rows this CTA updates, [o0, o1)
+        const int half = C / 2;
+        const int o0 = PAIR ? rank * half : 0, o1 = PAIR ? (rank ? C : half) : C;
+        const int own = o1 - o0;
         TileData Tl;
         Tl.RW = C + 2 * HALO;
-        Tl.RHF = C + 2 * HALO;
-        Tl.RHI = C + HALO + 10;
+        Tl.RHF = own + 2 * HALO;
+        Tl.RHI = own + HALO + 10;
         Tl.x0 = cx - HALO;
-        Tl.y0 = cy - HALO;
+        Tl.y0 = cy + o0 - HALO;
         Tl.W = W;
         Tl.H = H;
         Tl.ma = S.ma;
@@ -1266,13 +1363,22 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
         Tl.id_air = id_air;
         Tl.s_air = S.air;
         Tl.ax0 = cx - 1;
-        Tl.ay0 = cy + 1;
+        Tl.ay0 = cy + o0 + 1;
         Tl.aw = C + 2;
         const int nid = Tl.RW * Tl.RHI, nfull = Tl.RW * Tl.RHF;
         Tl.s_sc = (int32_t *)planes;
         Tl.s_col = (uint32_t *)(Tl.s_sc + nfull);
         Tl.s_id = (uint16_t *)(Tl.s_col + nfull);
         Tl.s_fl = (uint8_t *)(Tl.s_id + ((nid + 1) & ~1));
+        if constexpr (PAIR) {
+            // the partner's planes lie at the same offsets of its shared memory
+            const uint32_t pr = (uint32_t)(rank ^ 1);
+            Tl.p_id = mapa_rank(smem_addr(Tl.s_id), pr);
+            Tl.p_fl = mapa_rank(smem_addr(Tl.s_fl), pr);
+            Tl.p_sc = mapa_rank(smem_addr(Tl.s_sc), pr);
+            Tl.p_col = mapa_rank(smem_addr(Tl.s_col), pr);
+            Tl.py0 = cy + (rank ? 0 : half) - HALO;
+        }
 
         // ---- stage the tile, one warp per row. The 4-byte planes go straight to
         // shared memory with cp.async; ids and flags are loaded a row at a time, all
@@ -1321,7 +1427,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                     const int i = r * Tl.RW + lx;
                     Tl.s_id[i] = v[k];
                     if (full) Tl.s_fl[i] = f[k];
-                    if (gx >= cx && gx < cx + C && gy >= cy && gy < cy + C && rin && gx < W) {
+                    if (gx >= cx && gx < cx + C && gy >= cy + o0 && gy < cy + o1 && rin && gx < W) {
                         if (mt_iter(S.ma[v[k]]) > iter) active = 1;
                         if ((int)v[k] == c.id_fire) fire = 1;
                     }
@@ -1331,13 +1437,25 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
         active = __syncthreads_or(active);
         fire = __syncthreads_or(fire);
         cp_async_wait_all();
-        __syncthreads();
+        if constexpr (PAIR) {
+            // the pair decides together whether the chunk runs and with which lattice
+            const int slot_x = npass & 1;
+            if (tid == 0) st_cluster_u32(mapa_rank(smem_addr(&S.xch[slot_x]), (uint32_t)(rank ^ 1)),
+                                         (uint32_t)(active | (fire << 1)));
+            cluster_sync();
+            const uint32_t o = S.xch[slot_x];
+            active |= (int)(o & 1u);
+            fire |= (int)((o >> 1) & 1u);
+        } else {
+            __syncthreads();
+        }
+        npass++;
         FSE_PT(1)
         if (!active) {
             // every chunk cell has iterations <= iter: the pass only marks cells visited
             if constexpr (SEQ) {
                 if (tid < w.cp_rows) w.cp_count[cp * w.cp_rows + tid] = 0;
-            } else if (tid == 0) {
+            } else if (tid == 0 && rank == 0) {
                 w.cp_count[cp] = 0;
             }
             __syncthreads();
@@ -1348,6 +1466,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
         const int mode = c.has_inter ? 2 : (fire ? 1 : 0);
         const int cw = min(C, W - cx), chh = min(C, H - cy);
         int running = 0;  // spawns emitted so far by this chunk-pass
+        int nsub = 0;     // sweep-A sub-phases so far (CTA pair: alternate exchange slots)
         c.led_g = w.ledger;
         // the world bounds policy matters only where the tile crosses the world edge
         const bool edge = Tl.x0 < 0 || Tl.y0 < 0 || Tl.x0 + Tl.RW > W || Tl.y0 + Tl.RHI > H;
@@ -1401,8 +1520,8 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                     uint32_t bits = 0;
                     for (int b = 0; b < 32; b++) {
                         const int sy = wi * 32 + b;
-                        if (sy < C + 9) {
-                            const int gx = cx - 1 + sx, gy = cy + 1 + sy;
+                        if (sy < own + 9) {
+                            const int gx = cx - 1 + sx, gy = Tl.ay0 + sy;
                             if (Tl.inw(gx, gy) && Tl.type(gx, gy) == T_AIR) bits |= 1u << b;
                         }
                     }
@@ -1413,7 +1532,9 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
             int px, py;
             lattice(sweep, mode, px, py);
             for (int ry = py - 1; ry >= 0; ry--) {
-                const int ny = (C - ry + py - 1) / py;
+                // this CTA's rows of the sub-phase: dyb, dyb + py, ... below o1
+                const int dyb = ry + (o0 > ry ? (o0 - ry + py - 1) / py * py : 0);
+                const int ny = dyb < o1 ? (o1 - dyb + py - 1) / py : 0;
                 for (int rx = 0; rx < px; rx++) {
                     const int nx = (C - rx + px - 1) / px;
                     const int total = nx * ny;
@@ -1427,7 +1548,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                         if (e < total) {
                             int q, r;
                             divmod_small(e, nx, rnx, q, r);
-                            const int dy = ry + q * py, dx = rx + r * px;
+                            const int dy = dyb + q * py, dx = rx + r * px;
                             if (dx < cw && dy < chh) rule_a(Tl, c, cx + dx, cy + dy);
                         }
                         FSE_PT(3)
@@ -1435,7 +1556,26 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                         // scratch are next written after the next sub-phase's barrier, so no
                         // barrier is needed after this block.
                         if (c.ev.n > 0) S.cnt[e] = c.ev.n;
-                        if (__syncthreads_or(c.ev.n > 0)) {
+                        if constexpr (PAIR) {
+                            // the sub-phase's enumeration runs through rank 0's rows first:
+                            // each CTA ranks its own spawns, the partner's count of the
+                            // sub-phase comes through the cluster barrier that ends it
+                            int tot = 0, ex = 0;
+                            if (__syncthreads_or(c.ev.n > 0)) ex = block_excl_scan(S.cnt[tid], S.scan, &tot);
+                            const int slot_t = 2 + (nsub & 1);
+                            if (tid == 0)
+                                st_cluster_u32(mapa_rank(smem_addr(&S.xch[slot_t]), (uint32_t)(rank ^ 1)),
+                                               (uint32_t)tot);
+                            cluster_sync();
+                            const int tot_p = (int)S.xch[slot_t];
+                            nsub++;
+                            if (c.ev.n > 0) {
+                                const int base = atomicAdd(w.stage_count, c.ev.n);
+                                emit_spawns<TEMP, F32>(w, c.ev, cp, (uint32_t)(running + (rank ? tot_p : 0) + ex),
+                                                       base);
+                            }
+                            running += tot + tot_p;
+                        } else if (__syncthreads_or(c.ev.n > 0)) {
                             int tot;
                             const int ex = block_excl_scan(S.cnt[tid], S.scan, &tot);
                             if (c.ev.n > 0) {
@@ -1459,8 +1599,8 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                             // diffs requested together before either is processed
                             const int q1 = q + dq + (r + dr >= nx ? 1 : 0);
                             const int r1 = r + dr - (r + dr >= nx ? nx : 0);
-                            const int dy0 = ry + q * py, dx0 = rx + r * px;
-                            const int dy1 = ry + q1 * py, dx1 = rx + r1 * px;
+                            const int dy0 = dyb + q * py, dx0 = rx + r * px;
+                            const int dy1 = dyb + q1 * py, dx1 = rx + r1 * px;
                             const bool v0 = tid < total && dx0 < cw && dy0 < chh;
                             const bool v1 = tid + T < total && dx1 < cw && dy1 < chh;
                             const int32_t df0 = v0 ? w.df[(size_t)(cy + dy0) * W + cx + dx0] : 0;
@@ -1469,7 +1609,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                             if (v1) rule_b(Tl, c, cx + dx1, cy + dy1, df1);
                         } else {
                             for (int e = tid; e < total; e += T) {
-                                const int dy = ry + q * py, dx = rx + r * px;
+                                const int dy = dyb + q * py, dx = rx + r * px;
                                 if (dx < cw && dy < chh) rule_c(Tl, c, cx + dx, cy + dy);
                                 q += dq;
                                 r += dr;
@@ -1480,7 +1620,10 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                             }
                         }
                         FSE_PT(3 + 2 * sweep)
-                        __syncthreads();
+                        if constexpr (PAIR)
+                            cluster_sync();
+                        else
+                            __syncthreads();
                         FSE_PT(4 + 2 * sweep)
                     }
                 }
@@ -1494,9 +1637,9 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                 sweeps_seq(Tile<false, TEMP, true, F32>(Tl));
         } else {
             if (edge)
-                sweeps(Tile<true, TEMP, false, F32>(Tl));
+                sweeps(Tile<true, TEMP, false, F32, PAIR>(Tl));
             else
-                sweeps(Tile<false, TEMP, false, F32>(Tl));
+                sweeps(Tile<false, TEMP, false, F32, PAIR>(Tl));
         }
 
         // ---- write back the cells this CTA changed (full-state rows inside the world),
@@ -1506,6 +1649,9 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
             for (int r = wid; r < Tl.RHF; r += T / 32) {
                 const int gy = Tl.y0 + r;
                 if ((unsigned)gy >= (unsigned)H) continue;
+                // a CTA pair: rank 0 writes rows above the chunk's middle, rank 1 the
+                // others (each row is written by the CTA that owns it)
+                if (PAIR && (rank == 0 ? gy >= cy + half : gy < cy + half)) continue;
                 const size_t gb = (size_t)gy * W;
 #pragma unroll
                 for (int k = 0; k < MAXRW / 32; k++) {
@@ -1522,7 +1668,7 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
                 }
             }
         }
-        if (!SEQ && tid == 0) w.cp_count[cp] = running;
+        if (!SEQ && tid == 0 && rank == 0) w.cp_count[cp] = running;
         __syncthreads();
         FSE_PT(9)
     }
@@ -1533,10 +1679,12 @@ __global__ void __launch_bounds__(CP_THREADS, 1)
             if (v) atomicAdd((unsigned long long *)&led_g_last[(i / 64) * MAXMAT + (i % 64)], (unsigned long long)v);
         }
     }
+    // a CTA of a pair leaves only when its partner no longer writes to it
+    if constexpr (PAIR) cluster_sync();
     FSE_PT_FLUSH
 }
 
-#if !defined(FSE_TICK_TEMP_TU) && !defined(FSE_TICK_SEQ_TU) && !defined(FSE_TICK_F32_TU)
+#if !defined(FSE_TICK_TEMP_TU) && !defined(FSE_TICK_SEQ_TU) && !defined(FSE_TICK_F32_TU) && !defined(FSE_TICK_PAIR_TU)
 size_t colour_pass_smem(int C, int halo) {
     size_t RW = (size_t)C + 2 * halo, RHF = (size_t)C + 2 * halo, RHI = (size_t)C + halo + 10;
     size_t nid = RW * RHI, nfull = RW * RHF;
@@ -1560,9 +1708,62 @@ static cudaError_t launch_t(const WorldDev *worlds, const uint32_t *items, int n
     return cudaGetLastError();
 }
 
+// shared memory of one CTA of a pair: half the chunk's rows plus the reach of its rules
+static size_t colour_pass_smem_pair(int C, int halo) {
+    const size_t own = (size_t)C / 2;
+    size_t RW = (size_t)C + 2 * halo, RHF = own + 2 * halo, RHI = own + halo + 10;
+    size_t nid = RW * RHI, nfull = RW * RHF;
+    size_t head = (sizeof(SmemHeadT<CP_THREADS / 2>) + 15) & ~(size_t)15;
+    return head + nfull * 4 + nfull * 4 + ((nid + 1) & ~(size_t)1) * 2 + nfull;
+}
+
+// the chunks split over CTA pairs (thread-block clusters of two): `clusters` pairs
+template <int HALO, bool TEMP, bool F32>
+static cudaError_t launch_pair_t(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
+                                 const MatTable *mt, size_t sm, int clusters, cudaStream_t s) {
+    static size_t set = 0;
+    if (set < sm) {
+        cudaFuncSetAttribute(k_colour_pass<HALO, TEMP, false, F32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sm);
+        set = sm;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2 * clusters);
+    cfg.blockDim = dim3(CP_THREADS / 2);
+    cfg.dynamicSmemBytes = sm;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_colour_pass<HALO, TEMP, false, F32, true>, worlds, items, n_items, iter, tk, mt);
+}
+
 // Each translation unit that includes this file with one of the defines below
 // compiles one family of instantiations, so that they build in parallel.
-#if defined(FSE_TICK_F32_TU)
+#if defined(FSE_TICK_PAIR_TU)
+// chunks split over CTA pairs, Q16.16 amounts (FSE_TICK_PAIR_TU = 1) or f32 (2)
+#define FSE_PAIR_F32 (FSE_TICK_PAIR_TU == 2)
+#if FSE_TICK_PAIR_TU == 2
+cudaError_t launch_colour_pass_pair_f32(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
+                                        const MatTable *mt, int halo, int C, int clusters, cudaStream_t s, bool temp) {
+#else
+cudaError_t launch_colour_pass_pair(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
+                                    const MatTable *mt, int halo, int C, int clusters, cudaStream_t s, bool temp) {
+#endif
+    const size_t sm = colour_pass_smem_pair(C, halo);
+    if (temp) {
+        if (halo == 5)
+            return launch_pair_t<5, true, FSE_PAIR_F32>(worlds, items, n_items, iter, tk, mt, sm, clusters, s);
+        return launch_pair_t<2, true, FSE_PAIR_F32>(worlds, items, n_items, iter, tk, mt, sm, clusters, s);
+    }
+    if (halo == 5) return launch_pair_t<5, false, FSE_PAIR_F32>(worlds, items, n_items, iter, tk, mt, sm, clusters, s);
+    return launch_pair_t<2, false, FSE_PAIR_F32>(worlds, items, n_items, iter, tk, mt, sm, clusters, s);
+}
+#elif defined(FSE_TICK_F32_TU)
 // f32 liquid amounts (FSE_CFG_F32_FLUID), in the partitioned order (FSE_TICK_F32_TU
 // = 1) or in the reference's order (2)
 #define FSE_F32_SEQ (FSE_TICK_F32_TU == 2)
@@ -1606,13 +1807,24 @@ cudaError_t launch_colour_pass_f32(const WorldDev *worlds, const uint32_t *items
 cudaError_t launch_colour_pass_f32_seq(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
                                        const MatTable *mt, int halo, size_t sm, int grid, cudaStream_t s, bool temp);
 
+cudaError_t launch_colour_pass_pair(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
+                                    const MatTable *mt, int halo, int C, int clusters, cudaStream_t s, bool temp);
+cudaError_t launch_colour_pass_pair_f32(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
+                                        const MatTable *mt, int halo, int C, int clusters, cudaStream_t s, bool temp);
+
+// threads: CP_THREADS (one CTA per chunk) or CP_THREADS / 2 (each chunk split over a
+// CTA pair; the partitioned order and an even chunk edge only); grid: chunk workers
+// (CTAs, or pairs), 0 = one per chunk
 cudaError_t launch_colour_pass(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
                                const MatTable *mt, int halo, int C, int threads, int grid, cudaStream_t s,
                                bool temp, bool seq, bool f32) {
-    (void)threads;  // the colour pass always runs CP_THREADS threads (see above)
     size_t sm = colour_pass_smem(C, halo);
     if (n_items <= 0) return cudaSuccess;
     if (grid <= 0 || grid > n_items) grid = n_items;
+    if (threads == CP_THREADS / 2 && !seq && C % 2 == 0) {
+        if (f32) return launch_colour_pass_pair_f32(worlds, items, n_items, iter, tk, mt, halo, C, grid, s, temp);
+        return launch_colour_pass_pair(worlds, items, n_items, iter, tk, mt, halo, C, grid, s, temp);
+    }
     if (f32 && seq) return launch_colour_pass_f32_seq(worlds, items, n_items, iter, tk, mt, halo, sm, grid, s, temp);
     if (f32) return launch_colour_pass_f32(worlds, items, n_items, iter, tk, mt, halo, sm, grid, s, temp);
     if (seq) return launch_colour_pass_seq(worlds, items, n_items, iter, tk, mt, halo, sm, grid, s, temp);
@@ -1624,7 +1836,8 @@ cudaError_t launch_colour_pass(const WorldDev *worlds, const uint32_t *items, in
 
 }  // namespace fse
 
-#if defined(FSE_PHASE_CLOCKS) && !defined(FSE_TICK_TEMP_TU) && !defined(FSE_TICK_SEQ_TU) && !defined(FSE_TICK_F32_TU)
+#if defined(FSE_PHASE_CLOCKS) && !defined(FSE_TICK_TEMP_TU) && !defined(FSE_TICK_SEQ_TU) && !defined(FSE_TICK_F32_TU) && \
+    !defined(FSE_TICK_PAIR_TU)
 extern "C" int fse_debug_phase_clocks(unsigned long long out[16], int reset) {
     cudaDeviceSynchronize();
     cudaMemcpyFromSymbol(out, g_phase_clk, 16 * sizeof(unsigned long long));

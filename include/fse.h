@@ -203,6 +203,11 @@ int fse_world_set_tick(fse_world *world, uint32_t tick);
  * changes only its cells (world.cpp:1952-2001). The whole world by default. Batches
  * and servers use the zone their worlds had when they were made. */
 int fse_world_set_tick_zone(fse_world *world, int x, int y, int width, int height);
+/* The launch shape of the world's colour pass (results never depend on it):
+ * 0 one 1024-thread CTA per chunk, 1 one persistent CTA per SM walking the chunks,
+ * 2 each chunk split over a pair of 512-thread CTAs (a thread-block cluster; the
+ * partitioned order only), 3 persistent pairs. */
+int fse_world_set_launch(fse_world *world, int colour_shape);
 int fse_world_get_tile(fse_world *world, int x, int y, uint16_t *id, uint32_t *colour, int32_t *scalar,
                        uint8_t *flags);
 int fse_world_set_tile(fse_world *world, int x, int y, uint16_t id, uint32_t colour, int32_t scalar, uint8_t flags);
@@ -323,6 +328,9 @@ int fse_object_list_export(fse_world *world, uint32_t *host_idx, int64_t cap, in
  * enable = 1 starts (and zeroes) the timer, 0 stops it; both first report the
  * accumulated kernel milliseconds and launch count since the last start. */
 int fse_world_pass_timing(fse_world *world, int enable, double *out_ms, int64_t *out_launches);
+/* iterations the last particle update of this world needed to reach the list-order
+ * result (for a batch: recorded on its first world); diagnostics */
+int fse_world_particle_iterations(fse_world *world, int *out);
 /* kernels this library has launched so far (all worlds, batches and servers) */
 int64_t fse_launch_counter(void);
 
@@ -420,8 +428,9 @@ int fse_batch_prepare_graphs(fse_batch *batch, int n_ticks, int graph_ticks);
  * every world; results never change. out_choice: colour_ctas_per_sm,
  * particle_blocks, microseconds of two timed steps, candidate index */
 int fse_batch_autotune(fse_batch *batch, int32_t out_choice[4]);
-/* colour_ctas_per_sm: 0 = one CTA per chunk, 1 = one persistent CTA per SM walking
- * the chunk list; particle_blocks: blocks per world of the particle kernels
+/* colour_ctas_per_sm: the colour pass's launch shape as in fse_world_set_launch
+ * (0 one CTA per chunk, 1 one persistent CTA per SM, 2 a CTA pair per chunk,
+ * 3 persistent pairs); particle_blocks: blocks per world of the particle kernels
  * (0 = enough for the largest particle list) */
 int fse_batch_set_launch(fse_batch *batch, int colour_ctas_per_sm, int particle_blocks);
 int fse_batch_sync(fse_batch *batch);
