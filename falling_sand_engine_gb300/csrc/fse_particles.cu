@@ -451,14 +451,12 @@ __global__ void __launch_bounds__(256) k_part_serial(const WorldDev *__restrict_
                 const int32_t b1 = w.p_box1[i];
                 const int x0 = (b0 & 0xFFFF) >> 3, y0 = ((uint32_t)b0 >> 16) >> 3;
                 const int x1 = (b1 & 0xFFFF) >> 3, y1 = ((uint32_t)b1 >> 16) >> 3;
-                bool touched = false;
-                for (int by = y0; by <= y1 && !touched; by++)
-                    for (int bxx = x0; bxx <= x1; bxx++)
-                        if (__ldcg(&seen[by * w.amw + bxx]) < (uint32_t)i) {
-                            touched = true;
-                            break;
-                        }
-                if (!touched) continue;
+                // the lowest changing index over the box's blocks (the loads do not wait
+                // on each other)
+                uint32_t lo = 0xFFFFFFFFu;
+                for (int by = y0; by <= y1; by++)
+                    for (int bxx = x0; bxx <= x1; bxx++) lo = min(lo, __ldcg(&seen[by * w.amw + bxx]));
+                if (lo >= (uint32_t)i) continue;
                 before = fill_of(w, i);
             }
             part_outcome(w, s_type, i);

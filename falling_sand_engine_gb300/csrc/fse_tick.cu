@@ -1725,6 +1725,9 @@ static cudaError_t launch_pair_t(const WorldDev *worlds, const uint32_t *items, 
     if (set < sm) {
         cudaFuncSetAttribute(k_colour_pass<HALO, TEMP, false, F32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)sm);
+        // all of the unified L1/shared storage as shared memory, so that two CTAs fit an SM
+        cudaFuncSetAttribute(k_colour_pass<HALO, TEMP, false, F32, true>,
+                             cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         set = sm;
     }
     cudaLaunchConfig_t cfg = {};

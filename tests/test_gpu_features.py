@@ -185,7 +185,7 @@ def test_batch_equals_individual_worlds(fse):
 def test_autotune_never_changes_results(fse):
     ref = fse.World(384, 384, seed=44)
     ref.generate(fse.GEN_MIX, 44)
-    ref.step(6)
+    ref.step(9)
     w = fse.World(384, 384, seed=44)
     w.generate(fse.GEN_MIX, 44)
     b = fse.Batch([w])
