@@ -208,16 +208,19 @@ struct Box {
     }
 };
 
-// One particle of world.cpp:2032-2188 against the view of particle i; writes its
-// outcome (state into w.q, kind into p_state, target cell into p_cell, the box of
-// the cells read into p_box0 / p_box1).
-__device__ void part_outcome(const WorldDev &w, const uint8_t *s_type, int i) {
+// One particle's flight of world.cpp:2032-2188 against the view of particle i: writes
+// its state into w.q, its kind into p_state, its target cell into p_cell and the box
+// of the cells it read into p_box0 / p_box1. A particle that must search the spiral
+// (world.cpp:2093-2147) returns true with its kind and cell not yet written; the
+// caller's warp walks the spiral with it (warp_spiral) and finishes it.
+__device__ bool part_flight(const WorldDev &w, const uint8_t *s_type, int i) {
     uint8_t bits = w.p.bits[i];
     int32_t life = w.p.life[i];
     float x = w.p.x[i], y = w.p.y[i], vx = w.p.vx[i], vy = w.p.vy[i];
     const int W = w.W, H = w.H;
     uint8_t kind = PS_ALIVE;
     int cell = -1;
+    bool spiral = false;
     Box bx = {W, H, -1, -1};
     if ((bits & 2) && life <= 0) {  // :2033-2037
         kind = PS_DESTROY;
@@ -277,59 +280,7 @@ __device__ void part_outcome(const WorldDev &w, const uint8_t *s_type, int i) {
                 kind = PS_FILL;
                 cell = ly * W + lx;
             } else if (hit == 2) {
-                // :2093-2147, the 32x32 spiral from the collision point: the first cell
-                // that is AIR or holds the same liquid. A window (the 33x33 cells the walk
-                // reaches) whose 8x8 blocks held no AIR when the update began holds none
-                // now (deposits only take AIR), so unless the particle is a liquid that
-                // may merge the walk can only fail and is skipped.
-                const int pid = w.p.id[i];
-                const bool psoup = s_type[pid] == T_SOUP;
-                bool walk = true;
-                if (!psoup && x > -32.0f && x < (float)W + 32.0f && y > -32.0f && y < (float)H + 32.0f) {
-                    const int ix = (int)floorf(x), iy = (int)floorf(y);
-                    const int bx0 = max(0, (ix - 17) >> 3), bx1 = min(w.amw - 1, (ix + 17) >> 3);
-                    const int by0 = max(0, (iy - 17) >> 3), by1 = min(w.amh - 1, (iy + 17) >> 3);
-                    bool any = false;
-                    for (int by = by0; by <= by1 && !any; by++)
-                        for (int bxx = bx0; bxx <= bx1; bxx++)
-                            if (w.airmap[by * w.amw + bxx]) {
-                                any = true;
-                                break;
-                            }
-                    walk = any;
-                }
-                int found = -1, j = 0;
-                if (walk) {
-                    for (; j < c_spiral_n; j++) {
-                        const int cx = (int)__fadd_rn(x, (float)c_spiral[j][0]);
-                        const int cy = (int)__fadd_rn(y, (float)c_spiral[j][1]);
-                        if (cx < 0 || cy < 0 || cx >= W || cy >= H) continue;
-                        const int c = cy * W + cx;
-                        const int cid = view_id(w, s_type, c, i);
-                        if (s_type[cid] == T_AIR) {
-                            found = c;
-                            kind = PS_FILL;
-                            break;
-                        }
-                        if (psoup && cid == pid) {
-                            found = c;
-                            kind = PS_MERGE;
-                            break;
-                        }
-                    }
-                    // the cells looked at lie in the square of the last one's ring
-                    const int jr = j < c_spiral_n ? j : c_spiral_n - 1;
-                    const int r = max(abs((int)c_spiral[jr][0]), abs((int)c_spiral[jr][1])) + 1;
-                    bx.add((int)floorf(x) - r, (int)floorf(y) - r);
-                    bx.add((int)floorf(x) + r, (int)floorf(y) + r);
-                }
-                if (found >= 0) {
-                    cell = found;
-                } else {  // :2141-2144
-                    kind = PS_FAIL;
-                    vy = -4.0f;
-                    y = __fsub_rn(y, 16.0f);
-                }
+                spiral = true;
             }
         }
     }
@@ -339,12 +290,68 @@ __device__ void part_outcome(const WorldDev &w, const uint8_t *s_type, int i) {
     w.q.vy[i] = vy;
     w.q.bits[i] = bits;
     w.q.life[i] = life;
-    w.p_state[i] = kind;
-    w.p_cell[i] = cell;
+    if (!spiral) {
+        w.p_state[i] = kind;
+        w.p_cell[i] = cell;
+    }
     const int x0 = min(max(bx.x0, 0), W - 1), y0 = min(max(bx.y0, 0), H - 1);
     const int x1 = min(max(bx.x1, 0), W - 1), y1 = min(max(bx.y1, 0), H - 1);
     w.p_box0[i] = bx.x1 < 0 ? -1 : (int32_t)((uint32_t)x0 | ((uint32_t)y0 << 16));
     w.p_box1[i] = (int32_t)((uint32_t)x1 | ((uint32_t)y1 << 16));
+    return spiral;
+}
+
+// :2093-2147, the 32x32 spiral from the collision point (x, y) of particle i of world
+// w, walked by the whole warp, 32 cells a step: the first cell that is AIR or holds
+// the same liquid, in the particle's view. A window (the 33x33 cells the walk reaches)
+// whose 8x8 blocks held no AIR when the update began holds none now (deposits only
+// take AIR), so unless the particle is a liquid that may merge the walk can only fail
+// and is skipped. Every lane returns the result: kind PS_FILL / PS_MERGE with *cell,
+// or PS_FAIL; *ring = the ring of the last cell looked at (-1: no walk).
+__device__ uint8_t warp_spiral(const WorldDev &w, const uint8_t *s_type, int i, float x, float y, int *cell,
+                               int *ring) {
+    const int lane = threadIdx.x & 31;
+    const int W = w.W, H = w.H;
+    const int pid = w.p.id[i];
+    const bool psoup = s_type[pid] == T_SOUP;
+    bool walk = true;
+    if (!psoup && x > -32.0f && x < (float)W + 32.0f && y > -32.0f && y < (float)H + 32.0f) {
+        const int ix = (int)floorf(x), iy = (int)floorf(y);
+        const int bx0 = max(0, (ix - 17) >> 3), bx1 = min(w.amw - 1, (ix + 17) >> 3);
+        const int by0 = max(0, (iy - 17) >> 3), by1 = min(w.amh - 1, (iy + 17) >> 3);
+        const int nbx = bx1 - bx0 + 1, nblk = nbx * (by1 - by0 + 1);
+        bool any = false;
+        for (int k = lane; k < nblk; k += 32) any |= w.airmap[(by0 + k / nbx) * w.amw + bx0 + k % nbx] != 0;
+        walk = __any_sync(0xffffffffu, any);
+    }
+    *ring = -1;
+    *cell = -1;
+    if (!walk) return PS_FAIL;
+    const int n = c_spiral_n;
+    for (int base = 0; base < n; base += 32) {
+        const int j = base + lane;
+        int hit = 0, c = -1;
+        if (j < n) {
+            const int cx = (int)__fadd_rn(x, (float)c_spiral[j][0]);
+            const int cy = (int)__fadd_rn(y, (float)c_spiral[j][1]);
+            if (cx >= 0 && cy >= 0 && cx < W && cy < H) {
+                c = cy * W + cx;
+                const int cid = view_id(w, s_type, c, i);
+                hit = s_type[cid] == T_AIR ? 1 : ((psoup && cid == pid) ? 2 : 0);
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, hit != 0);
+        if (m) {
+            const int src = __ffs(m) - 1;
+            *cell = __shfl_sync(0xffffffffu, c, src);
+            const int h = __shfl_sync(0xffffffffu, hit, src);
+            const int jl = base + src;
+            *ring = max(abs((int)c_spiral[jl][0]), abs((int)c_spiral[jl][1]));
+            return h == 1 ? PS_FILL : PS_MERGE;
+        }
+    }
+    *ring = max(abs((int)c_spiral[n - 1][0]), abs((int)c_spiral[n - 1][1]));
+    return PS_FAIL;
 }
 
 // the fill a particle's outcome makes (-1: none)
@@ -427,6 +434,7 @@ __global__ void __launch_bounds__(256) k_part_serial(const WorldDev *__restrict_
     int32_t *err = worlds[0].err;
     int32_t *cnt = worlds[0].req_count;
     const int gtid = (int)(blockIdx.x * blockDim.x + threadIdx.x), gstride = (int)(gridDim.x * blockDim.x);
+    const int lane = threadIdx.x & 31;
     int it = 0;
     for (;; it++) {
         if (it >= SERIAL_MAX_ITER) {
@@ -436,38 +444,90 @@ __global__ void __launch_bounds__(256) k_part_serial(const WorldDev *__restrict_
         const int par = it & 1;
         // A: outcomes of the particles whose box saw a fill change by a lower index (all
         // at first); changed fills are counted and their blocks marked for the next
-        // iteration with the changing index
-        for (int g = gtid; g < total; g += gstride) {
-            const int wi = world_of(s_pref, n_worlds, g);
-            const WorldDev &w = worlds[wi];
-            const int i = g - s_pref[wi];
-            const int nblk = w.amw * w.amh;
-            const uint32_t *seen = w.chg + (size_t)par * nblk;
-            uint32_t *mark = w.chg + (size_t)(1 - par) * nblk;
-            int before = -1;
-            if (it > 0) {
-                const int32_t b0 = w.p_box0[i];
-                if (b0 < 0) continue;  // read no cell: nothing can change it
-                const int32_t b1 = w.p_box1[i];
-                const int x0 = (b0 & 0xFFFF) >> 3, y0 = ((uint32_t)b0 >> 16) >> 3;
-                const int x1 = (b1 & 0xFFFF) >> 3, y1 = ((uint32_t)b1 >> 16) >> 3;
-                // the lowest changing index over the box's blocks (the loads do not wait
-                // on each other)
-                uint32_t lo = 0xFFFFFFFFu;
-                for (int by = y0; by <= y1; by++)
-                    for (int bxx = x0; bxx <= x1; bxx++) lo = min(lo, __ldcg(&seen[by * w.amw + bxx]));
-                if (lo >= (uint32_t)i) continue;
-                before = fill_of(w, i);
+        // iteration with the changing index. A thread takes particle g, its warp walks
+        // the spirals of the warp's particles together.
+        for (int gb0 = gtid - lane; gb0 < total; gb0 += gstride) {
+            const int g = gb0 + lane;
+            bool work = g < total, spiral = false;
+            int wi = 0, i = 0, before = -1;
+            if (work) {
+                wi = world_of(s_pref, n_worlds, g);
+                i = g - s_pref[wi];
+                const WorldDev &w = worlds[wi];
+                if (it > 0) {
+                    const int32_t b0 = w.p_box0[i];
+                    if (b0 < 0) {
+                        work = false;  // read no cell: nothing can change it
+                    } else {
+                        const int nblk = w.amw * w.amh;
+                        const uint32_t *seen = w.chg + (size_t)par * nblk;
+                        const int32_t b1 = w.p_box1[i];
+                        const int x0 = (b0 & 0xFFFF) >> 3, y0 = ((uint32_t)b0 >> 16) >> 3;
+                        const int x1 = (b1 & 0xFFFF) >> 3, y1 = ((uint32_t)b1 >> 16) >> 3;
+                        // the lowest changing index over the box's blocks (the loads do not
+                        // wait on each other)
+                        uint32_t lo = 0xFFFFFFFFu;
+                        for (int by = y0; by <= y1; by++)
+                            for (int bxx = x0; bxx <= x1; bxx++) lo = min(lo, __ldcg(&seen[by * w.amw + bxx]));
+                        if (lo >= (uint32_t)i)
+                            work = false;
+                        else
+                            before = fill_of(w, i);
+                    }
+                }
+                if (work) spiral = part_flight(w, s_type, i);
             }
-            part_outcome(w, s_type, i);
-            const int after = fill_of(w, i);
-            if (after != before) {
-                atomicAdd(&cnt[par], 1);
-                if (before >= 0) atomicMin(&mark[(before / w.W >> 3) * w.amw + ((before % w.W) >> 3)], (uint32_t)i);
-                if (after >= 0) atomicMin(&mark[(after / w.W >> 3) * w.amw + ((after % w.W) >> 3)], (uint32_t)i);
-                w.p_prev[i] = before;  // the cell whose record B1 clears
-            } else {
-                w.p_prev[i] = -1;
+            // the spirals of this warp's particles, one after another, 32 cells a step
+            unsigned pend = __ballot_sync(0xffffffffu, spiral);
+            while (pend) {
+                const int src = __ffs(pend) - 1;
+                pend &= pend - 1;
+                const int swi = __shfl_sync(0xffffffffu, wi, src), si = __shfl_sync(0xffffffffu, i, src);
+                const WorldDev &sw = worlds[swi];
+                float sx = 0.f, sy = 0.f;
+                if (lane == src) {
+                    sx = sw.q.x[si];
+                    sy = sw.q.y[si];
+                }
+                sx = __shfl_sync(0xffffffffu, sx, src);
+                sy = __shfl_sync(0xffffffffu, sy, src);
+                int cell, ring;
+                const uint8_t k = warp_spiral(sw, s_type, si, sx, sy, &cell, &ring);
+                if (lane == src) {
+                    sw.p_state[si] = k;
+                    sw.p_cell[si] = cell;
+                    if (k == PS_FAIL) {  // :2141-2144
+                        sw.q.vy[si] = -4.0f;
+                        sw.q.y[si] = __fsub_rn(sy, 16.0f);
+                    }
+                    if (ring >= 0) {
+                        // the cells looked at lie in the square of the last one's ring
+                        const int r = ring + 1;
+                        const int32_t b0 = sw.p_box0[si], b1 = sw.p_box1[si];
+                        const int ix = (int)floorf(sx), iy = (int)floorf(sy);
+                        const int x0 = min(max(min((int)(b0 & 0xFFFF), ix - r), 0), sw.W - 1);
+                        const int y0 = min(max(min((int)((uint32_t)b0 >> 16), iy - r), 0), sw.H - 1);
+                        const int x1 = min(max(max((int)(b1 & 0xFFFF), ix + r), 0), sw.W - 1);
+                        const int y1 = min(max(max((int)((uint32_t)b1 >> 16), iy + r), 0), sw.H - 1);
+                        sw.p_box0[si] = (int32_t)((uint32_t)x0 | ((uint32_t)y0 << 16));
+                        sw.p_box1[si] = (int32_t)((uint32_t)x1 | ((uint32_t)y1 << 16));
+                    }
+                }
+            }
+            if (work) {
+                const WorldDev &w = worlds[wi];
+                const int nblk = w.amw * w.amh;
+                uint32_t *mark = w.chg + (size_t)(1 - par) * nblk;
+                const int after = fill_of(w, i);
+                if (after != before) {
+                    atomicAdd(&cnt[par], 1);
+                    if (before >= 0)
+                        atomicMin(&mark[(before / w.W >> 3) * w.amw + ((before % w.W) >> 3)], (uint32_t)i);
+                    if (after >= 0) atomicMin(&mark[(after / w.W >> 3) * w.amw + ((after % w.W) >> 3)], (uint32_t)i);
+                    w.p_prev[i] = before;  // the cell whose record B1 clears
+                } else {
+                    w.p_prev[i] = -1;
+                }
             }
         }
         grid_sync(gb, nb, err);
