@@ -783,6 +783,11 @@ def bench_config2(args, rank, local_rank, world_size):
     pass_ms, pass_n, tick_ms = batch.timing(False)
     b_ms = max_over_ranks(e0.elapsed_time(e1), world_size)
     value = total_cells * args.steps / (b_ms / 1e3) / 1e9
+    if args.batch_only:
+        # the batched timed region alone (the launch list of the profiles is taken this way)
+        return {"metric": METRIC, "value": round(value, 4), "unit": "Gcell/s", "steps": args.steps,
+                "ms_per_step": round(b_ms / args.steps, 4), "gpu_launches": int(launches), "autotune": choice,
+                "colour_pass_ms": round(pass_ms / max(pass_n, 1), 4), "note": "--batch-only: no other arm"}
     digest_b = worlds_digest(worlds, fse)
 
     # end to end through the C ABI with host buffers: every step uploads each
@@ -1310,6 +1315,8 @@ def main():
     ap.add_argument("--impl", default="fse", choices=["fse", "reference"])
     ap.add_argument("--workload", type=int, default=2, choices=[0, 1, 2, 3, 4])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="batch workload: time the batched steps only (no per-world arm, digests, e2e or CPU legs)")
     ap.add_argument("--no-config1", action="store_true",
                     help="batch workload: skip the 4096x2048 single-world line reported beside it")
     ap.add_argument("--only", default=None, choices=["render", "temperature", "pack", "reference_order"],
