@@ -245,7 +245,8 @@ class World:
 
     def set_launch(self, colour_shape):
         """Launch shape of the colour pass: 0 CTA per chunk, 1 persistent CTAs, 2 CTA pair
-        per chunk, 3 persistent pairs (results never depend on it)."""
+        per chunk, 3 persistent pairs, 4 the fused tick (every pass in one launch,
+        chunk-passes started as their neighbourhoods finish). Results never depend on it."""
         check(self.lib.fse_world_set_launch(self.h, colour_shape), "world_set_launch")
 
     def set_tick_zone(self, x, y, w, h):
@@ -514,7 +515,13 @@ class Batch:
 
 
 class Server:
-    """Device-resident worlds served by continuous batching under an HBM budget."""
+    """World-tick requests served by continuous batching under an HBM budget.
+
+    Worlds keep their state in HBM while they fit the budget; the rest are parked
+    in host memory as exact checkpoints and restored when a request for them is
+    admitted. step() enqueues one batched tick of the active requests and returns
+    while it runs (up to `depth` steps in flight); poll() reports finished requests
+    with their device completion times."""
 
     def __init__(self, hbm_budget_bytes, max_active):
         self.lib = lib()
@@ -579,6 +586,27 @@ class Server:
         n = C.c_int(0)
         check(self.lib.fse_server_poll(self.h, 0.0, ptr(ids), ptr(done), cap, C.byref(n)), "server_poll")
         return ids[: n.value], done[: n.value]
+
+    def set_depth(self, depth):
+        """Steps in flight before step() waits for the oldest (1..64)."""
+        check(self.lib.fse_server_set_depth(self.h, int(depth)), "server_set_depth")
+
+    def drain(self):
+        check(self.lib.fse_server_drain(self.h), "server_drain")
+
+    STAT_KEYS = ("steps", "restored", "parked_out", "resident", "parked", "max_in_flight", "queued", "active")
+
+    def stats(self):
+        out = np.zeros(len(self.STAT_KEYS), np.int64)
+        check(self.lib.fse_server_stats(self.h, ptr(out), len(out)), "server_stats")
+        return dict(zip(self.STAT_KEYS, (int(v) for v in out)))
+
+    def tick_times(self, cap=1 << 20):
+        """Device milliseconds of the steps retired since the last call."""
+        ms = np.zeros(cap, np.float32)
+        n = C.c_int(0)
+        check(self.lib.fse_server_tick_times(self.h, ptr(ms), cap, C.byref(n)), "server_tick_times")
+        return ms[: n.value].copy()
 
 
 def write_png(path, rgba):

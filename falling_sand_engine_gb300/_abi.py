@@ -150,6 +150,10 @@ SIGNATURES = {
     "fse_server_step": (_i, [_vp, C.POINTER(_i)]),
     "fse_server_now_us": (_d, [_vp]),
     "fse_server_poll": (_i, [_vp, _d, _vp, _vp, _i, C.POINTER(_i)]),
+    "fse_server_set_depth": (_i, [_vp, _i]),
+    "fse_server_drain": (_i, [_vp]),
+    "fse_server_stats": (_i, [_vp, _vp, _i]),
+    "fse_server_tick_times": (_i, [_vp, _vp, _i, C.POINTER(_i)]),
 }
 
 _lib = None

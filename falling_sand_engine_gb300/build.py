@@ -8,14 +8,15 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfse.so")
-SOURCES = ["fse_tick.cu", "fse_particles.cu", "fse_objects.cu", "fse_api.cu", "fse_batch.cu", "fse_noalloc.cu",
+SOURCES = ["fse_tick.cu", "fse_particles.cu", "fse_objects.cu", "fse_api.cu", "fse_batch.cu", "fse_server.cu", "fse_noalloc.cu",
            "fse_render.cu", "fse_islands.cu", "fse_temperature.cu", "fse_tick_temp.cu",
            "fse_pack.cu", "fse_tiles.cu", "fse_tick_seq.cu", "fse_tick_f32.cu", "fse_tick_f32_seq.cu",
-           "fse_tick_pair.cu", "fse_tick_pair_f32.cu"]
+           "fse_tick_pair.cu", "fse_tick_pair_f32.cu", "fse_tick_fused.cu", "fse_tick_fused_f32.cu"]
 # sources that include another source
 SOURCE_DEPS = {"fse_tick_temp.cu": ["fse_tick.cu"], "fse_tick_seq.cu": ["fse_tick.cu"],
                "fse_tick_f32.cu": ["fse_tick.cu"], "fse_tick_f32_seq.cu": ["fse_tick.cu"],
-               "fse_tick_pair.cu": ["fse_tick.cu"], "fse_tick_pair_f32.cu": ["fse_tick.cu"]}
+               "fse_tick_pair.cu": ["fse_tick.cu"], "fse_tick_pair_f32.cu": ["fse_tick.cu"],
+               "fse_tick_fused.cu": ["fse_tick.cu"], "fse_tick_fused_f32.cu": ["fse_tick.cu"]}
 HEADERS = ["fse_internal.cuh", "fse_host.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

@@ -393,7 +393,33 @@ int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], con
                  int threads, int grid, bool particles, int move_blocks, int stage_blocks, cudaStream_t s,
                  PassTimer *timer, int temp_tiles, bool temp_track, bool seq, bool f32) {
     int halo = tick_halo();
-    for (int iter = 0; iter < max_iter; iter++)  // world.cpp:1050
+    const bool fused = grid == FUSED_GRID && !seq && threads == CP_THREADS;
+    if (grid == FUSED_GRID && !fused) grid = 0;  // the reference's order runs pass by pass
+    if (fused && max_iter > 0) {
+        // the fused tick: one launch for every pass (world.cpp:1050-1060)
+        cudaEvent_t a = nullptr, b = nullptr;
+        if (timer) {
+            a = timer->get();
+            b = timer->get();
+            if (timer->record(a, s) != cudaSuccess) return FSE_E_CUDA;
+        }
+        FusedTick ft;
+        for (int tk = 0; tk < 4; tk++) {
+            ft.items[tk] = items[tk];
+            ft.n[tk] = n_items[tk];
+        }
+        ft.passes = 4 * max_iter;
+        ft.n_worlds = n_worlds;
+        cudaError_t e = f32 ? launch_colour_fused_f32(d_worlds, ft, g_dev_mt, halo, C, sm_count(), s, temp_track)
+                            : launch_colour_fused(d_worlds, ft, g_dev_mt, halo, C, sm_count(), s, temp_track);
+        if (e != cudaSuccess) return FSE_E_CUDA;
+        if (timer) {
+            if (timer->record(b, s) != cudaSuccess) return FSE_E_CUDA;
+            timer->record_pair(a, b);
+        }
+        count_launches(1);
+    }
+    for (int iter = 0; iter < max_iter && !fused; iter++)  // world.cpp:1050
         for (int tk = 0; tk < 4; tk++) {         // world.cpp:1057-1060
             cudaEvent_t a = nullptr, b = nullptr;
             if (timer) {
@@ -711,7 +737,7 @@ static void free_world(fse_world *w) {
     WorldDev &h = w->h;
     void *ptrs[] = {h.id, h.col, h.sc, h.fl, h.df, h.tp, h.tnew, h.stage, h.cp_count, h.cp_base, h.p_state, h.p_box0,
                     h.p_box1, h.p_cell, h.p_prev, h.chg, h.scan_tmp, h.ledger, h.airmap, w->ctr, w->d, w->claim,
-                    w->mask_bits, w->obj_list, w->obj_n, h.merge_list, h.merge_count, h.merge_claim};
+                    w->mask_bits, w->obj_list, w->obj_n, h.merge_list, h.merge_count, h.merge_claim, h.cdone};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     PartSoA *ps[2] = {&h.p, &h.q};
@@ -835,7 +861,7 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
               dalloc(w, &h.p_prev, (size_t)h.part_cap) && dalloc(w, &h.scan_tmp, particle_scan_blocks() + 1) &&
               dalloc(w, &h.airmap, (size_t)h.amw * h.amh) && dalloc(w, &h.chg, 2 * (size_t)h.amw * h.amh) &&
               dalloc(w, &h.merge_list, 2 * (size_t)h.part_cap) && dalloc(w, &h.merge_count, 1) &&
-              dalloc(w, &w->d, 1);
+              dalloc(w, &h.cdone, (size_t)h.nCx * h.nCy) && dalloc(w, &w->d, 1);
     PartSoA *ps[2] = {&h.p, &h.q};
     size_t pc = (size_t)h.part_cap;
     for (int k = 0; k < 2 && ok; k++) {
@@ -883,7 +909,9 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
     h.tick = (uint32_t *)(w->ctr + 6);
     h.bar = (unsigned *)(w->ctr + 8);  // [8] arrivals, [9] generation
     h.stats = w->ctr + 10;             // [10] iterations of the last particle update
+    h.sched = (uint32_t *)(w->ctr + 12);  // [12] next ticket, [13] CTAs finished, [14] a wait gave up (fused tick)
     cudaMemset(w->ctr, 0, 16 * sizeof(int32_t));
+    cudaMemset(h.cdone, 0, (size_t)h.nCx * h.nCy * sizeof(uint32_t));
     cudaMemset(h.ledger, 0, LED_ROWS * MAXMAT * sizeof(long long));
     cudaMemset(h.cp_count, 0, ncp * sizeof(int32_t));
     cudaMemset(h.merge_count, 0, sizeof(int32_t));
@@ -959,7 +987,7 @@ int fse_world_set_tick(fse_world *w, uint32_t tick) {
 }
 
 int fse_world_set_launch(fse_world *w, int colour_shape_id) {
-    if (!w || colour_shape_id < 0 || colour_shape_id > 3) return FSE_E_INVAL;
+    if (!w || colour_shape_id < 0 || colour_shape_id >= COLOUR_SHAPES) return FSE_E_INVAL;
     FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
     colour_shape(colour_shape_id, &w->threads, &w->grid);
     for (auto &g : w->graphs) cudaGraphExecDestroy(g.second);

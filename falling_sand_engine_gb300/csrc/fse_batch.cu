@@ -73,19 +73,23 @@ int build_tables(const std::vector<fse_world *> &ws, WorldDev **d_table, uint32_
     return FSE_OK;
 }
 
+}  // namespace
+
 // the most temperature tiles of the worlds that run the temperature step (0: none)
-int temp_tiles_of(const std::vector<fse_world *> &ws) {
+int fse::temp_tiles_of(const std::vector<fse_world *> &ws) {
     int t = 0;
     for (const fse_world *w : ws)
         if (w->h.temp_on) t = std::max(t, temperature_tiles(w->W, w->H));
     return t;
 }
 // some world keeps liquid temperatures: the colour pass that copies them runs
-bool temp_track_of(const std::vector<fse_world *> &ws) {
+bool fse::temp_track_of(const std::vector<fse_world *> &ws) {
     for (const fse_world *w : ws)
         if (w->h.tp) return true;
     return false;
 }
+
+namespace {
 
 int batch_enqueue(fse_batch *b, int n) {
     int rc = ensure_materials_pushed();
@@ -349,7 +353,8 @@ int fse_batch_timing(fse_batch *b, int enable, double *out_pass_ms, int64_t *out
 }
 
 int fse_batch_set_launch(fse_batch *b, int colour_ctas_per_sm, int particle_blocks) {
-    if (!b || colour_ctas_per_sm < 0 || colour_ctas_per_sm > 3 || particle_blocks < 0) return FSE_E_INVAL;
+    if (!b || colour_ctas_per_sm < 0 || colour_ctas_per_sm >= COLOUR_SHAPES || particle_blocks < 0)
+        return FSE_E_INVAL;
     colour_shape(colour_ctas_per_sm, &b->threads, &b->grid);
     b->move_blocks = particle_blocks == 0 ? b->max_move_blocks : std::min(particle_blocks, b->max_move_blocks);
     for (auto &g : b->graphs) cudaGraphExecDestroy(g.second);
@@ -361,10 +366,10 @@ int fse_batch_set_launch(fse_batch *b, int colour_ctas_per_sm, int particle_bloc
 // Time each launch shape on the batch itself and put every world back as it
 // was. The shape never changes results: a chunk's pass does not depend on which
 // CTA runs it or when, and particle kernels stride over their lists whatever the
-// grid. Knobs: the colour-pass grid (one CTA per chunk, scheduled by the hardware,
-// or one persistent CTA per SM walking the chunk list) and the number of blocks
-// each world's particle kernels get (batches of small worlds waste launches on
-// empty blocks).
+// grid. Knobs: the colour-pass shape (one CTA per chunk scheduled by the hardware,
+// one persistent CTA per SM walking the chunk list, a CTA pair per chunk, or the
+// fused tick with every pass in one launch) and the number of blocks each world's
+// particle kernels get (batches of small worlds waste launches on empty blocks).
 int fse_batch_autotune(fse_batch *b, int32_t out_choice[4]) {
     if (!b) return FSE_E_INVAL;
     int rc = batch_sync(b);
@@ -378,7 +383,7 @@ int fse_batch_autotune(fse_batch *b, int32_t out_choice[4]) {
     // the candidates' steps are not part of any timing the caller asked for
     PassTimer *keep_timer = b->timer;
     b->timer = nullptr;
-    const int cand[][2] = {{0, 0}, {1, 0}, {0, 4}, {0, 16}, {1, 16}, {2, 4}, {3, 4}, {2, 16}};
+    const int cand[][2] = {{0, 0}, {1, 0}, {4, 0}, {0, 4}, {0, 16}, {4, 16}, {1, 16}, {2, 4}};
     const int n_cand = (int)(sizeof(cand) / sizeof(cand[0]));
     float best = 1e30f;
     int bi = 0;
@@ -421,212 +426,5 @@ int fse_batch_sync(fse_batch *b) {
 }
 
 void *fse_batch_stream(fse_batch *b) { return b ? (void *)b->stream : nullptr; }
-
-}  // extern "C"
-
-// ================================================================ serving
-struct fse_server {
-    int64_t budget, in_use = 0;
-    int max_active;
-    std::vector<fse_world *> slots;
-    std::vector<int64_t> slot_bytes;
-    struct Req {
-        int64_t id;
-        int slot, left;
-        double arrival;
-    };
-    std::deque<Req> queue;
-    std::vector<Req> active;
-    std::vector<std::pair<int64_t, double>> done;
-    int64_t next_id = 0;
-    // batch tables for the current active set
-    WorldDev *d_table = nullptr;
-    uint32_t *items[4] = {nullptr, nullptr, nullptr, nullptr};
-    int n_items[4] = {0, 0, 0, 0};
-    std::vector<int> table_slots;
-    cudaStream_t stream = nullptr;
-    int C = 128;
-    std::chrono::steady_clock::time_point t0;
-};
-
-static int64_t world_footprint(int w, int h, const fse_config *cfg) {
-    long long cells = (long long)w * h;
-    long long pc = (cfg && cfg->particle_capacity > 0) ? cfg->particle_capacity : std::max<long long>(65536, cells / 4);
-    long long sc = (cfg && cfg->spawn_capacity > 0) ? cfg->spawn_capacity : pc;
-    // planes; two particle SoAs, the outcome byte, four outcome words and two merge-list words
-    return cells * 15 + pc * (2 * 56 + 1 + 4 * 6) + sc * (long long)sizeof(SpawnRec) + (1 << 20);
-}
-
-extern "C" {
-
-int fse_server_create(int64_t budget, int max_active, fse_server **out) {
-    if (!out || budget <= 0 || max_active <= 0) return FSE_E_INVAL;
-    fse_server *s = new fse_server();
-    s->budget = budget;
-    s->max_active = max_active;
-    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
-        delete s;
-        return FSE_E_CUDA;
-    }
-    s->t0 = std::chrono::steady_clock::now();
-    *out = s;
-    return FSE_OK;
-}
-
-int fse_server_destroy(fse_server *s) {
-    if (!s) return FSE_E_INVAL;
-    cudaStreamSynchronize(s->stream);
-    for (fse_world *w : s->slots)
-        if (w) fse_world_destroy(w);
-    if (s->d_table) cudaFree(s->d_table);
-    for (int k = 0; k < 4; k++)
-        if (s->items[k]) cudaFree(s->items[k]);
-    cudaStreamDestroy(s->stream);
-    delete s;
-    return FSE_OK;
-}
-
-int fse_server_add_world(fse_server *s, int w, int h, const fse_config *cfg, int gen_kind, uint32_t gen_seed,
-                         int *out_slot) {
-    if (!s || !out_slot) return FSE_E_INVAL;
-    int64_t need = world_footprint(w, h, cfg);
-    if (s->in_use + need > s->budget) return FSE_E_BUDGET;
-    fse_config c{};
-    if (cfg) c = *cfg;
-    if (c.chunk_size == 0) c.chunk_size = 128;
-    // servers batch their worlds in the partitioned order with Q16.16 amounts
-    if (c.flags & (FSE_CFG_REFERENCE_ORDER | FSE_CFG_F32_FLUID)) return FSE_E_INVAL;
-    if (!s->slots.empty()) {
-        for (fse_world *x : s->slots)
-            if (x && x->C != c.chunk_size) return FSE_E_INVAL;
-    }
-    c.stream = (void *)s->stream;
-    fse_world *wd = nullptr;
-    int rc = fse_world_create(w, h, &c, &wd);
-    if (rc) return rc;
-    rc = fse_world_generate(wd, gen_kind, gen_seed);
-    if (rc) {
-        fse_world_destroy(wd);
-        return rc;
-    }
-    s->C = c.chunk_size;
-    int slot = -1;
-    for (size_t i = 0; i < s->slots.size(); i++)
-        if (!s->slots[i]) slot = (int)i;
-    if (slot < 0) {
-        slot = (int)s->slots.size();
-        s->slots.push_back(nullptr);
-        s->slot_bytes.push_back(0);
-    }
-    s->slots[slot] = wd;
-    s->slot_bytes[slot] = (int64_t)wd->bytes;
-    s->in_use += (int64_t)wd->bytes;
-    *out_slot = slot;
-    return FSE_OK;
-}
-
-int fse_server_remove_world(fse_server *s, int slot) {
-    if (!s || slot < 0 || slot >= (int)s->slots.size() || !s->slots[slot]) return FSE_E_INVAL;
-    for (auto &r : s->active)
-        if (r.slot == slot) return FSE_E_STATE;
-    for (auto &r : s->queue)
-        if (r.slot == slot) return FSE_E_STATE;
-    fse_world_destroy(s->slots[slot]);
-    s->slots[slot] = nullptr;
-    s->in_use -= s->slot_bytes[slot];
-    s->slot_bytes[slot] = 0;
-    return FSE_OK;
-}
-
-int64_t fse_server_bytes_in_use(const fse_server *s) { return s ? s->in_use : -1; }
-
-double fse_server_now_us(const fse_server *s) {
-    if (!s) return 0.0;
-    return std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - s->t0).count();
-}
-
-fse_world *fse_server_world(fse_server *s, int slot) {
-    if (!s || slot < 0 || slot >= (int)s->slots.size()) return nullptr;
-    return s->slots[slot];
-}
-
-int fse_server_submit(fse_server *s, int slot, int n_ticks, double arrival_us, int64_t *out_request) {
-    if (!s || slot < 0 || slot >= (int)s->slots.size() || !s->slots[slot] || n_ticks <= 0) return FSE_E_INVAL;
-    fse_server::Req r{s->next_id++, slot, n_ticks, arrival_us};
-    s->queue.push_back(r);
-    if (out_request) *out_request = r.id;
-    return FSE_OK;
-}
-
-// one scheduling step: admit queued requests while slots are free (one request
-// per world at a time, arrival order), tick every active world once in one
-// batched launch sequence, retire finished requests
-int fse_server_step(fse_server *s, int *out_active) {
-    if (!s) return FSE_E_INVAL;
-    bool changed = false;
-    for (auto it = s->queue.begin(); it != s->queue.end() && (int)s->active.size() < s->max_active;) {
-        bool busy = false;
-        for (auto &a : s->active)
-            if (a.slot == it->slot) busy = true;
-        if (busy) {
-            ++it;
-            continue;
-        }
-        s->active.push_back(*it);
-        it = s->queue.erase(it);
-        changed = true;
-    }
-    if (out_active) *out_active = (int)s->active.size();
-    if (s->active.empty()) return FSE_OK;
-    std::vector<int> want;
-    for (auto &a : s->active) want.push_back(a.slot);
-    std::sort(want.begin(), want.end());
-    if (changed || want != s->table_slots) {
-        std::vector<fse_world *> ws;
-        for (int sl : want) ws.push_back(s->slots[sl]);
-        int rc = build_tables(ws, &s->d_table, s->items, s->n_items, s->stream);
-        if (rc) return rc;
-        s->table_slots = want;
-    }
-    int max_iter = 0, mb = 1, sb = 1;
-    for (int sl : want) {
-        fse_world *w = s->slots[sl];
-        max_iter = std::max(max_iter, w->cell_iter);
-        mb = std::max(mb, std::min(sm_count() * 2, ceil_div(w->part_cap, 256)));
-        sb = std::max(sb, std::min(sm_count(), ceil_div(w->stage_cap, 256)));
-    }
-    int rc = ensure_materials_pushed();
-    if (rc) return rc;
-    std::vector<fse_world *> act;
-    for (int sl : want) act.push_back(s->slots[sl]);
-    rc = enqueue_step(s->d_table, (int)want.size(), s->items, s->n_items, max_iter, s->C, 1024, 0, true, mb, sb,
-                      s->stream, nullptr, temp_tiles_of(act), temp_track_of(act));
-    if (rc) return rc;
-    if (cudaStreamSynchronize(s->stream) != cudaSuccess) return FSE_E_CUDA;
-    double now = std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - s->t0).count();
-    std::vector<fse_server::Req> keep;
-    for (auto &a : s->active) {
-        a.left--;
-        if (a.left <= 0)
-            s->done.push_back({a.id, now});
-        else
-            keep.push_back(a);
-    }
-    s->active.swap(keep);
-    return FSE_OK;
-}
-
-int fse_server_poll(fse_server *s, double now_us, int64_t *ids, double *done_us, int cap, int *out_n) {
-    (void)now_us;
-    if (!s || cap < 0) return FSE_E_INVAL;
-    int m = std::min<int>(cap, (int)s->done.size());
-    for (int i = 0; i < m; i++) {
-        if (ids) ids[i] = s->done[i].first;
-        if (done_us) done_us[i] = s->done[i].second;
-    }
-    s->done.erase(s->done.begin(), s->done.begin() + m);
-    if (out_n) *out_n = m;
-    return FSE_OK;
-}
 
 }  // extern "C"

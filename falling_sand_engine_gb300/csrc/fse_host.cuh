@@ -92,6 +92,11 @@ size_t colour_pass_smem(int C, int halo);
 cudaError_t launch_colour_pass(const WorldDev *worlds, const uint32_t *items, int n_items, int iter, int tk,
                                const MatTable *mt, int halo, int C, int threads, int grid, cudaStream_t s,
                                bool temp = false, bool seq = false, bool f32 = false);
+// every colour pass of a tick in one launch of `grid` CTAs (the fused tick)
+cudaError_t launch_colour_fused(const WorldDev *worlds, const FusedTick &ft, const MatTable *mt, int halo, int C,
+                                int grid, cudaStream_t s, bool temp);
+cudaError_t launch_colour_fused_f32(const WorldDev *worlds, const FusedTick &ft, const MatTable *mt, int halo, int C,
+                                    int grid, cudaStream_t s, bool temp);
 cudaError_t launch_spawn_append(WorldDev *d_worlds, int n_worlds, int stage_blocks, cudaStream_t s);
 cudaError_t launch_particle_tick(WorldDev *d_worlds, int n_worlds, const MatTable *mt, int move_blocks,
                                  cudaStream_t s);
@@ -116,14 +121,21 @@ int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], con
                  PassTimer *timer = nullptr, int temp_tiles = 0, bool temp_track = false, bool seq = false,
                  bool f32 = false);
 void count_launches(long long n);
+// the most temperature tiles of the worlds that run the temperature step (0: none)
+int temp_tiles_of(const std::vector<fse_world *> &ws);
+// some world keeps liquid temperatures: the colour pass that copies them runs
+bool temp_track_of(const std::vector<fse_world *> &ws);
 
 // Launch shapes of the colour pass (threads per CTA, chunk workers; 0 = one per chunk):
 // 0 one 1024-thread CTA per chunk; 1 one persistent CTA per SM walking the chunks;
 // 2 each chunk split over a CTA pair (a cluster of two 512-thread CTAs); 3 persistent
-// pairs, two CTAs per SM
+// pairs, two CTAs per SM; 4 the fused tick (every pass in one launch, one CTA per SM,
+// chunk-passes started as their neighbourhoods finish), FUSED_GRID
+constexpr int COLOUR_SHAPES = 5;
+constexpr int FUSED_GRID = -1;
 inline void colour_shape(int shape, int *threads, int *grid) {
-    *threads = shape >= 2 ? 512 : 1024;
-    *grid = (shape == 1 || shape == 3) ? sm_count() : 0;
+    *threads = (shape == 2 || shape == 3) ? 512 : 1024;
+    *grid = (shape == 1 || shape == 3) ? sm_count() : (shape == 4 ? FUSED_GRID : 0);
 }
 
 }  // namespace fse

@@ -14,6 +14,7 @@ enum : int { T_AIR = 0, T_SOLID = 1, T_SAND = 2, T_SOUP = 3, T_GAS = 4, T_OBJECT
 enum : int { INTER_TRANSFORM = 1, INTER_SPAWN = 2, REACT_BELOW = 4, REACT_ABOVE = 5 };
 
 constexpr int MAXMAT = 256;
+constexpr int CP_THREADS = 1024;  // colour-pass CTA: >= the largest sweep-A sub-phase (43 x 22 cells, 128-cell chunks)
 constexpr uint8_t MOVED = 0x80;
 constexpr uint8_t VISITED = 0x40;  // shared-memory copy only; never stored to HBM
 constexpr uint8_t SETTLE_MASK = 0x3F;
@@ -202,6 +203,23 @@ struct WorldDev {
     int32_t *merge_list;
     int32_t *merge_count;
     uint32_t *merge_claim;
+    // the fused tick (all colour passes of a tick in one launch, each chunk-pass
+    // started when the chunk-passes it depends on are done): per chunk of the zone,
+    // the index + 1 of the last pass done on it in the running launch (all zero
+    // between launches); sched = {next ticket, CTAs finished, a wait gave up} of a
+    // launch whose table starts with this world
+    uint32_t *cdone;
+    uint32_t *sched;
+};
+
+// The fused tick's work list: the chunk slots of each colour ((world << 20) | slot,
+// the per-pass launches' items), passes = cell_iter * 4 of the longest world, and
+// the worlds of the table (their completion flags are cleared at the end)
+struct FusedTick {
+    const uint32_t *items[4];
+    int n[4];
+    int passes;
+    int n_worlds;
 };
 
 // the amount of a new SOUP tile of material mid (TilesCreate, and the

@@ -59,7 +59,6 @@ __device__ unsigned long long g_phase_max[16];  // per phase: the largest CTA to
 
 namespace fse {
 
-constexpr int CP_THREADS = 1024;  // >= the largest sweep-A sub-phase (43 x 22 cells for 128-cell chunks)
 constexpr int MAXRW = 160;        // tile row width bound (chunk <= 128, halo <= 5), a multiple of 32
 
 // 4-byte global -> shared copy that does not pass through registers (sm_80+ cp.async)
@@ -159,6 +158,22 @@ __device__ __forceinline__ uint32_t cluster_rank() {
 __device__ __forceinline__ void cluster_sync() {
     asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
 }
+
+// ------------------------------------------------- fused-tick flag helpers
+__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(uint32_t *p, uint32_t v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+constexpr unsigned long long FUSED_WAIT_NS = 2000000000ull;  // a dependency wait gives up after 2 s
 
 // LIVE: the pillar reads the tile as it stands (the reference's own order, where
 // one thread updates the chunk's cells in turn) instead of the sweep-B snapshot.
@@ -1266,6 +1281,16 @@ struct SmemHeadT {
 using SmemHead = SmemHeadT<CP_THREADS>;
 
 // items: (world << 20) | chunk slot within the colour; iter, tk select the pass.
+// FUSED: every pass of the tick in one launch (iter, tk, items and n_items unused;
+// ft holds the work). CTAs take chunk-passes in pass order from a ticket counter; a
+// chunk-pass starts when the last earlier pass of each chunk of its 3 x 3
+// neighbourhood is done (a chunk-pass reads and writes its chunk plus a halo of at
+// most 5 cells, and each pass's chunks tile the zone, so these are all the
+// chunk-passes it can conflict with, directly or through a chain), and publishes
+// its own completion with a release store. A CTA only waits for tickets taken
+// before its own by CTAs that are running, so the launch cannot deadlock whatever
+// its grid; each wait is also bounded (ERR_TIMEOUT). The last CTA to finish clears
+// the flags and the counters for the next launch.
 // SEQ: the reference's own order inside each chunk (bottom row first, left to right,
 // sweep by sweep; world.cpp:1084-1087, 1589, 1823), with the same rules, run as a
 // wavefront of one thread per chunk row (see sweeps_seq)
@@ -1275,11 +1300,12 @@ using SmemHead = SmemHeadT<CP_THREADS>;
 // and writing back its own rows; sub-phases end with a cluster barrier. A chunk's
 // sub-phases then run on two SMs, and an SM holds halves of two chunks whose
 // barriers interleave.
-template <int HALO, bool TEMP, bool SEQ, bool F32, bool PAIR = false>
+template <int HALO, bool TEMP, bool SEQ, bool F32, bool PAIR = false, bool FUSED = false>
 __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 : 1)
-    k_colour_pass(const WorldDev *__restrict__ worlds, const uint32_t *__restrict__ items, int n_items, int iter, int tk,
-                  const MatTable *__restrict__ mt) {
+    k_colour_pass(const WorldDev *__restrict__ worlds, const uint32_t *__restrict__ items, int n_items, int iter_arg,
+                  int tk_arg, const MatTable *__restrict__ mt, const FusedTick ft) {
     static_assert(!(PAIR && SEQ), "the reference order runs a chunk in one CTA");
+    static_assert(!(FUSED && (PAIR || SEQ)), "the fused tick runs partitioned chunk-passes in one CTA each");
     constexpr int T = PAIR ? CP_THREADS / 2 : CP_THREADS;
     using Head = SmemHeadT<T>;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -1296,7 +1322,7 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
     }
     for (int i = tid; i < LED_ROWS * 64; i += T) S.led[i] = 0;
     Ctx c;
-    c.iter = iter;
+    c.iter = iter_arg;
     c.mt = mt;
     c.led_s = S.led;
     c.ma = S.ma;
@@ -1312,18 +1338,99 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
     FSE_PT_DECL
     __syncthreads();
 
-    const int ox = tk % 2, oy = 1 - tk / 2;
+    int iter = iter_arg, tk = tk_arg;
     long long *led_g_last = nullptr;
 
     const int wstart = PAIR ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
     const int wstride = PAIR ? (int)(gridDim.x >> 1) : (int)gridDim.x;
-    for (int it = wstart; it < n_items; it += wstride) {
-        const uint32_t item = __ldg(&items[it]);
+    // FUSED: the ticket taken, and the completion flag this CTA publishes before it
+    // takes the next one (kept in shared memory: the tile code needs the registers)
+    __shared__ int s_ticket;
+    __shared__ uint32_t *s_done_flag;
+    __shared__ uint32_t s_done_value;
+    if (FUSED && tid == 0) s_done_flag = nullptr;
+    for (int it = wstart;; it += wstride) {
+        uint32_t item;
+        if constexpr (FUSED) {
+            if (tid == 0) {
+                if (s_done_flag) {
+                    __threadfence();
+                    st_release_gpu(s_done_flag, s_done_value);
+                    s_done_flag = nullptr;
+                }
+                s_ticket = (int)atomicAdd(&worlds[0].sched[0], 1u);
+            }
+            __syncthreads();
+            int t = s_ticket;
+            const int per_iter = ft.n[0] + ft.n[1] + ft.n[2] + ft.n[3];
+            if (t >= per_iter * (ft.passes / 4)) break;
+            iter = t / per_iter;
+            t -= iter * per_iter;
+            // the colour and the index within it (no dynamic indexing of the parameters)
+            const uint32_t *li = ft.items[0];
+            tk = 0;
+            if (t >= ft.n[0]) {
+                t -= ft.n[0];
+                tk = 1;
+                li = ft.items[1];
+                if (t >= ft.n[1]) {
+                    t -= ft.n[1];
+                    tk = 2;
+                    li = ft.items[2];
+                    if (t >= ft.n[2]) {
+                        t -= ft.n[2];
+                        tk = 3;
+                        li = ft.items[3];
+                    }
+                }
+            }
+            item = __ldg(&li[t]);
+        } else {
+            if (it >= n_items) break;
+            item = __ldg(&items[it]);
+        }
+        const int ox = tk % 2, oy = 1 - tk / 2;
+        c.iter = iter;
         if (tid == 0) s_w = worlds[item >> 20];
         __syncthreads();
         FSE_PT(0)
         const WorldDev &w = s_w;
         const int slot = (int)(item & 0xFFFFF);
+        if constexpr (FUSED) {
+            // wait until the chunk-passes this one depends on are done: for each chunk
+            // of the 3 x 3 neighbourhood, its last pass before this one
+            const int nbq = (w.nCy - oy + 1) / 2;
+            const int a = ox + 2 * (slot / nbq), b = oy + 2 * (slot % nbq);
+            const int q = iter * 4 + tk;
+            if (tid < 9) {
+                const int a2 = a + tid % 3 - 1, b2 = b + tid / 3 - 1;
+                if (a2 >= 0 && a2 < w.nCx && b2 >= 0 && b2 < w.nCy) {
+                    const int tn = (a2 & 1) + 2 * (1 - (b2 & 1));
+                    const int p = tn < tk ? iter * 4 + tn : (iter - 1) * 4 + tn;
+                    if (p >= 0) {
+                        const uint32_t *f = &w.cdone[(size_t)b2 * w.nCx + a2];
+                        // sched[2]: a wait of this launch gave up; the others do not wait
+                        volatile uint32_t *abort = &worlds[0].sched[2];
+                        if (ld_acquire_gpu(f) <= (uint32_t)p && !*abort) {
+                            const unsigned long long t0 = global_ns();
+                            while (ld_acquire_gpu(f) <= (uint32_t)p && !*abort) {
+                                if (global_ns() - t0 > FUSED_WAIT_NS) {
+                                    atomicOr(w.err, ERR_TIMEOUT);
+                                    *abort = 1u;
+                                    break;
+                                }
+                                __nanosleep(64);
+                            }
+                        }
+                    }
+                }
+            }
+            if (tid == 0) {
+                s_done_flag = &w.cdone[(size_t)b * w.nCx + a];
+                s_done_value = (uint32_t)q + 1u;
+            }
+            __syncthreads();
+        }
         if (led_g_last != w.ledger && led_g_last != nullptr) {
             // flush the shared ledger before switching worlds
             for (int i = tid; i < LED_ROWS * 64; i += T) {
@@ -1428,7 +1535,7 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
                     Tl.s_id[i] = v[k];
                     if (full) Tl.s_fl[i] = f[k];
                     if (gx >= cx && gx < cx + C && gy >= cy + o0 && gy < cy + o1 && rin && gx < W) {
-                        if (mt_iter(S.ma[v[k]]) > iter) active = 1;
+                        if (mt_iter(S.ma[v[k]]) > c.iter) active = 1;
                         if ((int)v[k] == c.id_fire) fire = 1;
                     }
                 }
@@ -1484,7 +1591,7 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
             const bool row = k < chh;
             int spawned = 0;
             for (int sweep = 0; sweep < 3; sweep++) {
-                c.pk = pass_key(w.seed, *w.tick, (uint32_t)(iter * 3 + sweep));
+                c.pk = pass_key(w.seed, *w.tick, (uint32_t)(c.iter * 3 + sweep));
                 const int steps = cw + s * (chh - 1);
                 for (int t = 0; t < steps; t++) {
                     const int dx = t - s * k;
@@ -1512,7 +1619,7 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
         };
         auto sweeps = [&](const auto &Tl) {
         for (int sweep = 0; sweep < 3; sweep++) {
-            c.pk = pass_key(w.seed, *w.tick, (uint32_t)(iter * 3 + sweep));
+            c.pk = pass_key(w.seed, *w.tick, (uint32_t)(c.iter * 3 + sweep));
             if (sweep == 1) {
                 // AIR snapshot for the friction pillar: columns cx-1..cx+C, rows cy+1..cy+C+9
                 for (int task = tid; task < (C + 2) * 5; task += T) {
@@ -1681,10 +1788,33 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
     }
     // a CTA of a pair leaves only when its partner no longer writes to it
     if constexpr (PAIR) cluster_sync();
+    if constexpr (FUSED) {
+        // the last CTA out clears the completion flags and the counters
+        __syncthreads();
+        if (tid == 0) {
+            __threadfence();
+            s_ticket = (atomicAdd(&worlds[0].sched[1], 1u) == gridDim.x - 1) ? 1 : 0;
+        }
+        __syncthreads();
+        if (s_ticket) {
+            __threadfence();
+            for (int wi = 0; wi < ft.n_worlds; wi++) {
+                uint32_t *f = worlds[wi].cdone;
+                const int nc = worlds[wi].nCx * worlds[wi].nCy;
+                for (int i = tid; i < nc; i += T) f[i] = 0u;
+            }
+            if (tid == 0) {
+                worlds[0].sched[0] = 0u;
+                worlds[0].sched[1] = 0u;
+                worlds[0].sched[2] = 0u;
+            }
+        }
+    }
     FSE_PT_FLUSH
 }
 
-#if !defined(FSE_TICK_TEMP_TU) && !defined(FSE_TICK_SEQ_TU) && !defined(FSE_TICK_F32_TU) && !defined(FSE_TICK_PAIR_TU)
+#if !defined(FSE_TICK_TEMP_TU) && !defined(FSE_TICK_SEQ_TU) && !defined(FSE_TICK_F32_TU) && \
+    !defined(FSE_TICK_PAIR_TU) && !defined(FSE_TICK_FUSED_TU)
 size_t colour_pass_smem(int C, int halo) {
     size_t RW = (size_t)C + 2 * halo, RHF = (size_t)C + 2 * halo, RHI = (size_t)C + halo + 10;
     size_t nid = RW * RHI, nfull = RW * RHF;
@@ -1704,7 +1834,22 @@ static cudaError_t launch_t(const WorldDev *worlds, const uint32_t *items, int n
                              (int)sm);
         set = sm;
     }
-    k_colour_pass<HALO, TEMP, SEQ, F32><<<grid, CP_THREADS, sm, s>>>(worlds, items, n_items, iter, tk, mt);
+    k_colour_pass<HALO, TEMP, SEQ, F32><<<grid, CP_THREADS, sm, s>>>(worlds, items, n_items, iter, tk, mt,
+                                                                     FusedTick{});
+    return cudaGetLastError();
+}
+
+// the fused tick: one CTA per SM (the tile takes most of an SM's shared memory)
+template <int HALO, bool TEMP, bool F32>
+static cudaError_t launch_fused_t(const WorldDev *worlds, const FusedTick &ft, const MatTable *mt, size_t sm,
+                                  int grid, cudaStream_t s) {
+    static size_t set = 0;
+    if (set < sm) {
+        cudaFuncSetAttribute(k_colour_pass<HALO, TEMP, false, F32, false, true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        set = sm;
+    }
+    k_colour_pass<HALO, TEMP, false, F32, false, true><<<grid, CP_THREADS, sm, s>>>(worlds, nullptr, 0, 0, 0, mt, ft);
     return cudaGetLastError();
 }
 
@@ -1742,12 +1887,32 @@ static cudaError_t launch_pair_t(const WorldDev *worlds, const uint32_t *items, 
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_colour_pass<HALO, TEMP, false, F32, true>, worlds, items, n_items, iter, tk, mt);
+    return cudaLaunchKernelEx(&cfg, k_colour_pass<HALO, TEMP, false, F32, true>, worlds, items, n_items, iter, tk, mt,
+                              FusedTick{});
 }
 
 // Each translation unit that includes this file with one of the defines below
 // compiles one family of instantiations, so that they build in parallel.
-#if defined(FSE_TICK_PAIR_TU)
+#if defined(FSE_TICK_FUSED_TU)
+// the fused tick, Q16.16 amounts (FSE_TICK_FUSED_TU = 1) or f32 (2)
+#define FSE_FUSED_F32 (FSE_TICK_FUSED_TU == 2)
+size_t colour_pass_smem(int C, int halo);
+#if FSE_TICK_FUSED_TU == 2
+cudaError_t launch_colour_fused_f32(const WorldDev *worlds, const FusedTick &ft, const MatTable *mt, int halo, int C,
+                                    int grid, cudaStream_t s, bool temp) {
+#else
+cudaError_t launch_colour_fused(const WorldDev *worlds, const FusedTick &ft, const MatTable *mt, int halo, int C,
+                                int grid, cudaStream_t s, bool temp) {
+#endif
+    const size_t sm = colour_pass_smem(C, halo);
+    if (temp) {
+        if (halo == 5) return launch_fused_t<5, true, FSE_FUSED_F32>(worlds, ft, mt, sm, grid, s);
+        return launch_fused_t<2, true, FSE_FUSED_F32>(worlds, ft, mt, sm, grid, s);
+    }
+    if (halo == 5) return launch_fused_t<5, false, FSE_FUSED_F32>(worlds, ft, mt, sm, grid, s);
+    return launch_fused_t<2, false, FSE_FUSED_F32>(worlds, ft, mt, sm, grid, s);
+}
+#elif defined(FSE_TICK_PAIR_TU)
 // chunks split over CTA pairs, Q16.16 amounts (FSE_TICK_PAIR_TU = 1) or f32 (2)
 #define FSE_PAIR_F32 (FSE_TICK_PAIR_TU == 2)
 #if FSE_TICK_PAIR_TU == 2
@@ -1840,7 +2005,7 @@ cudaError_t launch_colour_pass(const WorldDev *worlds, const uint32_t *items, in
 }  // namespace fse
 
 #if defined(FSE_PHASE_CLOCKS) && !defined(FSE_TICK_TEMP_TU) && !defined(FSE_TICK_SEQ_TU) && !defined(FSE_TICK_F32_TU) && \
-    !defined(FSE_TICK_PAIR_TU)
+    !defined(FSE_TICK_PAIR_TU) && !defined(FSE_TICK_FUSED_TU)
 extern "C" int fse_debug_phase_clocks(unsigned long long out[16], int reset) {
     cudaDeviceSynchronize();
     cudaMemcpyFromSymbol(out, g_phase_clk, 16 * sizeof(unsigned long long));

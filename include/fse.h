@@ -206,7 +206,10 @@ int fse_world_set_tick_zone(fse_world *world, int x, int y, int width, int heigh
 /* The launch shape of the world's colour pass (results never depend on it):
  * 0 one 1024-thread CTA per chunk, 1 one persistent CTA per SM walking the chunks,
  * 2 each chunk split over a pair of 512-thread CTAs (a thread-block cluster; the
- * partitioned order only), 3 persistent pairs. */
+ * partitioned order only), 3 persistent pairs, 4 the fused tick: every pass of a
+ * tick in one launch of one CTA per SM, each chunk-pass started as soon as the
+ * chunk-passes of its 3 x 3 chunk neighbourhood it depends on are done (the
+ * partitioned order only; worlds in the reference's order run shape 0). */
 int fse_world_set_launch(fse_world *world, int colour_shape);
 int fse_world_get_tile(fse_world *world, int x, int y, uint16_t *id, uint32_t *colour, int32_t *scalar,
                        uint8_t *flags);
@@ -430,8 +433,8 @@ int fse_batch_prepare_graphs(fse_batch *batch, int n_ticks, int graph_ticks);
 int fse_batch_autotune(fse_batch *batch, int32_t out_choice[4]);
 /* colour_ctas_per_sm: the colour pass's launch shape as in fse_world_set_launch
  * (0 one CTA per chunk, 1 one persistent CTA per SM, 2 a CTA pair per chunk,
- * 3 persistent pairs); particle_blocks: blocks per world of the particle kernels
- * (0 = enough for the largest particle list) */
+ * 3 persistent pairs, 4 the fused tick); particle_blocks: blocks per world of the
+ * particle kernels (0 = enough for the largest particle list) */
 int fse_batch_set_launch(fse_batch *batch, int colour_ctas_per_sm, int particle_blocks);
 int fse_batch_sync(fse_batch *batch);
 /* Time the batch's steps with CUDA events on its stream: every colour-pass launch
@@ -447,23 +450,55 @@ int fse_batch_timing(fse_batch *batch, int enable, double *out_pass_ms, int64_t 
 void *fse_batch_stream(fse_batch *batch);
 
 /* ---------------------------------------------------------------- serving */
+/* Continuous batching of world-tick requests (no analogue in the reference, which
+ * ticks one world per frame). Worlds are registered with the server and keep their
+ * state in HBM; the budget caps the device bytes of the resident worlds. A world
+ * that does not fit is parked in host memory as an exact checkpoint and restored
+ * when a request for it is admitted; restored worlds continue bit for bit. At most
+ * max_active requests (up to 4095) run at once. */
 int fse_server_create(int64_t hbm_budget_bytes, int max_active, fse_server **out);
 int fse_server_destroy(fse_server *srv);
-/* admit a world (allocates it if the HBM budget allows); *out_slot = world slot */
+/* register a world, generated by fse_world_generate(gen_kind, gen_seed); *out_slot
+ * = its slot. It is resident when it fits the budget after parking idle worlds
+ * without queued requests (least recently ticked first). FSE_E_BUDGET when it
+ * could never be resident (its footprint exceeds the budget) or no idle world can
+ * make room; FSE_E_INVAL for FSE_CFG_REFERENCE_ORDER, FSE_CFG_F32_FLUID or a chunk
+ * size other than the server's first world's. */
 int fse_server_add_world(fse_server *srv, int width, int height, const fse_config *cfg, int gen_kind,
                          uint32_t gen_seed, int *out_slot);
+/* unregister a world with no queued or active request (FSE_E_STATE otherwise) */
 int fse_server_remove_world(fse_server *srv, int slot);
+/* device bytes of the resident worlds */
 int64_t fse_server_bytes_in_use(const fse_server *srv);
+/* the world of a slot, restored into HBM first when parked (NULL when no idle world
+ * can make room). The pointer stays valid until a later server call parks the world:
+ * only worlds without queued or active requests are parked. */
 fse_world *fse_server_world(fse_server *srv, int slot);
-/* queue a request of n_ticks steps for a world; arrival_us is the caller's clock */
+/* queue a request of n_ticks steps (world::tick + world::tickCells each) for a
+ * world; arrival_us is the caller's clock */
 int fse_server_submit(fse_server *srv, int slot, int n_ticks, double arrival_us, int64_t *out_request);
-/* run one scheduling step: every active request advances one tick in one batched
- * launch sequence; requests that finish are reported by fse_server_poll */
+/* One scheduling step: retire finished steps; admit queued requests in arrival
+ * order (one request per world at a time; a parked world is restored when its
+ * footprint fits, parking idle worlds first); enqueue one batched tick of every
+ * active world on the server's stream and return without waiting, unless more
+ * than `depth` steps are then in flight (it waits for the oldest). With no active
+ * request it waits for every step in flight. *out_active = requests this step ticks. */
 int fse_server_step(fse_server *srv, int *out_active);
 /* microseconds since the server was created: the clock of arrivals and completions */
 double fse_server_now_us(const fse_server *srv);
-/* completed requests: ids and completion times (fse_server_now_us clock) */
+/* completed requests: ids and completion times, the device timestamp of the end of
+ * the step that ran their last tick, on the fse_server_now_us clock */
 int fse_server_poll(fse_server *srv, double now_us, int64_t *ids, double *done_us, int cap, int *out_n);
+/* steps in flight before fse_server_step waits (1..64, default 3) */
+int fse_server_set_depth(fse_server *srv, int depth);
+/* wait for every step in flight */
+int fse_server_drain(fse_server *srv);
+/* out[0..n-1] of: steps enqueued, worlds restored, worlds parked, resident worlds,
+ * parked worlds, most steps in flight, queued requests, active requests */
+int fse_server_stats(fse_server *srv, int64_t *out, int n);
+/* device milliseconds of each retired step (start to end event), oldest first;
+ * the values returned are consumed */
+int fse_server_tick_times(fse_server *srv, float *ms, int cap, int *out_n);
 
 #ifdef __cplusplus
 }

@@ -272,6 +272,58 @@ def test_serving_alone_equals_in_the_mix(fse):
     srv.close()
 
 
+def test_serving_parks_worlds_beyond_the_budget(fse):
+    """Four worlds under a budget that holds two: requests for parked worlds are
+    admitted by parking idle ones; every world ends as if ticked alone."""
+    sizes = [(256, 256), (384, 256), (256, 512), (320, 320)]
+    probe = fse.Server(8 << 30, max_active=4)
+    foot = []
+    for i, (w, h) in enumerate(sizes):
+        before = probe.bytes_in_use()
+        probe.add_world(w, h, fse.GEN_MIX, 700 + i, seed=700 + i)
+        foot.append(probe.bytes_in_use() - before)
+    probe.close()
+    budget = int(2.3 * max(foot))
+    srv = fse.Server(budget, max_active=2)
+    srv.set_depth(4)
+    slots = [srv.add_world(w, h, fse.GEN_MIX, 700 + i, seed=700 + i) for i, (w, h) in enumerate(sizes)]
+    assert srv.bytes_in_use() <= budget
+    assert srv.stats()["parked"] >= 1
+    reqs = [(0, 3), (2, 2), (1, 4), (3, 1), (0, 2), (3, 3), (2, 1), (1, 1), (0, 1)]
+    t_sub = {}
+    for k, n in reqs:
+        t_sub[srv.submit(slots[k], n)] = srv.now_us()
+    got = {}
+    for _ in range(400):
+        srv.step()
+        assert srv.bytes_in_use() <= budget
+        ids, t_done = srv.poll()
+        got.update(zip(ids.tolist(), t_done.tolist()))
+        if len(got) == len(reqs):
+            break
+    assert len(got) == len(reqs)
+    for rid, td in got.items():
+        assert td >= t_sub[rid] - 50.0  # device completion after the submit (clock anchor slack)
+    st = srv.stats()
+    assert st["restored"] >= 1 and st["parked_out"] >= 1
+    assert len(srv.tick_times()) == st["steps"]
+    ticks = [0] * len(sizes)
+    for k, n in reqs:
+        ticks[k] += n
+    for i, (w, h) in enumerate(sizes):
+        alone = fse.World(w, h, seed=700 + i)
+        alone.generate(fse.GEN_MIX, 700 + i)
+        alone.step(ticks[i])
+        served = srv.world(slots[i])
+        assert served is not None and srv.bytes_in_use() <= budget
+        sa, sm = alone.state(), served.state()
+        for key in sa:
+            np.testing.assert_array_equal(sa[key], sm[key], err_msg="world %d %s" % (i, key))
+        assert alone.particles().tobytes() == served.particles().tobytes()
+        assert alone.tick_count == served.tick_count
+    srv.close()
+
+
 def test_serving_admission_respects_the_budget(fse):
     srv = fse.Server(64 << 20, max_active=4)
     assert srv.try_add_world(256, 256) is not None
