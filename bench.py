@@ -754,7 +754,14 @@ def bench_config2(args, rank, local_rank, world_size):
 
     worlds = make()
     batch = fse.Batch(worlds)
-    choice = batch.autotune()
+    if args.launch_shape is not None:
+        # a fixed launch shape instead of the autotuner (profiling: under a profiler the
+        # candidates' timings are not those of the plain run)
+        batch.set_launch(args.launch_shape[0], args.launch_shape[1])
+        choice = {"colour_ctas_per_sm": args.launch_shape[0], "particle_blocks": args.launch_shape[1],
+                  "fixed": True}
+    else:
+        choice = batch.autotune()
     bstream = torch.cuda.ExternalStream(batch.stream)
     batch.step(args.warmup)
     batch.timing(True)
@@ -1350,6 +1357,8 @@ def main():
                     help="batch workload: time the batched steps only (no per-world arm, digests, e2e or CPU legs)")
     ap.add_argument("--no-config1", action="store_true",
                     help="batch workload: skip the 4096x2048 single-world line reported beside it")
+    ap.add_argument("--launch-shape", type=int, nargs=2, default=None, metavar=("COLOUR", "PARTICLE_BLOCKS"),
+                    help="config 2: this batch launch shape instead of the autotuner's choice (for profiling)")
     ap.add_argument("--only", default=None, choices=["render", "temperature", "pack", "reference_order"],
                     help="run only one side measurement of the 4096x2048 workload (for profiling), print its dict")
     args = ap.parse_args()

@@ -855,7 +855,7 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
     int ncp = h.cell_iter * 4 * h.max_slots * h.cp_rows + 1;
     bool ok = dalloc(w, &h.id, n) && dalloc(w, &h.col, n) && dalloc(w, &h.sc, n) && dalloc(w, &h.fl, n) &&
               dalloc(w, &h.df, n) && dalloc(w, &h.stage, (size_t)h.stage_cap) && dalloc(w, &h.cp_count, ncp) &&
-              dalloc(w, &h.cp_base, ncp) && dalloc(w, &w->ctr, 16) && dalloc(w, &h.ledger, LED_ROWS * MAXMAT) &&
+              dalloc(w, &h.cp_base, ncp) && dalloc(w, &w->ctr, 24) && dalloc(w, &h.ledger, LED_ROWS * MAXMAT) &&
               dalloc(w, &h.p_state, (size_t)h.part_cap) && dalloc(w, &h.p_box0, (size_t)h.part_cap) &&
               dalloc(w, &h.p_box1, (size_t)h.part_cap) && dalloc(w, &h.p_cell, (size_t)h.part_cap) &&
               dalloc(w, &h.p_prev, (size_t)h.part_cap) && dalloc(w, &h.scan_tmp, particle_scan_blocks() + 1) &&
@@ -910,7 +910,8 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
     h.bar = (unsigned *)(w->ctr + 8);  // [8] arrivals, [9] generation
     h.stats = w->ctr + 10;             // [10] iterations of the last particle update
     h.sched = (uint32_t *)(w->ctr + 12);  // [12] next ticket, [13] CTAs finished, [14] a wait gave up (fused tick)
-    cudaMemset(w->ctr, 0, 16 * sizeof(int32_t));
+    h.chg_n = w->ctr + 16;                // [16..17] fill changes per iteration parity (particle update)
+    cudaMemset(w->ctr, 0, 24 * sizeof(int32_t));
     cudaMemset(h.cdone, 0, (size_t)h.nCx * h.nCy * sizeof(uint32_t));
     cudaMemset(h.ledger, 0, LED_ROWS * MAXMAT * sizeof(long long));
     cudaMemset(h.cp_count, 0, ncp * sizeof(int32_t));

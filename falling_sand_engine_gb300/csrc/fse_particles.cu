@@ -394,11 +394,12 @@ __device__ __forceinline__ void grid_sync(GridBar *gb, unsigned nblocks, int32_t
 
 constexpr int SERIAL_MAX_ITER = 1 << 16;
 constexpr int SERIAL_MAX_WORLDS = 4096;  // worlds of one launch (a batch holds at most 4095)
+constexpr int SERIAL_THREADS = 256;
 
-// particle g of the launch's worlds taken together: its world (s_pref: prefix sums of
-// the worlds' particle counts, in shared memory) and index in that world
-__device__ __forceinline__ int world_of(const int *s_pref, int n_worlds, int g) {
-    int lo = 0, hi = n_worlds - 1;
+// index g of a flattened index space: its entry in s_pref (prefix sums over the
+// entries, in shared memory)
+__device__ __forceinline__ int entry_of(const int *s_pref, int n, int g) {
+    int lo = 0, hi = n - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
         if (s_pref[mid] <= g)
@@ -409,17 +410,81 @@ __device__ __forceinline__ int world_of(const int *s_pref, int n_worlds, int g) 
     return lo;
 }
 
+// exclusive scan of one value per thread over the block (SERIAL_THREADS threads)
+__device__ __forceinline__ int block_excl_sum(int v, int *s_warp, int *total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int inc = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) s_warp[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        int x = lane < SERIAL_THREADS / 32 ? s_warp[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += t;
+        }
+        if (lane < SERIAL_THREADS / 32) s_warp[lane] = x;
+    }
+    __syncthreads();
+    const int ex = (wid > 0 ? s_warp[wid - 1] : 0) + inc - v;
+    *total = s_warp[SERIAL_THREADS / 32 - 1];
+    __syncthreads();
+    return ex;
+}
+
+// The worlds with a non-zero count(k), as a flattened index space in shared memory:
+// s_ids[j] the j-th such world, s_apref[j] the index its entries start at,
+// s_apref[n_act] the total. Every thread of the block calls it; returns n_act.
+template <class F>
+__device__ int active_worlds(int n_worlds, F count, int *s_ids, int *s_apref, int *s_warp) {
+    const int seg = (n_worlds + SERIAL_THREADS - 1) / SERIAL_THREADS;
+    const int k0 = min((int)threadIdx.x * seg, n_worlds), k1 = min(k0 + seg, n_worlds);
+    int sum = 0, nact = 0;
+    for (int k = k0; k < k1; k++) {
+        const int c = count(k);
+        sum += c;
+        nact += c > 0;
+    }
+    int tot_sum, tot_act;
+    int at = block_excl_sum(sum, s_warp, &tot_sum);
+    int j = block_excl_sum(nact, s_warp, &tot_act);
+    for (int k = k0; k < k1; k++) {
+        const int c = count(k);
+        if (c > 0) {
+            s_ids[j] = k;
+            s_apref[j] = at;
+            j++;
+            at += c;
+        }
+    }
+    if (threadIdx.x == 0) s_apref[tot_act] = tot_sum;
+    __syncthreads();
+    return tot_act;
+}
+
 // The fixed-point iteration and the commit for every world of the table, in one
-// cooperative launch (every block resident, so the grid barrier is safe). The
-// particles of all worlds are taken as one index space. Change marks are per 8x8
-// block the lowest index whose fill moved into or out of the block: a particle is
-// computed again only if a lower index changed a fill near what it read.
-// req_count[0..1] of world 0 count the fill changes of even and odd iterations;
-// stats[0] of world 0 receives the number of iterations.
-__global__ void __launch_bounds__(256) k_part_serial(const WorldDev *__restrict__ worlds, int n_worlds,
-                                                      const MatTable *__restrict__ mt) {
+// cooperative launch (every block resident, so the grid barrier is safe). Change
+// marks are per 8x8 block the lowest index whose fill moved into or out of the
+// block: a particle is computed again only if a lower index changed a fill near
+// what it read. Iteration work is restricted to the worlds that need it: a world
+// whose fills did not change in an iteration has converged (its particles read
+// only its own cells), so later iterations skip its particles, and the fills that
+// changed are listed per world (chg_n[parity] of them, their indices in the first
+// part_cap entries of merge_list, free until the commit) so that clearing their
+// records does not scan the particles. req_count[0..1] of world 0 count every
+// world's fill changes of even and odd iterations; stats[0] of world 0 receives
+// the number of iterations. Dynamic shared memory: 3 * n_worlds + 2 ints.
+__global__ void __launch_bounds__(SERIAL_THREADS) k_part_serial(const WorldDev *__restrict__ worlds, int n_worlds,
+                                                                 const MatTable *__restrict__ mt) {
     __shared__ uint8_t s_type[MAXMAT];
-    __shared__ int s_pref[SERIAL_MAX_WORLDS + 1];
+    __shared__ int s_warp[SERIAL_THREADS / 32];
+    extern __shared__ int s_dyn[];
+    int *s_pref = s_dyn;                       // [n_worlds + 1] particles before world k
+    int *s_apref = s_dyn + n_worlds + 1;       // [n_worlds + 1] the active index space
+    int *s_ids = s_dyn + 2 * (n_worlds + 1);   // [n_worlds]
     load_types(s_type, mt);
     for (int k = threadIdx.x; k < n_worlds; k += blockDim.x) s_pref[k + 1] = *worlds[k].part_count;
     __syncthreads();
@@ -429,6 +494,7 @@ __global__ void __launch_bounds__(256) k_part_serial(const WorldDev *__restrict_
     }
     __syncthreads();
     const int total = s_pref[n_worlds];
+    auto parts = [&](int k) { return s_pref[k + 1] - s_pref[k]; };
     GridBar *gb = (GridBar *)worlds[0].bar;
     const unsigned nb = gridDim.x;
     int32_t *err = worlds[0].err;
@@ -443,16 +509,24 @@ __global__ void __launch_bounds__(256) k_part_serial(const WorldDev *__restrict_
         }
         const int par = it & 1;
         // A: outcomes of the particles whose box saw a fill change by a lower index (all
-        // at first); changed fills are counted and their blocks marked for the next
+        // at first; later only in worlds whose fills changed in the last iteration);
+        // changed fills are counted, listed and their blocks marked for the next
         // iteration with the changing index. A thread takes particle g, its warp walks
         // the spirals of the warp's particles together.
-        for (int gb0 = gtid - lane; gb0 < total; gb0 += gstride) {
+        const int n_act = it == 0 ? active_worlds(n_worlds, parts, s_ids, s_apref, s_warp)
+                                  : active_worlds(
+                                        n_worlds,
+                                        [&](int k) { return __ldcg(&worlds[k].chg_n[1 - par]) > 0 ? parts(k) : 0; },
+                                        s_ids, s_apref, s_warp);
+        const int total_a = s_apref[n_act];
+        for (int gb0 = gtid - lane; gb0 < total_a; gb0 += gstride) {
             const int g = gb0 + lane;
-            bool work = g < total, spiral = false;
+            bool work = g < total_a, spiral = false;
             int wi = 0, i = 0, before = -1;
             if (work) {
-                wi = world_of(s_pref, n_worlds, g);
-                i = g - s_pref[wi];
+                const int j = entry_of(s_apref, n_act, g);
+                wi = s_ids[j];
+                i = g - s_apref[j];
                 const WorldDev &w = worlds[wi];
                 if (it > 0) {
                     const int32_t b0 = w.p_box0[i];
@@ -516,56 +590,71 @@ __global__ void __launch_bounds__(256) k_part_serial(const WorldDev *__restrict_
             }
             if (work) {
                 const WorldDev &w = worlds[wi];
-                const int nblk = w.amw * w.amh;
-                uint32_t *mark = w.chg + (size_t)(1 - par) * nblk;
                 const int after = fill_of(w, i);
                 if (after != before) {
+                    const int nblk = w.amw * w.amh;
+                    uint32_t *mark = w.chg + (size_t)(1 - par) * nblk;
                     atomicAdd(&cnt[par], 1);
+                    w.merge_list[atomicAdd(&w.chg_n[par], 1)] = i;  // at most once per particle
                     if (before >= 0)
                         atomicMin(&mark[(before / w.W >> 3) * w.amw + ((before % w.W) >> 3)], (uint32_t)i);
                     if (after >= 0) atomicMin(&mark[(after / w.W >> 3) * w.amw + ((after % w.W) >> 3)], (uint32_t)i);
                     w.p_prev[i] = before;  // the cell whose record B1 clears
-                } else {
-                    w.p_prev[i] = -1;
                 }
             }
         }
         grid_sync(gb, nb, err);
         const int changed = __ldcg(&cnt[par]);
         if (changed == 0) break;
-        // B1: clear the records of fills that moved away and the marks read in A
-        for (int g = gtid; g < total; g += gstride) {
-            const int wi = world_of(s_pref, n_worlds, g);
-            const WorldDev &w = worlds[wi];
-            const int i = g - s_pref[wi];
-            const int c = w.p_prev[i];
-            if (c >= 0) {
-                w.df[c] = 0;
-                w.p_prev[i] = -1;
+        // B1: clear the records of the fills that moved away (the listed particles of
+        // this iteration), and the marks A read (set by the last iteration's changes)
+        {
+            const int na = active_worlds(
+                n_worlds, [&](int k) { return __ldcg(&worlds[k].chg_n[par]); }, s_ids, s_apref, s_warp);
+            for (int g = gtid; g < s_apref[na]; g += gstride) {
+                const int j = entry_of(s_apref, na, g);
+                const WorldDev &w = worlds[s_ids[j]];
+                const int i = w.merge_list[g - s_apref[j]];
+                const int c = w.p_prev[i];
+                if (c >= 0) w.df[c] = 0;
             }
         }
-        for (int wi = 0; wi < n_worlds; wi++) {
-            const WorldDev &w = worlds[wi];
-            if (s_pref[wi + 1] == s_pref[wi]) continue;
-            const int nblk = w.amw * w.amh;
-            uint32_t *seen = w.chg + (size_t)par * nblk;
-            for (int b = gtid; b < nblk; b += gstride) seen[b] = 0xFFFFFFFFu;
+        if (it > 0) {
+            const int nm = active_worlds(
+                n_worlds,
+                [&](int k) {
+                    const WorldDev &w = worlds[k];
+                    return __ldcg(&w.chg_n[1 - par]) > 0 ? w.amw * w.amh : 0;
+                },
+                s_ids, s_apref, s_warp);
+            for (int g = gtid; g < s_apref[nm]; g += gstride) {
+                const int j = entry_of(s_apref, nm, g);
+                const WorldDev &w = worlds[s_ids[j]];
+                w.chg[(size_t)par * w.amw * w.amh + (g - s_apref[j])] = 0xFFFFFFFFu;
+            }
         }
         if (gtid == 0) cnt[1 - par] = 0;
         grid_sync(gb, nb, err);
-        // B2: every current fill records itself; the lowest index stays
-        for (int g = gtid; g < total; g += gstride) {
-            const int wi = world_of(s_pref, n_worlds, g);
-            const WorldDev &w = worlds[wi];
-            const int i = g - s_pref[wi];
-            const int c = fill_of(w, i);
-            if (c >= 0) atomicMax(&w.df[c], fill_code(i));
+        // B2: every current fill of the worlds that changed records itself; the lowest
+        // index stays. The last iteration's counts have been used: cleared for the next.
+        {
+            const int na = active_worlds(
+                n_worlds, [&](int k) { return __ldcg(&worlds[k].chg_n[par]) > 0 ? parts(k) : 0; }, s_ids,
+                s_apref, s_warp);
+            for (int g = gtid; g < s_apref[na]; g += gstride) {
+                const int j = entry_of(s_apref, na, g);
+                const WorldDev &w = worlds[s_ids[j]];
+                const int i = g - s_apref[j];
+                const int c = fill_of(w, i);
+                if (c >= 0) atomicMax(&w.df[c], fill_code(i));
+            }
+            for (int k = gtid; k < n_worlds; k += gstride) worlds[k].chg_n[1 - par] = 0;
         }
         grid_sync(gb, nb, err);
     }
     // the sequential outcome: commit it
     for (int g = gtid; g < total; g += gstride) {
-        const int wi = world_of(s_pref, n_worlds, g);
+        const int wi = entry_of(s_pref, n_worlds, g);
         const WorldDev &w = worlds[wi];
         const int i = g - s_pref[wi];
         const uint8_t k = w.p_state[i];
@@ -600,15 +689,22 @@ __global__ void __launch_bounds__(256) k_part_serial(const WorldDev *__restrict_
             w.p_state[i] = PS_ALIVE;
         }
     }
-    // the marks of the last iteration are cleared for the next update
-    {
+    // the marks A of the last iteration read (set by the changes of the one before)
+    // are cleared for the next update; the last iteration changed nothing, so it
+    // set none. The per-world counts are cleared by k_part_end.
+    if (it > 0 && it < SERIAL_MAX_ITER) {
         const int par = it & 1;
-        for (int wi = 0; wi < n_worlds; wi++) {
-            const WorldDev &w = worlds[wi];
-            if (s_pref[wi + 1] == s_pref[wi]) continue;
-            const int nblk = w.amw * w.amh;
-            uint32_t *mark = w.chg + (size_t)(1 - par) * nblk;
-            for (int b = gtid; b < nblk; b += gstride) mark[b] = 0xFFFFFFFFu;
+        const int nm = active_worlds(
+            n_worlds,
+            [&](int k) {
+                const WorldDev &w = worlds[k];
+                return __ldcg(&w.chg_n[1 - par]) > 0 ? w.amw * w.amh : 0;
+            },
+            s_ids, s_apref, s_warp);
+        for (int g = gtid; g < s_apref[nm]; g += gstride) {
+            const int j = entry_of(s_apref, nm, g);
+            const WorldDev &w = worlds[s_ids[j]];
+            w.chg[(size_t)par * w.amw * w.amh + (g - s_apref[j])] = 0xFFFFFFFFu;
         }
     }
     if (gtid == 0) {
@@ -803,6 +899,8 @@ __global__ void k_part_end(const WorldDev *worlds, int nblocks) {
         w.req_count[0] = 0;
         w.req_count[1] = 0;
         w.req_count[2] = 0;
+        w.chg_n[0] = 0;
+        w.chg_n[1] = 0;
     }
 }
 
@@ -858,20 +956,28 @@ cudaError_t launch_particle_tick(WorldDev *d_worlds, int n_worlds, const MatTabl
     dim3 gm(move_blocks, n_worlds);
     k_air_map<<<gm, 256, 0, s>>>(d_worlds, mt);
     {
-        // every block of a cooperative launch is resident, so the grid barrier is safe
-        static int coop_blocks = 0;
-        if (!coop_blocks) {
-            int per_sm = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_part_serial, 256, 0);
-            int dev = 0, nsm = 1;
+        // every block of a cooperative launch is resident, so the grid barrier is safe;
+        // the blocks per SM depend on the shared memory the table's size asks for
+        if (n_worlds > SERIAL_MAX_WORLDS) return cudaErrorInvalidValue;
+        const size_t dyn = (size_t)(3 * n_worlds + 2) * sizeof(int);
+        static size_t dyn_set = 0;
+        if (dyn > 48 * 1024 && dyn > dyn_set) {
+            cudaFuncSetAttribute(k_part_serial, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+            dyn_set = dyn;
+        }
+        static int nsm = 0;
+        if (!nsm) {
+            int dev = 0;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-            coop_blocks = std::max(1, std::min(per_sm, 4) * nsm);
         }
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_part_serial, SERIAL_THREADS, dyn);
+        const int coop_blocks = std::max(1, std::min(per_sm, 4) * nsm);
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(coop_blocks);
-        cfg.blockDim = dim3(256);
-        cfg.dynamicSmemBytes = 0;
+        cfg.blockDim = dim3(SERIAL_THREADS);
+        cfg.dynamicSmemBytes = dyn;
         cfg.stream = s;
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeCooperative;
