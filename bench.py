@@ -795,8 +795,7 @@ def bench_config2(args, rank, local_rank, world_size):
     # end to end through the C ABI with host buffers: every step uploads each
     # world's planes from pinned host memory, runs one batched step and reads the
     # planes back
-    e2e = e2e_worlds(worlds, lambda: batch.step(1), torch, cells, world_size,
-                     "fse_world_upload (every world) + fse_batch_step + fse_world_download (every world)")
+    e2e = e2e_batch(batch, worlds, torch, cells, world_size)
     batch.close()
     for w in worlds:
         w.close()
@@ -893,6 +892,40 @@ def e2e_worlds(worlds, step, torch, cells, world_size, path, steps=3):
     dt = max_over_ranks(time.perf_counter() - t0, world_size)
     return {"value": round(world_size * cells * steps / dt / 1e9, 4), "unit": "Gcell/s",
             "h2d_bytes_per_step": int(bi), "d2h_bytes_per_step": int(bi), "steps": steps, "path": path}
+
+
+def e2e_batch(batch, worlds, torch, cells, world_size, steps=3):
+    """The batched metric end to end through the C ABI: every step enqueues the upload
+    of each world's planes from pinned host memory (fse_batch_upload), one batched
+    step and the download of every plane (fse_batch_download) on the batch's stream,
+    then waits once (fse_batch_sync)."""
+    pinned = []
+    for w in worlds:
+        st = w.state()
+        host = {}
+        for k, v in st.items():
+            t = torch.empty(v.size, dtype={np.uint16: torch.int16, np.uint32: torch.int32, np.int32: torch.int32,
+                                           np.uint8: torch.uint8}[v.dtype.type], pin_memory=True)
+            a = t.numpy().view(v.dtype).reshape(v.shape)
+            a[...] = v
+            host[k] = (t, a)
+        pinned.append({k: a for k, (t, a) in host.items()})
+        pinned[-1]["_keep"] = host
+    bi = sum(a.nbytes for host in pinned for k, a in host.items() if k != "_keep")
+    batch.sync()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for k, host in enumerate(pinned):
+            batch.upload(k, host)
+        batch.step(1)
+        for k, host in enumerate(pinned):
+            batch.download(k, host)
+        batch.sync()
+    dt = max_over_ranks(time.perf_counter() - t0, world_size)
+    return {"value": round(world_size * cells * steps / dt / 1e9, 4), "unit": "Gcell/s",
+            "h2d_bytes_per_step": int(bi), "d2h_bytes_per_step": int(bi), "steps": steps,
+            "path": "fse_batch_upload (every world, pinned host planes) + fse_batch_step + fse_batch_download "
+                    "(every world) on the batch's stream, one fse_batch_sync per step"}
 
 
 def reference_timing_worlds(sizes, sample, steps, warm, budget_s):

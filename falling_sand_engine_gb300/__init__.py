@@ -496,6 +496,32 @@ class Batch:
     def set_launch(self, colour_ctas_per_sm, particle_blocks):
         check(self.lib.fse_batch_set_launch(self.h, colour_ctas_per_sm, particle_blocks), "batch_set_launch")
 
+    def upload(self, index, planes):
+        """Enqueue an upload of member `index`'s planes (host arrays, pinned for the copy
+        to run asynchronously; keep them alive until sync()) on the batch's stream."""
+        w = self.worlds[index]
+        n = w.width * w.height
+        arrs = []
+        for k, dt in World.PLANES:
+            a = planes.get(k)
+            if a is not None and (a.dtype != dt or a.size != n or not a.flags["C_CONTIGUOUS"]):
+                raise ValueError("plane %s must be a C-contiguous %s array of %d cells" % (k, np.dtype(dt), n))
+            arrs.append(a)
+        check(self.lib.fse_batch_upload(self.h, index, *[ptr(a) if a is not None else None for a in arrs]),
+              "batch_upload")
+
+    def download(self, index, out):
+        """Enqueue a download of member `index`'s planes into the host arrays of `out`
+        (filled after sync())."""
+        w = self.worlds[index]
+        n = w.width * w.height
+        for k, dt in World.PLANES:
+            a = out[k]
+            if a.dtype != dt or a.size != n or not a.flags["C_CONTIGUOUS"]:
+                raise ValueError("plane %s must be a C-contiguous %s array of %d cells" % (k, np.dtype(dt), n))
+        check(self.lib.fse_batch_download(self.h, index, *[ptr(out[k]) for k, _ in World.PLANES]),
+              "batch_download")
+
     def sync(self):
         check(self.lib.fse_batch_sync(self.h), "batch_sync")
 

@@ -1029,49 +1029,72 @@ __global__ void k_mask_flags(uint8_t *fl, size_t n) {
 }
 
 // uploaded material ids must index the table: out-of-range ids become GENERIC_AIR
-// and the upload reports FSE_E_INVAL
+// and the upload reports FSE_E_INVAL (*bad |= 1)
 __global__ void k_check_ids(uint16_t *id, size_t n, int nmat, int air, int *bad) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
         if (id[i] >= nmat) {
             id[i] = (uint16_t)air;
-            *bad = 1;
+            atomicOr(bad, 1);
         }
 }
+
+}  // extern "C"
+
+namespace fse {
+
+// the copies and checks of an upload, enqueued on s; out-of-range ids set *bad
+int world_upload_async(fse_world *w, const uint16_t *id, const uint32_t *col, const int32_t *sc, const uint8_t *fl,
+                       const int32_t *df, cudaStream_t s, int *bad) {
+    size_t n = (size_t)w->W * w->H;
+    const MatTable &t = host_table();
+    if (id) FSE_CUDA_TRY(cudaMemcpyAsync(w->h.id, id, n * 2, cudaMemcpyHostToDevice, s));
+    if (col) FSE_CUDA_TRY(cudaMemcpyAsync(w->h.col, col, n * 4, cudaMemcpyHostToDevice, s));
+    if (sc) FSE_CUDA_TRY(cudaMemcpyAsync(w->h.sc, sc, n * 4, cudaMemcpyHostToDevice, s));
+    if (fl) {
+        FSE_CUDA_TRY(cudaMemcpyAsync(w->h.fl, fl, n, cudaMemcpyHostToDevice, s));
+        // bit 6 of the flags is reserved for the kernel's visited mark
+        k_mask_flags<<<std::max(1, std::min<int>((int)(n / 1024) + 1, 4096)), 256, 0, s>>>(w->h.fl, n);
+    }
+    if (df) FSE_CUDA_TRY(cudaMemcpyAsync(w->h.df, df, n * 4, cudaMemcpyHostToDevice, s));
+    if (id) {
+        int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)sm_count() * 8);
+        k_check_ids<<<std::max(blocks, 1), 256, 0, s>>>(w->h.id, n, t.n, t.id_air, bad);
+    }
+    if (w->h.dirty) FSE_CUDA_TRY(cudaMemsetAsync(w->h.dirty, 1, n, s));  // repaint everything
+    return cudaGetLastError() == cudaSuccess ? FSE_OK : FSE_E_CUDA;
+}
+
+int world_download_async(fse_world *w, uint16_t *id, uint32_t *col, int32_t *sc, uint8_t *fl, int32_t *df,
+                         cudaStream_t s) {
+    size_t n = (size_t)w->W * w->H;
+    if (id) FSE_CUDA_TRY(cudaMemcpyAsync(id, w->h.id, n * 2, cudaMemcpyDeviceToHost, s));
+    if (col) FSE_CUDA_TRY(cudaMemcpyAsync(col, w->h.col, n * 4, cudaMemcpyDeviceToHost, s));
+    if (sc) FSE_CUDA_TRY(cudaMemcpyAsync(sc, w->h.sc, n * 4, cudaMemcpyDeviceToHost, s));
+    if (fl) FSE_CUDA_TRY(cudaMemcpyAsync(fl, w->h.fl, n, cudaMemcpyDeviceToHost, s));
+    if (df) FSE_CUDA_TRY(cudaMemcpyAsync(df, w->h.df, n * 4, cudaMemcpyDeviceToHost, s));
+    return FSE_OK;
+}
+
+}  // namespace fse
+
+extern "C" {
 
 int fse_world_upload(fse_world *w, const uint16_t *id, const uint32_t *col, const int32_t *sc, const uint8_t *fl,
                      const int32_t *df) {
     if (!w) return FSE_E_INVAL;
-    size_t n = (size_t)w->W * w->H;
-    const MatTable &t = host_table();
-    if (id) FSE_CUDA_TRY(cudaMemcpyAsync(w->h.id, id, n * 2, cudaMemcpyHostToDevice, w->stream));
-    if (col) FSE_CUDA_TRY(cudaMemcpyAsync(w->h.col, col, n * 4, cudaMemcpyHostToDevice, w->stream));
-    if (sc) FSE_CUDA_TRY(cudaMemcpyAsync(w->h.sc, sc, n * 4, cudaMemcpyHostToDevice, w->stream));
-    if (fl) {
-        FSE_CUDA_TRY(cudaMemcpyAsync(w->h.fl, fl, n, cudaMemcpyHostToDevice, w->stream));
-        // bit 6 of the flags is reserved for the kernel's visited mark
-        k_mask_flags<<<std::max(1, std::min<int>((int)(n / 1024) + 1, 4096)), 256, 0, w->stream>>>(w->h.fl, n);
-    }
-    if (df) FSE_CUDA_TRY(cudaMemcpyAsync(w->h.df, df, n * 4, cudaMemcpyHostToDevice, w->stream));
     int bad = 0;
-    if (id) {
-        int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)sm_count() * 8);
-        FSE_CUDA_TRY(cudaMemsetAsync(w->ctr + 7, 0, 4, w->stream));
-        k_check_ids<<<std::max(blocks, 1), 256, 0, w->stream>>>(w->h.id, n, t.n, t.id_air, w->ctr + 7);
-        FSE_CUDA_TRY(cudaMemcpyAsync(&bad, w->ctr + 7, 4, cudaMemcpyDeviceToHost, w->stream));
-    }
-    if (w->h.dirty) FSE_CUDA_TRY(cudaMemsetAsync(w->h.dirty, 1, n, w->stream));  // repaint everything
+    FSE_CUDA_TRY(cudaMemsetAsync(w->ctr + 7, 0, 4, w->stream));
+    int rc = world_upload_async(w, id, col, sc, fl, df, w->stream, w->ctr + 7);
+    if (rc) return rc;
+    if (id) FSE_CUDA_TRY(cudaMemcpyAsync(&bad, w->ctr + 7, 4, cudaMemcpyDeviceToHost, w->stream));
     FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
     return bad ? FSE_E_INVAL : FSE_OK;
 }
 
 int fse_world_download(fse_world *w, uint16_t *id, uint32_t *col, int32_t *sc, uint8_t *fl, int32_t *df) {
     if (!w) return FSE_E_INVAL;
-    size_t n = (size_t)w->W * w->H;
-    if (id) FSE_CUDA_TRY(cudaMemcpyAsync(id, w->h.id, n * 2, cudaMemcpyDeviceToHost, w->stream));
-    if (col) FSE_CUDA_TRY(cudaMemcpyAsync(col, w->h.col, n * 4, cudaMemcpyDeviceToHost, w->stream));
-    if (sc) FSE_CUDA_TRY(cudaMemcpyAsync(sc, w->h.sc, n * 4, cudaMemcpyDeviceToHost, w->stream));
-    if (fl) FSE_CUDA_TRY(cudaMemcpyAsync(fl, w->h.fl, n, cudaMemcpyDeviceToHost, w->stream));
-    if (df) FSE_CUDA_TRY(cudaMemcpyAsync(df, w->h.df, n * 4, cudaMemcpyDeviceToHost, w->stream));
+    int rc = world_download_async(w, id, col, sc, fl, df, w->stream);
+    if (rc) return rc;
     FSE_CUDA_TRY(cudaStreamSynchronize(w->stream));
     return FSE_OK;
 }
@@ -1203,7 +1226,12 @@ int fse_world_sync(fse_world *w) {
     int rc = read_ctr(w, c);
     if (rc) return rc;
     if (cudaGetLastError() != cudaSuccess) return FSE_E_CUDA;
-    return status_from_err(c[5]);
+    rc = status_from_err(c[5]);
+    if (c[15]) {  // an asynchronous upload (fse_batch_upload) replaced out-of-range ids
+        FSE_CUDA_TRY(cudaMemset(w->ctr + 15, 0, 4));
+        if (!rc) rc = FSE_E_INVAL;
+    }
+    return rc;
 }
 
 int fse_world_tick(fse_world *w, int n) {

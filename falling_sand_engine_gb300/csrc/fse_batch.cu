@@ -427,4 +427,16 @@ int fse_batch_sync(fse_batch *b) {
 
 void *fse_batch_stream(fse_batch *b) { return b ? (void *)b->stream : nullptr; }
 
+int fse_batch_upload(fse_batch *b, int index, const uint16_t *id, const uint32_t *col, const int32_t *sc,
+                     const uint8_t *fl, const int32_t *df) {
+    if (!b || index < 0 || index >= (int)b->worlds.size()) return FSE_E_INVAL;
+    fse_world *w = b->worlds[index];
+    return world_upload_async(w, id, col, sc, fl, df, b->stream, w->ctr + 15);
+}
+
+int fse_batch_download(fse_batch *b, int index, uint16_t *id, uint32_t *col, int32_t *sc, uint8_t *fl, int32_t *df) {
+    if (!b || index < 0 || index >= (int)b->worlds.size()) return FSE_E_INVAL;
+    return world_download_async(b->worlds[index], id, col, sc, fl, df, b->stream);
+}
+
 }  // extern "C"

@@ -121,6 +121,12 @@ int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], con
                  PassTimer *timer = nullptr, int temp_tiles = 0, bool temp_track = false, bool seq = false,
                  bool f32 = false);
 void count_launches(long long n);
+// a world's plane upload (copies, flag masking, id check into *bad, repaint) and
+// download, enqueued on stream s without waiting
+int world_upload_async(fse_world *w, const uint16_t *id, const uint32_t *col, const int32_t *sc, const uint8_t *fl,
+                       const int32_t *df, cudaStream_t s, int *bad);
+int world_download_async(fse_world *w, uint16_t *id, uint32_t *col, int32_t *sc, uint8_t *fl, int32_t *df,
+                         cudaStream_t s);
 // the most temperature tiles of the worlds that run the temperature step (0: none)
 int temp_tiles_of(const std::vector<fse_world *> &ws);
 // some world keeps liquid temperatures: the colour pass that copies them runs

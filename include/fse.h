@@ -448,6 +448,16 @@ int fse_batch_timing(fse_batch *batch, int enable, double *out_pass_ms, int64_t 
                      int cap, int *out_ticks);
 /* the CUDA stream (cudaStream_t) the batch enqueues its work on */
 void *fse_batch_stream(fse_batch *batch);
+/* Plane I/O of member `index` enqueued on the batch's stream, in order with its
+ * steps, without waiting (host buffers should be pinned for the copies to run
+ * asynchronously; the member's own stream must be idle). Upload: the planes given
+ * (NULL keeps a plane), as fse_world_upload; an out-of-range id becomes GENERIC_AIR
+ * and the next fse_batch_sync returns FSE_E_INVAL. Download: as fse_world_download;
+ * the host buffers hold the planes after the next fse_batch_sync. */
+int fse_batch_upload(fse_batch *batch, int index, const uint16_t *id, const uint32_t *colour, const int32_t *scalar,
+                     const uint8_t *flags, const int32_t *diff);
+int fse_batch_download(fse_batch *batch, int index, uint16_t *id, uint32_t *colour, int32_t *scalar, uint8_t *flags,
+                       int32_t *diff);
 
 /* ---------------------------------------------------------------- serving */
 /* Continuous batching of world-tick requests (no analogue in the reference, which

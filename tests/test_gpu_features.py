@@ -272,6 +272,45 @@ def test_serving_alone_equals_in_the_mix(fse):
     srv.close()
 
 
+def test_batch_async_plane_io(fse):
+    """fse_batch_upload / fse_batch_download on the batch's stream: a round trip of
+    planes between steps equals the world API; an out-of-range id becomes AIR and
+    the next sync reports it once."""
+    sizes = [(256, 200), (384, 256)]
+    worlds = [fse.World(w, h, seed=60 + i) for i, (w, h) in enumerate(sizes)]
+    twins = [fse.World(w, h, seed=60 + i) for i, (w, h) in enumerate(sizes)]
+    for i, (a, b) in enumerate(zip(worlds, twins)):
+        a.generate(fse.GEN_MIX, 60 + i)
+        b.generate(fse.GEN_MIX, 60 + i)
+    batch = fse.Batch(worlds)
+    host = [w.state() for w in twins]
+    for k, st in enumerate(host):
+        st["id"][:8, :8] = fse.material_find("WATER")
+        batch.upload(k, st)
+        twins[k].upload(st)
+    batch.step(2)
+    out = [{k: np.empty_like(v) for k, v in st.items()} for st in host]
+    for k in range(len(worlds)):
+        batch.download(k, out[k])
+    batch.sync()
+    for k, tw in enumerate(twins):
+        tw.step(2)
+        ref = tw.state()
+        for key in ref:
+            np.testing.assert_array_equal(out[k][key], ref[key], err_msg="world %d %s" % (k, key))
+    bad = dict(out[0])
+    bad["id"] = bad["id"].copy()
+    bad["id"][0, 0] = 999
+    batch.upload(0, bad)
+    with pytest.raises(fse.FseError):
+        batch.sync()
+    assert worlds[0].state()["id"][0, 0] == fse.material_find("GENERIC_AIR")
+    batch.sync()  # reported once
+    batch.close()
+    for w in worlds + twins:
+        w.close()
+
+
 def test_serving_parks_worlds_beyond_the_budget(fse):
     """Four worlds under a budget that holds two: requests for parked worlds are
     admitted by parking idle ones; every world ends as if ticked alone."""
