@@ -895,37 +895,30 @@ def e2e_worlds(worlds, step, torch, cells, world_size, path, steps=3):
 
 
 def e2e_batch(batch, worlds, torch, cells, world_size, steps=3):
-    """The batched metric end to end through the C ABI: every step enqueues the upload
-    of each world's planes from pinned host memory (fse_batch_upload), one batched
-    step and the download of every plane (fse_batch_download) on the batch's stream,
-    then waits once (fse_batch_sync)."""
-    pinned = []
-    for w in worlds:
+    """The batched metric end to end through the C ABI: every step copies every
+    world's planes from one pinned host buffer (fse_batch_upload_all: one copy and a
+    scatter kernel), runs one batched step, gathers every plane back into the buffer
+    (fse_batch_download_all: a gather kernel and one copy), all on the batch's
+    stream, then waits once (fse_batch_sync)."""
+    offs, total = batch.io_layout()
+    t = torch.empty(total, dtype=torch.uint8, pin_memory=True)
+    buf = t.numpy()
+    for v, w in zip(batch.io_views(buf), worlds):
         st = w.state()
-        host = {}
-        for k, v in st.items():
-            t = torch.empty(v.size, dtype={np.uint16: torch.int16, np.uint32: torch.int32, np.int32: torch.int32,
-                                           np.uint8: torch.uint8}[v.dtype.type], pin_memory=True)
-            a = t.numpy().view(v.dtype).reshape(v.shape)
-            a[...] = v
-            host[k] = (t, a)
-        pinned.append({k: a for k, (t, a) in host.items()})
-        pinned[-1]["_keep"] = host
-    bi = sum(a.nbytes for host in pinned for k, a in host.items() if k != "_keep")
+        for k in v:
+            v[k][...] = st[k]
     batch.sync()
     t0 = time.perf_counter()
     for _ in range(steps):
-        for k, host in enumerate(pinned):
-            batch.upload(k, host)
+        batch.upload_all(buf)
         batch.step(1)
-        for k, host in enumerate(pinned):
-            batch.download(k, host)
+        batch.download_all(buf)
         batch.sync()
     dt = max_over_ranks(time.perf_counter() - t0, world_size)
     return {"value": round(world_size * cells * steps / dt / 1e9, 4), "unit": "Gcell/s",
-            "h2d_bytes_per_step": int(bi), "d2h_bytes_per_step": int(bi), "steps": steps,
-            "path": "fse_batch_upload (every world, pinned host planes) + fse_batch_step + fse_batch_download "
-                    "(every world) on the batch's stream, one fse_batch_sync per step"}
+            "h2d_bytes_per_step": int(total), "d2h_bytes_per_step": int(total), "steps": steps,
+            "path": "fse_batch_upload_all (every world's planes, one pinned host buffer) + fse_batch_step + "
+                    "fse_batch_download_all on the batch's stream, one fse_batch_sync per step"}
 
 
 def reference_timing_worlds(sizes, sample, steps, warm, budget_s):

@@ -510,6 +510,39 @@ class Batch:
         check(self.lib.fse_batch_upload(self.h, index, *[ptr(a) if a is not None else None for a in arrs]),
               "batch_upload")
 
+    def io_layout(self):
+        """(offsets, bytes): member k's planes id, colour, scalar, flags, diff start at
+        offsets[k, 0..4] of a buffer of `bytes` bytes (upload_all / download_all)."""
+        offs = np.zeros((len(self.worlds), 5), np.int64)
+        total = C.c_int64(0)
+        check(self.lib.fse_batch_io_layout(self.h, ptr(offs), C.byref(total)), "batch_io_layout")
+        return offs, total.value
+
+    def io_views(self, buf):
+        """Per member, the plane arrays (World.state() keys) that live in `buf`, a
+        uint8 array of io_layout()'s size."""
+        offs, total = self.io_layout()
+        if buf.dtype != np.uint8 or buf.size != total or not buf.flags["C_CONTIGUOUS"]:
+            raise ValueError("need a C-contiguous uint8 buffer of %d bytes" % total)
+        out = []
+        for k, w in enumerate(self.worlds):
+            n = w.width * w.height
+            v = {}
+            for p, (key, dt) in enumerate(World.PLANES):
+                nb = n * np.dtype(dt).itemsize
+                v[key] = buf[offs[k, p]:offs[k, p] + nb].view(dt).reshape(w.height, w.width)
+            out.append(v)
+        return out
+
+    def upload_all(self, buf):
+        """Enqueue one copy of every member's planes from `buf` (io_layout; pinned for
+        an asynchronous copy; keep it alive until sync())."""
+        check(self.lib.fse_batch_upload_all(self.h, ptr(buf), buf.nbytes), "batch_upload_all")
+
+    def download_all(self, buf):
+        """Enqueue the gather of every member's planes into `buf` (filled after sync())."""
+        check(self.lib.fse_batch_download_all(self.h, ptr(buf), buf.nbytes), "batch_download_all")
+
     def download(self, index, out):
         """Enqueue a download of member `index`'s planes into the host arrays of `out`
         (filled after sync())."""

@@ -140,6 +140,9 @@ SIGNATURES = {
     "fse_batch_stream": (_vp, [_vp]),
     "fse_batch_upload": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp]),
     "fse_batch_download": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp]),
+    "fse_batch_io_layout": (_i, [_vp, _vp, C.POINTER(_i64)]),
+    "fse_batch_upload_all": (_i, [_vp, _vp, _i64]),
+    "fse_batch_download_all": (_i, [_vp, _vp, _i64]),
     "fse_batch_prepare_graphs": (_i, [_vp, _i, _i]),
     "fse_batch_timing": (_i, [_vp, _i, C.POINTER(_d), C.POINTER(_i64), _vp, _i, C.POINTER(_i)]),
     "fse_server_create": (_i, [_i64, _i, _pp]),

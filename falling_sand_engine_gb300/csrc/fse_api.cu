@@ -13,6 +13,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>  // CUtensorMap and its encoder's types (the encoder comes from the driver at run time)
+
 #include "fse_host.cuh"
 
 using namespace fse;
@@ -751,7 +753,8 @@ static void free_world(fse_world *w) {
         if (w->items[k]) cudaFree(w->items[k]);
     void *rs[] = {h.dirty,      h.flow,      w->pflow,    w->owner,    w->moving,   w->tex[0],   w->tex[1],
                   w->tex[2],    w->tex[3],   w->tex[4],   w->isl_mark, w->isl_lab,  w->isl_aux,  w->isl_list,
-                  w->isl_out,   w->isl_pix,  w->isl_tab,  w->isl_seg,  w->temp_io, w->tile_stage};
+                  w->isl_out,   w->isl_pix,  w->isl_tab,  w->isl_seg,  w->temp_io, w->tile_stage,
+                  w->tmaps};
     for (void *q : rs)
         if (q) cudaFree(q);
     for (void *q : w->pk_scr)
@@ -763,6 +766,59 @@ static void free_world(fse_world *w) {
         delete w->timer;
     }
     delete w;
+}
+
+// cuTensorMapEncodeTiled, taken from the driver through the runtime (no link
+// against the driver library); NULL when the driver does not offer it
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn tensor_map_encoder() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+        cudaGetLastError();
+    }
+    return fn;
+}
+
+// The tensor maps of the colour pass's TMA staging (2-cell halo): the scalar and
+// colour planes as W x H grids of 4-byte cells, boxes of tma_tile_width(C) x (C + 4)
+// cells. A row pitch that is not a multiple of 16 bytes (W % 4 != 0), or no encoder,
+// leaves h.tmap NULL and the tile is staged with cp.async.
+static bool world_tensor_maps(fse_world *w) {
+    WorldDev &h = w->h;
+    h.tmap = nullptr;
+    const int C = h.C, bw = tma_tile_width(C), bh = C + 4;
+    EncodeTiledFn enc = tensor_map_encoder();
+    if (!enc || h.W % 4 != 0 || bw > 256 || bh > 256) return true;
+    CUtensorMap maps[2];
+    const cuuint64_t dims[2] = {(cuuint64_t)h.W, (cuuint64_t)h.H};
+    const cuuint64_t strides[1] = {(cuuint64_t)h.W * 4};
+    const cuuint32_t box[2] = {(cuuint32_t)bw, (cuuint32_t)bh};
+    const cuuint32_t es[2] = {1, 1};
+    void *planes[2] = {h.sc, h.col};
+    for (int k = 0; k < 2; k++)
+        if (enc(&maps[k], k == 0 ? CU_TENSOR_MAP_DATA_TYPE_INT32 : CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, planes[k], dims,
+                strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return true;  // not encodable: cp.async staging
+    if (cudaMalloc(&w->tmaps, sizeof(maps)) != cudaSuccess) {
+        cudaGetLastError();
+        w->tmaps = nullptr;
+        return false;
+    }
+    w->bytes += sizeof(maps);
+    if (cudaMemcpy(w->tmaps, maps, sizeof(maps), cudaMemcpyHostToDevice) != cudaSuccess) return false;
+    h.tmap = w->tmaps;
+    return true;
 }
 
 // the chunk slots of each colour for the current tick zone
@@ -898,6 +954,7 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
     // chunk slots per colour: (world 0 << 20) | slot; room for the whole world's
     for (int tk = 0; tk < 4 && ok; tk++) ok = dalloc(w, &w->items[tk], (size_t)std::max(h.max_slots, 1));
     if (ok) ok = world_items(w) == FSE_OK;
+    if (ok) ok = world_tensor_maps(w);
     if (!ok) {
         free_world(w);
         return FSE_E_NOMEM;

@@ -41,6 +41,13 @@ struct fse_batch {
     std::map<int, cudaGraphExec_t> tgraphs;
     std::map<int, GraphEvents> tgraph_events;
     std::map<int, long long> tgraph_kernels;
+    // whole-batch plane I/O (fse_batch_upload_all / download_all): every member's
+    // planes in one device buffer laid out as the host buffer, and the segment table
+    // that scatters it into the members' planes (allocated on first use)
+    uint8_t *io_stage = nullptr;
+    void *io_segs = nullptr;
+    int io_nseg = 0;
+    int64_t io_bytes = 0;
 };
 
 namespace {
@@ -114,6 +121,118 @@ int batch_enqueue(fse_batch *b, int n) {
     if (n > 0 && (rc = boundary())) return rc;
     if (tm && !ticks.empty()) tm->tick_groups.push_back(ticks);
     return FSE_OK;
+}
+
+// ---- whole-batch plane I/O: planes id, colour, scalar, flags, diff of every member,
+// each starting on a 16-byte boundary of one buffer
+constexpr int IO_PLANES = 5;
+inline int64_t io_plane_size(int p) { return p == 0 ? 2 : (p == 3 ? 1 : 4); }
+
+struct IoSeg {
+    uint8_t *dev;    // the member's plane
+    int64_t off;     // its place in the buffer
+    int64_t bytes;
+    int kind;        // 0 copy, 1 material ids (checked on upload), 2 flags (visited bit cleared on upload)
+    int *bad;        // the member's flag for replaced ids
+};
+
+// one segment per blockIdx.y; 16-byte words by the grid-stride loop, the tail by bytes
+__global__ void k_io_segments(const IoSeg *__restrict__ segs, uint8_t *stage, int up, int nmat, int air) {
+    const IoSeg sg = segs[blockIdx.y];
+    uint8_t *buf = stage + sg.off;
+    const int64_t nv = sg.bytes >> 4;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    bool bad = false;
+    for (int64_t v = tid; v < nv; v += stride) {
+        if (!up) {
+            reinterpret_cast<uint4 *>(buf)[v] = reinterpret_cast<const uint4 *>(sg.dev)[v];
+            continue;
+        }
+        uint4 q = reinterpret_cast<const uint4 *>(buf)[v];
+        if (sg.kind == 2) {
+            q.x &= ~0x40404040u;  // bit 6 of a flags byte is the kernel's visited mark
+            q.y &= ~0x40404040u;
+            q.z &= ~0x40404040u;
+            q.w &= ~0x40404040u;
+        } else if (sg.kind == 1) {
+            uint32_t *u = &q.x;
+            for (int k = 0; k < 4; k++) {
+                uint32_t lo = u[k] & 0xFFFFu, hi = u[k] >> 16;
+                if ((int)lo >= nmat) lo = (uint32_t)air, bad = true;
+                if ((int)hi >= nmat) hi = (uint32_t)air, bad = true;
+                u[k] = lo | (hi << 16);
+            }
+        }
+        reinterpret_cast<uint4 *>(sg.dev)[v] = q;
+    }
+    // the last bytes (fewer than 16): whole cells, by thread 0 of block 0
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        for (int64_t i = nv << 4; i < sg.bytes; i++) {
+            if (!up) {
+                buf[i] = sg.dev[i];
+            } else if (sg.kind == 1) {
+                if ((i & 1) == 0) {
+                    uint16_t idv = (uint16_t)(buf[i] | (buf[i + 1] << 8));
+                    if ((int)idv >= nmat) idv = (uint16_t)air, bad = true;
+                    sg.dev[i] = (uint8_t)idv;
+                    sg.dev[i + 1] = (uint8_t)(idv >> 8);
+                }
+            } else {
+                sg.dev[i] = sg.kind == 2 ? (uint8_t)(buf[i] & ~0x40u) : buf[i];
+            }
+        }
+    }
+    if (bad) atomicOr(sg.bad, 1);
+}
+
+int batch_io_prepare(fse_batch *b) {
+    int64_t total = 0;
+    fse_batch_io_layout(b, nullptr, &total);
+    if (b->io_stage && b->io_bytes == total) return FSE_OK;
+    if (b->io_stage) cudaFree(b->io_stage);
+    if (b->io_segs) cudaFree(b->io_segs);
+    b->io_stage = nullptr;
+    b->io_segs = nullptr;
+    std::vector<IoSeg> segs;
+    int64_t at = 0;
+    for (fse_world *w : b->worlds) {
+        const int64_t n = (int64_t)w->W * w->H;
+        uint8_t *planes[IO_PLANES] = {(uint8_t *)w->h.id, (uint8_t *)w->h.col, (uint8_t *)w->h.sc, w->h.fl,
+                                      (uint8_t *)w->h.df};
+        for (int p = 0; p < IO_PLANES; p++) {
+            const int64_t nb = n * io_plane_size(p);
+            segs.push_back({planes[p], at, nb, p == 0 ? 1 : (p == 3 ? 2 : 0), w->ctr + 15});
+            at += (nb + 15) & ~(int64_t)15;
+        }
+    }
+    if (cudaMalloc(&b->io_stage, (size_t)std::max<int64_t>(total, 16)) != cudaSuccess ||
+        cudaMalloc(&b->io_segs, segs.size() * sizeof(IoSeg)) != cudaSuccess) {
+        cudaGetLastError();
+        return FSE_E_NOMEM;
+    }
+    if (cudaMemcpy(b->io_segs, segs.data(), segs.size() * sizeof(IoSeg), cudaMemcpyHostToDevice) != cudaSuccess)
+        return FSE_E_CUDA;
+    b->io_nseg = (int)segs.size();
+    b->io_bytes = total;
+    return FSE_OK;
+}
+
+int launch_io_segments(fse_batch *b, bool up) {
+    if (b->io_nseg == 0) return FSE_OK;
+    int rc = ensure_materials_pushed();
+    if (rc) return rc;
+    const MatTable &t = host_table();
+    // enough blocks per segment for the largest member's planes
+    int64_t most = 0;
+    for (fse_world *w : b->worlds) most = std::max<int64_t>(most, (int64_t)w->W * w->H * 4);
+    const int per_seg = (int)std::min<int64_t>(256, std::max<int64_t>(1, (most / 16 + 255) / 256 / 8));
+    for (int s0 = 0; s0 < b->io_nseg; s0 += 65535) {
+        dim3 g(per_seg, std::min(65535, b->io_nseg - s0));
+        k_io_segments<<<g, 256, 0, b->stream>>>(reinterpret_cast<const IoSeg *>(b->io_segs) + s0, b->io_stage,
+                                                up ? 1 : 0, t.n, t.id_air);
+    }
+    count_launches(1);
+    return cudaGetLastError() == cudaSuccess ? FSE_OK : FSE_E_CUDA;
 }
 
 void drop_timed_graphs(fse_batch *b) {
@@ -232,6 +351,8 @@ int fse_batch_destroy(fse_batch *b) {
     if (b->d_table) cudaFree(b->d_table);
     for (int k = 0; k < 4; k++)
         if (b->items[k]) cudaFree(b->items[k]);
+    if (b->io_stage) cudaFree(b->io_stage);
+    if (b->io_segs) cudaFree(b->io_segs);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return FSE_OK;
@@ -426,6 +547,44 @@ int fse_batch_sync(fse_batch *b) {
 }
 
 void *fse_batch_stream(fse_batch *b) { return b ? (void *)b->stream : nullptr; }
+
+int fse_batch_io_layout(fse_batch *b, int64_t *offsets, int64_t *out_bytes) {
+    if (!b) return FSE_E_INVAL;
+    int64_t at = 0;
+    for (size_t k = 0; k < b->worlds.size(); k++) {
+        const int64_t n = (int64_t)b->worlds[k]->W * b->worlds[k]->H;
+        for (int p = 0; p < IO_PLANES; p++) {
+            if (offsets) offsets[IO_PLANES * k + p] = at;
+            at += (n * io_plane_size(p) + 15) & ~(int64_t)15;
+        }
+    }
+    if (out_bytes) *out_bytes = at;
+    return FSE_OK;
+}
+
+int fse_batch_upload_all(fse_batch *b, const void *host, int64_t bytes) {
+    if (!b || !host) return FSE_E_INVAL;
+    int rc = batch_io_prepare(b);
+    if (rc) return rc;
+    if (bytes != b->io_bytes) return FSE_E_INVAL;
+    FSE_CUDA_TRY(cudaMemcpyAsync(b->io_stage, host, (size_t)bytes, cudaMemcpyHostToDevice, b->stream));
+    rc = launch_io_segments(b, true);
+    if (rc) return rc;
+    for (fse_world *w : b->worlds)  // repaint everything
+        if (w->h.dirty) FSE_CUDA_TRY(cudaMemsetAsync(w->h.dirty, 1, (size_t)w->W * w->H, b->stream));
+    return FSE_OK;
+}
+
+int fse_batch_download_all(fse_batch *b, void *host, int64_t bytes) {
+    if (!b || !host) return FSE_E_INVAL;
+    int rc = batch_io_prepare(b);
+    if (rc) return rc;
+    if (bytes != b->io_bytes) return FSE_E_INVAL;
+    rc = launch_io_segments(b, false);
+    if (rc) return rc;
+    FSE_CUDA_TRY(cudaMemcpyAsync(host, b->io_stage, (size_t)bytes, cudaMemcpyDeviceToHost, b->stream));
+    return FSE_OK;
+}
 
 int fse_batch_upload(fse_batch *b, int index, const uint16_t *id, const uint32_t *col, const int32_t *sc,
                      const uint8_t *fl, const int32_t *df) {

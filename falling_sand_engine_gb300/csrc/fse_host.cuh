@@ -73,6 +73,8 @@ struct fse_world {
     int isl_tab_cap;
     // temperature read/write staging (allocated on first use)
     int16_t *temp_io;
+    // the colour pass's tensor maps (h.tmap points here; NULL without TMA staging)
+    void *tmaps;
     // array-of-structs tile staging (allocated on first use)
     uint8_t *tile_stage;
     size_t tile_stage_bytes;

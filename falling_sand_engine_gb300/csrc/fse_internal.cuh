@@ -211,7 +211,16 @@ struct WorldDev {
     // launch whose table starts with this world
     uint32_t *cdone;
     uint32_t *sched;
+    // two CUtensorMaps (128 B each, scalar then colour) over the world's planes for
+    // the colour pass's TMA staging with a 2-cell halo; NULL when the world's row
+    // pitch is not a multiple of 16 bytes (then the tile is staged with cp.async)
+    const void *tmap;
 };
+
+// the TMA-staged tile's width for chunk edge C and a 2-cell halo: the row starts at
+// (cx - 2) rounded down to a multiple of 4 cells (a 16-byte boundary) and covers
+// cx + C + 1, in a whole number of 16-byte groups
+__host__ __device__ constexpr int tma_tile_width(int C) { return (C + 2 * 2 + 3 + 3) & ~3; }
 
 // The fused tick's work list: the chunk slots of each colour ((world << 20) | slot,
 // the per-pass launches' items), passes = cell_iter * 4 of the longest world, and

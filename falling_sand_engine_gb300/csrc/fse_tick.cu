@@ -159,6 +159,38 @@ __device__ __forceinline__ void cluster_sync() {
     asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
 }
 
+// ------------------------------------------------------ TMA staging helpers
+// The 4-byte planes of a tile come in as two 2D tensor copies (cp.async.bulk.tensor)
+// completing on one mbarrier; thread 0 issues them, every thread waits.
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// orders this thread's generic shared-memory accesses before later async-proxy ones
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// box of the tensor map at (x, y) (x a multiple of 4 cells: a 16-byte boundary) into
+// dst (128-byte aligned); complete_tx on bar
+__device__ __forceinline__ void tma_load_2d(void *dst, const void *tmap, int x, int y, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+        "[%4];" ::"r"(smem_addr(dst)),
+        "l"(tmap), "r"(x), "r"(y), "r"(smem_addr(bar))
+        : "memory");
+}
+
 // ------------------------------------------------- fused-tick flag helpers
 __device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t *p) {
     uint32_t v;
@@ -1310,7 +1342,14 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
     using Head = SmemHeadT<T>;
     extern __shared__ __align__(16) unsigned char smem[];
     Head &S = *reinterpret_cast<Head *>(smem);
-    unsigned char *planes = smem + ((sizeof(Head) + 15) & ~(size_t)15);
+    // the planes start on a 128-byte boundary of the shared window (TMA destinations)
+    const uint32_t sbase = smem_addr(smem);
+    unsigned char *planes = smem + (((sbase + (uint32_t)sizeof(Head) + 127u) & ~127u) - sbase);
+    // TMA staging of the 4-byte planes: the partitioned order with a 2-cell halo, in
+    // worlds with tensor maps (one phase of s_tma_bar per staged chunk-pass)
+    constexpr bool kTma = HALO == 2 && !PAIR && !SEQ;
+    __shared__ __align__(8) uint64_t s_tma_bar;
+    uint32_t tma_phase = 0;
 
     const int tid = threadIdx.x;
     const int rank = PAIR ? (int)cluster_rank() : 0;
@@ -1335,6 +1374,7 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
     c.has_inter = mt->has_inter;
     c.f32 = F32;
     const int id_solid = mt->id_solid, id_air = mt->id_air;
+    if (kTma && tid == 0) mbar_init(&s_tma_bar, 1);
     FSE_PT_DECL
     __syncthreads();
 
@@ -1391,6 +1431,9 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
         }
         const int ox = tk % 2, oy = 1 - tk / 2;
         c.iter = iter;
+        // the last chunk-pass's generic accesses to the planes come before this one's
+        // tensor copies into them
+        if constexpr (kTma) fence_proxy_async_smem();
         if (tid == 0) s_w = worlds[item >> 20];
         __syncthreads();
         FSE_PT(0)
@@ -1455,10 +1498,12 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
         const int o0 = PAIR ? rank * half : 0, o1 = PAIR ? (rank ? C : half) : C;
         const int own = o1 - o0;
         TileData Tl;
-        Tl.RW = C + 2 * HALO;
+        const bool tma = kTma && w.tmap != nullptr;
+        // with TMA the rows start on a 16-byte boundary and are tma_tile_width wide
+        Tl.RW = tma ? tma_tile_width(C) : C + 2 * HALO;
         Tl.RHF = own + 2 * HALO;
         Tl.RHI = own + HALO + 10;
-        Tl.x0 = cx - HALO;
+        Tl.x0 = tma ? ((cx - HALO) & ~3) : cx - HALO;
         Tl.y0 = cy + o0 - HALO;
         Tl.W = W;
         Tl.H = H;
@@ -1474,7 +1519,7 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
         Tl.aw = C + 2;
         const int nid = Tl.RW * Tl.RHI, nfull = Tl.RW * Tl.RHF;
         Tl.s_sc = (int32_t *)planes;
-        Tl.s_col = (uint32_t *)(Tl.s_sc + nfull);
+        Tl.s_col = (uint32_t *)(Tl.s_sc + ((nfull + 31) & ~31));  // 128-byte aligned
         Tl.s_id = (uint16_t *)(Tl.s_col + nfull);
         Tl.s_fl = (uint8_t *)(Tl.s_id + ((nid + 1) & ~1));
         if constexpr (PAIR) {
@@ -1488,9 +1533,15 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
         }
 
         // ---- stage the tile, one warp per row. The 4-byte planes go straight to
-        // shared memory with cp.async; ids and flags are loaded a row at a time, all
-        // loads of a row in flight together. The chunk's ids decide the skip and the
-        // lattice mode.
+        // shared memory, as two tensor copies (TMA) or with cp.async; ids and flags
+        // are loaded a row at a time, all loads of a row in flight together. The
+        // chunk's ids decide the skip and the lattice mode.
+        if (tma && tid == 0) {
+            const char *tm = static_cast<const char *>(w.tmap);
+            mbar_expect_tx(&s_tma_bar, 2u * (uint32_t)nfull * 4u);
+            tma_load_2d(Tl.s_sc, tm, Tl.x0, Tl.y0, &s_tma_bar);
+            tma_load_2d(Tl.s_col, tm + 128, Tl.x0, Tl.y0, &s_tma_bar);
+        }
         int active = 0, fire = 0;
         {
             const int lane = tid & 31, wid = tid >> 5;
@@ -1512,7 +1563,7 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
                         if (full) f[k] = w.fl[gb + gx];
                     }
                 }
-                if (full) {
+                if (full && !tma) {
 #pragma unroll
                     for (int k = 0; k < MAXRW / 32; k++) {
                         const int lx = lane + 32 * k, gx = Tl.x0 + lx;
@@ -1538,6 +1589,24 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
                         if (mt_iter(S.ma[v[k]]) > c.iter) active = 1;
                         if ((int)v[k] == c.id_fire) fire = 1;
                     }
+                }
+            }
+        }
+        if (tma) {
+            // the tensor copies have landed (a bounded wait); cells outside the world
+            // read as zero there and take the outside colour
+            long long spins = 0;
+            while (!mbar_try_wait(&s_tma_bar, tma_phase)) {
+                if (++spins > (1LL << 26)) {
+                    atomicOr(w.err, ERR_TIMEOUT);
+                    break;
+                }
+            }
+            tma_phase ^= 1u;
+            if (Tl.x0 < 0 || Tl.y0 < 0 || Tl.x0 + Tl.RW > W || Tl.y0 + Tl.RHF > H) {
+                for (int i = tid; i < nfull; i += T) {
+                    const int r = i / Tl.RW, gx = Tl.x0 + (i - r * Tl.RW), gy = Tl.y0 + r;
+                    if ((unsigned)gx >= (unsigned)W || (unsigned)gy >= (unsigned)H) Tl.s_col[i] = 0xff0000u;
                 }
             }
         }
@@ -1816,10 +1885,14 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
 #if !defined(FSE_TICK_TEMP_TU) && !defined(FSE_TICK_SEQ_TU) && !defined(FSE_TICK_F32_TU) && \
     !defined(FSE_TICK_PAIR_TU) && !defined(FSE_TICK_FUSED_TU)
 size_t colour_pass_smem(int C, int halo) {
-    size_t RW = (size_t)C + 2 * halo, RHF = (size_t)C + 2 * halo, RHI = (size_t)C + halo + 10;
+    // a 2-cell halo leaves room for the TMA-staged tile's wider rows
+    size_t RW = (size_t)C + 2 * halo;
+    if (halo == 2) RW = std::max(RW, (size_t)tma_tile_width(C));
+    size_t RHF = (size_t)C + 2 * halo, RHI = (size_t)C + halo + 10;
     size_t nid = RW * RHI, nfull = RW * RHF;
-    size_t head = (sizeof(SmemHead) + 15) & ~(size_t)15;
-    return head + nfull * 4 + nfull * 4 + ((nid + 1) & ~(size_t)1) * 2 + nfull;
+    // the planes start on a 128-byte boundary of the window: up to 128 bytes of padding
+    size_t head = (sizeof(SmemHead) + 127) & ~(size_t)127;
+    return 128 + head + ((nfull + 31) & ~(size_t)31) * 4 + nfull * 4 + ((nid + 1) & ~(size_t)1) * 2 + nfull;
 }
 
 #endif
@@ -1858,8 +1931,8 @@ static size_t colour_pass_smem_pair(int C, int halo) {
     const size_t own = (size_t)C / 2;
     size_t RW = (size_t)C + 2 * halo, RHF = own + 2 * halo, RHI = own + halo + 10;
     size_t nid = RW * RHI, nfull = RW * RHF;
-    size_t head = (sizeof(SmemHeadT<CP_THREADS / 2>) + 15) & ~(size_t)15;
-    return head + nfull * 4 + nfull * 4 + ((nid + 1) & ~(size_t)1) * 2 + nfull;
+    size_t head = (sizeof(SmemHeadT<CP_THREADS / 2>) + 127) & ~(size_t)127;
+    return 128 + head + ((nfull + 31) & ~(size_t)31) * 4 + nfull * 4 + ((nid + 1) & ~(size_t)1) * 2 + nfull;
 }
 
 // the chunks split over CTA pairs (thread-block clusters of two): `clusters` pairs

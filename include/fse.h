@@ -458,6 +458,17 @@ int fse_batch_upload(fse_batch *batch, int index, const uint16_t *id, const uint
                      const uint8_t *flags, const int32_t *diff);
 int fse_batch_download(fse_batch *batch, int index, uint16_t *id, uint32_t *colour, int32_t *scalar, uint8_t *flags,
                        int32_t *diff);
+/* Every member's planes in one host buffer, moved by one large copy each way (host
+ * buffer pinned for the copy to run asynchronously): member k's planes id, colour,
+ * scalar, flags, diff start at offsets[5k .. 5k + 4] (bytes, multiples of 16) of a
+ * buffer of *out_bytes bytes; offsets may be NULL. */
+int fse_batch_io_layout(fse_batch *batch, int64_t *offsets, int64_t *out_bytes);
+/* enqueue on the batch's stream the copy of the whole buffer and its scatter into
+ * the members' planes (ids checked and flags masked as fse_batch_upload does) */
+int fse_batch_upload_all(fse_batch *batch, const void *host, int64_t bytes);
+/* enqueue the gather of every member's planes and one copy into the buffer; the
+ * buffer holds them after the next fse_batch_sync */
+int fse_batch_download_all(fse_batch *batch, void *host, int64_t bytes);
 
 /* ---------------------------------------------------------------- serving */
 /* Continuous batching of world-tick requests (no analogue in the reference, which

@@ -306,6 +306,33 @@ def test_batch_async_plane_io(fse):
         batch.sync()
     assert worlds[0].state()["id"][0, 0] == fse.material_find("GENERIC_AIR")
     batch.sync()  # reported once
+    # the whole batch through one buffer
+    offs, total = batch.io_layout()
+    assert offs[0, 0] == 0 and total % 16 == 0 and np.all(offs % 16 == 0)
+    buf = np.zeros(total, np.uint8)
+    batch.download_all(buf)
+    batch.sync()
+    views = batch.io_views(buf)
+    for k, w in enumerate(worlds):
+        ref = w.state()
+        for key in ref:
+            np.testing.assert_array_equal(views[k][key], ref[key], err_msg="download_all %d %s" % (k, key))
+    for k, tw in enumerate(twins):
+        for key, v in tw.state().items():
+            views[k][key][...] = v
+    views[1]["flags"][...] |= 0x40  # the visited bit is cleared on upload
+    batch.upload_all(buf)
+    batch.step(1)
+    batch.sync()
+    for k, tw in enumerate(twins):
+        tw.step(1)
+        a, b = worlds[k].state(), tw.state()
+        for key in a:
+            np.testing.assert_array_equal(a[key], b[key], err_msg="upload_all %d %s" % (k, key))
+    views[1]["id"][3, 5] = 1000
+    batch.upload_all(buf)
+    with pytest.raises(fse.FseError):
+        batch.sync()
     batch.close()
     for w in worlds + twins:
         w.close()
