@@ -273,6 +273,11 @@ struct Tile : TileData {
     __device__ __forceinline__ bool inw(int x, int y) const {
         return !EDGE || ((unsigned)x < (unsigned)W && (unsigned)y < (unsigned)H);
     }
+    // inside the world whatever EDGE: the writes of fire and interactions can reach
+    // cells outside the world, where world.cpp:1003-1008 drops them
+    __device__ __forceinline__ bool in_world(int x, int y) const {
+        return (unsigned)x < (unsigned)W && (unsigned)y < (unsigned)H;
+    }
     __device__ __forceinline__ int li(int x, int y) const { return (y - y0) * RW + (x - x0); }
 
     // world.cpp:999-1002: outside the world reads Tiles_TEST_SOLID
@@ -794,9 +799,11 @@ __device__ __forceinline__ void rule_a(const TL &T, Ctx &c, int x, int y) {
                         found = true;
                         if (c.D() % 500 == 0) {
                             Cell f = create_tile(c, c.id_fire);
-                            led_replace_at(T, c, x + xx, y + yy, f);
-                            T.put_new(x + xx, y + yy, f, mt);
-                            T.setvis(x + xx, y + yy);
+                            if (T.in_world(x + xx, y + yy)) {
+                                led_replace_at(T, c, x + xx, y + yy, f);
+                                T.put_new(x + xx, y + yy, f, mt);
+                                T.setvis(x + xx, y + yy);
+                            }
                         }
                     }
                 }
@@ -830,9 +837,11 @@ __device__ __forceinline__ void rule_a(const TL &T, Ctx &c, int x, int y) {
                                             : ((xx == 0 && yy == 0) || T.id(x + xx, y + yy) == T.id_air);
                             if (doit) {
                                 Cell nt = create_tile(c, d1);
-                                led_replace_at(T, c, x + xx, y + yy, nt);
-                                T.put_new(x + xx, y + yy, nt, mt);
-                                T.setvis(x + xx, y + yy);
+                                if (T.in_world(x + xx, y + yy)) {
+                                    led_replace_at(T, c, x + xx, y + yy, nt);
+                                    T.put_new(x + xx, y + yy, nt, mt);
+                                    T.setvis(x + xx, y + yy);
+                                }
                             }
                         }
                 }
@@ -1371,7 +1380,8 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
     c.id_lava = mt->id_lava;
     c.id_steam = mt->id_steam;
     c.id_obsidian = mt->id_obsidian;
-    c.has_inter = mt->has_inter;
+    // interactions exist exactly when the launch runs the 5-cell halo (tick_halo)
+    c.has_inter = HALO == 5;
     c.f32 = F32;
     const int id_solid = mt->id_solid, id_air = mt->id_air;
     if (kTma && tid == 0) mbar_init(&s_tma_bar, 1);
@@ -1644,8 +1654,6 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
         int running = 0;  // spawns emitted so far by this chunk-pass
         int nsub = 0;     // sweep-A sub-phases so far (CTA pair: alternate exchange slots)
         c.led_g = w.ledger;
-        // the world bounds policy matters only where the tile crosses the world edge
-        const bool edge = Tl.x0 < 0 || Tl.y0 < 0 || Tl.x0 + Tl.RW > W || Tl.y0 + Tl.RHI > H;
         // The reference's order as a wavefront: thread k updates chunk row k counted
         // from the bottom (the row world.cpp's loop takes k-th), cell dx at step
         // dx + s*k. A cell reads and writes at most RX columns to either side
@@ -1806,17 +1814,16 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
             }
         }
         };
-        if constexpr (SEQ) {
-            if (edge)
-                sweeps_seq(Tile<true, TEMP, true, F32>(Tl));
-            else
-                sweeps_seq(Tile<false, TEMP, true, F32>(Tl));
-        } else {
-            if (edge)
-                sweeps(Tile<true, TEMP, false, F32, PAIR>(Tl));
-            else
-                sweeps(Tile<false, TEMP, false, F32, PAIR>(Tl));
-        }
+        // One instantiation of the sweeps for every chunk (a second one for the chunks
+        // at the world edge doubles the register pressure of the kernel, whose spills
+        // cost more than the checks they would save): the tile holds GENERIC_SOLID
+        // outside the world, which is what world.cpp:999-1002 reads there, and the only
+        // writes that can reach such cells (fire and interactions) check the world
+        // bounds themselves.
+        if constexpr (SEQ)
+            sweeps_seq(Tile<false, TEMP, true, F32>(Tl));
+        else
+            sweeps(Tile<false, TEMP, false, F32, PAIR>(Tl));
 
         // ---- write back the cells this CTA changed (full-state rows inside the world),
         // one warp per row
