@@ -394,7 +394,7 @@ __device__ __forceinline__ void grid_sync(GridBar *gb, unsigned nblocks, int32_t
 
 constexpr int SERIAL_MAX_ITER = 1 << 16;
 constexpr int SERIAL_MAX_WORLDS = 4096;  // worlds of one launch (a batch holds at most 4095)
-constexpr int SERIAL_THREADS = 256;
+constexpr int SERIAL_THREADS = 1024;  // one block per SM: 152 arrivals at each grid barrier
 
 // index g of a flattened index space: its entry in s_pref (prefix sums over the
 // entries, in shared memory)
@@ -646,7 +646,9 @@ __global__ void __launch_bounds__(SERIAL_THREADS) k_part_serial(const WorldDev *
                 const WorldDev &w = worlds[s_ids[j]];
                 const int i = g - s_apref[j];
                 const int c = fill_of(w, i);
-                if (c >= 0) atomicMax(&w.df[c], fill_code(i));
+                // records only grow, so one already at or above this fill's code stays
+                // there: only the cells cleared in B1 take atomics
+                if (c >= 0 && __ldcg(&w.df[c]) < fill_code(i)) atomicMax(&w.df[c], fill_code(i));
             }
             for (int k = gtid; k < n_worlds; k += gstride) worlds[k].chg_n[1 - par] = 0;
         }

@@ -31,8 +31,8 @@
 // -DFSE_PHASE_CLOCKS): thread 0 of each CTA accumulates clock64() deltas between
 // barriers; fse_debug_phase_clocks() reads the totals. Off by default: no cost.
 #ifdef FSE_PHASE_CLOCKS
-__device__ unsigned long long g_phase_clk[16];
-__device__ unsigned long long g_phase_max[16];  // per phase: the largest CTA total; [15]: largest CTA
+static __device__ unsigned long long g_phase_clk[16];  // per translation unit
+static __device__ unsigned long long g_phase_max[16];  // per phase: the largest CTA total; [15]: largest CTA
 #define FSE_PT_DECL                       \
     __shared__ long long pt_acc[16];      \
     long long pt_last = clock64();        \
