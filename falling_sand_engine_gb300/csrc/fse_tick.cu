@@ -1444,7 +1444,16 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
         // the last chunk-pass's generic accesses to the planes come before this one's
         // tensor copies into them
         if constexpr (kTma) fence_proxy_async_smem();
-        if (tid == 0) s_w = worlds[item >> 20];
+        {
+            // the world's descriptor into shared memory, 8 bytes a thread (one thread
+            // copying it load by load took ~5% of a chunk-pass)
+            static_assert(sizeof(WorldDev) % 8 == 0, "the descriptor is copied in 8-byte words");
+            constexpr int NW8 = (int)(sizeof(WorldDev) / 8);
+            static_assert(NW8 <= T, "one word per thread");
+            if (tid < NW8)
+                reinterpret_cast<uint2 *>(&s_w)[tid] =
+                    __ldg(reinterpret_cast<const uint2 *>(&worlds[item >> 20]) + tid);
+        }
         __syncthreads();
         FSE_PT(0)
         const WorldDev &w = s_w;
