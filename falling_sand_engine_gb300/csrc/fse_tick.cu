@@ -1318,6 +1318,7 @@ struct SmemHeadT {
     // CTA pair: what the partner wrote here: [0..1] its chunk flags, [2..3] its spawn
     // count of a sweep-A sub-phase (alternate slots)
     uint32_t xch[4];
+    uint32_t vote[32];  // each warp's activity (bit 0) and fire (bit 1) votes of the chunk-pass
 };
 using SmemHead = SmemHeadT<CP_THREADS>;
 
@@ -1629,10 +1630,10 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
                 }
             }
         }
-        active = __syncthreads_or(active);
-        fire = __syncthreads_or(fire);
-        cp_async_wait_all();
         if constexpr (PAIR) {
+            active = __syncthreads_or(active);
+            fire = __syncthreads_or(fire);
+            cp_async_wait_all();
             // the pair decides together whether the chunk runs and with which lattice
             const int slot_x = npass & 1;
             if (tid == 0) st_cluster_u32(mapa_rank(smem_addr(&S.xch[slot_x]), (uint32_t)(rank ^ 1)),
@@ -1642,7 +1643,15 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
             active |= (int)(o & 1u);
             fire |= (int)((o >> 1) & 1u);
         } else {
+            // the copies are in and the chunk's votes are taken with one barrier: each
+            // warp's leader writes its warp's votes, every warp ORs the 32 words after
+            cp_async_wait_all();
+            const unsigned bits = (__any_sync(0xffffffffu, active) ? 1u : 0u) | (__any_sync(0xffffffffu, fire) ? 2u : 0u);
+            if ((tid & 31) == 0) S.vote[tid >> 5] = bits;
             __syncthreads();
+            const unsigned vv = __reduce_or_sync(0xffffffffu, (tid & 31) < T / 32 ? S.vote[tid & 31] : 0u);
+            active = (int)(vv & 1u);
+            fire = (int)((vv >> 1) & 1u);
         }
         npass++;
         FSE_PT(1)

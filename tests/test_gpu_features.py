@@ -185,16 +185,16 @@ def test_batch_equals_individual_worlds(fse):
 def test_autotune_never_changes_results(fse):
     ref = fse.World(384, 384, seed=44)
     ref.generate(fse.GEN_MIX, 44)
-    ref.step(9)
+    ref.step(11)
     w = fse.World(384, 384, seed=44)
     w.generate(fse.GEN_MIX, 44)
     b = fse.Batch([w])
     choice = b.autotune()
-    assert choice["colour_ctas_per_sm"] in (0, 1, 2, 3) and choice["particle_blocks"] >= 0
+    assert choice["colour_ctas_per_sm"] in (0, 1, 2, 3, 4) and choice["particle_blocks"] >= 0
     assert w.tick_count == 0  # the autotuner restored the world
     b.step(3)
     # every launch shape gives the same world
-    for shape in ((1, 4), (0, 1), (1, 0), (2, 0), (3, 4), (2, 16)):
+    for shape in ((1, 4), (0, 1), (4, 0), (1, 0), (2, 0), (3, 4), (4, 16), (2, 16)):
         b.set_launch(*shape)
         b.step(1)
     sr, sw = ref.state(), w.state()
