@@ -876,8 +876,9 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
     w->seed = c.seed;
     w->part_cap = c.particle_capacity;
     w->stage_cap = c.spawn_capacity;
-    w->threads = 1024;
-    w->grid = 0;
+    // the fused tick (launch shape 4) by default; worlds in the reference's order
+    // run their passes one launch each whatever the shape
+    colour_shape(4, &w->threads, &w->grid);
     w->timer = nullptr;
     if (c.stream) {
         w->stream = (cudaStream_t)c.stream;

@@ -27,7 +27,9 @@ struct fse_batch {
     int n_items[4] = {0, 0, 0, 0};
     int C = 128, max_iter = 0, move_blocks = 1, stage_blocks = 1;
     int max_move_blocks = 1;       // particle blocks per world that cover the largest list
-    int threads = 1024, grid = 0;  // grid 0 = one CTA per chunk, else persistent CTAs
+    // the colour pass's launch shape (colour_shape): the fused tick until the autotuner
+    // or fse_batch_set_launch chooses
+    int threads = CP_THREADS, grid = FUSED_GRID;
     cudaStream_t stream = nullptr;
     std::map<int, cudaGraphExec_t> graphs;
     std::map<int, long long> graph_kernels;  // kernels one replay launches

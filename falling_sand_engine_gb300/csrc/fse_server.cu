@@ -474,8 +474,8 @@ int fse_server_step(fse_server *s, int *out_active) {
     f.end = take_event(s);
     if (!f.start || !f.end) return FSE_E_CUDA;
     FSE_CUDA_TRY(cudaEventRecord(f.start, s->stream));
-    rc = enqueue_step(s->d_table, (int)want.size(), s->items, s->n_items, max_iter, s->C, 1024, 0, true, mb, sb,
-                      s->stream, nullptr, temp_tiles_of(act), temp_track_of(act));
+    rc = enqueue_step(s->d_table, (int)want.size(), s->items, s->n_items, max_iter, s->C, CP_THREADS, FUSED_GRID, true,
+                      mb, sb, s->stream, nullptr, temp_tiles_of(act), temp_track_of(act));
     if (rc) return rc;
     FSE_CUDA_TRY(cudaEventRecord(f.end, s->stream));
     s->seq++;
