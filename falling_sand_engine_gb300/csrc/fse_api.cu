@@ -412,8 +412,12 @@ int enqueue_step(WorldDev *d_worlds, int n_worlds, uint32_t *const items[4], con
         }
         ft.passes = 4 * max_iter;
         ft.n_worlds = n_worlds;
-        cudaError_t e = f32 ? launch_colour_fused_f32(d_worlds, ft, g_dev_mt, halo, C, sm_count(), s, temp_track)
-                            : launch_colour_fused(d_worlds, ft, g_dev_mt, halo, C, sm_count(), s, temp_track);
+        // one CTA per SM, but no more than the chunks of an iteration: a CTA beyond them
+        // would only set up its shared memory and find no chunk-pass it may start
+        const int per_iter = n_items[0] + n_items[1] + n_items[2] + n_items[3];
+        const int grid_f = std::max(1, std::min(sm_count(), per_iter));
+        cudaError_t e = f32 ? launch_colour_fused_f32(d_worlds, ft, g_dev_mt, halo, C, grid_f, s, temp_track)
+                            : launch_colour_fused(d_worlds, ft, g_dev_mt, halo, C, grid_f, s, temp_track);
         if (e != cudaSuccess) return FSE_E_CUDA;
         if (timer) {
             if (timer->record(b, s) != cudaSuccess) return FSE_E_CUDA;
