@@ -1313,7 +1313,7 @@ struct SmemHeadT {
     long long led[LED_ROWS * 64];
     int scan[40];
     uint8_t mreact[MAXMAT];
-    int cnt[NT];  // sweep-A spawns per enumeration index, then their ranks
+    int cnt[NT];  // CTA pair: sweep-A spawns per enumeration index
     uint32_t air[(128 + 2) * 5];  // sweep-B pillar snapshot (chunk edge <= 128)
     // CTA pair: what the partner wrote here: [0..1] its chunk flags, [2..3] its spawn
     // count of a sweep-A sub-phase (alternate slots)
@@ -1746,7 +1746,7 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
                         // so every spawn event stays in its thread until it is ranked
                         const int e = tid;
                         c.ev.n = 0;
-                        S.cnt[tid] = 0;
+                        if constexpr (PAIR) S.cnt[tid] = 0;
                         if (e < total) {
                             int q, r;
                             divmod_small(e, nx, rnx, q, r);
@@ -1757,8 +1757,8 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
                         // rank spawned particles in enumeration order. S.cnt[e] and the scan
                         // scratch are next written after the next sub-phase's barrier, so no
                         // barrier is needed after this block.
-                        if (c.ev.n > 0) S.cnt[e] = c.ev.n;
                         if constexpr (PAIR) {
+                            if (c.ev.n > 0) S.cnt[e] = c.ev.n;
                             // the sub-phase's enumeration runs through rank 0's rows first:
                             // each CTA ranks its own spawns, the partner's count of the
                             // sub-phase comes through the cluster barrier that ends it
@@ -1778,8 +1778,23 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
                             }
                             running += tot + tot_p;
                         } else if (__syncthreads_or(c.ev.n > 0)) {
-                            int tot;
-                            const int ex = block_excl_scan(S.cnt[tid], S.scan, &tot);
+                            // ranks with one more barrier: each warp's total in shared
+                            // memory, a thread's rank the totals of the warps before it plus
+                            // its lanes' prefix (the scratch is next written after the next
+                            // sub-phase's barrier)
+                            const int lane = tid & 31, wid = tid >> 5;
+                            int inc = c.ev.n;
+#pragma unroll
+                            for (int o = 1; o < 32; o <<= 1) {
+                                const int t = __shfl_up_sync(0xffffffffu, inc, o);
+                                if (lane >= o) inc += t;
+                            }
+                            if (lane == 31) S.scan[wid] = inc;
+                            __syncthreads();
+                            const int ws = lane < T / 32 ? S.scan[lane] : 0;
+                            const int tot = (int)__reduce_add_sync(0xffffffffu, (unsigned)ws);
+                            const int ex = (int)__reduce_add_sync(0xffffffffu, lane < wid ? (unsigned)ws : 0u) + inc -
+                                           c.ev.n;
                             if (c.ev.n > 0) {
                                 // staging slots are taken in any order; the (chunk-pass, rank)
                                 // key orders the particles later
