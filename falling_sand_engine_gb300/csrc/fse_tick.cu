@@ -1313,7 +1313,7 @@ struct SmemHeadT {
     long long led[LED_ROWS * 64];
     int scan[40];
     uint8_t mreact[MAXMAT];
-    int cnt[NT];  // CTA pair: sweep-A spawns per enumeration index
+    int cnt[NT];  // sweep-A spawns per enumeration index, then their ranks
     uint32_t air[(128 + 2) * 5];  // sweep-B pillar snapshot (chunk edge <= 128)
     // CTA pair: what the partner wrote here: [0..1] its chunk flags, [2..3] its spawn
     // count of a sweep-A sub-phase (alternate slots)
@@ -1746,7 +1746,7 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
                         // so every spawn event stays in its thread until it is ranked
                         const int e = tid;
                         c.ev.n = 0;
-                        if constexpr (PAIR) S.cnt[tid] = 0;
+                        S.cnt[tid] = 0;
                         if (e < total) {
                             int q, r;
                             divmod_small(e, nx, rnx, q, r);
@@ -1757,8 +1757,8 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
                         // rank spawned particles in enumeration order. S.cnt[e] and the scan
                         // scratch are next written after the next sub-phase's barrier, so no
                         // barrier is needed after this block.
+                        if (c.ev.n > 0) S.cnt[e] = c.ev.n;
                         if constexpr (PAIR) {
-                            if (c.ev.n > 0) S.cnt[e] = c.ev.n;
                             // the sub-phase's enumeration runs through rank 0's rows first:
                             // each CTA ranks its own spawns, the partner's count of the
                             // sub-phase comes through the cluster barrier that ends it
