@@ -437,7 +437,9 @@ struct Ctx {
     long long *led_g;      // global ledger [LED_ROWS][MAXMAT]
     const uint32_t *ma;
     const uint8_t *mreact;  // reactions per material (shared)
-    SpawnEv ev;
+    // the cell's spawn event, a local of its own: emit_spawns takes its address, and a
+    // member whose address escapes keeps the whole context in local memory
+    SpawnEv *ev;
     // start the draws of the cell at (x, y); most cells never draw, so the key
     // (two hash rounds) is computed only when the first draw needs it
     __device__ __forceinline__ void at(int x, int y) {
@@ -605,16 +607,16 @@ __device__ __forceinline__ void soup_flow_f(const TL &T, Ctx &c, const Cell &t, 
 }
 
 __device__ __forceinline__ void spawn_one(Ctx &c, int kind, int x, int y, const Cell &t, float vx, float vy) {
-    c.ev.n = 1;
-    c.ev.kind = kind;
-    c.ev.x = x;
-    c.ev.y = y;
-    c.ev.id = t.id;
-    c.ev.fl = t.fl;
-    c.ev.col = t.col;
-    c.ev.sc = t.sc;
-    c.ev.vx = vx;
-    c.ev.vy = vy;
+    c.ev->n = 1;
+    c.ev->kind = kind;
+    c.ev->x = x;
+    c.ev->y = y;
+    c.ev->id = t.id;
+    c.ev->fl = t.fl;
+    c.ev->col = t.col;
+    c.ev->sc = t.sc;
+    c.ev->vx = vx;
+    c.ev->vy = vy;
 }
 
 // ------------------------------------------------- sweep A, f32 liquids
@@ -640,17 +642,17 @@ __device__ __forceinline__ void rule_a_soup_f32(const TL &T, Ctx &c, Cell &t, in
         int n = (int)__fdiv_rn(amount, 4.0f);  // int n = tile.fluidAmount / 4
         if (n < 1) n = 1;
         led_add(c, LED_CN, t.id, n - 1);
-        c.ev.n = n;
-        c.ev.kind = 2;
-        c.ev.x = x;
-        c.ev.y = y + 1;
-        c.ev.id = t.id;
-        c.ev.fl = 0;
-        c.ev.col = t.col;
-        c.ev.sc = t.sc;
-        if (TL::kTemp) c.ev.tp = T.tp_load(x, y);
-        c.ev.ck = c.key();
-        c.ev.k0 = c.k;
+        c.ev->n = n;
+        c.ev->kind = 2;
+        c.ev->x = x;
+        c.ev->y = y + 1;
+        c.ev->id = t.id;
+        c.ev->fl = 0;
+        c.ev->col = t.col;
+        c.ev->sc = t.sc;
+        if (TL::kTemp) c.ev->tp = T.tp_load(x, y);
+        c.ev->ck = c.key();
+        c.ev->k0 = c.k;
         c.k += 2 * n;
         return;
     }
@@ -909,17 +911,17 @@ __device__ __forceinline__ void rule_a(const TL &T, Ctx &c, int x, int y) {
             int n = t.sc >> 18;
             if (n < 1) n = 1;
             led_add(c, LED_CN, t.id, n - 1);
-            c.ev.n = n;
-            c.ev.kind = 2;
-            c.ev.x = x;
-            c.ev.y = y + 1;
-            c.ev.id = t.id;
-            c.ev.fl = 0;
-            c.ev.col = t.col;
-            c.ev.sc = t.sc;
-            if (TL::kTemp) c.ev.tp = T.tp_load(x, y);
-            c.ev.ck = c.key();
-            c.ev.k0 = c.k;
+            c.ev->n = n;
+            c.ev->kind = 2;
+            c.ev->x = x;
+            c.ev->y = y + 1;
+            c.ev->id = t.id;
+            c.ev->fl = 0;
+            c.ev->col = t.col;
+            c.ev->sc = t.sc;
+            if (TL::kTemp) c.ev->tp = T.tp_load(x, y);
+            c.ev->ck = c.key();
+            c.ev->k0 = c.k;
             c.k += 2 * n;
             return;
         }
@@ -1371,6 +1373,8 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
     }
     for (int i = tid; i < LED_ROWS * 64; i += T) S.led[i] = 0;
     Ctx c;
+    SpawnEv ev_store;  // outside the context (see Ctx::ev)
+    c.ev = &ev_store;
     c.iter = iter_arg;
     c.mt = mt;
     c.led_s = S.led;
@@ -1693,13 +1697,13 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
                     if (row && dx >= 0 && dx < cw) {
                         const int x = cx + dx, y = cy + dy;
                         if (sweep == 0) {
-                            c.ev.n = 0;
+                            c.ev->n = 0;
                             rule_a(Tl, c, x, y);
-                            if (c.ev.n > 0) {
-                                const int base = atomicAdd(w.stage_count, c.ev.n);
-                                emit_spawns<TEMP, F32>(w, c.ev, cp * (uint32_t)w.cp_rows + (uint32_t)k, (uint32_t)spawned,
+                            if (c.ev->n > 0) {
+                                const int base = atomicAdd(w.stage_count, c.ev->n);
+                                emit_spawns<TEMP, F32>(w, *c.ev, cp * (uint32_t)w.cp_rows + (uint32_t)k, (uint32_t)spawned,
                                                   base);
-                                spawned += c.ev.n;
+                                spawned += c.ev->n;
                             }
                         } else if (sweep == 1) {
                             rule_b(Tl, c, x, y, w.df[(size_t)y * W + x]);
@@ -1745,7 +1749,7 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
                         // sweep A sub-phases have at most 43 x 22 <= T cells: one per thread,
                         // so every spawn event stays in its thread until it is ranked
                         const int e = tid;
-                        c.ev.n = 0;
+                        c.ev->n = 0;
                         S.cnt[tid] = 0;
                         if (e < total) {
                             int q, r;
@@ -1757,13 +1761,13 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
                         // rank spawned particles in enumeration order. S.cnt[e] and the scan
                         // scratch are next written after the next sub-phase's barrier, so no
                         // barrier is needed after this block.
-                        if (c.ev.n > 0) S.cnt[e] = c.ev.n;
+                        if (c.ev->n > 0) S.cnt[e] = c.ev->n;
                         if constexpr (PAIR) {
                             // the sub-phase's enumeration runs through rank 0's rows first:
                             // each CTA ranks its own spawns, the partner's count of the
                             // sub-phase comes through the cluster barrier that ends it
                             int tot = 0, ex = 0;
-                            if (__syncthreads_or(c.ev.n > 0)) ex = block_excl_scan(S.cnt[tid], S.scan, &tot);
+                            if (__syncthreads_or(c.ev->n > 0)) ex = block_excl_scan(S.cnt[tid], S.scan, &tot);
                             const int slot_t = 2 + (nsub & 1);
                             if (tid == 0)
                                 st_cluster_u32(mapa_rank(smem_addr(&S.xch[slot_t]), (uint32_t)(rank ^ 1)),
@@ -1771,19 +1775,19 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
                             cluster_sync();
                             const int tot_p = (int)S.xch[slot_t];
                             nsub++;
-                            if (c.ev.n > 0) {
-                                const int base = atomicAdd(w.stage_count, c.ev.n);
-                                emit_spawns<TEMP, F32>(w, c.ev, cp, (uint32_t)(running + (rank ? tot_p : 0) + ex),
+                            if (c.ev->n > 0) {
+                                const int base = atomicAdd(w.stage_count, c.ev->n);
+                                emit_spawns<TEMP, F32>(w, *c.ev, cp, (uint32_t)(running + (rank ? tot_p : 0) + ex),
                                                        base);
                             }
                             running += tot + tot_p;
-                        } else if (__syncthreads_or(c.ev.n > 0)) {
+                        } else if (__syncthreads_or(c.ev->n > 0)) {
                             // ranks with one more barrier: each warp's total in shared
                             // memory, a thread's rank the totals of the warps before it plus
                             // its lanes' prefix (the scratch is next written after the next
                             // sub-phase's barrier)
                             const int lane = tid & 31, wid = tid >> 5;
-                            int inc = c.ev.n;
+                            int inc = c.ev->n;
 #pragma unroll
                             for (int o = 1; o < 32; o <<= 1) {
                                 const int t = __shfl_up_sync(0xffffffffu, inc, o);
@@ -1794,12 +1798,12 @@ __global__ void __launch_bounds__(PAIR ? CP_THREADS / 2 : CP_THREADS, PAIR ? 2 :
                             const int ws = lane < T / 32 ? S.scan[lane] : 0;
                             const int tot = (int)__reduce_add_sync(0xffffffffu, (unsigned)ws);
                             const int ex = (int)__reduce_add_sync(0xffffffffu, lane < wid ? (unsigned)ws : 0u) + inc -
-                                           c.ev.n;
-                            if (c.ev.n > 0) {
+                                           c.ev->n;
+                            if (c.ev->n > 0) {
                                 // staging slots are taken in any order; the (chunk-pass, rank)
                                 // key orders the particles later
-                                const int base = atomicAdd(w.stage_count, c.ev.n);
-                                emit_spawns<TEMP, F32>(w, c.ev, cp, (uint32_t)(running + ex), base);
+                                const int base = atomicAdd(w.stage_count, c.ev->n);
+                                emit_spawns<TEMP, F32>(w, *c.ev, cp, (uint32_t)(running + ex), base);
                             }
                             running += tot;
                         }
