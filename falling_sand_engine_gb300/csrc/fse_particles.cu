@@ -2,8 +2,10 @@
 // the cell tick (world.cpp:1078,1110-1119,1222,1298,1901-1913) and the particle
 // update world::tickCells() (world.cpp:2030-2195).
 //
-// Every kernel takes the world table and handles world blockIdx.y, so one launch
-// serves a single world or a whole batch. Arithmetic on particle state uses the
+// Every kernel takes the world table, so one launch serves a single world or a
+// whole batch: the per-world kernels handle world blockIdx.y (or blockIdx.x), the
+// cooperative update and the compaction run over one index space holding every
+// world's particles. Arithmetic on particle state uses the
 // explicitly rounded intrinsics (__fadd_rn, __fmul_rn, __fdiv_rn, __fsqrt_rn) so
 // that no multiply-add is contracted: the FP32 results equal a strict IEEE CPU
 // evaluation of the same expressions bit for bit.
@@ -13,8 +15,12 @@
 
 namespace fse {
 
-constexpr int PART_BLOCKS = 512;  // blocks per world for the particle list kernels (<= k_cmp_scan threads)
-constexpr int PART_THREADS = 256;
+constexpr int PART_BLOCKS = 512;  // scan_tmp holds PART_BLOCKS + 1 entries per world
+// per-world words of scan_tmp used by the compaction; world 0's entries
+// 0 .. CMP_BLOCKS - 1 hold the compaction blocks' kept counts, then their prefix
+constexpr int ST_KEPT_BEFORE = PART_BLOCKS - 2;  // kept particles of the worlds before
+constexpr int ST_KEPT = PART_BLOCKS - 1;         // this world's kept particles (atomics)
+constexpr int ST_COUNT = PART_BLOCKS;            // the world's new particle count
 
 // p_state values
 enum : uint8_t { PS_ALIVE = 0, PS_DEAD = 1 };
@@ -179,6 +185,7 @@ __global__ void k_air_map(const WorldDev *__restrict__ worlds, const MatTable *_
     load_types(s_type, mt);
     const WorldDev &w = worlds[blockIdx.y];
     const int nb = w.amw * w.amh;
+    if (blockIdx.x == 0 && threadIdx.x == 0) w.scan_tmp[ST_KEPT] = 0;  // for the compaction's counts
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
         const int bx = b % w.amw, by = b / w.amw;
         const int x0 = bx * 8, y0 = by * 8, x1 = min(x0 + 8, w.W), y1 = min(y0 + 8, w.H);
@@ -776,72 +783,117 @@ __device__ __forceinline__ bool keep(const WorldDev &w, int i) {
     return w.p_state[i] == PS_ALIVE && !(w.p.y[i] > (float)w.H);
 }
 
-__global__ void k_cmp_count(const WorldDev *__restrict__ worlds) {
-    const WorldDev &w = worlds[blockIdx.y];
-    const int n = *w.part_count;
-    const int seg = (n + gridDim.x - 1) / gridDim.x;
-    const int b0 = blockIdx.x * seg, b1 = min(n, b0 + seg);
+// The compaction runs over one index space holding every world's particles in
+// world order (world k's at s_pref[k] .. s_pref[k + 1]), cut into CMP_BLOCKS
+// contiguous ranges: a batch of many small worlds costs the blocks of one world of
+// the same total. g kept particles before index g of that space, G(g), give
+// particle g its place in its world's list: G(g) - G(start of its world), the
+// second term being the kept particles of the worlds before it.
+constexpr int CMP_THREADS = SERIAL_THREADS;  // block_excl_sum's block size
+constexpr int CMP_BLOCKS = 304;
+static_assert(CMP_BLOCKS < ST_KEPT_BEFORE && CMP_BLOCKS <= CMP_THREADS, "compaction scratch layout");
+
+// s_pref[k] = val(0) + ... + val(k - 1) for k = 0 .. n, in shared memory; every
+// thread of the block calls it
+template <class F>
+__device__ __forceinline__ void block_prefix(int n, F val, int *s_pref, int *s_warp) {
+    const int seg = (n + CMP_THREADS - 1) / CMP_THREADS;
+    const int k0 = min((int)threadIdx.x * seg, n), k1 = min(k0 + seg, n);
+    int sum = 0;
+    for (int k = k0; k < k1; k++) sum += val(k);
+    int tot;
+    int at = block_excl_sum(sum, s_warp, &tot);
+    for (int k = k0; k < k1; k++) {
+        s_pref[k] = at;
+        at += val(k);
+    }
+    if (threadIdx.x == 0) s_pref[n] = tot;
+    __syncthreads();
+}
+
+// this block's range of the particle index space
+__device__ __forceinline__ void cmp_range(int total, int *b0, int *b1) {
+    const int seg = (total + (int)gridDim.x - 1) / (int)gridDim.x;
+    *b0 = min(total, (int)blockIdx.x * seg);
+    *b1 = min(total, *b0 + seg);
+}
+
+// kept particles per block (world 0's scan_tmp) and per world (ST_KEPT, cleared
+// by k_air_map). Dynamic shared memory: n_worlds + 1 ints.
+__global__ void __launch_bounds__(CMP_THREADS) k_cmp_count(const WorldDev *__restrict__ worlds, int n_worlds) {
+    extern __shared__ int s_pref[];
+    __shared__ int s_warp[CMP_THREADS / 32];
+    block_prefix(n_worlds, [&](int k) { return *worlds[k].part_count; }, s_pref, s_warp);
+    int b0, b1;
+    cmp_range(s_pref[n_worlds], &b0, &b1);
+    const int lane = threadIdx.x & 31;
     int cnt = 0;
-    for (int i = b0 + threadIdx.x; i < b1; i += blockDim.x) cnt += keep(w, i) ? 1 : 0;
-    __shared__ int s[32];
-    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
-    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = cnt;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int t = 0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); k++) t += s[k];
-        w.scan_tmp[blockIdx.x] = t;
-    }
-}
-
-// exclusive scan of the per-block counts (nblocks <= blockDim.x), one block per world
-__global__ void k_cmp_scan(const WorldDev *__restrict__ worlds, int nblocks) {
-    const WorldDev &w = worlds[blockIdx.x];
-    __shared__ int s[32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int v = (int)threadIdx.x < nblocks ? w.scan_tmp[threadIdx.x] : 0;
-    int inc = v;
-    for (int o = 1; o < 32; o <<= 1) {
-        int t = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += t;
-    }
-    if (lane == 31) s[wid] = inc;
-    __syncthreads();
-    if (wid == 0) {
-        int a = lane < nw ? s[lane] : 0;
-        for (int o = 1; o < 32; o <<= 1) {
-            int t = __shfl_up_sync(0xffffffffu, a, o);
-            if (lane >= o) a += t;
+    for (int base = b0; base < b1; base += CMP_THREADS) {
+        const int g = base + (int)threadIdx.x;
+        int wi = -1;
+        bool v = false;
+        if (g < b1) {
+            wi = entry_of(s_pref, n_worlds, g);
+            v = keep(worlds[wi], g - s_pref[wi]);
         }
-        if (lane < nw) s[lane] = a;
+        cnt += v ? 1 : 0;
+        // one atomic per world among the warp's kept particles
+        const unsigned kept = __ballot_sync(0xffffffffu, v);
+        const unsigned same = __match_any_sync(0xffffffffu, wi) & kept;
+        if (v && lane == __ffs(same) - 1) atomicAdd(&worlds[wi].scan_tmp[ST_KEPT], __popc(same));
     }
-    __syncthreads();
-    const int excl = (wid > 0 ? s[wid - 1] : 0) + inc - v;
-    if ((int)threadIdx.x < nblocks) w.scan_tmp[threadIdx.x] = excl;
-    if ((int)threadIdx.x == nblocks - 1) w.scan_tmp[nblocks] = excl + v;
+    int tot;
+    block_excl_sum(cnt, s_warp, &tot);
+    if (threadIdx.x == 0) worlds[0].scan_tmp[blockIdx.x] = tot;
 }
 
-__global__ void k_cmp_scatter(const WorldDev *__restrict__ worlds) {
-    const WorldDev &w = worlds[blockIdx.y];
-    const int n = *w.part_count;
-    const int seg = (n + gridDim.x - 1) / gridDim.x;
-    const int b0 = blockIdx.x * seg, b1 = min(n, b0 + seg);
-    __shared__ int s[32];
-    __shared__ int s_carry;
-    if (threadIdx.x == 0) s_carry = w.scan_tmp[blockIdx.x];
-    __syncthreads();
-    for (int base = b0; base < b1; base += blockDim.x) {
-        int i = base + threadIdx.x;
-        int v = (i < b1 && keep(w, i)) ? 1 : 0;
-        int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-        unsigned m = __ballot_sync(0xffffffffu, v);
-        int inwarp = __popc(m & ((1u << lane) - 1u));
-        if (lane == 0) s[wid] = __popc(m);
-        __syncthreads();
-        int before = s_carry;
-        for (int k = 0; k < wid; k++) before += s[k];
+// one block: the blocks' exclusive prefix, each world's kept particles before it
+// and its new count
+__global__ void __launch_bounds__(CMP_THREADS) k_cmp_scan(const WorldDev *__restrict__ worlds, int n_worlds,
+                                                          int nblocks) {
+    __shared__ int s_warp[CMP_THREADS / 32];
+    int32_t *blk = worlds[0].scan_tmp;
+    const int v = (int)threadIdx.x < nblocks ? blk[threadIdx.x] : 0;
+    int tot;
+    const int ex = block_excl_sum(v, s_warp, &tot);
+    if ((int)threadIdx.x < nblocks) blk[threadIdx.x] = ex;
+    const int seg = (n_worlds + CMP_THREADS - 1) / CMP_THREADS;
+    const int k0 = min((int)threadIdx.x * seg, n_worlds), k1 = min(k0 + seg, n_worlds);
+    int sum = 0;
+    for (int k = k0; k < k1; k++) sum += worlds[k].scan_tmp[ST_KEPT];
+    int at = block_excl_sum(sum, s_warp, &tot);
+    for (int k = k0; k < k1; k++) {
+        int32_t *st = worlds[k].scan_tmp;
+        const int c = st[ST_KEPT];
+        st[ST_KEPT_BEFORE] = at;
+        st[ST_COUNT] = c;
+        at += c;
+    }
+}
+
+// the kept particles to their places in each world's second list (q), in order.
+// Dynamic shared memory: n_worlds + 1 ints.
+__global__ void __launch_bounds__(CMP_THREADS) k_cmp_scatter(const WorldDev *__restrict__ worlds, int n_worlds) {
+    extern __shared__ int s_pref[];
+    __shared__ int s_warp[CMP_THREADS / 32];
+    block_prefix(n_worlds, [&](int k) { return *worlds[k].part_count; }, s_pref, s_warp);
+    int b0, b1;
+    cmp_range(s_pref[n_worlds], &b0, &b1);
+    int run = worlds[0].scan_tmp[blockIdx.x];  // kept particles before the range
+    for (int base = b0; base < b1; base += CMP_THREADS) {
+        const int g = base + (int)threadIdx.x;
+        int wi = 0, i = 0;
+        bool v = false;
+        if (g < b1) {
+            wi = entry_of(s_pref, n_worlds, g);
+            i = g - s_pref[wi];
+            v = keep(worlds[wi], i);
+        }
+        int tot;
+        const int ex = block_excl_sum(v ? 1 : 0, s_warp, &tot);
         if (v) {
-            int o = before + inwarp;
+            const WorldDev &w = worlds[wi];
+            const int o = run + ex - w.scan_tmp[ST_KEPT_BEFORE];
             w.q.x[o] = w.p.x[i];
             w.q.y[o] = w.p.y[i];
             w.q.vx[o] = w.p.vx[i];
@@ -860,20 +912,21 @@ __global__ void k_cmp_scatter(const WorldDev *__restrict__ worlds) {
             w.q.fl[o] = w.p.fl[i];
             w.q.bits[o] = w.p.bits[i];
         }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int t = 0;
-            for (int k = 0; k < nw; k++) t += s[k];
-            s_carry += t;
-        }
-        __syncthreads();
+        run += tot;
     }
 }
 
-__global__ void k_cmp_copy(const WorldDev *__restrict__ worlds, int nblocks) {
-    const WorldDev &w = worlds[blockIdx.y];
-    const int m = w.scan_tmp[nblocks];
-    for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < m; o += gridDim.x * blockDim.x) {
+// the compacted lists back to the first list (p), over the index space of the kept
+// particles. Dynamic shared memory: n_worlds + 1 ints.
+__global__ void __launch_bounds__(CMP_THREADS) k_cmp_copy(const WorldDev *__restrict__ worlds, int n_worlds) {
+    extern __shared__ int s_pref[];
+    __shared__ int s_warp[CMP_THREADS / 32];
+    block_prefix(n_worlds, [&](int k) { return worlds[k].scan_tmp[ST_COUNT]; }, s_pref, s_warp);
+    const int total = s_pref[n_worlds];
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const int wi = entry_of(s_pref, n_worlds, g);
+        const WorldDev &w = worlds[wi];
+        const int o = g - s_pref[wi];
         w.p.x[o] = w.q.x[o];
         w.p.y[o] = w.q.y[o];
         w.p.vx[o] = w.q.vx[o];
@@ -989,11 +1042,11 @@ cudaError_t launch_particle_tick(WorldDev *d_worlds, int n_worlds, const MatTabl
         cudaLaunchKernelEx(&cfg, k_part_serial, (const WorldDev *)d_worlds, n_worlds, mt);
     }
     k_merge<<<n_worlds, 1024, 0, s>>>(d_worlds);
-    dim3 gc(PART_BLOCKS, n_worlds);
-    k_cmp_count<<<gc, PART_THREADS, 0, s>>>(d_worlds);
-    k_cmp_scan<<<n_worlds, PART_BLOCKS, 0, s>>>(d_worlds, PART_BLOCKS);
-    k_cmp_scatter<<<gc, PART_THREADS, 0, s>>>(d_worlds);
-    k_cmp_copy<<<gm, 256, 0, s>>>(d_worlds, PART_BLOCKS);
+    const size_t pref = (size_t)(n_worlds + 1) * sizeof(int);
+    k_cmp_count<<<CMP_BLOCKS, CMP_THREADS, pref, s>>>(d_worlds, n_worlds);
+    k_cmp_scan<<<1, CMP_THREADS, 0, s>>>(d_worlds, n_worlds, CMP_BLOCKS);
+    k_cmp_scatter<<<CMP_BLOCKS, CMP_THREADS, pref, s>>>(d_worlds, n_worlds);
+    k_cmp_copy<<<CMP_BLOCKS, CMP_THREADS, pref, s>>>(d_worlds, n_worlds);
     k_part_end<<<n_worlds, 32, 0, s>>>(d_worlds, PART_BLOCKS);
     return cudaGetLastError();
 }
