@@ -793,10 +793,9 @@ def bench_config2(args, rank, local_rank, world_size):
     digest_b = worlds_digest(worlds, fse)
 
     # end to end through the C ABI with host buffers: every step uploads each
-    # world's planes from pinned host memory, runs one batched step and reads the
-    # planes back
-    e2e = e2e_batch(batch, worlds, torch, cells, world_size)
+    # world's planes from pinned host memory, runs one step and reads the planes back
     batch.close()
+    e2e = e2e_batch(worlds, fse, torch, cells, world_size, choice)
     for w in worlds:
         w.close()
     del worlds
@@ -907,35 +906,59 @@ def e2e_worlds(worlds, step, torch, cells, world_size, path, steps=3):
             "h2d_bytes_per_step": int(bi), "d2h_bytes_per_step": int(bi), "steps": steps, "path": path}
 
 
-def e2e_batch(batch, worlds, torch, cells, world_size, steps=5):
-    """The batched metric end to end through the C ABI: every step copies every
-    world's planes from one pinned host buffer (fse_batch_upload_all: one copy and a
-    scatter kernel), runs one batched step, gathers every plane back into the buffer
-    (fse_batch_download_all: a gather kernel and one copy), all on the batch's
-    stream, then waits once (fse_batch_sync)."""
-    offs, total = batch.io_layout()
-    t = torch.empty(total, dtype=torch.uint8, pin_memory=True)
-    buf = t.numpy()
-    for v, w in zip(batch.io_views(buf), worlds):
-        st = w.state()
-        for k in v:
-            v[k][...] = st[k]
-    # one untimed round trip: the device staging buffer is allocated on first use
-    batch.upload_all(buf)
-    batch.step(1)
-    batch.download_all(buf)
-    batch.sync()
+def e2e_batch(worlds, fse, torch, cells, world_size, launch, steps=5, groups=4):
+    """The batched metric end to end through the C ABI, the host copies overlapping
+    the ticks: the worlds are split into `groups` batches of about equal cells, each
+    on its own stream, and every step each batch copies its worlds' planes from its
+    pinned host buffer (fse_batch_upload_all: one copy and a scatter kernel),
+    enqueues one step (fse_batch_enqueue) and gathers the planes back into the buffer
+    (fse_batch_download_all: a gather kernel and one copy); the step ends when every
+    batch has synchronised (fse_batch_sync). While one batch ticks, the others'
+    copies run."""
+    bins = [[] for _ in range(groups)]
+    load = [0] * groups
+    for k in sorted(range(len(worlds)), key=lambda k: -worlds[k].width * worlds[k].height):
+        g = load.index(min(load))
+        bins[g].append(k)
+        load[g] += worlds[k].width * worlds[k].height
+    subs, bufs = [], []
+    for ks in bins:
+        if not ks:
+            continue
+        sb = fse.Batch([worlds[k] for k in sorted(ks)])
+        sb.set_launch(launch["colour_ctas_per_sm"], launch["particle_blocks"])
+        offs, total = sb.io_layout()
+        t = torch.empty(total, dtype=torch.uint8, pin_memory=True)
+        buf = t.numpy()
+        for v, w in zip(sb.io_views(buf), sb.worlds):
+            st = w.state()
+            for key in v:
+                v[key][...] = st[key]
+        subs.append(sb)
+        bufs.append((t, buf))
+    total = sum(int(buf.nbytes) for _, buf in bufs)
+
+    def one_step():
+        for sb, (_, buf) in zip(subs, bufs):
+            sb.upload_all(buf)
+            sb.enqueue(1)
+            sb.download_all(buf)
+        for sb in subs:
+            sb.sync()
+
+    # one untimed round trip: the device staging buffers are allocated on first use
+    one_step()
     t0 = time.perf_counter()
     for _ in range(steps):
-        batch.upload_all(buf)
-        batch.step(1)
-        batch.download_all(buf)
-        batch.sync()
+        one_step()
     dt = max_over_ranks(time.perf_counter() - t0, world_size)
+    for sb in subs:
+        sb.close()
     return {"value": round(world_size * cells * steps / dt / 1e9, 4), "unit": "Gcell/s",
-            "h2d_bytes_per_step": int(total), "d2h_bytes_per_step": int(total), "steps": steps,
-            "path": "fse_batch_upload_all (every world's planes, one pinned host buffer) + fse_batch_step + "
-                    "fse_batch_download_all on the batch's stream, one fse_batch_sync per step"}
+            "h2d_bytes_per_step": total, "d2h_bytes_per_step": total, "steps": steps,
+            "path": "the worlds in %d batches of about equal cells, each on its own stream: fse_batch_upload_all "
+                    "(its worlds' planes, one pinned host buffer) + fse_batch_enqueue + fse_batch_download_all, "
+                    "then fse_batch_sync of every batch; one batch's copies overlap the others' ticks" % len(subs)}
 
 
 def reference_timing_worlds(sizes, sample, steps, warm, budget_s):

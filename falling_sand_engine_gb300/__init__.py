@@ -483,6 +483,11 @@ class Batch:
         else:
             check(self.lib.fse_batch_step(self.h, n), "batch_step")
 
+    def enqueue(self, n=1):
+        """Enqueue n ticks on the batch's stream without waiting; sync() waits and
+        reports their errors. Batches of disjoint worlds run concurrently."""
+        check(self.lib.fse_batch_enqueue(self.h, n), "batch_enqueue")
+
     def prepare_graphs(self, n, graph_ticks=32):
         """Capture the graphs step(n, graph_ticks) will replay, without running them."""
         check(self.lib.fse_batch_prepare_graphs(self.h, n, graph_ticks), "batch_prepare_graphs")

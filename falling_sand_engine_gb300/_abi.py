@@ -133,6 +133,7 @@ SIGNATURES = {
     "fse_batch_create": (_i, [_vp, _i, _pp]),
     "fse_batch_destroy": (_i, [_vp]),
     "fse_batch_step": (_i, [_vp, _i]),
+    "fse_batch_enqueue": (_i, [_vp, _i]),
     "fse_batch_step_graph": (_i, [_vp, _i, _i]),
     "fse_batch_autotune": (_i, [_vp, _vp]),
     "fse_batch_set_launch": (_i, [_vp, _i, _i]),

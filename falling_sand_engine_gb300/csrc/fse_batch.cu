@@ -367,6 +367,11 @@ int fse_batch_step(fse_batch *b, int n) {
     return batch_sync(b);
 }
 
+int fse_batch_enqueue(fse_batch *b, int n) {
+    if (!b || n < 0) return FSE_E_INVAL;
+    return batch_enqueue(b, n);
+}
+
 }  // extern "C"
 
 // The graph of k steps for the batch's current timing mode, captured on first use.

@@ -423,6 +423,10 @@ int fse_tick_noalloc(uint16_t *id, uint32_t *colour, int32_t *scalar, uint8_t *f
 int fse_batch_create(fse_world **worlds, int n, fse_batch **out);
 int fse_batch_destroy(fse_batch *batch);
 int fse_batch_step(fse_batch *batch, int n_ticks);
+/* enqueue n_ticks steps on the batch's stream and return without waiting (errors
+ * of those steps come from the next fse_batch_sync); batches of disjoint worlds
+ * step concurrently, each on its own stream */
+int fse_batch_enqueue(fse_batch *batch, int n_ticks);
 /* capture graph_ticks steps into one CUDA graph (default 32) and replay */
 int fse_batch_step_graph(fse_batch *batch, int n_ticks, int graph_ticks);
 /* capture (without running) the graphs a later fse_batch_step_graph(n_ticks,

@@ -182,6 +182,45 @@ def test_batch_equals_individual_worlds(fse):
     b.close()
 
 
+def test_disjoint_batches_enqueued_concurrently(fse):
+    """Two batches of disjoint worlds enqueued on their own streams without waiting
+    (fused ticks and cooperative particle updates of both in flight together), with
+    whole-batch plane I/O between steps as a pipelined round trip does: every world
+    equals the same world stepped alone."""
+    sizes = [(128, 192), (320, 128), (256, 256), (192, 448), (512, 320), (384, 384)]
+    solo, worlds = [], []
+    for i, (w, h) in enumerate(sizes):
+        for lst in (solo, worlds):
+            x = fse.World(w, h, seed=300 + i)
+            x.generate(fse.GEN_MIX, 300 + i)
+            lst.append(x)
+    for x in solo:
+        x.step(7)
+    torch = pytest.importorskip("torch")
+    groups = [fse.Batch(worlds[:3]), fse.Batch(worlds[3:])]
+    bufs = [torch.empty(g.io_layout()[1], dtype=torch.uint8, pin_memory=True).numpy() for g in groups]
+    for g, buf in zip(groups, bufs):
+        g.download_all(buf)
+    for g in groups:
+        g.sync()
+    for n in (4, 3):
+        for g, buf in zip(groups, bufs):
+            g.upload_all(buf)
+            g.enqueue(n)
+            g.download_all(buf)
+        for g in groups:
+            g.sync()
+    views = groups[0].io_views(bufs[0]) + groups[1].io_views(bufs[1])
+    for x, y, v in zip(solo, worlds, views):
+        sx, sy = x.state(), y.state()
+        for k in sx:
+            np.testing.assert_array_equal(sx[k], sy[k], err_msg=k)
+            np.testing.assert_array_equal(sx[k], v[k], err_msg="downloaded " + k)
+        assert x.particles().tobytes() == y.particles().tobytes()
+    for g in groups:
+        g.close()
+
+
 def test_autotune_never_changes_results(fse):
     ref = fse.World(384, 384, seed=44)
     ref.generate(fse.GEN_MIX, 44)
