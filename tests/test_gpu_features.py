@@ -182,6 +182,47 @@ def test_batch_equals_individual_worlds(fse):
     b.close()
 
 
+def _free_particles(fse, n, w, h, seed):
+    rng = np.random.default_rng(seed)
+    p = np.zeros(n, fse.PARTICLE_DTYPE)
+    p["x"] = rng.uniform(0, w, n).astype(np.float32)
+    p["y"] = rng.uniform(-8, h + 24, n).astype(np.float32)  # some start below the world
+    p["vx"] = rng.normal(0.0, 2.0, n).astype(np.float32)
+    p["vy"] = rng.normal(0.0, 2.0, n).astype(np.float32)
+    p["ay"] = np.float32(0.1)
+    p["fade_time"] = 60
+    p["id"] = fse.material_find("GENERIC_SAND")
+    p["colour"] = 0xFFFFFFFF
+    return p
+
+
+def test_batch_compaction_across_uneven_particle_lists(fse):
+    """The particle-list compaction runs over one index space of every world's
+    particles: worlds with no particles at all, with tens of thousands, and with
+    particles leaving through the bottom, side by side, equal the same worlds alone."""
+    specs = [(256, 192, fse.GEN_EMPTY, 0), (384, 320, fse.GEN_MIX, 20000), (128, 128, fse.GEN_EMPTY, 0),
+             (320, 256, fse.GEN_MIX, 3000), (192, 448, fse.GEN_EMPTY, 700)]
+    solo, worlds = [], []
+    for i, (w, h, kind, n) in enumerate(specs):
+        for lst in (solo, worlds):
+            x = fse.World(w, h, seed=500 + i)
+            x.generate(kind, 500 + i)
+            if n:
+                x.addCell(_free_particles(fse, n, w, h, 500 + i))
+            lst.append(x)
+    for x in solo:
+        x.step(5)
+    b = fse.Batch(worlds)
+    b.step(5)
+    assert worlds[0].particle_count() == 0 and worlds[2].particle_count() == 0
+    for x, y in zip(solo, worlds):
+        sx, sy = x.state(), y.state()
+        for k in sx:
+            np.testing.assert_array_equal(sx[k], sy[k], err_msg=k)
+        assert x.particles().tobytes() == y.particles().tobytes()
+    b.close()
+
+
 def test_disjoint_batches_enqueued_concurrently(fse):
     """Two batches of disjoint worlds enqueued on their own streams without waiting
     (fused ticks and cooperative particle updates of both in flight together), with
