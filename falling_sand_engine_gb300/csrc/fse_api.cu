@@ -972,7 +972,7 @@ int fse_world_create(int width, int height, const fse_config *cfg, fse_world **o
     h.bar = (unsigned *)(w->ctr + 8);  // [8] arrivals, [9] generation
     h.stats = w->ctr + 10;             // [10] iterations of the last particle update
     h.sched = (uint32_t *)(w->ctr + 12);  // [12] next ticket, [13] CTAs finished, [14] a wait gave up (fused tick)
-    h.chg_n = w->ctr + 16;                // [16..17] fill changes per iteration parity (particle update)
+    h.chg_n = w->ctr + 16;  // [16..17] fill changes per iteration parity, [18..19] their lowest index (particle update)
     cudaMemset(w->ctr, 0, 24 * sizeof(int32_t));
     cudaMemset(h.cdone, 0, (size_t)h.nCx * h.nCy * sizeof(uint32_t));
     cudaMemset(h.ledger, 0, LED_ROWS * MAXMAT * sizeof(long long));

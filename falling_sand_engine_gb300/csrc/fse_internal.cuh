@@ -179,7 +179,9 @@ struct WorldDev {
     int32_t *req_count;     // [3] counters of the update (fill changes of even / odd iterations)
     uint32_t *chg;          // 2 x airmap blocks: lowest index whose fill changed there (read / written by an iteration)
     int32_t *stats;         // [0]: iterations of the last particle update (of the launch's first world)
-    int32_t *chg_n;         // [2] fills of this world changed by the update's even / odd iterations
+    // [0..1] fills of this world changed by the update's even / odd iterations,
+    // [2..3] the lowest index among those changes
+    int32_t *chg_n;
     int32_t *scan_tmp;      // block sums for compaction
     long long *ledger;      // [LED_ROWS][MAXMAT]
     int32_t *err;

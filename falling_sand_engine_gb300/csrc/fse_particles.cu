@@ -185,7 +185,11 @@ __global__ void k_air_map(const WorldDev *__restrict__ worlds, const MatTable *_
     load_types(s_type, mt);
     const WorldDev &w = worlds[blockIdx.y];
     const int nb = w.amw * w.amh;
-    if (blockIdx.x == 0 && threadIdx.x == 0) w.scan_tmp[ST_KEPT] = 0;  // for the compaction's counts
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        w.scan_tmp[ST_KEPT] = 0;  // for the compaction's counts
+        w.chg_n[2] = 0x7FFFFFFF;  // the particle update's lowest changing index, per parity
+        w.chg_n[3] = 0x7FFFFFFF;
+    }
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
         const int bx = b % w.amw, by = b / w.amw;
         const int x0 = bx * 8, y0 = by * 8, x1 = min(x0 + 8, w.W), y1 = min(y0 + 8, w.H);
@@ -520,10 +524,18 @@ __global__ void __launch_bounds__(SERIAL_THREADS) k_part_serial(const WorldDev *
         // changed fills are counted, listed and their blocks marked for the next
         // iteration with the changing index. A thread takes particle g, its warp walks
         // the spirals of the warp's particles together.
+        // After the first iteration only particles above the lowest index whose fill
+        // changed in the last iteration can see a change (a particle is computed again
+        // only for a change by a lower index), so each world's space starts there.
         const int n_act = it == 0 ? active_worlds(n_worlds, parts, s_ids, s_apref, s_warp)
                                   : active_worlds(
                                         n_worlds,
-                                        [&](int k) { return __ldcg(&worlds[k].chg_n[1 - par]) > 0 ? parts(k) : 0; },
+                                        [&](int k) {
+                                            const int32_t *cn = worlds[k].chg_n;
+                                            return __ldcg(&cn[1 - par]) > 0
+                                                       ? max(0, parts(k) - 1 - __ldcg(&cn[2 + par]))
+                                                       : 0;
+                                        },
                                         s_ids, s_apref, s_warp);
         const int total_a = s_apref[n_act];
         for (int gb0 = gtid - lane; gb0 < total_a; gb0 += gstride) {
@@ -536,6 +548,7 @@ __global__ void __launch_bounds__(SERIAL_THREADS) k_part_serial(const WorldDev *
                 i = g - s_apref[j];
                 const WorldDev &w = worlds[wi];
                 if (it > 0) {
+                    i += __ldcg(&w.chg_n[2 + par]) + 1;
                     const int32_t b0 = w.p_box0[i];
                     if (b0 < 0) {
                         work = false;  // read no cell: nothing can change it
@@ -603,6 +616,7 @@ __global__ void __launch_bounds__(SERIAL_THREADS) k_part_serial(const WorldDev *
                     uint32_t *mark = w.chg + (size_t)(1 - par) * nblk;
                     atomicAdd(&cnt[par], 1);
                     w.merge_list[atomicAdd(&w.chg_n[par], 1)] = i;  // at most once per particle
+                    atomicMin(&w.chg_n[3 - par], i);
                     if (before >= 0)
                         atomicMin(&mark[(before / w.W >> 3) * w.amw + ((before % w.W) >> 3)], (uint32_t)i);
                     if (after >= 0) atomicMin(&mark[(after / w.W >> 3) * w.amw + ((after % w.W) >> 3)], (uint32_t)i);
@@ -657,7 +671,10 @@ __global__ void __launch_bounds__(SERIAL_THREADS) k_part_serial(const WorldDev *
                 // there: only the cells cleared in B1 take atomics
                 if (c >= 0 && __ldcg(&w.df[c]) < fill_code(i)) atomicMax(&w.df[c], fill_code(i));
             }
-            for (int k = gtid; k < n_worlds; k += gstride) worlds[k].chg_n[1 - par] = 0;
+            for (int k = gtid; k < n_worlds; k += gstride) {
+                worlds[k].chg_n[1 - par] = 0;
+                worlds[k].chg_n[2 + par] = 0x7FFFFFFF;  // read by this iteration's A
+            }
         }
         grid_sync(gb, nb, err);
     }
